@@ -1,0 +1,257 @@
+/*
+ * rive_cuda.h -- C ABI of the GB300 (sm_103a) flush backend for the Rive
+ * vector renderer.
+ *
+ * This is the drop-in seam for rive-runtime's backend interface,
+ * `rive::gpu::RenderContextImpl`
+ * (renderer/include/rive/renderer/render_context_impl.hpp:26-243). A C++
+ * `RenderContextCUDAImpl` (see rive-runtime_gb300/csrc/render_context_cuda_impl.hpp)
+ * forwards each virtual to one call below; any other host language binds the
+ * same symbols over its FFI. Signatures use plain pointers, sizes and PODs only.
+ *
+ * Every entry point returns an int status (RIVE_CUDA_OK == 0). On failure the
+ * context keeps a message, readable through rive_cuda_last_error(). No call
+ * throws and none aborts the process.
+ */
+#ifndef RIVE_CUDA_H
+#define RIVE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RIVE_CUDA_ABI_VERSION 1
+
+/* Status codes. */
+enum
+{
+    RIVE_CUDA_OK = 0,
+    RIVE_CUDA_ERR_INVALID_ARGUMENT = 1,
+    RIVE_CUDA_ERR_UNSUPPORTED = 2,   /* a draw type / interlock mode this
+                                        backend does not implement */
+    RIVE_CUDA_ERR_OUT_OF_MEMORY = 3,
+    RIVE_CUDA_ERR_CUDA = 4,          /* a CUDA runtime call failed */
+    RIVE_CUDA_ERR_DEVICE_STATUS = 5, /* a kernel reported an overflow or a
+                                        bounded wait that ran out */
+    RIVE_CUDA_ERR_NOT_MAPPED = 6,
+};
+
+/*
+ * Buffer kinds. One per `RenderContextImpl::resize*Buffer/map*Buffer/
+ * unmap*Buffer` triple (render_context_impl.hpp:108-174).
+ */
+enum
+{
+    RIVE_CUDA_BUFFER_FLUSH_UNIFORM = 0, /* gpu::FlushUniforms, 256 B each      */
+    RIVE_CUDA_BUFFER_PATH = 1,          /* gpu::PathData, 64 B each            */
+    RIVE_CUDA_BUFFER_PAINT = 2,         /* gpu::PaintData, 8 B each            */
+    RIVE_CUDA_BUFFER_PAINT_AUX = 3,     /* gpu::PaintAuxData, 128 B each       */
+    RIVE_CUDA_BUFFER_CONTOUR = 4,       /* gpu::ContourData, 16 B each         */
+    RIVE_CUDA_BUFFER_GRAD_SPAN = 5,     /* gpu::GradientSpan, 16 B each        */
+    RIVE_CUDA_BUFFER_TESS_SPAN = 6,     /* gpu::TessVertexSpan, 64 B each      */
+    RIVE_CUDA_BUFFER_TRIANGLE = 7,      /* gpu::TriangleVertex (unsupported)   */
+    RIVE_CUDA_BUFFER_IMAGE_DRAW = 8,    /* gpu::ImageDrawInstance (unsupported)*/
+    RIVE_CUDA_BUFFER_KIND_COUNT = 9,
+};
+
+/* gpu::LoadAction (gpu.hpp:774). */
+enum
+{
+    RIVE_CUDA_LOAD_CLEAR = 0,
+    RIVE_CUDA_LOAD_PRESERVE = 1,
+    RIVE_CUDA_LOAD_DONT_CARE = 2,
+};
+
+/* gpu::DrawType values this backend executes (gpu.hpp:657). */
+enum
+{
+    RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES = 0,
+};
+
+/*
+ * One gpu::DrawBatch (gpu.hpp:1219-1282), flattened. The reference keeps the
+ * batches in a linked list owned by a per-frame allocator; the caller flattens
+ * it into an array in list order.
+ */
+typedef struct rive_cuda_draw_batch
+{
+    uint32_t draw_type;         /* gpu::DrawType                          */
+    uint32_t element_count;     /* patch instances                        */
+    uint32_t base_element;      /* first patch instance                   */
+    uint32_t shader_features;   /* gpu::ShaderFeatures bits of this batch */
+    uint32_t draw_contents;     /* gpu::DrawContents bits                 */
+    uint32_t shader_misc_flags; /* gpu::ShaderMiscFlags bits              */
+    uint32_t first_blend_mode;  /* rive::BlendMode of the first draw      */
+    uint32_t barriers;          /* gpu::BarrierFlags                      */
+} rive_cuda_draw_batch;
+
+/*
+ * The fields of gpu::FlushDescriptor (gpu.hpp:1320-1438) that a
+ * rasterOrdering backend reads. `first_*` are element offsets into the frame's
+ * mapped buffers, exactly as RenderContext::LogicalFlush::layoutResources
+ * (render_context.cpp:1116-1392) computes them.
+ */
+typedef struct rive_cuda_flush_desc
+{
+    uint32_t render_target_width;
+    uint32_t render_target_height;
+    uint32_t interlock_mode;       /* gpu::InterlockMode; 0 = rasterOrdering */
+    uint32_t color_load_action;    /* RIVE_CUDA_LOAD_*                       */
+    uint32_t color_clear_value;    /* rive::ColorInt (0xAARRGGBB)            */
+    int32_t update_bounds[4];      /* renderTargetUpdateBounds l,t,r,b       */
+    uint32_t combined_shader_features;
+    uint32_t dither_mode;          /* gpu::DitherMode                        */
+    uint32_t flush_uniform_offset_bytes;
+    uint32_t path_count;
+    uint32_t first_path;
+    uint32_t first_paint;
+    uint32_t first_paint_aux;
+    uint32_t contour_count;
+    uint32_t first_contour;
+    uint32_t grad_span_count;
+    uint32_t first_grad_span;
+    uint32_t tess_span_count;
+    uint32_t first_tess_span;
+    uint32_t grad_data_height;
+    uint32_t tess_data_height;
+    uint32_t wireframe;
+    uint32_t clockwise_fill_override;
+    uint32_t has_triangle_vertices;
+    uint32_t draw_batch_count;
+    const rive_cuda_draw_batch* draw_batches; /* host array, list order */
+} rive_cuda_flush_desc;
+
+typedef struct rive_cuda_context rive_cuda_context;
+
+/* Creates a context bound to CUDA device `device`. */
+int rive_cuda_context_create(int device, rive_cuda_context** out_ctx);
+void rive_cuda_context_destroy(rive_cuda_context* ctx);
+
+/* Copies the last error message (NUL-terminated, truncated) into buf. */
+int rive_cuda_last_error(const rive_cuda_context* ctx, char* buf, size_t len);
+
+/*
+ * RenderContextImpl::resize*Buffer (render_context_impl.hpp:108-120). Sizes
+ * the ring of pinned host staging buffers and the device copy. A size of 0
+ * frees the buffer. "Cannot fail" in the reference; here a failed allocation
+ * returns RIVE_CUDA_ERR_OUT_OF_MEMORY and the next map returns NULL.
+ */
+int rive_cuda_resize_buffer(rive_cuda_context* ctx, int kind, size_t bytes);
+
+/*
+ * RenderContextImpl::map*Buffer (render_context_impl.hpp:155-164). Returns a
+ * write-only pointer into pinned host memory, valid until the matching unmap,
+ * or NULL (the reference then skips the frame, render_context.cpp:1012-1016).
+ */
+void* rive_cuda_map_buffer(rive_cuda_context* ctx, int kind, size_t bytes);
+
+/*
+ * RenderContextImpl::unmap*Buffer (render_context_impl.hpp:165-174). Enqueues
+ * the host->device copy of the mapped bytes on the context's upload stream.
+ */
+int rive_cuda_unmap_buffer(rive_cuda_context* ctx, int kind, size_t bytes);
+
+/* RenderContextImpl::resizeGradientTexture / resizeTessellationTexture
+ * (render_context_impl.hpp:177-178). */
+int rive_cuda_resize_gradient_texture(rive_cuda_context* ctx,
+                                      uint32_t width,
+                                      uint32_t height);
+int rive_cuda_resize_tessellation_texture(rive_cuda_context* ctx,
+                                          uint32_t width,
+                                          uint32_t height);
+
+/*
+ * Render targets (gpu::RenderTarget, render_target.hpp): an RGBA8 image in
+ * device memory, rows of width*4 bytes, row 0 at the top.
+ */
+typedef struct rive_cuda_render_target rive_cuda_render_target;
+int rive_cuda_render_target_create(rive_cuda_context* ctx,
+                                   uint32_t width,
+                                   uint32_t height,
+                                   rive_cuda_render_target** out_target);
+void rive_cuda_render_target_destroy(rive_cuda_context* ctx,
+                                     rive_cuda_render_target* target);
+/* Device address of the target's pixels (for zero-copy consumers). */
+void* rive_cuda_render_target_device_ptr(rive_cuda_render_target* target);
+/* Copies the target's pixels to host memory (width*height*4 bytes). */
+int rive_cuda_render_target_read(rive_cuda_context* ctx,
+                                  rive_cuda_render_target* target,
+                                  void* dst_host,
+                                  void* cuda_stream);
+
+/*
+ * RenderContextImpl::flush(const gpu::FlushDescriptor&)
+ * (render_context_impl.hpp:217). Runs, in stream order, the gradient-ramp,
+ * tessellation and draw/resolve kernels of one logical flush over the buffers
+ * last unmapped, into `target`. `cuda_stream` carries the role of
+ * FlushDescriptor::externalCommandBuffer (gpu.hpp:1416): a cudaStream_t, or
+ * NULL for the context's own stream. Returns once the work is enqueued;
+ * device-side overflow is reported by rive_cuda_sync().
+ */
+int rive_cuda_flush(rive_cuda_context* ctx,
+                    const rive_cuda_flush_desc* desc,
+                    rive_cuda_render_target* target,
+                    void* cuda_stream);
+
+/*
+ * Same as rive_cuda_flush, but the record buffers are device pointers the
+ * caller already holds (each at element 0 of the frame's buffer; desc->first_*
+ * still index into them). No host staging is touched. Used by batched and
+ * serving callers that keep path buffers resident in HBM.
+ */
+typedef struct rive_cuda_device_buffers
+{
+    const void* flush_uniforms;
+    const void* paths;
+    const void* paints;
+    const void* paint_aux;
+    const void* contours;
+    const void* grad_spans;
+    const void* tess_spans;
+} rive_cuda_device_buffers;
+
+int rive_cuda_flush_device(rive_cuda_context* ctx,
+                           const rive_cuda_flush_desc* desc,
+                           const rive_cuda_device_buffers* buffers,
+                           void* target_pixels_device,
+                           void* cuda_stream);
+
+/*
+ * Waits for the stream and returns RIVE_CUDA_ERR_DEVICE_STATUS if any kernel
+ * since the last sync reported an overflow; the message names it.
+ */
+int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream);
+
+/*
+ * Debug/parity read-backs of the intermediate textures of the last flush:
+ * the tessellation texture (uint4 per vertex, 2048 per row) and the gradient
+ * texture (RGBA8, 512 per row).
+ */
+int rive_cuda_read_tess_texture(rive_cuda_context* ctx,
+                                void* dst_host,
+                                size_t bytes);
+int rive_cuda_read_grad_texture(rive_cuda_context* ctx,
+                                void* dst_host,
+                                size_t bytes);
+
+/* Counters of the last flush (triangles set up, tile bin entries, ...). */
+typedef struct rive_cuda_flush_stats
+{
+    uint64_t tess_vertices;
+    uint64_t patches;
+    uint64_t triangles;
+    uint64_t bin_entries;
+    uint64_t tiles;
+    uint64_t kernel_launches;
+} rive_cuda_flush_stats;
+int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
+                               rive_cuda_flush_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RIVE_CUDA_H */

@@ -1,0 +1,108 @@
+/*
+ * rive_scene.h -- a flat, pointer-free recording of the rive::Renderer /
+ * rive::Factory calls that make one frame (include/rive/renderer.hpp:212-236,
+ * include/rive/factory.hpp:35-87).
+ *
+ * It is the input format of the planner (rive-runtime_gb300/csrc/planner) and
+ * of the reference front-end replay that pins it. Python's scene generator
+ * writes it. All fields are little-endian and 4-byte aligned.
+ *
+ *   rive_scene_header
+ *   rive_scene_path[path_count]
+ *   rive_scene_paint[paint_count]
+ *   rive_scene_cmd[cmd_count]
+ *   uint8_t verbs[verb_count]          (padded to a multiple of 4 bytes)
+ *   float   points[point_count * 2]
+ *   rive_scene_stop stops[stop_count]
+ */
+#ifndef RIVE_SCENE_H
+#define RIVE_SCENE_H
+
+#include <stdint.h>
+
+#define RIVE_SCENE_MAGIC 0x31435352u /* "RSC1" */
+
+/* rive::PathVerb (include/rive/math/path_types.hpp). */
+enum
+{
+    RIVE_SCENE_VERB_MOVE = 0,
+    RIVE_SCENE_VERB_LINE = 1,
+    RIVE_SCENE_VERB_QUAD = 2,
+    RIVE_SCENE_VERB_CUBIC = 4,
+    RIVE_SCENE_VERB_CLOSE = 5,
+};
+
+/* Renderer calls. */
+enum
+{
+    RIVE_SCENE_CMD_SAVE = 0,
+    RIVE_SCENE_CMD_RESTORE = 1,
+    RIVE_SCENE_CMD_TRANSFORM = 2, /* m[6] = xx, xy, yx, yy, tx, ty */
+    RIVE_SCENE_CMD_DRAW_PATH = 3, /* a = path index, b = paint index */
+    RIVE_SCENE_CMD_CLIP_PATH = 4, /* a = path index */
+};
+
+/* rive::RenderPaintStyle / gradient kinds. */
+enum
+{
+    RIVE_SCENE_STYLE_STROKE = 0,
+    RIVE_SCENE_STYLE_FILL = 1,
+    RIVE_SCENE_SHADER_NONE = 0,
+    RIVE_SCENE_SHADER_LINEAR = 1,
+    RIVE_SCENE_SHADER_RADIAL = 2,
+};
+
+typedef struct rive_scene_header
+{
+    uint32_t magic;
+    uint32_t width;
+    uint32_t height;
+    uint32_t clear_color; /* rive::ColorInt 0xAARRGGBB */
+    uint32_t path_count;
+    uint32_t paint_count;
+    uint32_t cmd_count;
+    uint32_t verb_count;
+    uint32_t point_count;
+    uint32_t stop_count;
+    uint32_t dither_mode; /* gpu::DitherMode: 0 none, 1 IGN */
+    uint32_t reserved;
+} rive_scene_header;
+
+typedef struct rive_scene_path
+{
+    uint32_t verb_offset;
+    uint32_t verb_count;
+    uint32_t point_offset;
+    uint32_t point_count;
+    uint32_t fill_rule; /* rive::FillRule: 0 nonZero, 1 evenOdd */
+} rive_scene_path;
+
+typedef struct rive_scene_paint
+{
+    uint32_t style;      /* RIVE_SCENE_STYLE_* */
+    uint32_t color;      /* rive::ColorInt */
+    float thickness;
+    uint32_t join;       /* rive::StrokeJoin: 0 miter, 1 round, 2 bevel */
+    uint32_t cap;        /* rive::StrokeCap: 0 butt, 1 round, 2 square */
+    uint32_t blend_mode; /* rive::BlendMode enum value (3 = srcOver) */
+    uint32_t shader;     /* RIVE_SCENE_SHADER_* */
+    float g[4];          /* linear: sx, sy, ex, ey; radial: cx, cy, r, 0 */
+    uint32_t stop_offset;
+    uint32_t stop_count;
+} rive_scene_paint;
+
+typedef struct rive_scene_cmd
+{
+    uint32_t op;
+    uint32_t a;
+    uint32_t b;
+    float m[6];
+} rive_scene_cmd;
+
+typedef struct rive_scene_stop
+{
+    float position;
+    uint32_t color; /* rive::ColorInt */
+} rive_scene_stop;
+
+#endif /* RIVE_SCENE_H */

@@ -1,0 +1,409 @@
+/*
+ * ref_capture -- TEST INFRASTRUCTURE (oracle). Never linked into the product.
+ *
+ * Replays a rive_scene.h recording through rive-runtime's own, unmodified CPU
+ * front end (RiveRenderer -> RenderContext, renderer/src/rive_renderer.cpp and
+ * renderer/src/render_context.cpp) into a RenderContextImpl that records every
+ * buffer it is handed and every FlushDescriptor (render_context_impl.hpp:217).
+ * The recording ("capture") is the golden INPUT of the device passes and the
+ * golden OUTPUT of this project's own planner.
+ *
+ * Built by oracle/Makefile from the reference sources where they lie; the
+ * binary lands in oracle/_ref/ and is never committed.
+ *
+ * Usage: ref_capture <scene.bin> <capture.bin>
+ *
+ * Capture file layout (little-endian):
+ *   u32 magic 'RCP1', u32 width, u32 height, u32 buffer_kinds (= 7)
+ *   7 x { u64 bytes, bytes of data, zero pad to 8 }  in rive_cuda.h order
+ *   u32 flush_count
+ *   flush_count x { rive_cuda_flush_desc (draw_batches = 0),
+ *                   rive_cuda_draw_batch[draw_batch_count] }
+ */
+#include "rive/renderer/texture.hpp"
+#include "common/render_context_null.hpp"
+#include "rive/renderer/render_context.hpp"
+#include "rive/renderer/rive_renderer.hpp"
+#include "rive/renderer/gpu.hpp"
+#include "rive/math/raw_path.hpp"
+#include "rive/shapes/paint/blend_mode.hpp"
+#include "rive/shapes/paint/stroke_cap.hpp"
+#include "rive/shapes/paint/stroke_join.hpp"
+
+#include "rive_cuda.h"
+#include "rive_scene.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+using namespace rive;
+using namespace rive::gpu;
+
+namespace
+{
+// Buffer ring whose unmap keeps a copy of the bytes the front end wrote.
+class CaptureRing : public BufferRing
+{
+public:
+    CaptureRing(size_t capacity, std::vector<uint8_t>* sink) :
+        BufferRing(capacity), m_sink(sink)
+    {}
+
+private:
+    void* onMapBuffer(int, size_t) override { return shadowBuffer(); }
+    void onUnmapAndSubmitBuffer(int, size_t bytes) override
+    {
+        m_sink->assign(shadowBuffer(), shadowBuffer() + bytes);
+    }
+    std::vector<uint8_t>* m_sink;
+};
+
+struct FlushRecord
+{
+    rive_cuda_flush_desc desc;
+    std::vector<rive_cuda_draw_batch> batches;
+};
+
+class CaptureImpl : public RenderContextNULL
+{
+public:
+    // Buffers in rive_cuda.h kind order 0..6.
+    std::vector<uint8_t> buffers[7];
+    std::vector<FlushRecord> flushes;
+
+    static std::unique_ptr<RenderContext> Make(CaptureImpl** out)
+    {
+        auto impl = std::make_unique<CaptureImpl>();
+        *out = impl.get();
+        return std::make_unique<RenderContext>(std::move(impl));
+    }
+
+private:
+    // Sizes decide which ring a storage buffer belongs to; the helper impl
+    // creates them in a fixed order, so route by call order instead.
+    std::unique_ptr<BufferRing> makeUniformBufferRing(size_t cap) override
+    {
+        return std::make_unique<CaptureRing>(cap, &buffers[0]);
+    }
+    std::unique_ptr<BufferRing> makeStorageBufferRing(
+        size_t cap,
+        StorageBufferStructure) override
+    {
+        return std::make_unique<CaptureRing>(cap, m_nextStorageSink);
+    }
+    std::unique_ptr<BufferRing> makeVertexBufferRing(size_t cap) override
+    {
+        return std::make_unique<CaptureRing>(cap, m_nextVertexSink);
+    }
+
+public:
+    // RenderContextHelperImpl::resize*Buffer call make*BufferRing; set the
+    // sink before forwarding.
+    void resizePathBuffer(size_t n, StorageBufferStructure s) override
+    {
+        m_nextStorageSink = &buffers[1];
+        RenderContextHelperImpl::resizePathBuffer(n, s);
+    }
+    void resizePaintBuffer(size_t n, StorageBufferStructure s) override
+    {
+        m_nextStorageSink = &buffers[2];
+        RenderContextHelperImpl::resizePaintBuffer(n, s);
+    }
+    void resizePaintAuxBuffer(size_t n, StorageBufferStructure s) override
+    {
+        m_nextStorageSink = &buffers[3];
+        RenderContextHelperImpl::resizePaintAuxBuffer(n, s);
+    }
+    void resizeContourBuffer(size_t n, StorageBufferStructure s) override
+    {
+        m_nextStorageSink = &buffers[4];
+        RenderContextHelperImpl::resizeContourBuffer(n, s);
+    }
+    void resizeGradSpanBuffer(size_t n) override
+    {
+        m_nextVertexSink = &buffers[5];
+        RenderContextHelperImpl::resizeGradSpanBuffer(n);
+    }
+    void resizeTessVertexSpanBuffer(size_t n) override
+    {
+        m_nextVertexSink = &buffers[6];
+        RenderContextHelperImpl::resizeTessVertexSpanBuffer(n);
+    }
+    void resizeTriangleVertexBuffer(size_t n) override
+    {
+        m_nextVertexSink = &m_discard;
+        RenderContextHelperImpl::resizeTriangleVertexBuffer(n);
+    }
+    void resizeImageDrawInstanceBuffer(size_t n) override
+    {
+        m_nextVertexSink = &m_discard;
+        RenderContextHelperImpl::resizeImageDrawInstanceBuffer(n);
+    }
+
+    void flush(const FlushDescriptor& d) override
+    {
+        FlushRecord rec;
+        memset(&rec.desc, 0, sizeof(rec.desc));
+        rive_cuda_flush_desc& o = rec.desc;
+        o.render_target_width = d.renderTarget->width();
+        o.render_target_height = d.renderTarget->height();
+        o.interlock_mode = static_cast<uint32_t>(d.interlockMode);
+        o.color_load_action = static_cast<uint32_t>(d.colorLoadAction);
+        o.color_clear_value = d.colorClearValue;
+        o.update_bounds[0] = d.renderTargetUpdateBounds.left;
+        o.update_bounds[1] = d.renderTargetUpdateBounds.top;
+        o.update_bounds[2] = d.renderTargetUpdateBounds.right;
+        o.update_bounds[3] = d.renderTargetUpdateBounds.bottom;
+        o.combined_shader_features =
+            static_cast<uint32_t>(d.combinedShaderFeatures);
+        o.dither_mode = static_cast<uint32_t>(d.ditherMode);
+        o.flush_uniform_offset_bytes =
+            static_cast<uint32_t>(d.flushUniformDataOffsetInBytes);
+        o.path_count = d.pathCount;
+        o.first_path = static_cast<uint32_t>(d.firstPath);
+        o.first_paint = static_cast<uint32_t>(d.firstPaint);
+        o.first_paint_aux = static_cast<uint32_t>(d.firstPaintAux);
+        o.contour_count = d.contourCount;
+        o.first_contour = static_cast<uint32_t>(d.firstContour);
+        o.grad_span_count = d.gradSpanCount;
+        o.first_grad_span = static_cast<uint32_t>(d.firstGradSpan);
+        o.tess_span_count = d.tessVertexSpanCount;
+        o.first_tess_span = static_cast<uint32_t>(d.firstTessVertexSpan);
+        o.grad_data_height = d.gradDataHeight;
+        o.tess_data_height = d.tessDataHeight;
+        o.wireframe = d.wireframe;
+        o.clockwise_fill_override = d.clockwiseFillOverride;
+        o.has_triangle_vertices = d.hasTriangleVertices;
+        if (d.drawList != nullptr)
+        {
+            for (const DrawBatch& b : *d.drawList)
+            {
+                rive_cuda_draw_batch ob;
+                ob.draw_type = static_cast<uint32_t>(b.drawType);
+                ob.element_count = b.elementCount;
+                ob.base_element = b.baseElement;
+                ob.shader_features = static_cast<uint32_t>(b.shaderFeatures);
+                ob.draw_contents = static_cast<uint32_t>(b.drawContents);
+                ob.shader_misc_flags =
+                    static_cast<uint32_t>(b.shaderMiscFlags);
+                ob.first_blend_mode = static_cast<uint32_t>(b.firstBlendMode);
+                ob.barriers = static_cast<uint32_t>(b.barriers);
+                rec.batches.push_back(ob);
+            }
+        }
+        o.draw_batch_count = static_cast<uint32_t>(rec.batches.size());
+        flushes.push_back(std::move(rec));
+    }
+
+private:
+    std::vector<uint8_t>* m_nextStorageSink = &m_discard;
+    std::vector<uint8_t>* m_nextVertexSink = &m_discard;
+    std::vector<uint8_t> m_discard;
+};
+
+std::vector<uint8_t> read_file(const char* path)
+{
+    std::vector<uint8_t> data;
+    FILE* f = fopen(path, "rb");
+    if (!f)
+        return data;
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    data.resize(static_cast<size_t>(n));
+    if (n > 0 && fread(data.data(), 1, static_cast<size_t>(n), f) !=
+                     static_cast<size_t>(n))
+        data.clear();
+    fclose(f);
+    return data;
+}
+
+int fail(const char* msg)
+{
+    fprintf(stderr, "ref_capture: %s\n", msg);
+    return 1;
+}
+} // namespace
+
+int main(int argc, char** argv)
+{
+    if (argc != 3)
+        return fail("usage: ref_capture <scene.bin> <capture.bin>");
+    std::vector<uint8_t> scene = read_file(argv[1]);
+    if (scene.size() < sizeof(rive_scene_header))
+        return fail("cannot read scene");
+    rive_scene_header hdr;
+    memcpy(&hdr, scene.data(), sizeof(hdr));
+    if (hdr.magic != RIVE_SCENE_MAGIC)
+        return fail("bad scene magic");
+    size_t off = sizeof(hdr);
+    auto* paths = reinterpret_cast<const rive_scene_path*>(scene.data() + off);
+    off += sizeof(rive_scene_path) * hdr.path_count;
+    auto* paints = reinterpret_cast<const rive_scene_paint*>(scene.data() + off);
+    off += sizeof(rive_scene_paint) * hdr.paint_count;
+    auto* cmds = reinterpret_cast<const rive_scene_cmd*>(scene.data() + off);
+    off += sizeof(rive_scene_cmd) * hdr.cmd_count;
+    const uint8_t* verbs = scene.data() + off;
+    off += (hdr.verb_count + 3u) & ~3u;
+    auto* points = reinterpret_cast<const float*>(scene.data() + off);
+    off += sizeof(float) * 2 * hdr.point_count;
+    auto* stops = reinterpret_cast<const rive_scene_stop*>(scene.data() + off);
+    off += sizeof(rive_scene_stop) * hdr.stop_count;
+    if (off > scene.size())
+        return fail("truncated scene");
+
+    CaptureImpl* impl = nullptr;
+    std::unique_ptr<RenderContext> ctx = CaptureImpl::Make(&impl);
+
+    std::vector<rcp<RenderPath>> renderPaths;
+    for (uint32_t i = 0; i < hdr.path_count; ++i)
+    {
+        const rive_scene_path& p = paths[i];
+        RawPath raw;
+        const float* pts = points + 2 * p.point_offset;
+        for (uint32_t v = 0; v < p.verb_count; ++v)
+        {
+            switch (verbs[p.verb_offset + v])
+            {
+                case RIVE_SCENE_VERB_MOVE:
+                    raw.move({pts[0], pts[1]});
+                    pts += 2;
+                    break;
+                case RIVE_SCENE_VERB_LINE:
+                    raw.line({pts[0], pts[1]});
+                    pts += 2;
+                    break;
+                case RIVE_SCENE_VERB_QUAD:
+                    raw.quad({pts[0], pts[1]}, {pts[2], pts[3]});
+                    pts += 4;
+                    break;
+                case RIVE_SCENE_VERB_CUBIC:
+                    raw.cubic({pts[0], pts[1]},
+                              {pts[2], pts[3]},
+                              {pts[4], pts[5]});
+                    pts += 6;
+                    break;
+                case RIVE_SCENE_VERB_CLOSE:
+                    raw.close();
+                    break;
+                default:
+                    return fail("bad verb");
+            }
+        }
+        renderPaths.push_back(
+            ctx->makeRenderPath(raw, static_cast<FillRule>(p.fill_rule)));
+    }
+
+    std::vector<rcp<RenderPaint>> renderPaints;
+    for (uint32_t i = 0; i < hdr.paint_count; ++i)
+    {
+        const rive_scene_paint& s = paints[i];
+        rcp<RenderPaint> paint = ctx->makeRenderPaint();
+        paint->style(s.style == RIVE_SCENE_STYLE_FILL ? RenderPaintStyle::fill
+                                                      : RenderPaintStyle::stroke);
+        paint->color(s.color);
+        paint->thickness(s.thickness);
+        paint->join(static_cast<StrokeJoin>(s.join));
+        paint->cap(static_cast<StrokeCap>(s.cap));
+        paint->blendMode(static_cast<BlendMode>(s.blend_mode));
+        if (s.shader != RIVE_SCENE_SHADER_NONE)
+        {
+            std::vector<ColorInt> colors(s.stop_count);
+            std::vector<float> pos(s.stop_count);
+            for (uint32_t k = 0; k < s.stop_count; ++k)
+            {
+                colors[k] = stops[s.stop_offset + k].color;
+                pos[k] = stops[s.stop_offset + k].position;
+            }
+            rcp<RenderShader> shader =
+                s.shader == RIVE_SCENE_SHADER_LINEAR
+                    ? ctx->makeLinearGradient(s.g[0],
+                                              s.g[1],
+                                              s.g[2],
+                                              s.g[3],
+                                              colors.data(),
+                                              pos.data(),
+                                              s.stop_count)
+                    : ctx->makeRadialGradient(s.g[0],
+                                              s.g[1],
+                                              s.g[2],
+                                              colors.data(),
+                                              pos.data(),
+                                              s.stop_count);
+            paint->shader(shader);
+        }
+        renderPaints.push_back(paint);
+    }
+
+    rcp<RenderTarget> target =
+        impl->makeRenderTarget(hdr.width, hdr.height);
+    RenderContext::FrameDescriptor fd;
+    fd.renderTargetWidth = hdr.width;
+    fd.renderTargetHeight = hdr.height;
+    fd.loadAction = LoadAction::clear;
+    fd.clearColor = hdr.clear_color;
+    fd.ditherMode = static_cast<DitherMode>(hdr.dither_mode);
+    // Never triangulate: midpoint fans for every fill, independent of timing.
+    fd.triangulationThresholds.frameBudgetMs = 0;
+    ctx->beginFrame(fd);
+    {
+        RiveRenderer renderer(ctx.get());
+        for (uint32_t i = 0; i < hdr.cmd_count; ++i)
+        {
+            const rive_scene_cmd& c = cmds[i];
+            switch (c.op)
+            {
+                case RIVE_SCENE_CMD_SAVE:
+                    renderer.save();
+                    break;
+                case RIVE_SCENE_CMD_RESTORE:
+                    renderer.restore();
+                    break;
+                case RIVE_SCENE_CMD_TRANSFORM:
+                    renderer.transform(
+                        Mat2D(c.m[0], c.m[1], c.m[2], c.m[3], c.m[4], c.m[5]));
+                    break;
+                case RIVE_SCENE_CMD_DRAW_PATH:
+                    renderer.drawPath(renderPaths[c.a].get(),
+                                      renderPaints[c.b].get());
+                    break;
+                case RIVE_SCENE_CMD_CLIP_PATH:
+                    renderer.clipPath(renderPaths[c.a].get());
+                    break;
+                default:
+                    return fail("bad command");
+            }
+        }
+    }
+    ctx->flush({.renderTarget = target.get()});
+
+    FILE* f = fopen(argv[2], "wb");
+    if (!f)
+        return fail("cannot open output");
+    uint32_t head[4] = {0x31504352u /*RCP1*/, hdr.width, hdr.height, 7};
+    fwrite(head, sizeof(head), 1, f);
+    static const uint8_t zeros[8] = {};
+    for (int k = 0; k < 7; ++k)
+    {
+        uint64_t n = impl->buffers[k].size();
+        fwrite(&n, sizeof(n), 1, f);
+        if (n)
+            fwrite(impl->buffers[k].data(), 1, n, f);
+        fwrite(zeros, 1, (8 - (n & 7)) & 7, f);
+    }
+    uint32_t nf = static_cast<uint32_t>(impl->flushes.size());
+    fwrite(&nf, sizeof(nf), 1, f);
+    for (const FlushRecord& r : impl->flushes)
+    {
+        fwrite(&r.desc, sizeof(r.desc), 1, f);
+        if (!r.batches.empty())
+            fwrite(r.batches.data(),
+                   sizeof(rive_cuda_draw_batch),
+                   r.batches.size(),
+                   f);
+    }
+    fclose(f);
+    return 0;
+}

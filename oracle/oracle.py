@@ -1,0 +1,184 @@
+"""TEST INFRASTRUCTURE: ctypes binding of the CPU oracle (passes.c) and of the
+reference front-end replay (oracle/_ref/ref_capture, built here only).
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg import this
+module, and only to check or time against; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_build", "liboracle_passes.so")
+REF_CAPTURE = os.path.join(HERE, "_ref", "ref_capture")
+REFERENCE_SOURCES = "/root/reference"
+
+BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
+                "grad_spans", "tess_spans")
+
+
+class FlushDesc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "render_target_width", "render_target_height", "interlock_mode",
+        "color_load_action", "color_clear_value")] + [
+        ("update_bounds", ctypes.c_int32 * 4)] + [
+        (n, ctypes.c_uint32) for n in (
+            "combined_shader_features", "dither_mode",
+            "flush_uniform_offset_bytes", "path_count", "first_path",
+            "first_paint", "first_paint_aux", "contour_count", "first_contour",
+            "grad_span_count", "first_grad_span", "tess_span_count",
+            "first_tess_span", "grad_data_height", "tess_data_height",
+            "wireframe", "clockwise_fill_override", "has_triangle_vertices",
+            "draw_batch_count")] + [("draw_batches", ctypes.c_void_p)]
+
+
+class OracleBuffers(ctypes.Structure):
+    _fields_ = []
+    for _n in BUFFER_NAMES:
+        _fields_ += [(_n, ctypes.c_void_p), (_n + "_bytes", ctypes.c_size_t)]
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "passes"])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+        for name in ("oracle_color_ramps", "oracle_tessellate", "oracle_draw",
+                     "oracle_flush", "oracle_tessellate_f64"):
+            getattr(_lib, name).restype = ctypes.c_int
+        _lib.oracle_f32_to_f16.restype = ctypes.c_uint16
+        _lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
+        _lib.oracle_f16_to_f32.restype = ctypes.c_float
+        _lib.oracle_f16_to_f32.argtypes = [ctypes.c_uint16]
+    return _lib
+
+
+def make_desc(flush):
+    """rive_cuda_flush_desc for one capture.Flush (keeps the batch array alive)."""
+    d = FlushDesc()
+    for k, v in flush.desc.items():
+        if k.startswith("ub"):
+            d.update_bounds[int(k[2])] = v
+        elif k != "draw_batch_count":
+            setattr(d, k, v)
+    batches = np.ascontiguousarray(flush.batches, dtype=np.uint32)
+    d.draw_batch_count = len(batches)
+    d.draw_batches = batches.ctypes.data if len(batches) else None
+    return d, batches
+
+
+def make_buffers(cap):
+    keep = []
+    b = OracleBuffers()
+    for n in BUFFER_NAMES:
+        data = cap.buffers.get(n, b"")
+        arr = np.frombuffer(data, dtype=np.uint8).copy() if data else np.zeros(16, np.uint8)
+        keep.append(arr)
+        setattr(b, n, arr.ctypes.data)
+        setattr(b, n + "_bytes", len(data))
+    return b, keep
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with {rc}")
+
+
+def color_ramps(cap, fi=0):
+    f = cap.flushes[fi]
+    d, _k1 = make_desc(f)
+    b, _k2 = make_buffers(cap)
+    h = max(int(f.desc["grad_data_height"]), 1)
+    out = np.zeros((h, 512, 4), np.uint8)
+    _check(lib().oracle_color_ramps(ctypes.byref(d), ctypes.byref(b),
+                                    out.ctypes.data_as(ctypes.c_void_p)), "color ramps")
+    return out
+
+
+def tessellate(cap, fi=0):
+    f = cap.flushes[fi]
+    d, _k1 = make_desc(f)
+    b, _k2 = make_buffers(cap)
+    h = max(int(f.desc["tess_data_height"]), 1)
+    out = np.zeros((h * 2048, 4), np.uint32)
+    _check(lib().oracle_tessellate(ctypes.byref(d), ctypes.byref(b),
+                                   out.ctypes.data_as(ctypes.c_void_p)), "tessellate")
+    return out
+
+
+def tessellate_f64(cap, fi=0):
+    f = cap.flushes[fi]
+    d, _k1 = make_desc(f)
+    b, _k2 = make_buffers(cap)
+    h = max(int(f.desc["tess_data_height"]), 1)
+    xy = np.zeros((h * 2048, 2), np.float64)
+    flags = np.zeros(h * 2048, np.uint32)
+    _check(lib().oracle_tessellate_f64(ctypes.byref(d), ctypes.byref(b),
+                                       xy.ctypes.data_as(ctypes.c_void_p),
+                                       flags.ctypes.data_as(ctypes.c_void_p)),
+           "tessellate_f64")
+    return xy, flags
+
+
+def render(cap, threads=0, fb=None):
+    """Runs every logical flush of the capture in order; returns HxWx4 RGBA8."""
+    if fb is None:
+        fb = np.zeros((cap.height, cap.width, 4), np.uint8)
+    b, _keep = make_buffers(cap)
+    for f in cap.flushes:
+        d, _k = make_desc(f)
+        _check(lib().oracle_flush(ctypes.byref(d), ctypes.byref(b),
+                                  fb.ctypes.data_as(ctypes.c_void_p), int(threads)),
+               "flush")
+    return fb
+
+
+def last_stats():
+    t = ctypes.c_uint64()
+    fr = ctypes.c_uint64()
+    lib().oracle_last_stats(ctypes.byref(t), ctypes.byref(fr))
+    return t.value, fr.value
+
+
+def f32_to_f16(x):
+    return lib().oracle_f32_to_f16(float(x))
+
+
+def f16_to_f32(h):
+    return lib().oracle_f16_to_f32(int(h))
+
+
+def reference_available():
+    return os.path.isdir(REFERENCE_SOURCES)
+
+
+def build_reference():
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"])
+
+
+def reference_capture(scene_bytes: bytes) -> bytes:
+    """Runs the reference front end on a scene; returns the capture bytes."""
+    if not os.path.exists(REF_CAPTURE):
+        build_reference()
+    with tempfile.TemporaryDirectory() as td:
+        sp = os.path.join(td, "scene.bin")
+        cp = os.path.join(td, "capture.bin")
+        with open(sp, "wb") as f:
+            f.write(scene_bytes)
+        subprocess.check_call([REF_CAPTURE, sp, cp])
+        with open(cp, "rb") as f:
+            return f.read()

@@ -1,0 +1,1849 @@
+/*
+ * passes.c -- TEST INFRASTRUCTURE (the oracle). A plain, unoptimised C
+ * restatement of rive-runtime's rasterOrdering GPU passes. Only tests, the
+ * smoke check and the benchmark's CPU-baseline leg may load it, and only as
+ * the checker. See passes.h for what each function restates.
+ *
+ * Arithmetic follows the GLSL statement by statement in fp32 (built with
+ * -ffp-contract=off), with libm for acos/sin/cos/sqrt. `half` values of the
+ * shaders are computed in fp32 (desktop mediump) and rounded to fp16 exactly
+ * where the shaders pack them into pixel local storage (packHalf2x16).
+ */
+#include "passes.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- constants (renderer/src/shaders/constants.glsl) --------------------- */
+#define TESS_TEXTURE_WIDTH 2048
+#define GRAD_TEXTURE_WIDTH 512
+#define PI_F 3.14159265359f
+#define TWO_PI_F 6.28318530718f
+#define AA_RADIUS 0.5f
+#define GRAD_SPAN_FLAG_LEFT_BORDER 0x80000000u
+#define GRAD_SPAN_FLAG_RIGHT_BORDER 0x40000000u
+#define GRAD_SPAN_FLAG_COMPLEX_BORDER 0x20000000u
+#define GRAD_SPAN_FLAGS_MASK 0xe0000000u
+#define RETROFIT_TRI_STRIP_CONTOUR_FLAG (1u << 31)
+#define CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG (1u << 29)
+#define JOIN_TYPE_MASK (7u << 26)
+#define MITER_CLIP_JOIN_CONTOUR_FLAG (5u << 26)
+#define MITER_REVERT_JOIN_CONTOUR_FLAG (4u << 26)
+#define BEVEL_JOIN_CONTOUR_FLAG (3u << 26)
+#define ROUND_JOIN_CONTOUR_FLAG (2u << 26)
+#define FEATHER_JOIN_CONTOUR_FLAG (1u << 26)
+#define EMULATED_STROKE_CAP_CONTOUR_FLAG (1u << 25)
+#define NEGATE_PATH_FILL_COVERAGE_FLAG (1u << 24)
+#define MIRRORED_CONTOUR_CONTOUR_FLAG (1u << 23)
+#define JOIN_TANGENT_0_CONTOUR_FLAG (1u << 22)
+#define JOIN_TANGENT_INNER_CONTOUR_FLAG (1u << 21)
+#define LEFT_JOIN_CONTOUR_FLAG (1u << 20)
+#define RIGHT_JOIN_CONTOUR_FLAG (1u << 19)
+#define CONTOUR_ID_MASK 0xffffu
+#define STROKE_VERTEX 0
+#define FAN_VERTEX 1
+#define FAN_MIDPOINT_VERTEX 2
+#define CLIP_UPDATE_PAINT_TYPE 0u
+#define SOLID_COLOR_PAINT_TYPE 1u
+#define LINEAR_GRADIENT_PAINT_TYPE 2u
+#define RADIAL_GRADIENT_PAINT_TYPE 3u
+#define PAINT_FLAG_EVEN_ODD_FILL 0x200u
+#define PAINT_FLAG_HAS_CLIP_RECT 0x400u
+#define MAX_DENORM_F16 1023u
+#define EPSILON_FP16_NON_DENORM 6.2e-5f
+#define BLEND_SRC_OVER 0
+#define BLEND_MODE_SCREEN 1
+#define BLEND_MODE_OVERLAY 2
+#define BLEND_MODE_DARKEN 3
+#define BLEND_MODE_LIGHTEN 4
+#define BLEND_MODE_COLORDODGE 5
+#define BLEND_MODE_COLORBURN 6
+#define BLEND_MODE_HARDLIGHT 7
+#define BLEND_MODE_SOFTLIGHT 8
+#define BLEND_MODE_DIFFERENCE 9
+#define BLEND_MODE_EXCLUSION 10
+#define BLEND_MODE_MULTIPLY 11
+#define BLEND_MODE_HUE 12
+#define BLEND_MODE_SATURATION 13
+#define BLEND_MODE_COLOR 14
+#define BLEND_MODE_LUMINOSITY 15
+
+/* gpu::ShaderFeatures (gpu.hpp:840-856). */
+#define SF_CLIPPING (1u << 0)
+#define SF_CLIP_RECT (1u << 1)
+#define SF_ADVANCED_BLEND (1u << 2)
+#define SF_FEATHER (1u << 3)
+#define SF_EVEN_ODD (1u << 4)
+#define SF_NESTED_CLIPPING (1u << 5)
+#define SF_HSL_BLEND_MODES (1u << 6)
+#define SF_DITHER (1u << 7)
+
+/* Patch geometry (gpu.hpp:591-640). */
+#define PATCH_SEGMENT_SPAN 8
+#define PATCH_VERTEX_COUNT 42
+#define PATCH_INDEX_COUNT 72
+
+/* Sub-pixel precision of the rasteriser (Vulkan minimum is 4 bits; desktop
+ * parts use 8). */
+#define SUBPIXEL_BITS 8
+#define SUBPIXEL_ONE (1 << SUBPIXEL_BITS)
+
+typedef struct
+{
+    float x, y;
+} f2;
+
+static uint64_t g_stat_triangles, g_stat_fragments;
+
+/* ---- half floats --------------------------------------------------------- */
+uint16_t oracle_f32_to_f16(float f)
+{
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    uint32_t sign = (x >> 16) & 0x8000u;
+    uint32_t e = (x >> 23) & 0xffu;
+    uint32_t m = x & 0x7fffffu;
+    if (e == 0xffu) /* inf / nan */
+        return (uint16_t)(sign | 0x7c00u | (m ? 0x200u : 0));
+    int32_t he = (int32_t)e - 127 + 15;
+    if (he >= 31)
+        return (uint16_t)(sign | 0x7c00u);
+    if (he <= 0)
+    {
+        if (he < -10)
+            return (uint16_t)sign;
+        m |= 0x800000u;
+        uint32_t shift = (uint32_t)(14 - he);
+        uint32_t hm = m >> shift;
+        uint32_t rem = m & ((1u << shift) - 1);
+        uint32_t half = 1u << (shift - 1);
+        if (rem > half || (rem == half && (hm & 1u)))
+            ++hm;
+        return (uint16_t)(sign | hm);
+    }
+    uint32_t hm = m >> 13;
+    uint32_t rem = m & 0x1fffu;
+    uint32_t h = ((uint32_t)he << 10) | hm;
+    if (rem > 0x1000u || (rem == 0x1000u && (hm & 1u)))
+        ++h; /* may carry into the exponent, which is correct */
+    return (uint16_t)(sign | h);
+}
+
+float oracle_f16_to_f32(uint16_t h)
+{
+    uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+    uint32_t e = (h >> 10) & 0x1fu;
+    uint32_t m = h & 0x3ffu;
+    uint32_t x;
+    if (e == 0)
+    {
+        if (m == 0)
+            x = sign;
+        else
+        {
+            int32_t ee = -1;
+            do
+            {
+                ++ee;
+                m <<= 1;
+            } while ((m & 0x400u) == 0);
+            x = sign | ((uint32_t)(127 - 15 - ee) << 23) | ((m & 0x3ffu) << 13);
+        }
+    }
+    else if (e == 31)
+        x = sign | 0x7f800000u | (m << 13);
+    else
+        x = sign | ((e - 15 + 127) << 23) | (m << 13);
+    float f;
+    memcpy(&f, &x, 4);
+    return f;
+}
+
+static inline float u2f(uint32_t u)
+{
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+static inline uint32_t f2u(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
+static inline float clampf(float x, float lo, float hi)
+{
+    return x < lo ? lo : (x > hi ? hi : x);
+}
+static inline float minf(float a, float b) { return a < b ? a : b; }
+static inline float maxf(float a, float b) { return a > b ? a : b; }
+static inline float signf(float x)
+{
+    return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);
+}
+static inline float fractf(float x) { return x - floorf(x); }
+/* GLSL mod(x, y) = x - y * floor(x / y). */
+static inline float glsl_mod(float x, float y) { return x - y * floorf(x / y); }
+static inline float dot2(f2 a, f2 b) { return a.x * b.x + a.y * b.y; }
+static inline f2 sub2(f2 a, f2 b) { return (f2){a.x - b.x, a.y - b.y}; }
+static inline f2 add2(f2 a, f2 b) { return (f2){a.x + b.x, a.y + b.y}; }
+static inline f2 mul2(f2 a, float s) { return (f2){a.x * s, a.y * s}; }
+static inline f2 normalize2(f2 v)
+{
+    float inv = 1.f / sqrtf(dot2(v, v));
+    return (f2){v.x * inv, v.y * inv};
+}
+static inline float det2(f2 c0, f2 c1) { return c0.x * c1.y - c1.x * c0.y; }
+static inline int neq2(f2 a, f2 b) { return a.x != b.x || a.y != b.y; }
+
+/* bezier_utils.glsl:24-32 */
+static float cosine_between_vectors(f2 a, f2 b)
+{
+    float ab_cosTheta = dot2(a, b);
+    float ab_pow2 = dot2(a, a) * dot2(b, b);
+    return (ab_pow2 == 0.f) ? 1.f
+                            : clampf(ab_cosTheta * (1.f / sqrtf(ab_pow2)),
+                                     -1.f,
+                                     1.f);
+}
+
+/* bezier_utils.glsl:65-71 */
+static void find_cubic_tangents(f2 p0, f2 p1, f2 p2, f2 p3, f2* t0, f2* t1)
+{
+    *t0 = sub2(neq2(p0, p1) ? p1 : neq2(p1, p2) ? p2 : p3, p0);
+    *t1 = sub2(p3, neq2(p3, p2) ? p2 : neq2(p2, p1) ? p1 : p0);
+}
+
+/* common.glsl atan2 */
+static float rive_atan2(f2 v)
+{
+    v = normalize2(v);
+    float theta = acosf(clampf(v.x, -1.f, 1.f));
+    return v.y >= 0.f ? theta : -theta;
+}
+
+/* ---- pass 1: color ramps (color_ramp.glsl:40-107) ------------------------ */
+static void unpack_color_int(uint32_t c, float out[4])
+{
+    out[0] = (float)((c >> 16) & 0xffu) / 255.f;
+    out[1] = (float)((c >> 8) & 0xffu) / 255.f;
+    out[2] = (float)((c >> 0) & 0xffu) / 255.f;
+    out[3] = (float)((c >> 24) & 0xffu) / 255.f;
+}
+
+static inline uint8_t unorm8(float x)
+{
+    x = clampf(x, 0.f, 1.f);
+    return (uint8_t)floorf(x * 255.f + 0.5f);
+}
+
+int oracle_color_ramps(const rive_cuda_flush_desc* d,
+                       const oracle_buffers* b,
+                       uint8_t* grad)
+{
+    const uint32_t H = d->grad_data_height;
+    memset(grad, 0, (size_t)GRAD_TEXTURE_WIDTH * H * 4);
+    if (d->grad_span_count == 0)
+        return 0;
+    if ((size_t)(d->first_grad_span + d->grad_span_count) * 16 >
+        b->grad_spans_bytes)
+        return -1;
+    const uint32_t* spans = (const uint32_t*)b->grad_spans;
+    for (uint32_t s = 0; s < d->grad_span_count; ++s)
+    {
+        const uint32_t* sp = spans + 4 * (size_t)(d->first_grad_span + s);
+        uint32_t yWithFlags = sp[1];
+        uint32_t y = yWithFlags & ~GRAD_SPAN_FLAGS_MASK;
+        if (y >= H)
+            continue;
+        /* Column x positions of the 8-vertex strip, in texels. */
+        float cx[4];
+        cx[0] = cx[1] = (float)(sp[0] & 0xffffu) / 65536.f;
+        cx[2] = cx[3] = (float)(sp[0] >> 16) / 65536.f;
+        if (yWithFlags & GRAD_SPAN_FLAG_LEFT_BORDER)
+            cx[0] = (yWithFlags & GRAD_SPAN_FLAG_COMPLEX_BORDER)
+                        ? 0.f
+                        : cx[0] - 1.f / GRAD_TEXTURE_WIDTH;
+        if (yWithFlags & GRAD_SPAN_FLAG_RIGHT_BORDER)
+            cx[3] = (yWithFlags & GRAD_SPAN_FLAG_COMPLEX_BORDER)
+                        ? 1.f
+                        : cx[3] + 1.f / GRAD_TEXTURE_WIDTH;
+        float c0[4], c1[4];
+        unpack_color_int(sp[2], c0);
+        unpack_color_int(sp[3], c1);
+        for (int q = 0; q < 3; ++q)
+        {
+            float xa = cx[q] * GRAD_TEXTURE_WIDTH;
+            float xb = cx[q + 1] * GRAD_TEXTURE_WIDTH;
+            if (!(xb > xa))
+                continue;
+            for (int i = 0; i < GRAD_TEXTURE_WIDTH; ++i)
+            {
+                float pc = (float)i + .5f;
+                /* Left edge inclusive, right edge exclusive (top-left). */
+                if (pc < xa || pc >= xb)
+                    continue;
+                float col[4];
+                if (q == 0)
+                    memcpy(col, c0, sizeof(col));
+                else if (q == 2)
+                    memcpy(col, c1, sizeof(col));
+                else
+                {
+                    float t = (pc - xa) / (xb - xa);
+                    for (int k = 0; k < 4; ++k)
+                        col[k] = c0[k] + (c1[k] - c0[k]) * t;
+                }
+                uint8_t* px = grad + ((size_t)y * GRAD_TEXTURE_WIDTH + i) * 4;
+                for (int k = 0; k < 4; ++k)
+                    px[k] = unorm8(col[k]);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ---- pass 2: tessellation (tessellate.glsl:61-567) ------------------------ */
+typedef struct
+{
+    f2 p0, p1, p2, p3;
+    float totalVertexCount;
+    float parametricSegmentCount;
+    float joinSegmentCount;
+    float radsPerPolarSegment;
+    f2 joinTangent;
+    float radsPerJoinSegment;
+    uint32_t contourIDWithFlags;
+} tess_varyings;
+
+static const float* path_record(const rive_cuda_flush_desc* d,
+                                const oracle_buffers* b,
+                                uint32_t pathID)
+{
+    size_t idx = (size_t)d->first_path + pathID;
+    if ((idx + 1) * 64 > b->paths_bytes)
+        return NULL;
+    return (const float*)b->paths + idx * 16;
+}
+
+static const uint32_t* contour_record(const rive_cuda_flush_desc* d,
+                                      const oracle_buffers* b,
+                                      uint32_t contourID)
+{
+    size_t idx = (size_t)d->first_contour + contourID - 1;
+    if ((idx + 1) * 16 > b->contours_bytes)
+        return NULL;
+    return (const uint32_t*)b->contours + idx * 4;
+}
+
+/* Vertex-shader half of pass 2, evaluated once per span rectangle. */
+static int tess_setup(const rive_cuda_flush_desc* d,
+                      const oracle_buffers* b,
+                      const uint32_t* sp,
+                      int second,
+                      tess_varyings* v,
+                      int* out_x0,
+                      int* out_x1,
+                      float* out_y)
+{
+    const float* spf = (const float*)sp;
+    f2 p0 = {spf[0], spf[1]}, p1 = {spf[2], spf[3]};
+    f2 p2 = {spf[4], spf[5]}, p3 = {spf[6], spf[7]};
+    float y = second ? spf[11] : spf[10];
+    int32_t x0x1 = (int32_t)(second ? sp[13] : sp[12]);
+    int x0 = (int32_t)((uint32_t)x0x1 << 16) >> 16;
+    int x1 = x0x1 >> 16;
+    uint32_t args_z = sp[14];
+    uint32_t parametricSegmentCount = args_z & 0x3ffu;
+    uint32_t polarSegmentCount = (args_z >> 10) & 0x3ffu;
+    uint32_t joinSegmentCount = args_z >> 20;
+    uint32_t contourIDWithFlags = sp[15];
+    uint32_t contourID = contourIDWithFlags & CONTOUR_ID_MASK;
+    uint32_t pathID = 0;
+    if (contourID > 0)
+    {
+        const uint32_t* c = contour_record(d, b, contourID);
+        if (!c)
+            return -1;
+        pathID = c[2];
+    }
+    float strokeRadius = 0, featherRadius = 0;
+    const float* path = NULL;
+    if (pathID != 0)
+    {
+        path = path_record(d, b, pathID);
+        if (!path)
+            return -1;
+        strokeRadius = path[6];
+        featherRadius = path[7];
+    }
+    if (featherRadius != 0.f && strokeRadius == 0.f)
+        return -2; /* feathered fills: not supported */
+    if (contourIDWithFlags & CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG)
+    {
+        if (!path)
+            path = path_record(d, b, pathID);
+        if (!path)
+            return -1;
+        /* mat = [[m0, m1], [m2, m3]] columns; MUL(mat, v). */
+        f2 a = {-2.f * p1.x + p2.x + p0.x, -2.f * p1.y + p2.y + p0.y};
+        f2 c = {-2.f * p2.x + p3.x + p1.x, -2.f * p2.y + p3.y + p1.y};
+        f2 d0 = {path[0] * a.x + path[2] * a.y, path[1] * a.x + path[3] * a.y};
+        f2 d1 = {path[0] * c.x + path[2] * c.y, path[1] * c.x + path[3] * c.y};
+        float m = maxf(dot2(d0, d0), dot2(d1, d1));
+        float n = maxf(ceilf(sqrtf(.75f * 4.f * sqrtf(m))), 1.f);
+        uint32_t un = (uint32_t)n;
+        parametricSegmentCount =
+            un < parametricSegmentCount ? un : parametricSegmentCount;
+    }
+    uint32_t totalVertexCount =
+        parametricSegmentCount + polarSegmentCount + joinSegmentCount - 1u;
+    f2 t0, t1;
+    find_cubic_tangents(p0, p1, p2, p3, &t0, &t1);
+    float theta = acosf(cosine_between_vectors(t0, t1));
+    float radsPerPolarSegment = theta / (float)polarSegmentCount;
+    float turn = det2(sub2(p2, p0), sub2(p3, p1));
+    if (turn == 0.f)
+        turn = det2(t0, t1);
+    if (turn < 0.f)
+        radsPerPolarSegment = -radsPerPolarSegment;
+    v->p0 = p0;
+    v->p1 = p1;
+    v->p2 = p2;
+    v->p3 = p3;
+    v->totalVertexCount = (float)totalVertexCount;
+    v->parametricSegmentCount = (float)parametricSegmentCount;
+    v->joinSegmentCount = (float)joinSegmentCount;
+    v->radsPerPolarSegment = radsPerPolarSegment;
+    v->joinTangent = (f2){spf[8], spf[9]};
+    v->radsPerJoinSegment = 0.f;
+    if (joinSegmentCount > 1u)
+    {
+        f2 jt = v->joinTangent;
+        float joinTheta = acosf(cosine_between_vectors(t1, jt));
+        float joinSpan = (float)joinSegmentCount;
+        if ((contourIDWithFlags &
+             (JOIN_TYPE_MASK | EMULATED_STROKE_CAP_CONTOUR_FLAG)) ==
+            (ROUND_JOIN_CONTOUR_FLAG | EMULATED_STROKE_CAP_CONTOUR_FLAG))
+            joinSpan -= 2.f;
+        float radsPerJoinSegment = joinTheta / joinSpan;
+        if (det2(t1, jt) < 0.f)
+            radsPerJoinSegment = -radsPerJoinSegment;
+        v->radsPerJoinSegment = radsPerJoinSegment;
+    }
+    if (x1 < x0)
+        contourIDWithFlags |= MIRRORED_CONTOUR_CONTOUR_FLAG;
+    v->contourIDWithFlags = contourIDWithFlags;
+    *out_x0 = x0;
+    *out_x1 = x1;
+    *out_y = y;
+    return 0;
+}
+
+/* Fragment half of pass 2 (tessellate.glsl:294-567): one vertex. */
+static void tess_fragment(const tess_varyings* v,
+                          float vertexIdxIn,
+                          uint32_t out[4])
+{
+    f2 p0 = v->p0, p1 = v->p1, p2 = v->p2, p3 = v->p3;
+    f2 tan0, tan1;
+    find_cubic_tangents(p0, p1, p2, p3, &tan0, &tan1);
+    float vertexIdx = maxf(floorf(vertexIdxIn), 0.f);
+    float totalVertexCount = v->totalVertexCount;
+    float parametricSegmentCount = v->parametricSegmentCount;
+    float joinSegmentCount = v->joinSegmentCount;
+    float radsPerPolarSegment = v->radsPerPolarSegment;
+    uint32_t contourIDWithFlags = v->contourIDWithFlags;
+
+    float mergedSegmentCount = totalVertexCount - joinSegmentCount;
+    float mergedVertexID = vertexIdx;
+    if (mergedVertexID <= mergedSegmentCount)
+    {
+        contourIDWithFlags &= ~JOIN_TYPE_MASK;
+    }
+    else
+    {
+        p0 = p1 = p2 = p3;
+        tan0 = tan1;
+        tan1 = v->joinTangent;
+        parametricSegmentCount = 1.f;
+        mergedVertexID -= mergedSegmentCount;
+        mergedSegmentCount = joinSegmentCount;
+        radsPerPolarSegment = v->radsPerJoinSegment;
+        if ((contourIDWithFlags & JOIN_TYPE_MASK) > ROUND_JOIN_CONTOUR_FLAG)
+        {
+            if (mergedVertexID < 2.5f)
+                contourIDWithFlags |= JOIN_TANGENT_0_CONTOUR_FLAG;
+            if (mergedVertexID > 1.5f && mergedVertexID < 3.5f)
+                contourIDWithFlags |= JOIN_TANGENT_INNER_CONTOUR_FLAG;
+        }
+        else if ((contourIDWithFlags & EMULATED_STROKE_CAP_CONTOUR_FLAG) ||
+                 (contourIDWithFlags & JOIN_TYPE_MASK) ==
+                     FEATHER_JOIN_CONTOUR_FLAG)
+        {
+            mergedSegmentCount -= 2.f;
+            mergedVertexID -= 1.f;
+        }
+        contourIDWithFlags |= radsPerPolarSegment < 0.f
+                                  ? LEFT_JOIN_CONTOUR_FLAG
+                                  : RIGHT_JOIN_CONTOUR_FLAG;
+    }
+
+    f2 tessCoord;
+    float theta = 0.f;
+    if (mergedVertexID == 0.f || mergedVertexID == mergedSegmentCount ||
+        (contourIDWithFlags & JOIN_TYPE_MASK) > ROUND_JOIN_CONTOUR_FLAG)
+    {
+        int isTan0 = mergedVertexID < mergedSegmentCount * .5f;
+        tessCoord = isTan0 ? p0 : p3;
+        theta = rive_atan2(isTan0 ? tan0 : tan1);
+    }
+    else if (contourIDWithFlags & RETROFIT_TRI_STRIP_CONTOUR_FLAG)
+    {
+        tessCoord = p0;
+        if (mergedVertexID >= 8.f)
+            tessCoord = p1;
+        if (mergedVertexID >= 12.f)
+            tessCoord = p2;
+        if (mergedVertexID >= 14.f)
+            tessCoord = v->joinTangent;
+    }
+    else
+    {
+        float T, polarT;
+        if (parametricSegmentCount == mergedSegmentCount)
+        {
+            T = mergedVertexID / parametricSegmentCount;
+            polarT = 0.f;
+        }
+        else
+        {
+            f2 C = sub2(p1, p0);
+            f2 D = sub2(p3, p0);
+            f2 E = sub2(p2, p1);
+            f2 B = sub2(E, C);
+            f2 A = add2(mul2(E, -3.f), D);
+            f2 B_ = mul2(B, parametricSegmentCount * 2.f);
+            f2 C_ = mul2(C, parametricSegmentCount * parametricSegmentCount);
+            float lastParametricVertexID = 0.f;
+            float maxParametricVertexID =
+                minf(parametricSegmentCount - 1.f, mergedVertexID);
+            f2 tan0norm = normalize2(tan0);
+            float negAbsRadsPerSegment = -fabsf(radsPerPolarSegment);
+            float maxRotation0 = (1.f + mergedVertexID) * fabsf(radsPerPolarSegment);
+            for (int p = 9; p >= 0; --p)
+            {
+                float testParametricID = lastParametricVertexID + exp2f((float)p);
+                if (testParametricID <= maxParametricVertexID)
+                {
+                    f2 testTan = add2(mul2(A, testParametricID), B_);
+                    testTan = add2(mul2(testTan, testParametricID), C_);
+                    float cosRotation = dot2(normalize2(testTan), tan0norm);
+                    float maxRotation =
+                        testParametricID * negAbsRadsPerSegment + maxRotation0;
+                    maxRotation = minf(maxRotation, PI_F);
+                    if (cosRotation >= cosf(maxRotation))
+                        lastParametricVertexID = testParametricID;
+                }
+            }
+            float parametricT = lastParametricVertexID / parametricSegmentCount;
+            float lastPolarVertexID = mergedVertexID - lastParametricVertexID;
+            float theta0 = acosf(clampf(tan0norm.x, -1.f, 1.f));
+            theta0 = tan0norm.y >= 0.f ? theta0 : -theta0;
+            theta = lastPolarVertexID * radsPerPolarSegment + theta0;
+            f2 norm = {sinf(theta), -cosf(theta)};
+            float a = dot2(norm, A), b_over_2 = dot2(norm, B), c = dot2(norm, C);
+            float discr_over_4 = maxf(b_over_2 * b_over_2 - a * c, 0.f);
+            float q = sqrtf(discr_over_4);
+            if (b_over_2 > 0.f)
+                q = -q;
+            q -= b_over_2;
+            float _5qa = -.5f * q * a;
+            float rs, rt;
+            if (fabsf(q * q + _5qa) < fabsf(a * c + _5qa))
+            {
+                rs = q;
+                rt = a;
+            }
+            else
+            {
+                rs = c;
+                rt = q;
+            }
+            polarT = (rt != 0.f) ? rs / rt : 0.f;
+            polarT = clampf(polarT, 0.f, 1.f);
+            if (lastPolarVertexID == 0.f)
+                polarT = 0.f;
+            T = maxf(parametricT, polarT);
+        }
+        /* unchecked_mix(a, b, t) = (b - a) * t + a */
+        f2 ab = add2(mul2(sub2(p1, p0), T), p0);
+        f2 bc = add2(mul2(sub2(p2, p1), T), p1);
+        f2 cd = add2(mul2(sub2(p3, p2), T), p2);
+        f2 abc = add2(mul2(sub2(bc, ab), T), ab);
+        f2 bcd = add2(mul2(sub2(cd, bc), T), bc);
+        tessCoord = add2(mul2(sub2(bcd, abc), T), abc);
+        if (T != polarT)
+            theta = rive_atan2(sub2(bcd, abc));
+    }
+    out[0] = f2u(tessCoord.x);
+    out[1] = f2u(tessCoord.y);
+    out[2] = f2u(glsl_mod(theta, TWO_PI_F));
+    out[3] = contourIDWithFlags;
+}
+
+int oracle_tessellate(const rive_cuda_flush_desc* d,
+                      const oracle_buffers* b,
+                      uint32_t* tess)
+{
+    const uint32_t H = d->tess_data_height;
+    memset(tess, 0, (size_t)TESS_TEXTURE_WIDTH * H * 16);
+    if ((size_t)(d->first_tess_span + d->tess_span_count) * 64 >
+        b->tess_spans_bytes)
+        return -1;
+    const uint32_t* spans = (const uint32_t*)b->tess_spans;
+    for (uint32_t s = 0; s < d->tess_span_count; ++s)
+    {
+        const uint32_t* sp = spans + 16 * (size_t)(d->first_tess_span + s);
+        for (int second = 0; second < 2; ++second)
+        {
+            tess_varyings v;
+            int x0, x1;
+            float y;
+            int rc = tess_setup(d, b, sp, second, &v, &x0, &x1, &y);
+            if (rc != 0)
+                return rc;
+            if (isnan(y) || x0 == x1)
+                continue;
+            if (y < 0.f || y >= (float)H)
+                continue;
+            int row = (int)y;
+            int lo = x0 < x1 ? x0 : x1, hi = x0 < x1 ? x1 : x0;
+            if (lo < 0)
+                lo = 0;
+            if (hi > TESS_TEXTURE_WIDTH)
+                hi = TESS_TEXTURE_WIDTH;
+            for (int px = lo; px < hi; ++px)
+            {
+                float vertexIdx =
+                    v.totalVertexCount - fabsf((float)x1 - ((float)px + .5f));
+                tess_fragment(&v, vertexIdx,
+                              tess + ((size_t)row * TESS_TEXTURE_WIDTH + px) * 4);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ---- FP64 twin of pass 2 --------------------------------------------------
+ * The same algorithm evaluated in double, for the tessellated-vertex
+ * tolerance. Discrete choices (segment indices) are re-derived in double too.
+ */
+typedef struct
+{
+    double x, y;
+} d2;
+static inline d2 dsub(d2 a, d2 b) { return (d2){a.x - b.x, a.y - b.y}; }
+static inline d2 dadd(d2 a, d2 b) { return (d2){a.x + b.x, a.y + b.y}; }
+static inline d2 dmul(d2 a, double s) { return (d2){a.x * s, a.y * s}; }
+static inline double ddot(d2 a, d2 b) { return a.x * b.x + a.y * b.y; }
+static inline d2 dnorm(d2 v)
+{
+    double inv = 1.0 / sqrt(ddot(v, v));
+    return (d2){v.x * inv, v.y * inv};
+}
+static inline double ddet(d2 a, d2 b) { return a.x * b.y - b.x * a.y; }
+static inline double dclamp(double x, double lo, double hi)
+{
+    return x < lo ? lo : (x > hi ? hi : x);
+}
+static double dcos_between(d2 a, d2 b)
+{
+    double ab = ddot(a, b), p = ddot(a, a) * ddot(b, b);
+    return p == 0.0 ? 1.0 : dclamp(ab / sqrt(p), -1.0, 1.0);
+}
+static inline int dneq(d2 a, d2 b) { return a.x != b.x || a.y != b.y; }
+static void dtangents(d2 p0, d2 p1, d2 p2, d2 p3, d2* t0, d2* t1)
+{
+    *t0 = dsub(dneq(p0, p1) ? p1 : dneq(p1, p2) ? p2 : p3, p0);
+    *t1 = dsub(p3, dneq(p3, p2) ? p2 : dneq(p2, p1) ? p1 : p0);
+}
+
+int oracle_tessellate_f64(const rive_cuda_flush_desc* d,
+                          const oracle_buffers* b,
+                          double* xy,
+                          uint32_t* tess_flags)
+{
+    const uint32_t H = d->tess_data_height;
+    const size_t N = (size_t)TESS_TEXTURE_WIDTH * H;
+    memset(xy, 0, N * 2 * sizeof(double));
+    memset(tess_flags, 0, N * sizeof(uint32_t));
+    if ((size_t)(d->first_tess_span + d->tess_span_count) * 64 >
+        b->tess_spans_bytes)
+        return -1;
+    const uint32_t* spans = (const uint32_t*)b->tess_spans;
+    for (uint32_t s = 0; s < d->tess_span_count; ++s)
+    {
+        const uint32_t* sp = spans + 16 * (size_t)(d->first_tess_span + s);
+        for (int second = 0; second < 2; ++second)
+        {
+            tess_varyings v;
+            int x0, x1;
+            float y;
+            int rc = tess_setup(d, b, sp, second, &v, &x0, &x1, &y);
+            if (rc != 0)
+                return rc;
+            if (isnan(y) || x0 == x1 || y < 0.f || y >= (float)H)
+                continue;
+            int row = (int)y;
+            int lo = x0 < x1 ? x0 : x1, hi = x0 < x1 ? x1 : x0;
+            if (lo < 0)
+                lo = 0;
+            if (hi > TESS_TEXTURE_WIDTH)
+                hi = TESS_TEXTURE_WIDTH;
+            d2 P0 = {v.p0.x, v.p0.y}, P1 = {v.p1.x, v.p1.y};
+            d2 P2 = {v.p2.x, v.p2.y}, P3 = {v.p3.x, v.p3.y};
+            /* Re-derive radsPerPolarSegment in double. */
+            d2 T0, T1;
+            dtangents(P0, P1, P2, P3, &T0, &T1);
+            double polarCount = (double)(((sp[14]) >> 10) & 0x3ffu);
+            double rpp = acos(dcos_between(T0, T1)) / polarCount;
+            if (v.radsPerPolarSegment < 0.f)
+                rpp = -rpp;
+            for (int px = lo; px < hi; ++px)
+            {
+                size_t texel = (size_t)row * TESS_TEXTURE_WIDTH + px;
+                uint32_t f32out[4];
+                float vertexIdx =
+                    v.totalVertexCount - fabsf((float)x1 - ((float)px + .5f));
+                tess_fragment(&v, vertexIdx, f32out);
+                tess_flags[texel] = f32out[3];
+                /* Evaluate the same merged vertex in double. */
+                double vid = floor((double)vertexIdx);
+                if (vid < 0)
+                    vid = 0;
+                double merged = (double)v.totalVertexCount - v.joinSegmentCount;
+                d2 q0 = P0, q1 = P1, q2 = P2, q3 = P3;
+                d2 t0 = T0;
+                double pc = v.parametricSegmentCount;
+                double r = rpp;
+                double mid = vid;
+                int isJoin = 0;
+                if (mid > merged)
+                {
+                    isJoin = 1;
+                    q0 = q1 = q2 = q3;
+                    mid -= merged;
+                    merged = v.joinSegmentCount;
+                }
+                d2 out;
+                if (isJoin || mid == 0.0 || mid == merged ||
+                    (f32out[3] & RETROFIT_TRI_STRIP_CONTOUR_FLAG))
+                {
+                    out = (d2){u2f(f32out[0]), u2f(f32out[1])};
+                    if (!isJoin && !(f32out[3] & RETROFIT_TRI_STRIP_CONTOUR_FLAG))
+                        out = (mid < merged * .5) ? q0 : q3;
+                    else if (isJoin)
+                        out = q3;
+                }
+                else
+                {
+                    double T, polarT;
+                    if (pc == merged)
+                    {
+                        T = mid / pc;
+                        polarT = 0;
+                    }
+                    else
+                    {
+                        d2 C = dsub(q1, q0), D = dsub(q3, q0), E = dsub(q2, q1);
+                        d2 B = dsub(E, C), A = dadd(dmul(E, -3.0), D);
+                        d2 B_ = dmul(B, pc * 2.0), C_ = dmul(C, pc * pc);
+                        double last = 0, maxP = fmin(pc - 1.0, mid);
+                        d2 t0n = dnorm(t0);
+                        double neg = -fabs(r), mr0 = (1.0 + mid) * fabs(r);
+                        for (int p = 9; p >= 0; --p)
+                        {
+                            double tp = last + ldexp(1.0, p);
+                            if (tp <= maxP)
+                            {
+                                d2 tt = dadd(dmul(A, tp), B_);
+                                tt = dadd(dmul(tt, tp), C_);
+                                double cr = ddot(dnorm(tt), t0n);
+                                double mr = fmin(tp * neg + mr0, 3.14159265358979323846);
+                                if (cr >= cos(mr))
+                                    last = tp;
+                            }
+                        }
+                        double parametricT = last / pc;
+                        double lastPolar = mid - last;
+                        double th0 = acos(dclamp(t0n.x, -1, 1));
+                        th0 = t0n.y >= 0 ? th0 : -th0;
+                        double th = lastPolar * r + th0;
+                        d2 nrm = {sin(th), -cos(th)};
+                        double a = ddot(nrm, A), bo2 = ddot(nrm, B), c = ddot(nrm, C);
+                        double disc = fmax(bo2 * bo2 - a * c, 0.0);
+                        double q = sqrt(disc);
+                        if (bo2 > 0)
+                            q = -q;
+                        q -= bo2;
+                        double h = -.5 * q * a, rs, rt;
+                        if (fabs(q * q + h) < fabs(a * c + h))
+                        {
+                            rs = q;
+                            rt = a;
+                        }
+                        else
+                        {
+                            rs = c;
+                            rt = q;
+                        }
+                        polarT = rt != 0 ? rs / rt : 0;
+                        polarT = dclamp(polarT, 0, 1);
+                        if (lastPolar == 0)
+                            polarT = 0;
+                        T = fmax(parametricT, polarT);
+                    }
+                    d2 ab = dadd(dmul(dsub(q1, q0), T), q0);
+                    d2 bc = dadd(dmul(dsub(q2, q1), T), q1);
+                    d2 cd = dadd(dmul(dsub(q3, q2), T), q2);
+                    d2 abc = dadd(dmul(dsub(bc, ab), T), ab);
+                    d2 bcd = dadd(dmul(dsub(cd, bc), T), bc);
+                    out = dadd(dmul(dsub(bcd, abc), T), abc);
+                }
+                xy[texel * 2 + 0] = out.x;
+                xy[texel * 2 + 1] = out.y;
+            }
+        }
+    }
+    return 0;
+}
+
+/* ---- pass 3: draw + raster-ordered resolve -------------------------------- */
+
+/* Patch vertex/index tables for PatchType::midpointFan (gpu.cpp:446-687). */
+typedef struct
+{
+    float localVertexID, outset, fillCoverage;
+    int32_t params;
+    float mLocalVertexID, mOutset, mFillCoverage;
+} patch_vertex;
+
+static patch_vertex g_patch[PATCH_VERTEX_COUNT];
+static uint16_t g_patch_idx[PATCH_INDEX_COUNT];
+static int g_patch_ready = 0;
+
+static void pv_set(patch_vertex* v, float l, float o, float c, int32_t params)
+{
+    v->localVertexID = l;
+    v->outset = o;
+    v->fillCoverage = c;
+    v->params = params;
+    v->mLocalVertexID = l;
+    v->mOutset = o;
+    v->mFillCoverage = c;
+}
+static void pv_mirror(patch_vertex* v, float l, float o, float c)
+{
+    v->mLocalVertexID = l;
+    v->mOutset = o;
+    v->mFillCoverage = c;
+}
+
+static void build_patch_tables(void)
+{
+    if (g_patch_ready)
+        return;
+    int n = 0;
+    const int span = PATCH_SEGMENT_SPAN;
+    int32_t strokeParams = (span << 2) | STROKE_VERTEX;
+    for (int i = 0; i < span; ++i)
+    {
+        float l = (float)i, r = l + 1.f;
+        pv_set(&g_patch[n + 0], l, -1.f, 1.f, strokeParams);
+        pv_set(&g_patch[n + 1], l, +1.f, 0.f, strokeParams);
+        pv_set(&g_patch[n + 2], r, -1.f, 1.f, strokeParams);
+        pv_set(&g_patch[n + 3], r, +1.f, 0.f, strokeParams);
+        pv_mirror(&g_patch[n + 0], r - 1.f, -1.f, 1.f);
+        pv_mirror(&g_patch[n + 1], l - 1.f, -1.f, 1.f);
+        pv_mirror(&g_patch[n + 2], r - 1.f, +1.f, 0.f);
+        pv_mirror(&g_patch[n + 3], l - 1.f, +1.f, 0.f);
+        n += 4;
+    }
+    int fanIdx = n;
+    for (int i = 0; i <= span; ++i)
+    {
+        pv_set(&g_patch[n], (float)i, -1.f, 1.f, (span << 2) | FAN_VERTEX);
+        pv_mirror(&g_patch[n], (float)i - 1.f, -1.f, 1.f);
+        ++n;
+    }
+    int midIdx = n;
+    pv_set(&g_patch[n++], 0.f, 0.f, 1.f, (span << 2) | FAN_MIDPOINT_VERTEX);
+    static const uint16_t border[6] = {0, 1, 2, 2, 1, 3};
+    int k = 0, e = 0;
+    for (int s = 0; s < span; ++s)
+    {
+        for (int i = 0; i < 6; ++i)
+            g_patch_idx[k++] = (uint16_t)(e + border[i]);
+        e += 4;
+    }
+    for (int step = 1; step < span; step <<= 1)
+        for (int i = 0; i < span; i += step * 2)
+        {
+            g_patch_idx[k++] = (uint16_t)(fanIdx + i);
+            g_patch_idx[k++] = (uint16_t)(fanIdx + i + step);
+            g_patch_idx[k++] = (uint16_t)(fanIdx + i + step * 2);
+        }
+    g_patch_idx[k++] = (uint16_t)fanIdx;
+    g_patch_idx[k++] = (uint16_t)(fanIdx + span);
+    g_patch_idx[k++] = (uint16_t)midIdx;
+    (void)n;
+    g_patch_ready = 1;
+}
+
+/* float2x2 from 4 floats: columns (m0, m1) and (m2, m3). */
+static inline f2 mat_mul(const float m[4], f2 v)
+{
+    return (f2){m[0] * v.x + m[2] * v.y, m[1] * v.x + m[3] * v.y};
+}
+
+/* draw_path_common.glsl:267-274 */
+static float manhattan_pixel_width(const float M[4], f2 normalized)
+{
+    f2 v = mat_mul(M, normalized);
+    return (fabsf(v.x) + fabsf(v.y)) * (1.f / dot2(v, v));
+}
+
+typedef struct
+{
+    f2 pos;
+    float cov[2];
+    uint32_t pathID;
+    int discard;
+} vtx_out;
+
+/* unpack_tessellated_path_vertex (draw_path_common.glsl:275-789), for
+ * midpointFan patches without feathering, rasterOrdering mode. */
+static int patch_vertex_shader(const rive_cuda_flush_desc* d,
+                               const oracle_buffers* b,
+                               const uint32_t* tess,
+                               size_t tessTexels,
+                               const patch_vertex* pv,
+                               uint32_t instanceID,
+                               vtx_out* o)
+{
+    float localVertexID = pv->localVertexID;
+    float outset = pv->outset;
+    float fillCoverage = pv->fillCoverage;
+    int patchSegmentSpan = pv->params >> 2;
+    int vertexType = pv->params & 3;
+    int lv = (int)localVertexID;
+    int vertexIDOnContour = lv < patchSegmentSpan - 1 ? lv : patchSegmentSpan - 1;
+    int64_t tessVertexIdx =
+        (int64_t)instanceID * patchSegmentSpan + vertexIDOnContour;
+    if (tessVertexIdx < 0 || (size_t)tessVertexIdx >= tessTexels)
+        return -1;
+    const uint32_t* tv = tess + (size_t)tessVertexIdx * 4;
+    uint32_t contourIDWithFlags = tv[3];
+    uint32_t contourID = contourIDWithFlags & CONTOUR_ID_MASK;
+    if (contourID < 1)
+        contourID = 1;
+    const uint32_t* cd = contour_record(d, b, contourID);
+    if (!cd)
+        return -1;
+    f2 midpoint = {u2f(cd[0]), u2f(cd[1])};
+    uint32_t pathID = cd[2] & 0xffffu;
+    uint32_t vertexIndex0 = cd[3];
+    const float* path = path_record(d, b, pathID);
+    if (!path)
+        return -1;
+    float M[4] = {path[0], path[1], path[2], path[3]};
+    f2 translate = {path[4], path[5]};
+    float strokeRadius = path[6];
+    float featherRadius = path[7];
+    if (featherRadius != 0.f)
+        return -2;
+    uint32_t mirroredContourFlag =
+        contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG;
+    if (mirroredContourFlag)
+    {
+        localVertexID = pv->mLocalVertexID;
+        outset = pv->mOutset;
+        fillCoverage = pv->mFillCoverage;
+        lv = (int)localVertexID;
+    }
+    if (lv != vertexIDOnContour)
+    {
+        int64_t repl = tessVertexIdx + lv - vertexIDOnContour;
+        if (repl < 0 || (size_t)repl >= tessTexels)
+            return -1;
+        const uint32_t* rv = tess + (size_t)repl * 4;
+        if ((rv[3] & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)) !=
+            (contourIDWithFlags & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)))
+        {
+            int isClosed = strokeRadius == 0.f || midpoint.x != 0.f;
+            if (isClosed)
+            {
+                if ((size_t)vertexIndex0 >= tessTexels)
+                    return -1;
+                tessVertexIdx = vertexIndex0;
+                tv = tess + (size_t)vertexIndex0 * 4;
+            }
+        }
+        else
+        {
+            tessVertexIdx = repl;
+            tv = rv;
+        }
+        contourIDWithFlags =
+            (tv[3] & ~MIRRORED_CONTOUR_CONTOUR_FLAG) | mirroredContourFlag;
+    }
+    float theta = u2f(tv[2]);
+    f2 norm = {sinf(theta), -cosf(theta)};
+    f2 origin = {u2f(tv[0]), u2f(tv[1])};
+    f2 postTransformVertexOffset = {0.f, 0.f};
+    float cov[2] = {0.f, 0.f};
+    o->discard = 0;
+
+    if (strokeRadius != 0.f)
+    {
+        float detM = M[0] * M[3] - M[2] * M[1];
+        outset *= signf(detM);
+        if (contourIDWithFlags & LEFT_JOIN_CONTOUR_FLAG)
+            outset = minf(outset, 0.f);
+        if (contourIDWithFlags & RIGHT_JOIN_CONTOUR_FLAG)
+            outset = maxf(outset, 0.f);
+        float aaRadius = manhattan_pixel_width(M, norm) * AA_RADIUS;
+        float globalCoverage = 1.f;
+        if (aaRadius > strokeRadius)
+        {
+            globalCoverage = strokeRadius / aaRadius;
+            strokeRadius = aaRadius;
+        }
+        f2 vertexOffset = mul2(norm, strokeRadius + aaRadius);
+        float x = outset * (strokeRadius + aaRadius);
+        float k = 1.f / (aaRadius * 2.f);
+        cov[0] = k * (x + strokeRadius) + .5f;
+        cov[1] = k * (-x + strokeRadius) + .5f;
+        uint32_t joinType = contourIDWithFlags & JOIN_TYPE_MASK;
+        if (joinType > ROUND_JOIN_CONTOUR_FLAG)
+        {
+            int peekDir = 2;
+            if (!(contourIDWithFlags & JOIN_TANGENT_0_CONTOUR_FLAG))
+                peekDir = -peekDir;
+            if (contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG)
+                peekDir = -peekDir;
+            int64_t other = tessVertexIdx + peekDir;
+            if (other < 0 || (size_t)other >= tessTexels)
+                return -1;
+            float otherJoinTheta = u2f(tess[(size_t)other * 4 + 2]);
+            float joinAngle = fabsf(otherJoinTheta - theta);
+            if (joinAngle > PI_F)
+                joinAngle = TWO_PI_F - joinAngle;
+            int isTan0 = (contourIDWithFlags & JOIN_TANGENT_0_CONTOUR_FLAG) != 0;
+            int isLeftJoin = (contourIDWithFlags & LEFT_JOIN_CONTOUR_FLAG) != 0;
+            float bisectTheta =
+                joinAngle * (isTan0 == isLeftJoin ? -.5f : .5f) + theta;
+            f2 bisector = {sinf(bisectTheta), -cosf(bisectTheta)};
+            float bisectPixelWidth = manhattan_pixel_width(M, bisector);
+            float miterRatio = cosf(joinAngle * .5f);
+            float clipRadius;
+            if (joinType == MITER_CLIP_JOIN_CONTOUR_FLAG ||
+                (joinType == MITER_REVERT_JOIN_CONTOUR_FLAG && miterRatio >= .25f))
+            {
+                float miterInverseLimit =
+                    (contourIDWithFlags & EMULATED_STROKE_CAP_CONTOUR_FLAG) ? 1.f
+                                                                             : .25f;
+                clipRadius = strokeRadius * (1.f / maxf(miterRatio, miterInverseLimit));
+            }
+            else
+            {
+                clipRadius = strokeRadius * miterRatio + bisectPixelWidth * .5f;
+            }
+            float clipAARadius = clipRadius + bisectPixelWidth * AA_RADIUS;
+            if (contourIDWithFlags & JOIN_TANGENT_INNER_CONTOUR_FLAG)
+            {
+                float strokeAARaidus = strokeRadius + aaRadius;
+                float slop = aaRadius * .125f;
+                if (strokeAARaidus <= clipAARadius * miterRatio + slop)
+                {
+                    float miterAARadius = strokeAARaidus * (1.f / miterRatio);
+                    vertexOffset = mul2(bisector, miterAARadius);
+                }
+                else
+                {
+                    f2 bisectAAOffset = mul2(bisector, clipAARadius);
+                    f2 kk = {dot2(vertexOffset, vertexOffset),
+                             dot2(bisectAAOffset, bisectAAOffset)};
+                    /* MUL(k, inverse(float2x2(vertexOffset, bisectAAOffset)))
+                     * = row vector k times the inverse of the matrix whose
+                     * columns are vertexOffset and bisectAAOffset. */
+                    float a = vertexOffset.x, bb = vertexOffset.y;
+                    float c = bisectAAOffset.x, dd = bisectAAOffset.y;
+                    float det = a * dd - c * bb;
+                    float inv00 = dd / det, inv01 = -bb / det; /* column 0 */
+                    float inv10 = -c / det, inv11 = a / det;   /* column 1 */
+                    vertexOffset.x = kk.x * inv00 + kk.y * inv01;
+                    vertexOffset.y = kk.x * inv10 + kk.y * inv11;
+                }
+            }
+            f2 pt = mul2(vertexOffset, fabsf(outset));
+            float clipDistance = (clipAARadius - dot2(pt, bisector)) /
+                                 (bisectPixelWidth * (AA_RADIUS * 2.f));
+            if (contourIDWithFlags & LEFT_JOIN_CONTOUR_FLAG)
+                cov[1] = clipDistance;
+            else
+                cov[0] = clipDistance;
+        }
+        cov[0] *= globalCoverage;
+        cov[1] *= globalCoverage;
+        cov[1] = maxf(cov[1], 1e-4f);
+        postTransformVertexOffset = mat_mul(M, mul2(vertexOffset, outset));
+        if (vertexType != STROKE_VERTEX)
+            o->discard = 1;
+    }
+    else
+    {
+        cov[0] = fillCoverage;
+        cov[1] = -1.f;
+        /* sign(MUL(outset * norm, inverse(M))) * AA_RADIUS: row vector times
+         * the inverse matrix. */
+        f2 on = mul2(norm, outset);
+        float det = M[0] * M[3] - M[2] * M[1];
+        float i00 = M[3] / det, i01 = -M[1] / det; /* column 0 of inverse */
+        float i10 = -M[2] / det, i11 = M[0] / det; /* column 1 of inverse */
+        f2 r = {on.x * i00 + on.y * i01, on.x * i10 + on.y * i11};
+        postTransformVertexOffset = (f2){signf(r.x) * AA_RADIUS, signf(r.y) * AA_RADIUS};
+        if (((contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
+            ((contourIDWithFlags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
+            cov[0] = -cov[0];
+        if (vertexType == FAN_MIDPOINT_VERTEX)
+            origin = midpoint;
+        if ((contourIDWithFlags & RETROFIT_TRI_STRIP_CONTOUR_FLAG) &&
+            vertexType != FAN_VERTEX)
+            o->discard = 1;
+    }
+    if (d->wireframe)
+    {
+        cov[0] = 1.f;
+        cov[1] = -1.f;
+    }
+    f2 mo = mat_mul(M, origin);
+    o->pos = add2(add2(mo, postTransformVertexOffset), translate);
+    o->cov[0] = cov[0];
+    o->cov[1] = cov[1];
+    o->pathID = pathID;
+    return 0;
+}
+
+typedef struct
+{
+    int64_t x[3], y[3]; /* fixed point, SUBPIXEL_BITS */
+    float cov[3][2];
+    uint32_t pathID;
+    uint32_t features;
+    int32_t bx0, by0, bx1, by1; /* pixel bbox, inclusive-exclusive */
+} tri_rec;
+
+static inline int64_t snap(float v)
+{
+    return (int64_t)llrint((double)v * SUBPIXEL_ONE);
+}
+
+/* PLS state of one pixel (draw_raster_order_path.frag:7-12). */
+typedef struct
+{
+    uint8_t color[4];
+    uint32_t clip;
+    uint8_t scratch[4];
+    uint32_t coverage;
+} pls_pixel;
+
+static inline uint16_t id_bits_to_f16(uint32_t idBits, uint32_t granularity)
+{
+    return idBits == 0 ? 0 : (uint16_t)((idBits + MAX_DENORM_F16) * granularity);
+}
+static inline float h2f(uint16_t h) { return oracle_f16_to_f32(h); }
+
+/* advanced_blend.glsl:94-154 */
+static float lum_from_rgb(const float c[3])
+{
+    return c[0] * .30f + c[1] * .59f + c[2] * .11f;
+}
+static float min3(const float c[3]) { return minf(minf(c[0], c[1]), c[2]); }
+static float max3(const float c[3]) { return maxf(maxf(c[0], c[1]), c[2]); }
+static void set_lum(const float base[3], const float lumColor[3], float out[3])
+{
+    float lumTarget = lum_from_rgb(lumColor);
+    float lb = lum_from_rgb(base);
+    float biased[3] = {base[0] - lb, base[1] - lb, base[2] - lb};
+    float sx = lumTarget / maxf(EPSILON_FP16_NON_DENORM, -min3(biased));
+    float sy = (1.f - lumTarget) / maxf(EPSILON_FP16_NON_DENORM, max3(biased));
+    float satScale = minf(1.f, minf(sx, sy));
+    for (int i = 0; i < 3; ++i)
+        out[i] = biased[i] * satScale + lumTarget;
+}
+static void set_lum_sat(const float hue[3],
+                        const float sat[3],
+                        const float lum[3],
+                        float out[3])
+{
+    float satTarget = max3(sat) - min3(sat);
+    float mn = min3(hue);
+    float h[3] = {hue[0] - mn, hue[1] - mn, hue[2] - mn};
+    float satSource = max3(h);
+    float scale = satTarget / maxf(EPSILON_FP16_NON_DENORM, satSource);
+    float hs[3] = {h[0] * scale, h[1] * scale, h[2] * scale};
+    set_lum(hs, lum, out);
+}
+
+/* advanced_blend.glsl:156-327 */
+void oracle_advanced_blend(const float srcIn[3],
+                           const float dstPremulIn[4],
+                           int mode,
+                           float out[3])
+{
+    float src[3] = {srcIn[0], srcIn[1], srcIn[2]};
+    float dp[4] = {dstPremulIn[0], dstPremulIn[1], dstPremulIn[2], dstPremulIn[3]};
+    float inv = dp[3] != 0.f ? 1.f / dp[3] : 0.f;
+    float dst[3] = {dp[0] * inv, dp[1] * inv, dp[2] * inv};
+    float co[3] = {0, 0, 0};
+    switch (mode)
+    {
+        case BLEND_MODE_MULTIPLY:
+            for (int i = 0; i < 3; ++i)
+                co[i] = src[i] * dst[i];
+            break;
+        case BLEND_MODE_SCREEN:
+            for (int i = 0; i < 3; ++i)
+                co[i] = src[i] + dst[i] - src[i] * dst[i];
+            break;
+        case BLEND_MODE_OVERLAY:
+            for (int i = 0; i < 3; ++i)
+            {
+                float sd = src[i] * dst[i];
+                co[i] = 2.f * (dst[i] > .5f ? src[i] + dst[i] - sd - .5f : sd);
+            }
+            break;
+        case BLEND_MODE_DARKEN:
+            for (int i = 0; i < 3; ++i)
+                co[i] = minf(src[i], dst[i]);
+            break;
+        case BLEND_MODE_LIGHTEN:
+            for (int i = 0; i < 3; ++i)
+                co[i] = maxf(src[i], dst[i]);
+            break;
+        case BLEND_MODE_COLORDODGE:
+            for (int i = 0; i < 3; ++i)
+            {
+                float dpc = clampf(dp[i], 0.f, dp[3]);
+                float denom = clampf(1.f - src[i], 0.f, 1.f) * dp[3];
+                co[i] = denom == 0.f ? signf(dpc) : minf(1.f, dpc / denom);
+            }
+            break;
+        case BLEND_MODE_COLORBURN:
+        {
+            float a = dp[3] == 0.f ? 1.f : dp[3];
+            for (int i = 0; i < 3; ++i)
+            {
+                float s = clampf(src[i], 0.f, 1.f);
+                float dpc = clampf(dp[i], 0.f, dp[3]);
+                float numer = a - dpc;
+                co[i] = 1.f - (s == 0.f ? signf(numer) : minf(1.f, numer / (s * a)));
+            }
+            break;
+        }
+        case BLEND_MODE_HARDLIGHT:
+            for (int i = 0; i < 3; ++i)
+            {
+                float sd = src[i] * dst[i];
+                co[i] = 2.f * (src[i] > .5f ? src[i] + dst[i] - sd - .5f : sd);
+            }
+            break;
+        case BLEND_MODE_SOFTLIGHT:
+            for (int i = 0; i < 3; ++i)
+            {
+                float c;
+                if (src[i] <= .5f)
+                    c = 1.f - dst[i];
+                else if (dst[i] <= .25f)
+                    c = (16.f * dst[i] - 12.f) * dst[i] + 3.f;
+                else
+                    c = 1.f / sqrtf(dst[i]) - 1.f;
+                co[i] = dst[i] + dst[i] * (2.f * src[i] - 1.f) * c;
+            }
+            break;
+        case BLEND_MODE_DIFFERENCE:
+            for (int i = 0; i < 3; ++i)
+                co[i] = fabsf(dst[i] - src[i]);
+            break;
+        case BLEND_MODE_EXCLUSION:
+            for (int i = 0; i < 3; ++i)
+                co[i] = src[i] + dst[i] - 2.f * src[i] * dst[i];
+            break;
+        case BLEND_MODE_HUE:
+        case BLEND_MODE_SATURATION:
+        case BLEND_MODE_COLOR:
+        case BLEND_MODE_LUMINOSITY:
+        {
+            float s[3];
+            for (int i = 0; i < 3; ++i)
+                s[i] = clampf(src[i], 0.f, 1.f);
+            if (mode == BLEND_MODE_HUE)
+                set_lum_sat(s, dst, dst, co);
+            else if (mode == BLEND_MODE_SATURATION)
+                set_lum_sat(dst, s, dst, co);
+            else if (mode == BLEND_MODE_COLOR)
+                set_lum(s, dst, co);
+            else
+                set_lum(dst, s, co);
+            break;
+        }
+        default:
+            break;
+    }
+    /* mix(src, coeffs, dstPremul.a) = src * (1 - a) + coeffs * a, with the
+     * caller's (unclamped) src: advanced_blend_coeffs takes src by value. */
+    float a = dstPremulIn[3];
+    for (int i = 0; i < 3; ++i)
+        out[i] = srcIn[i] * (1.f - a) + co[i] * a;
+}
+
+/* Bilinear sample of the RGBA8 gradient texture with clamp-to-edge. */
+static void sample_grad(const uint8_t* grad,
+                        uint32_t H,
+                        float u,
+                        float v,
+                        float out[4])
+{
+    float fx = u * GRAD_TEXTURE_WIDTH - .5f;
+    float fy = v * (float)H - .5f;
+    float x0f = floorf(fx), y0f = floorf(fy);
+    float ax = fx - x0f, ay = fy - y0f;
+    int x0 = (int)x0f, y0 = (int)y0f;
+    for (int k = 0; k < 4; ++k)
+        out[k] = 0.f;
+    for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i)
+        {
+            int xi = x0 + i, yj = y0 + j;
+            xi = xi < 0 ? 0 : (xi >= GRAD_TEXTURE_WIDTH ? GRAD_TEXTURE_WIDTH - 1 : xi);
+            yj = yj < 0 ? 0 : (yj >= (int)H ? (int)H - 1 : yj);
+            float w = (i ? ax : 1.f - ax) * (j ? ay : 1.f - ay);
+            const uint8_t* t = grad + ((size_t)yj * GRAD_TEXTURE_WIDTH + xi) * 4;
+            for (int k = 0; k < 4; ++k)
+                out[k] += w * ((float)t[k] / 255.f);
+        }
+}
+
+/* common.glsl:269-274 */
+static float ign(float fx, float fy, float scale, float bias)
+{
+    float v1 = fractf(0.06711056f * fx + 0.00583715f * fy);
+    float v2 = fractf(52.9829189f * v1);
+    return v2 * scale + bias;
+}
+
+typedef struct
+{
+    const rive_cuda_flush_desc* d;
+    const oracle_buffers* b;
+    const uint8_t* grad;
+    uint32_t granularity;
+    float ditherScale, ditherBias;
+} frag_ctx;
+
+/* One fragment of draw_raster_order_path.frag:14-238. */
+static void fragment(const frag_ctx* fc,
+                     const tri_rec* t,
+                     float covx,
+                     float covy,
+                     int px,
+                     int py,
+                     pls_pixel* pls)
+{
+    const uint32_t features = t->features;
+    const uint32_t pathID = t->pathID;
+    const uint32_t* paint =
+        (const uint32_t*)fc->b->paints + 2 * ((size_t)fc->d->first_paint + pathID);
+    const float* aux =
+        (const float*)fc->b->paint_aux + 32 * ((size_t)fc->d->first_paint_aux + pathID);
+    uint16_t vPathID = id_bits_to_f16(pathID, fc->granularity);
+    int evenOdd = (paint[0] & PAINT_FLAG_EVEN_ODD_FILL) != 0;
+    if (evenOdd)
+        vPathID ^= 0x8000u;
+    uint32_t paintType = paint[0] & 0xfu;
+    float fragX = (float)px + .5f, fragY = (float)py + .5f;
+
+    /* Coverage. */
+    uint16_t covBufferID = (uint16_t)(pls->coverage >> 16);
+    float coverageCount =
+        covBufferID == vPathID ? h2f((uint16_t)(pls->coverage & 0xffffu)) : 0.f;
+    if (covy >= 0.f) /* stroke */
+        coverageCount = maxf(minf(covx, covy), coverageCount);
+    else
+        coverageCount = coverageCount + covx;
+    uint16_t storedCount = oracle_f32_to_f16(coverageCount);
+    pls->coverage = ((uint32_t)vPathID << 16) | storedCount;
+    coverageCount = h2f(storedCount);
+
+    float coverage = fabsf(coverageCount);
+    if ((features & SF_EVEN_ODD) && evenOdd)
+        coverage = 1.f - fabsf(fractf(coverage * .5f) * 2.f + -1.f);
+    coverage = minf(coverage, 1.f);
+
+    /* Clip IDs (draw_path.vert:203-220). */
+    float clipIDx = 0.f, clipIDy = 0.f;
+    uint16_t clipIDxBits = 0;
+    if (features & SF_CLIPPING)
+    {
+        uint32_t clipIDBits =
+            (paintType == CLIP_UPDATE_PAINT_TYPE ? paint[1] : paint[0]) >> 16;
+        clipIDxBits = id_bits_to_f16(clipIDBits, fc->granularity);
+        clipIDx = h2f(clipIDxBits);
+        if (paintType == CLIP_UPDATE_PAINT_TYPE)
+        {
+            clipIDx = -clipIDx;
+            clipIDy = h2f(id_bits_to_f16(paint[0] >> 16, fc->granularity));
+        }
+    }
+
+    if ((features & SF_CLIPPING) && clipIDx < 0.f)
+    {
+        uint16_t clipIDBitsPos = clipIDxBits; /* == -clipIDx */
+        if ((features & SF_NESTED_CLIPPING) && clipIDy != 0.f)
+        {
+            uint16_t outerBits = id_bits_to_f16(paint[0] >> 16, fc->granularity);
+            uint16_t clipContentID = (uint16_t)(pls->clip >> 16);
+            float outerClipCoverage;
+            if (clipContentID != clipIDBitsPos)
+            {
+                outerClipCoverage = clipContentID == outerBits
+                                        ? h2f((uint16_t)(pls->clip & 0xffffu))
+                                        : 0.f;
+                pls->scratch[0] = unorm8(outerClipCoverage);
+                pls->scratch[1] = pls->scratch[2] = pls->scratch[3] = 0;
+            }
+            else
+            {
+                outerClipCoverage = (float)pls->scratch[0] / 255.f;
+            }
+            coverage = minf(coverage, outerClipCoverage);
+        }
+        pls->clip = ((uint32_t)clipIDBitsPos << 16) | oracle_f32_to_f16(coverage);
+        return;
+    }
+
+    if (features & SF_CLIPPING)
+    {
+        if (clipIDx != 0.f)
+        {
+            uint16_t clipContentID = (uint16_t)(pls->clip >> 16);
+            coverage = clipContentID == clipIDxBits
+                           ? minf(h2f((uint16_t)(pls->clip & 0xffffu)), coverage)
+                           : 0.f;
+        }
+    }
+    if ((features & SF_CLIP_RECT))
+    {
+        /* find_clip_rect_coverage_distances (common.glsl:376-400) at the
+         * pixel centre. */
+        float cm[4] = {aux[8], aux[9], aux[10], aux[11]};
+        f2 ct = {aux[12], aux[13]};
+        f2 aaw = {fabsf(cm[0]) + fabsf(cm[2]), fabsf(cm[1]) + fabsf(cm[3])};
+        float cr[4];
+        if (aaw.x != 0.f && aaw.y != 0.f)
+        {
+            f2 r = {1.f / aaw.x, 1.f / aaw.y};
+            f2 cc = add2(mat_mul(cm, (f2){fragX, fragY}), ct);
+            cr[0] = cc.x * r.x + r.x + .5f;
+            cr[1] = cc.y * r.y + r.y + .5f;
+            cr[2] = -cc.x * r.x + r.x + .5f;
+            cr[3] = -cc.y * r.y + r.y + .5f;
+        }
+        else
+        {
+            cr[0] = cr[2] = ct.x;
+            cr[1] = cr[3] = ct.y;
+        }
+        float m = minf(minf(cr[0], cr[1]), minf(cr[2], cr[3]));
+        coverage = clampf(m, 0.f, coverage);
+    }
+
+    int unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
+    float color[4];
+    if (paintType == SOLID_COLOR_PAINT_TYPE)
+    {
+        uint32_t c = paint[1];
+        color[0] = (float)(c & 0xffu) / 255.f;
+        color[1] = (float)((c >> 8) & 0xffu) / 255.f;
+        color[2] = (float)((c >> 16) & 0xffu) / 255.f;
+        color[3] = (float)(c >> 24) / 255.f;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+            for (int k = 0; k < 4; ++k)
+                color[k] *= coverage;
+        }
+        else
+            color[3] *= coverage;
+    }
+    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE ||
+             paintType == RADIAL_GRADIENT_PAINT_TYPE)
+    {
+        float pm[4] = {aux[0], aux[1], aux[2], aux[3]};
+        f2 pc = add2(mat_mul(pm, (f2){fragX, fragY}), (f2){aux[4], aux[5]});
+        float gradientSpan = aux[6];
+        float spanB = gradientSpan > .9f ? 2.f : aux[7];
+        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pc.x
+                                                          : sqrtf(dot2(pc, pc));
+        t = clampf(t, 0.f, 1.f);
+        float x = spanB > 1.f
+                      ? (1.f - 1.f / GRAD_TEXTURE_WIDTH) * t + (.5f / GRAD_TEXTURE_WIDTH)
+                      : (1.f / GRAD_TEXTURE_WIDTH) * t + spanB;
+        float row = u2f(paint[1]);
+        sample_grad(fc->grad, fc->d->grad_data_height, x, row, color);
+        color[3] *= coverage;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+        }
+    }
+    else
+    {
+        /* Clip-update paint outside ENABLE_CLIPPING draws nothing sensible;
+         * the reference leaves v_paint zero. */
+        color[0] = color[1] = color[2] = color[3] = 0.f;
+    }
+
+    float dst[4];
+    if (covBufferID != vPathID)
+    {
+        for (int k = 0; k < 4; ++k)
+            dst[k] = (float)pls->color[k] / 255.f;
+        memcpy(pls->scratch, pls->color, 4);
+    }
+    else
+    {
+        for (int k = 0; k < 4; ++k)
+            dst[k] = (float)pls->scratch[k] / 255.f;
+    }
+
+    if (unmultiplied)
+    {
+        uint32_t blendMode = (paint[0] >> 4) & 0xfu;
+        if (blendMode != BLEND_SRC_OVER)
+        {
+            int mode = (int)blendMode;
+            if (mode >= BLEND_MODE_HUE && !(features & SF_HSL_BLEND_MODES))
+            {
+                /* Without the HSL feature the coeffs are left undefined in the
+                 * reference; treat as srcOver. */
+            }
+            else
+            {
+                float rgb[3];
+                oracle_advanced_blend(color, dst, mode, rgb);
+                color[0] = rgb[0];
+                color[1] = rgb[1];
+                color[2] = rgb[2];
+            }
+        }
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    float paintAlpha = color[3];
+    for (int k = 0; k < 4; ++k)
+        color[k] += dst[k] * (1.f - paintAlpha);
+    if ((features & SF_DITHER) && paintAlpha != 0.f)
+    {
+        float n = ign(fragX, fragY, fc->ditherScale, fc->ditherBias);
+        color[0] += n;
+        color[1] += n;
+        color[2] += n;
+    }
+    for (int k = 0; k < 4; ++k)
+        pls->color[k] = unorm8(color[k]);
+}
+
+static int setup_triangle(const vtx_out* a,
+                          const vtx_out* bb,
+                          const vtx_out* c,
+                          uint32_t features,
+                          int W,
+                          int H,
+                          tri_rec* t)
+{
+    if (a->discard || bb->discard || c->discard)
+        return 0;
+    const vtx_out* v[3] = {a, bb, c};
+    for (int i = 0; i < 3; ++i)
+    {
+        if (!isfinite(v[i]->pos.x) || !isfinite(v[i]->pos.y))
+            return 0;
+        if (fabsf(v[i]->pos.x) > 4.0e6f || fabsf(v[i]->pos.y) > 4.0e6f)
+            return -3; /* outside the fixed-point range of this rasteriser */
+        t->x[i] = snap(v[i]->pos.x);
+        t->y[i] = snap(v[i]->pos.y);
+        t->cov[i][0] = v[i]->cov[0];
+        t->cov[i][1] = v[i]->cov[1];
+    }
+    int64_t area2 = (t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
+                    (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]);
+    if (area2 <= 0) /* counterclockwise faces are culled; degenerate drop */
+        return 0;
+    int64_t minx = t->x[0], maxx = t->x[0], miny = t->y[0], maxy = t->y[0];
+    for (int i = 1; i < 3; ++i)
+    {
+        if (t->x[i] < minx) minx = t->x[i];
+        if (t->x[i] > maxx) maxx = t->x[i];
+        if (t->y[i] < miny) miny = t->y[i];
+        if (t->y[i] > maxy) maxy = t->y[i];
+    }
+    /* Pixels whose centres (k + 1/2) lie in [min, max]. */
+    int64_t bx0 = (minx - SUBPIXEL_ONE / 2 + SUBPIXEL_ONE - 1) >> SUBPIXEL_BITS;
+    int64_t bx1 = ((maxx - SUBPIXEL_ONE / 2) >> SUBPIXEL_BITS) + 1;
+    int64_t by0 = (miny - SUBPIXEL_ONE / 2 + SUBPIXEL_ONE - 1) >> SUBPIXEL_BITS;
+    int64_t by1 = ((maxy - SUBPIXEL_ONE / 2) >> SUBPIXEL_BITS) + 1;
+    if (bx0 < 0) bx0 = 0;
+    if (by0 < 0) by0 = 0;
+    if (bx1 > W) bx1 = W;
+    if (by1 > H) by1 = H;
+    if (bx0 >= bx1 || by0 >= by1)
+        return 0;
+    t->bx0 = (int32_t)bx0;
+    t->bx1 = (int32_t)bx1;
+    t->by0 = (int32_t)by0;
+    t->by1 = (int32_t)by1;
+    t->pathID = v[0]->pathID;
+    t->features = features;
+    return 1;
+}
+
+/* Edge function of edge a->b at point p, with the top-left tie rule for
+ * clockwise (screen-space, y down) triangles. Returns > 0 when p is inside. */
+static inline int edge_inside(int64_t ax, int64_t ay, int64_t bx, int64_t by,
+                              int64_t px, int64_t py, int64_t* e)
+{
+    int64_t dx = bx - ax, dy = by - ay;
+    int64_t v = dx * (py - ay) - dy * (px - ax);
+    *e = v;
+    if (v > 0)
+        return 1;
+    if (v < 0)
+        return 0;
+    return (dy == 0 && dx > 0) || dy < 0;
+}
+
+static void raster_triangle_rows(const frag_ctx* fc,
+                                 const tri_rec* t,
+                                 int row0,
+                                 int row1,
+                                 pls_pixel* pls,
+                                 int W,
+                                 uint64_t* frags)
+{
+    int y0 = t->by0 > row0 ? t->by0 : row0;
+    int y1 = t->by1 < row1 ? t->by1 : row1;
+    if (y0 >= y1)
+        return;
+    double area2 = (double)((t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
+                            (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]));
+    for (int py = y0; py < y1; ++py)
+    {
+        int64_t cy = ((int64_t)py << SUBPIXEL_BITS) + SUBPIXEL_ONE / 2;
+        for (int px = t->bx0; px < t->bx1; ++px)
+        {
+            int64_t cx = ((int64_t)px << SUBPIXEL_BITS) + SUBPIXEL_ONE / 2;
+            int64_t e0, e1, e2;
+            /* e0: edge v1->v2 (weight of v0), e1: v2->v0, e2: v0->v1 */
+            if (!edge_inside(t->x[1], t->y[1], t->x[2], t->y[2], cx, cy, &e0))
+                continue;
+            if (!edge_inside(t->x[2], t->y[2], t->x[0], t->y[0], cx, cy, &e1))
+                continue;
+            if (!edge_inside(t->x[0], t->y[0], t->x[1], t->y[1], cx, cy, &e2))
+                continue;
+            float l0 = (float)((double)e0 / area2);
+            float l1 = (float)((double)e1 / area2);
+            float l2 = (float)((double)e2 / area2);
+            float covx = l0 * t->cov[0][0] + l1 * t->cov[1][0] + l2 * t->cov[2][0];
+            float covy = l0 * t->cov[0][1] + l1 * t->cov[1][1] + l2 * t->cov[2][1];
+            fragment(fc, t, covx, covy, px, py, pls + (size_t)py * W + px);
+            ++*frags;
+        }
+    }
+}
+
+int oracle_draw(const rive_cuda_flush_desc* d,
+                const oracle_buffers* b,
+                const uint32_t* tess,
+                const uint8_t* grad,
+                uint8_t* fb,
+                int threads)
+{
+    build_patch_tables();
+    const int W = (int)d->render_target_width, H = (int)d->render_target_height;
+    const size_t tessTexels = (size_t)TESS_TEXTURE_WIDTH * d->tess_data_height;
+    if (d->interlock_mode != 0)
+        return -2;
+    if (b->flush_uniforms_bytes < d->flush_uniform_offset_bytes + 256u)
+        return -1;
+    const uint8_t* uni = (const uint8_t*)b->flush_uniforms + d->flush_uniform_offset_bytes;
+    /* FlushUniforms (gpu.hpp:1466-1537): pathIDGranularity at byte 72,
+     * ditherScale at 88, ditherBias at 92. */
+    uint32_t granularity;
+    float ditherScale, ditherBias;
+    memcpy(&granularity, uni + 72, 4);
+    memcpy(&ditherScale, uni + 88, 4);
+    memcpy(&ditherBias, uni + 92, 4);
+
+    /* Vertex processing + primitive assembly, in primitive order. */
+    size_t cap = 1024, n = 0;
+    tri_rec* tris = (tri_rec*)malloc(cap * sizeof(tri_rec));
+    if (!tris)
+        return -4;
+    for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
+    {
+        const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
+        if (batch->draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
+        {
+            free(tris);
+            return -2;
+        }
+        if (batch->shader_features & SF_FEATHER)
+        {
+            free(tris);
+            return -2;
+        }
+        for (uint32_t inst = batch->base_element;
+             inst < batch->base_element + batch->element_count;
+             ++inst)
+        {
+            vtx_out vo[PATCH_VERTEX_COUNT];
+            for (int k = 0; k < PATCH_VERTEX_COUNT; ++k)
+            {
+                int rc = patch_vertex_shader(d, b, tess, tessTexels, &g_patch[k], inst, &vo[k]);
+                if (rc != 0)
+                {
+                    free(tris);
+                    return rc;
+                }
+            }
+            for (int k = 0; k < PATCH_INDEX_COUNT; k += 3)
+            {
+                if (n == cap)
+                {
+                    cap *= 2;
+                    tri_rec* nt = (tri_rec*)realloc(tris, cap * sizeof(tri_rec));
+                    if (!nt)
+                    {
+                        free(tris);
+                        return -4;
+                    }
+                    tris = nt;
+                }
+                int rc = setup_triangle(&vo[g_patch_idx[k]], &vo[g_patch_idx[k + 1]],
+                                        &vo[g_patch_idx[k + 2]], batch->shader_features,
+                                        W, H, &tris[n]);
+                if (rc < 0)
+                {
+                    free(tris);
+                    return rc;
+                }
+                n += (size_t)rc;
+            }
+        }
+    }
+
+    /* PLS planes at the start of the render pass. */
+    pls_pixel* pls = (pls_pixel*)malloc((size_t)W * H * sizeof(pls_pixel));
+    if (!pls)
+    {
+        free(tris);
+        return -4;
+    }
+    uint8_t clear[4];
+    {
+        float c[4];
+        unpack_color_int(d->color_clear_value, c);
+        clear[0] = unorm8(c[0] * c[3]);
+        clear[1] = unorm8(c[1] * c[3]);
+        clear[2] = unorm8(c[2] * c[3]);
+        clear[3] = unorm8(c[3]);
+    }
+    for (size_t i = 0; i < (size_t)W * H; ++i)
+    {
+        if (d->color_load_action == RIVE_CUDA_LOAD_CLEAR)
+            memcpy(pls[i].color, clear, 4);
+        else
+            memcpy(pls[i].color, fb + i * 4, 4);
+        pls[i].clip = 0;
+        pls[i].coverage = 0;
+        memset(pls[i].scratch, 0, 4);
+    }
+
+    frag_ctx fc = {d, b, grad, granularity, ditherScale, ditherBias};
+    const int band = 8;
+    const int nbands = (H + band - 1) / band;
+    uint64_t frags = 0;
+#ifdef _OPENMP
+    if (threads > 0)
+        omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : frags)
+#endif
+    for (int bnd = 0; bnd < nbands; ++bnd)
+    {
+        int r0 = bnd * band, r1 = r0 + band < H ? r0 + band : H;
+        uint64_t local = 0;
+        for (size_t i = 0; i < n; ++i)
+            raster_triangle_rows(&fc, &tris[i], r0, r1, pls, W, &local);
+        frags += local;
+    }
+    for (size_t i = 0; i < (size_t)W * H; ++i)
+        memcpy(fb + i * 4, pls[i].color, 4);
+    g_stat_triangles = n;
+    g_stat_fragments = frags;
+    free(pls);
+    free(tris);
+    return 0;
+}
+
+void oracle_last_stats(uint64_t* triangles, uint64_t* fragments)
+{
+    if (triangles)
+        *triangles = g_stat_triangles;
+    if (fragments)
+        *fragments = g_stat_fragments;
+}
+
+int oracle_flush(const rive_cuda_flush_desc* d,
+                 const oracle_buffers* b,
+                 uint8_t* fb,
+                 int threads)
+{
+    size_t gradBytes = (size_t)GRAD_TEXTURE_WIDTH * (d->grad_data_height ? d->grad_data_height : 1) * 4;
+    size_t tessBytes = (size_t)TESS_TEXTURE_WIDTH * (d->tess_data_height ? d->tess_data_height : 1) * 16;
+    uint8_t* grad = (uint8_t*)calloc(1, gradBytes);
+    uint32_t* tess = (uint32_t*)calloc(1, tessBytes);
+    int rc = -4;
+    if (grad && tess)
+    {
+        rc = oracle_color_ramps(d, b, grad);
+        if (rc == 0)
+            rc = oracle_tessellate(d, b, tess);
+        if (rc == 0)
+            rc = oracle_draw(d, b, tess, grad, fb, threads);
+    }
+    free(grad);
+    free(tess);
+    return rc;
+}

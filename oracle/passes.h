@@ -1,0 +1,107 @@
+/*
+ * passes.h -- TEST INFRASTRUCTURE. CPU restatement of rive-runtime's GPU
+ * passes for InterlockMode::rasterOrdering, used only as the parity checker
+ * (tests, smoke check, and the timed CPU baseline of the benchmark). Never
+ * linked into the product library.
+ *
+ *   pass 1  color ramps     renderer/src/shaders/color_ramp.glsl:40-107
+ *   pass 2  tessellation    renderer/src/shaders/tessellate.glsl:61-567
+ *   pass 3  draw + resolve  renderer/src/shaders/draw_path.vert:96-549,
+ *                           draw_path_common.glsl:275-789,
+ *                           draw_raster_order_path.frag:14-238,
+ *                           advanced_blend.glsl:94-327, common.glsl:185-336
+ *
+ * Rasterisation follows the Vulkan rules the reference backend runs under
+ * (render_context_vulkan_impl.cpp, draw_pipeline_vulkan.cpp:333-334):
+ * pixel-centre sampling, 8 sub-pixel bits, top-left fill rule, clockwise front
+ * faces with counterclockwise faces culled (gpu.cpp:1552-1567), no-perspective
+ * barycentric interpolation.
+ *
+ * Parity pin: the inputs (records) are pinned by the reference's own front
+ * end; the pixel arithmetic is pinned only by this restatement (no graphics
+ * API exists to run the reference shaders), with the reference's own shader
+ * known-answer tests re-run against it.
+ */
+#ifndef RIVE_ORACLE_PASSES_H
+#define RIVE_ORACLE_PASSES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "rive_cuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The frame's record buffers, each at element 0 (desc->first_* index in). */
+typedef struct oracle_buffers
+{
+    const void* flush_uniforms;
+    size_t flush_uniforms_bytes;
+    const void* paths;
+    size_t paths_bytes;
+    const void* paints;
+    size_t paints_bytes;
+    const void* paint_aux;
+    size_t paint_aux_bytes;
+    const void* contours;
+    size_t contours_bytes;
+    const void* grad_spans;
+    size_t grad_spans_bytes;
+    const void* tess_spans;
+    size_t tess_spans_bytes;
+} oracle_buffers;
+
+/* Pass 1 into grad (512 x grad_data_height RGBA8). Returns 0 on success. */
+int oracle_color_ramps(const rive_cuda_flush_desc* d,
+                       const oracle_buffers* b,
+                       uint8_t* grad);
+
+/* Pass 2 into tess (2048 x tess_data_height uint4). fp32 arithmetic. */
+int oracle_tessellate(const rive_cuda_flush_desc* d,
+                      const oracle_buffers* b,
+                      uint32_t* tess);
+
+/* Pass 2 evaluated in double precision (same algorithm): the FP64 twin the
+ * tessellated-vertex tolerance is measured against. Flags and theta words
+ * are produced the same way; x,y are written as floats rounded from double. */
+int oracle_tessellate_f64(const rive_cuda_flush_desc* d,
+                          const oracle_buffers* b,
+                          double* xy /* 2 per texel */,
+                          uint32_t* tess_flags /* 1 per texel */);
+
+/* Pass 3 into fb (width x height RGBA8, row 0 at top), reading the textures
+ * of passes 1 and 2. threads <= 0 uses all cores. */
+int oracle_draw(const rive_cuda_flush_desc* d,
+                const oracle_buffers* b,
+                const uint32_t* tess,
+                const uint8_t* grad,
+                uint8_t* fb,
+                int threads);
+
+/* All three passes of one logical flush. */
+int oracle_flush(const rive_cuda_flush_desc* d,
+                 const oracle_buffers* b,
+                 uint8_t* fb,
+                 int threads);
+
+/* Counters of the last oracle_draw (triangles after culling, fragments). */
+void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
+
+/* Half-float helpers exposed for known-answer tests. */
+uint16_t oracle_f32_to_f16(float f);
+float oracle_f16_to_f32(uint16_t h);
+
+/* Advanced blend of one unmultiplied src over a premultiplied dst
+ * (advanced_blend.glsl:156-327), exposed for known-answer tests. */
+void oracle_advanced_blend(const float src[3],
+                           const float dst_premul[4],
+                           int mode,
+                           float out_rgb[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

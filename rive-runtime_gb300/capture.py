@@ -1,0 +1,99 @@
+"""Reader/writer for flush captures: the frame's record buffers plus the list
+of logical flushes (rive_cuda_flush_desc + rive_cuda_draw_batch[]).
+
+A capture is exactly what rive::gpu::RenderContext hands its RenderContextImpl
+for one frame (render_context.cpp:970-1010): the bytes written into the mapped
+path/paint/paintAux/contour/gradSpan/tessVertexSpan/flushUniform buffers, and
+one gpu::FlushDescriptor per logical flush.
+"""
+from __future__ import annotations
+
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+CAPTURE_MAGIC = 0x31504352  # "RCP1"
+
+BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
+                "grad_spans", "tess_spans")
+
+# rive_cuda_flush_desc field order (include/rive_cuda.h); 36 u32-sized fields,
+# then the draw_batches pointer (8 bytes, LP64).
+DESC_FIELDS = (
+    "render_target_width", "render_target_height", "interlock_mode",
+    "color_load_action", "color_clear_value", "ub0", "ub1", "ub2", "ub3",
+    "combined_shader_features", "dither_mode", "flush_uniform_offset_bytes",
+    "path_count", "first_path", "first_paint", "first_paint_aux",
+    "contour_count", "first_contour", "grad_span_count", "first_grad_span",
+    "tess_span_count", "first_tess_span", "grad_data_height",
+    "tess_data_height", "wireframe", "clockwise_fill_override",
+    "has_triangle_vertices", "draw_batch_count",
+)
+DESC_STRUCT = struct.Struct("<5I4i19I")
+DESC_SIZE = 120  # 28 fields * 4 = 112, + 8-byte draw_batches pointer (LP64)
+BATCH_FIELDS = ("draw_type", "element_count", "base_element", "shader_features",
+                "draw_contents", "shader_misc_flags", "first_blend_mode",
+                "barriers")
+BATCH_SIZE = 32
+
+
+@dataclass
+class Flush:
+    desc: dict
+    batches: np.ndarray  # (n, 8) uint32
+
+
+@dataclass
+class Capture:
+    width: int
+    height: int
+    buffers: dict = field(default_factory=dict)  # name -> bytes
+    flushes: list = field(default_factory=list)
+
+    def buffer_array(self, name, dtype=np.uint32):
+        return np.frombuffer(self.buffers[name], dtype=dtype)
+
+    @property
+    def tess_span_count(self):
+        return len(self.buffers["tess_spans"]) // 64
+
+
+def parse(data: bytes) -> Capture:
+    magic, w, h, nk = struct.unpack_from("<4I", data, 0)
+    if magic != CAPTURE_MAGIC:
+        raise ValueError("not a flush capture")
+    off = 16
+    cap = Capture(w, h)
+    for k in range(nk):
+        (n,) = struct.unpack_from("<Q", data, off)
+        off += 8
+        cap.buffers[BUFFER_NAMES[k]] = bytes(data[off:off + n])
+        off += n + ((8 - (n & 7)) & 7)
+    (nf,) = struct.unpack_from("<I", data, off)
+    off += 4
+    for _ in range(nf):
+        vals = DESC_STRUCT.unpack_from(data, off)
+        desc = dict(zip(DESC_FIELDS, vals))
+        off += DESC_SIZE
+        nb = desc["draw_batch_count"]
+        batches = np.frombuffer(data, dtype="<u4", count=nb * 8, offset=off).reshape(nb, 8).copy()
+        off += nb * BATCH_SIZE
+        cap.flushes.append(Flush(desc, batches))
+    return cap
+
+
+def serialize(cap: Capture) -> bytes:
+    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC, cap.width, cap.height,
+                                len(BUFFER_NAMES)))
+    for name in BUFFER_NAMES:
+        b = cap.buffers.get(name, b"")
+        out += struct.pack("<Q", len(b)) + b + bytes((8 - (len(b) & 7)) & 7)
+    out += struct.pack("<I", len(cap.flushes))
+    for f in cap.flushes:
+        d = dict(f.desc)
+        d["draw_batch_count"] = len(f.batches)
+        out += DESC_STRUCT.pack(*[d[k] for k in DESC_FIELDS])
+        out += bytes(DESC_SIZE - DESC_STRUCT.size)
+        out += np.asarray(f.batches, dtype="<u4").tobytes()
+    return bytes(out)

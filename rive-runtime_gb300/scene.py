@@ -1,0 +1,296 @@
+"""Seeded synthetic scenes, written in the rive_scene.h recording format.
+
+A scene is the list of rive::Renderer / rive::Factory calls that make one frame
+(include/rive/renderer.hpp:212-236, include/rive/factory.hpp:35-87): paths
+(RawPath + FillRule), paints (RiveRenderPaint, renderer/src/rive_render_paint.hpp)
+and save/restore/transform/clipPath/drawPath commands.
+
+The workloads:
+
+* ``plain_small``: a 512x512 canvas cleared to opaque white; 200 closed filled
+  paths, each one contour of 8 cubics with every control point uniform in
+  [0,512)^2; nonzero; identity transforms; solid colours with RGB uniform in
+  [0,1] and alpha uniform in [0.5,1]; srcOver; painter's order.
+* ``full_feature``: a 2048x2048 canvas, 5,000 paths. 60% fills (half nonzero,
+  half even-odd; 1-4 contours of 4-64 cubics), 40% strokes (width
+  lognormal(ln 4, 0.7); joins miter/round/bevel; caps butt/round/square).
+  Each path has an affine transform: rotation U[0, 2pi), scale log-U[0.25, 4],
+  translation U(canvas). 30% of paints are linear/radial gradients with 2-8
+  stops, 10% use a blend mode drawn from the 16 modes, 10% sit under nested
+  clip paths of depth 1-3. Path geometry is drawn in a local box of
+  [-LOCAL_HALF_EXTENT, LOCAL_HALF_EXTENT]^2 before its transform.
+* ``stroke_stress``: strokes of 1-16 cubics, 20% of them cusps or
+  near-degenerate; width log-U[0.5, 64]; round joins and caps; alpha 0.8.
+
+Everything is drawn from numpy's PCG64 generator, so the same seed gives the
+same bytes on every machine.
+"""
+from __future__ import annotations
+
+import math
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+MAGIC = 0x31435352  # "RSC1"
+
+VERB_MOVE, VERB_LINE, VERB_QUAD, VERB_CUBIC, VERB_CLOSE = 0, 1, 2, 4, 5
+CMD_SAVE, CMD_RESTORE, CMD_TRANSFORM, CMD_DRAW_PATH, CMD_CLIP_PATH = 0, 1, 2, 3, 4
+STYLE_STROKE, STYLE_FILL = 0, 1
+SHADER_NONE, SHADER_LINEAR, SHADER_RADIAL = 0, 1, 2
+FILL_NONZERO, FILL_EVENODD = 0, 1
+JOIN_MITER, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2
+CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
+
+# rive::BlendMode values (include/rive/shapes/paint/blend_mode.hpp).
+BLEND_SRC_OVER = 3
+BLEND_MODES = [3, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28]
+
+LOCAL_HALF_EXTENT = 48.0
+
+DITHER_NONE, DITHER_IGN = 0, 1
+
+
+@dataclass
+class Path:
+    verbs: list
+    points: np.ndarray  # float32 (n, 2)
+    fill_rule: int = FILL_NONZERO
+
+
+@dataclass
+class Paint:
+    style: int = STYLE_FILL
+    color: int = 0xFF000000
+    thickness: float = 1.0
+    join: int = JOIN_MITER
+    cap: int = CAP_BUTT
+    blend_mode: int = BLEND_SRC_OVER
+    shader: int = SHADER_NONE
+    g: tuple = (0.0, 0.0, 0.0, 0.0)
+    stops: list = field(default_factory=list)  # [(pos, color)]
+
+
+@dataclass
+class Scene:
+    width: int
+    height: int
+    clear_color: int = 0xFFFFFFFF
+    dither_mode: int = DITHER_IGN
+    paths: list = field(default_factory=list)
+    paints: list = field(default_factory=list)
+    cmds: list = field(default_factory=list)  # (op, a, b, m6)
+
+    def add_path(self, p: Path) -> int:
+        self.paths.append(p)
+        return len(self.paths) - 1
+
+    def add_paint(self, p: Paint) -> int:
+        self.paints.append(p)
+        return len(self.paints) - 1
+
+    def cmd(self, op, a=0, b=0, m=(0, 0, 0, 0, 0, 0)):
+        self.cmds.append((op, a, b, tuple(float(v) for v in m)))
+
+    def to_bytes(self) -> bytes:
+        verbs = bytearray()
+        pts = []
+        stops = []
+        path_recs = []
+        npts = 0
+        for p in self.paths:
+            pa = np.asarray(p.points, dtype=np.float32).reshape(-1, 2)
+            path_recs.append(struct.pack("<5I", len(verbs), len(p.verbs), npts,
+                                         len(pa), p.fill_rule))
+            verbs.extend(bytes(p.verbs))
+            pts.append(pa)
+            npts += len(pa)
+        paint_recs = []
+        for q in self.paints:
+            paint_recs.append(struct.pack(
+                "<IIfIIII4fII", q.style, q.color & 0xFFFFFFFF, q.thickness,
+                q.join, q.cap, q.blend_mode, q.shader, *[float(v) for v in q.g],
+                len(stops), len(q.stops)))
+            stops.extend(q.stops)
+        cmd_recs = [struct.pack("<3I6f", op, a, b, *m) for (op, a, b, m) in self.cmds]
+        header = struct.pack("<12I", MAGIC, self.width, self.height,
+                             self.clear_color & 0xFFFFFFFF, len(self.paths),
+                             len(self.paints), len(self.cmds), len(verbs), npts,
+                             len(stops), self.dither_mode, 0)
+        vpad = bytes((4 - len(verbs) % 4) % 4)
+        pts_bytes = (np.concatenate(pts).astype("<f4").tobytes()
+                     if pts else b"")
+        stop_bytes = b"".join(struct.pack("<fI", float(s), c & 0xFFFFFFFF)
+                              for s, c in stops)
+        return (header + b"".join(path_recs) + b"".join(paint_recs)
+                + b"".join(cmd_recs) + bytes(verbs) + vpad + pts_bytes + stop_bytes)
+
+    @property
+    def draw_count(self):
+        return sum(1 for c in self.cmds if c[0] == CMD_DRAW_PATH)
+
+
+def color_int(r, g, b, a) -> int:
+    """Packs unit floats into rive::ColorInt 0xAARRGGBB (round to nearest)."""
+    q = [int(round(float(v) * 255.0)) for v in (a, r, g, b)]
+    return (q[0] << 24) | (q[1] << 16) | (q[2] << 8) | q[3]
+
+
+def _random_color(rng, alpha_lo=0.5, alpha_hi=1.0):
+    r, g, b = rng.uniform(0.0, 1.0, 3)
+    a = rng.uniform(alpha_lo, alpha_hi)
+    return color_int(r, g, b, a)
+
+
+def _closed_cubic_contour(rng, ncubics, lo, hi):
+    """One contour: move + ncubics cubics returning to the start + close."""
+    p0 = rng.uniform(lo, hi, 2)
+    pts = [p0]
+    verbs = [VERB_MOVE]
+    for i in range(ncubics):
+        c = rng.uniform(lo, hi, (3, 2))
+        if i == ncubics - 1:
+            c[2] = p0
+        pts.extend(c)
+        verbs.append(VERB_CUBIC)
+    verbs.append(VERB_CLOSE)
+    return verbs, pts
+
+
+def _open_cubic_contour(rng, ncubics, lo, hi):
+    pts = [rng.uniform(lo, hi, 2)]
+    verbs = [VERB_MOVE]
+    for _ in range(ncubics):
+        pts.extend(rng.uniform(lo, hi, (3, 2)))
+        verbs.append(VERB_CUBIC)
+    return verbs, pts
+
+
+def plain_small(seed: int = 1, width: int = 512, height: int = 512,
+                n_paths: int = 200, cubics: int = 8) -> Scene:
+    """The plain small workload (512x512, 200 closed 8-cubic fills)."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, clear_color=0xFFFFFFFF)
+    for _ in range(n_paths):
+        verbs, pts = _closed_cubic_contour(rng, cubics, 0.0, float(min(width, height)))
+        pi = sc.add_path(Path(verbs, np.array(pts, np.float32), FILL_NONZERO))
+        qi = sc.add_paint(Paint(style=STYLE_FILL, color=_random_color(rng)))
+        sc.cmd(CMD_DRAW_PATH, pi, qi)
+    return sc
+
+
+def _random_affine(rng, width, height):
+    theta = rng.uniform(0.0, 2.0 * math.pi)
+    s = math.exp(rng.uniform(math.log(0.25), math.log(4.0)))
+    tx = rng.uniform(0.0, width)
+    ty = rng.uniform(0.0, height)
+    c, sn = math.cos(theta) * s, math.sin(theta) * s
+    return (c, sn, -sn, c, tx, ty)
+
+
+def _gradient_paint(rng, paint: Paint):
+    h = LOCAL_HALF_EXTENT
+    nstops = int(rng.integers(2, 9))
+    pos = np.sort(rng.uniform(0.0, 1.0, nstops)).astype(np.float32)
+    pos[0] = 0.0 if rng.uniform() < 0.5 else pos[0]
+    cols = [_random_color(rng) for _ in range(nstops)]
+    if rng.uniform() < 0.5:
+        paint.shader = SHADER_LINEAR
+        a = rng.uniform(-h, h, 2)
+        b = rng.uniform(-h, h, 2)
+        paint.g = (a[0], a[1], b[0], b[1])
+    else:
+        paint.shader = SHADER_RADIAL
+        c = rng.uniform(-h, h, 2)
+        paint.g = (c[0], c[1], rng.uniform(h * 0.2, h * 2.0), 0.0)
+    paint.stops = [(float(p), c) for p, c in zip(pos, cols)]
+
+
+def full_feature(seed: int = 2, width: int = 2048, height: int = 2048,
+                 n_paths: int = 5000, max_contours: int = 4,
+                 min_cubics: int = 4, max_cubics: int = 64) -> Scene:
+    """The full-feature single scene (defaults: 2048x2048, 5,000 paths)."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, clear_color=0xFFFFFFFF)
+    h = LOCAL_HALF_EXTENT
+    for _ in range(n_paths):
+        is_fill = rng.uniform() < 0.6
+        ncont = int(rng.integers(1, max_contours + 1))
+        verbs, pts = [], []
+        for _c in range(ncont):
+            nc = int(rng.integers(min_cubics, max_cubics + 1))
+            if is_fill:
+                v, p = _closed_cubic_contour(rng, nc, -h, h)
+            else:
+                v, p = _open_cubic_contour(rng, nc, -h, h)
+            verbs += v
+            pts += p
+        fill_rule = FILL_EVENODD if (is_fill and rng.uniform() < 0.5) else FILL_NONZERO
+        pi = sc.add_path(Path(verbs, np.array(pts, np.float32), fill_rule))
+        paint = Paint(style=STYLE_FILL if is_fill else STYLE_STROKE,
+                      color=_random_color(rng))
+        if not is_fill:
+            paint.thickness = float(np.exp(rng.normal(math.log(4.0), 0.7)))
+            paint.join = int(rng.integers(0, 3))
+            paint.cap = int(rng.integers(0, 3))
+        if rng.uniform() < 0.3:
+            _gradient_paint(rng, paint)
+        if rng.uniform() < 0.1:
+            paint.blend_mode = int(BLEND_MODES[int(rng.integers(0, 16))])
+        qi = sc.add_paint(paint)
+        m = _random_affine(rng, width, height)
+        clipped = rng.uniform() < 0.1
+        sc.cmd(CMD_SAVE)
+        sc.cmd(CMD_TRANSFORM, m=m)
+        if clipped:
+            depth = int(rng.integers(1, 4))
+            for _d in range(depth):
+                v, p = _closed_cubic_contour(rng, int(rng.integers(3, 9)), -h * 1.2, h * 1.2)
+                ci = sc.add_path(Path(v, np.array(p, np.float32), FILL_NONZERO))
+                sc.cmd(CMD_CLIP_PATH, ci)
+        sc.cmd(CMD_DRAW_PATH, pi, qi)
+        sc.cmd(CMD_RESTORE)
+    return sc
+
+
+def stroke_stress(seed: int = 4, width: int = 1024, height: int = 1024,
+                  n_strokes: int = 5000) -> Scene:
+    """Tessellation-heavy strokes: 1-16 cubics, 20% cusp/near-degenerate."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, clear_color=0xFFFFFFFF)
+    for _ in range(n_strokes):
+        n = int(rng.integers(1, 17))
+        cx, cy = rng.uniform(0, width), rng.uniform(0, height)
+        span = rng.uniform(8.0, 160.0)
+        p = np.array([cx, cy]) + rng.uniform(-span, span, 2)
+        pts = [p]
+        verbs = [VERB_MOVE]
+        for _k in range(n):
+            p3 = np.array([cx, cy]) + rng.uniform(-span, span, 2)
+            if rng.uniform() < 0.2:
+                kind = int(rng.integers(0, 3))
+                chord = p3 - p
+                if kind == 0:   # inner points within 0.1 px of the chord
+                    t = rng.uniform(0, 1, 2)
+                    nrm = np.array([-chord[1], chord[0]])
+                    nrm = nrm / max(np.linalg.norm(nrm), 1e-6)
+                    p1 = p + chord * t[0] + nrm * rng.uniform(-0.1, 0.1)
+                    p2 = p + chord * t[1] + nrm * rng.uniform(-0.1, 0.1)
+                elif kind == 1:  # coincident with the endpoints
+                    p1, p2 = p.copy(), p3.copy()
+                else:           # cusp: control points crossed over
+                    p1, p2 = p3 + (p3 - p) * 0.5, p - (p3 - p) * 0.5
+            else:
+                p1 = np.array([cx, cy]) + rng.uniform(-span, span, 2)
+                p2 = np.array([cx, cy]) + rng.uniform(-span, span, 2)
+            pts += [p1, p2, p3]
+            verbs.append(VERB_CUBIC)
+            p = p3
+        pi = sc.add_path(Path(verbs, np.array(pts, np.float32), FILL_NONZERO))
+        r, g, b = rng.uniform(0, 1, 3)
+        width_px = float(math.exp(rng.uniform(math.log(0.5), math.log(64.0))))
+        qi = sc.add_paint(Paint(style=STYLE_STROKE, color=color_int(r, g, b, 0.8),
+                                thickness=width_px, join=JOIN_ROUND, cap=CAP_ROUND))
+        sc.cmd(CMD_DRAW_PATH, pi, qi)
+    return sc
