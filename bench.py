@@ -1,0 +1,329 @@
+"""Benchmark of the GB300 flush backend on the full-feature single scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload full_feature|plain_small] [--capture FILE]
+
+A step is one frame: every logical flush of the frame (gradient ramps,
+tessellation, patch set-up, tile binning + sort, raster resolve) over the
+frame's record buffers. Workload (default): the full-feature scene, a
+2048x2048 RGBA8 canvas with 5,000 paths (seeded synthetic, see
+rive-runtime_gb300/scene.py), turned into flush records by the planner (or read
+from --capture).
+
+Printed JSON (one line, rank 0):
+  value        frames/s with the records resident in HBM (rive_cuda_flush_device)
+  e2e          frames/s through the C ABI with host buffers: map/write/unmap of
+               every record buffer (H2D) + all flushes + read-back of the
+               RGBA8 target (D2H), inside the timed region
+  roofline     the dominant kernel's algorithmic bytes per launch over its
+               CUDA-event duration, against the measured HBM copy peak
+  cpu_baseline the oracle (CPU restatement of the passes) on the host cores
+--impl reference times that CPU implementation alone, on the same workload.
+
+Multi-GPU: the path shards by scene only (replicas). With N>1 each rank
+renders its own copy of the workload; value = frames of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+
+def _package():
+    from conftest import load_package
+    return load_package()
+
+
+def build_workload(args):
+    _package()
+    from rive_runtime_gb300 import capture, scene
+    if args.capture:
+        with open(args.capture, "rb") as f:
+            return capture.parse(f.read()), f"capture:{os.path.basename(args.capture)}"
+    from rive_runtime_gb300 import planner
+    if args.workload == "full_feature":
+        sc = scene.full_feature(seed=2)
+    elif args.workload == "plain_small":
+        sc = scene.plain_small(seed=1)
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    return planner.plan(sc.to_bytes()), args.workload
+
+
+def workload_counts(cap):
+    spans = paths = contours = grad_spans = grad_rows = verts = 0
+    for f in cap.flushes:
+        d = f.desc
+        spans += d["tess_span_count"]
+        paths += d["path_count"]
+        contours += d["contour_count"]
+        grad_spans += d["grad_span_count"]
+        grad_rows += d["grad_data_height"]
+        verts += int(f.batches[:, 1].sum()) * 8 if len(f.batches) else 0
+    return dict(spans=spans, paths=paths, contours=contours, grad_spans=grad_spans,
+                grad_rows=grad_rows, tess_vertices=verts, flushes=len(cap.flushes))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(cap, threads):
+    """The oracle (CPU restatement of the passes) on one whole frame."""
+    import oracle
+    t0 = time.perf_counter()
+    oracle.render(cap, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt
+
+
+def run_reference(args, cap, wname, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(max(args.warmup_cpu, 0)):
+        cpu_baseline(cap, threads)
+    times = [cpu_baseline(cap, threads) for _ in range(args.steps_cpu)]
+    fps = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup_cpu,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wname, "width": cap.width, "height": cap.height},
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} whole frame(s) of {wname} through the oracle "
+                                   "(CPU restatement of the three GPU passes)"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "vs_baseline": None,
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, cap, wname, rank, world):
+    import numpy as np
+    import torch
+    from rive_runtime_gb300 import rive_cuda
+    from rive_runtime_gb300.capture import BUFFER_NAMES
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    ctx = rive_cuda.Context(dev)
+    W, H = cap.width, cap.height
+
+    # Device-resident records for the `value` measurement.
+    dbufs = rive_cuda.DeviceBuffers()
+    keep = []
+    for name in BUFFER_NAMES:
+        b = cap.buffers.get(name, b"")
+        t = torch.from_numpy(np.frombuffer(b, np.uint8).copy()).cuda() if b else None
+        keep.append(t)
+        setattr(dbufs, name, t.data_ptr() if t is not None else None)
+    target = torch.zeros((H, W, 4), dtype=torch.uint8, device="cuda")
+
+    def frame_device():
+        for f in cap.flushes:
+            ctx.flush_device(f, dbufs, target.data_ptr(), stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        frame_device()
+    ctx.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+
+    # Timed region (device-resident). Inputs per frame (records, 4 tess
+    # textures, triangle records, bins) are far larger than the 129 MB L2.
+    sampler = ClockSampler(dev)
+    sampler.start()
+    ctx.set_profiling(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        frame_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clocks = sampler.stop()
+    prof = ctx.profile_collect()
+    ctx.set_profiling(False)
+    ctx.sync(stream.cuda_stream)
+    stats = ctx.stats()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    fps = world * args.steps / (ms / 1e3)
+
+    # End to end through the C ABI with host buffers.
+    frame_bytes = sum(len(cap.buffers.get(n, b"")) for n in BUFFER_NAMES)
+    host_t = ctx.render_target(W, H)
+    out = np.empty((H, W, 4), np.uint8)
+
+    def frame_e2e():
+        ctx.upload_frame(cap)
+        for f in cap.flushes:
+            ctx.flush(f, host_t)
+        ctx.read_target(host_t, W, H, out)
+
+    for _ in range(args.warmup):
+        frame_e2e()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        frame_e2e()
+    e2e_s = time.perf_counter() - t0
+    e2e_fps = args.steps / e2e_s
+
+    # Roofline of the dominant stage.
+    counts = workload_counts(cap)
+    peak, peak_kind = measured_peak_gbs()
+    dominant = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_launches = prof[dominant]
+    per_launch_s = (dom_ms / max(dom_launches, 1)) / 1e3
+    pairs_per_frame = None
+    if dominant == "raster":
+        # bin entries of the last flush scaled to one launch; B_r =
+        # entries x (4 B slot index + 80 B triangle record) + 4 W H (+ 4 W H
+        # read when preserving).
+        entries = stats["bin_entries"]
+        traffic_units = entries * 84 + 4 * W * H * 2
+        alg_bytes = traffic_units
+    elif dominant == "tessellate":
+        alg_bytes = 64 * counts["spans"] / counts["flushes"] + 16 * counts["tess_vertices"] / counts["flushes"]
+    else:
+        alg_bytes = 0
+    achieved = alg_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    line = {
+        "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": wname, "width": W, "height": H, "flushes_per_frame": len(cap.flushes),
+                   "l2": "inputs per frame far larger than L2 (no flush needed)",
+                   "gpx_per_s": fps * W * H / 1e9, **counts},
+        "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
+                "d2h_bytes_per_step": W * H * 4},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": None},
+        "stage_ms_per_frame": {k: v[0] / args.steps for k, v in prof.items()},
+        "gpu_launches": int(sum(v[1] for v in prof.values())),
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        dt = cpu_baseline(cap, threads)
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "frames/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"1 whole frame of {wname} through the oracle"}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="full_feature")
+    ap.add_argument("--capture", default=None)
+    ap.add_argument("--steps-cpu", type=int, default=2)
+    ap.add_argument("--warmup-cpu", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if args.impl == "ours":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group(backend)
+    cap, wname = build_workload(args)
+    if args.impl == "reference":
+        run_reference(args, cap, wname, rank, world)
+    else:
+        run_ours(args, cap, wname, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

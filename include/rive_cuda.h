@@ -250,6 +250,28 @@ typedef struct rive_cuda_flush_stats
 int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
                                rive_cuda_flush_stats* out);
 
+/*
+ * Per-stage device timing with CUDA events recorded on the flush stream
+ * (off by default; no counterpart in the reference, whose backends time
+ * nothing). Stages of one flush, in launch order:
+ */
+enum
+{
+    RIVE_CUDA_STAGE_COLOR_RAMP = 0,  /* color_ramp_kernel                 */
+    RIVE_CUDA_STAGE_TESSELLATE = 1,  /* tessellate_kernel                 */
+    RIVE_CUDA_STAGE_PATCH_SETUP = 2, /* patch_setup_kernel                */
+    RIVE_CUDA_STAGE_BIN = 3,         /* scan + bin_scatter_kernel         */
+    RIVE_CUDA_STAGE_SORT = 4,        /* radix sort + tile_ranges_kernel   */
+    RIVE_CUDA_STAGE_RASTER = 5,      /* raster_tile_kernel                */
+    RIVE_CUDA_STAGE_COUNT = 6,
+};
+int rive_cuda_set_profiling(rive_cuda_context* ctx, int enabled);
+/* Waits for the recorded events, returns the summed milliseconds and launch
+ * counts per stage since the last collect, and clears them. */
+int rive_cuda_profile_collect(rive_cuda_context* ctx,
+                              double ms[RIVE_CUDA_STAGE_COUNT],
+                              uint64_t launches[RIVE_CUDA_STAGE_COUNT]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,7 +52,13 @@ public:
     {}
 
 private:
-    void* onMapBuffer(int, size_t) override { return shadowBuffer(); }
+    // Zero the staging memory so padding the front end skips (alignment gaps,
+    // unused record fields) is deterministic in the capture.
+    void* onMapBuffer(int, size_t bytes) override
+    {
+        memset(shadowBuffer(), 0, bytes);
+        return shadowBuffer();
+    }
     void onUnmapAndSubmitBuffer(int, size_t bytes) override
     {
         m_sink->assign(shadowBuffer(), shadowBuffer() + bytes);

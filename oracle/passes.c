@@ -445,9 +445,11 @@ static int tess_setup(const rive_cuda_flush_desc* d,
 }
 
 /* Fragment half of pass 2 (tessellate.glsl:294-567): one vertex. */
-static void tess_fragment(const tess_varyings* v,
-                          float vertexIdxIn,
-                          uint32_t out[4])
+static void tess_fragment_t(const tess_varyings* v,
+                            float vertexIdxIn,
+                            uint32_t out[4],
+                            float* outT,
+                            f2 outPts[4])
 {
     f2 p0 = v->p0, p1 = v->p1, p2 = v->p2, p3 = v->p3;
     f2 tan0, tan1;
@@ -589,11 +591,24 @@ static void tess_fragment(const tess_varyings* v,
         tessCoord = add2(mul2(sub2(bcd, abc), T), abc);
         if (T != polarT)
             theta = rive_atan2(sub2(bcd, abc));
+        if (outT)
+        {
+            *outT = T;
+            outPts[0] = p0;
+            outPts[1] = p1;
+            outPts[2] = p2;
+            outPts[3] = p3;
+        }
     }
     out[0] = f2u(tessCoord.x);
     out[1] = f2u(tessCoord.y);
     out[2] = f2u(glsl_mod(theta, TWO_PI_F));
     out[3] = contourIDWithFlags;
+}
+
+static void tess_fragment(const tess_varyings* v, float vertexIdxIn, uint32_t out[4])
+{
+    tess_fragment_t(v, vertexIdxIn, out, NULL, NULL);
 }
 
 int oracle_tessellate(const rive_cuda_flush_desc* d,
@@ -640,39 +655,11 @@ int oracle_tessellate(const rive_cuda_flush_desc* d,
 }
 
 /* ---- FP64 twin of pass 2 --------------------------------------------------
- * The same algorithm evaluated in double, for the tessellated-vertex
- * tolerance. Discrete choices (segment indices) are re-derived in double too.
+ * For the tessellated-vertex tolerance: the same segment parameters (the
+ * merged vertex's T, chosen by the fp32 algorithm above) evaluated in double
+ * precision with De Casteljau. Endpoint and join vertices are exact copies of
+ * control points in both and are returned as such.
  */
-typedef struct
-{
-    double x, y;
-} d2;
-static inline d2 dsub(d2 a, d2 b) { return (d2){a.x - b.x, a.y - b.y}; }
-static inline d2 dadd(d2 a, d2 b) { return (d2){a.x + b.x, a.y + b.y}; }
-static inline d2 dmul(d2 a, double s) { return (d2){a.x * s, a.y * s}; }
-static inline double ddot(d2 a, d2 b) { return a.x * b.x + a.y * b.y; }
-static inline d2 dnorm(d2 v)
-{
-    double inv = 1.0 / sqrt(ddot(v, v));
-    return (d2){v.x * inv, v.y * inv};
-}
-static inline double ddet(d2 a, d2 b) { return a.x * b.y - b.x * a.y; }
-static inline double dclamp(double x, double lo, double hi)
-{
-    return x < lo ? lo : (x > hi ? hi : x);
-}
-static double dcos_between(d2 a, d2 b)
-{
-    double ab = ddot(a, b), p = ddot(a, a) * ddot(b, b);
-    return p == 0.0 ? 1.0 : dclamp(ab / sqrt(p), -1.0, 1.0);
-}
-static inline int dneq(d2 a, d2 b) { return a.x != b.x || a.y != b.y; }
-static void dtangents(d2 p0, d2 p1, d2 p2, d2 p3, d2* t0, d2* t1)
-{
-    *t0 = dsub(dneq(p0, p1) ? p1 : dneq(p1, p2) ? p2 : p3, p0);
-    *t1 = dsub(p3, dneq(p3, p2) ? p2 : dneq(p2, p1) ? p1 : p0);
-}
-
 int oracle_tessellate_f64(const rive_cuda_flush_desc* d,
                           const oracle_buffers* b,
                           double* xy,
@@ -705,118 +692,33 @@ int oracle_tessellate_f64(const rive_cuda_flush_desc* d,
                 lo = 0;
             if (hi > TESS_TEXTURE_WIDTH)
                 hi = TESS_TEXTURE_WIDTH;
-            d2 P0 = {v.p0.x, v.p0.y}, P1 = {v.p1.x, v.p1.y};
-            d2 P2 = {v.p2.x, v.p2.y}, P3 = {v.p3.x, v.p3.y};
-            /* Re-derive radsPerPolarSegment in double. */
-            d2 T0, T1;
-            dtangents(P0, P1, P2, P3, &T0, &T1);
-            double polarCount = (double)(((sp[14]) >> 10) & 0x3ffu);
-            double rpp = acos(dcos_between(T0, T1)) / polarCount;
-            if (v.radsPerPolarSegment < 0.f)
-                rpp = -rpp;
             for (int px = lo; px < hi; ++px)
             {
                 size_t texel = (size_t)row * TESS_TEXTURE_WIDTH + px;
-                uint32_t f32out[4];
+                uint32_t o[4];
+                float T = -1.f;
+                f2 q[4];
                 float vertexIdx =
                     v.totalVertexCount - fabsf((float)x1 - ((float)px + .5f));
-                tess_fragment(&v, vertexIdx, f32out);
-                tess_flags[texel] = f32out[3];
-                /* Evaluate the same merged vertex in double. */
-                double vid = floor((double)vertexIdx);
-                if (vid < 0)
-                    vid = 0;
-                double merged = (double)v.totalVertexCount - v.joinSegmentCount;
-                d2 q0 = P0, q1 = P1, q2 = P2, q3 = P3;
-                d2 t0 = T0;
-                double pc = v.parametricSegmentCount;
-                double r = rpp;
-                double mid = vid;
-                int isJoin = 0;
-                if (mid > merged)
+                tess_fragment_t(&v, vertexIdx, o, &T, q);
+                tess_flags[texel] = o[3];
+                if (T < 0.f)
                 {
-                    isJoin = 1;
-                    q0 = q1 = q2 = q3;
-                    mid -= merged;
-                    merged = v.joinSegmentCount;
+                    xy[texel * 2 + 0] = u2f(o[0]);
+                    xy[texel * 2 + 1] = u2f(o[1]);
+                    continue;
                 }
-                d2 out;
-                if (isJoin || mid == 0.0 || mid == merged ||
-                    (f32out[3] & RETROFIT_TRI_STRIP_CONTOUR_FLAG))
-                {
-                    out = (d2){u2f(f32out[0]), u2f(f32out[1])};
-                    if (!isJoin && !(f32out[3] & RETROFIT_TRI_STRIP_CONTOUR_FLAG))
-                        out = (mid < merged * .5) ? q0 : q3;
-                    else if (isJoin)
-                        out = q3;
-                }
-                else
-                {
-                    double T, polarT;
-                    if (pc == merged)
-                    {
-                        T = mid / pc;
-                        polarT = 0;
-                    }
-                    else
-                    {
-                        d2 C = dsub(q1, q0), D = dsub(q3, q0), E = dsub(q2, q1);
-                        d2 B = dsub(E, C), A = dadd(dmul(E, -3.0), D);
-                        d2 B_ = dmul(B, pc * 2.0), C_ = dmul(C, pc * pc);
-                        double last = 0, maxP = fmin(pc - 1.0, mid);
-                        d2 t0n = dnorm(t0);
-                        double neg = -fabs(r), mr0 = (1.0 + mid) * fabs(r);
-                        for (int p = 9; p >= 0; --p)
-                        {
-                            double tp = last + ldexp(1.0, p);
-                            if (tp <= maxP)
-                            {
-                                d2 tt = dadd(dmul(A, tp), B_);
-                                tt = dadd(dmul(tt, tp), C_);
-                                double cr = ddot(dnorm(tt), t0n);
-                                double mr = fmin(tp * neg + mr0, 3.14159265358979323846);
-                                if (cr >= cos(mr))
-                                    last = tp;
-                            }
-                        }
-                        double parametricT = last / pc;
-                        double lastPolar = mid - last;
-                        double th0 = acos(dclamp(t0n.x, -1, 1));
-                        th0 = t0n.y >= 0 ? th0 : -th0;
-                        double th = lastPolar * r + th0;
-                        d2 nrm = {sin(th), -cos(th)};
-                        double a = ddot(nrm, A), bo2 = ddot(nrm, B), c = ddot(nrm, C);
-                        double disc = fmax(bo2 * bo2 - a * c, 0.0);
-                        double q = sqrt(disc);
-                        if (bo2 > 0)
-                            q = -q;
-                        q -= bo2;
-                        double h = -.5 * q * a, rs, rt;
-                        if (fabs(q * q + h) < fabs(a * c + h))
-                        {
-                            rs = q;
-                            rt = a;
-                        }
-                        else
-                        {
-                            rs = c;
-                            rt = q;
-                        }
-                        polarT = rt != 0 ? rs / rt : 0;
-                        polarT = dclamp(polarT, 0, 1);
-                        if (lastPolar == 0)
-                            polarT = 0;
-                        T = fmax(parametricT, polarT);
-                    }
-                    d2 ab = dadd(dmul(dsub(q1, q0), T), q0);
-                    d2 bc = dadd(dmul(dsub(q2, q1), T), q1);
-                    d2 cd = dadd(dmul(dsub(q3, q2), T), q2);
-                    d2 abc = dadd(dmul(dsub(bc, ab), T), ab);
-                    d2 bcd = dadd(dmul(dsub(cd, bc), T), bc);
-                    out = dadd(dmul(dsub(bcd, abc), T), abc);
-                }
-                xy[texel * 2 + 0] = out.x;
-                xy[texel * 2 + 1] = out.y;
+                double t = T;
+                double ax = q[0].x + (q[1].x - (double)q[0].x) * t;
+                double ay = q[0].y + (q[1].y - (double)q[0].y) * t;
+                double bx = q[1].x + (q[2].x - (double)q[1].x) * t;
+                double by = q[1].y + (q[2].y - (double)q[1].y) * t;
+                double cx = q[2].x + (q[3].x - (double)q[2].x) * t;
+                double cy = q[2].y + (q[3].y - (double)q[2].y) * t;
+                double abx = ax + (bx - ax) * t, aby = ay + (by - ay) * t;
+                double bcx = bx + (cx - bx) * t, bcy = by + (cy - by) * t;
+                xy[texel * 2 + 0] = abx + (bcx - abx) * t;
+                xy[texel * 2 + 1] = aby + (bcy - aby) * t;
             }
         }
     }
@@ -1201,17 +1103,17 @@ static void set_lum_sat(const float hue[3],
     set_lum(hs, lum, out);
 }
 
-/* advanced_blend.glsl:156-327 */
-void oracle_advanced_blend(const float srcIn[3],
-                           const float dstPremulIn[4],
-                           int mode,
-                           float out[3])
+/* advanced_blend_coeffs (advanced_blend.glsl:156-301). */
+void oracle_advanced_blend_coeffs(const float srcIn[3],
+                                  const float dstPremulIn[4],
+                                  int mode,
+                                  float co[3])
 {
     float src[3] = {srcIn[0], srcIn[1], srcIn[2]};
     float dp[4] = {dstPremulIn[0], dstPremulIn[1], dstPremulIn[2], dstPremulIn[3]};
     float inv = dp[3] != 0.f ? 1.f / dp[3] : 0.f;
     float dst[3] = {dp[0] * inv, dp[1] * inv, dp[2] * inv};
-    float co[3] = {0, 0, 0};
+    co[0] = co[1] = co[2] = 0.f;
     switch (mode)
     {
         case BLEND_MODE_MULTIPLY:
@@ -1306,6 +1208,16 @@ void oracle_advanced_blend(const float srcIn[3],
         default:
             break;
     }
+}
+
+/* advanced_color_blend (advanced_blend.glsl:303-327). */
+void oracle_advanced_blend(const float srcIn[3],
+                           const float dstPremulIn[4],
+                           int mode,
+                           float out[3])
+{
+    float co[3];
+    oracle_advanced_blend_coeffs(srcIn, dstPremulIn, mode, co);
     /* mix(src, coeffs, dstPremul.a) = src * (1 - a) + coeffs * a, with the
      * caller's (unclamped) src: advanced_blend_coeffs takes src by value. */
     float a = dstPremulIn[3];

@@ -93,6 +93,12 @@ void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
 uint16_t oracle_f32_to_f16(float f);
 float oracle_f16_to_f32(uint16_t h);
 
+/* Blend coefficients of one mode (advanced_blend.glsl:156-301). */
+void oracle_advanced_blend_coeffs(const float src[3],
+                                  const float dst_premul[4],
+                                  int mode,
+                                  float out_rgb[3]);
+
 /* Advanced blend of one unmultiplied src over a premultiplied dst
  * (advanced_blend.glsl:156-327), exposed for known-answer tests. */
 void oracle_advanced_blend(const float src[3],

@@ -1,0 +1,987 @@
+// Draw pass of a rasterOrdering flush: patch expansion, triangle set-up, tile
+// binning and the raster-ordered pixel resolve.
+//
+// Reference semantics:
+//  * patch expansion: renderer/src/shaders/draw_path.vert:96-422 with
+//    unpack_tessellated_path_vertex (draw_path_common.glsl:275-789) over the
+//    midpointFan patch (gpu.cpp:446-687: 42 vertices, 72 indices);
+//  * rasterisation: Vulkan rules of the reference backend -- pixel centres,
+//    top-left ties, clockwise front faces, counterclockwise culled
+//    (gpu.cpp:1552-1567, vulkan/draw_pipeline_vulkan.cpp:333-334);
+//  * resolve: draw_raster_order_path.frag:14-238 (fp16 coverage keyed by
+//    path ID, nonzero/even-odd, nested clip, clip rect, paint colour,
+//    advanced blend, src-over, dither).
+//
+// GB300 design: instead of a hardware rasteriser with fragment interlock, the
+// flush is tiled. Each triangle is set up once (edge functions with canonical
+// anchors, coverage planes) into an 80-byte record; (tile, triangle) pairs are
+// radix-sorted by tile, which keeps primitive order inside each tile; then one
+// 256-thread CTA per 16x16 tile walks its triangles in order with each thread
+// owning one pixel and its pixel-local-storage planes in registers. Raster
+// order therefore holds by construction, with no interlock and no atomics.
+#include "rive_cuda_internal.cuh"
+
+#include <cuda_fp16.h>
+
+namespace rivecuda
+{
+namespace
+{
+struct PatchVertexDesc
+{
+    float localVertexID, outset, fillCoverage;
+    float mLocalVertexID, mOutset, mFillCoverage;
+    int vertexType;
+};
+
+// The midpointFan patch vertex table of gpu.cpp:446-560, by vertex index.
+__device__ __forceinline__ PatchVertexDesc patch_vertex_desc(int v)
+{
+    PatchVertexDesc d;
+    if (v < 32)
+    {
+        int seg = v >> 2, k = v & 3;
+        float l = (float)seg, r = l + 1.f;
+        d.vertexType = STROKE_VERTEX;
+        switch (k)
+        {
+            case 0:
+                d.localVertexID = l; d.outset = -1.f; d.fillCoverage = 1.f;
+                d.mLocalVertexID = r - 1.f; d.mOutset = -1.f; d.mFillCoverage = 1.f;
+                break;
+            case 1:
+                d.localVertexID = l; d.outset = 1.f; d.fillCoverage = 0.f;
+                d.mLocalVertexID = l - 1.f; d.mOutset = -1.f; d.mFillCoverage = 1.f;
+                break;
+            case 2:
+                d.localVertexID = r; d.outset = -1.f; d.fillCoverage = 1.f;
+                d.mLocalVertexID = r - 1.f; d.mOutset = 1.f; d.mFillCoverage = 0.f;
+                break;
+            default:
+                d.localVertexID = r; d.outset = 1.f; d.fillCoverage = 0.f;
+                d.mLocalVertexID = l - 1.f; d.mOutset = 1.f; d.mFillCoverage = 0.f;
+                break;
+        }
+    }
+    else if (v < 41)
+    {
+        float i = (float)(v - 32);
+        d.vertexType = FAN_VERTEX;
+        d.localVertexID = i; d.outset = -1.f; d.fillCoverage = 1.f;
+        d.mLocalVertexID = i - 1.f; d.mOutset = -1.f; d.mFillCoverage = 1.f;
+    }
+    else
+    {
+        d.vertexType = FAN_MIDPOINT_VERTEX;
+        d.localVertexID = 0.f; d.outset = 0.f; d.fillCoverage = 1.f;
+        d.mLocalVertexID = 0.f; d.mOutset = 0.f; d.mFillCoverage = 1.f;
+    }
+    return d;
+}
+
+// The midpointFan index table (gpu.cpp:600-680), by triangle index.
+__device__ __forceinline__ void patch_triangle(int t, int& a, int& b, int& c)
+{
+    if (t < 16)
+    {
+        int e = (t >> 1) * 4;
+        if ((t & 1) == 0) { a = e; b = e + 1; c = e + 2; }
+        else { a = e + 2; b = e + 1; c = e + 3; }
+        return;
+    }
+    // Middle-out fan over the 9 fan vertices (32..40), then the triangle to
+    // the contour midpoint (41).
+    switch (t)
+    {
+        case 16: a = 32; b = 33; c = 34; return;
+        case 17: a = 34; b = 35; c = 36; return;
+        case 18: a = 36; b = 37; c = 38; return;
+        case 19: a = 38; b = 39; c = 40; return;
+        case 20: a = 32; b = 34; c = 36; return;
+        case 21: a = 36; b = 38; c = 40; return;
+        case 22: a = 32; b = 36; c = 40; return;
+        default: a = 32; b = 40; c = 41; return;
+    }
+}
+
+__device__ __forceinline__ float2 mat_mul(float4 m, float2 v)
+{
+    // float2x2 columns (m.x, m.y) and (m.z, m.w).
+    return make_float2(__fadd_rn(__fmul_rn(m.x, v.x), __fmul_rn(m.z, v.y)),
+                       __fadd_rn(__fmul_rn(m.y, v.x), __fmul_rn(m.w, v.y)));
+}
+
+// draw_path_common.glsl:267-274
+__device__ __forceinline__ float manhattan_pixel_width(float4 M, float2 n)
+{
+    float2 v = mat_mul(M, n);
+    return __fmul_rn(__fadd_rn(fabsf(v.x), fabsf(v.y)),
+                     __fdiv_rn(1.f, __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y))));
+}
+
+__device__ __forceinline__ float signf(float x)
+{
+    return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);
+}
+
+struct VertexOut
+{
+    float2 pos;
+    float2 cov;
+    uint32_t pathID;
+    bool discard;
+};
+
+__device__ __forceinline__ bool tess_fetch(const FlushParams& P, long long idx, uint4& out)
+{
+    if (idx < 0 || idx >= (long long)P.tessDataHeight * kTessTextureWidth)
+    {
+        atomicOr(P.error, ERR_BAD_TESS_INDEX);
+        return false;
+    }
+    out = P.tess[idx];
+    return true;
+}
+
+// unpack_tessellated_path_vertex for a midpointFan patch vertex, plus the
+// position math of @drawVertexMain. Returns false on a malformed input.
+__device__ bool shade_patch_vertex(const FlushParams& P,
+                                   int v,
+                                   uint32_t instanceID,
+                                   VertexOut& o)
+{
+    PatchVertexDesc pv = patch_vertex_desc(v);
+    int localVertexID = (int)pv.localVertexID;
+    float outset = pv.outset;
+    float fillCoverage = pv.fillCoverage;
+    const int span = kPatchSegmentSpan;
+    int vertexIDOnContour = min(localVertexID, span - 1);
+    long long tessVertexIdx = (long long)instanceID * span + vertexIDOnContour;
+    uint4 tv;
+    if (!tess_fetch(P, tessVertexIdx, tv))
+        return false;
+    uint32_t flags = tv.w;
+    uint32_t contourID = max(flags & CONTOUR_ID_MASK, 1u);
+    if (contourID > P.contourCount)
+    {
+        atomicOr(P.error, ERR_BAD_CONTOUR);
+        return false;
+    }
+    uint4 cd = P.contours[P.firstContour + contourID - 1];
+    float2 midpoint = make_float2(__uint_as_float(cd.x), __uint_as_float(cd.y));
+    uint32_t pathID = cd.z & 0xffffu;
+    uint32_t vertexIndex0 = cd.w;
+    if (pathID >= P.pathCount)
+    {
+        atomicOr(P.error, ERR_BAD_PATH);
+        return false;
+    }
+    const uint4* path = P.paths + 4 * (size_t)(P.firstPath + pathID);
+    uint4 r0 = path[0], r1 = path[1];
+    float4 M = make_float4(__uint_as_float(r0.x), __uint_as_float(r0.y),
+                           __uint_as_float(r0.z), __uint_as_float(r0.w));
+    float2 translate = make_float2(__uint_as_float(r1.x), __uint_as_float(r1.y));
+    float strokeRadius = __uint_as_float(r1.z);
+    float featherRadius = __uint_as_float(r1.w);
+    if (featherRadius != 0.f)
+    {
+        atomicOr(P.error, ERR_FEATHER);
+        return false;
+    }
+    uint32_t mirrored = flags & MIRRORED_CONTOUR_CONTOUR_FLAG;
+    if (mirrored)
+    {
+        localVertexID = (int)pv.mLocalVertexID;
+        outset = pv.mOutset;
+        fillCoverage = pv.mFillCoverage;
+    }
+    if (localVertexID != vertexIDOnContour)
+    {
+        long long repl = tessVertexIdx + localVertexID - vertexIDOnContour;
+        uint4 rv;
+        if (!tess_fetch(P, repl, rv))
+            return false;
+        if ((rv.w & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)) !=
+            (flags & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)))
+        {
+            bool isClosed = strokeRadius == 0.f || midpoint.x != 0.f;
+            if (isClosed)
+            {
+                tessVertexIdx = vertexIndex0;
+                if (!tess_fetch(P, tessVertexIdx, tv))
+                    return false;
+            }
+        }
+        else
+        {
+            tessVertexIdx = repl;
+            tv = rv;
+        }
+        flags = (tv.w & ~MIRRORED_CONTOUR_CONTOUR_FLAG) | mirrored;
+    }
+    float theta = __uint_as_float(tv.z);
+    float sn, cs;
+    sincosf(theta, &sn, &cs);
+    float2 norm = make_float2(sn, -cs);
+    float2 origin = make_float2(__uint_as_float(tv.x), __uint_as_float(tv.y));
+    float2 offset = make_float2(0.f, 0.f);
+    float2 cov;
+    o.discard = false;
+    if (strokeRadius != 0.f)
+    {
+        float detM = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
+        outset = __fmul_rn(outset, signf(detM));
+        if (flags & LEFT_JOIN_CONTOUR_FLAG)
+            outset = fminf(outset, 0.f);
+        if (flags & RIGHT_JOIN_CONTOUR_FLAG)
+            outset = fmaxf(outset, 0.f);
+        float aaRadius = __fmul_rn(manhattan_pixel_width(M, norm), kAARadius);
+        float globalCoverage = 1.f;
+        if (aaRadius > strokeRadius)
+        {
+            globalCoverage = __fdiv_rn(strokeRadius, aaRadius);
+            strokeRadius = aaRadius;
+        }
+        float sr = __fadd_rn(strokeRadius, aaRadius);
+        float2 vertexOffset = make_float2(__fmul_rn(norm.x, sr), __fmul_rn(norm.y, sr));
+        float x = __fmul_rn(outset, sr);
+        float k = __fdiv_rn(1.f, __fmul_rn(aaRadius, 2.f));
+        cov.x = __fadd_rn(__fmul_rn(k, __fadd_rn(x, strokeRadius)), .5f);
+        cov.y = __fadd_rn(__fmul_rn(k, __fadd_rn(-x, strokeRadius)), .5f);
+        uint32_t joinType = flags & JOIN_TYPE_MASK;
+        if (joinType > ROUND_JOIN_CONTOUR_FLAG)
+        {
+            int peekDir = 2;
+            if (!(flags & JOIN_TANGENT_0_CONTOUR_FLAG))
+                peekDir = -peekDir;
+            if (flags & MIRRORED_CONTOUR_CONTOUR_FLAG)
+                peekDir = -peekDir;
+            uint4 ov;
+            if (!tess_fetch(P, tessVertexIdx + peekDir, ov))
+                return false;
+            float otherTheta = __uint_as_float(ov.z);
+            float joinAngle = fabsf(__fsub_rn(otherTheta, theta));
+            if (joinAngle > kPi)
+                joinAngle = __fsub_rn(k2Pi, joinAngle);
+            bool isTan0 = (flags & JOIN_TANGENT_0_CONTOUR_FLAG) != 0;
+            bool isLeft = (flags & LEFT_JOIN_CONTOUR_FLAG) != 0;
+            float bisectTheta =
+                __fadd_rn(__fmul_rn(joinAngle, isTan0 == isLeft ? -.5f : .5f), theta);
+            float bs, bc;
+            sincosf(bisectTheta, &bs, &bc);
+            float2 bisector = make_float2(bs, -bc);
+            float bisectPixelWidth = manhattan_pixel_width(M, bisector);
+            float miterRatio = cosf(__fmul_rn(joinAngle, .5f));
+            float clipRadius;
+            if (joinType == MITER_CLIP_JOIN_CONTOUR_FLAG ||
+                (joinType == MITER_REVERT_JOIN_CONTOUR_FLAG && miterRatio >= .25f))
+            {
+                float inverseLimit = (flags & EMULATED_STROKE_CAP_CONTOUR_FLAG) ? 1.f : .25f;
+                clipRadius = __fmul_rn(strokeRadius,
+                                       __fdiv_rn(1.f, fmaxf(miterRatio, inverseLimit)));
+            }
+            else
+            {
+                clipRadius = __fadd_rn(__fmul_rn(strokeRadius, miterRatio),
+                                       __fmul_rn(bisectPixelWidth, .5f));
+            }
+            float clipAARadius = __fadd_rn(clipRadius, __fmul_rn(bisectPixelWidth, kAARadius));
+            if (flags & JOIN_TANGENT_INNER_CONTOUR_FLAG)
+            {
+                float strokeAARadius = __fadd_rn(strokeRadius, aaRadius);
+                float slop = __fmul_rn(aaRadius, .125f);
+                if (strokeAARadius <= __fadd_rn(__fmul_rn(clipAARadius, miterRatio), slop))
+                {
+                    float miterAARadius = __fmul_rn(strokeAARadius, __fdiv_rn(1.f, miterRatio));
+                    vertexOffset = make_float2(__fmul_rn(bisector.x, miterAARadius),
+                                               __fmul_rn(bisector.y, miterAARadius));
+                }
+                else
+                {
+                    float2 bo = make_float2(__fmul_rn(bisector.x, clipAARadius),
+                                            __fmul_rn(bisector.y, clipAARadius));
+                    float kx = __fadd_rn(__fmul_rn(vertexOffset.x, vertexOffset.x),
+                                         __fmul_rn(vertexOffset.y, vertexOffset.y));
+                    float ky = __fadd_rn(__fmul_rn(bo.x, bo.x), __fmul_rn(bo.y, bo.y));
+                    // Row vector k times inverse of the matrix with columns
+                    // vertexOffset and bo.
+                    float det = __fsub_rn(__fmul_rn(vertexOffset.x, bo.y),
+                                          __fmul_rn(bo.x, vertexOffset.y));
+                    float i00 = __fdiv_rn(bo.y, det), i01 = __fdiv_rn(-vertexOffset.y, det);
+                    float i10 = __fdiv_rn(-bo.x, det), i11 = __fdiv_rn(vertexOffset.x, det);
+                    vertexOffset = make_float2(__fadd_rn(__fmul_rn(kx, i00), __fmul_rn(ky, i01)),
+                                               __fadd_rn(__fmul_rn(kx, i10), __fmul_rn(ky, i11)));
+                }
+            }
+            float ao = fabsf(outset);
+            float2 pt = make_float2(__fmul_rn(vertexOffset.x, ao), __fmul_rn(vertexOffset.y, ao));
+            float clipDistance =
+                __fdiv_rn(__fsub_rn(clipAARadius,
+                                    __fadd_rn(__fmul_rn(pt.x, bisector.x), __fmul_rn(pt.y, bisector.y))),
+                          __fmul_rn(bisectPixelWidth, kAARadius * 2.f));
+            if (flags & LEFT_JOIN_CONTOUR_FLAG)
+                cov.y = clipDistance;
+            else
+                cov.x = clipDistance;
+        }
+        cov.x = __fmul_rn(cov.x, globalCoverage);
+        cov.y = __fmul_rn(cov.y, globalCoverage);
+        cov.y = fmaxf(cov.y, 1e-4f);
+        offset = mat_mul(M, make_float2(__fmul_rn(vertexOffset.x, outset),
+                                        __fmul_rn(vertexOffset.y, outset)));
+        if (pv.vertexType != STROKE_VERTEX)
+            o.discard = true;
+    }
+    else
+    {
+        cov = make_float2(fillCoverage, -1.f);
+        float2 on = make_float2(__fmul_rn(norm.x, outset), __fmul_rn(norm.y, outset));
+        float det = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
+        float i00 = __fdiv_rn(M.w, det), i01 = __fdiv_rn(-M.y, det);
+        float i10 = __fdiv_rn(-M.z, det), i11 = __fdiv_rn(M.x, det);
+        float rx = __fadd_rn(__fmul_rn(on.x, i00), __fmul_rn(on.y, i01));
+        float ry = __fadd_rn(__fmul_rn(on.x, i10), __fmul_rn(on.y, i11));
+        offset = make_float2(signf(rx) * kAARadius, signf(ry) * kAARadius);
+        if (((flags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
+            ((flags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
+            cov.x = -cov.x;
+        if (pv.vertexType == FAN_MIDPOINT_VERTEX)
+            origin = midpoint;
+        if ((flags & RETROFIT_TRI_STRIP_CONTOUR_FLAG) && pv.vertexType != FAN_VERTEX)
+            o.discard = true;
+    }
+    if (P.wireframe)
+        cov = make_float2(1.f, -1.f);
+    float2 mo = mat_mul(M, origin);
+    o.pos = make_float2(__fadd_rn(__fadd_rn(mo.x, offset.x), translate.x),
+                        __fadd_rn(__fadd_rn(mo.y, offset.y), translate.y));
+    o.cov = cov;
+    o.pathID = pathID;
+    return true;
+}
+
+// E(p) = A * (p.x - ax) + B * (p.y - ay), evaluated identically by the binner
+// and the raster so their tile/pixel decisions agree.
+__device__ __forceinline__ float edge_eval(float4 e, float px, float py)
+{
+    return __fmaf_rn(e.z, __fsub_rn(px, e.x), __fmul_rn(e.w, __fsub_rn(py, e.y)));
+}
+
+__device__ __forceinline__ bool edge_inside(float4 e, float E)
+{
+    // Top-left tie rule for clockwise (y-down) triangles: edge direction
+    // (dx, dy) = (B, -A); inclusive when dy < 0, or dy == 0 and dx > 0.
+    return E > 0.f || (E == 0.f && (e.z > 0.f || (e.z == 0.f && e.w > 0.f)));
+}
+
+// Builds the oriented, canonically-anchored edge P->Q of a triangle.
+__device__ __forceinline__ float4 make_edge(float2 P, float2 Q)
+{
+    bool pFirst = P.y < Q.y || (P.y == Q.y && P.x < Q.x);
+    float2 a = pFirst ? P : Q, b = pFirst ? Q : P;
+    float A = -(b.y - a.y), B = b.x - a.x; // exact: snapped coordinates
+    if (!pFirst)
+    {
+        A = -A;
+        B = -B;
+    }
+    return make_float4(a.x, a.y, A, B);
+}
+
+struct TileRect
+{
+    int bx0, by0, bx1, by1; // pixel bbox, [b0, b1)
+};
+
+__device__ __forceinline__ bool tile_overlaps(const TriRecord& T, const TileRect& r, int tx, int ty)
+{
+    float xlo = (float)max(tx * kTileSize, r.bx0) + .5f;
+    float xhi = (float)(min(tx * kTileSize + kTileSize, r.bx1) - 1) + .5f;
+    float ylo = (float)max(ty * kTileSize, r.by0) + .5f;
+    float yhi = (float)(min(ty * kTileSize + kTileSize, r.by1) - 1) + .5f;
+    const float4 e[3] = {T.e0, T.e1, T.e2};
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        float x = e[k].z > 0.f ? xhi : xlo;
+        float y = e[k].w > 0.f ? yhi : ylo;
+        if (edge_eval(e[k], x, y) < 0.f)
+            return false;
+    }
+    return true;
+}
+
+// Snaps to the 1/256-pixel grid of the rasteriser.
+__device__ __forceinline__ float snap(float v) { return rintf(v * 256.f) * (1.f / 256.f); }
+} // namespace
+
+// Per patch instance (one warp): shade 42 vertices, assemble and set up 24
+// triangles, and count the tiles each one touches. Triangle slot order is
+// primitive order (batch, instance, triangle-in-patch).
+__global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
+                                                          uint32_t baseInstance,
+                                                          uint32_t instanceCount,
+                                                          uint32_t slotBase,
+                                                          uint32_t features,
+                                                          TriRecord* __restrict__ tris,
+                                                          uint32_t* __restrict__ tileCounts,
+                                                          int4* __restrict__ bboxes)
+{
+    __shared__ VertexOut sv[4][kPatchVertexCount];
+    __shared__ bool sok[4];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t local = blockIdx.x * 4 + w;
+    const bool active = local < instanceCount;
+    const uint32_t instance = baseInstance + local;
+    if (lane == 0)
+        sok[w] = true;
+    __syncwarp();
+    if (active)
+    {
+        for (int v = lane; v < kPatchVertexCount; v += 32)
+        {
+            VertexOut o;
+            if (!shade_patch_vertex(P, v, instance, o))
+            {
+                sok[w] = false;
+                o.discard = true;
+            }
+            sv[w][v] = o;
+        }
+    }
+    __syncwarp();
+    if (!active || lane >= kPatchTriangleCount)
+        return;
+    const uint32_t slot = slotBase + local * kPatchTriangleCount + lane;
+    int ia, ib, ic;
+    patch_triangle(lane, ia, ib, ic);
+    const VertexOut& A = sv[w][ia];
+    const VertexOut& B = sv[w][ib];
+    const VertexOut& C = sv[w][ic];
+    uint32_t count = 0;
+    int4 bb = make_int4(0, 0, 0, 0);
+    bool valid = sok[w] && !A.discard && !B.discard && !C.discard;
+    float2 p0, p1, p2;
+    if (valid)
+    {
+        p0 = make_float2(snap(A.pos.x), snap(A.pos.y));
+        p1 = make_float2(snap(B.pos.x), snap(B.pos.y));
+        p2 = make_float2(snap(C.pos.x), snap(C.pos.y));
+        float m = fmaxf(fmaxf(fmaxf(fabsf(p0.x), fabsf(p0.y)), fmaxf(fabsf(p1.x), fabsf(p1.y))),
+                        fmaxf(fabsf(p2.x), fabsf(p2.y)));
+        if (!(m < 32768.f)) // NaN or outside the exact snapping range
+        {
+            if (!(isnan(m)))
+                atomicOr(P.error, ERR_COORD_RANGE);
+            valid = false;
+        }
+    }
+    double area2 = 0.0;
+    if (valid)
+    {
+        // Exact: coordinates are multiples of 1/256 below 2^15.
+        double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
+        double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
+        area2 = d1x * d2y - d2x * d1y;
+        valid = area2 > 0.0; // counterclockwise culled, degenerate dropped
+    }
+    if (valid)
+    {
+        float minx = fminf(fminf(p0.x, p1.x), p2.x), maxx = fmaxf(fmaxf(p0.x, p1.x), p2.x);
+        float miny = fminf(fminf(p0.y, p1.y), p2.y), maxy = fmaxf(fmaxf(p0.y, p1.y), p2.y);
+        // Pixels whose centres k + 1/2 lie inside [min, max].
+        int bx0 = max((int)ceilf(minx - .5f), 0), bx1 = min((int)floorf(maxx - .5f) + 1, (int)P.width);
+        int by0 = max((int)ceilf(miny - .5f), 0), by1 = min((int)floorf(maxy - .5f) + 1, (int)P.height);
+        if (bx0 >= bx1 || by0 >= by1)
+            valid = false;
+        else
+            bb = make_int4(bx0, by0, bx1, by1);
+    }
+    if (valid)
+    {
+        TriRecord T;
+        T.e0 = make_edge(p0, p1);
+        T.e1 = make_edge(p1, p2);
+        T.e2 = make_edge(p2, p0);
+        double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
+        double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
+        double inv = 1.0 / area2;
+        double ax = (double)T.e0.x - p0.x, ay = (double)T.e0.y - p0.y;
+        {
+            double c0 = A.cov.x, c1 = B.cov.x, c2 = C.cov.x;
+            double gx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
+            double gy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
+            T.covx = make_float4((float)(c0 + gx * ax + gy * ay), (float)gx, (float)gy, 0.f);
+        }
+        {
+            double c0 = A.cov.y, c1 = B.cov.y, c2 = C.cov.y;
+            double gx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
+            double gy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
+            T.covy_c = (float)(c0 + gx * ax + gy * ay);
+            T.covy_gx = (float)gx;
+            T.covy_gy = (float)gy;
+        }
+        T.pathAndFeatures = (A.pathID & 0xffffu) | (features << 16);
+        tris[slot] = T;
+        TileRect r = {bb.x, bb.y, bb.z, bb.w};
+        for (int ty = bb.y >> kTileLog2; ty <= (bb.w - 1) >> kTileLog2; ++ty)
+            for (int tx = bb.x >> kTileLog2; tx <= (bb.z - 1) >> kTileLog2; ++tx)
+                count += tile_overlaps(T, r, tx, ty) ? 1u : 0u;
+        if (count == 0)
+            bb = make_int4(0, 0, 0, 0);
+    }
+    tileCounts[slot] = count;
+    bboxes[slot] = bb;
+}
+
+// Writes the (tile, slot) pairs of each triangle at its scanned offset, in
+// primitive order.
+__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
+                                                          uint32_t tilesX,
+                                                          const TriRecord* __restrict__ tris,
+                                                          const uint32_t* __restrict__ tileCounts,
+                                                          const uint32_t* __restrict__ offsets,
+                                                          const int4* __restrict__ bboxes,
+                                                          uint32_t* __restrict__ keys,
+                                                          uint32_t* __restrict__ vals)
+{
+    uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= slotCount || tileCounts[slot] == 0)
+        return;
+    const TriRecord T = tris[slot];
+    int4 bb = bboxes[slot];
+    TileRect r = {bb.x, bb.y, bb.z, bb.w};
+    uint32_t o = offsets[slot];
+    for (int ty = bb.y >> kTileLog2; ty <= (bb.w - 1) >> kTileLog2; ++ty)
+        for (int tx = bb.x >> kTileLog2; tx <= (bb.z - 1) >> kTileLog2; ++tx)
+            if (tile_overlaps(T, r, tx, ty))
+            {
+                keys[o] = (uint32_t)ty * tilesX + (uint32_t)tx;
+                vals[o] = slot;
+                ++o;
+            }
+}
+
+__global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
+                                                          const uint32_t* __restrict__ keys,
+                                                          uint2* __restrict__ ranges)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pairCount)
+        return;
+    uint32_t k = keys[i];
+    if (i == 0 || keys[i - 1] != k)
+        ranges[k].x = i;
+    if (i == pairCount - 1 || keys[i + 1] != k)
+        ranges[k].y = i + 1;
+}
+
+namespace
+{
+__device__ __forceinline__ uint16_t id_bits_to_f16(uint32_t idBits, uint32_t granularity)
+{
+    return idBits == 0 ? 0 : (uint16_t)((idBits + MAX_DENORM_F16) * granularity);
+}
+__device__ __forceinline__ float h2f(uint32_t bits)
+{
+    return __half2float(__ushort_as_half((unsigned short)bits));
+}
+__device__ __forceinline__ uint32_t f2h(float f)
+{
+    return (uint32_t)__half_as_ushort(__float2half_rn(f));
+}
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.f), 1.f); }
+__device__ __forceinline__ uint32_t unorm8(float x)
+{
+    return (uint32_t)__float2int_rn(clamp01(x) * 255.f);
+}
+__device__ __forceinline__ void unpack_rgba8(uint32_t c, float out[4])
+{
+    out[0] = (float)(c & 0xffu) / 255.f;
+    out[1] = (float)((c >> 8) & 0xffu) / 255.f;
+    out[2] = (float)((c >> 16) & 0xffu) / 255.f;
+    out[3] = (float)(c >> 24) / 255.f;
+}
+__device__ __forceinline__ uint32_t pack_rgba8(const float c[4])
+{
+    return unorm8(c[0]) | (unorm8(c[1]) << 8) | (unorm8(c[2]) << 16) | (unorm8(c[3]) << 24);
+}
+
+__device__ __forceinline__ float min3f(float a, float b, float c) { return fminf(fminf(a, b), c); }
+__device__ __forceinline__ float max3f(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+
+// advanced_blend.glsl:94-154
+__device__ void set_lum(const float base[3], const float lum[3], float out[3])
+{
+    float lumTarget = lum[0] * .30f + lum[1] * .59f + lum[2] * .11f;
+    float lb = base[0] * .30f + base[1] * .59f + base[2] * .11f;
+    float bi[3] = {base[0] - lb, base[1] - lb, base[2] - lb};
+    float sx = lumTarget / fmaxf(EPSILON_FP16_NON_DENORM, -min3f(bi[0], bi[1], bi[2]));
+    float sy = (1.f - lumTarget) / fmaxf(EPSILON_FP16_NON_DENORM, max3f(bi[0], bi[1], bi[2]));
+    float s = fminf(1.f, fminf(sx, sy));
+    for (int i = 0; i < 3; ++i)
+        out[i] = bi[i] * s + lumTarget;
+}
+__device__ void set_lum_sat(const float hue[3], const float sat[3], const float lum[3], float out[3])
+{
+    float satTarget = max3f(sat[0], sat[1], sat[2]) - min3f(sat[0], sat[1], sat[2]);
+    float mn = min3f(hue[0], hue[1], hue[2]);
+    float h[3] = {hue[0] - mn, hue[1] - mn, hue[2] - mn};
+    float scale = satTarget / fmaxf(EPSILON_FP16_NON_DENORM, max3f(h[0], h[1], h[2]));
+    float hs[3] = {h[0] * scale, h[1] * scale, h[2] * scale};
+    set_lum(hs, lum, out);
+}
+
+// advanced_color_blend (advanced_blend.glsl:156-327): src unmultiplied,
+// dst premultiplied; returns mix(src, coeffs, dst.a).
+__device__ void advanced_blend(float src[3], const float dp[4], uint32_t mode)
+{
+    float inv = dp[3] != 0.f ? 1.f / dp[3] : 0.f;
+    float dst[3] = {dp[0] * inv, dp[1] * inv, dp[2] * inv};
+    float co[3];
+    switch (mode)
+    {
+        case 11: // multiply
+            for (int i = 0; i < 3; ++i) co[i] = src[i] * dst[i];
+            break;
+        case 1: // screen
+            for (int i = 0; i < 3; ++i) co[i] = src[i] + dst[i] - src[i] * dst[i];
+            break;
+        case 2: // overlay
+            for (int i = 0; i < 3; ++i)
+            {
+                float sd = src[i] * dst[i];
+                co[i] = 2.f * (dst[i] > .5f ? src[i] + dst[i] - sd - .5f : sd);
+            }
+            break;
+        case 3: // darken
+            for (int i = 0; i < 3; ++i) co[i] = fminf(src[i], dst[i]);
+            break;
+        case 4: // lighten
+            for (int i = 0; i < 3; ++i) co[i] = fmaxf(src[i], dst[i]);
+            break;
+        case 5: // colordodge
+            for (int i = 0; i < 3; ++i)
+            {
+                float d = fminf(fmaxf(dp[i], 0.f), dp[3]);
+                float denom = clamp01(1.f - src[i]) * dp[3];
+                co[i] = denom == 0.f ? signf(d) : fminf(1.f, d / denom);
+            }
+            break;
+        case 6: // colorburn
+        {
+            float a = dp[3] == 0.f ? 1.f : dp[3];
+            for (int i = 0; i < 3; ++i)
+            {
+                float s = clamp01(src[i]);
+                float d = fminf(fmaxf(dp[i], 0.f), dp[3]);
+                float numer = a - d;
+                co[i] = 1.f - (s == 0.f ? signf(numer) : fminf(1.f, numer / (s * a)));
+            }
+            break;
+        }
+        case 7: // hardlight
+            for (int i = 0; i < 3; ++i)
+            {
+                float sd = src[i] * dst[i];
+                co[i] = 2.f * (src[i] > .5f ? src[i] + dst[i] - sd - .5f : sd);
+            }
+            break;
+        case 8: // softlight
+            for (int i = 0; i < 3; ++i)
+            {
+                float c;
+                if (src[i] <= .5f)
+                    c = 1.f - dst[i];
+                else if (dst[i] <= .25f)
+                    c = (16.f * dst[i] - 12.f) * dst[i] + 3.f;
+                else
+                    c = rsqrtf(dst[i]) - 1.f;
+                co[i] = dst[i] + dst[i] * (2.f * src[i] - 1.f) * c;
+            }
+            break;
+        case 9: // difference
+            for (int i = 0; i < 3; ++i) co[i] = fabsf(dst[i] - src[i]);
+            break;
+        case 10: // exclusion
+            for (int i = 0; i < 3; ++i) co[i] = src[i] + dst[i] - 2.f * src[i] * dst[i];
+            break;
+        case 12: case 13: case 14: case 15:
+        {
+            float s[3] = {clamp01(src[0]), clamp01(src[1]), clamp01(src[2])};
+            if (mode == 12) set_lum_sat(s, dst, dst, co);
+            else if (mode == 13) set_lum_sat(dst, s, dst, co);
+            else if (mode == 14) set_lum(s, dst, co);
+            else set_lum(dst, s, co);
+            break;
+        }
+        default:
+            co[0] = src[0]; co[1] = src[1]; co[2] = src[2];
+            break;
+    }
+    float a = dp[3];
+    for (int i = 0; i < 3; ++i)
+        src[i] = src[i] * (1.f - a) + co[i] * a;
+}
+
+__device__ __forceinline__ void sample_grad(const FlushParams& P, float u, float v, float out[4])
+{
+    float fx = u * kGradTextureWidth - .5f;
+    float fy = v * (float)P.gradDataHeight - .5f;
+    float x0f = floorf(fx), y0f = floorf(fy);
+    float ax = fx - x0f, ay = fy - y0f;
+    int x0 = (int)x0f, y0 = (int)y0f;
+    out[0] = out[1] = out[2] = out[3] = 0.f;
+    // The gradient texture always has at least one row allocated.
+    const int H = max((int)P.gradDataHeight, 1);
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+        {
+            int xi = min(max(x0 + i, 0), kGradTextureWidth - 1);
+            int yj = min(max(y0 + j, 0), H - 1);
+            float wgt = (i ? ax : 1.f - ax) * (j ? ay : 1.f - ay);
+            uchar4 t = P.grad[(size_t)yj * kGradTextureWidth + xi];
+            out[0] += wgt * ((float)t.x / 255.f);
+            out[1] += wgt * ((float)t.y / 255.f);
+            out[2] += wgt * ((float)t.z / 255.f);
+            out[3] += wgt * ((float)t.w / 255.f);
+        }
+}
+
+struct Pls
+{
+    uint32_t color;    // RGBA8
+    uint32_t clip;     // packHalf2x16(coverage, clipID)
+    uint32_t scratch;  // RGBA8
+    uint32_t coverage; // packHalf2x16(coverageCount, pathID)
+};
+
+// One fragment of draw_raster_order_path.frag for pixel centre (fx, fy).
+__device__ void fragment(const FlushParams& P,
+                         uint32_t pathID,
+                         uint32_t features,
+                         float covx,
+                         float covy,
+                         float fx,
+                         float fy,
+                         float dither,
+                         Pls& s)
+{
+    const uint2 paint = P.paints[P.firstPaint + pathID];
+    uint32_t vPathID = id_bits_to_f16(pathID, P.pathIDGranularity);
+    const bool evenOdd = (paint.x & PAINT_FLAG_EVEN_ODD_FILL) != 0;
+    if (evenOdd)
+        vPathID ^= 0x8000u;
+    const uint32_t paintType = paint.x & 0xfu;
+
+    const uint32_t covBufferID = s.coverage >> 16;
+    float count = covBufferID == vPathID ? h2f(s.coverage & 0xffffu) : 0.f;
+    if (covy >= 0.f)
+        count = fmaxf(fminf(covx, covy), count); // stroke
+    else
+        count = count + covx; // fill
+    uint32_t stored = f2h(count);
+    s.coverage = (vPathID << 16) | stored;
+    count = h2f(stored);
+
+    float coverage = fabsf(count);
+    if ((features & SF_EVEN_ODD) && evenOdd)
+        coverage = 1.f - fabsf((coverage * .5f - floorf(coverage * .5f)) * 2.f + -1.f);
+    coverage = fminf(coverage, 1.f);
+
+    if (features & SF_CLIPPING)
+    {
+        const uint32_t clipBits = id_bits_to_f16(
+            (paintType == CLIP_UPDATE_PAINT_TYPE ? paint.y : paint.x) >> 16,
+            P.pathIDGranularity);
+        if (paintType == CLIP_UPDATE_PAINT_TYPE && clipBits != 0)
+        {
+            // Clip update: write coverage into the clip plane.
+            if (features & SF_NESTED_CLIPPING)
+            {
+                uint32_t outerBits = id_bits_to_f16(paint.x >> 16, P.pathIDGranularity);
+                if (outerBits != 0)
+                {
+                    uint32_t contentID = s.clip >> 16;
+                    float outer;
+                    if (contentID != clipBits)
+                    {
+                        outer = contentID == outerBits ? h2f(s.clip & 0xffffu) : 0.f;
+                        s.scratch = unorm8(outer);
+                    }
+                    else
+                    {
+                        outer = (float)(s.scratch & 0xffu) / 255.f;
+                    }
+                    coverage = fminf(coverage, outer);
+                }
+            }
+            s.clip = (clipBits << 16) | f2h(coverage);
+            return;
+        }
+        if (clipBits != 0)
+        {
+            coverage = (s.clip >> 16) == clipBits ? fminf(h2f(s.clip & 0xffffu), coverage) : 0.f;
+        }
+    }
+    if (features & SF_CLIP_RECT)
+    {
+        const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+        float4 cm = aux[2], ct = aux[3];
+        float awx = fabsf(cm.x) + fabsf(cm.z), awy = fabsf(cm.y) + fabsf(cm.w);
+        float d0, d1, d2, d3;
+        if (awx != 0.f && awy != 0.f)
+        {
+            float rx = 1.f / awx, ry = 1.f / awy;
+            float cx = cm.x * fx + cm.z * fy + ct.x;
+            float cy = cm.y * fx + cm.w * fy + ct.y;
+            d0 = cx * rx + rx + .5f;
+            d1 = cy * ry + ry + .5f;
+            d2 = -cx * rx + rx + .5f;
+            d3 = -cy * ry + ry + .5f;
+        }
+        else
+        {
+            d0 = d2 = ct.x;
+            d1 = d3 = ct.y;
+        }
+        float m = fminf(fminf(d0, d1), fminf(d2, d3));
+        coverage = fminf(fmaxf(m, 0.f), coverage);
+    }
+
+    const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
+    float color[4];
+    if (paintType == SOLID_COLOR_PAINT_TYPE)
+    {
+        unpack_rgba8(paint.y, color);
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+            for (int k = 0; k < 4; ++k)
+                color[k] *= coverage;
+        }
+        else
+            color[3] *= coverage;
+    }
+    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE || paintType == RADIAL_GRADIENT_PAINT_TYPE)
+    {
+        const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+        float4 pm = aux[0], pt = aux[1];
+        float pcx = pm.x * fx + pm.z * fy + pt.x;
+        float pcy = pm.y * fx + pm.w * fy + pt.y;
+        float spanB = pt.z > .9f ? 2.f : pt.w;
+        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pcx : sqrtf(pcx * pcx + pcy * pcy);
+        t = clamp01(t);
+        float x = spanB > 1.f ? (1.f - 1.f / kGradTextureWidth) * t + (.5f / kGradTextureWidth)
+                              : (1.f / kGradTextureWidth) * t + spanB;
+        sample_grad(P, x, __uint_as_float(paint.y), color);
+        color[3] *= coverage;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+        }
+    }
+    else
+    {
+        color[0] = color[1] = color[2] = color[3] = 0.f;
+    }
+
+    float dst[4];
+    if (covBufferID != vPathID)
+    {
+        unpack_rgba8(s.color, dst);
+        s.scratch = s.color;
+    }
+    else
+    {
+        unpack_rgba8(s.scratch, dst);
+    }
+    if (unmultiplied)
+    {
+        uint32_t mode = (paint.x >> 4) & 0xfu;
+        if (mode != 0 && (mode < 12 || (features & SF_HSL_BLEND_MODES)))
+            advanced_blend(color, dst, mode);
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    const float paintAlpha = color[3];
+    for (int k = 0; k < 4; ++k)
+        color[k] += dst[k] * (1.f - paintAlpha);
+    if ((features & SF_DITHER) && paintAlpha != 0.f)
+    {
+        color[0] += dither;
+        color[1] += dither;
+        color[2] += dither;
+    }
+    s.color = pack_rgba8(color);
+}
+} // namespace
+
+// One 256-thread CTA per 16x16 tile; thread = pixel; PLS planes in registers.
+__global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
+                                                          uint32_t tilesX,
+                                                          const TriRecord* __restrict__ tris,
+                                                          const uint32_t* __restrict__ sortedSlots,
+                                                          const uint2* __restrict__ ranges,
+                                                          uint32_t* __restrict__ fb)
+{
+    __shared__ TriRecord sTris[256];
+    const uint32_t tile = blockIdx.x;
+    const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
+    const int px = tx * kTileSize + (threadIdx.x & (kTileSize - 1));
+    const int py = ty * kTileSize + (threadIdx.x >> kTileLog2);
+    const bool inBounds = px < (int)P.width && py < (int)P.height;
+    const uint2 range = ranges[tile];
+    if (range.y <= range.x && !P.loadClear)
+        return;
+    Pls s;
+    s.color = P.loadClear ? P.clearColorPremulRGBA
+                          : (inBounds ? fb[(size_t)py * P.width + px] : 0u);
+    s.clip = 0;
+    s.scratch = 0;
+    s.coverage = 0;
+    const float fx = (float)px + .5f, fy = (float)py + .5f;
+    // common.glsl:269-274 interleaved gradient noise (depends on the pixel only).
+    float v1 = 0.06711056f * fx + 0.00583715f * fy;
+    v1 = v1 - floorf(v1);
+    float v2 = 52.9829189f * v1;
+    v2 = v2 - floorf(v2);
+    const float dither = v2 * P.ditherScale + P.ditherBias;
+
+    for (uint32_t base = range.x; base < range.y; base += 256)
+    {
+        const uint32_t k = base + threadIdx.x;
+        if (k < range.y)
+            sTris[threadIdx.x] = tris[sortedSlots[k]];
+        __syncthreads();
+        const uint32_t n = min(256u, range.y - base);
+        if (inBounds)
+        {
+            for (uint32_t i = 0; i < n; ++i)
+            {
+                const TriRecord& T = sTris[i];
+                float E0 = edge_eval(T.e0, fx, fy);
+                float E1 = edge_eval(T.e1, fx, fy);
+                float E2 = edge_eval(T.e2, fx, fy);
+                if (!(edge_inside(T.e0, E0) && edge_inside(T.e1, E1) && edge_inside(T.e2, E2)))
+                    continue;
+                float dx = fx - T.e0.x, dy = fy - T.e0.y;
+                float covx = T.covx.x + T.covx.y * dx + T.covx.z * dy;
+                float covy = T.covy_c + T.covy_gx * dx + T.covy_gy * dy;
+                fragment(P, T.pathAndFeatures & 0xffffu, T.pathAndFeatures >> 16,
+                         covx, covy, fx, fy, dither, s);
+            }
+        }
+        __syncthreads();
+    }
+    if (inBounds)
+        fb[(size_t)py * P.width + px] = s.color;
+}
+} // namespace rivecuda

@@ -1,0 +1,433 @@
+// Color-ramp and tessellation kernels (GPU passes 1 and 2 of a rasterOrdering
+// flush).
+//
+//  * color_ramp_kernel restates renderer/src/shaders/color_ramp.glsl:40-107:
+//    each GradientSpan paints a 1-texel-tall strip of the 512-wide RGBA8
+//    gradient texture: a solid left border, a linear ramp between x0 and x1,
+//    and a solid right border.
+//  * tessellate_kernel restates renderer/src/shaders/tessellate.glsl:61-567:
+//    each TessVertexSpan covers [x0, x1) (and optionally a mirrored range) of
+//    one row of the 2048-wide tessellation texture; every texel is one
+//    tessellated vertex (x, y, theta, contourIDWithFlags).
+//
+// GB300 mapping: one warp per span; the per-span set-up (tangents, polar step,
+// join step) is evaluated once per lane without divergence, then lanes stride
+// across the span's texels so each warp-wide store is 32 consecutive 16-byte
+// texels (512 B, fully coalesced). The texture is plain linear HBM memory
+// (row-major, 2048 texels per row), so the draw kernels read it with ordinary
+// 128-bit loads.
+#include "rive_cuda_internal.cuh"
+
+namespace rivecuda
+{
+namespace
+{
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
+{
+    return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 f2add(float2 a, float2 b)
+{
+    return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 f2scale(float2 a, float s)
+{
+    return make_float2(__fmul_rn(a.x, s), __fmul_rn(a.y, s));
+}
+__device__ __forceinline__ float f2dot(float2 a, float2 b)
+{
+    return __fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+__device__ __forceinline__ float f2cross(float2 a, float2 b)
+{
+    return __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(b.x, a.y));
+}
+__device__ __forceinline__ bool f2ne(float2 a, float2 b)
+{
+    return a.x != b.x || a.y != b.y;
+}
+__device__ __forceinline__ float2 f2normalize(float2 v)
+{
+    float inv = __fdiv_rn(1.f, __fsqrt_rn(f2dot(v, v)));
+    return f2scale(v, inv);
+}
+// (b - a) * t + a
+__device__ __forceinline__ float2 f2lerp(float2 a, float2 b, float t)
+{
+    return f2add(f2scale(f2sub(b, a), t), a);
+}
+
+// bezier_utils.glsl:24-32
+__device__ __forceinline__ float cos_between(float2 a, float2 b)
+{
+    float ab = f2dot(a, b);
+    float p = __fmul_rn(f2dot(a, a), f2dot(b, b));
+    if (p == 0.f)
+        return 1.f;
+    return fminf(fmaxf(__fmul_rn(ab, __fdiv_rn(1.f, __fsqrt_rn(p))), -1.f), 1.f);
+}
+
+// bezier_utils.glsl:65-71
+__device__ __forceinline__ void cubic_tangents(float2 p0,
+                                               float2 p1,
+                                               float2 p2,
+                                               float2 p3,
+                                               float2& t0,
+                                               float2& t1)
+{
+    t0 = f2sub(f2ne(p0, p1) ? p1 : (f2ne(p1, p2) ? p2 : p3), p0);
+    t1 = f2sub(p3, f2ne(p3, p2) ? p2 : (f2ne(p2, p1) ? p1 : p0));
+}
+
+// common.glsl atan2(): acos of the normalized x, signed by y.
+__device__ __forceinline__ float rive_atan2(float2 v)
+{
+    v = f2normalize(v);
+    float theta = acosf(fminf(fmaxf(v.x, -1.f), 1.f));
+    return v.y >= 0.f ? theta : -theta;
+}
+
+struct SpanSetup
+{
+    float2 p0, p1, p2, p3;
+    float2 joinTangent;
+    float totalVertexCount;
+    float parametricSegmentCount;
+    float joinSegmentCount;
+    float radsPerPolarSegment;
+    float radsPerJoinSegment;
+    uint32_t contourIDWithFlags; // without the mirrored flag
+    bool valid;
+};
+
+// Per-span half of tessellate.glsl (the vertex shader, 61-287).
+__device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
+{
+    SpanSetup s;
+    uint4 q0 = sp[0], q1 = sp[1], q2 = sp[2], q3 = sp[3];
+    s.p0 = make_float2(__uint_as_float(q0.x), __uint_as_float(q0.y));
+    s.p1 = make_float2(__uint_as_float(q0.z), __uint_as_float(q0.w));
+    s.p2 = make_float2(__uint_as_float(q1.x), __uint_as_float(q1.y));
+    s.p3 = make_float2(__uint_as_float(q1.z), __uint_as_float(q1.w));
+    s.joinTangent = make_float2(__uint_as_float(q2.x), __uint_as_float(q2.y));
+    uint32_t counts = q3.z;
+    uint32_t parametric = counts & 0x3ffu;
+    uint32_t polar = (counts >> 10) & 0x3ffu;
+    uint32_t join = counts >> 20;
+    uint32_t flags = q3.w;
+    uint32_t contourID = flags & CONTOUR_ID_MASK;
+    s.valid = true;
+    uint32_t pathID = 0;
+    if (contourID > 0)
+    {
+        if (contourID > P.contourCount)
+        {
+            atomicOr(P.error, ERR_BAD_CONTOUR);
+            s.valid = false;
+            return s;
+        }
+        pathID = P.contours[P.firstContour + contourID - 1].z;
+    }
+    float strokeRadius = 0.f, featherRadius = 0.f;
+    uint4 pathRow0 = make_uint4(0, 0, 0, 0);
+    if (pathID != 0)
+    {
+        if (pathID >= P.pathCount)
+        {
+            atomicOr(P.error, ERR_BAD_PATH);
+            s.valid = false;
+            return s;
+        }
+        const uint4* path = P.paths + 4 * (size_t)(P.firstPath + pathID);
+        uint4 row1 = path[1];
+        pathRow0 = path[0];
+        strokeRadius = __uint_as_float(row1.z);
+        featherRadius = __uint_as_float(row1.w);
+    }
+    if (featherRadius != 0.f && strokeRadius == 0.f)
+    {
+        atomicOr(P.error, ERR_FEATHER);
+        s.valid = false;
+        return s;
+    }
+    if (flags & CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG)
+    {
+        float m0 = __uint_as_float(pathRow0.x), m1 = __uint_as_float(pathRow0.y);
+        float m2 = __uint_as_float(pathRow0.z), m3 = __uint_as_float(pathRow0.w);
+        float2 a = f2add(f2add(f2scale(s.p1, -2.f), s.p2), s.p0);
+        float2 c = f2add(f2add(f2scale(s.p2, -2.f), s.p3), s.p1);
+        float2 d0 = make_float2(__fadd_rn(__fmul_rn(m0, a.x), __fmul_rn(m2, a.y)),
+                                __fadd_rn(__fmul_rn(m1, a.x), __fmul_rn(m3, a.y)));
+        float2 d1 = make_float2(__fadd_rn(__fmul_rn(m0, c.x), __fmul_rn(m2, c.y)),
+                                __fadd_rn(__fmul_rn(m1, c.x), __fmul_rn(m3, c.y)));
+        float m = fmaxf(f2dot(d0, d0), f2dot(d1, d1));
+        float n = fmaxf(ceilf(__fsqrt_rn(__fmul_rn(.75f * 4.f, __fsqrt_rn(m)))), 1.f);
+        uint32_t un = (uint32_t)n;
+        parametric = min(un, parametric);
+    }
+    uint32_t total = parametric + polar + join - 1u;
+    float2 t0, t1;
+    cubic_tangents(s.p0, s.p1, s.p2, s.p3, t0, t1);
+    float theta = acosf(cos_between(t0, t1));
+    float rpp = __fdiv_rn(theta, (float)polar);
+    float turn = f2cross(f2sub(s.p2, s.p0), f2sub(s.p3, s.p1));
+    if (turn == 0.f)
+        turn = f2cross(t0, t1);
+    if (turn < 0.f)
+        rpp = -rpp;
+    s.totalVertexCount = (float)total;
+    s.parametricSegmentCount = (float)parametric;
+    s.joinSegmentCount = (float)join;
+    s.radsPerPolarSegment = rpp;
+    s.radsPerJoinSegment = 0.f;
+    if (join > 1u)
+    {
+        float joinTheta = acosf(cos_between(t1, s.joinTangent));
+        float joinSpan = (float)join;
+        if ((flags & (JOIN_TYPE_MASK | EMULATED_STROKE_CAP_CONTOUR_FLAG)) ==
+            (ROUND_JOIN_CONTOUR_FLAG | EMULATED_STROKE_CAP_CONTOUR_FLAG))
+            joinSpan = __fsub_rn(joinSpan, 2.f);
+        float rpj = __fdiv_rn(joinTheta, joinSpan);
+        if (f2cross(t1, s.joinTangent) < 0.f)
+            rpj = -rpj;
+        s.radsPerJoinSegment = rpj;
+    }
+    s.contourIDWithFlags = flags;
+    return s;
+}
+
+// Per-texel half of tessellate.glsl (the fragment shader, 294-567).
+__device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flagsIn)
+{
+    float2 p0 = s.p0, p1 = s.p1, p2 = s.p2, p3 = s.p3;
+    float2 tan0, tan1;
+    cubic_tangents(p0, p1, p2, p3, tan0, tan1);
+    float vertexIdx = fmaxf(floorf(vertexIdxF), 0.f);
+    float parametricSegmentCount = s.parametricSegmentCount;
+    float radsPerPolarSegment = s.radsPerPolarSegment;
+    uint32_t flags = flagsIn;
+    float mergedSegmentCount = __fsub_rn(s.totalVertexCount, s.joinSegmentCount);
+    float mergedVertexID = vertexIdx;
+    if (mergedVertexID <= mergedSegmentCount)
+    {
+        flags &= ~JOIN_TYPE_MASK;
+    }
+    else
+    {
+        p0 = p1 = p2 = p3;
+        tan0 = tan1;
+        tan1 = s.joinTangent;
+        parametricSegmentCount = 1.f;
+        mergedVertexID = __fsub_rn(mergedVertexID, mergedSegmentCount);
+        mergedSegmentCount = s.joinSegmentCount;
+        radsPerPolarSegment = s.radsPerJoinSegment;
+        if ((flags & JOIN_TYPE_MASK) > ROUND_JOIN_CONTOUR_FLAG)
+        {
+            if (mergedVertexID < 2.5f)
+                flags |= JOIN_TANGENT_0_CONTOUR_FLAG;
+            if (mergedVertexID > 1.5f && mergedVertexID < 3.5f)
+                flags |= JOIN_TANGENT_INNER_CONTOUR_FLAG;
+        }
+        else if ((flags & EMULATED_STROKE_CAP_CONTOUR_FLAG) ||
+                 (flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG)
+        {
+            mergedSegmentCount = __fsub_rn(mergedSegmentCount, 2.f);
+            mergedVertexID = __fsub_rn(mergedVertexID, 1.f);
+        }
+        flags |= radsPerPolarSegment < 0.f ? LEFT_JOIN_CONTOUR_FLAG
+                                           : RIGHT_JOIN_CONTOUR_FLAG;
+    }
+
+    float2 coord;
+    float theta = 0.f;
+    if (mergedVertexID == 0.f || mergedVertexID == mergedSegmentCount ||
+        (flags & JOIN_TYPE_MASK) > ROUND_JOIN_CONTOUR_FLAG)
+    {
+        bool isTan0 = mergedVertexID < __fmul_rn(mergedSegmentCount, .5f);
+        coord = isTan0 ? p0 : p3;
+        theta = rive_atan2(isTan0 ? tan0 : tan1);
+    }
+    else if (flags & RETROFIT_TRI_STRIP_CONTOUR_FLAG)
+    {
+        coord = p0;
+        if (mergedVertexID >= 8.f)
+            coord = p1;
+        if (mergedVertexID >= 12.f)
+            coord = p2;
+        if (mergedVertexID >= 14.f)
+            coord = s.joinTangent;
+    }
+    else
+    {
+        float T, polarT;
+        if (parametricSegmentCount == mergedSegmentCount)
+        {
+            T = __fdiv_rn(mergedVertexID, parametricSegmentCount);
+            polarT = 0.f;
+        }
+        else
+        {
+            float2 C = f2sub(p1, p0);
+            float2 D = f2sub(p3, p0);
+            float2 E = f2sub(p2, p1);
+            float2 B = f2sub(E, C);
+            float2 A = f2add(f2scale(E, -3.f), D);
+            float2 B_ = f2scale(B, __fmul_rn(parametricSegmentCount, 2.f));
+            float2 C_ = f2scale(C, __fmul_rn(parametricSegmentCount, parametricSegmentCount));
+            float lastParametricID = 0.f;
+            float maxParametricID =
+                fminf(__fsub_rn(parametricSegmentCount, 1.f), mergedVertexID);
+            float2 tan0norm = f2normalize(tan0);
+            float absRads = fabsf(radsPerPolarSegment);
+            float maxRotation0 = __fmul_rn(__fadd_rn(1.f, mergedVertexID), absRads);
+#pragma unroll
+            for (int p = 9; p >= 0; --p)
+            {
+                float testID = __fadd_rn(lastParametricID, (float)(1 << p));
+                if (testID <= maxParametricID)
+                {
+                    float2 testTan = f2add(f2scale(A, testID), B_);
+                    testTan = f2add(f2scale(testTan, testID), C_);
+                    float cosRotation = f2dot(f2normalize(testTan), tan0norm);
+                    float maxRotation =
+                        __fadd_rn(__fmul_rn(testID, -absRads), maxRotation0);
+                    maxRotation = fminf(maxRotation, kPi);
+                    if (cosRotation >= cosf(maxRotation))
+                        lastParametricID = testID;
+                }
+            }
+            float parametricT = __fdiv_rn(lastParametricID, parametricSegmentCount);
+            float lastPolarID = __fsub_rn(mergedVertexID, lastParametricID);
+            float theta0 = acosf(fminf(fmaxf(tan0norm.x, -1.f), 1.f));
+            theta0 = tan0norm.y >= 0.f ? theta0 : -theta0;
+            theta = __fadd_rn(__fmul_rn(lastPolarID, radsPerPolarSegment), theta0);
+            float sn, cs;
+            sincosf(theta, &sn, &cs);
+            float2 norm = make_float2(sn, -cs);
+            float a = f2dot(norm, A), bHalf = f2dot(norm, B), c = f2dot(norm, C);
+            float disc = fmaxf(__fsub_rn(__fmul_rn(bHalf, bHalf), __fmul_rn(a, c)), 0.f);
+            float q = __fsqrt_rn(disc);
+            if (bHalf > 0.f)
+                q = -q;
+            q = __fsub_rn(q, bHalf);
+            float qa5 = __fmul_rn(__fmul_rn(-.5f, q), a);
+            float rs, rt;
+            if (fabsf(__fadd_rn(__fmul_rn(q, q), qa5)) < fabsf(__fadd_rn(__fmul_rn(a, c), qa5)))
+            {
+                rs = q;
+                rt = a;
+            }
+            else
+            {
+                rs = c;
+                rt = q;
+            }
+            polarT = (rt != 0.f) ? __fdiv_rn(rs, rt) : 0.f;
+            polarT = fminf(fmaxf(polarT, 0.f), 1.f);
+            if (lastPolarID == 0.f)
+                polarT = 0.f;
+            T = fmaxf(parametricT, polarT);
+        }
+        float2 ab = f2lerp(p0, p1, T);
+        float2 bc = f2lerp(p1, p2, T);
+        float2 cd = f2lerp(p2, p3, T);
+        float2 abc = f2lerp(ab, bc, T);
+        float2 bcd = f2lerp(bc, cd, T);
+        coord = f2lerp(abc, bcd, T);
+        if (T != polarT)
+            theta = rive_atan2(f2sub(bcd, abc));
+    }
+    // GLSL mod(theta, 2pi) = theta - 2pi * floor(theta / 2pi)
+    float m = __fsub_rn(theta, __fmul_rn(k2Pi, floorf(__fdiv_rn(theta, k2Pi))));
+    return make_uint4(__float_as_uint(coord.x), __float_as_uint(coord.y),
+                      __float_as_uint(m), flags);
+}
+} // namespace
+
+// One block of 128 threads per GradientSpan; each thread owns 4 of the 512
+// texel columns.
+__global__ void __launch_bounds__(128) color_ramp_kernel(FlushParams P)
+{
+    const uint32_t s = blockIdx.x;
+    if (s >= P.gradSpanCount)
+        return;
+    uint4 sp = P.gradSpans[P.firstGradSpan + s];
+    uint32_t y = sp.y & ~GRAD_SPAN_FLAGS_MASK;
+    if (y >= P.gradDataHeight)
+        return;
+    float x0 = (float)(sp.x & 0xffffu) * (1.f / 65536.f);
+    float x1 = (float)(sp.x >> 16) * (1.f / 65536.f);
+    float cx0 = x0, cx3 = x1;
+    if (sp.y & GRAD_SPAN_FLAG_LEFT_BORDER)
+        cx0 = (sp.y & GRAD_SPAN_FLAG_COMPLEX_BORDER) ? 0.f : x0 - 1.f / kGradTextureWidth;
+    if (sp.y & GRAD_SPAN_FLAG_RIGHT_BORDER)
+        cx3 = (sp.y & GRAD_SPAN_FLAG_COMPLEX_BORDER) ? 1.f : x1 + 1.f / kGradTextureWidth;
+    // Quad edges in texel units (exact: the texture width is a power of two).
+    float e0 = cx0 * kGradTextureWidth, e1 = x0 * kGradTextureWidth;
+    float e2 = x1 * kGradTextureWidth, e3 = cx3 * kGradTextureWidth;
+    float c0[4] = {(float)((sp.z >> 16) & 0xffu) / 255.f, (float)((sp.z >> 8) & 0xffu) / 255.f,
+                   (float)(sp.z & 0xffu) / 255.f, (float)(sp.z >> 24) / 255.f};
+    float c1[4] = {(float)((sp.w >> 16) & 0xffu) / 255.f, (float)((sp.w >> 8) & 0xffu) / 255.f,
+                   (float)(sp.w & 0xffu) / 255.f, (float)(sp.w >> 24) / 255.f};
+    uchar4* row = P.grad + (size_t)y * kGradTextureWidth;
+    for (int i = threadIdx.x; i < kGradTextureWidth; i += blockDim.x)
+    {
+        float pc = (float)i + .5f;
+        float t;
+        if (pc >= e0 && pc < e1)
+            t = 0.f;
+        else if (pc >= e1 && pc < e2)
+            t = (pc - e1) / (e2 - e1);
+        else if (pc >= e2 && pc < e3)
+            t = 1.f;
+        else
+            continue;
+        float v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            float x = t == 0.f ? c0[k] : (t == 1.f ? c1[k] : c0[k] + (c1[k] - c0[k]) * t);
+            v[k] = fminf(fmaxf(x, 0.f), 1.f);
+        }
+        row[i] = make_uchar4((unsigned char)__float2int_rn(v[0] * 255.f),
+                             (unsigned char)__float2int_rn(v[1] * 255.f),
+                             (unsigned char)__float2int_rn(v[2] * 255.f),
+                             (unsigned char)__float2int_rn(v[3] * 255.f));
+    }
+}
+
+// One warp per TessVertexSpan (both its forward and mirrored rectangles).
+__global__ void __launch_bounds__(256) tessellate_kernel(FlushParams P)
+{
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= P.tessSpanCount)
+        return;
+    const uint4* sp = P.tessSpans + 4 * (size_t)(P.firstTessSpan + warp);
+    SpanSetup s = span_setup(P, sp);
+    if (!s.valid)
+        return;
+    uint4 q2 = sp[2], q3 = sp[3];
+    for (int second = 0; second < 2; ++second)
+    {
+        float y = __uint_as_float(second ? q2.w : q2.z);
+        int32_t x0x1 = (int32_t)(second ? q3.y : q3.x);
+        int x0 = (int32_t)((uint32_t)x0x1 << 16) >> 16;
+        int x1 = x0x1 >> 16;
+        if (isnan(y) || x0 == x1 || y < 0.f || y >= (float)P.tessDataHeight)
+            continue;
+        int rowIdx = (int)y;
+        int lo = max(min(x0, x1), 0), hi = min(max(x0, x1), kTessTextureWidth);
+        uint32_t flags = s.contourIDWithFlags;
+        if (x1 < x0)
+            flags |= MIRRORED_CONTOUR_CONTOUR_FLAG;
+        uint4* row = P.tess + (size_t)rowIdx * kTessTextureWidth;
+        for (int px = lo + lane; px < hi; px += 32)
+        {
+            float vertexIdx = __fsub_rn(s.totalVertexCount,
+                                        fabsf(__fsub_rn((float)x1, __fadd_rn((float)px, .5f))));
+            row[px] = tess_vertex(s, vertexIdx, flags);
+        }
+    }
+}
+} // namespace rivecuda

@@ -1,0 +1,127 @@
+// Internal definitions shared by the sm_103a kernels of the flush backend.
+//
+// Record layouts are the reference's GPU records (renderer/include/rive/
+// renderer/gpu.hpp): TessVertexSpan (291-376), GradientSpan (248-271),
+// PathData (1593-1619), PaintData (1627-1653), PaintAuxData (1660-1691),
+// ContourData (1698-1716), FlushUniforms (1466-1537). Flag values are those of
+// renderer/src/shaders/constants.glsl.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rivecuda
+{
+constexpr int kTessTextureWidth = 2048;
+constexpr int kTessTextureWidthLog2 = 11;
+constexpr int kGradTextureWidth = 512;
+constexpr int kPatchSegmentSpan = 8;   // kMidpointFanPatchSegmentSpan
+constexpr int kPatchVertexCount = 42;  // kMidpointFanPatchVertexCount
+constexpr int kPatchIndexCount = 72;   // kMidpointFanPatchIndexCount
+constexpr int kPatchTriangleCount = 24;
+
+constexpr float kPi = 3.14159265359f;
+constexpr float k2Pi = 6.28318530718f;
+constexpr float kAARadius = .5f;
+
+constexpr uint32_t GRAD_SPAN_FLAG_LEFT_BORDER = 0x80000000u;
+constexpr uint32_t GRAD_SPAN_FLAG_RIGHT_BORDER = 0x40000000u;
+constexpr uint32_t GRAD_SPAN_FLAG_COMPLEX_BORDER = 0x20000000u;
+constexpr uint32_t GRAD_SPAN_FLAGS_MASK = 0xe0000000u;
+
+constexpr uint32_t RETROFIT_TRI_STRIP_CONTOUR_FLAG = 1u << 31;
+constexpr uint32_t CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG = 1u << 29;
+constexpr uint32_t JOIN_TYPE_MASK = 7u << 26;
+constexpr uint32_t MITER_CLIP_JOIN_CONTOUR_FLAG = 5u << 26;
+constexpr uint32_t MITER_REVERT_JOIN_CONTOUR_FLAG = 4u << 26;
+constexpr uint32_t ROUND_JOIN_CONTOUR_FLAG = 2u << 26;
+constexpr uint32_t FEATHER_JOIN_CONTOUR_FLAG = 1u << 26;
+constexpr uint32_t EMULATED_STROKE_CAP_CONTOUR_FLAG = 1u << 25;
+constexpr uint32_t NEGATE_PATH_FILL_COVERAGE_FLAG = 1u << 24;
+constexpr uint32_t MIRRORED_CONTOUR_CONTOUR_FLAG = 1u << 23;
+constexpr uint32_t JOIN_TANGENT_0_CONTOUR_FLAG = 1u << 22;
+constexpr uint32_t JOIN_TANGENT_INNER_CONTOUR_FLAG = 1u << 21;
+constexpr uint32_t LEFT_JOIN_CONTOUR_FLAG = 1u << 20;
+constexpr uint32_t RIGHT_JOIN_CONTOUR_FLAG = 1u << 19;
+constexpr uint32_t CONTOUR_ID_MASK = 0xffffu;
+
+constexpr int STROKE_VERTEX = 0;
+constexpr int FAN_VERTEX = 1;
+constexpr int FAN_MIDPOINT_VERTEX = 2;
+
+constexpr uint32_t CLIP_UPDATE_PAINT_TYPE = 0u;
+constexpr uint32_t SOLID_COLOR_PAINT_TYPE = 1u;
+constexpr uint32_t LINEAR_GRADIENT_PAINT_TYPE = 2u;
+constexpr uint32_t RADIAL_GRADIENT_PAINT_TYPE = 3u;
+constexpr uint32_t PAINT_FLAG_EVEN_ODD_FILL = 0x200u;
+
+constexpr uint32_t MAX_DENORM_F16 = 1023u;
+constexpr float EPSILON_FP16_NON_DENORM = 6.2e-5f;
+
+// gpu::ShaderFeatures (gpu.hpp:840-856).
+constexpr uint32_t SF_CLIPPING = 1u << 0;
+constexpr uint32_t SF_CLIP_RECT = 1u << 1;
+constexpr uint32_t SF_ADVANCED_BLEND = 1u << 2;
+constexpr uint32_t SF_FEATHER = 1u << 3;
+constexpr uint32_t SF_EVEN_ODD = 1u << 4;
+constexpr uint32_t SF_NESTED_CLIPPING = 1u << 5;
+constexpr uint32_t SF_HSL_BLEND_MODES = 1u << 6;
+constexpr uint32_t SF_DITHER = 1u << 7;
+constexpr uint32_t SF_MODULATED_IMAGE = 1u << 8;
+
+// Raster tiles.
+constexpr int kTileSize = 16;
+constexpr int kTileLog2 = 4;
+constexpr int kTilePixels = kTileSize * kTileSize;
+
+// Device error word bits (read by rive_cuda_sync).
+constexpr uint32_t ERR_BAD_TESS_INDEX = 1u << 0;
+constexpr uint32_t ERR_BAD_CONTOUR = 1u << 1;
+constexpr uint32_t ERR_BAD_PATH = 1u << 2;
+constexpr uint32_t ERR_FEATHER = 1u << 3;
+constexpr uint32_t ERR_COORD_RANGE = 1u << 4;
+constexpr uint32_t ERR_BIN_OVERFLOW = 1u << 5;
+
+// One set-up triangle, ready for the tile raster (80 bytes). Edge k is
+// E_k(p) = A_k * (p.x - ax_k) + B_k * (p.y - ay_k), positive inside. Each edge
+// is anchored at its canonical endpoint (the same vertex for the two triangles
+// that share the edge), so shared edges evaluate to bitwise-negated values and
+// the fill is watertight. Coverage components are planes anchored at edge 0's
+// anchor: cov(p) = c + gx * (p.x - ax_0) + gy * (p.y - ay_0).
+struct __align__(16) TriRecord
+{
+    float4 e0;   // ax, ay, A, B
+    float4 e1;
+    float4 e2;
+    float4 covx; // c, gx, gy, unused
+    float covy_c, covy_gx, covy_gy;
+    uint32_t pathAndFeatures; // pathID (16 bits) | shaderFeatures << 16
+};
+static_assert(sizeof(TriRecord) == 80, "TriRecord layout");
+
+struct FlushParams
+{
+    // Record buffers at the frame's element 0.
+    const uint4* paths;      // PathData as 4 x uint4
+    const uint2* paints;     // PaintData
+    const float4* paintAux;  // PaintAuxData as 8 x float4
+    const uint4* contours;   // ContourData
+    const uint4* gradSpans;  // GradientSpan
+    const uint4* tessSpans;  // TessVertexSpan as 4 x uint4
+    uint32_t firstPath, firstPaint, firstPaintAux, firstContour;
+    uint32_t firstGradSpan, gradSpanCount;
+    uint32_t firstTessSpan, tessSpanCount;
+    uint32_t pathCount, contourCount;
+    uint32_t gradDataHeight, tessDataHeight;
+    uint32_t width, height;
+    uint32_t pathIDGranularity;
+    float ditherScale, ditherBias;
+    uint32_t wireframe;
+    uint32_t loadClear;
+    uint32_t clearColorPremulRGBA; // packed RGBA8, R in the low byte
+    // Intermediate textures.
+    uint4* tess;    // 2048 x tessDataHeight
+    uchar4* grad;   // 512 x gradDataHeight
+    uint32_t* error;
+};
+} // namespace rivecuda

@@ -1,0 +1,250 @@
+"""ctypes binding of the C ABI in include/rive_cuda.h (librive_cuda.so).
+
+This is the Python face of the drop-in backend: the same calls a
+RenderContextImpl makes (resize/map/unmap per record buffer, then one flush per
+logical flush), plus render-target read-back. The library is built in-tree by
+``build.py``; importing this module on a machine without it raises, so no code
+path can silently fall back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from . import build as _build
+from .capture import BUFFER_NAMES
+
+LIB_PATH = _build.LIB
+HEADER = os.path.join(_build.REPO, "include", "rive_cuda.h")
+
+OK = 0
+STAGES = ("color_ramp", "tessellate", "patch_setup", "bin", "sort", "raster")
+BUFFER_KINDS = {n: i for i, n in enumerate(BUFFER_NAMES)}
+
+
+class FlushDesc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "render_target_width", "render_target_height", "interlock_mode",
+        "color_load_action", "color_clear_value")] + [
+        ("update_bounds", ctypes.c_int32 * 4)] + [
+        (n, ctypes.c_uint32) for n in (
+            "combined_shader_features", "dither_mode",
+            "flush_uniform_offset_bytes", "path_count", "first_path",
+            "first_paint", "first_paint_aux", "contour_count", "first_contour",
+            "grad_span_count", "first_grad_span", "tess_span_count",
+            "first_tess_span", "grad_data_height", "tess_data_height",
+            "wireframe", "clockwise_fill_override", "has_triangle_vertices",
+            "draw_batch_count")] + [("draw_batches", ctypes.c_void_p)]
+
+
+class DeviceBuffers(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "flush_uniforms", "paths", "paints", "paint_aux", "contours",
+        "grad_spans", "tess_spans")]
+
+
+class FlushStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "tess_vertices", "patches", "triangles", "bin_entries", "tiles",
+        "kernel_launches")]
+
+
+class RiveCudaError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def exported_functions():
+    """Names of the functions include/rive_cuda.h declares."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"\b(rive_cuda_[a-z0-9_]+)\s*\(", text)))
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"librive_cuda.so is not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, sz, u32, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int
+    sig = {
+        "rive_cuda_context_create": (i32, [i32, ctypes.POINTER(vp)]),
+        "rive_cuda_context_destroy": (None, [vp]),
+        "rive_cuda_last_error": (i32, [vp, ctypes.c_char_p, sz]),
+        "rive_cuda_resize_buffer": (i32, [vp, i32, sz]),
+        "rive_cuda_map_buffer": (vp, [vp, i32, sz]),
+        "rive_cuda_unmap_buffer": (i32, [vp, i32, sz]),
+        "rive_cuda_resize_gradient_texture": (i32, [vp, u32, u32]),
+        "rive_cuda_resize_tessellation_texture": (i32, [vp, u32, u32]),
+        "rive_cuda_render_target_create": (i32, [vp, u32, u32, ctypes.POINTER(vp)]),
+        "rive_cuda_render_target_destroy": (None, [vp, vp]),
+        "rive_cuda_render_target_device_ptr": (vp, [vp]),
+        "rive_cuda_render_target_read": (i32, [vp, vp, vp, vp]),
+        "rive_cuda_flush": (i32, [vp, ctypes.POINTER(FlushDesc), vp, vp]),
+        "rive_cuda_flush_device": (i32, [vp, ctypes.POINTER(FlushDesc),
+                                         ctypes.POINTER(DeviceBuffers), vp, vp]),
+        "rive_cuda_sync": (i32, [vp, vp]),
+        "rive_cuda_read_tess_texture": (i32, [vp, vp, sz]),
+        "rive_cuda_read_grad_texture": (i32, [vp, vp, sz]),
+        "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
+        "rive_cuda_set_profiling": (i32, [vp, i32]),
+        "rive_cuda_profile_collect": (i32, [vp, ctypes.POINTER(ctypes.c_double),
+                                            ctypes.POINTER(ctypes.c_uint64)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def make_desc(flush):
+    d = FlushDesc()
+    for k, v in flush.desc.items():
+        if k.startswith("ub"):
+            d.update_bounds[int(k[2])] = v
+        elif k != "draw_batch_count":
+            setattr(d, k, int(v))
+    batches = np.ascontiguousarray(flush.batches, dtype=np.uint32)
+    d.draw_batch_count = len(batches)
+    d.draw_batches = batches.ctypes.data if len(batches) else None
+    return d, batches
+
+
+class Context:
+    """One rive_cuda_context (one GPU, one stream)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.rive_cuda_context_create(device, ctypes.byref(h))
+        if rc != OK:
+            raise RiveCudaError(f"rive_cuda_context_create failed ({rc})")
+        self.h = h
+        self._targets = []
+        self._capacity = {}
+
+    def close(self):
+        if self.h:
+            for t in self._targets:
+                self.lib.rive_cuda_render_target_destroy(self.h, t)
+            self._targets = []
+            self.lib.rive_cuda_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def error(self):
+        buf = ctypes.create_string_buffer(512)
+        self.lib.rive_cuda_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    def check(self, rc, what):
+        if rc != OK:
+            raise RiveCudaError(f"{what}: status {rc}: {self.error()}")
+
+    # -- RenderContextImpl-shaped calls -------------------------------------
+    def resize_buffer(self, kind: int, nbytes: int):
+        self.check(self.lib.rive_cuda_resize_buffer(self.h, kind, nbytes), "resize_buffer")
+        self._capacity[kind] = nbytes
+
+    def upload(self, kind: int, data: bytes):
+        """resize (grow x1.25) / map / write / unmap, as RenderContext does."""
+        n = len(data)
+        if n == 0:
+            return
+        if self._capacity.get(kind, 0) < n:
+            self.resize_buffer(kind, n + n // 4)
+        p = self.lib.rive_cuda_map_buffer(self.h, kind, n)
+        if not p:
+            raise RiveCudaError(f"map_buffer failed: {self.error()}")
+        ctypes.memmove(p, data, n)
+        self.check(self.lib.rive_cuda_unmap_buffer(self.h, kind, n), "unmap_buffer")
+
+    def render_target(self, width: int, height: int):
+        t = ctypes.c_void_p()
+        self.check(self.lib.rive_cuda_render_target_create(self.h, width, height, ctypes.byref(t)),
+                   "render_target_create")
+        self._targets.append(t)
+        return t
+
+    def flush(self, flush, target, stream=None):
+        d, keep = make_desc(flush)
+        self.check(self.lib.rive_cuda_flush(self.h, ctypes.byref(d), target, stream), "flush")
+        del keep
+
+    def flush_device(self, flush, bufs: DeviceBuffers, target_ptr: int, stream=None):
+        d, keep = make_desc(flush)
+        self.check(self.lib.rive_cuda_flush_device(self.h, ctypes.byref(d), ctypes.byref(bufs),
+                                                   ctypes.c_void_p(target_ptr), stream),
+                   "flush_device")
+        del keep
+
+    def sync(self, stream=None):
+        self.check(self.lib.rive_cuda_sync(self.h, stream), "sync")
+
+    def read_target(self, target, width, height, out=None):
+        if out is None:
+            out = np.empty((height, width, 4), np.uint8)
+        self.check(self.lib.rive_cuda_render_target_read(
+            self.h, target, out.ctypes.data_as(ctypes.c_void_p), None), "render_target_read")
+        return out
+
+    def target_device_ptr(self, target):
+        return self.lib.rive_cuda_render_target_device_ptr(target)
+
+    def read_tess(self, height):
+        out = np.empty((height * 2048, 4), np.uint32)
+        self.check(self.lib.rive_cuda_read_tess_texture(
+            self.h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes), "read_tess_texture")
+        return out
+
+    def read_grad(self, height):
+        out = np.empty((height, 512, 4), np.uint8)
+        self.check(self.lib.rive_cuda_read_grad_texture(
+            self.h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes), "read_grad_texture")
+        return out
+
+    def stats(self):
+        s = FlushStats()
+        self.check(self.lib.rive_cuda_last_flush_stats(self.h, ctypes.byref(s)), "stats")
+        return {k: getattr(s, k) for k, _ in FlushStats._fields_}
+
+    def set_profiling(self, on: bool):
+        self.check(self.lib.rive_cuda_set_profiling(self.h, 1 if on else 0), "set_profiling")
+
+    def profile_collect(self):
+        ms = (ctypes.c_double * len(STAGES))()
+        n = (ctypes.c_uint64 * len(STAGES))()
+        self.check(self.lib.rive_cuda_profile_collect(self.h, ms, n), "profile_collect")
+        return {st: (ms[i], n[i]) for i, st in enumerate(STAGES)}
+
+    # -- helpers --------------------------------------------------------------
+    def upload_frame(self, cap):
+        for name in BUFFER_NAMES:
+            self.upload(BUFFER_KINDS[name], cap.buffers.get(name, b""))
+
+    def render(self, cap, target=None, read=True):
+        """Uploads a captured frame, runs all its logical flushes, reads back."""
+        if target is None:
+            target = self.render_target(cap.width, cap.height)
+        self.upload_frame(cap)
+        for f in cap.flushes:
+            self.flush(f, target)
+        self.sync()
+        if read:
+            return self.read_target(target, cap.width, cap.height)
+        return target

@@ -180,9 +180,9 @@ def plain_small(seed: int = 1, width: int = 512, height: int = 512,
     return sc
 
 
-def _random_affine(rng, width, height):
+def _random_affine(rng, width, height, scale_range=(0.25, 4.0)):
     theta = rng.uniform(0.0, 2.0 * math.pi)
-    s = math.exp(rng.uniform(math.log(0.25), math.log(4.0)))
+    s = math.exp(rng.uniform(math.log(scale_range[0]), math.log(scale_range[1])))
     tx = rng.uniform(0.0, width)
     ty = rng.uniform(0.0, height)
     c, sn = math.cos(theta) * s, math.sin(theta) * s
@@ -209,13 +209,16 @@ def _gradient_paint(rng, paint: Paint):
 
 def full_feature(seed: int = 2, width: int = 2048, height: int = 2048,
                  n_paths: int = 5000, max_contours: int = 4,
-                 min_cubics: int = 4, max_cubics: int = 64) -> Scene:
+                 min_cubics: int = 4, max_cubics: int = 64,
+                 p_fill: float = 0.6, p_gradient: float = 0.3,
+                 p_blend: float = 0.1, p_clip: float = 0.1,
+                 scale_range=(0.25, 4.0)) -> Scene:
     """The full-feature single scene (defaults: 2048x2048, 5,000 paths)."""
     rng = np.random.default_rng(seed)
     sc = Scene(width, height, clear_color=0xFFFFFFFF)
     h = LOCAL_HALF_EXTENT
     for _ in range(n_paths):
-        is_fill = rng.uniform() < 0.6
+        is_fill = rng.uniform() < p_fill
         ncont = int(rng.integers(1, max_contours + 1))
         verbs, pts = [], []
         for _c in range(ncont):
@@ -234,13 +237,13 @@ def full_feature(seed: int = 2, width: int = 2048, height: int = 2048,
             paint.thickness = float(np.exp(rng.normal(math.log(4.0), 0.7)))
             paint.join = int(rng.integers(0, 3))
             paint.cap = int(rng.integers(0, 3))
-        if rng.uniform() < 0.3:
+        if rng.uniform() < p_gradient:
             _gradient_paint(rng, paint)
-        if rng.uniform() < 0.1:
+        if rng.uniform() < p_blend:
             paint.blend_mode = int(BLEND_MODES[int(rng.integers(0, 16))])
         qi = sc.add_paint(paint)
-        m = _random_affine(rng, width, height)
-        clipped = rng.uniform() < 0.1
+        m = _random_affine(rng, width, height, scale_range)
+        clipped = rng.uniform() < p_clip
         sc.cmd(CMD_SAVE)
         sc.cmd(CMD_TRANSFORM, m=m)
         if clipped:

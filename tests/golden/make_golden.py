@@ -1,0 +1,61 @@
+"""Regenerates the golden flush captures in this directory.
+
+Each fixture pair is <name>.scene (a seeded rive_scene.h recording written by
+the scene generator) and <name>.cap: what rive-runtime's own, unmodified CPU
+front end (RiveRenderer -> RenderContext, compiled from its sources by
+oracle/Makefile into oracle/_ref/ref_capture) hands its RenderContextImpl for
+that scene. Needs the reference sources, so it runs only where they exist:
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+from conftest import load_package  # noqa: E402
+
+pkg = load_package()
+from rive_runtime_gb300 import scene  # noqa: E402
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle"))
+import oracle  # noqa: E402
+
+SCENES = {
+    # The plain small workload at full size: 512x512, 200 closed 8-cubic fills.
+    "plain_small_s1": lambda: scene.plain_small(seed=1),
+    # Full-feature distribution, shrunk: fills (nonzero/even-odd), strokes
+    # (all joins and caps), gradients, blend modes, nested clips.
+    "full_small_s7": lambda: scene.full_feature(seed=7, width=256, height=256, n_paths=40,
+                                                max_cubics=12, scale_range=(0.5, 2.0)),
+    # Odd canvas size (not a multiple of the tile), heavier blend/clip mix.
+    "full_odd_s11": lambda: scene.full_feature(seed=11, width=300, height=200, n_paths=50,
+                                               max_cubics=8, p_gradient=0.5, p_blend=0.5,
+                                               p_clip=0.4, scale_range=(0.5, 2.0)),
+    # Strokes only: every join and cap, thin to thick.
+    "strokes_s3": lambda: scene.full_feature(seed=3, width=256, height=256, n_paths=40,
+                                             max_cubics=6, p_fill=0.0, p_gradient=0.2,
+                                             p_blend=0.0, p_clip=0.0, scale_range=(0.5, 2.0)),
+    # Tessellation stress: cusps, near-degenerate cubics, round joins/caps.
+    "stroke_stress_s5": lambda: scene.stroke_stress(seed=5, width=256, height=256, n_strokes=60),
+    # Deep nested clipping.
+    "clips_s13": lambda: scene.full_feature(seed=13, width=192, height=192, n_paths=30,
+                                            max_cubics=6, p_clip=1.0, p_gradient=0.3,
+                                            p_blend=0.2, scale_range=(0.75, 1.5)),
+}
+
+
+def main():
+    for name, make in SCENES.items():
+        sc = make()
+        sb = sc.to_bytes()
+        cb = oracle.reference_capture(sb)
+        with open(os.path.join(HERE, name + ".scene"), "wb") as f:
+            f.write(sb)
+        with open(os.path.join(HERE, name + ".cap"), "wb") as f:
+            f.write(cb)
+        print(f"{name}: scene {len(sb)} B, capture {len(cb)} B")
+
+
+if __name__ == "__main__":
+    main()
