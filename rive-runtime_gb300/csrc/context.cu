@@ -333,7 +333,11 @@ int run_flush(rive_cuda_context* ctx,
         P.grad = (uchar4*)ctx->grad.ptr;
         uint64_t launches = 0;
 
-        // Pass 1: gradient ramps.
+        // Pass 1: gradient ramps. Texels no span covers are never sampled;
+        // zero them so the texture is deterministic.
+        if (d->grad_data_height)
+            CK(cudaMemsetAsync(ctx->grad.ptr, 0, (size_t)kGradTextureWidth * d->grad_data_height * 4,
+                               stream));
         if (d->grad_span_count)
         {
             stage_begin(ctx, RIVE_CUDA_STAGE_COLOR_RAMP, stream);

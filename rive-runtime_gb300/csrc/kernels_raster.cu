@@ -388,18 +388,14 @@ __device__ __forceinline__ float4 make_edge(float2 P, float2 Q)
     return make_float4(a.x, a.y, A, B);
 }
 
-struct TileRect
+// Does any pixel centre of [x0, x1) x [y0, y1) (already clipped to the
+// triangle's pixel bounds) lie inside the triangle? Conservative on ties. Uses
+// the same edge_eval as the raster, and float rounding is monotone, so a
+// rejected region never holds a pixel the raster would accept.
+__device__ __forceinline__ bool rect_overlaps(const float4* e, int x0, int x1, int y0, int y1)
 {
-    int bx0, by0, bx1, by1; // pixel bbox, [b0, b1)
-};
-
-__device__ __forceinline__ bool tile_overlaps(const TriRecord& T, const TileRect& r, int tx, int ty)
-{
-    float xlo = (float)max(tx * kTileSize, r.bx0) + .5f;
-    float xhi = (float)(min(tx * kTileSize + kTileSize, r.bx1) - 1) + .5f;
-    float ylo = (float)max(ty * kTileSize, r.by0) + .5f;
-    float yhi = (float)(min(ty * kTileSize + kTileSize, r.by1) - 1) + .5f;
-    const float4 e[3] = {T.e0, T.e1, T.e2};
+    float xlo = (float)x0 + .5f, xhi = (float)(x1 - 1) + .5f;
+    float ylo = (float)y0 + .5f, yhi = (float)(y1 - 1) + .5f;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
@@ -411,13 +407,29 @@ __device__ __forceinline__ bool tile_overlaps(const TriRecord& T, const TileRect
     return true;
 }
 
+__device__ __forceinline__ bool tile_overlaps(const float4* e, int4 bb, int tx, int ty)
+{
+    return rect_overlaps(e,
+                         max(tx * kTileSize, bb.x),
+                         min(tx * kTileSize + kTileSize, bb.z),
+                         max(ty * kTileSize, bb.y),
+                         min(ty * kTileSize + kTileSize, bb.w));
+}
+
 // Snaps to the 1/256-pixel grid of the rasteriser.
 __device__ __forceinline__ float snap(float v) { return rintf(v * 256.f) * (1.f / 256.f); }
+
+__device__ __forceinline__ int4 unpack_bbox(uint4 meta)
+{
+    return make_int4((int)(meta.y & 0xffffu), (int)(meta.z & 0xffffu), (int)(meta.y >> 16),
+                     (int)(meta.z >> 16));
+}
 } // namespace
 
 // Per patch instance (one warp): shade 42 vertices, assemble and set up 24
-// triangles, and count the tiles each one touches. Triangle slot order is
-// primitive order (batch, instance, triangle-in-patch).
+// triangles, then count the tiles each one touches, the warp striding over
+// each triangle's tile rectangle. Triangle slot order is primitive order
+// (batch, instance, triangle-in-patch).
 __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
                                                           uint32_t baseInstance,
                                                           uint32_t instanceCount,
@@ -428,114 +440,176 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
                                                           int4* __restrict__ bboxes)
 {
     __shared__ VertexOut sv[4][kPatchVertexCount];
+    __shared__ float4 sEdges[4][kPatchTriangleCount][3];
+    __shared__ int4 sBox[4][kPatchTriangleCount];
     __shared__ bool sok[4];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t local = blockIdx.x * 4 + w;
-    const bool active = local < instanceCount;
+    if (local >= instanceCount)
+        return; // whole warp exits together
     const uint32_t instance = baseInstance + local;
     if (lane == 0)
         sok[w] = true;
     __syncwarp();
-    if (active)
+    for (int v = lane; v < kPatchVertexCount; v += 32)
     {
-        for (int v = lane; v < kPatchVertexCount; v += 32)
+        VertexOut o;
+        if (!shade_patch_vertex(P, v, instance, o))
         {
-            VertexOut o;
-            if (!shade_patch_vertex(P, v, instance, o))
-            {
-                sok[w] = false;
-                o.discard = true;
-            }
-            sv[w][v] = o;
+            sok[w] = false;
+            o.discard = true;
         }
+        sv[w][v] = o;
     }
     __syncwarp();
-    if (!active || lane >= kPatchTriangleCount)
-        return;
-    const uint32_t slot = slotBase + local * kPatchTriangleCount + lane;
-    int ia, ib, ic;
-    patch_triangle(lane, ia, ib, ic);
-    const VertexOut& A = sv[w][ia];
-    const VertexOut& B = sv[w][ib];
-    const VertexOut& C = sv[w][ic];
-    uint32_t count = 0;
-    int4 bb = make_int4(0, 0, 0, 0);
-    bool valid = sok[w] && !A.discard && !B.discard && !C.discard;
-    float2 p0, p1, p2;
-    if (valid)
+    const uint32_t slot0 = slotBase + local * kPatchTriangleCount;
+    if (lane < kPatchTriangleCount)
     {
-        p0 = make_float2(snap(A.pos.x), snap(A.pos.y));
-        p1 = make_float2(snap(B.pos.x), snap(B.pos.y));
-        p2 = make_float2(snap(C.pos.x), snap(C.pos.y));
-        float m = fmaxf(fmaxf(fmaxf(fabsf(p0.x), fabsf(p0.y)), fmaxf(fabsf(p1.x), fabsf(p1.y))),
-                        fmaxf(fabsf(p2.x), fabsf(p2.y)));
-        if (!(m < 32768.f)) // NaN or outside the exact snapping range
+        int ia, ib, ic;
+        patch_triangle(lane, ia, ib, ic);
+        const VertexOut& A = sv[w][ia];
+        const VertexOut& B = sv[w][ib];
+        const VertexOut& C = sv[w][ic];
+        int4 bb = make_int4(0, 0, 0, 0);
+        bool valid = sok[w] && !A.discard && !B.discard && !C.discard;
+        float2 p0, p1, p2;
+        if (valid)
         {
-            if (!(isnan(m)))
-                atomicOr(P.error, ERR_COORD_RANGE);
-            valid = false;
+            p0 = make_float2(snap(A.pos.x), snap(A.pos.y));
+            p1 = make_float2(snap(B.pos.x), snap(B.pos.y));
+            p2 = make_float2(snap(C.pos.x), snap(C.pos.y));
+            float m = fmaxf(fmaxf(fmaxf(fabsf(p0.x), fabsf(p0.y)), fmaxf(fabsf(p1.x), fabsf(p1.y))),
+                            fmaxf(fabsf(p2.x), fabsf(p2.y)));
+            if (!(m < 32768.f)) // NaN or outside the exact snapping range
+            {
+                if (!isnan(m))
+                    atomicOr(P.error, ERR_COORD_RANGE);
+                valid = false;
+            }
         }
+        double area2 = 0.0;
+        if (valid)
+        {
+            // Exact: coordinates are multiples of 1/256 below 2^15.
+            double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
+            double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
+            area2 = d1x * d2y - d2x * d1y;
+            valid = area2 > 0.0; // counterclockwise culled, degenerate dropped
+        }
+        if (valid)
+        {
+            float minx = fminf(fminf(p0.x, p1.x), p2.x), maxx = fmaxf(fmaxf(p0.x, p1.x), p2.x);
+            float miny = fminf(fminf(p0.y, p1.y), p2.y), maxy = fmaxf(fmaxf(p0.y, p1.y), p2.y);
+            // Pixels whose centres k + 1/2 lie inside [min, max].
+            int bx0 = max((int)ceilf(minx - .5f), 0);
+            int bx1 = min((int)floorf(maxx - .5f) + 1, (int)P.width);
+            int by0 = max((int)ceilf(miny - .5f), 0);
+            int by1 = min((int)floorf(maxy - .5f) + 1, (int)P.height);
+            if (bx0 >= bx1 || by0 >= by1)
+                valid = false;
+            else
+                bb = make_int4(bx0, by0, bx1, by1);
+        }
+        if (valid)
+        {
+            TriRecord T;
+            T.e0 = make_edge(p0, p1);
+            T.e1 = make_edge(p1, p2);
+            T.e2 = make_edge(p2, p0);
+            double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
+            double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
+            double inv = 1.0 / area2;
+            double ax = (double)T.e0.x - p0.x, ay = (double)T.e0.y - p0.y;
+            double cxc, cxgx, cxgy, cyc, cygx, cygy;
+            {
+                double c0 = A.cov.x, c1 = B.cov.x, c2 = C.cov.x;
+                cxgx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
+                cxgy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
+                cxc = c0 + cxgx * ax + cxgy * ay;
+            }
+            {
+                double c0 = A.cov.y, c1 = B.cov.y, c2 = C.cov.y;
+                cygx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
+                cygy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
+                cyc = c0 + cygx * ax + cygy * ay;
+            }
+            const uint2 paint = P.paints[P.firstPaint + A.pathID];
+            T.cov0 = make_float4((float)cxc, (float)cxgx, (float)cxgy, (float)cyc);
+            T.cov1 = make_float4((float)cygx, (float)cygy, __uint_as_float(paint.x),
+                                 __uint_as_float(paint.y));
+            T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16),
+                                (uint32_t)bb.x | ((uint32_t)bb.z << 16),
+                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), 0u);
+            tris[slot0 + lane] = T;
+            sEdges[w][lane][0] = T.e0;
+            sEdges[w][lane][1] = T.e1;
+            sEdges[w][lane][2] = T.e2;
+        }
+        sBox[w][lane] = bb;
     }
-    double area2 = 0.0;
-    if (valid)
+    __syncwarp();
+    // Tile counts. A triangle whose box spans few tiles is counted by its own
+    // lane; larger ones are walked by the whole warp, one after another.
+    constexpr int kLaneTiles = 8;
+    uint32_t bigMask = 0;
+    if (lane < kPatchTriangleCount)
     {
-        // Exact: coordinates are multiples of 1/256 below 2^15.
-        double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
-        double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
-        area2 = d1x * d2y - d2x * d1y;
-        valid = area2 > 0.0; // counterclockwise culled, degenerate dropped
-    }
-    if (valid)
-    {
-        float minx = fminf(fminf(p0.x, p1.x), p2.x), maxx = fmaxf(fmaxf(p0.x, p1.x), p2.x);
-        float miny = fminf(fminf(p0.y, p1.y), p2.y), maxy = fmaxf(fmaxf(p0.y, p1.y), p2.y);
-        // Pixels whose centres k + 1/2 lie inside [min, max].
-        int bx0 = max((int)ceilf(minx - .5f), 0), bx1 = min((int)floorf(maxx - .5f) + 1, (int)P.width);
-        int by0 = max((int)ceilf(miny - .5f), 0), by1 = min((int)floorf(maxy - .5f) + 1, (int)P.height);
-        if (bx0 >= bx1 || by0 >= by1)
-            valid = false;
+        const int4 bb = sBox[w][lane];
+        uint32_t count = 0;
+        if (bb.z > bb.x)
+        {
+            const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
+            const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
+            const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+            if (ntx * nty <= kLaneTiles)
+            {
+                const float4 e[3] = {sEdges[w][lane][0], sEdges[w][lane][1], sEdges[w][lane][2]};
+                for (int ty = ty0; ty < ty0 + nty; ++ty)
+                    for (int tx = tx0; tx < tx0 + ntx; ++tx)
+                        count += tile_overlaps(e, bb, tx, ty) ? 1u : 0u;
+                tileCounts[slot0 + lane] = count;
+                bboxes[slot0 + lane] = count ? bb : make_int4(0, 0, 0, 0);
+            }
+            else
+            {
+                bigMask = 1u;
+            }
+        }
         else
-            bb = make_int4(bx0, by0, bx1, by1);
+        {
+            tileCounts[slot0 + lane] = 0;
+            bboxes[slot0 + lane] = make_int4(0, 0, 0, 0);
+        }
     }
-    if (valid)
+    uint32_t big = __ballot_sync(0xffffffffu, bigMask != 0);
+    while (big)
     {
-        TriRecord T;
-        T.e0 = make_edge(p0, p1);
-        T.e1 = make_edge(p1, p2);
-        T.e2 = make_edge(p2, p0);
-        double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
-        double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
-        double inv = 1.0 / area2;
-        double ax = (double)T.e0.x - p0.x, ay = (double)T.e0.y - p0.y;
+        const int t = __ffs(big) - 1;
+        big &= big - 1;
+        const int4 bb = sBox[w][t];
+        const float4 e[3] = {sEdges[w][t][0], sEdges[w][t][1], sEdges[w][t][2]};
+        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
+        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
+        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+        const int n = ntx * nty;
+        uint32_t count = 0;
+        for (int i = lane; i < n; i += 32)
+            count += tile_overlaps(e, bb, tx0 + i % ntx, ty0 + i / ntx) ? 1u : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            count += __shfl_xor_sync(0xffffffffu, count, o);
+        if (lane == 0)
         {
-            double c0 = A.cov.x, c1 = B.cov.x, c2 = C.cov.x;
-            double gx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
-            double gy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
-            T.covx = make_float4((float)(c0 + gx * ax + gy * ay), (float)gx, (float)gy, 0.f);
+            tileCounts[slot0 + t] = count;
+            bboxes[slot0 + t] = count ? bb : make_int4(0, 0, 0, 0);
         }
-        {
-            double c0 = A.cov.y, c1 = B.cov.y, c2 = C.cov.y;
-            double gx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
-            double gy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
-            T.covy_c = (float)(c0 + gx * ax + gy * ay);
-            T.covy_gx = (float)gx;
-            T.covy_gy = (float)gy;
-        }
-        T.pathAndFeatures = (A.pathID & 0xffffu) | (features << 16);
-        tris[slot] = T;
-        TileRect r = {bb.x, bb.y, bb.z, bb.w};
-        for (int ty = bb.y >> kTileLog2; ty <= (bb.w - 1) >> kTileLog2; ++ty)
-            for (int tx = bb.x >> kTileLog2; tx <= (bb.z - 1) >> kTileLog2; ++tx)
-                count += tile_overlaps(T, r, tx, ty) ? 1u : 0u;
-        if (count == 0)
-            bb = make_int4(0, 0, 0, 0);
     }
-    tileCounts[slot] = count;
-    bboxes[slot] = bb;
 }
 
-// Writes the (tile, slot) pairs of each triangle at its scanned offset, in
-// primitive order.
+// Writes the (tile, slot) pairs of each triangle at its scanned offset. One
+// warp per 32 consecutive slots: a lane writes its own triangle's pairs when
+// its box spans few tiles; larger triangles are walked by the whole warp with
+// a ballot assigning output positions.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                                                           uint32_t tilesX,
                                                           const TriRecord* __restrict__ tris,
@@ -545,21 +619,75 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                                                           uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals)
 {
-    uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= slotCount || tileCounts[slot] == 0)
+    constexpr int kLaneTiles = 8;
+    const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t first = warpId * 32;
+    if (first >= slotCount)
         return;
-    const TriRecord T = tris[slot];
-    int4 bb = bboxes[slot];
-    TileRect r = {bb.x, bb.y, bb.z, bb.w};
-    uint32_t o = offsets[slot];
-    for (int ty = bb.y >> kTileLog2; ty <= (bb.w - 1) >> kTileLog2; ++ty)
-        for (int tx = bb.x >> kTileLog2; tx <= (bb.z - 1) >> kTileLog2; ++tx)
-            if (tile_overlaps(T, r, tx, ty))
+    const uint32_t mySlot = first + lane;
+    const uint32_t myCount = mySlot < slotCount ? tileCounts[mySlot] : 0u;
+    bool isBig = false;
+    if (myCount)
+    {
+        const int4 bb = bboxes[mySlot];
+        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
+        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
+        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+        if (ntx * nty <= kLaneTiles)
+        {
+            const TriRecord* T = tris + mySlot;
+            const float4 e[3] = {T->e0, T->e1, T->e2};
+            uint32_t o = offsets[mySlot];
+            for (int ty = ty0; ty < ty0 + nty; ++ty)
+                for (int tx = tx0; tx < tx0 + ntx; ++tx)
+                    if (tile_overlaps(e, bb, tx, ty))
+                    {
+                        keys[o] = (uint32_t)ty * tilesX + (uint32_t)tx;
+                        vals[o] = mySlot;
+                        ++o;
+                    }
+        }
+        else
+        {
+            isBig = true;
+        }
+    }
+    uint32_t pending = __ballot_sync(0xffffffffu, isBig);
+    while (pending)
+    {
+        const int t = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t slot = first + t;
+        const int4 bb = bboxes[slot];
+        const TriRecord* T = tris + slot;
+        const float4 e[3] = {T->e0, T->e1, T->e2};
+        uint32_t o = offsets[slot];
+        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
+        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
+        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+        const int n = ntx * nty;
+        for (int base = 0; base < n; base += 32)
+        {
+            const int i = base + lane;
+            bool hit = false;
+            int tx = 0, ty = 0;
+            if (i < n)
             {
-                keys[o] = (uint32_t)ty * tilesX + (uint32_t)tx;
-                vals[o] = slot;
-                ++o;
+                tx = tx0 + i % ntx;
+                ty = ty0 + i / ntx;
+                hit = tile_overlaps(e, bb, tx, ty);
             }
+            const uint32_t mask = __ballot_sync(0xffffffffu, hit);
+            if (hit)
+            {
+                const uint32_t pos = o + __popc(mask & ((1u << lane) - 1u));
+                keys[pos] = (uint32_t)ty * tilesX + (uint32_t)tx;
+                vals[pos] = slot;
+            }
+            o += __popc(mask);
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
@@ -578,9 +706,9 @@ __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
 
 namespace
 {
-__device__ __forceinline__ uint16_t id_bits_to_f16(uint32_t idBits, uint32_t granularity)
+__device__ __forceinline__ uint32_t id_bits_to_f16(uint32_t idBits, uint32_t granularity)
 {
-    return idBits == 0 ? 0 : (uint16_t)((idBits + MAX_DENORM_F16) * granularity);
+    return idBits == 0 ? 0u : ((idBits + MAX_DENORM_F16) * granularity) & 0xffffu;
 }
 __device__ __forceinline__ float h2f(uint32_t bits)
 {
@@ -634,7 +762,7 @@ __device__ void set_lum_sat(const float hue[3], const float sat[3], const float 
 
 // advanced_color_blend (advanced_blend.glsl:156-327): src unmultiplied,
 // dst premultiplied; returns mix(src, coeffs, dst.a).
-__device__ void advanced_blend(float src[3], const float dp[4], uint32_t mode)
+__device__ __noinline__ void advanced_blend(float src[3], const float dp[4], uint32_t mode)
 {
     float inv = dp[3] != 0.f ? 1.f / dp[3] : 0.f;
     float dst[3] = {dp[0] * inv, dp[1] * inv, dp[2] * inv};
@@ -724,16 +852,16 @@ __device__ void advanced_blend(float src[3], const float dp[4], uint32_t mode)
         src[i] = src[i] * (1.f - a) + co[i] * a;
 }
 
-__device__ __forceinline__ void sample_grad(const FlushParams& P, float u, float v, float out[4])
+__device__ __noinline__ void sample_grad(const FlushParams& P, float u, float v, float out[4])
 {
     float fx = u * kGradTextureWidth - .5f;
+    // The gradient texture always has at least one row allocated.
+    const int H = max((int)P.gradDataHeight, 1);
     float fy = v * (float)P.gradDataHeight - .5f;
     float x0f = floorf(fx), y0f = floorf(fy);
     float ax = fx - x0f, ay = fy - y0f;
     int x0 = (int)x0f, y0 = (int)y0f;
     out[0] = out[1] = out[2] = out[3] = 0.f;
-    // The gradient texture always has at least one row allocated.
-    const int H = max((int)P.gradDataHeight, 1);
 #pragma unroll
     for (int j = 0; j < 2; ++j)
 #pragma unroll
@@ -750,43 +878,37 @@ __device__ __forceinline__ void sample_grad(const FlushParams& P, float u, float
         }
 }
 
-struct Pls
+// Pixel-local storage of one pixel (draw_raster_order_path.frag:7-12), plus
+// the path whose fragments are still being accumulated.
+struct Pixel
 {
-    uint32_t color;    // RGBA8
+    uint32_t color;    // RGBA8, the colour before the pending path
     uint32_t clip;     // packHalf2x16(coverage, clipID)
-    uint32_t scratch;  // RGBA8
+    uint32_t scratch;  // RGBA8 scratch plane
     uint32_t coverage; // packHalf2x16(coverageCount, pathID)
+    uint32_t pendMeta; // pathAndFeatures of the pending path (0: none)
+    uint32_t pendPaintX, pendPaintY;
+    uint32_t pendFrags; // fragments of the pending path so far (saturating)
 };
 
-// One fragment of draw_raster_order_path.frag for pixel centre (fx, fy).
-__device__ void fragment(const FlushParams& P,
-                         uint32_t pathID,
-                         uint32_t features,
-                         float covx,
-                         float covy,
-                         float fx,
-                         float fy,
-                         float dither,
-                         Pls& s)
+// The colour / clip write of the last fragment of a path at this pixel.
+//
+// draw_raster_order_path.frag writes the colour (or clip) plane on every
+// fragment, each time from the path's accumulated coverage and the same dst
+// colour (stashed at the path's first fragment); only the last write
+// survives. Evaluating it once, when the next path arrives or the tile ends,
+// gives the same result. The one value an earlier fragment feeds forward is
+// the nested-clip stash, which the reference keeps in RGBA8: its
+// quantisation is applied when the path had more than one fragment here.
+__device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float fx, float fy,
+                                          float dither)
 {
-    const uint2 paint = P.paints[P.firstPaint + pathID];
-    uint32_t vPathID = id_bits_to_f16(pathID, P.pathIDGranularity);
-    const bool evenOdd = (paint.x & PAINT_FLAG_EVEN_ODD_FILL) != 0;
-    if (evenOdd)
-        vPathID ^= 0x8000u;
-    const uint32_t paintType = paint.x & 0xfu;
-
-    const uint32_t covBufferID = s.coverage >> 16;
-    float count = covBufferID == vPathID ? h2f(s.coverage & 0xffffu) : 0.f;
-    if (covy >= 0.f)
-        count = fmaxf(fminf(covx, covy), count); // stroke
-    else
-        count = count + covx; // fill
-    uint32_t stored = f2h(count);
-    s.coverage = (vPathID << 16) | stored;
-    count = h2f(stored);
-
-    float coverage = fabsf(count);
+    const uint32_t meta = s.pendMeta;
+    const uint32_t pathID = meta & 0xffffu, features = meta >> 16;
+    const uint32_t paintX = s.pendPaintX, paintY = s.pendPaintY;
+    const uint32_t paintType = paintX & 0xfu;
+    const bool evenOdd = (paintX & PAINT_FLAG_EVEN_ODD_FILL) != 0;
+    float coverage = fabsf(h2f(s.coverage & 0xffffu));
     if ((features & SF_EVEN_ODD) && evenOdd)
         coverage = 1.f - fabsf((coverage * .5f - floorf(coverage * .5f)) * 2.f + -1.f);
     coverage = fminf(coverage, 1.f);
@@ -794,22 +916,23 @@ __device__ void fragment(const FlushParams& P,
     if (features & SF_CLIPPING)
     {
         const uint32_t clipBits = id_bits_to_f16(
-            (paintType == CLIP_UPDATE_PAINT_TYPE ? paint.y : paint.x) >> 16,
-            P.pathIDGranularity);
+            (paintType == CLIP_UPDATE_PAINT_TYPE ? paintY : paintX) >> 16, P.pathIDGranularity);
         if (paintType == CLIP_UPDATE_PAINT_TYPE && clipBits != 0)
         {
-            // Clip update: write coverage into the clip plane.
             if (features & SF_NESTED_CLIPPING)
             {
-                uint32_t outerBits = id_bits_to_f16(paint.x >> 16, P.pathIDGranularity);
+                const uint32_t outerBits = id_bits_to_f16(paintX >> 16, P.pathIDGranularity);
                 if (outerBits != 0)
                 {
-                    uint32_t contentID = s.clip >> 16;
+                    const uint32_t contentID = s.clip >> 16;
                     float outer;
                     if (contentID != clipBits)
                     {
                         outer = contentID == outerBits ? h2f(s.clip & 0xffffu) : 0.f;
-                        s.scratch = unorm8(outer);
+                        const uint32_t stash = unorm8(outer);
+                        s.scratch = stash;
+                        if (s.pendFrags > 1)
+                            outer = (float)stash / 255.f;
                     }
                     else
                     {
@@ -822,9 +945,7 @@ __device__ void fragment(const FlushParams& P,
             return;
         }
         if (clipBits != 0)
-        {
             coverage = (s.clip >> 16) == clipBits ? fminf(h2f(s.clip & 0xffffu), coverage) : 0.f;
-        }
     }
     if (features & SF_CLIP_RECT)
     {
@@ -855,7 +976,7 @@ __device__ void fragment(const FlushParams& P,
     float color[4];
     if (paintType == SOLID_COLOR_PAINT_TYPE)
     {
-        unpack_rgba8(paint.y, color);
+        unpack_rgba8(paintY, color);
         if (!unmultiplied)
         {
             color[0] *= color[3];
@@ -878,7 +999,7 @@ __device__ void fragment(const FlushParams& P,
         t = clamp01(t);
         float x = spanB > 1.f ? (1.f - 1.f / kGradTextureWidth) * t + (.5f / kGradTextureWidth)
                               : (1.f / kGradTextureWidth) * t + spanB;
-        sample_grad(P, x, __uint_as_float(paint.y), color);
+        sample_grad(P, x, __uint_as_float(paintY), color);
         color[3] *= coverage;
         if (!unmultiplied)
         {
@@ -893,18 +1014,11 @@ __device__ void fragment(const FlushParams& P,
     }
 
     float dst[4];
-    if (covBufferID != vPathID)
-    {
-        unpack_rgba8(s.color, dst);
-        s.scratch = s.color;
-    }
-    else
-    {
-        unpack_rgba8(s.scratch, dst);
-    }
+    unpack_rgba8(s.color, dst);
+    s.scratch = s.color;
     if (unmultiplied)
     {
-        uint32_t mode = (paint.x >> 4) & 0xfu;
+        uint32_t mode = (paintX >> 4) & 0xfu;
         if (mode != 0 && (mode < 12 || (features & SF_HSL_BLEND_MODES)))
             advanced_blend(color, dst, mode);
         color[0] *= color[3];
@@ -924,7 +1038,10 @@ __device__ void fragment(const FlushParams& P,
 }
 } // namespace
 
-// One 256-thread CTA per 16x16 tile; thread = pixel; PLS planes in registers.
+// One 256-thread CTA per 16x16 tile. Warp w owns the 8x4 block at
+// (8 * (w & 1), 4 * (w >> 1)) of the tile; each lane owns one pixel and its
+// pixel-local storage in registers. Triangles are walked in primitive order;
+// a warp skips a triangle whose bounding box misses its block.
 __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                                                           uint32_t tilesX,
                                                           const TriRecord* __restrict__ tris,
@@ -935,18 +1052,21 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
     __shared__ TriRecord sTris[256];
     const uint32_t tile = blockIdx.x;
     const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
-    const int px = tx * kTileSize + (threadIdx.x & (kTileSize - 1));
-    const int py = ty * kTileSize + (threadIdx.x >> kTileLog2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bx = tx * kTileSize + (warp & 1) * 8, by = ty * kTileSize + (warp >> 1) * 4;
+    const int px = bx + (lane & 7), py = by + (lane >> 3);
     const bool inBounds = px < (int)P.width && py < (int)P.height;
     const uint2 range = ranges[tile];
     if (range.y <= range.x && !P.loadClear)
         return;
-    Pls s;
-    s.color = P.loadClear ? P.clearColorPremulRGBA
-                          : (inBounds ? fb[(size_t)py * P.width + px] : 0u);
+    Pixel s;
+    s.color = P.loadClear ? P.clearColorPremulRGBA : (inBounds ? fb[(size_t)py * P.width + px] : 0u);
     s.clip = 0;
     s.scratch = 0;
     s.coverage = 0;
+    s.pendMeta = 0;
+    s.pendPaintX = s.pendPaintY = 0;
+    s.pendFrags = 0;
     const float fx = (float)px + .5f, fy = (float)py + .5f;
     // common.glsl:269-274 interleaved gradient noise (depends on the pixel only).
     float v1 = 0.06711056f * fx + 0.00583715f * fy;
@@ -962,25 +1082,54 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
             sTris[threadIdx.x] = tris[sortedSlots[k]];
         __syncthreads();
         const uint32_t n = min(256u, range.y - base);
-        if (inBounds)
+        for (uint32_t i = 0; i < n; ++i)
         {
-            for (uint32_t i = 0; i < n; ++i)
+            const TriRecord& T = sTris[i];
+            const uint4 meta = T.meta;
+            // Warp-uniform reject of triangles whose pixel box misses the block.
+            if ((int)(meta.y >> 16) <= bx || (int)(meta.y & 0xffffu) >= bx + 8 ||
+                (int)(meta.z >> 16) <= by || (int)(meta.z & 0xffffu) >= by + 4)
+                continue;
+            const float4 e0 = T.e0, e1 = T.e1, e2 = T.e2;
+            const float E0 = edge_eval(e0, fx, fy);
+            const float E1 = edge_eval(e1, fx, fy);
+            const float E2 = edge_eval(e2, fx, fy);
+            if (!(edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)) || !inBounds)
+                continue;
+            const float4 c0 = T.cov0, c1 = T.cov1;
+            const float dx = fx - e0.x, dy = fy - e0.y;
+            const float covx = c0.x + c0.y * dx + c0.z * dy;
+            const float covy = c0.w + c1.x * dx + c1.y * dy;
+            const uint32_t paintX = __float_as_uint(c1.z);
+            uint32_t vPathID = id_bits_to_f16(meta.x & 0xffffu, P.pathIDGranularity);
+            if (paintX & PAINT_FLAG_EVEN_ODD_FILL)
+                vPathID ^= 0x8000u;
+            float count;
+            if ((s.coverage >> 16) != vPathID)
             {
-                const TriRecord& T = sTris[i];
-                float E0 = edge_eval(T.e0, fx, fy);
-                float E1 = edge_eval(T.e1, fx, fy);
-                float E2 = edge_eval(T.e2, fx, fy);
-                if (!(edge_inside(T.e0, E0) && edge_inside(T.e1, E1) && edge_inside(T.e2, E2)))
-                    continue;
-                float dx = fx - T.e0.x, dy = fy - T.e0.y;
-                float covx = T.covx.x + T.covx.y * dx + T.covx.z * dy;
-                float covy = T.covy_c + T.covy_gx * dx + T.covy_gy * dy;
-                fragment(P, T.pathAndFeatures & 0xffffu, T.pathAndFeatures >> 16,
-                         covx, covy, fx, fy, dither, s);
+                if (s.pendMeta)
+                    resolve_path(P, s, fx, fy, dither);
+                s.pendMeta = meta.x;
+                s.pendPaintX = paintX;
+                s.pendPaintY = __float_as_uint(c1.w);
+                s.pendFrags = 0;
+                count = 0.f;
             }
+            else
+            {
+                count = h2f(s.coverage & 0xffffu);
+            }
+            if (covy >= 0.f)
+                count = fmaxf(fminf(covx, covy), count); // stroke
+            else
+                count = count + covx; // fill
+            s.coverage = (vPathID << 16) | f2h(count);
+            s.pendFrags = min(s.pendFrags + 1u, 2u);
         }
         __syncthreads();
     }
+    if (s.pendMeta)
+        resolve_path(P, s, fx, fy, dither);
     if (inBounds)
         fb[(size_t)py * P.width + px] = s.color;
 }

@@ -82,22 +82,24 @@ constexpr uint32_t ERR_FEATHER = 1u << 3;
 constexpr uint32_t ERR_COORD_RANGE = 1u << 4;
 constexpr uint32_t ERR_BIN_OVERFLOW = 1u << 5;
 
-// One set-up triangle, ready for the tile raster (80 bytes). Edge k is
+// One set-up triangle, ready for the tile raster (96 bytes). Edge k is
 // E_k(p) = A_k * (p.x - ax_k) + B_k * (p.y - ay_k), positive inside. Each edge
 // is anchored at its canonical endpoint (the same vertex for the two triangles
 // that share the edge), so shared edges evaluate to bitwise-negated values and
 // the fill is watertight. Coverage components are planes anchored at edge 0's
-// anchor: cov(p) = c + gx * (p.x - ax_0) + gy * (p.y - ay_0).
+// anchor: cov(p) = c + gx * (p.x - ax_0) + gy * (p.y - ay_0). The record also
+// carries the path's PaintData words, so the raster never reads them from
+// global memory, and the pixel bounding box for sub-tile rejection.
 struct __align__(16) TriRecord
 {
     float4 e0;   // ax, ay, A, B
     float4 e1;
     float4 e2;
-    float4 covx; // c, gx, gy, unused
-    float covy_c, covy_gx, covy_gy;
-    uint32_t pathAndFeatures; // pathID (16 bits) | shaderFeatures << 16
+    float4 cov0; // covx: c, gx, gy; covy: c
+    float4 cov1; // covy: gx, gy; paint.x, paint.y (as float bits)
+    uint4 meta;  // pathAndFeatures, x0 | x1 << 16, y0 | y1 << 16, unused
 };
-static_assert(sizeof(TriRecord) == 80, "TriRecord layout");
+static_assert(sizeof(TriRecord) == 96, "TriRecord layout");
 
 struct FlushParams
 {
