@@ -117,6 +117,11 @@ typedef struct rive_cuda_flush_desc
     uint32_t first_tess_span;
     uint32_t grad_data_height;
     uint32_t tess_data_height;
+    /* Height the gradient texture was last sized to
+     * (RenderContextImpl::resizeGradientTexture, render_context_impl.hpp:177).
+     * PaintData's gradient row coordinate is normalised to it (gpu.cpp:906-917,
+     * render_context.cpp:1442-1443). 0 means grad_data_height. */
+    uint32_t grad_texture_height;
     uint32_t wireframe;
     uint32_t clockwise_fill_override;
     uint32_t has_triangle_vertices;

@@ -148,6 +148,11 @@ public:
         RenderContextHelperImpl::resizeImageDrawInstanceBuffer(n);
     }
 
+    void resizeGradientTexture(uint32_t width, uint32_t height) override
+    {
+        m_gradTextureHeight = height;
+    }
+
     void flush(const FlushDescriptor& d) override
     {
         FlushRecord rec;
@@ -179,6 +184,7 @@ public:
         o.first_tess_span = static_cast<uint32_t>(d.firstTessVertexSpan);
         o.grad_data_height = d.gradDataHeight;
         o.tess_data_height = d.tessDataHeight;
+        o.grad_texture_height = m_gradTextureHeight;
         o.wireframe = d.wireframe;
         o.clockwise_fill_override = d.clockwiseFillOverride;
         o.has_triangle_vertices = d.hasTriangleVertices;
@@ -204,6 +210,7 @@ public:
     }
 
 private:
+    uint32_t m_gradTextureHeight = 0;
     std::vector<uint8_t>* m_nextStorageSink = &m_discard;
     std::vector<uint8_t>* m_nextVertexSink = &m_discard;
     std::vector<uint8_t> m_discard;

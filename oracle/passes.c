@@ -1228,12 +1228,15 @@ void oracle_advanced_blend(const float srcIn[3],
 /* Bilinear sample of the RGBA8 gradient texture with clamp-to-edge. */
 static void sample_grad(const uint8_t* grad,
                         uint32_t H,
+                        uint32_t textureH,
                         float u,
                         float v,
                         float out[4])
 {
+    /* Normalised coordinates address the whole allocated texture (textureH
+     * rows); only the first H rows hold ramps. */
     float fx = u * GRAD_TEXTURE_WIDTH - .5f;
-    float fy = v * (float)H - .5f;
+    float fy = v * (float)textureH - .5f;
     float x0f = floorf(fx), y0f = floorf(fy);
     float ax = fx - x0f, ay = fy - y0f;
     int x0 = (int)x0f, y0 = (int)y0f;
@@ -1420,7 +1423,10 @@ static void fragment(const frag_ctx* fc,
                       ? (1.f - 1.f / GRAD_TEXTURE_WIDTH) * t + (.5f / GRAD_TEXTURE_WIDTH)
                       : (1.f / GRAD_TEXTURE_WIDTH) * t + spanB;
         float row = u2f(paint[1]);
-        sample_grad(fc->grad, fc->d->grad_data_height, x, row, color);
+        sample_grad(fc->grad, fc->d->grad_data_height,
+                    fc->d->grad_texture_height ? fc->d->grad_texture_height
+                                               : fc->d->grad_data_height,
+                    x, row, color);
         color[3] *= coverage;
         if (!unmultiplied)
         {

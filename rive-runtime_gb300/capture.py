@@ -27,11 +27,11 @@ DESC_FIELDS = (
     "path_count", "first_path", "first_paint", "first_paint_aux",
     "contour_count", "first_contour", "grad_span_count", "first_grad_span",
     "tess_span_count", "first_tess_span", "grad_data_height",
-    "tess_data_height", "wireframe", "clockwise_fill_override",
-    "has_triangle_vertices", "draw_batch_count",
+    "tess_data_height", "grad_texture_height", "wireframe",
+    "clockwise_fill_override", "has_triangle_vertices", "draw_batch_count",
 )
-DESC_STRUCT = struct.Struct("<5I4i19I")
-DESC_SIZE = 120  # 28 fields * 4 = 112, + 8-byte draw_batches pointer (LP64)
+DESC_STRUCT = struct.Struct("<5I4i20I")
+DESC_SIZE = 128  # 29 fields * 4 = 116, pad 4, + 8-byte draw_batches pointer (LP64)
 BATCH_FIELDS = ("draw_type", "element_count", "base_element", "shader_features",
                 "draw_contents", "shader_misc_flags", "first_blend_mode",
                 "barriers")

@@ -291,6 +291,9 @@ int run_flush(rive_cuda_context* ctx,
     P.pathCount = d->path_count;
     P.contourCount = d->contour_count;
     P.gradDataHeight = d->grad_data_height;
+    P.gradTextureHeight = d->grad_texture_height ? d->grad_texture_height
+                          : ctx->gradHeight       ? ctx->gradHeight
+                                                  : d->grad_data_height;
     P.tessDataHeight = d->tess_data_height;
     P.width = d->render_target_width;
     P.height = d->render_target_height;

@@ -857,7 +857,7 @@ __device__ __noinline__ void sample_grad(const FlushParams& P, float u, float v,
     float fx = u * kGradTextureWidth - .5f;
     // The gradient texture always has at least one row allocated.
     const int H = max((int)P.gradDataHeight, 1);
-    float fy = v * (float)P.gradDataHeight - .5f;
+    float fy = v * (float)P.gradTextureHeight - .5f;
     float x0f = floorf(fx), y0f = floorf(fy);
     float ax = fx - x0f, ay = fy - y0f;
     int x0 = (int)x0f, y0 = (int)y0f;

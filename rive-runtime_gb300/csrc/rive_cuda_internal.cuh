@@ -115,6 +115,7 @@ struct FlushParams
     uint32_t firstTessSpan, tessSpanCount;
     uint32_t pathCount, contourCount;
     uint32_t gradDataHeight, tessDataHeight;
+    uint32_t gradTextureHeight; // rows the normalised gradient coordinate spans
     uint32_t width, height;
     uint32_t pathIDGranularity;
     float ditherScale, ditherBias;

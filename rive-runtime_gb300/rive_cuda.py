@@ -36,7 +36,8 @@ class FlushDesc(ctypes.Structure):
             "first_paint", "first_paint_aux", "contour_count", "first_contour",
             "grad_span_count", "first_grad_span", "tess_span_count",
             "first_tess_span", "grad_data_height", "tess_data_height",
-            "wireframe", "clockwise_fill_override", "has_triangle_vertices",
+            "grad_texture_height", "wireframe", "clockwise_fill_override",
+            "has_triangle_vertices",
             "draw_batch_count")] + [("draw_batches", ctypes.c_void_p)]
 
 
