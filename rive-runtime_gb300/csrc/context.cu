@@ -34,14 +34,12 @@ __global__ void patch_setup_kernel(FlushParams P,
                                    uint32_t slotBase,
                                    uint32_t features,
                                    TriRecord* tris,
-                                   uint32_t* tileCounts,
-                                   int4* bboxes);
+                                   uint32_t* tileCounts);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    uint32_t tilesX,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
                                    const uint32_t* offsets,
-                                   const int4* bboxes,
                                    uint32_t* keys,
                                    uint32_t* vals);
 __global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
@@ -113,7 +111,7 @@ struct rive_cuda_context
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
     uint32_t tessWidth = 0, tessHeight = 0, gradWidth = 0, gradHeight = 0;
-    DeviceBuffer tris, tileCounts, offsets, bboxes;
+    DeviceBuffer tris, tileCounts, offsets;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
     uint32_t* dError = nullptr;
     uint32_t* hError = nullptr;  // pinned
@@ -370,7 +368,6 @@ int run_flush(rive_cuda_context* ctx,
             CK(ctx->tris.reserve((size_t)slots * sizeof(TriRecord)));
             CK(ctx->tileCounts.reserve((size_t)slots * 4));
             CK(ctx->offsets.reserve((size_t)slots * 4 + 4));
-            CK(ctx->bboxes.reserve((size_t)slots * sizeof(int4)));
             uint32_t slotBase = 0;
             stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
             for (uint32_t i = 0; i < d->draw_batch_count; ++i)
@@ -380,8 +377,7 @@ int run_flush(rive_cuda_context* ctx,
                     continue;
                 patch_setup_kernel<<<(b.element_count + 3) / 4, 128, 0, stream>>>(
                     P, b.base_element, b.element_count, slotBase, b.shader_features,
-                    (TriRecord*)ctx->tris.ptr, (uint32_t*)ctx->tileCounts.ptr,
-                    (int4*)ctx->bboxes.ptr);
+                    (TriRecord*)ctx->tris.ptr, (uint32_t*)ctx->tileCounts.ptr);
                 ++launches;
                 slotBase += b.element_count * kPatchTriangleCount;
             }
@@ -411,8 +407,7 @@ int run_flush(rive_cuda_context* ctx,
             stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
             bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
                 slots, tilesX, (const TriRecord*)ctx->tris.ptr, (const uint32_t*)ctx->tileCounts.ptr,
-                (const uint32_t*)ctx->offsets.ptr, (const int4*)ctx->bboxes.ptr,
-                (uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->vals.ptr);
+                (const uint32_t*)ctx->offsets.ptr, (uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->vals.ptr);
             stage_end(ctx, stream);
             ++launches;
             int endBit = 1;
@@ -509,7 +504,7 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         r.device.release();
     }
     for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->offsets,
-                            &ctx->bboxes, &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
+                            &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
                             &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges})
         b->release();
     if (ctx->dError)

@@ -335,13 +335,14 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     else
     {
         cov = make_float2(fillCoverage, -1.f);
+        // sign(MUL(outset * norm, inverse(M))): the row vector times the
+        // adjugate, signed by the determinant (no division needed).
         float2 on = make_float2(__fmul_rn(norm.x, outset), __fmul_rn(norm.y, outset));
         float det = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
-        float i00 = __fdiv_rn(M.w, det), i01 = __fdiv_rn(-M.y, det);
-        float i10 = __fdiv_rn(-M.z, det), i11 = __fdiv_rn(M.x, det);
-        float rx = __fadd_rn(__fmul_rn(on.x, i00), __fmul_rn(on.y, i01));
-        float ry = __fadd_rn(__fmul_rn(on.x, i10), __fmul_rn(on.y, i11));
-        offset = make_float2(signf(rx) * kAARadius, signf(ry) * kAARadius);
+        float sd = signf(det);
+        float rx = __fsub_rn(__fmul_rn(on.x, M.w), __fmul_rn(on.y, M.y));
+        float ry = __fsub_rn(__fmul_rn(on.y, M.x), __fmul_rn(on.x, M.z));
+        offset = make_float2(signf(rx) * sd * kAARadius, signf(ry) * sd * kAARadius);
         if (((flags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
             ((flags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
             cov.x = -cov.x;
@@ -436,8 +437,7 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
                                                           uint32_t slotBase,
                                                           uint32_t features,
                                                           TriRecord* __restrict__ tris,
-                                                          uint32_t* __restrict__ tileCounts,
-                                                          int4* __restrict__ bboxes)
+                                                          uint32_t* __restrict__ tileCounts)
 {
     __shared__ VertexOut sv[4][kPatchVertexCount];
     __shared__ float4 sEdges[4][kPatchTriangleCount][3];
@@ -472,39 +472,46 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
         const VertexOut& C = sv[w][ic];
         int4 bb = make_int4(0, 0, 0, 0);
         bool valid = sok[w] && !A.discard && !B.discard && !C.discard;
-        float2 p0, p1, p2;
+        // Snap to the rasteriser's 1/256-pixel grid in integers.
+        int X0 = 0, Y0 = 0, X1 = 0, Y1 = 0, X2 = 0, Y2 = 0;
         if (valid)
         {
-            p0 = make_float2(snap(A.pos.x), snap(A.pos.y));
-            p1 = make_float2(snap(B.pos.x), snap(B.pos.y));
-            p2 = make_float2(snap(C.pos.x), snap(C.pos.y));
-            float m = fmaxf(fmaxf(fmaxf(fabsf(p0.x), fabsf(p0.y)), fmaxf(fabsf(p1.x), fabsf(p1.y))),
-                            fmaxf(fabsf(p2.x), fabsf(p2.y)));
+            float m = fmaxf(fmaxf(fmaxf(fabsf(A.pos.x), fabsf(A.pos.y)),
+                                  fmaxf(fabsf(B.pos.x), fabsf(B.pos.y))),
+                            fmaxf(fabsf(C.pos.x), fabsf(C.pos.y)));
             if (!(m < 32768.f)) // NaN or outside the exact snapping range
             {
                 if (!isnan(m))
                     atomicOr(P.error, ERR_COORD_RANGE);
                 valid = false;
             }
+            else
+            {
+                X0 = __float2int_rn(A.pos.x * 256.f);
+                Y0 = __float2int_rn(A.pos.y * 256.f);
+                X1 = __float2int_rn(B.pos.x * 256.f);
+                Y1 = __float2int_rn(B.pos.y * 256.f);
+                X2 = __float2int_rn(C.pos.x * 256.f);
+                Y2 = __float2int_rn(C.pos.y * 256.f);
+            }
         }
-        double area2 = 0.0;
+        long long area2 = 0;
         if (valid)
         {
-            // Exact: coordinates are multiples of 1/256 below 2^15.
-            double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
-            double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
-            area2 = d1x * d2y - d2x * d1y;
-            valid = area2 > 0.0; // counterclockwise culled, degenerate dropped
+            // Exact twice-area in 1/65536 px^2: counterclockwise culled,
+            // degenerate dropped.
+            area2 = (long long)(X1 - X0) * (Y2 - Y0) - (long long)(X2 - X0) * (Y1 - Y0);
+            valid = area2 > 0;
         }
         if (valid)
         {
-            float minx = fminf(fminf(p0.x, p1.x), p2.x), maxx = fmaxf(fmaxf(p0.x, p1.x), p2.x);
-            float miny = fminf(fminf(p0.y, p1.y), p2.y), maxy = fmaxf(fmaxf(p0.y, p1.y), p2.y);
-            // Pixels whose centres k + 1/2 lie inside [min, max].
-            int bx0 = max((int)ceilf(minx - .5f), 0);
-            int bx1 = min((int)floorf(maxx - .5f) + 1, (int)P.width);
-            int by0 = max((int)ceilf(miny - .5f), 0);
-            int by1 = min((int)floorf(maxy - .5f) + 1, (int)P.height);
+            const int mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
+            const int mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
+            // Pixels k whose centres (256 k + 128) lie in [min, max].
+            int bx0 = max(-((-(mnx - 128)) >> 8), 0);
+            int bx1 = min(((mxx - 128) >> 8) + 1, (int)P.width);
+            int by0 = max(-((-(mny - 128)) >> 8), 0);
+            int by1 = min(((mxy - 128) >> 8) + 1, (int)P.height);
             if (bx0 >= bx1 || by0 >= by1)
                 valid = false;
             else
@@ -512,31 +519,25 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
         }
         if (valid)
         {
+            const float s = 1.f / 256.f;
+            const float2 p0 = make_float2(X0 * s, Y0 * s), p1 = make_float2(X1 * s, Y1 * s);
+            const float2 p2 = make_float2(X2 * s, Y2 * s);
             TriRecord T;
             T.e0 = make_edge(p0, p1);
             T.e1 = make_edge(p1, p2);
             T.e2 = make_edge(p2, p0);
-            double d1x = (double)p1.x - p0.x, d1y = (double)p1.y - p0.y;
-            double d2x = (double)p2.x - p0.x, d2y = (double)p2.y - p0.y;
-            double inv = 1.0 / area2;
-            double ax = (double)T.e0.x - p0.x, ay = (double)T.e0.y - p0.y;
-            double cxc, cxgx, cxgy, cyc, cygx, cygy;
-            {
-                double c0 = A.cov.x, c1 = B.cov.x, c2 = C.cov.x;
-                cxgx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
-                cxgy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
-                cxc = c0 + cxgx * ax + cxgy * ay;
-            }
-            {
-                double c0 = A.cov.y, c1 = B.cov.y, c2 = C.cov.y;
-                cygx = ((c1 - c0) * d2y - (c2 - c0) * d1y) * inv;
-                cygy = ((c2 - c0) * d1x - (c1 - c0) * d2x) * inv;
-                cyc = c0 + cygx * ax + cygy * ay;
-            }
+            const float d1x = p1.x - p0.x, d1y = p1.y - p0.y;
+            const float d2x = p2.x - p0.x, d2y = p2.y - p0.y;
+            const float inv = 1.f / ((float)area2 * (s * s));
+            const float ax = T.e0.x - p0.x, ay = T.e0.y - p0.y;
+            const float cxgx = ((B.cov.x - A.cov.x) * d2y - (C.cov.x - A.cov.x) * d1y) * inv;
+            const float cxgy = ((C.cov.x - A.cov.x) * d1x - (B.cov.x - A.cov.x) * d2x) * inv;
+            const float cygx = ((B.cov.y - A.cov.y) * d2y - (C.cov.y - A.cov.y) * d1y) * inv;
+            const float cygy = ((C.cov.y - A.cov.y) * d1x - (B.cov.y - A.cov.y) * d2x) * inv;
             const uint2 paint = P.paints[P.firstPaint + A.pathID];
-            T.cov0 = make_float4((float)cxc, (float)cxgx, (float)cxgy, (float)cyc);
-            T.cov1 = make_float4((float)cygx, (float)cygy, __uint_as_float(paint.x),
-                                 __uint_as_float(paint.y));
+            T.cov0 = make_float4(A.cov.x + cxgx * ax + cxgy * ay, cxgx, cxgy,
+                                 A.cov.y + cygx * ax + cygy * ay);
+            T.cov1 = make_float4(cygx, cygy, __uint_as_float(paint.x), __uint_as_float(paint.y));
             T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16),
                                 (uint32_t)bb.x | ((uint32_t)bb.z << 16),
                                 (uint32_t)bb.y | ((uint32_t)bb.w << 16), 0u);
@@ -568,7 +569,6 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
                     for (int tx = tx0; tx < tx0 + ntx; ++tx)
                         count += tile_overlaps(e, bb, tx, ty) ? 1u : 0u;
                 tileCounts[slot0 + lane] = count;
-                bboxes[slot0 + lane] = count ? bb : make_int4(0, 0, 0, 0);
             }
             else
             {
@@ -578,7 +578,6 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
         else
         {
             tileCounts[slot0 + lane] = 0;
-            bboxes[slot0 + lane] = make_int4(0, 0, 0, 0);
         }
     }
     uint32_t big = __ballot_sync(0xffffffffu, bigMask != 0);
@@ -601,7 +600,6 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
         if (lane == 0)
         {
             tileCounts[slot0 + t] = count;
-            bboxes[slot0 + t] = count ? bb : make_int4(0, 0, 0, 0);
         }
     }
 }
@@ -615,7 +613,6 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ tileCounts,
                                                           const uint32_t* __restrict__ offsets,
-                                                          const int4* __restrict__ bboxes,
                                                           uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals)
 {
@@ -630,7 +627,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
     bool isBig = false;
     if (myCount)
     {
-        const int4 bb = bboxes[mySlot];
+        const int4 bb = unpack_bbox(tris[mySlot].meta);
         const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
         const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
         const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
@@ -659,7 +656,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         const int t = __ffs(pending) - 1;
         pending &= pending - 1;
         const uint32_t slot = first + t;
-        const int4 bb = bboxes[slot];
+        const int4 bb = unpack_bbox(tris[slot].meta);
         const TriRecord* T = tris + slot;
         const float4 e[3] = {T->e0, T->e1, T->e2};
         uint32_t o = offsets[slot];
@@ -1050,6 +1047,7 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                                                           uint32_t* __restrict__ fb)
 {
     __shared__ TriRecord sTris[256];
+    __shared__ uint8_t sMask[256];
     const uint32_t tile = blockIdx.x;
     const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1077,54 +1075,77 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
 
     for (uint32_t base = range.x; base < range.y; base += 256)
     {
+        // Each thread stages one triangle and marks which of the tile's eight
+        // 8x4 warp blocks hold a pixel centre it may cover (exact corner test
+        // per block, so a cleared bit is never a missed pixel).
         const uint32_t k = base + threadIdx.x;
+        uint32_t m = 0;
         if (k < range.y)
-            sTris[threadIdx.x] = tris[sortedSlots[k]];
+        {
+            const TriRecord T = tris[sortedSlots[k]];
+            sTris[threadIdx.x] = T;
+            const int4 bb = unpack_bbox(T.meta);
+            const float4 e[3] = {T.e0, T.e1, T.e2};
+#pragma unroll
+            for (int b = 0; b < 8; ++b)
+            {
+                const int qx = tx * kTileSize + (b & 1) * 8, qy = ty * kTileSize + (b >> 1) * 4;
+                const int x0 = max(bb.x, qx), x1 = min(bb.z, qx + 8);
+                const int y0 = max(bb.y, qy), y1 = min(bb.w, qy + 4);
+                if (x0 < x1 && y0 < y1 && rect_overlaps(e, x0, x1, y0, y1))
+                    m |= 1u << b;
+            }
+        }
+        sMask[threadIdx.x] = (uint8_t)m;
         __syncthreads();
         const uint32_t n = min(256u, range.y - base);
-        for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t g = 0; g < n; g += 32)
         {
-            const TriRecord& T = sTris[i];
-            const uint4 meta = T.meta;
-            // Warp-uniform reject of triangles whose pixel box misses the block.
-            if ((int)(meta.y >> 16) <= bx || (int)(meta.y & 0xffffu) >= bx + 8 ||
-                (int)(meta.z >> 16) <= by || (int)(meta.z & 0xffffu) >= by + 4)
-                continue;
-            const float4 e0 = T.e0, e1 = T.e1, e2 = T.e2;
-            const float E0 = edge_eval(e0, fx, fy);
-            const float E1 = edge_eval(e1, fx, fy);
-            const float E2 = edge_eval(e2, fx, fy);
-            if (!(edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)) || !inBounds)
-                continue;
-            const float4 c0 = T.cov0, c1 = T.cov1;
-            const float dx = fx - e0.x, dy = fy - e0.y;
-            const float covx = c0.x + c0.y * dx + c0.z * dy;
-            const float covy = c0.w + c1.x * dx + c1.y * dy;
-            const uint32_t paintX = __float_as_uint(c1.z);
-            uint32_t vPathID = id_bits_to_f16(meta.x & 0xffffu, P.pathIDGranularity);
-            if (paintX & PAINT_FLAG_EVEN_ODD_FILL)
-                vPathID ^= 0x8000u;
-            float count;
-            if ((s.coverage >> 16) != vPathID)
+            // Triangles of this group touching this warp's block, in order.
+            uint32_t bits = __ballot_sync(0xffffffffu, (sMask[g + lane] >> warp) & 1u);
+            while (bits)
             {
-                if (s.pendMeta)
-                    resolve_path(P, s, fx, fy, dither);
-                s.pendMeta = meta.x;
-                s.pendPaintX = paintX;
-                s.pendPaintY = __float_as_uint(c1.w);
-                s.pendFrags = 0;
-                count = 0.f;
+                const uint32_t i = g + (uint32_t)(__ffs(bits) - 1);
+                bits &= bits - 1;
+                const TriRecord& T = sTris[i];
+                const float4 e0 = T.e0, e1 = T.e1, e2 = T.e2;
+                const float E0 = edge_eval(e0, fx, fy);
+                const float E1 = edge_eval(e1, fx, fy);
+                const float E2 = edge_eval(e2, fx, fy);
+                if (!(edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)) ||
+                    !inBounds)
+                    continue;
+                const uint32_t metaX = T.meta.x;
+                const float4 c0 = T.cov0, c1 = T.cov1;
+                const float dx = fx - e0.x, dy = fy - e0.y;
+                const float covx = c0.x + c0.y * dx + c0.z * dy;
+                const float covy = c0.w + c1.x * dx + c1.y * dy;
+                const uint32_t paintX = __float_as_uint(c1.z);
+                uint32_t vPathID = id_bits_to_f16(metaX & 0xffffu, P.pathIDGranularity);
+                if (paintX & PAINT_FLAG_EVEN_ODD_FILL)
+                    vPathID ^= 0x8000u;
+                float count;
+                if ((s.coverage >> 16) != vPathID)
+                {
+                    if (s.pendMeta)
+                        resolve_path(P, s, fx, fy, dither);
+                    s.pendMeta = metaX;
+                    s.pendPaintX = paintX;
+                    s.pendPaintY = __float_as_uint(c1.w);
+                    s.pendFrags = 0;
+                    count = 0.f;
+                }
+                else
+                {
+                    count = h2f(s.coverage & 0xffffu);
+                }
+                if (covy >= 0.f)
+                    count = fmaxf(fminf(covx, covy), count); // stroke
+                else
+                    count = count + covx; // fill
+                s.coverage = (vPathID << 16) | f2h(count);
+                s.pendFrags = min(s.pendFrags + 1u, 2u);
             }
-            else
-            {
-                count = h2f(s.coverage & 0xffffu);
-            }
-            if (covy >= 0.f)
-                count = fmaxf(fminf(covx, covy), count); // stroke
-            else
-                count = count + covx; // fill
-            s.coverage = (vPathID << 16) | f2h(count);
-            s.pendFrags = min(s.pendFrags + 1u, 2u);
         }
         __syncthreads();
     }
