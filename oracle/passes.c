@@ -8,6 +8,15 @@
  * -ffp-contract=off), with libm for acos/sin/cos/sqrt. `half` values of the
  * shaders are computed in fp32 (desktop mediump) and rounded to fp16 exactly
  * where the shaders pack them into pixel local storage (packHalf2x16).
+ *
+ * What pins it: its inputs are the reference front end's own records
+ * (captured from the compiled reference, byte for byte); the advanced blend
+ * functions reproduce the known answers of the reference's
+ * advanced_blend_test.cpp; tessellated vertices agree with an FP64 twin of
+ * the same segment parameters. The composed pixels themselves have no
+ * reference output to compare with (the reference ships no pixel goldens and
+ * its GPU backends need a graphics API, which none of the machines this runs
+ * on provides): for the final images this oracle is "parity unpinned".
  */
 #include "passes.h"
 

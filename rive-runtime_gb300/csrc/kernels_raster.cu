@@ -538,9 +538,15 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
             T.cov0 = make_float4(A.cov.x + cxgx * ax + cxgy * ay, cxgx, cxgy,
                                  A.cov.y + cygx * ax + cygy * ay);
             T.cov1 = make_float4(cygx, cygy, __uint_as_float(paint.x), __uint_as_float(paint.y));
+            // The fp16 coverage key of the path (draw_raster_order_path.frag:
+            // pathID bits, sign bit flipped for even-odd fills).
+            uint32_t key = A.pathID == 0 ? 0u
+                                         : ((A.pathID + MAX_DENORM_F16) * P.pathIDGranularity) & 0xffffu;
+            if (paint.x & PAINT_FLAG_EVEN_ODD_FILL)
+                key ^= 0x8000u;
             T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16),
                                 (uint32_t)bb.x | ((uint32_t)bb.z << 16),
-                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), 0u);
+                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), key);
             tris[slot0 + lane] = T;
             sEdges[w][lane][0] = T.e0;
             sEdges[w][lane][1] = T.e1;
@@ -1072,6 +1078,7 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
     float v2 = 52.9829189f * v1;
     v2 = v2 - floorf(v2);
     const float dither = v2 * P.ditherScale + P.ditherBias;
+    uint32_t streamPath = 0xffffffffu; // coverage key of the warp's current path
 
     for (uint32_t base = range.x; base < range.y; base += 256)
     {
@@ -1108,12 +1115,29 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                 const uint32_t i = g + (uint32_t)(__ffs(bits) - 1);
                 bits &= bits - 1;
                 const TriRecord& T = sTris[i];
+                const uint32_t vPathID = T.meta.w;
+                // A path's triangles are contiguous in primitive order, so when
+                // the warp's stream moves to another path every pixel still
+                // holding the previous path's coverage has seen all of it:
+                // resolve them together (one convergent call per path).
+                if (vPathID != streamPath)
+                {
+                    if (s.pendMeta)
+                    {
+                        resolve_path(P, s, fx, fy, dither);
+                        s.pendMeta = 0;
+                    }
+                    streamPath = vPathID;
+                }
                 const float4 e0 = T.e0, e1 = T.e1, e2 = T.e2;
                 const float E0 = edge_eval(e0, fx, fy);
                 const float E1 = edge_eval(e1, fx, fy);
                 const float E2 = edge_eval(e2, fx, fy);
-                if (!(edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)) ||
-                    !inBounds)
+                const float emin = fminf(fminf(E0, E1), E2);
+                if (!(emin > 0.f) &&
+                    !(emin == 0.f && edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)))
+                    continue;
+                if (!inBounds)
                     continue;
                 const uint32_t metaX = T.meta.x;
                 const float4 c0 = T.cov0, c1 = T.cov1;
@@ -1121,9 +1145,6 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                 const float covx = c0.x + c0.y * dx + c0.z * dy;
                 const float covy = c0.w + c1.x * dx + c1.y * dy;
                 const uint32_t paintX = __float_as_uint(c1.z);
-                uint32_t vPathID = id_bits_to_f16(metaX & 0xffffu, P.pathIDGranularity);
-                if (paintX & PAINT_FLAG_EVEN_ODD_FILL)
-                    vPathID ^= 0x8000u;
                 float count;
                 if ((s.coverage >> 16) != vPathID)
                 {
@@ -1138,6 +1159,12 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                 else
                 {
                     count = h2f(s.coverage & 0xffffu);
+                    if (!s.pendMeta) // the key's path came back after a resolve
+                    {
+                        s.pendMeta = metaX;
+                        s.pendPaintX = paintX;
+                        s.pendPaintY = __float_as_uint(c1.w);
+                    }
                 }
                 if (covy >= 0.f)
                     count = fmaxf(fminf(covx, covy), count); // stroke
