@@ -1,0 +1,207 @@
+/*
+ * abi_recorder.c -- TEST INFRASTRUCTURE (oracle). A recording stand-in for
+ * the rive_cuda.h entry points that RenderContextCUDAImpl calls: it runs no
+ * GPU work, keeps the bytes each record buffer holds at unmap and every
+ * flush descriptor with its draw batches, and writes them in the capture
+ * layout of ref_capture.cpp. Linked with the reference front end and the
+ * product's RenderContextCUDAImpl, it shows that the backend hands the
+ * C ABI exactly what the reference's RenderContext produced.
+ */
+#include "rive_cuda.h"
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define KINDS RIVE_CUDA_BUFFER_KIND_COUNT
+#define CAPTURED_KINDS 7 /* flush uniforms .. tess spans */
+#define MAX_FLUSHES 256
+
+struct rive_cuda_context
+{
+    unsigned char* staging[KINDS];
+    size_t capacity[KINDS];
+    unsigned char* data[KINDS]; /* bytes at the last unmap */
+    size_t bytes[KINDS];
+    uint32_t flush_count;
+    rive_cuda_flush_desc descs[MAX_FLUSHES];
+    rive_cuda_draw_batch* batches[MAX_FLUSHES];
+    uint32_t width, height;
+    int failed;
+};
+
+struct rive_cuda_render_target
+{
+    uint32_t width, height;
+};
+
+static rive_cuda_context* g_last; /* the context abi_recorder_write dumps */
+
+int rive_cuda_context_create(int device, rive_cuda_context** out)
+{
+    (void)device;
+    if (!out)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *out = (rive_cuda_context*)calloc(1, sizeof(rive_cuda_context));
+    g_last = *out;
+    return *out ? RIVE_CUDA_OK : RIVE_CUDA_ERR_OUT_OF_MEMORY;
+}
+
+void rive_cuda_context_destroy(rive_cuda_context* ctx)
+{
+    if (!ctx)
+        return;
+    for (int k = 0; k < KINDS; ++k)
+    {
+        free(ctx->staging[k]);
+        free(ctx->data[k]);
+    }
+    for (uint32_t i = 0; i < ctx->flush_count; ++i)
+        free(ctx->batches[i]);
+    if (g_last == ctx)
+        g_last = NULL;
+    free(ctx);
+}
+
+int rive_cuda_last_error(const rive_cuda_context* ctx, char* buf, size_t len)
+{
+    (void)ctx;
+    if (buf && len)
+        buf[0] = 0;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_resize_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
+{
+    if (!ctx || kind < 0 || kind >= KINDS)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    free(ctx->staging[kind]);
+    ctx->staging[kind] = bytes ? (unsigned char*)malloc(bytes) : NULL;
+    ctx->capacity[kind] = bytes;
+    return RIVE_CUDA_OK;
+}
+
+void* rive_cuda_map_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
+{
+    if (!ctx || kind < 0 || kind >= KINDS || bytes > ctx->capacity[kind] || !ctx->staging[kind])
+        return NULL;
+    /* Zeroed, as ref_capture's rings are, so skipped padding compares equal. */
+    memset(ctx->staging[kind], 0, bytes);
+    return ctx->staging[kind];
+}
+
+int rive_cuda_unmap_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
+{
+    if (!ctx || kind < 0 || kind >= KINDS)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    free(ctx->data[kind]);
+    ctx->data[kind] = (unsigned char*)malloc(bytes ? bytes : 1);
+    if (bytes)
+        memcpy(ctx->data[kind], ctx->staging[kind], bytes);
+    ctx->bytes[kind] = bytes;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_resize_gradient_texture(rive_cuda_context* ctx, uint32_t w, uint32_t h)
+{
+    (void)ctx, (void)w, (void)h;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_resize_tessellation_texture(rive_cuda_context* ctx, uint32_t w, uint32_t h)
+{
+    (void)ctx, (void)w, (void)h;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_render_target_create(rive_cuda_context* ctx,
+                                   uint32_t width,
+                                   uint32_t height,
+                                   rive_cuda_render_target** out)
+{
+    if (!ctx || !out)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *out = (rive_cuda_render_target*)calloc(1, sizeof(rive_cuda_render_target));
+    (*out)->width = width;
+    (*out)->height = height;
+    ctx->width = width;
+    ctx->height = height;
+    return RIVE_CUDA_OK;
+}
+
+void rive_cuda_render_target_destroy(rive_cuda_context* ctx, rive_cuda_render_target* t)
+{
+    (void)ctx;
+    free(t);
+}
+
+void* rive_cuda_render_target_device_ptr(rive_cuda_render_target* t)
+{
+    (void)t;
+    return NULL;
+}
+
+int rive_cuda_render_target_read(rive_cuda_context* ctx,
+                                 rive_cuda_render_target* t,
+                                 void* dst,
+                                 void* stream)
+{
+    (void)ctx, (void)t, (void)dst, (void)stream;
+    return RIVE_CUDA_ERR_UNSUPPORTED;
+}
+
+int rive_cuda_flush(rive_cuda_context* ctx,
+                    const rive_cuda_flush_desc* desc,
+                    rive_cuda_render_target* target,
+                    void* stream)
+{
+    (void)target, (void)stream;
+    if (!ctx || !desc || ctx->flush_count >= MAX_FLUSHES)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    uint32_t i = ctx->flush_count++;
+    ctx->descs[i] = *desc;
+    ctx->descs[i].draw_batches = NULL;
+    size_t n = desc->draw_batch_count;
+    ctx->batches[i] = (rive_cuda_draw_batch*)malloc(n ? n * sizeof(rive_cuda_draw_batch) : 1);
+    if (n)
+        memcpy(ctx->batches[i], desc->draw_batches, n * sizeof(rive_cuda_draw_batch));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_sync(rive_cuda_context* ctx, void* stream)
+{
+    (void)ctx, (void)stream;
+    return RIVE_CUDA_OK;
+}
+
+/* Writes the recording of the most recently created context. */
+int abi_recorder_write(const char* path)
+{
+    rive_cuda_context* ctx = g_last;
+    if (!ctx)
+        return 1;
+    FILE* f = fopen(path, "wb");
+    if (!f)
+        return 1;
+    uint32_t head[4] = {0x31504352u /* RCP1 */, ctx->width, ctx->height, CAPTURED_KINDS};
+    fwrite(head, sizeof(head), 1, f);
+    static const unsigned char zeros[8] = {0};
+    for (int k = 0; k < CAPTURED_KINDS; ++k)
+    {
+        uint64_t n = ctx->bytes[k];
+        fwrite(&n, sizeof(n), 1, f);
+        if (n)
+            fwrite(ctx->data[k], 1, n, f);
+        fwrite(zeros, 1, (8 - (n & 7)) & 7, f);
+    }
+    fwrite(&ctx->flush_count, sizeof(uint32_t), 1, f);
+    for (uint32_t i = 0; i < ctx->flush_count; ++i)
+    {
+        fwrite(&ctx->descs[i], sizeof(rive_cuda_flush_desc), 1, f);
+        if (ctx->descs[i].draw_batch_count)
+            fwrite(ctx->batches[i], sizeof(rive_cuda_draw_batch), ctx->descs[i].draw_batch_count,
+                   f);
+    }
+    fclose(f);
+    return 0;
+}

@@ -23,15 +23,10 @@
 #include "rive/renderer/texture.hpp"
 #include "common/render_context_null.hpp"
 #include "rive/renderer/render_context.hpp"
-#include "rive/renderer/rive_renderer.hpp"
 #include "rive/renderer/gpu.hpp"
-#include "rive/math/raw_path.hpp"
-#include "rive/shapes/paint/blend_mode.hpp"
-#include "rive/shapes/paint/stroke_cap.hpp"
-#include "rive/shapes/paint/stroke_join.hpp"
 
 #include "rive_cuda.h"
-#include "rive_scene.h"
+#include "scene_replay.hpp"
 
 #include <cstdio>
 #include <cstdlib>
@@ -247,150 +242,15 @@ int main(int argc, char** argv)
     std::vector<uint8_t> scene = read_file(argv[1]);
     if (scene.size() < sizeof(rive_scene_header))
         return fail("cannot read scene");
-    rive_scene_header hdr;
-    memcpy(&hdr, scene.data(), sizeof(hdr));
-    if (hdr.magic != RIVE_SCENE_MAGIC)
-        return fail("bad scene magic");
-    size_t off = sizeof(hdr);
-    auto* paths = reinterpret_cast<const rive_scene_path*>(scene.data() + off);
-    off += sizeof(rive_scene_path) * hdr.path_count;
-    auto* paints = reinterpret_cast<const rive_scene_paint*>(scene.data() + off);
-    off += sizeof(rive_scene_paint) * hdr.paint_count;
-    auto* cmds = reinterpret_cast<const rive_scene_cmd*>(scene.data() + off);
-    off += sizeof(rive_scene_cmd) * hdr.cmd_count;
-    const uint8_t* verbs = scene.data() + off;
-    off += (hdr.verb_count + 3u) & ~3u;
-    auto* points = reinterpret_cast<const float*>(scene.data() + off);
-    off += sizeof(float) * 2 * hdr.point_count;
-    auto* stops = reinterpret_cast<const rive_scene_stop*>(scene.data() + off);
-    off += sizeof(rive_scene_stop) * hdr.stop_count;
-    if (off > scene.size())
-        return fail("truncated scene");
-
     CaptureImpl* impl = nullptr;
     std::unique_ptr<RenderContext> ctx = CaptureImpl::Make(&impl);
-
-    std::vector<rcp<RenderPath>> renderPaths;
-    for (uint32_t i = 0; i < hdr.path_count; ++i)
-    {
-        const rive_scene_path& p = paths[i];
-        RawPath raw;
-        const float* pts = points + 2 * p.point_offset;
-        for (uint32_t v = 0; v < p.verb_count; ++v)
-        {
-            switch (verbs[p.verb_offset + v])
-            {
-                case RIVE_SCENE_VERB_MOVE:
-                    raw.move({pts[0], pts[1]});
-                    pts += 2;
-                    break;
-                case RIVE_SCENE_VERB_LINE:
-                    raw.line({pts[0], pts[1]});
-                    pts += 2;
-                    break;
-                case RIVE_SCENE_VERB_QUAD:
-                    raw.quad({pts[0], pts[1]}, {pts[2], pts[3]});
-                    pts += 4;
-                    break;
-                case RIVE_SCENE_VERB_CUBIC:
-                    raw.cubic({pts[0], pts[1]},
-                              {pts[2], pts[3]},
-                              {pts[4], pts[5]});
-                    pts += 6;
-                    break;
-                case RIVE_SCENE_VERB_CLOSE:
-                    raw.close();
-                    break;
-                default:
-                    return fail("bad verb");
-            }
-        }
-        renderPaths.push_back(
-            ctx->makeRenderPath(raw, static_cast<FillRule>(p.fill_rule)));
-    }
-
-    std::vector<rcp<RenderPaint>> renderPaints;
-    for (uint32_t i = 0; i < hdr.paint_count; ++i)
-    {
-        const rive_scene_paint& s = paints[i];
-        rcp<RenderPaint> paint = ctx->makeRenderPaint();
-        paint->style(s.style == RIVE_SCENE_STYLE_FILL ? RenderPaintStyle::fill
-                                                      : RenderPaintStyle::stroke);
-        paint->color(s.color);
-        paint->thickness(s.thickness);
-        paint->join(static_cast<StrokeJoin>(s.join));
-        paint->cap(static_cast<StrokeCap>(s.cap));
-        paint->blendMode(static_cast<BlendMode>(s.blend_mode));
-        if (s.shader != RIVE_SCENE_SHADER_NONE)
-        {
-            std::vector<ColorInt> colors(s.stop_count);
-            std::vector<float> pos(s.stop_count);
-            for (uint32_t k = 0; k < s.stop_count; ++k)
-            {
-                colors[k] = stops[s.stop_offset + k].color;
-                pos[k] = stops[s.stop_offset + k].position;
-            }
-            rcp<RenderShader> shader =
-                s.shader == RIVE_SCENE_SHADER_LINEAR
-                    ? ctx->makeLinearGradient(s.g[0],
-                                              s.g[1],
-                                              s.g[2],
-                                              s.g[3],
-                                              colors.data(),
-                                              pos.data(),
-                                              s.stop_count)
-                    : ctx->makeRadialGradient(s.g[0],
-                                              s.g[1],
-                                              s.g[2],
-                                              colors.data(),
-                                              pos.data(),
-                                              s.stop_count);
-            paint->shader(shader);
-        }
-        renderPaints.push_back(paint);
-    }
-
-    rcp<RenderTarget> target =
-        impl->makeRenderTarget(hdr.width, hdr.height);
-    RenderContext::FrameDescriptor fd;
-    fd.renderTargetWidth = hdr.width;
-    fd.renderTargetHeight = hdr.height;
-    fd.loadAction = LoadAction::clear;
-    fd.clearColor = hdr.clear_color;
-    fd.ditherMode = static_cast<DitherMode>(hdr.dither_mode);
-    // Never triangulate: midpoint fans for every fill, independent of timing.
-    fd.triangulationThresholds.frameBudgetMs = 0;
-    ctx->beginFrame(fd);
-    {
-        RiveRenderer renderer(ctx.get());
-        for (uint32_t i = 0; i < hdr.cmd_count; ++i)
-        {
-            const rive_scene_cmd& c = cmds[i];
-            switch (c.op)
-            {
-                case RIVE_SCENE_CMD_SAVE:
-                    renderer.save();
-                    break;
-                case RIVE_SCENE_CMD_RESTORE:
-                    renderer.restore();
-                    break;
-                case RIVE_SCENE_CMD_TRANSFORM:
-                    renderer.transform(
-                        Mat2D(c.m[0], c.m[1], c.m[2], c.m[3], c.m[4], c.m[5]));
-                    break;
-                case RIVE_SCENE_CMD_DRAW_PATH:
-                    renderer.drawPath(renderPaths[c.a].get(),
-                                      renderPaints[c.b].get());
-                    break;
-                case RIVE_SCENE_CMD_CLIP_PATH:
-                    renderer.clipPath(renderPaths[c.a].get());
-                    break;
-                default:
-                    return fail("bad command");
-            }
-        }
-    }
-    ctx->flush({.renderTarget = target.get()});
+    const char* err = replay_scene(ctx.get(), scene, [&](uint32_t w, uint32_t h) {
+        return rcp<RenderTarget>(impl->makeRenderTarget(w, h));
+    });
+    if (err)
+        return fail(err);
+    rive_scene_header hdr;
+    memcpy(&hdr, scene.data(), sizeof(hdr));
 
     FILE* f = fopen(argv[2], "wb");
     if (!f)

@@ -17,6 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "_build", "liboracle_passes.so")
 REF_CAPTURE = os.path.join(HERE, "_ref", "ref_capture")
+ADAPTER_CAPTURE = os.path.join(HERE, "_ref", "adapter_capture")
 REFERENCE_SOURCES = "/root/reference"
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
@@ -171,15 +172,26 @@ def build_reference():
     subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"])
 
 
-def reference_capture(scene_bytes: bytes) -> bytes:
-    """Runs the reference front end on a scene; returns the capture bytes."""
-    if not os.path.exists(REF_CAPTURE):
-        build_reference()
+def _run_capture(tool: str, scene_bytes: bytes) -> bytes:
     with tempfile.TemporaryDirectory() as td:
         sp = os.path.join(td, "scene.bin")
         cp = os.path.join(td, "capture.bin")
         with open(sp, "wb") as f:
             f.write(scene_bytes)
-        subprocess.check_call([REF_CAPTURE, sp, cp])
+        subprocess.check_call([tool, sp, cp])
         with open(cp, "rb") as f:
             return f.read()
+
+
+def reference_capture(scene_bytes: bytes) -> bytes:
+    """Runs the reference front end on a scene; returns the capture bytes."""
+    if not os.path.exists(REF_CAPTURE):
+        build_reference()
+    return _run_capture(REF_CAPTURE, scene_bytes)
+
+
+def adapter_capture(scene_bytes: bytes) -> bytes:
+    """Runs the reference front end into the product's RenderContextCUDAImpl
+    over the recording C ABI; returns what reached the ABI as a capture."""
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "adapter"])
+    return _run_capture(ADAPTER_CAPTURE, scene_bytes)

@@ -1,0 +1,260 @@
+// RenderContextCUDAImpl (render_context_cuda_impl.hpp): each RenderContextImpl
+// call becomes one rive_cuda.h call. Buffer kinds follow the order of the
+// resize/map/unmap families in render_context_impl.hpp:108-174; the flush
+// descriptor and draw list are copied field by field into
+// rive_cuda_flush_desc / rive_cuda_draw_batch (gpu.hpp:1219-1282, 1320-1438)
+// before RenderContext frees them (render_context.cpp:1028).
+#include "render_context_cuda_impl.hpp"
+
+#include "rive/renderer/gpu.hpp"
+#include "rive/renderer/render_context.hpp"
+#include "rive/renderer/texture.hpp"
+#include "rive/gpu_texture_format.hpp"
+#include "rive/renderer.hpp"
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+namespace rive::gpu
+{
+namespace
+{
+// Host memory for RenderBuffers (vertex/index data of image meshes, which
+// this backend does not draw; kept so Factory calls still succeed).
+class HostRenderBuffer : public RenderBuffer
+{
+public:
+    HostRenderBuffer(RenderBufferType type, RenderBufferFlags flags, size_t bytes) :
+        RenderBuffer(type, flags, bytes), m_bytes(bytes)
+    {}
+
+protected:
+    void* onMap() override { return m_bytes.data(); }
+    void onUnmap() override {}
+
+private:
+    std::vector<uint8_t> m_bytes;
+};
+} // namespace
+
+RenderTargetCUDA::RenderTargetCUDA(rive_cuda_context* ctx,
+                                   rive_cuda_render_target* target,
+                                   uint32_t width,
+                                   uint32_t height) :
+    RenderTarget(width, height), m_ctx(ctx), m_target(target)
+{}
+
+RenderTargetCUDA::~RenderTargetCUDA() { rive_cuda_render_target_destroy(m_ctx, m_target); }
+
+void* RenderTargetCUDA::devicePixels() const
+{
+    return rive_cuda_render_target_device_ptr(m_target);
+}
+
+int RenderTargetCUDA::readPixels(void* dstHost) const
+{
+    return rive_cuda_render_target_read(m_ctx, m_target, dstHost, nullptr);
+}
+
+std::unique_ptr<RenderContext> RenderContextCUDAImpl::MakeContext(int device)
+{
+    rive_cuda_context* ctx = nullptr;
+    int rc = rive_cuda_context_create(device, &ctx);
+    if (rc != RIVE_CUDA_OK)
+    {
+        fprintf(stderr, "RenderContextCUDAImpl: cannot open CUDA device %d (status %d)\n", device,
+                rc);
+        return nullptr;
+    }
+    std::unique_ptr<RenderContextCUDAImpl> impl(new RenderContextCUDAImpl(ctx));
+    return std::make_unique<RenderContext>(std::move(impl));
+}
+
+RenderContextCUDAImpl::RenderContextCUDAImpl(rive_cuda_context* ctx) : m_ctx(ctx)
+{
+    // Only pixel-local-storage-style raster ordering is implemented; the
+    // tile kernel gives the ordering guarantee that mode relies on.
+    m_platformFeatures.supportsRasterOrderingMode = true;
+}
+
+RenderContextCUDAImpl::~RenderContextCUDAImpl() { rive_cuda_context_destroy(m_ctx); }
+
+rcp<RenderTargetCUDA> RenderContextCUDAImpl::makeRenderTarget(uint32_t width, uint32_t height)
+{
+    rive_cuda_render_target* t = nullptr;
+    int rc = rive_cuda_render_target_create(m_ctx, width, height, &t);
+    note(rc);
+    if (rc != RIVE_CUDA_OK)
+        return nullptr;
+    return rcp<RenderTargetCUDA>(new RenderTargetCUDA(m_ctx, t, width, height));
+}
+
+std::string RenderContextCUDAImpl::lastError() const
+{
+    char buf[512] = {};
+    rive_cuda_last_error(m_ctx, buf, sizeof(buf));
+    return buf;
+}
+
+int RenderContextCUDAImpl::syncAndCheck()
+{
+    int rc = rive_cuda_sync(m_ctx, nullptr);
+    note(rc);
+    return rc;
+}
+
+void RenderContextCUDAImpl::note(int status)
+{
+    if (status != RIVE_CUDA_OK)
+        m_lastStatus = status;
+}
+
+rcp<RenderBuffer> RenderContextCUDAImpl::makeRenderBuffer(RenderBufferType type,
+                                                          RenderBufferFlags flags,
+                                                          size_t bytes)
+{
+    return make_rcp<HostRenderBuffer>(type, flags, bytes);
+}
+
+rcp<Texture> RenderContextCUDAImpl::makeImageTexture(uint32_t width,
+                                                     uint32_t height,
+                                                     uint32_t,
+                                                     GPUTextureFormat,
+                                                     const uint8_t[],
+                                                     uint8_t,
+                                                     uint8_t,
+                                                     bool,
+                                                     bool)
+{
+    // Image paints are not drawn by this backend; the texture object only
+    // carries its size so RenderImage bookkeeping works.
+    return make_rcp<Texture>(width, height);
+}
+
+// RenderContextImpl::resize* "cannot fail" (render_context_impl.hpp:99-107):
+// a failure is recorded and the next map of that buffer returns nullptr,
+// which makes RenderContext skip the frame.
+void RenderContextCUDAImpl::resize(int kind, size_t bytes)
+{
+    note(rive_cuda_resize_buffer(m_ctx, kind, bytes));
+}
+
+void* RenderContextCUDAImpl::map(int kind, size_t bytes)
+{
+    void* p = rive_cuda_map_buffer(m_ctx, kind, bytes);
+    if (!p)
+        note(RIVE_CUDA_ERR_NOT_MAPPED);
+    return p;
+}
+
+void RenderContextCUDAImpl::unmap(int kind, size_t bytes)
+{
+    note(rive_cuda_unmap_buffer(m_ctx, kind, bytes));
+}
+
+void RenderContextCUDAImpl::resizeFlushUniformBuffer(size_t n) { resize(RIVE_CUDA_BUFFER_FLUSH_UNIFORM, n); }
+void RenderContextCUDAImpl::resizePathBuffer(size_t n, StorageBufferStructure) { resize(RIVE_CUDA_BUFFER_PATH, n); }
+void RenderContextCUDAImpl::resizePaintBuffer(size_t n, StorageBufferStructure) { resize(RIVE_CUDA_BUFFER_PAINT, n); }
+void RenderContextCUDAImpl::resizePaintAuxBuffer(size_t n, StorageBufferStructure) { resize(RIVE_CUDA_BUFFER_PAINT_AUX, n); }
+void RenderContextCUDAImpl::resizeContourBuffer(size_t n, StorageBufferStructure) { resize(RIVE_CUDA_BUFFER_CONTOUR, n); }
+void RenderContextCUDAImpl::resizeGradSpanBuffer(size_t n) { resize(RIVE_CUDA_BUFFER_GRAD_SPAN, n); }
+void RenderContextCUDAImpl::resizeTessVertexSpanBuffer(size_t n) { resize(RIVE_CUDA_BUFFER_TESS_SPAN, n); }
+void RenderContextCUDAImpl::resizeTriangleVertexBuffer(size_t n) { resize(RIVE_CUDA_BUFFER_TRIANGLE, n); }
+void RenderContextCUDAImpl::resizeImageDrawInstanceBuffer(size_t n) { resize(RIVE_CUDA_BUFFER_IMAGE_DRAW, n); }
+
+void* RenderContextCUDAImpl::mapFlushUniformBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_FLUSH_UNIFORM, n); }
+void* RenderContextCUDAImpl::mapPathBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_PATH, n); }
+void* RenderContextCUDAImpl::mapPaintBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_PAINT, n); }
+void* RenderContextCUDAImpl::mapPaintAuxBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_PAINT_AUX, n); }
+void* RenderContextCUDAImpl::mapContourBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_CONTOUR, n); }
+void* RenderContextCUDAImpl::mapGradSpanBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_GRAD_SPAN, n); }
+void* RenderContextCUDAImpl::mapTessVertexSpanBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_TESS_SPAN, n); }
+void* RenderContextCUDAImpl::mapTriangleVertexBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_TRIANGLE, n); }
+void* RenderContextCUDAImpl::mapImageDrawInstanceBuffer(size_t n) { return map(RIVE_CUDA_BUFFER_IMAGE_DRAW, n); }
+
+void RenderContextCUDAImpl::unmapFlushUniformBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_FLUSH_UNIFORM, n); }
+void RenderContextCUDAImpl::unmapPathBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_PATH, n); }
+void RenderContextCUDAImpl::unmapPaintBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_PAINT, n); }
+void RenderContextCUDAImpl::unmapPaintAuxBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_PAINT_AUX, n); }
+void RenderContextCUDAImpl::unmapContourBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_CONTOUR, n); }
+void RenderContextCUDAImpl::unmapGradSpanBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_GRAD_SPAN, n); }
+void RenderContextCUDAImpl::unmapTessVertexSpanBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_TESS_SPAN, n); }
+void RenderContextCUDAImpl::unmapTriangleVertexBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_TRIANGLE, n); }
+void RenderContextCUDAImpl::unmapImageDrawInstanceBuffer(size_t n) { unmap(RIVE_CUDA_BUFFER_IMAGE_DRAW, n); }
+
+void RenderContextCUDAImpl::resizeGradientTexture(uint32_t width, uint32_t height)
+{
+    m_gradTextureHeight = height;
+    note(rive_cuda_resize_gradient_texture(m_ctx, width, height));
+}
+
+void RenderContextCUDAImpl::resizeTessellationTexture(uint32_t width, uint32_t height)
+{
+    note(rive_cuda_resize_tessellation_texture(m_ctx, width, height));
+}
+
+void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
+{
+    rive_cuda_flush_desc o;
+    memset(&o, 0, sizeof(o));
+    o.render_target_width = d.renderTarget->width();
+    o.render_target_height = d.renderTarget->height();
+    o.interlock_mode = static_cast<uint32_t>(d.interlockMode);
+    o.color_load_action = static_cast<uint32_t>(d.colorLoadAction);
+    o.color_clear_value = d.colorClearValue;
+    o.update_bounds[0] = d.renderTargetUpdateBounds.left;
+    o.update_bounds[1] = d.renderTargetUpdateBounds.top;
+    o.update_bounds[2] = d.renderTargetUpdateBounds.right;
+    o.update_bounds[3] = d.renderTargetUpdateBounds.bottom;
+    o.combined_shader_features = static_cast<uint32_t>(d.combinedShaderFeatures);
+    o.dither_mode = static_cast<uint32_t>(d.ditherMode);
+    o.flush_uniform_offset_bytes = static_cast<uint32_t>(d.flushUniformDataOffsetInBytes);
+    o.path_count = d.pathCount;
+    o.first_path = static_cast<uint32_t>(d.firstPath);
+    o.first_paint = static_cast<uint32_t>(d.firstPaint);
+    o.first_paint_aux = static_cast<uint32_t>(d.firstPaintAux);
+    o.contour_count = d.contourCount;
+    o.first_contour = static_cast<uint32_t>(d.firstContour);
+    o.grad_span_count = d.gradSpanCount;
+    o.first_grad_span = static_cast<uint32_t>(d.firstGradSpan);
+    o.tess_span_count = d.tessVertexSpanCount;
+    o.first_tess_span = static_cast<uint32_t>(d.firstTessVertexSpan);
+    o.grad_data_height = d.gradDataHeight;
+    o.tess_data_height = d.tessDataHeight;
+    o.grad_texture_height = m_gradTextureHeight;
+    o.wireframe = d.wireframe ? 1u : 0u;
+    o.clockwise_fill_override = d.clockwiseFillOverride ? 1u : 0u;
+    o.has_triangle_vertices = d.hasTriangleVertices ? 1u : 0u;
+
+    std::vector<rive_cuda_draw_batch> batches;
+    if (d.drawList != nullptr)
+    {
+        for (const DrawBatch& b : *d.drawList)
+        {
+            rive_cuda_draw_batch ob;
+            ob.draw_type = static_cast<uint32_t>(b.drawType);
+            ob.element_count = b.elementCount;
+            ob.base_element = b.baseElement;
+            ob.shader_features = static_cast<uint32_t>(b.shaderFeatures);
+            ob.draw_contents = static_cast<uint32_t>(b.drawContents);
+            ob.shader_misc_flags = static_cast<uint32_t>(b.shaderMiscFlags);
+            ob.first_blend_mode = static_cast<uint32_t>(b.firstBlendMode);
+            ob.barriers = static_cast<uint32_t>(b.barriers);
+            batches.push_back(ob);
+        }
+    }
+    o.draw_batch_count = static_cast<uint32_t>(batches.size());
+    o.draw_batches = batches.empty() ? nullptr : batches.data();
+
+    auto* target = static_cast<RenderTargetCUDA*>(d.renderTarget);
+    note(rive_cuda_flush(m_ctx, &o, target->handle(), d.externalCommandBuffer));
+}
+
+double RenderContextCUDAImpl::secondsNow() const
+{
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+} // namespace rive::gpu
