@@ -1,7 +1,7 @@
 """Benchmark of the GB300 flush backend on the full-feature single scene.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload full_feature|plain_small] [--capture FILE]
+                    [--workload full_feature|full_feature_1024|plain_small|stroke_stress_1024] [--capture FILE]
 
 A step is one frame: every logical flush of the frame (gradient ramps,
 tessellation, patch set-up, tile binning + sort, raster resolve) over the
@@ -52,8 +52,14 @@ def build_workload(args):
     from rive_runtime_gb300 import planner
     if args.workload == "full_feature":
         sc = scene.full_feature(seed=2)
+    elif args.workload == "full_feature_1024":
+        # The same distributions on a quarter of the area (profiling size).
+        sc = scene.full_feature(seed=21, width=1024, height=1024, n_paths=1250)
     elif args.workload == "plain_small":
         sc = scene.plain_small(seed=1)
+    elif args.workload == "stroke_stress_1024":
+        # One 1024x1024 canvas of the tessellation-heavy stress: 5,000 strokes.
+        sc = scene.stroke_stress(seed=4, width=1024, height=1024, n_strokes=5000)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     return planner.plan(sc.to_bytes()), args.workload
