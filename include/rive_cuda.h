@@ -225,6 +225,49 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
                            void* cuda_stream);
 
 /*
+ * No-allocation flush (no counterpart in the reference). Same inputs and
+ * result as rive_cuda_flush_device, without a context: every intermediate
+ * lives in one fixed device pool of RIVE_CUDA_NOALLOC_POOL_BYTES per device,
+ * reserved when the library's module loads, so the call never allocates or
+ * frees memory. It is for callers that may not allocate while they render: a
+ * render thread with a frame deadline (cudaFree waits for the whole device),
+ * or an embedder whose device memory budget is fixed up front.
+ *
+ * Limits (larger flushes return RIVE_CUDA_ERR_INVALID_ARGUMENT with a message
+ * naming the limit, before anything is launched or written): render target
+ * up to RIVE_CUDA_NOALLOC_MAX_WIDTH x RIVE_CUDA_NOALLOC_MAX_HEIGHT, up to
+ * RIVE_CUDA_NOALLOC_MAX_TESS_ROWS tessellation rows (so up to
+ * RIVE_CUDA_NOALLOC_MAX_PATCHES patches), RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS
+ * gradient rows, and RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES tile bin entries (this
+ * one is known only after set-up; the call then returns without writing the
+ * target).
+ *
+ * The call clears what must start at zero (status word, tile ranges,
+ * gradient rows in use) itself. It waits for `cuda_stream` (NULL: the legacy
+ * default stream) twice, to read the flush uniforms and the bin total, and
+ * returns after the whole flush has run, with the device status checked
+ * (RIVE_CUDA_ERR_DEVICE_STATUS as rive_cuda_sync reports it). The first call
+ * on each device looks up the pool's address (cudaGetSymbolAddress); make
+ * that first call before any stream capture begins. There is one pool per
+ * device and process: calls that overlap in time, from two threads or on two
+ * streams of one device, race on it and must be serialised by the caller.
+ * `err` (may be NULL) receives a message on failure.
+ */
+#define RIVE_CUDA_NOALLOC_MAX_WIDTH 1024u
+#define RIVE_CUDA_NOALLOC_MAX_HEIGHT 1024u
+#define RIVE_CUDA_NOALLOC_MAX_TESS_ROWS 32u
+#define RIVE_CUDA_NOALLOC_MAX_PATCHES 8192u /* 32 rows x 2048 vertices / 8 */
+#define RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS 64u
+#define RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES 1048576u
+#define RIVE_CUDA_NOALLOC_POOL_BYTES 42697216u /* about 40.7 MiB */
+int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* desc,
+                                   const rive_cuda_device_buffers* buffers,
+                                   void* target_pixels_device,
+                                   void* cuda_stream,
+                                   char* err,
+                                   size_t err_len);
+
+/*
  * Waits for the stream and returns RIVE_CUDA_ERR_DEVICE_STATUS if any kernel
  * since the last sync reported an overflow; the message names it.
  */

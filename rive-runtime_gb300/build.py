@@ -18,7 +18,7 @@ LIB = os.path.join(OUT, "librive_cuda.so")
 PLANNER_LIB = os.path.join(OUT, "librive_planner.so")
 PLANNER_SOURCES = [os.path.join(CSRC, "planner", "planner.cpp")]
 CXX = os.environ.get("CXX", "g++")
-SOURCES = ["context.cu", "kernels_tess.cu", "kernels_raster.cu"]
+SOURCES = ["context.cu", "kernels_tess.cu", "kernels_raster.cu", "flush_noalloc.cu"]
 HEADERS = ["rive_cuda_internal.cuh"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

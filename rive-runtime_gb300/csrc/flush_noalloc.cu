@@ -1,0 +1,328 @@
+// rive_cuda_flush_device_noalloc (include/rive_cuda.h): one logical flush of a
+// small frame whose every intermediate (tessellation and gradient textures,
+// triangle records, tile bins, scan/sort temporaries, status words) lives in
+// one fixed, file-scope device pool. The call allocates nothing: no
+// cudaMalloc/cudaFree, no allocating library routine. It launches the same
+// kernels, in the same order, as rive_cuda_flush_device.
+//
+// The pool is one per device and per process, so calls that overlap in time
+// (two host threads, or two streams of one device) race on it.
+#include "rive_cuda.h"
+#include "rive_cuda_internal.cuh"
+
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace rivecuda
+{
+__global__ void color_ramp_kernel(FlushParams P);
+__global__ void tessellate_kernel(FlushParams P);
+__global__ void patch_setup_kernel(FlushParams P,
+                                   uint32_t baseInstance,
+                                   uint32_t instanceCount,
+                                   uint32_t slotBase,
+                                   uint32_t features,
+                                   TriRecord* tris,
+                                   uint32_t* tileCounts);
+__global__ void bin_scatter_kernel(uint32_t slotCount,
+                                   uint32_t tilesX,
+                                   const TriRecord* tris,
+                                   const uint32_t* tileCounts,
+                                   const uint32_t* offsets,
+                                   uint32_t* keys,
+                                   uint32_t* vals);
+__global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
+__global__ void raster_tile_kernel(FlushParams P,
+                                   uint32_t tilesX,
+                                   const TriRecord* tris,
+                                   const uint32_t* sortedSlots,
+                                   const uint2* ranges,
+                                   uint32_t* fb);
+} // namespace rivecuda
+
+using namespace rivecuda;
+
+namespace
+{
+constexpr size_t align256(size_t n) { return (n + 255) & ~(size_t)255; }
+
+// Pool layout: each region starts on a 256-byte boundary.
+constexpr size_t kMaxTiles = (RIVE_CUDA_NOALLOC_MAX_WIDTH / kTileSize) *
+                             (RIVE_CUDA_NOALLOC_MAX_HEIGHT / kTileSize);
+constexpr size_t kMaxSlots = (size_t)RIVE_CUDA_NOALLOC_MAX_PATCHES * kPatchTriangleCount;
+constexpr size_t kStatusOff = 0;                                     // error word, pair total
+constexpr size_t kTessOff = 256;
+constexpr size_t kTessBytes = (size_t)kTessTextureWidth * RIVE_CUDA_NOALLOC_MAX_TESS_ROWS * 16;
+constexpr size_t kGradOff = kTessOff + align256(kTessBytes);
+constexpr size_t kGradBytes = (size_t)kGradTextureWidth * RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS * 4;
+constexpr size_t kTrisOff = kGradOff + align256(kGradBytes);
+constexpr size_t kTrisBytes = kMaxSlots * sizeof(TriRecord);
+constexpr size_t kCountsOff = kTrisOff + align256(kTrisBytes);
+constexpr size_t kOffsetsOff = kCountsOff + align256(kMaxSlots * 4);
+constexpr size_t kKeysOff = kOffsetsOff + align256(kMaxSlots * 4 + 4);
+constexpr size_t kPairBytes = (size_t)RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES * 4;
+constexpr size_t kValsOff = kKeysOff + align256(kPairBytes);
+constexpr size_t kKeysAltOff = kValsOff + align256(kPairBytes);
+constexpr size_t kValsAltOff = kKeysAltOff + align256(kPairBytes);
+constexpr size_t kRangesOff = kValsAltOff + align256(kPairBytes);
+constexpr size_t kScanTempOff = kRangesOff + align256(kMaxTiles * sizeof(uint2));
+constexpr size_t kScanTempBytes = 64u << 10;
+constexpr size_t kSortTempOff = kScanTempOff + kScanTempBytes;
+constexpr size_t kSortTempBytes = 4u << 20;
+constexpr size_t kPoolBytes = kSortTempOff + kSortTempBytes;
+static_assert(kPoolBytes == RIVE_CUDA_NOALLOC_POOL_BYTES,
+              "RIVE_CUDA_NOALLOC_POOL_BYTES must match the pool layout");
+
+constexpr int kMaxDevices = 64;
+std::mutex gPoolMutex;
+uint8_t* gPool[kMaxDevices] = {};
+
+int fail(char* err, size_t len, int code, const char* fmt, ...)
+{
+    if (err && len)
+    {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err, len, fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CKN(call)                                                                                  \
+    do                                                                                             \
+    {                                                                                              \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return fail(err, err_len, RIVE_CUDA_ERR_CUDA, "%s: %s", #call,                         \
+                        cudaGetErrorString(_e));                                                   \
+    } while (0)
+
+uint32_t premul_clear(uint32_t argb)
+{
+    float a = (float)(argb >> 24) / 255.f;
+    float r = (float)((argb >> 16) & 0xffu) / 255.f * a;
+    float g = (float)((argb >> 8) & 0xffu) / 255.f * a;
+    float b = (float)(argb & 0xffu) / 255.f * a;
+    auto q = [](float x) {
+        x = x < 0.f ? 0.f : (x > 1.f ? 1.f : x);
+        return (uint32_t)(x * 255.f + .5f);
+    };
+    return q(r) | (q(g) << 8) | (q(b) << 16) | (q(a) << 24);
+}
+} // namespace
+
+// The pool itself: zero-initialised at module load, never resized or freed.
+static __device__ __align__(256) uint8_t gNoAllocScratch[RIVE_CUDA_NOALLOC_POOL_BYTES];
+
+extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
+                                              const rive_cuda_device_buffers* buffers,
+                                              void* target_pixels_device,
+                                              void* cuda_stream,
+                                              char* err,
+                                              size_t err_len)
+{
+    if (err && err_len)
+        err[0] = 0;
+    if (!d || !buffers || !target_pixels_device)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!buffers->flush_uniforms)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush_uniforms is NULL");
+    if (d->interlock_mode != 0)
+        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                    "interlock mode %u not supported (rasterOrdering only)", d->interlock_mode);
+    if (d->has_triangle_vertices)
+        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                    "interior triangulation draws are not supported");
+    if (d->draw_batch_count && !d->draw_batches)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT, "draw_batches is NULL");
+    // Size limits of the fixed pool: refused before anything is launched.
+    if (d->render_target_width == 0 || d->render_target_height == 0)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT, "empty render target");
+    if (d->render_target_width > RIVE_CUDA_NOALLOC_MAX_WIDTH ||
+        d->render_target_height > RIVE_CUDA_NOALLOC_MAX_HEIGHT)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                    "render target %ux%u exceeds the no-allocation limit %ux%u",
+                    d->render_target_width, d->render_target_height, RIVE_CUDA_NOALLOC_MAX_WIDTH,
+                    RIVE_CUDA_NOALLOC_MAX_HEIGHT);
+    if (d->tess_data_height > RIVE_CUDA_NOALLOC_MAX_TESS_ROWS)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                    "tessellation texture height %u exceeds the no-allocation limit %u rows",
+                    d->tess_data_height, RIVE_CUDA_NOALLOC_MAX_TESS_ROWS);
+    if (d->grad_data_height > RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                    "gradient texture height %u exceeds the no-allocation limit %u rows",
+                    d->grad_data_height, RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS);
+    uint64_t instances = 0;
+    for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+    {
+        const rive_cuda_draw_batch& b = d->draw_batches[i];
+        if (b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
+            return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
+                        b.draw_type);
+        if (b.shader_features & SF_FEATHER)
+            return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
+        if (((uint64_t)b.base_element + b.element_count) * kPatchSegmentSpan >
+            (uint64_t)d->tess_data_height * kTessTextureWidth)
+            return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                        "batch %u reads past the tessellation texture", i);
+        instances += b.element_count;
+    }
+    if (instances > RIVE_CUDA_NOALLOC_MAX_PATCHES)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                    "%llu patches exceed the no-allocation limit %u",
+                    (unsigned long long)instances, RIVE_CUDA_NOALLOC_MAX_PATCHES);
+
+    int dev = 0;
+    CKN(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices)
+        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    uint8_t* pool = nullptr;
+    {
+        // The pool's address is looked up once per device, on the first call.
+        std::lock_guard<std::mutex> lock(gPoolMutex);
+        if (!gPool[dev])
+        {
+            void* p = nullptr;
+            CKN(cudaGetSymbolAddress(&p, gNoAllocScratch));
+            gPool[dev] = (uint8_t*)p;
+        }
+        pool = gPool[dev];
+    }
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    uint32_t* dError = (uint32_t*)(pool + kStatusOff);
+    uint32_t* fb = (uint32_t*)target_pixels_device;
+
+    FlushParams P = {};
+    P.paths = (const uint4*)buffers->paths;
+    P.paints = (const uint2*)buffers->paints;
+    P.paintAux = (const float4*)buffers->paint_aux;
+    P.contours = (const uint4*)buffers->contours;
+    P.gradSpans = (const uint4*)buffers->grad_spans;
+    P.tessSpans = (const uint4*)buffers->tess_spans;
+    P.firstPath = d->first_path;
+    P.firstPaint = d->first_paint;
+    P.firstPaintAux = d->first_paint_aux;
+    P.firstContour = d->first_contour;
+    P.firstGradSpan = d->first_grad_span;
+    P.gradSpanCount = d->grad_span_count;
+    P.firstTessSpan = d->first_tess_span;
+    P.tessSpanCount = d->tess_span_count;
+    P.pathCount = d->path_count;
+    P.contourCount = d->contour_count;
+    P.gradDataHeight = d->grad_data_height;
+    P.gradTextureHeight = d->grad_texture_height ? d->grad_texture_height : d->grad_data_height;
+    P.tessDataHeight = d->tess_data_height;
+    P.width = d->render_target_width;
+    P.height = d->render_target_height;
+    P.wireframe = d->wireframe;
+    P.loadClear = d->color_load_action == RIVE_CUDA_LOAD_CLEAR;
+    P.clearColorPremulRGBA = premul_clear(d->color_clear_value);
+    P.error = dError;
+    P.tess = (uint4*)(pool + kTessOff);
+    P.grad = (uchar4*)(pool + kGradOff);
+
+    // FlushUniforms fields (renderer/include/rive/renderer/gpu.hpp:1466-1537),
+    // read into a stack copy.
+    uint8_t uni[256];
+    CKN(cudaMemcpyAsync(uni, (const uint8_t*)buffers->flush_uniforms + d->flush_uniform_offset_bytes,
+                        sizeof(uni), cudaMemcpyDeviceToHost, stream));
+    CKN(cudaStreamSynchronize(stream));
+    memcpy(&P.pathIDGranularity, uni + 72, 4);
+    memcpy(&P.ditherScale, uni + 88, 4);
+    memcpy(&P.ditherBias, uni + 92, 4);
+    if (P.pathIDGranularity == 0)
+        P.pathIDGranularity = 1;
+
+    // What must start at zero on every call: the error word, the tile
+    // ranges, the gradient rows in use and the scan's leading offset.
+    const uint32_t tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
+    const uint32_t tilesY = (d->render_target_height + kTileSize - 1) / kTileSize;
+    const uint32_t tiles = tilesX * tilesY;
+    uint2* ranges = (uint2*)(pool + kRangesOff);
+    CKN(cudaMemsetAsync(dError, 0, 4, stream));
+    CKN(cudaMemsetAsync(ranges, 0, (size_t)tiles * sizeof(uint2), stream));
+    if (d->grad_data_height)
+        CKN(cudaMemsetAsync(P.grad, 0, (size_t)kGradTextureWidth * d->grad_data_height * 4, stream));
+
+    if (d->grad_span_count)
+        color_ramp_kernel<<<d->grad_span_count, 128, 0, stream>>>(P);
+    if (d->tess_span_count)
+        tessellate_kernel<<<(d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(P);
+
+    TriRecord* tris = (TriRecord*)(pool + kTrisOff);
+    uint32_t* counts = (uint32_t*)(pool + kCountsOff);
+    uint32_t* offs = (uint32_t*)(pool + kOffsetsOff);
+    const uint32_t slots = (uint32_t)(instances * kPatchTriangleCount);
+    uint32_t pairs = 0;
+    if (slots)
+    {
+        uint32_t slotBase = 0;
+        for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+        {
+            const rive_cuda_draw_batch& b = d->draw_batches[i];
+            if (!b.element_count)
+                continue;
+            patch_setup_kernel<<<(b.element_count + 3) / 4, 128, 0, stream>>>(
+                P, b.base_element, b.element_count, slotBase, b.shader_features, tris, counts);
+            slotBase += b.element_count * kPatchTriangleCount;
+        }
+        size_t tempBytes = 0;
+        CKN(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
+        if (tempBytes > kScanTempBytes)
+            return fail(err, err_len, RIVE_CUDA_ERR_OUT_OF_MEMORY,
+                        "scan needs %zu temporary bytes, pool holds %zu", tempBytes,
+                        kScanTempBytes);
+        CKN(cudaMemsetAsync(offs, 0, 4, stream));
+        CKN(cub::DeviceScan::InclusiveSum(pool + kScanTempOff, tempBytes, counts, offs + 1, slots,
+                                          stream));
+        CKN(cudaMemcpyAsync(&pairs, offs + slots, 4, cudaMemcpyDeviceToHost, stream));
+        CKN(cudaStreamSynchronize(stream));
+        if (pairs > RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES)
+            return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                        "%u tile bin entries exceed the no-allocation limit %u (target not "
+                        "written)",
+                        pairs, RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES);
+    }
+    uint32_t* keys = (uint32_t*)(pool + kKeysOff);
+    uint32_t* vals = (uint32_t*)(pool + kValsOff);
+    const uint32_t* sortedSlots = nullptr;
+    if (pairs)
+    {
+        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(slots, tilesX, tris, counts, offs,
+                                                                   keys, vals);
+        int endBit = 1;
+        while ((1u << endBit) < tiles)
+            ++endBit;
+        cub::DoubleBuffer<uint32_t> k(keys, (uint32_t*)(pool + kKeysAltOff));
+        cub::DoubleBuffer<uint32_t> v(vals, (uint32_t*)(pool + kValsAltOff));
+        size_t tempBytes = 0;
+        CKN(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, k, v, (int)pairs, 0, endBit, stream));
+        if (tempBytes > kSortTempBytes)
+            return fail(err, err_len, RIVE_CUDA_ERR_OUT_OF_MEMORY,
+                        "sort needs %zu temporary bytes, pool holds %zu", tempBytes,
+                        kSortTempBytes);
+        CKN(cub::DeviceRadixSort::SortPairs(pool + kSortTempOff, tempBytes, k, v, (int)pairs, 0,
+                                            endBit, stream));
+        tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(), ranges);
+        sortedSlots = v.Current();
+    }
+    raster_tile_kernel<<<tiles, 256, 0, stream>>>(P, tilesX, tris, sortedSlots, ranges, fb);
+    CKN(cudaGetLastError());
+
+    // Device status of this flush (overflow and range flags of the kernels).
+    uint32_t status = 0;
+    CKN(cudaMemcpyAsync(&status, dError, 4, cudaMemcpyDeviceToHost, stream));
+    CKN(cudaStreamSynchronize(stream));
+    if (status)
+        return fail(err, err_len, RIVE_CUDA_ERR_DEVICE_STATUS,
+                    "device status 0x%x (1 tess index, 2 contour, 4 path, 8 feather, "
+                    "16 coordinate range, 32 bin overflow)",
+                    status);
+    return RIVE_CUDA_OK;
+}

@@ -92,6 +92,9 @@ def load():
         "rive_cuda_flush": (i32, [vp, ctypes.POINTER(FlushDesc), vp, vp]),
         "rive_cuda_flush_device": (i32, [vp, ctypes.POINTER(FlushDesc),
                                          ctypes.POINTER(DeviceBuffers), vp, vp]),
+        "rive_cuda_flush_device_noalloc": (i32, [ctypes.POINTER(FlushDesc),
+                                                 ctypes.POINTER(DeviceBuffers), vp, vp,
+                                                 ctypes.c_char_p, sz]),
         "rive_cuda_sync": (i32, [vp, vp]),
         "rive_cuda_read_tess_texture": (i32, [vp, vp, sz]),
         "rive_cuda_read_grad_texture": (i32, [vp, vp, sz]),
@@ -119,6 +122,20 @@ def make_desc(flush):
     d.draw_batch_count = len(batches)
     d.draw_batches = batches.ctypes.data if len(batches) else None
     return d, batches
+
+
+def flush_device_noalloc(flush, bufs: DeviceBuffers, target_ptr: int, stream=None):
+    """rive_cuda_flush_device_noalloc: one flush of a small frame with every
+    intermediate in the library's fixed device pool (no context, no
+    allocation). Synchronous; raises RiveCudaError with the library's message."""
+    lib = load()
+    d, keep = make_desc(flush)
+    err = ctypes.create_string_buffer(512)
+    rc = lib.rive_cuda_flush_device_noalloc(ctypes.byref(d), ctypes.byref(bufs),
+                                            ctypes.c_void_p(target_ptr), stream, err, 512)
+    del keep
+    if rc != OK:
+        raise RiveCudaError(f"flush_device_noalloc: status {rc}: {err.value.decode()}")
 
 
 class Context:
