@@ -368,13 +368,6 @@ __device__ __forceinline__ float edge_eval(float4 e, float px, float py)
     return __fmaf_rn(e.z, __fsub_rn(px, e.x), __fmul_rn(e.w, __fsub_rn(py, e.y)));
 }
 
-__device__ __forceinline__ bool edge_inside(float4 e, float E)
-{
-    // Top-left tie rule for clockwise (y-down) triangles: edge direction
-    // (dx, dy) = (B, -A); inclusive when dy < 0, or dy == 0 and dx > 0.
-    return E > 0.f || (E == 0.f && (e.z > 0.f || (e.z == 0.f && e.w > 0.f)));
-}
-
 // Builds the oriented, canonically-anchored edge P->Q of a triangle.
 __device__ __forceinline__ float4 make_edge(float2 P, float2 Q)
 {
@@ -389,20 +382,42 @@ __device__ __forceinline__ float4 make_edge(float2 P, float2 Q)
     return make_float4(a.x, a.y, A, B);
 }
 
-// Does any pixel centre of [x0, x1) x [y0, y1) (already clipped to the
-// triangle's pixel bounds) lie inside the triangle? Conservative on ties. Uses
-// the same edge_eval as the raster, and float rounding is monotone, so a
-// rejected region never holds a pixel the raster would accept.
-__device__ __forceinline__ bool rect_overlaps(const float4* e, int x0, int x1, int y0, int y1)
+// Tile-local edge functions. The raster tests pixel (lx, ly) of a tile (lx,
+// ly = 0..15 pixel offsets from the tile's first pixel centre) as
+//   E = fma(A, lx, fma(B, ly, C)),  C = edge_eval at the tile's first centre.
+// The two triangles sharing an edge hold bitwise-negated (A, B, C), so their
+// E values are exact negations and the fill stays watertight. Tile counting,
+// binning and the raster's block masks all use this same expression; float
+// rounding is monotone in lx and ly, so testing the corner of a rectangle
+// that maximises E never rejects a pixel the raster would accept.
+__device__ __forceinline__ float tile_edge_origin(float4 e, int tx, int ty)
 {
-    float xlo = (float)x0 + .5f, xhi = (float)(x1 - 1) + .5f;
-    float ylo = (float)y0 + .5f, yhi = (float)(y1 - 1) + .5f;
+    return edge_eval(e, (float)(tx * kTileSize) + .5f, (float)(ty * kTileSize) + .5f);
+}
+
+__device__ __forceinline__ float local_edge(float c, float a, float b, float lx, float ly)
+{
+    return __fmaf_rn(a, lx, __fmaf_rn(b, ly, c));
+}
+
+__device__ __forceinline__ bool local_inside(float a, float b, float E)
+{
+    // Top-left tie rule for clockwise (y-down) triangles: edge direction
+    // (dx, dy) = (B, -A); inclusive when dy < 0, or dy == 0 and dx > 0.
+    return E > 0.f || (E == 0.f && (a > 0.f || (a == 0.f && b > 0.f)));
+}
+
+// Can any pixel of the tile-local rectangle [x0, x1) x [y0, y1) lie inside
+// all three edges (tile constants c[k], slopes e[k].z, e[k].w)?
+__device__ __forceinline__ bool local_rect_overlaps(const float* c, const float4* e, int x0, int x1,
+                                                    int y0, int y1)
+{
 #pragma unroll
     for (int k = 0; k < 3; ++k)
     {
-        float x = e[k].z > 0.f ? xhi : xlo;
-        float y = e[k].w > 0.f ? yhi : ylo;
-        if (edge_eval(e[k], x, y) < 0.f)
+        const float lx = (float)(e[k].z > 0.f ? x1 - 1 : x0);
+        const float ly = (float)(e[k].w > 0.f ? y1 - 1 : y0);
+        if (local_edge(c[k], e[k].z, e[k].w, lx, ly) < 0.f)
             return false;
     }
     return true;
@@ -410,15 +425,12 @@ __device__ __forceinline__ bool rect_overlaps(const float4* e, int x0, int x1, i
 
 __device__ __forceinline__ bool tile_overlaps(const float4* e, int4 bb, int tx, int ty)
 {
-    return rect_overlaps(e,
-                         max(tx * kTileSize, bb.x),
-                         min(tx * kTileSize + kTileSize, bb.z),
-                         max(ty * kTileSize, bb.y),
-                         min(ty * kTileSize + kTileSize, bb.w));
+    const int ox = tx * kTileSize, oy = ty * kTileSize;
+    const float c[3] = {tile_edge_origin(e[0], tx, ty), tile_edge_origin(e[1], tx, ty),
+                        tile_edge_origin(e[2], tx, ty)};
+    return local_rect_overlaps(c, e, max(ox, bb.x) - ox, min(ox + kTileSize, bb.z) - ox,
+                               max(oy, bb.y) - oy, min(oy + kTileSize, bb.w) - oy);
 }
-
-// Snaps to the 1/256-pixel grid of the rasteriser.
-__device__ __forceinline__ float snap(float v) { return rintf(v * 256.f) * (1.f / 256.f); }
 
 __device__ __forceinline__ int4 unpack_bbox(uint4 meta)
 {
@@ -888,7 +900,8 @@ struct Pixel
     uint32_t color;    // RGBA8, the colour before the pending path
     uint32_t clip;     // packHalf2x16(coverage, clipID)
     uint32_t scratch;  // RGBA8 scratch plane
-    uint32_t coverage; // packHalf2x16(coverageCount, pathID)
+    uint32_t key;      // coverage plane's path key (fp16 bits of the pathID)
+    float count;       // coverage plane's count (always an fp16 value)
     uint32_t pendMeta; // pathAndFeatures of the pending path (0: none)
     uint32_t pendPaintX, pendPaintY;
     uint32_t pendFrags; // fragments of the pending path so far (saturating)
@@ -911,7 +924,7 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
     const uint32_t paintX = s.pendPaintX, paintY = s.pendPaintY;
     const uint32_t paintType = paintX & 0xfu;
     const bool evenOdd = (paintX & PAINT_FLAG_EVEN_ODD_FILL) != 0;
-    float coverage = fabsf(h2f(s.coverage & 0xffffu));
+    float coverage = fabsf(s.count);
     if ((features & SF_EVEN_ODD) && evenOdd)
         coverage = 1.f - fabsf((coverage * .5f - floorf(coverage * .5f)) * 2.f + -1.f);
     coverage = fminf(coverage, 1.f);
@@ -1041,24 +1054,42 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
 }
 } // namespace
 
-// One 256-thread CTA per 16x16 tile. Warp w owns the 8x4 block at
-// (8 * (w & 1), 4 * (w >> 1)) of the tile; each lane owns one pixel and its
-// pixel-local storage in registers. Triangles are walked in primitive order;
-// a warp skips a triangle whose bounding box misses its block.
-__global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
+// One CTA per 16x16 tile, one thread per pixel; warp w owns the 8x4 block at
+// (8 (w & 1), 4 (w >> 1)). The tile's bin entries (triangle slots in
+// primitive order) are staged 256 at a time into shared memory in tile-local
+// form, each with a mask of the warp blocks it may cover; warps then walk
+// their own triangles in order and keep every pixel's planes in registers.
+struct __align__(16) TileTri
+{
+    float4 q0; // C0, A0, B0, C1
+    float4 q1; // A1, B1, C2, A2
+    float4 q2; // B2, covx at the tile origin, d covx/dx, d covx/dy
+    float4 q3; // covy at the tile origin, d covy/dx, d covy/dy, paint.x bits
+    uint4 q4;  // paint.y, pathAndFeatures, coverage key, unused
+};
+static_assert(sizeof(TileTri) == 80, "TileTri layout");
+
+// Resident CTAs per SM the register allocation is bounded for.
+#ifndef RIVE_RASTER_MIN_BLOCKS
+#define RIVE_RASTER_MIN_BLOCKS 5
+#endif
+
+__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(FlushParams P,
                                                           uint32_t tilesX,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ sortedSlots,
                                                           const uint2* __restrict__ ranges,
                                                           uint32_t* __restrict__ fb)
 {
-    __shared__ TriRecord sTris[256];
+    __shared__ TileTri sTris[256];
     __shared__ uint8_t sMask[256];
     const uint32_t tile = blockIdx.x;
     const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
+    const int ox = tx * kTileSize, oy = ty * kTileSize;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int bx = tx * kTileSize + (warp & 1) * 8, by = ty * kTileSize + (warp >> 1) * 4;
-    const int px = bx + (lane & 7), py = by + (lane >> 3);
+    const int lxi = (warp & 1) * 8 + (lane & 7), lyi = (warp >> 1) * 4 + (lane >> 3);
+    const int px = ox + lxi, py = oy + lyi;
+    const float lx = (float)lxi, ly = (float)lyi;
     const bool inBounds = px < (int)P.width && py < (int)P.height;
     const uint2 range = ranges[tile];
     if (range.y <= range.x && !P.loadClear)
@@ -1067,7 +1098,8 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
     s.color = P.loadClear ? P.clearColorPremulRGBA : (inBounds ? fb[(size_t)py * P.width + px] : 0u);
     s.clip = 0;
     s.scratch = 0;
-    s.coverage = 0;
+    s.key = 0;
+    s.count = 0.f;
     s.pendMeta = 0;
     s.pendPaintX = s.pendPaintY = 0;
     s.pendFrags = 0;
@@ -1082,24 +1114,35 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
 
     for (uint32_t base = range.x; base < range.y; base += 256)
     {
-        // Each thread stages one triangle and marks which of the tile's eight
-        // 8x4 warp blocks hold a pixel centre it may cover (exact corner test
-        // per block, so a cleared bit is never a missed pixel).
+        // Each thread stages one triangle in tile-local form and marks which
+        // of the eight warp blocks may hold a pixel it covers.
         const uint32_t k = base + threadIdx.x;
         uint32_t m = 0;
         if (k < range.y)
         {
             const TriRecord T = tris[sortedSlots[k]];
-            sTris[threadIdx.x] = T;
-            const int4 bb = unpack_bbox(T.meta);
             const float4 e[3] = {T.e0, T.e1, T.e2};
+            const float c[3] = {tile_edge_origin(e[0], tx, ty), tile_edge_origin(e[1], tx, ty),
+                                tile_edge_origin(e[2], tx, ty)};
+            const float dx0 = (float)ox + .5f - T.e0.x, dy0 = (float)oy + .5f - T.e0.y;
+            TileTri L;
+            L.q0 = make_float4(c[0], e[0].z, e[0].w, c[1]);
+            L.q1 = make_float4(e[1].z, e[1].w, c[2], e[2].z);
+            L.q2 = make_float4(e[2].w, T.cov0.x + T.cov0.y * dx0 + T.cov0.z * dy0, T.cov0.y,
+                               T.cov0.z);
+            L.q3 = make_float4(T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x, T.cov1.y,
+                               T.cov1.z);
+            L.q4 = make_uint4(__float_as_uint(T.cov1.w), T.meta.x, T.meta.w, 0u);
+            sTris[threadIdx.x] = L;
+            const int4 bb = unpack_bbox(T.meta);
+            const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;
 #pragma unroll
             for (int b = 0; b < 8; ++b)
             {
-                const int qx = tx * kTileSize + (b & 1) * 8, qy = ty * kTileSize + (b >> 1) * 4;
-                const int x0 = max(bb.x, qx), x1 = min(bb.z, qx + 8);
-                const int y0 = max(bb.y, qy), y1 = min(bb.w, qy + 4);
-                if (x0 < x1 && y0 < y1 && rect_overlaps(e, x0, x1, y0, y1))
+                const int qx = (b & 1) * 8, qy = (b >> 1) * 4;
+                const int x0 = max(bx0, qx), x1 = min(bx1, qx + 8);
+                const int y0 = max(by0, qy), y1 = min(by1, qy + 4);
+                if (x0 < x1 && y0 < y1 && local_rect_overlaps(c, e, x0, x1, y0, y1))
                     m |= 1u << b;
             }
         }
@@ -1114,8 +1157,8 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
             {
                 const uint32_t i = g + (uint32_t)(__ffs(bits) - 1);
                 bits &= bits - 1;
-                const TriRecord& T = sTris[i];
-                const uint32_t vPathID = T.meta.w;
+                const TileTri& T = sTris[i];
+                const uint32_t vPathID = T.q4.z;
                 // A path's triangles are contiguous in primitive order, so when
                 // the warp's stream moves to another path every pixel still
                 // holding the previous path's coverage has seen all of it:
@@ -1129,48 +1172,50 @@ __global__ void __launch_bounds__(256) raster_tile_kernel(FlushParams P,
                     }
                     streamPath = vPathID;
                 }
-                const float4 e0 = T.e0, e1 = T.e1, e2 = T.e2;
-                const float E0 = edge_eval(e0, fx, fy);
-                const float E1 = edge_eval(e1, fx, fy);
-                const float E2 = edge_eval(e2, fx, fy);
+                const float4 q0 = T.q0, q1 = T.q1;
+                const float b2 = T.q2.x;
+                const float E0 = local_edge(q0.x, q0.y, q0.z, lx, ly);
+                const float E1 = local_edge(q0.w, q1.x, q1.y, lx, ly);
+                const float E2 = local_edge(q1.z, q1.w, b2, lx, ly);
                 const float emin = fminf(fminf(E0, E1), E2);
                 if (!(emin > 0.f) &&
-                    !(emin == 0.f && edge_inside(e0, E0) && edge_inside(e1, E1) && edge_inside(e2, E2)))
+                    !(emin == 0.f && local_inside(q0.y, q0.z, E0) && local_inside(q1.x, q1.y, E1) &&
+                      local_inside(q1.w, b2, E2)))
                     continue;
                 if (!inBounds)
                     continue;
-                const uint32_t metaX = T.meta.x;
-                const float4 c0 = T.cov0, c1 = T.cov1;
-                const float dx = fx - e0.x, dy = fy - e0.y;
-                const float covx = c0.x + c0.y * dx + c0.z * dy;
-                const float covy = c0.w + c1.x * dx + c1.y * dy;
-                const uint32_t paintX = __float_as_uint(c1.z);
+                const float4 q2 = T.q2, q3 = T.q3;
+                const uint2 q4 = make_uint2(T.q4.x, T.q4.y);
+                const float covx = __fmaf_rn(q2.z, lx, __fmaf_rn(q2.w, ly, q2.y));
+                const float covy = __fmaf_rn(q3.y, lx, __fmaf_rn(q3.z, ly, q3.x));
+                const uint32_t paintX = __float_as_uint(q3.w);
                 float count;
-                if ((s.coverage >> 16) != vPathID)
+                if (s.key != vPathID)
                 {
                     if (s.pendMeta)
                         resolve_path(P, s, fx, fy, dither);
-                    s.pendMeta = metaX;
+                    s.pendMeta = q4.y;
                     s.pendPaintX = paintX;
-                    s.pendPaintY = __float_as_uint(c1.w);
+                    s.pendPaintY = q4.x;
                     s.pendFrags = 0;
+                    s.key = vPathID;
                     count = 0.f;
                 }
                 else
                 {
-                    count = h2f(s.coverage & 0xffffu);
+                    count = s.count;
                     if (!s.pendMeta) // the key's path came back after a resolve
                     {
-                        s.pendMeta = metaX;
+                        s.pendMeta = q4.y;
                         s.pendPaintX = paintX;
-                        s.pendPaintY = __float_as_uint(c1.w);
+                        s.pendPaintY = q4.x;
                     }
                 }
                 if (covy >= 0.f)
                     count = fmaxf(fminf(covx, covy), count); // stroke
                 else
                     count = count + covx; // fill
-                s.coverage = (vPathID << 16) | f2h(count);
+                s.count = h2f(f2h(count)); // the plane stores fp16
                 s.pendFrags = min(s.pendFrags + 1u, 2u);
             }
         }
