@@ -225,6 +225,27 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
                            void* cuda_stream);
 
 /*
+ * Batched form (no counterpart in the reference, whose backends flush one
+ * render target at a time): `count` independent logical flushes, each with
+ * its own records (device pointers, as in rive_cuda_flush_device) and its own
+ * target, rendered by ONE sequence of launches whose every stage covers all
+ * of them. Each target receives exactly what rive_cuda_flush_device would
+ * have written. Targets must be distinct within a batch; the logical flushes
+ * of one multi-flush frame go in successive batches. Up to 65535 flushes.
+ */
+typedef struct rive_cuda_batch_flush
+{
+    const rive_cuda_flush_desc* desc;
+    rive_cuda_device_buffers buffers;
+    void* target_pixels_device; /* RGBA8, width * height * 4 bytes */
+} rive_cuda_batch_flush;
+
+int rive_cuda_flush_batch(rive_cuda_context* ctx,
+                          const rive_cuda_batch_flush* flushes,
+                          uint32_t count,
+                          void* cuda_stream);
+
+/*
  * No-allocation flush (no counterpart in the reference). Same inputs and
  * result as rive_cuda_flush_device, without a context: every intermediate
  * lives in one fixed device pool of RIVE_CUDA_NOALLOC_POOL_BYTES per device,
@@ -259,7 +280,7 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
 #define RIVE_CUDA_NOALLOC_MAX_PATCHES 8192u /* 32 rows x 2048 vertices / 8 */
 #define RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS 64u
 #define RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES 1048576u
-#define RIVE_CUDA_NOALLOC_POOL_BYTES 42697216u /* about 40.7 MiB */
+#define RIVE_CUDA_NOALLOC_POOL_BYTES 42702848u /* about 40.7 MiB */
 int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* desc,
                                    const rive_cuda_device_buffers* buffers,
                                    void* target_pixels_device,

@@ -26,29 +26,21 @@
 
 namespace rivecuda
 {
-__global__ void color_ramp_kernel(FlushParams P);
-__global__ void tessellate_kernel(FlushParams P);
-__global__ void patch_setup_kernel(FlushParams P,
-                                   uint32_t baseInstance,
-                                   uint32_t instanceCount,
-                                   uint32_t slotBase,
-                                   uint32_t features,
-                                   TriRecord* tris,
-                                   uint32_t* tileCounts);
+__global__ void color_ramp_kernel(BatchTables B);
+__global__ void tessellate_kernel(BatchTables B);
+__global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
-                                   uint32_t tilesX,
+                                   const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
                                    const uint32_t* offsets,
                                    uint32_t* keys,
                                    uint32_t* vals);
 __global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
-__global__ void raster_tile_kernel(FlushParams P,
-                                   uint32_t tilesX,
+__global__ void raster_tile_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
-                                   const uint2* ranges,
-                                   uint32_t* fb);
+                                   const uint2* ranges);
 } // namespace rivecuda
 
 using namespace rivecuda;
@@ -85,6 +77,34 @@ struct DeviceBuffer
     }
 };
 
+struct HostBuffer
+{
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t need)
+    {
+        if (need <= bytes)
+            return cudaSuccess;
+        if (ptr)
+            cudaFreeHost(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        size_t n = std::max(need, (size_t)4096);
+        n = n + n / 4;
+        cudaError_t e = cudaMallocHost(&ptr, n);
+        if (e == cudaSuccess)
+            bytes = n;
+        return e;
+    }
+    void release()
+    {
+        if (ptr)
+            cudaFreeHost(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
 struct RecordRing
 {
     void* host[kRingSize] = {};
@@ -113,6 +133,9 @@ struct rive_cuda_context
     uint32_t tessWidth = 0, tessHeight = 0, gradWidth = 0, gradHeight = 0;
     DeviceBuffer tris, tileCounts, offsets;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
+    DeviceBuffer dTables;           // batch tables (device)
+    HostBuffer hTables, hUniforms;  // pinned staging of tables and uniforms
+    cudaEvent_t tablesCopied = nullptr;
     uint32_t* dError = nullptr;
     uint32_t* hError = nullptr;  // pinned
     uint32_t* hPairs = nullptr;  // pinned: scanned pair total
@@ -212,11 +235,17 @@ struct ResolvedBuffers
     const void* hostUniforms = nullptr;
 };
 
-int run_flush(rive_cuda_context* ctx,
-              const rive_cuda_flush_desc* d,
-              const ResolvedBuffers& rb,
-              uint32_t* fbDevice,
-              cudaStream_t stream)
+// One logical flush of a batch.
+struct FlushInput
+{
+    const rive_cuda_flush_desc* d;
+    ResolvedBuffers rb;
+    uint32_t* fb;
+};
+
+// Host-side checks of one flush; counts its patch instances.
+int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const ResolvedBuffers& rb,
+                   uint64_t& instances)
 {
     if (d->interlock_mode != 0)
         return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
@@ -252,7 +281,7 @@ int run_flush(rive_cuda_context* ctx,
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush uniforms out of range");
     if (d->grad_data_height > 65536 || d->tess_data_height > 65536)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "texture height out of range");
-    uint64_t instances = 0;
+    instances = 0;
     for (uint32_t i = 0; i < d->draw_batch_count; ++i)
     {
         const rive_cuda_draw_batch& b = d->draw_batches[i];
@@ -267,189 +296,310 @@ int run_flush(rive_cuda_context* ctx,
                              "batch %u reads past the tessellation texture", i);
         instances += b.element_count;
     }
-    if (instances * kPatchTriangleCount > 0xffffffffull)
-        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "too many patches in one flush");
+    return RIVE_CUDA_OK;
+}
 
-    // Flush uniforms are read on the host (one 256-byte record).
-    FlushParams P = {};
-    P.paths = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_PATH];
-    P.paints = (const uint2*)rb.ptr[RIVE_CUDA_BUFFER_PAINT];
-    P.paintAux = (const float4*)rb.ptr[RIVE_CUDA_BUFFER_PAINT_AUX];
-    P.contours = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_CONTOUR];
-    P.gradSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_GRAD_SPAN];
-    P.tessSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_TESS_SPAN];
-    P.firstPath = d->first_path;
-    P.firstPaint = d->first_paint;
-    P.firstPaintAux = d->first_paint_aux;
-    P.firstContour = d->first_contour;
-    P.firstGradSpan = d->first_grad_span;
-    P.gradSpanCount = d->grad_span_count;
-    P.firstTessSpan = d->first_tess_span;
-    P.tessSpanCount = d->tess_span_count;
-    P.pathCount = d->path_count;
-    P.contourCount = d->contour_count;
-    P.gradDataHeight = d->grad_data_height;
-    P.gradTextureHeight = d->grad_texture_height ? d->grad_texture_height
-                          : ctx->gradHeight       ? ctx->gradHeight
-                                                  : d->grad_data_height;
-    P.tessDataHeight = d->tess_data_height;
-    P.width = d->render_target_width;
-    P.height = d->render_target_height;
-    P.wireframe = d->wireframe;
-    P.loadClear = d->color_load_action == RIVE_CUDA_LOAD_CLEAR;
-    P.clearColorPremulRGBA = premul_rgba8(d->color_clear_value);
-    P.error = ctx->dError;
-    return 0 + [&]() -> int {
-        // FlushUniforms fields (gpu.hpp:1466-1537).
-        const uint8_t* uni = nullptr;
-        std::vector<uint8_t> hostUni(256);
-        // The uniforms live wherever the records live; copy them back only if
-        // they are device-resident.
-        if (rb.hostUniforms)
-        {
-            memcpy(hostUni.data(),
-                   (const uint8_t*)rb.hostUniforms + d->flush_uniform_offset_bytes, 256);
-        }
+size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
+
+// Runs a batch of independent logical flushes (distinct targets) as one
+// sequence of launches: every stage covers the work of all flushes at once.
+int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStream_t stream)
+{
+    if (n == 0)
+        return RIVE_CUDA_OK;
+    if (n > 65535)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "at most 65535 flushes per batch");
+    std::vector<uint64_t> inst(n);
+    uint64_t totalInstances = 0, segCount = 0;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        int rc = validate_flush(ctx, in[i].d, in[i].rb, inst[i]);
+        if (rc)
+            return rc;
+        if (!in[i].fb)
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u has no target", i);
+        totalInstances += inst[i];
+        for (uint32_t b = 0; b < in[i].d->draw_batch_count; ++b)
+            segCount += in[i].d->draw_batches[b].element_count ? 1 : 0;
+    }
+    if (totalInstances * kPatchTriangleCount > 0xffffffffull)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "too many patches in one batch");
+    if (n > 1)
+    {
+        // The flushes of one batch run concurrently: each needs its own target.
+        std::vector<const uint32_t*> fbs(n);
+        for (uint32_t i = 0; i < n; ++i)
+            fbs[i] = in[i].fb;
+        std::sort(fbs.begin(), fbs.end());
+        if (std::adjacent_find(fbs.begin(), fbs.end()) != fbs.end())
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                             "two flushes of one batch share a render target");
+    }
+
+    // The previous batch's tables may still be in flight from the staging.
+    if (ctx->tablesCopied)
+        CK(cudaEventSynchronize(ctx->tablesCopied));
+
+    // Flush uniforms (FlushUniforms, gpu.hpp:1466-1537): from the mapped ring
+    // when staged there, else copied back from the device in one wait.
+    CK(ctx->hUniforms.reserve((size_t)n * 256));
+    uint8_t* uni = (uint8_t*)ctx->hUniforms.ptr;
+    bool waitUniforms = false;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const rive_cuda_flush_desc* d = in[i].d;
+        if (in[i].rb.hostUniforms)
+            memcpy(uni + 256 * (size_t)i,
+                   (const uint8_t*)in[i].rb.hostUniforms + d->flush_uniform_offset_bytes, 256);
         else
         {
-            const uint8_t* src = (const uint8_t*)rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM] +
-                                 d->flush_uniform_offset_bytes;
-            CK(cudaMemcpyAsync(hostUni.data(), src, 256, cudaMemcpyDeviceToHost, stream));
-            CK(cudaStreamSynchronize(stream));
+            CK(cudaMemcpyAsync(uni + 256 * (size_t)i,
+                               (const uint8_t*)in[i].rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM] +
+                                   d->flush_uniform_offset_bytes,
+                               256, cudaMemcpyDeviceToHost, stream));
+            waitUniforms = true;
         }
-        uni = hostUni.data();
-        memcpy(&P.pathIDGranularity, uni + 72, 4);
-        memcpy(&P.ditherScale, uni + 88, 4);
-        memcpy(&P.ditherBias, uni + 92, 4);
+    }
+    if (waitUniforms)
+        CK(cudaStreamSynchronize(stream));
+
+    // Layout of the batch: per-flush texture rows, tiles, spans and slots.
+    uint64_t tessRows = 0, gradRows = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
+    std::vector<uint64_t> tessRow0(n), gradRow0(n);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const rive_cuda_flush_desc* d = in[i].d;
+        tessRow0[i] = tessRows;
+        gradRow0[i] = gradRows;
+        tessRows += std::max(d->tess_data_height, 1u);
+        gradRows += std::max(d->grad_data_height, 1u);
+        const uint64_t tx = (d->render_target_width + kTileSize - 1) / kTileSize;
+        const uint64_t ty = (d->render_target_height + kTileSize - 1) / kTileSize;
+        tiles += tx * ty;
+        gradSpans += d->grad_span_count;
+        tessSpans += d->tess_span_count;
+    }
+    if (tiles > 0x7fffffffull || gradSpans > 0x7fffffffull || tessSpans * 32 > 0xffffffffull)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "batch too large");
+    const size_t tessBytes = (size_t)kTessTextureWidth * tessRows * 16;
+    const size_t gradBytes = (size_t)kGradTextureWidth * gradRows * 4;
+    CK(ctx->tess.reserve(tessBytes));
+    CK(ctx->grad.reserve(gradBytes));
+    ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
+    ctx->lastGradBytes = (size_t)kGradTextureWidth * std::max(in[0].d->grad_data_height, 1u) * 4;
+
+    // Tables, staged in pinned memory and copied in one piece.
+    const size_t oScenes = 0;
+    const size_t oGradBase = align16(oScenes + sizeof(FlushParams) * n);
+    const size_t oTessBase = align16(oGradBase + 4 * (n + 1));
+    const size_t oTileBase = align16(oTessBase + 4 * (n + 1));
+    const size_t oSceneTiles = align16(oTileBase + 4 * (n + 1));
+    const size_t oSegments = align16(oSceneTiles + 8 * n);
+    const size_t oSegBase = align16(oSegments + sizeof(PatchSegment) * std::max<uint64_t>(segCount, 1));
+    const size_t tableBytes = align16(oSegBase + 4 * (segCount + 1));
+    CK(ctx->hTables.reserve(tableBytes));
+    CK(ctx->dTables.reserve(tableBytes));
+    uint8_t* h = (uint8_t*)ctx->hTables.ptr;
+    uint8_t* dT = (uint8_t*)ctx->dTables.ptr;
+    auto* scenes = (FlushParams*)(h + oScenes);
+    auto* gradBase = (uint32_t*)(h + oGradBase);
+    auto* tessBase = (uint32_t*)(h + oTessBase);
+    auto* tileBase = (uint32_t*)(h + oTileBase);
+    auto* sceneTiles = (uint2*)(h + oSceneTiles);
+    auto* segs = (PatchSegment*)(h + oSegments);
+    auto* segBase = (uint32_t*)(h + oSegBase);
+    uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, segAcc = 0, instAcc = 0, slotAcc = 0;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const rive_cuda_flush_desc* d = in[i].d;
+        const ResolvedBuffers& rb = in[i].rb;
+        FlushParams& P = scenes[i];
+        memset(&P, 0, sizeof(P));
+        P.paths = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_PATH];
+        P.paints = (const uint2*)rb.ptr[RIVE_CUDA_BUFFER_PAINT];
+        P.paintAux = (const float4*)rb.ptr[RIVE_CUDA_BUFFER_PAINT_AUX];
+        P.contours = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_CONTOUR];
+        P.gradSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_GRAD_SPAN];
+        P.tessSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_TESS_SPAN];
+        P.firstPath = d->first_path;
+        P.firstPaint = d->first_paint;
+        P.firstPaintAux = d->first_paint_aux;
+        P.firstContour = d->first_contour;
+        P.firstGradSpan = d->first_grad_span;
+        P.gradSpanCount = d->grad_span_count;
+        P.firstTessSpan = d->first_tess_span;
+        P.tessSpanCount = d->tess_span_count;
+        P.pathCount = d->path_count;
+        P.contourCount = d->contour_count;
+        P.gradDataHeight = d->grad_data_height;
+        P.gradTextureHeight = d->grad_texture_height              ? d->grad_texture_height
+                              : (n == 1 && ctx->gradHeight != 0u) ? ctx->gradHeight
+                                                                  : d->grad_data_height;
+        P.tessDataHeight = d->tess_data_height;
+        P.width = d->render_target_width;
+        P.height = d->render_target_height;
+        P.wireframe = d->wireframe;
+        P.loadClear = d->color_load_action == RIVE_CUDA_LOAD_CLEAR;
+        P.clearColorPremulRGBA = premul_rgba8(d->color_clear_value);
+        P.error = ctx->dError;
+        P.fb = in[i].fb;
+        P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
+        const uint8_t* u = uni + 256 * (size_t)i;
+        memcpy(&P.pathIDGranularity, u + 72, 4);
+        memcpy(&P.ditherScale, u + 88, 4);
+        memcpy(&P.ditherBias, u + 92, 4);
         if (P.pathIDGranularity == 0)
             P.pathIDGranularity = 1;
+        P.tess = (uint4*)ctx->tess.ptr + (size_t)tessRow0[i] * kTessTextureWidth;
+        P.grad = (uchar4*)ctx->grad.ptr + (size_t)gradRow0[i] * kGradTextureWidth;
 
-        const size_t tessBytes = (size_t)kTessTextureWidth * std::max(d->tess_data_height, 1u) * 16;
-        const size_t gradBytes = (size_t)kGradTextureWidth * std::max(d->grad_data_height, 1u) * 4;
-        CK(ctx->tess.reserve(tessBytes));
-        CK(ctx->grad.reserve(gradBytes));
-        ctx->lastTessBytes = tessBytes;
-        ctx->lastGradBytes = gradBytes;
-        P.tess = (uint4*)ctx->tess.ptr;
-        P.grad = (uchar4*)ctx->grad.ptr;
-        uint64_t launches = 0;
+        gradBase[i] = gAcc;
+        tessBase[i] = tAcc;
+        tileBase[i] = tileAcc;
+        sceneTiles[i] = make_uint2(tileAcc, P.tilesX);
+        gAcc += d->grad_span_count;
+        tAcc += d->tess_span_count;
+        tileAcc += P.tilesX * ((d->render_target_height + kTileSize - 1) / kTileSize);
+        for (uint32_t b = 0; b < d->draw_batch_count; ++b)
+        {
+            const rive_cuda_draw_batch& db = d->draw_batches[b];
+            if (!db.element_count)
+                continue;
+            segs[segAcc] = PatchSegment{i, db.base_element, db.shader_features, slotAcc};
+            segBase[segAcc] = instAcc;
+            ++segAcc;
+            instAcc += db.element_count;
+            slotAcc += db.element_count * kPatchTriangleCount;
+        }
+    }
+    gradBase[n] = gAcc;
+    tessBase[n] = tAcc;
+    tileBase[n] = tileAcc;
+    segBase[segAcc] = instAcc;
+    CK(cudaMemcpyAsync(dT, h, tableBytes, cudaMemcpyHostToDevice, stream));
+    if (!ctx->tablesCopied)
+        CK(cudaEventCreateWithFlags(&ctx->tablesCopied, cudaEventDisableTiming));
+    CK(cudaEventRecord(ctx->tablesCopied, stream));
 
-        // Pass 1: gradient ramps. Texels no span covers are never sampled;
-        // zero them so the texture is deterministic.
-        if (d->grad_data_height)
-            CK(cudaMemsetAsync(ctx->grad.ptr, 0, (size_t)kGradTextureWidth * d->grad_data_height * 4,
-                               stream));
-        if (d->grad_span_count)
-        {
-            stage_begin(ctx, RIVE_CUDA_STAGE_COLOR_RAMP, stream);
-            color_ramp_kernel<<<d->grad_span_count, 128, 0, stream>>>(P);
-            stage_end(ctx, stream);
-            ++launches;
-        }
-        // Pass 2: tessellation.
-        if (d->tess_span_count)
-        {
-            uint32_t blocks = (d->tess_span_count * 32u + 255u) / 256u;
-            stage_begin(ctx, RIVE_CUDA_STAGE_TESSELLATE, stream);
-            tessellate_kernel<<<blocks, 256, 0, stream>>>(P);
-            stage_end(ctx, stream);
-            ++launches;
-        }
-        // Pass 3a: patch set-up + tile counts.
-        const uint32_t slots = (uint32_t)(instances * kPatchTriangleCount);
-        const uint32_t tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
-        const uint32_t tilesY = (d->render_target_height + kTileSize - 1) / kTileSize;
-        const uint32_t tiles = tilesX * tilesY;
-        CK(ctx->ranges.reserve((size_t)tiles * sizeof(uint2)));
-        CK(cudaMemsetAsync(ctx->ranges.ptr, 0, (size_t)tiles * sizeof(uint2), stream));
-        uint32_t pairs = 0;
-        if (slots)
-        {
-            CK(ctx->tris.reserve((size_t)slots * sizeof(TriRecord)));
-            CK(ctx->tileCounts.reserve((size_t)slots * 4));
-            CK(ctx->offsets.reserve((size_t)slots * 4 + 4));
-            uint32_t slotBase = 0;
-            stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
-            for (uint32_t i = 0; i < d->draw_batch_count; ++i)
-            {
-                const rive_cuda_draw_batch& b = d->draw_batches[i];
-                if (!b.element_count)
-                    continue;
-                patch_setup_kernel<<<(b.element_count + 3) / 4, 128, 0, stream>>>(
-                    P, b.base_element, b.element_count, slotBase, b.shader_features,
-                    (TriRecord*)ctx->tris.ptr, (uint32_t*)ctx->tileCounts.ptr);
-                ++launches;
-                slotBase += b.element_count * kPatchTriangleCount;
-            }
-            stage_end(ctx, stream);
-            stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
-            // Exclusive scan of tile counts -> pair offsets; slot `slots` holds
-            // the total.
-            size_t tempBytes = 0;
-            uint32_t* counts = (uint32_t*)ctx->tileCounts.ptr;
-            uint32_t* offs = (uint32_t*)ctx->offsets.ptr;
-            CK(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
-            CK(ctx->scanTemp.reserve(tempBytes));
-            CK(cudaMemsetAsync(offs, 0, 4, stream));
-            CK(cub::DeviceScan::InclusiveSum(ctx->scanTemp.ptr, tempBytes, counts, offs + 1, slots,
-                                             stream));
-            stage_end(ctx, stream);
-            CK(cudaMemcpyAsync(ctx->hPairs, offs + slots, 4, cudaMemcpyDeviceToHost, stream));
-            CK(cudaStreamSynchronize(stream));
-            pairs = *ctx->hPairs;
-        }
-        if (pairs)
-        {
-            CK(ctx->keys.reserve((size_t)pairs * 4));
-            CK(ctx->vals.reserve((size_t)pairs * 4));
-            CK(ctx->keysAlt.reserve((size_t)pairs * 4));
-            CK(ctx->valsAlt.reserve((size_t)pairs * 4));
-            stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
-            bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
-                slots, tilesX, (const TriRecord*)ctx->tris.ptr, (const uint32_t*)ctx->tileCounts.ptr,
-                (const uint32_t*)ctx->offsets.ptr, (uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->vals.ptr);
-            stage_end(ctx, stream);
-            ++launches;
-            int endBit = 1;
-            while ((1u << endBit) < tiles)
-                ++endBit;
-            cub::DoubleBuffer<uint32_t> k((uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->keysAlt.ptr);
-            cub::DoubleBuffer<uint32_t> v((uint32_t*)ctx->vals.ptr, (uint32_t*)ctx->valsAlt.ptr);
-            size_t tempBytes = 0;
-            CK(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, k, v, (int)pairs, 0, endBit, stream));
-            CK(ctx->sortTemp.reserve(tempBytes));
-            stage_begin(ctx, RIVE_CUDA_STAGE_SORT, stream);
-            CK(cub::DeviceRadixSort::SortPairs(ctx->sortTemp.ptr, tempBytes, k, v, (int)pairs, 0,
-                                               endBit, stream));
-            tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(),
-                                                                      (uint2*)ctx->ranges.ptr);
-            stage_end(ctx, stream);
-            ++launches;
-            stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
-            raster_tile_kernel<<<tiles, 256, 0, stream>>>(P, tilesX, (const TriRecord*)ctx->tris.ptr,
-                                                          v.Current(), (const uint2*)ctx->ranges.ptr,
-                                                          fbDevice);
-            stage_end(ctx, stream);
-            ++launches;
-        }
-        else
-        {
-            stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
-            raster_tile_kernel<<<tiles, 256, 0, stream>>>(P, tilesX, (const TriRecord*)ctx->tris.ptr,
-                                                          nullptr, (const uint2*)ctx->ranges.ptr,
-                                                          fbDevice);
-            stage_end(ctx, stream);
-            ++launches;
-        }
-        CK(cudaGetLastError());
-        ctx->stats.tess_vertices = (uint64_t)d->tess_data_height * kTessTextureWidth;
-        ctx->stats.patches = instances;
-        ctx->stats.triangles = slots;
-        ctx->stats.bin_entries = pairs;
-        ctx->stats.tiles = tiles;
-        ctx->stats.kernel_launches = launches;
-        return RIVE_CUDA_OK;
-    }();
+    BatchTables B = {};
+    B.scenes = (const FlushParams*)(dT + oScenes);
+    B.gradSpanBase = (const uint32_t*)(dT + oGradBase);
+    B.tessSpanBase = (const uint32_t*)(dT + oTessBase);
+    B.tileBase = (const uint32_t*)(dT + oTileBase);
+    B.sceneTiles = (const uint2*)(dT + oSceneTiles);
+    B.segments = (const PatchSegment*)(dT + oSegments);
+    B.segInstanceBase = (const uint32_t*)(dT + oSegBase);
+    B.sceneCount = n;
+    B.segmentCount = segAcc;
+    B.totalGradSpans = gAcc;
+    B.totalTessSpans = tAcc;
+    B.totalInstances = instAcc;
+    B.totalTiles = tileAcc;
+
+    uint64_t launches = 0;
+    // Pass 1: gradient ramps. Texels no span covers are never sampled; zero
+    // them so the texture is deterministic.
+    CK(cudaMemsetAsync(ctx->grad.ptr, 0, gradBytes, stream));
+    if (gAcc)
+    {
+        stage_begin(ctx, RIVE_CUDA_STAGE_COLOR_RAMP, stream);
+        color_ramp_kernel<<<gAcc, 128, 0, stream>>>(B);
+        stage_end(ctx, stream);
+        ++launches;
+    }
+    // Pass 2: tessellation.
+    if (tAcc)
+    {
+        stage_begin(ctx, RIVE_CUDA_STAGE_TESSELLATE, stream);
+        tessellate_kernel<<<(tAcc * 32u + 255u) / 256u, 256, 0, stream>>>(B);
+        stage_end(ctx, stream);
+        ++launches;
+    }
+    // Pass 3: patch set-up + tile counts, scan, binning, sort, raster.
+    const uint32_t slots = slotAcc;
+    CK(ctx->ranges.reserve((size_t)tileAcc * sizeof(uint2)));
+    CK(cudaMemsetAsync(ctx->ranges.ptr, 0, (size_t)tileAcc * sizeof(uint2), stream));
+    uint32_t pairs = 0;
+    if (slots)
+    {
+        CK(ctx->tris.reserve((size_t)slots * sizeof(TriRecord)));
+        CK(ctx->tileCounts.reserve((size_t)slots * 4));
+        CK(ctx->offsets.reserve((size_t)slots * 4 + 4));
+        stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
+        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, (TriRecord*)ctx->tris.ptr,
+                                                                   (uint32_t*)ctx->tileCounts.ptr);
+        stage_end(ctx, stream);
+        ++launches;
+        stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
+        // Exclusive scan of tile counts -> pair offsets; slot `slots` holds
+        // the total.
+        size_t tempBytes = 0;
+        uint32_t* counts = (uint32_t*)ctx->tileCounts.ptr;
+        uint32_t* offs = (uint32_t*)ctx->offsets.ptr;
+        CK(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
+        CK(ctx->scanTemp.reserve(tempBytes));
+        CK(cudaMemsetAsync(offs, 0, 4, stream));
+        CK(cub::DeviceScan::InclusiveSum(ctx->scanTemp.ptr, tempBytes, counts, offs + 1, slots,
+                                         stream));
+        stage_end(ctx, stream);
+        CK(cudaMemcpyAsync(ctx->hPairs, offs + slots, 4, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        pairs = *ctx->hPairs;
+    }
+    const uint32_t* sortedSlots = nullptr;
+    if (pairs)
+    {
+        CK(ctx->keys.reserve((size_t)pairs * 4));
+        CK(ctx->vals.reserve((size_t)pairs * 4));
+        CK(ctx->keysAlt.reserve((size_t)pairs * 4));
+        CK(ctx->valsAlt.reserve((size_t)pairs * 4));
+        stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
+        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
+            slots, B.sceneTiles, (const TriRecord*)ctx->tris.ptr,
+            (const uint32_t*)ctx->tileCounts.ptr, (const uint32_t*)ctx->offsets.ptr,
+            (uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->vals.ptr);
+        stage_end(ctx, stream);
+        ++launches;
+        int endBit = 1;
+        while ((1ull << endBit) < tileAcc)
+            ++endBit;
+        cub::DoubleBuffer<uint32_t> k((uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->keysAlt.ptr);
+        cub::DoubleBuffer<uint32_t> v((uint32_t*)ctx->vals.ptr, (uint32_t*)ctx->valsAlt.ptr);
+        size_t tempBytes = 0;
+        CK(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, k, v, (int)pairs, 0, endBit, stream));
+        CK(ctx->sortTemp.reserve(tempBytes));
+        stage_begin(ctx, RIVE_CUDA_STAGE_SORT, stream);
+        CK(cub::DeviceRadixSort::SortPairs(ctx->sortTemp.ptr, tempBytes, k, v, (int)pairs, 0,
+                                           endBit, stream));
+        tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(),
+                                                                  (uint2*)ctx->ranges.ptr);
+        stage_end(ctx, stream);
+        ++launches;
+        sortedSlots = v.Current();
+    }
+    stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
+    raster_tile_kernel<<<tileAcc, 256, 0, stream>>>(B, (const TriRecord*)ctx->tris.ptr, sortedSlots,
+                                                    (const uint2*)ctx->ranges.ptr);
+    stage_end(ctx, stream);
+    ++launches;
+    CK(cudaGetLastError());
+    ctx->stats.tess_vertices = (uint64_t)tessRows * kTessTextureWidth;
+    ctx->stats.patches = instAcc;
+    ctx->stats.triangles = slots;
+    ctx->stats.bin_entries = pairs;
+    ctx->stats.tiles = tileAcc;
+    ctx->stats.kernel_launches = launches;
+    return RIVE_CUDA_OK;
+}
+
+int run_flush(rive_cuda_context* ctx,
+              const rive_cuda_flush_desc* d,
+              const ResolvedBuffers& rb,
+              uint32_t* fbDevice,
+              cudaStream_t stream)
+{
+    FlushInput in{d, rb, fbDevice};
+    return run_batch(ctx, &in, 1, stream);
 }
 } // namespace
 
@@ -505,8 +655,12 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
     }
     for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->offsets,
                             &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
-                            &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges})
+                            &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables})
         b->release();
+    ctx->hTables.release();
+    ctx->hUniforms.release();
+    if (ctx->tablesCopied)
+        cudaEventDestroy(ctx->tablesCopied);
     if (ctx->dError)
         cudaFree(ctx->dError);
     if (ctx->hError)
@@ -750,6 +904,36 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
     }
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     return run_flush(ctx, desc, rb, (uint32_t*)target_pixels_device, s);
+}
+
+int rive_cuda_flush_batch(rive_cuda_context* ctx,
+                          const rive_cuda_batch_flush* flushes,
+                          uint32_t count,
+                          void* cuda_stream)
+{
+    if (!ctx || (count && !flushes))
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "NULL argument to flush_batch");
+    std::vector<FlushInput> in(count);
+    for (uint32_t i = 0; i < count; ++i)
+    {
+        const rive_cuda_batch_flush& f = flushes[i];
+        if (!f.desc || !f.target_pixels_device)
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u: NULL desc or target",
+                             i);
+        const void* p[7] = {f.buffers.flush_uniforms, f.buffers.paths,    f.buffers.paints,
+                            f.buffers.paint_aux,      f.buffers.contours, f.buffers.grad_spans,
+                            f.buffers.tess_spans};
+        in[i].d = f.desc;
+        for (int k = 0; k < 7; ++k)
+        {
+            in[i].rb.ptr[k] = p[k];
+            in[i].rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0; // caller-sized
+        }
+        in[i].fb = (uint32_t*)f.target_pixels_device;
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+    return run_batch(ctx, in.data(), count, s);
 }
 
 int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)

@@ -20,29 +20,21 @@
 
 namespace rivecuda
 {
-__global__ void color_ramp_kernel(FlushParams P);
-__global__ void tessellate_kernel(FlushParams P);
-__global__ void patch_setup_kernel(FlushParams P,
-                                   uint32_t baseInstance,
-                                   uint32_t instanceCount,
-                                   uint32_t slotBase,
-                                   uint32_t features,
-                                   TriRecord* tris,
-                                   uint32_t* tileCounts);
+__global__ void color_ramp_kernel(BatchTables B);
+__global__ void tessellate_kernel(BatchTables B);
+__global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
-                                   uint32_t tilesX,
+                                   const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
                                    const uint32_t* offsets,
                                    uint32_t* keys,
                                    uint32_t* vals);
 __global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
-__global__ void raster_tile_kernel(FlushParams P,
-                                   uint32_t tilesX,
+__global__ void raster_tile_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
-                                   const uint2* ranges,
-                                   uint32_t* fb);
+                                   const uint2* ranges);
 } // namespace rivecuda
 
 using namespace rivecuda;
@@ -74,7 +66,17 @@ constexpr size_t kScanTempOff = kRangesOff + align256(kMaxTiles * sizeof(uint2))
 constexpr size_t kScanTempBytes = 64u << 10;
 constexpr size_t kSortTempOff = kScanTempOff + kScanTempBytes;
 constexpr size_t kSortTempBytes = 4u << 20;
-constexpr size_t kPoolBytes = kSortTempOff + kSortTempBytes;
+// Launch tables of the flush (a batch of one): FlushParams, prefix arrays and
+// one PatchSegment per draw batch.
+constexpr uint32_t kMaxSegments = 256;
+constexpr size_t kTabScenes = 0;
+constexpr size_t kTabPrefix = align256(sizeof(FlushParams));        // 3 x 2 u32
+constexpr size_t kTabSceneTiles = kTabPrefix + 32;                  // 1 uint2
+constexpr size_t kTabSegments = kTabSceneTiles + 16;
+constexpr size_t kTabSegBase = kTabSegments + kMaxSegments * sizeof(PatchSegment);
+constexpr size_t kTablesBytes = align256(kTabSegBase + 4 * (kMaxSegments + 1));
+constexpr size_t kTablesOff = kSortTempOff + kSortTempBytes;
+constexpr size_t kPoolBytes = kTablesOff + kTablesBytes;
 static_assert(kPoolBytes == RIVE_CUDA_NOALLOC_POOL_BYTES,
               "RIVE_CUDA_NOALLOC_POOL_BYTES must match the pool layout");
 
@@ -173,6 +175,10 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                         "batch %u reads past the tessellation texture", i);
         instances += b.element_count;
     }
+    if (d->draw_batch_count > kMaxSegments)
+        return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                    "%u draw batches exceed the no-allocation limit %u", d->draw_batch_count,
+                    kMaxSegments);
     if (instances > RIVE_CUDA_NOALLOC_MAX_PATCHES)
         return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                     "%llu patches exceed the no-allocation limit %u",
@@ -196,7 +202,6 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     }
     cudaStream_t stream = (cudaStream_t)cuda_stream;
     uint32_t* dError = (uint32_t*)(pool + kStatusOff);
-    uint32_t* fb = (uint32_t*)target_pixels_device;
 
     FlushParams P = {};
     P.paths = (const uint4*)buffers->paths;
@@ -226,6 +231,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     P.error = dError;
     P.tess = (uint4*)(pool + kTessOff);
     P.grad = (uchar4*)(pool + kGradOff);
+    P.fb = (uint32_t*)target_pixels_device;
+    P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
 
     // FlushUniforms fields (renderer/include/rive/renderer/gpu.hpp:1466-1537),
     // read into a stack copy.
@@ -239,11 +246,53 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (P.pathIDGranularity == 0)
         P.pathIDGranularity = 1;
 
-    // What must start at zero on every call: the error word, the tile
-    // ranges, the gradient rows in use and the scan's leading offset.
-    const uint32_t tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
+    const uint32_t tilesX = P.tilesX;
     const uint32_t tilesY = (d->render_target_height + kTileSize - 1) / kTileSize;
     const uint32_t tiles = tilesX * tilesY;
+
+    // Launch tables, built on the stack and copied into the pool.
+    alignas(16) uint8_t tab[kTablesBytes];
+    memset(tab, 0, sizeof(tab));
+    memcpy(tab + kTabScenes, &P, sizeof(P));
+    uint32_t* prefix = (uint32_t*)(tab + kTabPrefix); // grad, tess, tile bases: {0, total}
+    prefix[1] = d->grad_span_count;
+    prefix[3] = d->tess_span_count;
+    prefix[5] = tiles;
+    *(uint2*)(tab + kTabSceneTiles) = make_uint2(0u, tilesX);
+    PatchSegment* segs = (PatchSegment*)(tab + kTabSegments);
+    uint32_t* segBase = (uint32_t*)(tab + kTabSegBase);
+    uint32_t segCount = 0, instAcc = 0;
+    for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+    {
+        const rive_cuda_draw_batch& b = d->draw_batches[i];
+        if (!b.element_count)
+            continue;
+        segs[segCount] = PatchSegment{0u, b.base_element, b.shader_features,
+                                      instAcc * kPatchTriangleCount};
+        segBase[segCount] = instAcc;
+        ++segCount;
+        instAcc += b.element_count;
+    }
+    segBase[segCount] = instAcc;
+    uint8_t* dTab = pool + kTablesOff;
+    CKN(cudaMemcpyAsync(dTab, tab, sizeof(tab), cudaMemcpyHostToDevice, stream));
+    BatchTables B = {};
+    B.scenes = (const FlushParams*)(dTab + kTabScenes);
+    B.gradSpanBase = (const uint32_t*)(dTab + kTabPrefix);
+    B.tessSpanBase = (const uint32_t*)(dTab + kTabPrefix) + 2;
+    B.tileBase = (const uint32_t*)(dTab + kTabPrefix) + 4;
+    B.sceneTiles = (const uint2*)(dTab + kTabSceneTiles);
+    B.segments = (const PatchSegment*)(dTab + kTabSegments);
+    B.segInstanceBase = (const uint32_t*)(dTab + kTabSegBase);
+    B.sceneCount = 1;
+    B.segmentCount = segCount;
+    B.totalGradSpans = d->grad_span_count;
+    B.totalTessSpans = d->tess_span_count;
+    B.totalInstances = instAcc;
+    B.totalTiles = tiles;
+
+    // What must start at zero on every call: the error word, the tile
+    // ranges, the gradient rows in use and the scan's leading offset.
     uint2* ranges = (uint2*)(pool + kRangesOff);
     CKN(cudaMemsetAsync(dError, 0, 4, stream));
     CKN(cudaMemsetAsync(ranges, 0, (size_t)tiles * sizeof(uint2), stream));
@@ -251,9 +300,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         CKN(cudaMemsetAsync(P.grad, 0, (size_t)kGradTextureWidth * d->grad_data_height * 4, stream));
 
     if (d->grad_span_count)
-        color_ramp_kernel<<<d->grad_span_count, 128, 0, stream>>>(P);
+        color_ramp_kernel<<<d->grad_span_count, 128, 0, stream>>>(B);
     if (d->tess_span_count)
-        tessellate_kernel<<<(d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(P);
+        tessellate_kernel<<<(d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(B);
 
     TriRecord* tris = (TriRecord*)(pool + kTrisOff);
     uint32_t* counts = (uint32_t*)(pool + kCountsOff);
@@ -262,16 +311,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     uint32_t pairs = 0;
     if (slots)
     {
-        uint32_t slotBase = 0;
-        for (uint32_t i = 0; i < d->draw_batch_count; ++i)
-        {
-            const rive_cuda_draw_batch& b = d->draw_batches[i];
-            if (!b.element_count)
-                continue;
-            patch_setup_kernel<<<(b.element_count + 3) / 4, 128, 0, stream>>>(
-                P, b.base_element, b.element_count, slotBase, b.shader_features, tris, counts);
-            slotBase += b.element_count * kPatchTriangleCount;
-        }
+        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, tris, counts);
         size_t tempBytes = 0;
         CKN(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
         if (tempBytes > kScanTempBytes)
@@ -294,8 +334,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     const uint32_t* sortedSlots = nullptr;
     if (pairs)
     {
-        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(slots, tilesX, tris, counts, offs,
-                                                                   keys, vals);
+        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(slots, B.sceneTiles, tris,
+                                                                   counts, offs, keys, vals);
         int endBit = 1;
         while ((1u << endBit) < tiles)
             ++endBit;
@@ -312,7 +352,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(), ranges);
         sortedSlots = v.Current();
     }
-    raster_tile_kernel<<<tiles, 256, 0, stream>>>(P, tilesX, tris, sortedSlots, ranges, fb);
+    raster_tile_kernel<<<tiles, 256, 0, stream>>>(B, tris, sortedSlots, ranges);
     CKN(cudaGetLastError());
 
     // Device status of this flush (overflow and range flags of the kernels).

@@ -439,15 +439,11 @@ __device__ __forceinline__ int4 unpack_bbox(uint4 meta)
 }
 } // namespace
 
-// Per patch instance (one warp): shade 42 vertices, assemble and set up 24
-// triangles, then count the tiles each one touches, the warp striding over
-// each triangle's tile rectangle. Triangle slot order is primitive order
-// (batch, instance, triangle-in-patch).
-__global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
-                                                          uint32_t baseInstance,
-                                                          uint32_t instanceCount,
-                                                          uint32_t slotBase,
-                                                          uint32_t features,
+// Per patch instance of the batch (one warp): shade 42 vertices, assemble and
+// set up 24 triangles, then count the tiles each one touches, the warp
+// striding over each triangle's tile rectangle. Triangle slot order is
+// primitive order (scene, draw batch, instance, triangle-in-patch).
+__global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
                                                           TriRecord* __restrict__ tris,
                                                           uint32_t* __restrict__ tileCounts)
 {
@@ -456,10 +452,15 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
     __shared__ int4 sBox[4][kPatchTriangleCount];
     __shared__ bool sok[4];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t local = blockIdx.x * 4 + w;
-    if (local >= instanceCount)
+    const uint32_t gi = blockIdx.x * 4 + w;
+    if (gi >= B.totalInstances)
         return; // whole warp exits together
-    const uint32_t instance = baseInstance + local;
+    const uint32_t seg = find_range(B.segInstanceBase, B.segmentCount, gi);
+    const PatchSegment S = B.segments[seg];
+    const FlushParams& P = B.scenes[S.scene];
+    const uint32_t local = gi - B.segInstanceBase[seg];
+    const uint32_t instance = S.baseInstance + local;
+    const uint32_t slotBase = S.slotBase, features = S.features;
     if (lane == 0)
         sok[w] = true;
     __syncwarp();
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
                 key ^= 0x8000u;
             T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16),
                                 (uint32_t)bb.x | ((uint32_t)bb.z << 16),
-                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), key);
+                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), key | (S.scene << 16));
             tris[slot0 + lane] = T;
             sEdges[w][lane][0] = T.e0;
             sEdges[w][lane][1] = T.e1;
@@ -627,7 +628,7 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(FlushParams P,
 // its box spans few tiles; larger triangles are walked by the whole warp with
 // a ballot assigning output positions.
 __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
-                                                          uint32_t tilesX,
+                                                          const uint2* __restrict__ sceneTiles,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ tileCounts,
                                                           const uint32_t* __restrict__ offsets,
@@ -653,12 +654,13 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         {
             const TriRecord* T = tris + mySlot;
             const float4 e[3] = {T->e0, T->e1, T->e2};
+            const uint2 st = sceneTiles[T->meta.w >> 16]; // (tileBase, tilesX)
             uint32_t o = offsets[mySlot];
             for (int ty = ty0; ty < ty0 + nty; ++ty)
                 for (int tx = tx0; tx < tx0 + ntx; ++tx)
                     if (tile_overlaps(e, bb, tx, ty))
                     {
-                        keys[o] = (uint32_t)ty * tilesX + (uint32_t)tx;
+                        keys[o] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
                         vals[o] = mySlot;
                         ++o;
                     }
@@ -677,6 +679,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         const int4 bb = unpack_bbox(tris[slot].meta);
         const TriRecord* T = tris + slot;
         const float4 e[3] = {T->e0, T->e1, T->e2};
+        const uint2 st = sceneTiles[T->meta.w >> 16];
         uint32_t o = offsets[slot];
         const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
         const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
@@ -697,7 +700,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
             if (hit)
             {
                 const uint32_t pos = o + __popc(mask & ((1u << lane) - 1u));
-                keys[pos] = (uint32_t)ty * tilesX + (uint32_t)tx;
+                keys[pos] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
                 vals[pos] = slot;
             }
             o += __popc(mask);
@@ -1074,16 +1077,27 @@ static_assert(sizeof(TileTri) == 80, "TileTri layout");
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
 
-__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(FlushParams P,
-                                                          uint32_t tilesX,
-                                                          const TriRecord* __restrict__ tris,
-                                                          const uint32_t* __restrict__ sortedSlots,
-                                                          const uint2* __restrict__ ranges,
-                                                          uint32_t* __restrict__ fb)
+__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(
+    BatchTables B,
+    const TriRecord* __restrict__ tris,
+    const uint32_t* __restrict__ sortedSlots,
+    const uint2* __restrict__ ranges)
 {
     __shared__ TileTri sTris[256];
     __shared__ uint8_t sMask[256];
-    const uint32_t tile = blockIdx.x;
+    __shared__ FlushParams sP;
+    const uint32_t gtile = blockIdx.x;
+    const uint2 range = ranges[gtile];
+    // The tile's scene: its parameters are staged once for the whole CTA.
+    const uint32_t scene = find_range(B.tileBase, B.sceneCount, gtile);
+    if (threadIdx.x < sizeof(FlushParams) / 4)
+        reinterpret_cast<uint32_t*>(&sP)[threadIdx.x] =
+            reinterpret_cast<const uint32_t*>(B.scenes + scene)[threadIdx.x];
+    __syncthreads();
+    const FlushParams& P = sP;
+    uint32_t* __restrict__ fb = P.fb;
+    const uint32_t tilesX = P.tilesX;
+    const uint32_t tile = gtile - B.tileBase[scene];
     const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
     const int ox = tx * kTileSize, oy = ty * kTileSize;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1091,7 +1105,6 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
     const int px = ox + lxi, py = oy + lyi;
     const float lx = (float)lxi, ly = (float)lyi;
     const bool inBounds = px < (int)P.width && py < (int)P.height;
-    const uint2 range = ranges[tile];
     if (range.y <= range.x && !P.loadClear)
         return;
     Pixel s;

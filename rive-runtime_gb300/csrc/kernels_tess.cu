@@ -344,13 +344,16 @@ __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flag
 }
 } // namespace
 
-// One block of 128 threads per GradientSpan; each thread owns 4 of the 512
-// texel columns.
-__global__ void __launch_bounds__(128) color_ramp_kernel(FlushParams P)
+// One block of 128 threads per GradientSpan of the batch; each thread owns 4
+// of the 512 texel columns.
+__global__ void __launch_bounds__(128) color_ramp_kernel(BatchTables B)
 {
-    const uint32_t s = blockIdx.x;
-    if (s >= P.gradSpanCount)
+    const uint32_t g = blockIdx.x;
+    if (g >= B.totalGradSpans)
         return;
+    const uint32_t scene = find_range(B.gradSpanBase, B.sceneCount, g);
+    const FlushParams& P = B.scenes[scene];
+    const uint32_t s = g - B.gradSpanBase[scene];
     uint4 sp = P.gradSpans[P.firstGradSpan + s];
     uint32_t y = sp.y & ~GRAD_SPAN_FLAGS_MASK;
     if (y >= P.gradDataHeight)
@@ -396,13 +399,17 @@ __global__ void __launch_bounds__(128) color_ramp_kernel(FlushParams P)
     }
 }
 
-// One warp per TessVertexSpan (both its forward and mirrored rectangles).
-__global__ void __launch_bounds__(256) tessellate_kernel(FlushParams P)
+// One warp per TessVertexSpan of the batch (both its forward and mirrored
+// rectangles).
+__global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
 {
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= P.tessSpanCount)
+    if (gw >= B.totalTessSpans)
         return;
+    const uint32_t scene = find_range(B.tessSpanBase, B.sceneCount, gw);
+    const FlushParams& P = B.scenes[scene];
+    const uint32_t warp = gw - B.tessSpanBase[scene];
     const uint4* sp = P.tessSpans + 4 * (size_t)(P.firstTessSpan + warp);
     SpanSetup s = span_setup(P, sp);
     if (!s.valid)

@@ -97,7 +97,7 @@ struct __align__(16) TriRecord
     float4 e2;
     float4 cov0; // covx: c, gx, gy; covy: c
     float4 cov1; // covy: gx, gy; paint.x, paint.y (as float bits)
-    uint4 meta;  // pathAndFeatures, x0 | x1 << 16, y0 | y1 << 16, unused
+    uint4 meta;  // pathAndFeatures, x0 | x1 << 16, y0 | y1 << 16, key | scene << 16
 };
 static_assert(sizeof(TriRecord) == 96, "TriRecord layout");
 
@@ -126,5 +126,46 @@ struct FlushParams
     uint4* tess;    // 2048 x tessDataHeight
     uchar4* grad;   // 512 x gradDataHeight
     uint32_t* error;
+    uint32_t* fb;   // render target, RGBA8, width x height
+    uint32_t tilesX;
 };
+
+// A run of patch instances of one flush drawn with one set of shader
+// features (one DrawBatch), and where its triangle slots start.
+struct PatchSegment
+{
+    uint32_t scene, baseInstance, features, slotBase;
+};
+
+// The work of a batch of independent logical flushes ("scenes"); a single
+// flush is a batch of one. Every kernel maps its global work index to a scene
+// through the prefix arrays (base[0] = 0, base[count] = total).
+struct BatchTables
+{
+    const FlushParams* scenes;       // [sceneCount]
+    const uint32_t* gradSpanBase;    // [sceneCount + 1]
+    const uint32_t* tessSpanBase;    // [sceneCount + 1]
+    const uint32_t* tileBase;        // [sceneCount + 1]
+    const uint2* sceneTiles;         // [sceneCount]: (tileBase, tilesX)
+    const PatchSegment* segments;    // [segmentCount]
+    const uint32_t* segInstanceBase; // [segmentCount + 1]
+    uint32_t sceneCount, segmentCount;
+    uint32_t totalGradSpans, totalTessSpans, totalInstances, totalTiles;
+};
+
+// Index j with base[j] <= i < base[j + 1] (empty ranges skipped), n >= 1.
+__device__ __forceinline__ uint32_t find_range(const uint32_t* __restrict__ base, uint32_t n,
+                                               uint32_t i)
+{
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(base + mid) <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
 } // namespace rivecuda

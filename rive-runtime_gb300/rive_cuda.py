@@ -47,6 +47,11 @@ class DeviceBuffers(ctypes.Structure):
         "grad_spans", "tess_spans")]
 
 
+class BatchFlush(ctypes.Structure):
+    _fields_ = [("desc", ctypes.c_void_p), ("buffers", DeviceBuffers),
+                ("target_pixels_device", ctypes.c_void_p)]
+
+
 class FlushStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "tess_vertices", "patches", "triangles", "bin_entries", "tiles",
@@ -92,6 +97,7 @@ def load():
         "rive_cuda_flush": (i32, [vp, ctypes.POINTER(FlushDesc), vp, vp]),
         "rive_cuda_flush_device": (i32, [vp, ctypes.POINTER(FlushDesc),
                                          ctypes.POINTER(DeviceBuffers), vp, vp]),
+        "rive_cuda_flush_batch": (i32, [vp, ctypes.POINTER(BatchFlush), u32, vp]),
         "rive_cuda_flush_device_noalloc": (i32, [ctypes.POINTER(FlushDesc),
                                                  ctypes.POINTER(DeviceBuffers), vp, vp,
                                                  ctypes.c_char_p, sz]),
@@ -209,6 +215,20 @@ class Context:
         self.check(self.lib.rive_cuda_flush_device(self.h, ctypes.byref(d), ctypes.byref(bufs),
                                                    ctypes.c_void_p(target_ptr), stream),
                    "flush_device")
+        del keep
+
+    def flush_batch(self, items, stream=None):
+        """rive_cuda_flush_batch over [(capture.Flush, DeviceBuffers, target_ptr), ...]:
+        independent flushes (distinct targets) in one sequence of launches."""
+        arr = (BatchFlush * len(items))()
+        keep = []
+        for i, (flush, bufs, target_ptr) in enumerate(items):
+            d, k = make_desc(flush)
+            keep.append((d, k))
+            arr[i].desc = ctypes.cast(ctypes.pointer(d), ctypes.c_void_p)
+            arr[i].buffers = bufs
+            arr[i].target_pixels_device = target_ptr
+        self.check(self.lib.rive_cuda_flush_batch(self.h, arr, len(items), stream), "flush_batch")
         del keep
 
     def sync(self, stream=None):

@@ -180,6 +180,48 @@ def plain_small(seed: int = 1, width: int = 512, height: int = 512,
     return sc
 
 
+def plain_canvas(rng, width: int, height: int, n_paths: int, cubics: int = 8) -> Scene:
+    """The plain path distribution on a width x height canvas: closed
+    single-contour fills of `cubics` cubics with every control point uniform
+    over the canvas, nonzero, identity transform, solid colours (RGB uniform,
+    alpha uniform in [0.5, 1]), srcOver, cleared to opaque white."""
+    sc = Scene(width, height, clear_color=0xFFFFFFFF)
+    ext = np.array([width, height], np.float64)
+    for _ in range(n_paths):
+        p0 = rng.uniform(0.0, 1.0, 2) * ext
+        pts = [p0]
+        verbs = [VERB_MOVE]
+        for i in range(cubics):
+            c = rng.uniform(0.0, 1.0, (3, 2)) * ext
+            if i == cubics - 1:
+                c[2] = p0
+            pts.extend(c)
+            verbs.append(VERB_CUBIC)
+        verbs.append(VERB_CLOSE)
+        pi = sc.add_path(Path(verbs, np.array(pts, np.float32), FILL_NONZERO))
+        qi = sc.add_paint(Paint(style=STYLE_FILL, color=_random_color(rng)))
+        sc.cmd(CMD_DRAW_PATH, pi, qi)
+    return sc
+
+
+def batched_scenes(seed: int = 3, count: int = 256, size_range=(256, 1920),
+                   paths_median: float = 400.0, paths_sigma: float = 1.0,
+                   paths_range=(50, 3000)):
+    """The batched workload: `count` independent scenes with the plain path
+    distribution; width and height independently log-uniform in size_range,
+    path count lognormal(ln paths_median, paths_sigma) clipped to paths_range."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(size_range[0]), math.log(size_range[1])
+    scenes = []
+    for _ in range(count):
+        w = int(round(math.exp(rng.uniform(lo, hi))))
+        h = int(round(math.exp(rng.uniform(lo, hi))))
+        n = int(np.clip(round(rng.lognormal(math.log(paths_median), paths_sigma)),
+                        paths_range[0], paths_range[1]))
+        scenes.append(plain_canvas(rng, w, h, n))
+    return scenes
+
+
 def _random_affine(rng, width, height, scale_range=(0.25, 4.0)):
     theta = rng.uniform(0.0, 2.0 * math.pi)
     s = math.exp(rng.uniform(math.log(scale_range[0]), math.log(scale_range[1])))
