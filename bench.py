@@ -181,7 +181,10 @@ def run_ours(args, cap, wname, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
-    stream = torch.cuda.current_stream()
+    # A stream of our own: the flushes and the timing events must share one
+    # stream (the library's default stream does not order with torch's).
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = rive_cuda.Context(dev)
     W, H = cap.width, cap.height
 
@@ -293,6 +296,10 @@ def run_ours(args, cap, wname, rank, world):
         "gpu_launches": int(sum(v[1] for v in prof.values())),
         "clocks": clocks,
     }
+    ctx.close()
+    del keep, target
+    if args.batch_scenes > 0:
+        line["batched"] = run_batched(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -301,7 +308,74 @@ def run_ours(args, cap, wname, rank, world):
                                 "sample": f"1 whole frame of {wname} through the oracle"}
     if rank == 0:
         print(json.dumps(line))
+
+
+def run_batched(args, dev):
+    """The batched form: N independent scenes of uneven canvas sizes and path
+    counts (scene.batched_scenes), rendered (a) one flush at a time, (b) as
+    one rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch
+    per flush index. Frames/s counts scenes; each pass renders every scene
+    once, with the records resident in HBM."""
+    import numpy as np
+    import torch
+    from rive_runtime_gb300 import planner, rive_cuda, scene
+    from rive_runtime_gb300.capture import BUFFER_NAMES
+
+    caps = [planner.plan(sc.to_bytes()) for sc in scene.batched_scenes(count=args.batch_scenes)]
+    stream = torch.cuda.current_stream()
+    keep, bufs, targets = [], [], []
+    for cap in caps:
+        b = rive_cuda.DeviceBuffers()
+        for name in BUFFER_NAMES:
+            d = cap.buffers.get(name, b"")
+            t = torch.from_numpy(np.frombuffer(d, np.uint8).copy()).cuda() if d else None
+            keep.append(t)
+            setattr(b, name, t.data_ptr() if t is not None else None)
+        bufs.append(b)
+        targets.append(torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8, device="cuda"))
+    nflush = max(len(c.flushes) for c in caps)
+    waves = [[(c.flushes[k], b, t.data_ptr()) for c, b, t in zip(caps, bufs, targets)
+              if k < len(c.flushes)] for k in range(nflush)]
+    steps = max(1, args.batch_steps)
+
+    def timed(fn):
+        fn()  # warm-up pass (also sizes every buffer)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ctx = rive_cuda.Context(dev)
+    ms_plain = timed(lambda: [ctx.flush_device(f, b, tp, stream.cuda_stream)
+                              for w in waves for (f, b, tp) in w])
+    ms_batch = timed(lambda: [ctx.flush_batch(w, stream.cuda_stream) for w in waves])
+    ctx.sync(stream.cuda_stream)
+    entries = ctx.stats()["bin_entries"]
     ctx.close()
+    ctx = rive_cuda.Context(dev)
+    graphs = [ctx.graph(w) for w in waves]
+    ms_graph = timed(lambda: [g.launch(stream.cuda_stream) for g in graphs])
+    for g in graphs:
+        g.check(stream.cuda_stream)
+        g.close()
+    ctx.close()
+    n = len(caps)
+    px = sum(c.width * c.height for c in caps)
+    return {"workload": f"batched_{n}", "scenes": n, "mpx": px / 1e6,
+            "paths": int(sum(f.desc["path_count"] for c in caps for f in c.flushes)),
+            "flushes": int(sum(len(c.flushes) for c in caps)),
+            "bin_entries_last_wave": int(entries),
+            "plain_frames_per_s": n * 1e3 / ms_plain,
+            "batch_frames_per_s": n * 1e3 / ms_batch,
+            "graph_frames_per_s": n * 1e3 / ms_graph,
+            "graph_gpx_per_s": px / (ms_graph * 1e6),
+            "speedup_vs_plain": ms_plain / ms_graph,
+            "steps": steps}
 
 
 def main():
@@ -315,6 +389,9 @@ def main():
     ap.add_argument("--steps-cpu", type=int, default=2)
     ap.add_argument("--warmup-cpu", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=256,
+                    help="scenes of the batched-form measurement (0 skips it)")
+    ap.add_argument("--batch-steps", type=int, default=2)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -246,6 +246,32 @@ int rive_cuda_flush_batch(rive_cuda_context* ctx,
                           void* cuda_stream);
 
 /*
+ * A batch captured as a CUDA graph (no counterpart in the reference). Takes
+ * the same flushes as rive_cuda_flush_batch and captures the whole batch --
+ * every pass of every flush -- into one graph that owns all intermediates.
+ * A launch replays it with no host synchronisation and no allocation: the
+ * records are read through the device pointers given here, so the caller may
+ * rewrite their contents between launches as long as every count and offset
+ * in the descriptors stays the same.
+ *
+ * `bin_capacity` fixes the number of tile bin entries the graph holds; 0 runs
+ * the set-up once at creation and takes the measured total plus an eighth.
+ * A launch that needs more drops the excess and sets a device status, which
+ * rive_cuda_graph_check (waits for the stream) returns as
+ * RIVE_CUDA_ERR_DEVICE_STATUS. Launches on one graph must not overlap in
+ * time (they share its intermediates); NULL stream: the graph's own stream.
+ */
+typedef struct rive_cuda_graph rive_cuda_graph;
+int rive_cuda_graph_create(rive_cuda_context* ctx,
+                           const rive_cuda_batch_flush* flushes,
+                           uint32_t count,
+                           uint32_t bin_capacity,
+                           rive_cuda_graph** out_graph);
+int rive_cuda_graph_launch(rive_cuda_graph* graph, void* cuda_stream);
+int rive_cuda_graph_check(rive_cuda_graph* graph, void* cuda_stream);
+void rive_cuda_graph_destroy(rive_cuda_graph* graph);
+
+/*
  * No-allocation flush (no counterpart in the reference). Same inputs and
  * result as rive_cuda_flush_device, without a context: every intermediate
  * lives in one fixed device pool of RIVE_CUDA_NOALLOC_POOL_BYTES per device,
@@ -259,13 +285,13 @@ int rive_cuda_flush_batch(rive_cuda_context* ctx,
  * up to RIVE_CUDA_NOALLOC_MAX_WIDTH x RIVE_CUDA_NOALLOC_MAX_HEIGHT, up to
  * RIVE_CUDA_NOALLOC_MAX_TESS_ROWS tessellation rows (so up to
  * RIVE_CUDA_NOALLOC_MAX_PATCHES patches), RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS
- * gradient rows, and RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES tile bin entries (this
- * one is known only after set-up; the call then returns without writing the
- * target).
+ * gradient rows, 256 draw batches and RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES tile
+ * bin entries (this one is known only after set-up; the call then returns
+ * without writing the target).
  *
  * The call clears what must start at zero (status word, tile ranges,
  * gradient rows in use) itself. It waits for `cuda_stream` (NULL: the legacy
- * default stream) twice, to read the flush uniforms and the bin total, and
+ * default stream) twice, to read the bin total and at the end, and
  * returns after the whole flush has run, with the device status checked
  * (RIVE_CUDA_ERR_DEVICE_STATUS as rive_cuda_sync reports it). The first call
  * on each device looks up the pool's address (cudaGetSymbolAddress); make
@@ -318,6 +344,8 @@ typedef struct rive_cuda_flush_stats
 } rive_cuda_flush_stats;
 int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
                                rive_cuda_flush_stats* out);
+/* Counters of a graph's batch (bin_entries as measured at creation). */
+int rive_cuda_graph_stats(const rive_cuda_graph* graph, rive_cuda_flush_stats* out);
 
 /*
  * Per-stage device timing with CUDA events recorded on the flush stream

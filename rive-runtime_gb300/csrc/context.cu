@@ -29,14 +29,24 @@ namespace rivecuda
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
+__global__ void bin_fill_kernel(const uint32_t* pairTotal,
+                                uint32_t capacity,
+                                uint32_t sentinel,
+                                uint32_t* keys);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
                                    const uint32_t* offsets,
+                                   uint32_t capacity,
+                                   uint32_t* error,
                                    uint32_t* keys,
                                    uint32_t* vals);
-__global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
+__global__ void tile_ranges_kernel(uint32_t pairCount,
+                                   uint32_t tileCount,
+                                   const uint32_t* keys,
+                                   uint2* ranges);
 __global__ void raster_tile_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
@@ -133,8 +143,8 @@ struct rive_cuda_context
     uint32_t tessWidth = 0, tessHeight = 0, gradWidth = 0, gradHeight = 0;
     DeviceBuffer tris, tileCounts, offsets;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
-    DeviceBuffer dTables;           // batch tables (device)
-    HostBuffer hTables, hUniforms;  // pinned staging of tables and uniforms
+    DeviceBuffer dTables;  // batch tables (device)
+    HostBuffer hTables;    // pinned staging of the tables
     cudaEvent_t tablesCopied = nullptr;
     uint32_t* dError = nullptr;
     uint32_t* hError = nullptr;  // pinned
@@ -148,6 +158,21 @@ struct rive_cuda_context
     int openStage = -1;
     // Last flush's texture extents (for debug read-backs).
     size_t lastTessBytes = 0, lastGradBytes = 0;
+};
+
+// A batch captured as a CUDA graph (rive_cuda_graph_*): it owns every
+// intermediate, so replays never allocate and never wait for the host.
+struct rive_cuda_graph
+{
+    rive_cuda_context* ctx = nullptr;
+    DeviceBuffer tables, tess, grad, tris, counts, offsets, keys, vals, keysAlt, valsAlt, scanTemp,
+        sortTemp, ranges, error;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t* hError = nullptr; // pinned
+    uint32_t capacity = 0, measured = 0;
+    rive_cuda_flush_stats stats = {};
 };
 
 namespace
@@ -230,9 +255,6 @@ struct ResolvedBuffers
 {
     const void* ptr[7];
     size_t bytes[7];
-    // Host copy of the flush-uniform buffer when the caller staged it through
-    // a mapped ring (read directly instead of copying it back).
-    const void* hostUniforms = nullptr;
 };
 
 // One logical flush of a batch.
@@ -301,29 +323,63 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
 
 size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 
-// Runs a batch of independent logical flushes (distinct targets) as one
-// sequence of launches: every stage covers the work of all flushes at once.
-int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStream_t stream)
+// Host-side layout of a batch of independent logical flushes.
+struct BatchLayout
 {
-    if (n == 0)
-        return RIVE_CUDA_OK;
-    if (n > 65535)
-        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "at most 65535 flushes per batch");
-    std::vector<uint64_t> inst(n);
-    uint64_t totalInstances = 0, segCount = 0;
+    uint32_t n = 0, segCount = 0;
+    uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, instances = 0, slots = 0;
+    uint64_t tessRows = 0, gradRows = 0;
+    std::vector<uint64_t> tessRow0, gradRow0;
+    // Table blob offsets.
+    size_t oScenes = 0, oGradBase = 0, oTessBase = 0, oTileBase = 0, oSceneTiles = 0,
+           oSegments = 0, oSegBase = 0, tableBytes = 0;
+    size_t tessBytes() const { return (size_t)kTessTextureWidth * tessRows * 16; }
+    size_t gradBytes() const { return (size_t)kGradTextureWidth * gradRows * 4; }
+    int endBit() const
+    {
+        int b = 1;
+        while ((1ull << b) <= tiles) // room for the sentinel key `tiles`
+            ++b;
+        return b;
+    }
+};
+
+// Validates the flushes and lays out their work.
+int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLayout& L)
+{
+    if (n == 0 || n > 65535)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "a batch holds 1 to 65535 flushes");
+    L = BatchLayout();
+    L.n = n;
+    L.tessRow0.resize(n);
+    L.gradRow0.resize(n);
+    uint64_t instances = 0, segs = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
     for (uint32_t i = 0; i < n; ++i)
     {
-        int rc = validate_flush(ctx, in[i].d, in[i].rb, inst[i]);
+        uint64_t inst = 0;
+        int rc = validate_flush(ctx, in[i].d, in[i].rb, inst);
         if (rc)
             return rc;
         if (!in[i].fb)
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u has no target", i);
-        totalInstances += inst[i];
-        for (uint32_t b = 0; b < in[i].d->draw_batch_count; ++b)
-            segCount += in[i].d->draw_batches[b].element_count ? 1 : 0;
+        if (!in[i].rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM])
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u has no uniforms", i);
+        const rive_cuda_flush_desc* d = in[i].d;
+        instances += inst;
+        for (uint32_t b = 0; b < d->draw_batch_count; ++b)
+            segs += d->draw_batches[b].element_count ? 1 : 0;
+        L.tessRow0[i] = L.tessRows;
+        L.gradRow0[i] = L.gradRows;
+        L.tessRows += std::max(d->tess_data_height, 1u);
+        L.gradRows += std::max(d->grad_data_height, 1u);
+        tiles += (uint64_t)((d->render_target_width + kTileSize - 1) / kTileSize) *
+                 ((d->render_target_height + kTileSize - 1) / kTileSize);
+        gradSpans += d->grad_span_count;
+        tessSpans += d->tess_span_count;
     }
-    if (totalInstances * kPatchTriangleCount > 0xffffffffull)
-        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "too many patches in one batch");
+    if (instances * kPatchTriangleCount > 0xffffffffull || tiles >= 0x7fffffffull ||
+        gradSpans > 0x7fffffffull || tessSpans * 32 > 0xffffffffull)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "batch too large");
     if (n > 1)
     {
         // The flushes of one batch run concurrently: each needs its own target.
@@ -335,81 +391,57 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                              "two flushes of one batch share a render target");
     }
+    L.segCount = (uint32_t)segs;
+    L.gradSpans = (uint32_t)gradSpans;
+    L.tessSpans = (uint32_t)tessSpans;
+    L.tiles = (uint32_t)tiles;
+    L.instances = (uint32_t)instances;
+    L.slots = (uint32_t)(instances * kPatchTriangleCount);
+    L.oScenes = 0;
+    L.oGradBase = align16(L.oScenes + sizeof(FlushParams) * n);
+    L.oTessBase = align16(L.oGradBase + 4 * (n + 1));
+    L.oTileBase = align16(L.oTessBase + 4 * (n + 1));
+    L.oSceneTiles = align16(L.oTileBase + 4 * (n + 1));
+    L.oSegments = align16(L.oSceneTiles + 8 * n);
+    L.oSegBase = align16(L.oSegments + sizeof(PatchSegment) * std::max<uint64_t>(segs, 1));
+    L.tableBytes = align16(L.oSegBase + 4 * (segs + 1));
+    return RIVE_CUDA_OK;
+}
 
-    // The previous batch's tables may still be in flight from the staging.
-    if (ctx->tablesCopied)
-        CK(cudaEventSynchronize(ctx->tablesCopied));
+// Device pointers of a batch's intermediates.
+struct Scratch
+{
+    uint8_t* tables = nullptr; // device copy of the table blob
+    uint4* tess = nullptr;
+    uchar4* grad = nullptr;
+    TriRecord* tris = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* offsets = nullptr; // slots + 1 entries
+    uint32_t *keys = nullptr, *vals = nullptr, *keysAlt = nullptr, *valsAlt = nullptr;
+    void* scanTemp = nullptr;
+    size_t scanTempBytes = 0;
+    void* sortTemp = nullptr;
+    size_t sortTempBytes = 0;
+    uint2* ranges = nullptr;
+    uint32_t* error = nullptr;
+};
 
-    // Flush uniforms (FlushUniforms, gpu.hpp:1466-1537): from the mapped ring
-    // when staged there, else copied back from the device in one wait.
-    CK(ctx->hUniforms.reserve((size_t)n * 256));
-    uint8_t* uni = (uint8_t*)ctx->hUniforms.ptr;
-    bool waitUniforms = false;
-    for (uint32_t i = 0; i < n; ++i)
-    {
-        const rive_cuda_flush_desc* d = in[i].d;
-        if (in[i].rb.hostUniforms)
-            memcpy(uni + 256 * (size_t)i,
-                   (const uint8_t*)in[i].rb.hostUniforms + d->flush_uniform_offset_bytes, 256);
-        else
-        {
-            CK(cudaMemcpyAsync(uni + 256 * (size_t)i,
-                               (const uint8_t*)in[i].rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM] +
-                                   d->flush_uniform_offset_bytes,
-                               256, cudaMemcpyDeviceToHost, stream));
-            waitUniforms = true;
-        }
-    }
-    if (waitUniforms)
-        CK(cudaStreamSynchronize(stream));
-
-    // Layout of the batch: per-flush texture rows, tiles, spans and slots.
-    uint64_t tessRows = 0, gradRows = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
-    std::vector<uint64_t> tessRow0(n), gradRow0(n);
-    for (uint32_t i = 0; i < n; ++i)
-    {
-        const rive_cuda_flush_desc* d = in[i].d;
-        tessRow0[i] = tessRows;
-        gradRow0[i] = gradRows;
-        tessRows += std::max(d->tess_data_height, 1u);
-        gradRows += std::max(d->grad_data_height, 1u);
-        const uint64_t tx = (d->render_target_width + kTileSize - 1) / kTileSize;
-        const uint64_t ty = (d->render_target_height + kTileSize - 1) / kTileSize;
-        tiles += tx * ty;
-        gradSpans += d->grad_span_count;
-        tessSpans += d->tess_span_count;
-    }
-    if (tiles > 0x7fffffffull || gradSpans > 0x7fffffffull || tessSpans * 32 > 0xffffffffull)
-        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "batch too large");
-    const size_t tessBytes = (size_t)kTessTextureWidth * tessRows * 16;
-    const size_t gradBytes = (size_t)kGradTextureWidth * gradRows * 4;
-    CK(ctx->tess.reserve(tessBytes));
-    CK(ctx->grad.reserve(gradBytes));
-    ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
-    ctx->lastGradBytes = (size_t)kGradTextureWidth * std::max(in[0].d->grad_data_height, 1u) * 4;
-
-    // Tables, staged in pinned memory and copied in one piece.
-    const size_t oScenes = 0;
-    const size_t oGradBase = align16(oScenes + sizeof(FlushParams) * n);
-    const size_t oTessBase = align16(oGradBase + 4 * (n + 1));
-    const size_t oTileBase = align16(oTessBase + 4 * (n + 1));
-    const size_t oSceneTiles = align16(oTileBase + 4 * (n + 1));
-    const size_t oSegments = align16(oSceneTiles + 8 * n);
-    const size_t oSegBase = align16(oSegments + sizeof(PatchSegment) * std::max<uint64_t>(segCount, 1));
-    const size_t tableBytes = align16(oSegBase + 4 * (segCount + 1));
-    CK(ctx->hTables.reserve(tableBytes));
-    CK(ctx->dTables.reserve(tableBytes));
-    uint8_t* h = (uint8_t*)ctx->hTables.ptr;
-    uint8_t* dT = (uint8_t*)ctx->dTables.ptr;
-    auto* scenes = (FlushParams*)(h + oScenes);
-    auto* gradBase = (uint32_t*)(h + oGradBase);
-    auto* tessBase = (uint32_t*)(h + oTessBase);
-    auto* tileBase = (uint32_t*)(h + oTileBase);
-    auto* sceneTiles = (uint2*)(h + oSceneTiles);
-    auto* segs = (PatchSegment*)(h + oSegments);
-    auto* segBase = (uint32_t*)(h + oSegBase);
+// Fills the table blob (host memory) and returns the device view of it.
+BatchTables write_tables(rive_cuda_context* ctx,
+                         const FlushInput* in,
+                         const BatchLayout& L,
+                         const Scratch& S,
+                         uint8_t* h)
+{
+    auto* scenes = (FlushParams*)(h + L.oScenes);
+    auto* gradBase = (uint32_t*)(h + L.oGradBase);
+    auto* tessBase = (uint32_t*)(h + L.oTessBase);
+    auto* tileBase = (uint32_t*)(h + L.oTileBase);
+    auto* sceneTiles = (uint2*)(h + L.oSceneTiles);
+    auto* segs = (PatchSegment*)(h + L.oSegments);
+    auto* segBase = (uint32_t*)(h + L.oSegBase);
     uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, segAcc = 0, instAcc = 0, slotAcc = 0;
-    for (uint32_t i = 0; i < n; ++i)
+    for (uint32_t i = 0; i < L.n; ++i)
     {
         const rive_cuda_flush_desc* d = in[i].d;
         const ResolvedBuffers& rb = in[i].rb;
@@ -421,6 +453,8 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         P.contours = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_CONTOUR];
         P.gradSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_GRAD_SPAN];
         P.tessSpans = (const uint4*)rb.ptr[RIVE_CUDA_BUFFER_TESS_SPAN];
+        P.uniforms = (const uint8_t*)rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM] +
+                     d->flush_uniform_offset_bytes;
         P.firstPath = d->first_path;
         P.firstPaint = d->first_paint;
         P.firstPaintAux = d->first_paint_aux;
@@ -432,26 +466,21 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         P.pathCount = d->path_count;
         P.contourCount = d->contour_count;
         P.gradDataHeight = d->grad_data_height;
-        P.gradTextureHeight = d->grad_texture_height              ? d->grad_texture_height
-                              : (n == 1 && ctx->gradHeight != 0u) ? ctx->gradHeight
-                                                                  : d->grad_data_height;
+        P.gradTextureHeight = d->grad_texture_height                ? d->grad_texture_height
+                              : (L.n == 1 && ctx->gradHeight != 0u) ? ctx->gradHeight
+                                                                    : d->grad_data_height;
         P.tessDataHeight = d->tess_data_height;
         P.width = d->render_target_width;
         P.height = d->render_target_height;
         P.wireframe = d->wireframe;
         P.loadClear = d->color_load_action == RIVE_CUDA_LOAD_CLEAR;
         P.clearColorPremulRGBA = premul_rgba8(d->color_clear_value);
-        P.error = ctx->dError;
+        P.pathIDGranularity = 1; // replaced on the device by scene_uniforms_kernel
+        P.error = S.error;
         P.fb = in[i].fb;
         P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
-        const uint8_t* u = uni + 256 * (size_t)i;
-        memcpy(&P.pathIDGranularity, u + 72, 4);
-        memcpy(&P.ditherScale, u + 88, 4);
-        memcpy(&P.ditherBias, u + 92, 4);
-        if (P.pathIDGranularity == 0)
-            P.pathIDGranularity = 1;
-        P.tess = (uint4*)ctx->tess.ptr + (size_t)tessRow0[i] * kTessTextureWidth;
-        P.grad = (uchar4*)ctx->grad.ptr + (size_t)gradRow0[i] * kGradTextureWidth;
+        P.tess = S.tess + (size_t)L.tessRow0[i] * kTessTextureWidth;
+        P.grad = S.grad + (size_t)L.gradRow0[i] * kGradTextureWidth;
 
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
@@ -472,123 +501,203 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
             slotAcc += db.element_count * kPatchTriangleCount;
         }
     }
-    gradBase[n] = gAcc;
-    tessBase[n] = tAcc;
-    tileBase[n] = tileAcc;
+    gradBase[L.n] = gAcc;
+    tessBase[L.n] = tAcc;
+    tileBase[L.n] = tileAcc;
     segBase[segAcc] = instAcc;
-    CK(cudaMemcpyAsync(dT, h, tableBytes, cudaMemcpyHostToDevice, stream));
-    if (!ctx->tablesCopied)
-        CK(cudaEventCreateWithFlags(&ctx->tablesCopied, cudaEventDisableTiming));
-    CK(cudaEventRecord(ctx->tablesCopied, stream));
 
     BatchTables B = {};
-    B.scenes = (const FlushParams*)(dT + oScenes);
-    B.gradSpanBase = (const uint32_t*)(dT + oGradBase);
-    B.tessSpanBase = (const uint32_t*)(dT + oTessBase);
-    B.tileBase = (const uint32_t*)(dT + oTileBase);
-    B.sceneTiles = (const uint2*)(dT + oSceneTiles);
-    B.segments = (const PatchSegment*)(dT + oSegments);
-    B.segInstanceBase = (const uint32_t*)(dT + oSegBase);
-    B.sceneCount = n;
+    const uint8_t* dT = S.tables;
+    B.scenes = (const FlushParams*)(dT + L.oScenes);
+    B.gradSpanBase = (const uint32_t*)(dT + L.oGradBase);
+    B.tessSpanBase = (const uint32_t*)(dT + L.oTessBase);
+    B.tileBase = (const uint32_t*)(dT + L.oTileBase);
+    B.sceneTiles = (const uint2*)(dT + L.oSceneTiles);
+    B.segments = (const PatchSegment*)(dT + L.oSegments);
+    B.segInstanceBase = (const uint32_t*)(dT + L.oSegBase);
+    B.sceneCount = L.n;
     B.segmentCount = segAcc;
     B.totalGradSpans = gAcc;
     B.totalTessSpans = tAcc;
     B.totalInstances = instAcc;
     B.totalTiles = tileAcc;
+    return B;
+}
 
-    uint64_t launches = 0;
-    // Pass 1: gradient ramps. Texels no span covers are never sampled; zero
-    // them so the texture is deterministic.
-    CK(cudaMemsetAsync(ctx->grad.ptr, 0, gradBytes, stream));
-    if (gAcc)
+// Enqueues the passes up to and including the scan of tile counts (so
+// S.offsets[L.slots] holds the batch's bin-entry total on the device).
+int enqueue_front(rive_cuda_context* ctx,
+                  const BatchLayout& L,
+                  const BatchTables& B,
+                  const Scratch& S,
+                  cudaStream_t stream)
+{
+    scene_uniforms_kernel<<<(L.n + 127) / 128, 128, 0, stream>>>(
+        const_cast<FlushParams*>(B.scenes), L.n);
+    // Texels no span covers are never sampled; zero them so the gradient
+    // texture is deterministic.
+    CK(cudaMemsetAsync(S.grad, 0, L.gradBytes(), stream));
+    CK(cudaMemsetAsync(S.ranges, 0, (size_t)L.tiles * sizeof(uint2), stream));
+    if (L.gradSpans)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_COLOR_RAMP, stream);
-        color_ramp_kernel<<<gAcc, 128, 0, stream>>>(B);
+        color_ramp_kernel<<<L.gradSpans, 128, 0, stream>>>(B);
         stage_end(ctx, stream);
-        ++launches;
     }
-    // Pass 2: tessellation.
-    if (tAcc)
+    if (L.tessSpans)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_TESSELLATE, stream);
-        tessellate_kernel<<<(tAcc * 32u + 255u) / 256u, 256, 0, stream>>>(B);
+        tessellate_kernel<<<(L.tessSpans * 32u + 255u) / 256u, 256, 0, stream>>>(B);
         stage_end(ctx, stream);
-        ++launches;
     }
-    // Pass 3: patch set-up + tile counts, scan, binning, sort, raster.
-    const uint32_t slots = slotAcc;
-    CK(ctx->ranges.reserve((size_t)tileAcc * sizeof(uint2)));
-    CK(cudaMemsetAsync(ctx->ranges.ptr, 0, (size_t)tileAcc * sizeof(uint2), stream));
-    uint32_t pairs = 0;
-    if (slots)
+    if (L.slots)
     {
-        CK(ctx->tris.reserve((size_t)slots * sizeof(TriRecord)));
-        CK(ctx->tileCounts.reserve((size_t)slots * 4));
-        CK(ctx->offsets.reserve((size_t)slots * 4 + 4));
         stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
-        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, (TriRecord*)ctx->tris.ptr,
-                                                                   (uint32_t*)ctx->tileCounts.ptr);
+        patch_setup_kernel<<<(L.instances + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
         stage_end(ctx, stream);
-        ++launches;
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
-        // Exclusive scan of tile counts -> pair offsets; slot `slots` holds
-        // the total.
-        size_t tempBytes = 0;
-        uint32_t* counts = (uint32_t*)ctx->tileCounts.ptr;
-        uint32_t* offs = (uint32_t*)ctx->offsets.ptr;
-        CK(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
-        CK(ctx->scanTemp.reserve(tempBytes));
-        CK(cudaMemsetAsync(offs, 0, 4, stream));
-        CK(cub::DeviceScan::InclusiveSum(ctx->scanTemp.ptr, tempBytes, counts, offs + 1, slots,
+        size_t tempBytes = S.scanTempBytes;
+        CK(cudaMemsetAsync(S.offsets, 0, 4, stream));
+        CK(cub::DeviceScan::InclusiveSum(S.scanTemp, tempBytes, S.counts, S.offsets + 1, L.slots,
                                          stream));
         stage_end(ctx, stream);
-        CK(cudaMemcpyAsync(ctx->hPairs, offs + slots, 4, cudaMemcpyDeviceToHost, stream));
+    }
+    return RIVE_CUDA_OK;
+}
+
+// Enqueues binning, sort, ranges and raster over `entries` bin slots. With
+// `padded`, entries is a fixed capacity: the tail past the device's total is
+// filled with the sentinel key and overflow is flagged on the device.
+int enqueue_back(rive_cuda_context* ctx,
+                 const BatchLayout& L,
+                 const BatchTables& B,
+                 const Scratch& S,
+                 uint32_t entries,
+                 bool padded,
+                 cudaStream_t stream)
+{
+    const uint32_t* sortedSlots = nullptr;
+    if (entries && L.slots)
+    {
+        stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
+        if (padded)
+            bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots, entries,
+                                                                      L.tiles, S.keys);
+        bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+            L.slots, B.sceneTiles, S.tris, S.counts, S.offsets, entries, S.error, S.keys, S.vals);
+        stage_end(ctx, stream);
+        cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
+        cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
+        size_t tempBytes = S.sortTempBytes;
+        stage_begin(ctx, RIVE_CUDA_STAGE_SORT, stream);
+        CK(cub::DeviceRadixSort::SortPairs(S.sortTemp, tempBytes, k, v, (int)entries, 0,
+                                           L.endBit(), stream));
+        tile_ranges_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(entries, L.tiles, k.Current(),
+                                                                    S.ranges);
+        stage_end(ctx, stream);
+        sortedSlots = v.Current();
+    }
+    stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
+    raster_tile_kernel<<<L.tiles, 256, 0, stream>>>(B, S.tris, sortedSlots, S.ranges);
+    stage_end(ctx, stream);
+    CK(cudaGetLastError());
+    return RIVE_CUDA_OK;
+}
+
+size_t scan_temp_bytes(uint32_t slots)
+{
+    size_t b = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                  std::max(slots, 1u));
+    return b;
+}
+
+size_t sort_temp_bytes(uint32_t entries, int endBit)
+{
+    size_t b = 0;
+    cub::DoubleBuffer<uint32_t> k(nullptr, nullptr), v(nullptr, nullptr);
+    cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, (int)std::max(entries, 1u), 0, endBit);
+    return b;
+}
+
+// Runs a batch of independent logical flushes (distinct targets) as one
+// sequence of launches: every stage covers the work of all flushes at once.
+// The bin-entry total is read back after the scan, so bins are sized exactly.
+int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStream_t stream)
+{
+    if (n == 0)
+        return RIVE_CUDA_OK;
+    BatchLayout L;
+    int rc = plan_batch(ctx, in, n, L);
+    if (rc)
+        return rc;
+    // The previous batch's tables may still be in flight from the staging.
+    if (ctx->tablesCopied)
+        CK(cudaEventSynchronize(ctx->tablesCopied));
+    CK(ctx->tess.reserve(L.tessBytes()));
+    CK(ctx->grad.reserve(L.gradBytes()));
+    CK(ctx->hTables.reserve(L.tableBytes));
+    CK(ctx->dTables.reserve(L.tableBytes));
+    CK(ctx->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
+    CK(ctx->tris.reserve((size_t)std::max(L.slots, 1u) * sizeof(TriRecord)));
+    CK(ctx->tileCounts.reserve((size_t)std::max(L.slots, 1u) * 4));
+    CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
+    const size_t scanBytes = scan_temp_bytes(L.slots);
+    CK(ctx->scanTemp.reserve(scanBytes));
+    ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
+    ctx->lastGradBytes = (size_t)kGradTextureWidth * std::max(in[0].d->grad_data_height, 1u) * 4;
+
+    Scratch S;
+    S.tables = (uint8_t*)ctx->dTables.ptr;
+    S.tess = (uint4*)ctx->tess.ptr;
+    S.grad = (uchar4*)ctx->grad.ptr;
+    S.tris = (TriRecord*)ctx->tris.ptr;
+    S.counts = (uint32_t*)ctx->tileCounts.ptr;
+    S.offsets = (uint32_t*)ctx->offsets.ptr;
+    S.scanTemp = ctx->scanTemp.ptr;
+    S.scanTempBytes = scanBytes;
+    S.ranges = (uint2*)ctx->ranges.ptr;
+    S.error = ctx->dError;
+    BatchTables B = write_tables(ctx, in, L, S, (uint8_t*)ctx->hTables.ptr);
+    CK(cudaMemcpyAsync(S.tables, ctx->hTables.ptr, L.tableBytes, cudaMemcpyHostToDevice, stream));
+    if (!ctx->tablesCopied)
+        CK(cudaEventCreateWithFlags(&ctx->tablesCopied, cudaEventDisableTiming));
+    CK(cudaEventRecord(ctx->tablesCopied, stream));
+
+    rc = enqueue_front(ctx, L, B, S, stream);
+    if (rc)
+        return rc;
+    uint32_t pairs = 0;
+    if (L.slots)
+    {
+        CK(cudaMemcpyAsync(ctx->hPairs, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         pairs = *ctx->hPairs;
     }
-    const uint32_t* sortedSlots = nullptr;
     if (pairs)
     {
         CK(ctx->keys.reserve((size_t)pairs * 4));
         CK(ctx->vals.reserve((size_t)pairs * 4));
         CK(ctx->keysAlt.reserve((size_t)pairs * 4));
         CK(ctx->valsAlt.reserve((size_t)pairs * 4));
-        stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
-        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
-            slots, B.sceneTiles, (const TriRecord*)ctx->tris.ptr,
-            (const uint32_t*)ctx->tileCounts.ptr, (const uint32_t*)ctx->offsets.ptr,
-            (uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->vals.ptr);
-        stage_end(ctx, stream);
-        ++launches;
-        int endBit = 1;
-        while ((1ull << endBit) < tileAcc)
-            ++endBit;
-        cub::DoubleBuffer<uint32_t> k((uint32_t*)ctx->keys.ptr, (uint32_t*)ctx->keysAlt.ptr);
-        cub::DoubleBuffer<uint32_t> v((uint32_t*)ctx->vals.ptr, (uint32_t*)ctx->valsAlt.ptr);
-        size_t tempBytes = 0;
-        CK(cub::DeviceRadixSort::SortPairs(nullptr, tempBytes, k, v, (int)pairs, 0, endBit, stream));
-        CK(ctx->sortTemp.reserve(tempBytes));
-        stage_begin(ctx, RIVE_CUDA_STAGE_SORT, stream);
-        CK(cub::DeviceRadixSort::SortPairs(ctx->sortTemp.ptr, tempBytes, k, v, (int)pairs, 0,
-                                           endBit, stream));
-        tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(),
-                                                                  (uint2*)ctx->ranges.ptr);
-        stage_end(ctx, stream);
-        ++launches;
-        sortedSlots = v.Current();
+        S.sortTempBytes = sort_temp_bytes(pairs, L.endBit());
+        CK(ctx->sortTemp.reserve(S.sortTempBytes));
+        S.keys = (uint32_t*)ctx->keys.ptr;
+        S.vals = (uint32_t*)ctx->vals.ptr;
+        S.keysAlt = (uint32_t*)ctx->keysAlt.ptr;
+        S.valsAlt = (uint32_t*)ctx->valsAlt.ptr;
+        S.sortTemp = ctx->sortTemp.ptr;
     }
-    stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
-    raster_tile_kernel<<<tileAcc, 256, 0, stream>>>(B, (const TriRecord*)ctx->tris.ptr, sortedSlots,
-                                                    (const uint2*)ctx->ranges.ptr);
-    stage_end(ctx, stream);
-    ++launches;
-    CK(cudaGetLastError());
-    ctx->stats.tess_vertices = (uint64_t)tessRows * kTessTextureWidth;
-    ctx->stats.patches = instAcc;
-    ctx->stats.triangles = slots;
+    rc = enqueue_back(ctx, L, B, S, pairs, false, stream);
+    if (rc)
+        return rc;
+    ctx->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
+    ctx->stats.patches = L.instances;
+    ctx->stats.triangles = L.slots;
     ctx->stats.bin_entries = pairs;
-    ctx->stats.tiles = tileAcc;
-    ctx->stats.kernel_launches = launches;
+    ctx->stats.tiles = L.tiles;
+    ctx->stats.kernel_launches = 1 + (L.gradSpans ? 1 : 0) + (L.tessSpans ? 1 : 0) +
+                                 (L.slots ? 1 : 0) + (pairs ? 3 : 0) + 1;
     return RIVE_CUDA_OK;
 }
 
@@ -658,7 +767,6 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
                             &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables})
         b->release();
     ctx->hTables.release();
-    ctx->hUniforms.release();
     if (ctx->tablesCopied)
         cudaEventDestroy(ctx->tablesCopied);
     if (ctx->dError)
@@ -880,8 +988,6 @@ int rive_cuda_flush(rive_cuda_context* ctx,
         rb.ptr[k] = ctx->rings[k].device.ptr;
         rb.bytes[k] = ctx->rings[k].deviceValidBytes;
     }
-    const RecordRing& ur = ctx->rings[RIVE_CUDA_BUFFER_FLUSH_UNIFORM];
-    rb.hostUniforms = ur.host[ur.current];
     return run_flush(ctx, desc, rb, target->pixels, s);
 }
 
@@ -904,6 +1010,211 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
     }
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     return run_flush(ctx, desc, rb, (uint32_t*)target_pixels_device, s);
+}
+
+namespace
+{
+void graph_free(rive_cuda_graph* g)
+{
+    if (g->exec)
+        cudaGraphExecDestroy(g->exec);
+    if (g->graph)
+        cudaGraphDestroy(g->graph);
+    for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->offsets,
+                            &g->keys, &g->vals, &g->keysAlt, &g->valsAlt, &g->scanTemp,
+                            &g->sortTemp, &g->ranges, &g->error})
+        b->release();
+    if (g->hError)
+        cudaFreeHost(g->hError);
+    if (g->stream)
+        cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+int graph_build(rive_cuda_context* ctx,
+                rive_cuda_graph* g,
+                const FlushInput* in,
+                uint32_t n,
+                uint32_t capacity)
+{
+    BatchLayout L;
+    int rc = plan_batch(ctx, in, n, L);
+    if (rc)
+        return rc;
+    CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    CK(cudaMallocHost(&g->hError, 4));
+    CK(g->tables.reserve(L.tableBytes));
+    CK(g->tess.reserve(L.tessBytes()));
+    CK(g->grad.reserve(L.gradBytes()));
+    CK(g->tris.reserve((size_t)std::max(L.slots, 1u) * sizeof(TriRecord)));
+    CK(g->counts.reserve((size_t)std::max(L.slots, 1u) * 4));
+    CK(g->offsets.reserve((size_t)L.slots * 4 + 4));
+    CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
+    CK(g->error.reserve(4));
+    const size_t scanBytes = scan_temp_bytes(L.slots);
+    CK(g->scanTemp.reserve(scanBytes));
+    CK(cudaMemset(g->error.ptr, 0, 4));
+
+    Scratch S;
+    S.tables = (uint8_t*)g->tables.ptr;
+    S.tess = (uint4*)g->tess.ptr;
+    S.grad = (uchar4*)g->grad.ptr;
+    S.tris = (TriRecord*)g->tris.ptr;
+    S.counts = (uint32_t*)g->counts.ptr;
+    S.offsets = (uint32_t*)g->offsets.ptr;
+    S.scanTemp = g->scanTemp.ptr;
+    S.scanTempBytes = scanBytes;
+    S.ranges = (uint2*)g->ranges.ptr;
+    S.error = (uint32_t*)g->error.ptr;
+    std::vector<uint8_t> h(L.tableBytes);
+    BatchTables B = write_tables(ctx, in, L, S, h.data());
+    CK(cudaMemcpy(S.tables, h.data(), L.tableBytes, cudaMemcpyHostToDevice));
+
+    const bool profiling = ctx->profiling;
+    ctx->profiling = false; // stage events are not recorded inside a graph
+    if (capacity == 0 && L.slots)
+    {
+        // Size the bins from one run of the front half: the exact total plus
+        // an eighth of headroom for records that change between launches.
+        rc = enqueue_front(ctx, L, B, S, g->stream);
+        if (rc)
+        {
+            ctx->profiling = profiling;
+            return rc;
+        }
+        CK(cudaMemcpyAsync(g->hError, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost, g->stream));
+        CK(cudaStreamSynchronize(g->stream));
+        g->measured = *g->hError;
+        capacity = g->measured + g->measured / 8 + 4096;
+    }
+    if (!L.slots)
+        capacity = 0;
+    g->capacity = capacity;
+    if (capacity)
+    {
+        for (DeviceBuffer* b : {&g->keys, &g->vals, &g->keysAlt, &g->valsAlt})
+            CK(b->reserve((size_t)capacity * 4));
+        S.keys = (uint32_t*)g->keys.ptr;
+        S.vals = (uint32_t*)g->vals.ptr;
+        S.keysAlt = (uint32_t*)g->keysAlt.ptr;
+        S.valsAlt = (uint32_t*)g->valsAlt.ptr;
+        S.sortTempBytes = sort_temp_bytes(capacity, L.endBit());
+        CK(g->sortTemp.reserve(S.sortTempBytes));
+        S.sortTemp = g->sortTemp.ptr;
+    }
+    cudaError_t e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess)
+    {
+        rc = enqueue_front(ctx, L, B, S, g->stream);
+        if (!rc)
+            rc = enqueue_back(ctx, L, B, S, capacity, true, g->stream);
+        e = cudaStreamEndCapture(g->stream, &g->graph);
+    }
+    ctx->profiling = profiling;
+    if (rc)
+        return rc;
+    CK(e);
+    CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
+    g->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
+    g->stats.patches = L.instances;
+    g->stats.triangles = L.slots;
+    g->stats.bin_entries = g->measured;
+    g->stats.tiles = L.tiles;
+    g->stats.kernel_launches = 1 + (L.gradSpans ? 1 : 0) + (L.tessSpans ? 1 : 0) +
+                               (L.slots ? 2 : 0) + (capacity ? 4 : 0) + 1;
+    return RIVE_CUDA_OK;
+}
+} // namespace
+
+int rive_cuda_graph_create(rive_cuda_context* ctx,
+                           const rive_cuda_batch_flush* flushes,
+                           uint32_t count,
+                           uint32_t bin_capacity,
+                           rive_cuda_graph** out)
+{
+    if (!ctx || !out || !count || !flushes)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "NULL argument to graph_create");
+    *out = nullptr;
+    std::vector<FlushInput> in(count);
+    for (uint32_t i = 0; i < count; ++i)
+    {
+        const rive_cuda_batch_flush& f = flushes[i];
+        if (!f.desc || !f.target_pixels_device)
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u: NULL desc or target",
+                             i);
+        const void* p[7] = {f.buffers.flush_uniforms, f.buffers.paths,    f.buffers.paints,
+                            f.buffers.paint_aux,      f.buffers.contours, f.buffers.grad_spans,
+                            f.buffers.tess_spans};
+        in[i].d = f.desc;
+        for (int k = 0; k < 7; ++k)
+        {
+            in[i].rb.ptr[k] = p[k];
+            in[i].rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0;
+        }
+        in[i].fb = (uint32_t*)f.target_pixels_device;
+    }
+    CK(cudaSetDevice(ctx->device));
+    auto* g = new (std::nothrow) rive_cuda_graph();
+    if (!g)
+        return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+    g->ctx = ctx;
+    int rc = graph_build(ctx, g, in.data(), count, bin_capacity);
+    if (rc)
+    {
+        graph_free(g);
+        return rc;
+    }
+    *out = g;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_graph_launch(rive_cuda_graph* g, void* cuda_stream)
+{
+    if (!g)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    rive_cuda_context* ctx = g->ctx;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaGraphLaunch(g->exec, cuda_stream ? (cudaStream_t)cuda_stream : g->stream));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_graph_check(rive_cuda_graph* g, void* cuda_stream)
+{
+    if (!g)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    rive_cuda_context* ctx = g->ctx;
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : g->stream;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(g->hError, g->error.ptr, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint32_t err = *g->hError;
+    if (err)
+    {
+        CK(cudaMemsetAsync(g->error.ptr, 0, 4, s));
+        CK(cudaStreamSynchronize(s));
+        return set_error(ctx, RIVE_CUDA_ERR_DEVICE_STATUS,
+                         "graph device status 0x%x (32: more bin entries than the capacity %u)",
+                         err, g->capacity);
+    }
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_graph_stats(const rive_cuda_graph* g, rive_cuda_flush_stats* out)
+{
+    if (!g || !out)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *out = g->stats;
+    return RIVE_CUDA_OK;
+}
+
+void rive_cuda_graph_destroy(rive_cuda_graph* g)
+{
+    if (!g)
+        return;
+    cudaSetDevice(g->ctx->device);
+    if (g->stream)
+        cudaStreamSynchronize(g->stream);
+    graph_free(g);
 }
 
 int rive_cuda_flush_batch(rive_cuda_context* ctx,

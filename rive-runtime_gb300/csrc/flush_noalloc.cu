@@ -23,14 +23,20 @@ namespace rivecuda
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
                                    const uint32_t* offsets,
+                                   uint32_t capacity,
+                                   uint32_t* error,
                                    uint32_t* keys,
                                    uint32_t* vals);
-__global__ void tile_ranges_kernel(uint32_t pairCount, const uint32_t* keys, uint2* ranges);
+__global__ void tile_ranges_kernel(uint32_t pairCount,
+                                   uint32_t tileCount,
+                                   const uint32_t* keys,
+                                   uint2* ranges);
 __global__ void raster_tile_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
@@ -234,17 +240,10 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     P.fb = (uint32_t*)target_pixels_device;
     P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
 
-    // FlushUniforms fields (renderer/include/rive/renderer/gpu.hpp:1466-1537),
-    // read into a stack copy.
-    uint8_t uni[256];
-    CKN(cudaMemcpyAsync(uni, (const uint8_t*)buffers->flush_uniforms + d->flush_uniform_offset_bytes,
-                        sizeof(uni), cudaMemcpyDeviceToHost, stream));
-    CKN(cudaStreamSynchronize(stream));
-    memcpy(&P.pathIDGranularity, uni + 72, 4);
-    memcpy(&P.ditherScale, uni + 88, 4);
-    memcpy(&P.ditherBias, uni + 92, 4);
-    if (P.pathIDGranularity == 0)
-        P.pathIDGranularity = 1;
+    // FlushUniforms (renderer/include/rive/renderer/gpu.hpp:1466-1537) stay on
+    // the device; scene_uniforms_kernel copies the fields the passes use.
+    P.uniforms = (const uint8_t*)buffers->flush_uniforms + d->flush_uniform_offset_bytes;
+    P.pathIDGranularity = 1;
 
     const uint32_t tilesX = P.tilesX;
     const uint32_t tilesY = (d->render_target_height + kTileSize - 1) / kTileSize;
@@ -276,6 +275,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     segBase[segCount] = instAcc;
     uint8_t* dTab = pool + kTablesOff;
     CKN(cudaMemcpyAsync(dTab, tab, sizeof(tab), cudaMemcpyHostToDevice, stream));
+    scene_uniforms_kernel<<<1, 32, 0, stream>>>((FlushParams*)(dTab + kTabScenes), 1u);
     BatchTables B = {};
     B.scenes = (const FlushParams*)(dTab + kTabScenes);
     B.gradSpanBase = (const uint32_t*)(dTab + kTabPrefix);
@@ -334,10 +334,10 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     const uint32_t* sortedSlots = nullptr;
     if (pairs)
     {
-        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(slots, B.sceneTiles, tris,
-                                                                   counts, offs, keys, vals);
+        bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
+            slots, B.sceneTiles, tris, counts, offs, pairs, dError, keys, vals);
         int endBit = 1;
-        while ((1u << endBit) < tiles)
+        while ((1u << endBit) <= tiles)
             ++endBit;
         cub::DoubleBuffer<uint32_t> k(keys, (uint32_t*)(pool + kKeysAltOff));
         cub::DoubleBuffer<uint32_t> v(vals, (uint32_t*)(pool + kValsAltOff));
@@ -349,7 +349,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                         kSortTempBytes);
         CKN(cub::DeviceRadixSort::SortPairs(pool + kSortTempOff, tempBytes, k, v, (int)pairs, 0,
                                             endBit, stream));
-        tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, k.Current(), ranges);
+        tile_ranges_kernel<<<(pairs + 255) / 256, 256, 0, stream>>>(pairs, tiles, k.Current(),
+                                                                  ranges);
         sortedSlots = v.Current();
     }
     raster_tile_kernel<<<tiles, 256, 0, stream>>>(B, tris, sortedSlots, ranges);

@@ -623,15 +623,46 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
     }
 }
 
+// FlushUniforms fields the passes use (gpu.hpp:1466-1537: pathIDGranularity
+// at byte 72, ditherScale at 88, ditherBias at 92), read on the device so no
+// pass waits for the host. One thread per flush of the batch.
+__global__ void scene_uniforms_kernel(FlushParams* __restrict__ scenes, uint32_t sceneCount)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sceneCount)
+        return;
+    const uint8_t* u = scenes[i].uniforms;
+    const uint32_t granularity = *reinterpret_cast<const uint32_t*>(u + 72);
+    scenes[i].pathIDGranularity = granularity ? granularity : 1u;
+    scenes[i].ditherScale = *reinterpret_cast<const float*>(u + 88);
+    scenes[i].ditherBias = *reinterpret_cast<const float*>(u + 92);
+}
+
+// Fixed-capacity binning: entries [total, capacity) get the sentinel key (one
+// past the batch's last tile) so a sort over the whole capacity leaves them
+// at the end, where tile_ranges_kernel ignores them.
+__global__ void bin_fill_kernel(const uint32_t* __restrict__ pairTotal,
+                                uint32_t capacity,
+                                uint32_t sentinel,
+                                uint32_t* __restrict__ keys)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < capacity && i >= *pairTotal)
+        keys[i] = sentinel;
+}
+
 // Writes the (tile, slot) pairs of each triangle at its scanned offset. One
 // warp per 32 consecutive slots: a lane writes its own triangle's pairs when
 // its box spans few tiles; larger triangles are walked by the whole warp with
-// a ballot assigning output positions.
+// a ballot assigning output positions. Pairs at or past `capacity` are
+// dropped and flagged (ERR_BIN_OVERFLOW).
 __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                                                           const uint2* __restrict__ sceneTiles,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ tileCounts,
                                                           const uint32_t* __restrict__ offsets,
+                                                          uint32_t capacity,
+                                                          uint32_t* __restrict__ error,
                                                           uint32_t* __restrict__ keys,
                                                           uint32_t* __restrict__ vals)
 {
@@ -660,8 +691,15 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                 for (int tx = tx0; tx < tx0 + ntx; ++tx)
                     if (tile_overlaps(e, bb, tx, ty))
                     {
-                        keys[o] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
-                        vals[o] = mySlot;
+                        if (o < capacity)
+                        {
+                            keys[o] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
+                            vals[o] = mySlot;
+                        }
+                        else
+                        {
+                            atomicOr(error, ERR_BIN_OVERFLOW);
+                        }
                         ++o;
                     }
         }
@@ -700,8 +738,15 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
             if (hit)
             {
                 const uint32_t pos = o + __popc(mask & ((1u << lane) - 1u));
-                keys[pos] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
-                vals[pos] = slot;
+                if (pos < capacity)
+                {
+                    keys[pos] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
+                    vals[pos] = slot;
+                }
+                else
+                {
+                    atomicOr(error, ERR_BIN_OVERFLOW);
+                }
             }
             o += __popc(mask);
         }
@@ -709,6 +754,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
 }
 
 __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
+                                                          uint32_t tileCount,
                                                           const uint32_t* __restrict__ keys,
                                                           uint2* __restrict__ ranges)
 {
@@ -716,6 +762,8 @@ __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
     if (i >= pairCount)
         return;
     uint32_t k = keys[i];
+    if (k >= tileCount) // capacity padding
+        return;
     if (i == 0 || keys[i - 1] != k)
         ranges[k].x = i;
     if (i == pairCount - 1 || keys[i + 1] != k)
@@ -1145,7 +1193,7 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
                                T.cov0.z);
             L.q3 = make_float4(T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x, T.cov1.y,
                                T.cov1.z);
-            L.q4 = make_uint4(__float_as_uint(T.cov1.w), T.meta.x, T.meta.w, 0u);
+            L.q4 = make_uint4(__float_as_uint(T.cov1.w), T.meta.x, T.meta.w & 0xffffu, 0u);
             sTris[threadIdx.x] = L;
             const int4 bb = unpack_bbox(T.meta);
             const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;

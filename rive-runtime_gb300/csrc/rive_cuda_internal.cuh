@@ -128,6 +128,9 @@ struct FlushParams
     uint32_t* error;
     uint32_t* fb;   // render target, RGBA8, width x height
     uint32_t tilesX;
+    // This flush's FlushUniforms record (device); scene_uniforms_kernel copies
+    // pathIDGranularity and the dither terms from it before any other pass.
+    const uint8_t* uniforms;
 };
 
 // A run of patch instances of one flush drawn with one set of shader

@@ -98,6 +98,12 @@ def load():
         "rive_cuda_flush_device": (i32, [vp, ctypes.POINTER(FlushDesc),
                                          ctypes.POINTER(DeviceBuffers), vp, vp]),
         "rive_cuda_flush_batch": (i32, [vp, ctypes.POINTER(BatchFlush), u32, vp]),
+        "rive_cuda_graph_create": (i32, [vp, ctypes.POINTER(BatchFlush), u32, u32,
+                                         ctypes.POINTER(vp)]),
+        "rive_cuda_graph_launch": (i32, [vp, vp]),
+        "rive_cuda_graph_check": (i32, [vp, vp]),
+        "rive_cuda_graph_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
+        "rive_cuda_graph_destroy": (None, [vp]),
         "rive_cuda_flush_device_noalloc": (i32, [ctypes.POINTER(FlushDesc),
                                                  ctypes.POINTER(DeviceBuffers), vp, vp,
                                                  ctypes.c_char_p, sz]),
@@ -142,6 +148,35 @@ def flush_device_noalloc(flush, bufs: DeviceBuffers, target_ptr: int, stream=Non
     del keep
     if rc != OK:
         raise RiveCudaError(f"flush_device_noalloc: status {rc}: {err.value.decode()}")
+
+
+class Graph:
+    """A batch captured as a CUDA graph (rive_cuda_graph_*)."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.h = ctx, handle
+
+    def launch(self, stream=None):
+        self.ctx.check(self.ctx.lib.rive_cuda_graph_launch(self.h, stream), "graph_launch")
+
+    def check(self, stream=None):
+        self.ctx.check(self.ctx.lib.rive_cuda_graph_check(self.h, stream), "graph_check")
+
+    def stats(self):
+        s = FlushStats()
+        self.ctx.check(self.ctx.lib.rive_cuda_graph_stats(self.h, ctypes.byref(s)), "graph_stats")
+        return {k: getattr(s, k) for k, _ in FlushStats._fields_}
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.rive_cuda_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Context:
@@ -217,10 +252,9 @@ class Context:
                    "flush_device")
         del keep
 
-    def flush_batch(self, items, stream=None):
-        """rive_cuda_flush_batch over [(capture.Flush, DeviceBuffers, target_ptr), ...]:
-        independent flushes (distinct targets) in one sequence of launches."""
-        arr = (BatchFlush * len(items))()
+    @staticmethod
+    def _batch_array(items):
+        arr = (BatchFlush * max(len(items), 1))()
         keep = []
         for i, (flush, bufs, target_ptr) in enumerate(items):
             d, k = make_desc(flush)
@@ -228,8 +262,23 @@ class Context:
             arr[i].desc = ctypes.cast(ctypes.pointer(d), ctypes.c_void_p)
             arr[i].buffers = bufs
             arr[i].target_pixels_device = target_ptr
+        return arr, keep
+
+    def flush_batch(self, items, stream=None):
+        """rive_cuda_flush_batch over [(capture.Flush, DeviceBuffers, target_ptr), ...]:
+        independent flushes (distinct targets) in one sequence of launches."""
+        arr, keep = self._batch_array(items)
         self.check(self.lib.rive_cuda_flush_batch(self.h, arr, len(items), stream), "flush_batch")
         del keep
+
+    def graph(self, items, bin_capacity=0):
+        """rive_cuda_graph_create: the batch captured as one CUDA graph."""
+        arr, keep = self._batch_array(items)
+        g = ctypes.c_void_p()
+        self.check(self.lib.rive_cuda_graph_create(self.h, arr, len(items), bin_capacity,
+                                                   ctypes.byref(g)), "graph_create")
+        del keep
+        return Graph(self, g)
 
     def sync(self, stream=None):
         self.check(self.lib.rive_cuda_sync(self.h, stream), "sync")

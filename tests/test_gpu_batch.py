@@ -94,3 +94,52 @@ def test_batch_refuses_a_shared_target(ctx):
     with pytest.raises(rive_cuda.RiveCudaError, match="share a render target"):
         ctx.flush_batch([(a.flushes[0], ba, t.data_ptr()), (a.flushes[0], ba, t.data_ptr())])
     ctx.flush_batch([])  # an empty batch is a no-op
+
+
+@pytest.mark.gpu
+def test_graph_replays_match_single_flushes(ctx):
+    """A batch captured as a CUDA graph: every launch gives every target the
+    one-by-one image, and the device status stays clean."""
+    import torch
+    caps = [load_golden(n)[0] for n in golden_names()]
+    pairs = [_device_buffers(c) for c in caps]
+    bufs = [p[0] for p in pairs]
+    stream = torch.cuda.current_stream().cuda_stream
+    want = _one_by_one(ctx, caps, bufs, stream)
+    targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda") for c in caps]
+    g = ctx.graph([(c.flushes[0], b, t.data_ptr()) for c, b, t in zip(caps, bufs, targets)])
+    try:
+        for _ in range(2):
+            for t in targets:
+                t.zero_()
+            torch.cuda.synchronize()
+            g.launch()
+            g.check()
+            torch.cuda.synchronize()
+            for name, t, w in zip(golden_names(), targets, want):
+                assert np.array_equal(t.cpu().numpy(), w), name
+        assert g.stats()["bin_entries"] > 0
+    finally:
+        g.close()
+
+
+@pytest.mark.gpu
+def test_graph_reports_a_bin_capacity_overflow(ctx):
+    """Too small a capacity drops entries on the device and is reported by
+    the check (no fault, no out-of-range write); the context stays usable."""
+    import torch
+    from rive_runtime_gb300 import rive_cuda
+    a = load_golden("strokes_s3")[0]
+    ba, ka = _device_buffers(a)
+    t = torch.zeros((a.height, a.width, 4), dtype=torch.uint8, device="cuda")
+    g = ctx.graph([(a.flushes[0], ba, t.data_ptr())], bin_capacity=64)
+    try:
+        g.launch()
+        with pytest.raises(rive_cuda.RiveCudaError, match="capacity"):
+            g.check()
+        g.check()  # the status was cleared
+    finally:
+        g.close()
+    stream = torch.cuda.current_stream().cuda_stream
+    (want,) = _one_by_one(ctx, [a], [ba], stream)
+    assert want.any()
