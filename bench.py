@@ -38,6 +38,9 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "tests"))
 
 
+RASTER_DRAM_BYTES_PER_ENTRY = 696.4e6 / 9.766e6
+
+
 def _package():
     from conftest import load_package
     return load_package()
@@ -150,27 +153,50 @@ def cpu_baseline(cap, threads):
 
 
 def run_reference(args, cap, wname, rank, world):
+    """The reference's CPU implementation of the path (the oracle port: the
+    reference's pixel passes exist only as shaders) on all host cores. A step
+    is one logical flush of the frame, in turn, so a step is a bounded sample;
+    frames/s = frames' worth of flushes / time."""
     if rank != 0:
         return
+    import numpy as np
+    import oracle
     threads = os.cpu_count() or 1
-    for _ in range(max(args.warmup_cpu, 0)):
-        cpu_baseline(cap, threads)
-    times = [cpu_baseline(cap, threads) for _ in range(args.steps_cpu)]
-    fps = len(times) / sum(times)
+    nflush = len(cap.flushes)
+    fb = np.zeros((cap.height, cap.width, 4), np.uint8)
+
+    def step(i):
+        oracle.render_flush(cap, i % nflush, fb, threads=threads)
+
+    for i in range(args.warmup):
+        step(i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        step(i)
+    dt = time.perf_counter() - t0
+    fps = (args.steps / nflush) / dt
     line = {
         "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
-        "n_gpus": args.gpus, "steps": len(times), "warmup": args.warmup_cpu,
-        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": wname, "width": cap.width, "height": cap.height},
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "dtype": "f32", "data": "synthetic",
+        "config": workload_config(cap, wname),
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(times)} whole frame(s) of {wname} through the oracle "
-                                   "(CPU restatement of the three GPU passes)"},
+                         "sample": f"{args.steps} logical flushes ({args.steps / nflush:.2f} "
+                                   f"frames) of {wname} through the oracle, OpenMP on "
+                                   f"{threads} threads"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "vs_baseline": None,
     }
     print(json.dumps(line))
+
+
+def workload_config(cap, wname):
+    return {"workload": wname, "width": cap.width, "height": cap.height,
+            "flushes_per_frame": len(cap.flushes),
+            "l2": "inputs per frame far larger than L2 (no flush needed)",
+            **workload_counts(cap)}
 
 
 def run_ours(args, cap, wname, rank, world):
@@ -267,6 +293,7 @@ def run_ours(args, cap, wname, rank, world):
     dominant = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_launches = prof[dominant]
     per_launch_s = (dom_ms / max(dom_launches, 1)) / 1e3
+    traffic = None
     if dominant == "raster":
         # Per launch: bin entries x (4 B slot index + 96 B triangle record)
         # + 4 B per pixel written (+ 4 B read when the flush preserves the
@@ -274,6 +301,10 @@ def run_ours(args, cap, wname, rank, world):
         preserve = sum(1 for f in cap.flushes if f.desc["color_load_action"] != 0)
         frame_bytes_raster = frame_entries * 100 + 4 * W * H * (len(cap.flushes) + preserve)
         alg_bytes = frame_bytes_raster / len(cap.flushes)
+        # DRAM bytes (read + write) per launch, scaled by bin entries from one
+        # ncu capture of this kernel on the 1024x1024 full-feature frame
+        # (696.4 MB for 9.77 M entries); the full frame is too large to capture.
+        traffic = RASTER_DRAM_BYTES_PER_ENTRY * frame_entries / len(cap.flushes)
     elif dominant == "tessellate":
         alg_bytes = 64 * counts["spans"] / counts["flushes"] + 16 * counts["tess_vertices"] / counts["flushes"]
     else:
@@ -284,14 +315,13 @@ def run_ours(args, cap, wname, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": wname, "width": W, "height": H, "flushes_per_frame": len(cap.flushes),
-                   "l2": "inputs per frame far larger than L2 (no flush needed)",
-                   "gpx_per_s": fps * W * H / 1e9, **counts},
+        "config": workload_config(cap, wname),
+        "gpx_per_s": fps * W * H / 1e9,
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
                 "d2h_bytes_per_step": W * H * 4},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": None},
+                     "traffic": traffic},
         "stage_ms_per_frame": {k: v[0] / args.steps for k, v in prof.items()},
         "gpu_launches": int(sum(v[1] for v in prof.values())),
         "clocks": clocks,
@@ -386,8 +416,6 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="full_feature")
     ap.add_argument("--capture", default=None)
-    ap.add_argument("--steps-cpu", type=int, default=2)
-    ap.add_argument("--warmup-cpu", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched-form measurement (0 skips it)")

@@ -149,6 +149,15 @@ def render(cap, threads=0, fb=None):
     return fb
 
 
+def render_flush(cap, fi, fb, threads=0):
+    """Runs logical flush `fi` of the capture onto `fb` (HxWx4 RGBA8)."""
+    b, _keep = make_buffers(cap)
+    d, _k = make_desc(cap.flushes[fi])
+    _check(lib().oracle_flush(ctypes.byref(d), ctypes.byref(b),
+                              fb.ctypes.data_as(ctypes.c_void_p), int(threads)), "flush")
+    return fb
+
+
 def last_stats():
     t = ctypes.c_uint64()
     fr = ctypes.c_uint64()
