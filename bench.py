@@ -330,6 +330,8 @@ def run_ours(args, cap, wname, rank, world):
     del keep, target
     if args.batch_scenes > 0:
         line["batched"] = run_batched(args, dev)
+    if args.serve_sessions > 0:
+        line["serving"] = run_serving(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -338,6 +340,32 @@ def run_ours(args, cap, wname, rank, world):
                                 "sample": f"1 whole frame of {wname} through the oracle"}
     if rank == 0:
         print(json.dumps(line))
+
+
+def run_serving(args, dev):
+    """The serving loop (rive-runtime_gb300/serving.py): sessions with the
+    full-feature distributions on a smaller canvas, Poisson arrivals at 50/s,
+    each animated for a fixed number of frames at a fixed frame rate."""
+    import numpy as np
+    from rive_runtime_gb300 import rive_cuda, scene, serving
+    scs = [scene.full_feature(seed=1000 + i, width=args.serve_size, height=args.serve_size,
+                              n_paths=args.serve_paths) for i in range(args.serve_sessions)]
+    sessions = serving.poisson_sessions(scs, 50.0, frames=args.serve_frames,
+                                        fps=args.serve_fps, seed=7)
+    ctx = rive_cuda.Context(dev)
+    try:
+        server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
+                                     planner_threads=min(16, os.cpu_count() or 1))
+        st = server.run(sessions, timeout_s=600.0)
+    finally:
+        ctx.close()
+    offered = args.serve_sessions * args.serve_fps
+    return {"workload": f"serving_{args.serve_sessions}x{args.serve_frames}",
+            "scene": f"full_feature distributions, {args.serve_size}x{args.serve_size}, "
+                     f"{args.serve_paths} paths",
+            "arrivals_per_s": 50.0, "fps_per_session": args.serve_fps,
+            "offered_frames_per_s_at_full_concurrency": offered,
+            "hbm_budget_gb": 120, **st}
 
 
 def run_batched(args, dev):
@@ -420,6 +448,12 @@ def main():
     ap.add_argument("--batch-scenes", type=int, default=256,
                     help="scenes of the batched-form measurement (0 skips it)")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--serve-sessions", type=int, default=64,
+                    help="sessions of the serving-loop measurement (0 skips it)")
+    ap.add_argument("--serve-size", type=int, default=512)
+    ap.add_argument("--serve-paths", type=int, default=300)
+    ap.add_argument("--serve-frames", type=int, default=60)
+    ap.add_argument("--serve-fps", type=float, default=8.0)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -1112,11 +1112,11 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
 // their own triangles in order and keep every pixel's planes in registers.
 struct __align__(16) TileTri
 {
-    float4 q0; // C0, A0, B0, C1
-    float4 q1; // A1, B1, C2, A2
-    float4 q2; // B2, covx at the tile origin, d covx/dx, d covx/dy
-    float4 q3; // covy at the tile origin, d covy/dx, d covy/dy, paint.x bits
-    uint4 q4;  // paint.y, pathAndFeatures, coverage key, unused
+    float4 v0; // coverage key (bits), C0, A0, B0
+    float4 v1; // C1, A1, B1, C2
+    float4 v2; // A2, B2, covx at the tile origin, d covx/dx
+    float4 v3; // d covx/dy, covy at the tile origin, d covy/dx, d covy/dy
+    uint4 v4;  // paint.x, paint.y, pathAndFeatures, unused
 };
 static_assert(sizeof(TileTri) == 80, "TileTri layout");
 
@@ -1187,13 +1187,13 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
                                 tile_edge_origin(e[2], tx, ty)};
             const float dx0 = (float)ox + .5f - T.e0.x, dy0 = (float)oy + .5f - T.e0.y;
             TileTri L;
-            L.q0 = make_float4(c[0], e[0].z, e[0].w, c[1]);
-            L.q1 = make_float4(e[1].z, e[1].w, c[2], e[2].z);
-            L.q2 = make_float4(e[2].w, T.cov0.x + T.cov0.y * dx0 + T.cov0.z * dy0, T.cov0.y,
-                               T.cov0.z);
-            L.q3 = make_float4(T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x, T.cov1.y,
-                               T.cov1.z);
-            L.q4 = make_uint4(__float_as_uint(T.cov1.w), T.meta.x, T.meta.w & 0xffffu, 0u);
+            L.v0 = make_float4(__uint_as_float(T.meta.w & 0xffffu), c[0], e[0].z, e[0].w);
+            L.v1 = make_float4(c[1], e[1].z, e[1].w, c[2]);
+            L.v2 = make_float4(e[2].z, e[2].w, T.cov0.x + T.cov0.y * dx0 + T.cov0.z * dy0,
+                               T.cov0.y);
+            L.v3 = make_float4(T.cov0.z, T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x,
+                               T.cov1.y);
+            L.v4 = make_uint4(__float_as_uint(T.cov1.z), __float_as_uint(T.cov1.w), T.meta.x, 0u);
             sTris[threadIdx.x] = L;
             const int4 bb = unpack_bbox(T.meta);
             const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;
@@ -1219,7 +1219,8 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
                 const uint32_t i = g + (uint32_t)(__ffs(bits) - 1);
                 bits &= bits - 1;
                 const TileTri& T = sTris[i];
-                const uint32_t vPathID = T.q4.z;
+                const float4 v0 = T.v0;
+                const uint32_t vPathID = __float_as_uint(v0.x);
                 // A path's triangles are contiguous in primitive order, so when
                 // the warp's stream moves to another path every pixel still
                 // holding the previous path's coverage has seen all of it:
@@ -1233,43 +1234,43 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
                     }
                     streamPath = vPathID;
                 }
-                const float4 q0 = T.q0, q1 = T.q1;
-                const float b2 = T.q2.x;
-                const float E0 = local_edge(q0.x, q0.y, q0.z, lx, ly);
-                const float E1 = local_edge(q0.w, q1.x, q1.y, lx, ly);
-                const float E2 = local_edge(q1.z, q1.w, b2, lx, ly);
+                const float4 v1 = T.v1, v2 = T.v2;
+                const float E0 = local_edge(v0.y, v0.z, v0.w, lx, ly);
+                const float E1 = local_edge(v1.x, v1.y, v1.z, lx, ly);
+                const float E2 = local_edge(v1.w, v2.x, v2.y, lx, ly);
                 const float emin = fminf(fminf(E0, E1), E2);
                 if (!(emin > 0.f) &&
-                    !(emin == 0.f && local_inside(q0.y, q0.z, E0) && local_inside(q1.x, q1.y, E1) &&
-                      local_inside(q1.w, b2, E2)))
+                    !(emin == 0.f && local_inside(v0.z, v0.w, E0) && local_inside(v1.y, v1.z, E1) &&
+                      local_inside(v2.x, v2.y, E2)))
                     continue;
                 if (!inBounds)
                     continue;
-                const float4 q2 = T.q2, q3 = T.q3;
-                const uint2 q4 = make_uint2(T.q4.x, T.q4.y);
-                const float covx = __fmaf_rn(q2.z, lx, __fmaf_rn(q2.w, ly, q2.y));
-                const float covy = __fmaf_rn(q3.y, lx, __fmaf_rn(q3.z, ly, q3.x));
-                const uint32_t paintX = __float_as_uint(q3.w);
+                const float4 v3 = T.v3;
+                const float covx = __fmaf_rn(v2.w, lx, __fmaf_rn(v3.x, ly, v2.z));
+                const float covy = __fmaf_rn(v3.z, lx, __fmaf_rn(v3.w, ly, v3.y));
                 float count;
                 if (s.key != vPathID)
                 {
                     if (s.pendMeta)
                         resolve_path(P, s, fx, fy, dither);
-                    s.pendMeta = q4.y;
-                    s.pendPaintX = paintX;
-                    s.pendPaintY = q4.x;
-                    s.pendFrags = 0;
+                    const uint4 v4 = T.v4;
+                    s.pendMeta = v4.z;
+                    s.pendPaintX = v4.x;
+                    s.pendPaintY = v4.y;
+                    s.pendFrags = 1;
                     s.key = vPathID;
                     count = 0.f;
                 }
                 else
                 {
                     count = s.count;
+                    s.pendFrags = 2;
                     if (!s.pendMeta) // the key's path came back after a resolve
                     {
-                        s.pendMeta = q4.y;
-                        s.pendPaintX = paintX;
-                        s.pendPaintY = q4.x;
+                        const uint4 v4 = T.v4;
+                        s.pendMeta = v4.z;
+                        s.pendPaintX = v4.x;
+                        s.pendPaintY = v4.y;
                     }
                 }
                 if (covy >= 0.f)
@@ -1277,7 +1278,6 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
                 else
                     count = count + covx; // fill
                 s.count = h2f(f2h(count)); // the plane stores fp16
-                s.pendFrags = min(s.pendFrags + 1u, 2u);
             }
         }
         __syncthreads();
