@@ -68,6 +68,15 @@ def build_workload(args):
     return planner.plan(sc.to_bytes()), args.workload
 
 
+def max_over_ranks(value, device):
+    """The largest `value` over all ranks (host-side timing only; the path has
+    no data exchange)."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_counts(cap):
     spans = paths = contours = grad_spans = grad_rows = verts = 0
     for f in cap.flushes:
@@ -261,9 +270,7 @@ def run_ours(args, cap, wname, rank, world):
     ctx.sync(stream.cuda_stream)
     stats = ctx.stats()
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, "cuda")
     fps = world * args.steps / (ms / 1e3)
 
     # End to end through the C ABI with host buffers.
@@ -328,9 +335,10 @@ def run_ours(args, cap, wname, rank, world):
     }
     ctx.close()
     del keep, target
-    if args.batch_scenes > 0:
+    # The batched and serving measurements are single-GPU (rank 0 of N=1).
+    if args.batch_scenes > 0 and world == 1:
         line["batched"] = run_batched(args, dev)
-    if args.serve_sessions > 0:
+    if args.serve_sessions > 0 and world == 1:
         line["serving"] = run_serving(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
