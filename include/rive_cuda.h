@@ -52,7 +52,7 @@ enum
     RIVE_CUDA_BUFFER_CONTOUR = 4,       /* gpu::ContourData, 16 B each         */
     RIVE_CUDA_BUFFER_GRAD_SPAN = 5,     /* gpu::GradientSpan, 16 B each        */
     RIVE_CUDA_BUFFER_TESS_SPAN = 6,     /* gpu::TessVertexSpan, 64 B each      */
-    RIVE_CUDA_BUFFER_TRIANGLE = 7,      /* gpu::TriangleVertex (unsupported)   */
+    RIVE_CUDA_BUFFER_TRIANGLE = 7,      /* gpu::TriangleVertex, 12 B each      */
     RIVE_CUDA_BUFFER_IMAGE_DRAW = 8,    /* gpu::ImageDrawInstance (unsupported)*/
     RIVE_CUDA_BUFFER_KIND_COUNT = 9,
 };
@@ -65,10 +65,12 @@ enum
     RIVE_CUDA_LOAD_DONT_CARE = 2,
 };
 
-/* gpu::DrawType values this backend executes (gpu.hpp:657). */
+/* gpu::DrawType values this backend executes (gpu.hpp:657-668). */
 enum
 {
     RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES = 0,
+    RIVE_CUDA_DRAW_OUTER_CURVE_PATCHES = 2,   /* interior triangulation: the curves */
+    RIVE_CUDA_DRAW_INTERIOR_TRIANGULATION = 3, /* ... and the interior triangles  */
 };
 
 /*
@@ -216,6 +218,7 @@ typedef struct rive_cuda_device_buffers
     const void* contours;
     const void* grad_spans;
     const void* tess_spans;
+    const void* triangle_vertices; /* gpu::TriangleVertex, 12 B each; may be NULL */
 } rive_cuda_device_buffers;
 
 int rive_cuda_flush_device(rive_cuda_context* ctx,

@@ -65,8 +65,15 @@ typedef struct rive_scene_header
     uint32_t point_count;
     uint32_t stop_count;
     uint32_t dither_mode; /* gpu::DitherMode: 0 none, 1 IGN */
-    uint32_t reserved;
+    uint32_t flags;       /* RIVE_SCENE_FLAG_* */
 } rive_scene_header;
+
+/* Let the front end triangulate the interiors of large fills: the frame is
+ * recorded with TriangulationThresholds::frameBudgetMs = infinity (every
+ * eligible path, independent of timing; triangulation_controller.cpp), so it
+ * draws outer-curve patches plus interior triangles for them. Without it,
+ * frameBudgetMs = 0 and every fill is a midpoint fan. */
+#define RIVE_SCENE_FLAG_TRIANGULATE 1u
 
 typedef struct rive_scene_path
 {

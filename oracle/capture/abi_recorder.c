@@ -14,7 +14,7 @@
 #include <string.h>
 
 #define KINDS RIVE_CUDA_BUFFER_KIND_COUNT
-#define CAPTURED_KINDS 7 /* flush uniforms .. tess spans */
+#define CAPTURED_KINDS 7 /* flush uniforms .. tess spans (+ triangle vertices) */
 #define MAX_FLUSHES 256
 
 struct rive_cuda_context
@@ -183,10 +183,12 @@ int abi_recorder_write(const char* path)
     FILE* f = fopen(path, "wb");
     if (!f)
         return 1;
-    uint32_t head[4] = {0x31504352u /* RCP1 */, ctx->width, ctx->height, CAPTURED_KINDS};
+    /* Seven kinds, or eight when the frame has interior triangles. */
+    const uint32_t kinds = ctx->bytes[CAPTURED_KINDS] ? CAPTURED_KINDS + 1 : CAPTURED_KINDS;
+    uint32_t head[4] = {0x31504352u /* RCP1 */, ctx->width, ctx->height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const unsigned char zeros[8] = {0};
-    for (int k = 0; k < CAPTURED_KINDS; ++k)
+    for (uint32_t k = 0; k < kinds; ++k)
     {
         uint64_t n = ctx->bytes[k];
         fwrite(&n, sizeof(n), 1, f);

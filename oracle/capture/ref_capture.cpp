@@ -14,8 +14,9 @@
  * Usage: ref_capture <scene.bin> <capture.bin>
  *
  * Capture file layout (little-endian):
- *   u32 magic 'RCP1', u32 width, u32 height, u32 buffer_kinds (= 7)
- *   7 x { u64 bytes, bytes of data, zero pad to 8 }  in rive_cuda.h order
+ *   u32 magic 'RCP1', u32 width, u32 height, u32 buffer_kinds (7, or 8 when
+ *   the frame has interior triangles)
+ *   buffer_kinds x { u64 bytes, bytes of data, zero pad to 8 }  in rive_cuda.h order
  *   u32 flush_count
  *   flush_count x { rive_cuda_flush_desc (draw_batches = 0),
  *                   rive_cuda_draw_batch[draw_batch_count] }
@@ -70,8 +71,8 @@ struct FlushRecord
 class CaptureImpl : public RenderContextNULL
 {
 public:
-    // Buffers in rive_cuda.h kind order 0..6.
-    std::vector<uint8_t> buffers[7];
+    // Buffers in rive_cuda.h kind order 0..7.
+    std::vector<uint8_t> buffers[8];
     std::vector<FlushRecord> flushes;
 
     static std::unique_ptr<RenderContext> Make(CaptureImpl** out)
@@ -134,7 +135,7 @@ public:
     }
     void resizeTriangleVertexBuffer(size_t n) override
     {
-        m_nextVertexSink = &m_discard;
+        m_nextVertexSink = &buffers[7];
         RenderContextHelperImpl::resizeTriangleVertexBuffer(n);
     }
     void resizeImageDrawInstanceBuffer(size_t n) override
@@ -255,10 +256,12 @@ int main(int argc, char** argv)
     FILE* f = fopen(argv[2], "wb");
     if (!f)
         return fail("cannot open output");
-    uint32_t head[4] = {0x31504352u /*RCP1*/, hdr.width, hdr.height, 7};
+    // Seven buffer kinds, or eight when the frame has interior triangles.
+    const uint32_t kinds = impl->buffers[7].empty() ? 7u : 8u;
+    uint32_t head[4] = {0x31504352u /*RCP1*/, hdr.width, hdr.height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const uint8_t zeros[8] = {};
-    for (int k = 0; k < 7; ++k)
+    for (uint32_t k = 0; k < kinds; ++k)
     {
         uint64_t n = impl->buffers[k].size();
         fwrite(&n, sizeof(n), 1, f);

@@ -18,6 +18,7 @@
 #include "rive_scene.h"
 
 #include <cstring>
+#include <limits>
 #include <vector>
 
 // Returns nullptr on success, else a message. `makeTarget(width, height)`
@@ -142,8 +143,10 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
     fd.loadAction = LoadAction::clear;
     fd.clearColor = hdr.clear_color;
     fd.ditherMode = static_cast<DitherMode>(hdr.dither_mode);
-    // Never triangulate: midpoint fans for every fill, independent of timing.
-    fd.triangulationThresholds.frameBudgetMs = 0;
+    // Midpoint fans for every fill, or (flag) triangulate every eligible fill;
+    // both are independent of timing.
+    fd.triangulationThresholds.frameBudgetMs =
+        (hdr.flags & RIVE_SCENE_FLAG_TRIANGULATE) ? std::numeric_limits<float>::infinity() : 0.f;
     ctx->beginFrame(fd);
     {
         RiveRenderer renderer(ctx);

@@ -21,7 +21,7 @@ ADAPTER_CAPTURE = os.path.join(HERE, "_ref", "adapter_capture")
 REFERENCE_SOURCES = "/root/reference"
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
-                "grad_spans", "tess_spans")
+                "grad_spans", "tess_spans", "triangles")
 
 
 class FlushDesc(ctypes.Structure):

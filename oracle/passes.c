@@ -95,6 +95,14 @@
 #define PATCH_SEGMENT_SPAN 8
 #define PATCH_VERTEX_COUNT 42
 #define PATCH_INDEX_COUNT 72
+/* Outer-curve patches (gpu.hpp:591-646): 16 curve segments plus a zero-length
+ * bowtie join; AA ramps on both sides of the curve, a middle-out fan over the
+ * 16 curve segments, no midpoint triangle. */
+#define OUTER_SEGMENT_SPAN 17
+#define OUTER_VERTEX_COUNT (OUTER_SEGMENT_SPAN * 8 + OUTER_SEGMENT_SPAN)
+#define OUTER_INDEX_COUNT (OUTER_SEGMENT_SPAN * 12 + 15 * 3)
+#define DRAW_TYPE_OUTER_CURVE_PATCHES 2u
+#define DRAW_TYPE_INTERIOR_TRIANGULATION 3u
 
 /* Sub-pixel precision of the rasteriser (Vulkan minimum is 4 bits; desktop
  * parts use 8). */
@@ -746,6 +754,8 @@ typedef struct
 
 static patch_vertex g_patch[PATCH_VERTEX_COUNT];
 static uint16_t g_patch_idx[PATCH_INDEX_COUNT];
+static patch_vertex g_outer[OUTER_VERTEX_COUNT];
+static uint16_t g_outer_idx[OUTER_INDEX_COUNT];
 static int g_patch_ready = 0;
 
 static void pv_set(patch_vertex* v, float l, float o, float c, int32_t params)
@@ -813,6 +823,62 @@ static void build_patch_tables(void)
     g_patch_idx[k++] = (uint16_t)(fanIdx + span);
     g_patch_idx[k++] = (uint16_t)midIdx;
     (void)n;
+
+    /* Outer-curve patch (gpu.cpp:446-687, PatchType::outerCurves). */
+    const int ospan = OUTER_SEGMENT_SPAN;
+    const int32_t oStroke = (ospan << 2) | STROKE_VERTEX;
+    n = 0;
+    for (int i = 0; i < ospan; ++i) /* top side of the centred AA ramp */
+    {
+        float l = (float)i, r = l + 1.f;
+        pv_set(&g_outer[n + 0], l, 0.f, .5f, oStroke);
+        pv_set(&g_outer[n + 1], l, 1.f, 0.f, oStroke);
+        pv_set(&g_outer[n + 2], r, 0.f, .5f, oStroke);
+        pv_set(&g_outer[n + 3], r, 1.f, 0.f, oStroke);
+        pv_mirror(&g_outer[n + 0], r, 0.f, .5f);
+        pv_mirror(&g_outer[n + 1], l, 0.f, .5f);
+        pv_mirror(&g_outer[n + 2], r, 1.f, 0.f);
+        pv_mirror(&g_outer[n + 3], l, 1.f, 0.f);
+        n += 4;
+    }
+    for (int i = 0; i < ospan; ++i) /* bottom (negative coverage) side */
+    {
+        float l = (float)i, r = l + 1.f;
+        pv_set(&g_outer[n + 0], l, -0.f, .5f, oStroke);
+        pv_set(&g_outer[n + 1], r, -0.f, .5f, oStroke);
+        pv_set(&g_outer[n + 2], l, -1.f, 0.f, oStroke);
+        pv_set(&g_outer[n + 3], r, -1.f, 0.f, oStroke);
+        pv_mirror(&g_outer[n + 0], r, -0.f, .5f);
+        pv_mirror(&g_outer[n + 1], r, -1.f, 0.f);
+        pv_mirror(&g_outer[n + 2], l, -0.f, .5f);
+        pv_mirror(&g_outer[n + 3], l, -1.f, 0.f);
+        n += 4;
+    }
+    const int ofan = n;
+    for (int i = 0; i <= ospan - 1; ++i) /* fan over the 16 curve segments */
+        pv_set(&g_outer[n++], (float)i, 0.f, 1.f, (ospan << 2) | FAN_VERTEX);
+    static const uint16_t negBorder[6] = {0, 2, 1, 1, 2, 3};
+    k = 0;
+    e = 0;
+    for (int sgm = 0; sgm < ospan; ++sgm)
+    {
+        for (int i = 0; i < 6; ++i)
+            g_outer_idx[k++] = (uint16_t)(e + border[i]);
+        e += 4;
+    }
+    for (int sgm = 0; sgm < ospan; ++sgm)
+    {
+        for (int i = 0; i < 6; ++i)
+            g_outer_idx[k++] = (uint16_t)(e + negBorder[i]);
+        e += 4;
+    }
+    for (int step = 1; step < ospan - 1; step <<= 1)
+        for (int i = 0; i < ospan - 1; i += step * 2)
+        {
+            g_outer_idx[k++] = (uint16_t)(ofan + i);
+            g_outer_idx[k++] = (uint16_t)(ofan + i + step);
+            g_outer_idx[k++] = (uint16_t)(ofan + i + step * 2);
+        }
     g_patch_ready = 1;
 }
 
@@ -1058,6 +1124,7 @@ typedef struct
     uint32_t pathID;
     uint32_t features;
     int32_t bx0, by0, bx1, by1; /* pixel bbox, inclusive-exclusive */
+    int interior; /* an interior-triangulation triangle (DRAW_INTERIOR_TRIANGLES) */
 } tri_rec;
 
 static inline int64_t snap(float v)
@@ -1307,13 +1374,22 @@ static void fragment(const frag_ctx* fc,
     uint16_t covBufferID = (uint16_t)(pls->coverage >> 16);
     float coverageCount =
         covBufferID == vPathID ? h2f((uint16_t)(pls->coverage & 0xffffu)) : 0.f;
-    if (covy >= 0.f) /* stroke */
-        coverageCount = maxf(minf(covx, covy), coverageCount);
-    else
+    if (t->interior)
+    {
+        /* draw_raster_order_path.frag:48-53: add the winding weight; the
+         * coverage plane is preserved, not written. */
         coverageCount = coverageCount + covx;
-    uint16_t storedCount = oracle_f32_to_f16(coverageCount);
-    pls->coverage = ((uint32_t)vPathID << 16) | storedCount;
-    coverageCount = h2f(storedCount);
+    }
+    else
+    {
+        if (covy >= 0.f) /* stroke */
+            coverageCount = maxf(minf(covx, covy), coverageCount);
+        else
+            coverageCount = coverageCount + covx;
+        uint16_t storedCount = oracle_f32_to_f16(coverageCount);
+        pls->coverage = ((uint32_t)vPathID << 16) | storedCount;
+        coverageCount = h2f(storedCount);
+    }
 
     float coverage = fabsf(coverageCount);
     if ((features & SF_EVEN_ODD) && evenOdd)
@@ -1349,8 +1425,11 @@ static void fragment(const frag_ctx* fc,
                 outerClipCoverage = clipContentID == outerBits
                                         ? h2f((uint16_t)(pls->clip & 0xffffu))
                                         : 0.f;
-                pls->scratch[0] = unorm8(outerClipCoverage);
-                pls->scratch[1] = pls->scratch[2] = pls->scratch[3] = 0;
+                if (!t->interior) /* interior triangles never hit twice */
+                {
+                    pls->scratch[0] = unorm8(outerClipCoverage);
+                    pls->scratch[1] = pls->scratch[2] = pls->scratch[3] = 0;
+                }
             }
             else
             {
@@ -1456,7 +1535,8 @@ static void fragment(const frag_ctx* fc,
     {
         for (int k = 0; k < 4; ++k)
             dst[k] = (float)pls->color[k] / 255.f;
-        memcpy(pls->scratch, pls->color, 4);
+        if (!t->interior) /* interior triangles are a path's last fragment here */
+            memcpy(pls->scratch, pls->color, 4);
     }
     else
     {
@@ -1553,6 +1633,7 @@ static int setup_triangle(const vtx_out* a,
     t->by1 = (int32_t)by1;
     t->pathID = v[0]->pathID;
     t->features = features;
+    t->interior = 0;
     return 1;
 }
 
@@ -1610,6 +1691,19 @@ static void raster_triangle_rows(const frag_ctx* fc,
     }
 }
 
+static int grow_tris(tri_rec** tris, size_t* cap, size_t n)
+{
+    if (n < *cap)
+        return 0;
+    size_t nc = *cap * 2;
+    tri_rec* nt = (tri_rec*)realloc(*tris, nc * sizeof(tri_rec));
+    if (!nt)
+        return -4;
+    *tris = nt;
+    *cap = nc;
+    return 0;
+}
+
 int oracle_draw(const rive_cuda_flush_desc* d,
                 const oracle_buffers* b,
                 const uint32_t* tess,
@@ -1641,53 +1735,94 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
     {
         const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
-        if (batch->draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
-        {
-            free(tris);
-            return -2;
-        }
         if (batch->shader_features & SF_FEATHER)
         {
             free(tris);
             return -2;
         }
-        for (uint32_t inst = batch->base_element;
-             inst < batch->base_element + batch->element_count;
-             ++inst)
+        int rc = 0;
+        if (batch->draw_type == RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES ||
+            batch->draw_type == DRAW_TYPE_OUTER_CURVE_PATCHES)
         {
-            vtx_out vo[PATCH_VERTEX_COUNT];
-            for (int k = 0; k < PATCH_VERTEX_COUNT; ++k)
+            const int outer = batch->draw_type == DRAW_TYPE_OUTER_CURVE_PATCHES;
+            const patch_vertex* table = outer ? g_outer : g_patch;
+            const uint16_t* idx = outer ? g_outer_idx : g_patch_idx;
+            const int nv = outer ? OUTER_VERTEX_COUNT : PATCH_VERTEX_COUNT;
+            const int ni = outer ? OUTER_INDEX_COUNT : PATCH_INDEX_COUNT;
+            for (uint32_t inst = batch->base_element;
+                 inst < batch->base_element + batch->element_count && rc == 0;
+                 ++inst)
             {
-                int rc = patch_vertex_shader(d, b, tess, tessTexels, &g_patch[k], inst, &vo[k]);
-                if (rc != 0)
+                vtx_out vo[OUTER_VERTEX_COUNT];
+                for (int k = 0; k < nv && rc == 0; ++k)
+                    rc = patch_vertex_shader(d, b, tess, tessTexels, &table[k], inst, &vo[k]);
+                for (int k = 0; k < ni && rc == 0; k += 3)
                 {
-                    free(tris);
-                    return rc;
-                }
-            }
-            for (int k = 0; k < PATCH_INDEX_COUNT; k += 3)
-            {
-                if (n == cap)
-                {
-                    cap *= 2;
-                    tri_rec* nt = (tri_rec*)realloc(tris, cap * sizeof(tri_rec));
-                    if (!nt)
+                    rc = grow_tris(&tris, &cap, n);
+                    if (rc == 0)
                     {
-                        free(tris);
-                        return -4;
+                        int r = setup_triangle(&vo[idx[k]], &vo[idx[k + 1]], &vo[idx[k + 2]],
+                                               batch->shader_features, W, H, &tris[n]);
+                        if (r < 0)
+                            rc = r;
+                        else
+                            n += (size_t)r;
                     }
-                    tris = nt;
                 }
-                int rc = setup_triangle(&vo[g_patch_idx[k]], &vo[g_patch_idx[k + 1]],
-                                        &vo[g_patch_idx[k + 2]], batch->shader_features,
-                                        W, H, &tris[n]);
-                if (rc < 0)
-                {
-                    free(tris);
-                    return rc;
-                }
-                n += (size_t)rc;
             }
+        }
+        else if (batch->draw_type == DRAW_TYPE_INTERIOR_TRIANGULATION)
+        {
+            /* unpack_interior_triangle_vertex (draw_path_common.glsl:792-819):
+             * three TriangleVertex records {x, y, weight << 16 | pathID} per
+             * triangle, drawn with the winding weight as constant coverage. */
+            if (batch->element_count % 3 ||
+                ((size_t)batch->base_element + batch->element_count) * 12 > b->triangles_bytes)
+                rc = -1;
+            const uint32_t* tv = (const uint32_t*)b->triangles;
+            for (uint32_t v = batch->base_element;
+                 v < batch->base_element + batch->element_count && rc == 0; v += 3)
+            {
+                vtx_out vo[3];
+                for (int k = 0; k < 3 && rc == 0; ++k)
+                {
+                    const uint32_t* r = tv + 3 * ((size_t)v + k);
+                    uint32_t pathID = r[2] & 0xffffu;
+                    const float* path = path_record(d, b, pathID);
+                    if (!path)
+                    {
+                        rc = -1;
+                        break;
+                    }
+                    float M[4] = {path[0], path[1], path[2], path[3]};
+                    f2 p = mat_mul(M, (f2){u2f(r[0]), u2f(r[1])});
+                    vo[k].pos = (f2){p.x + path[4], p.y + path[5]};
+                    vo[k].cov[0] = (float)((int32_t)r[2] >> 16);
+                    vo[k].cov[1] = -1.f;
+                    vo[k].pathID = pathID;
+                    vo[k].discard = 0;
+                }
+                if (rc == 0)
+                    rc = grow_tris(&tris, &cap, n);
+                if (rc == 0)
+                {
+                    int r = setup_triangle(&vo[0], &vo[1], &vo[2], batch->shader_features, W, H,
+                                           &tris[n]);
+                    if (r < 0)
+                        rc = r;
+                    else if (r > 0)
+                        tris[n++].interior = 1;
+                }
+            }
+        }
+        else
+        {
+            rc = -2;
+        }
+        if (rc != 0)
+        {
+            free(tris);
+            return rc;
         }
     }
 

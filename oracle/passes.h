@@ -51,6 +51,8 @@ typedef struct oracle_buffers
     size_t grad_spans_bytes;
     const void* tess_spans;
     size_t tess_spans_bytes;
+    const void* triangles; /* gpu::TriangleVertex, 12 B each (interior triangulation) */
+    size_t triangles_bytes;
 } oracle_buffers;
 
 /* Pass 1 into grad (512 x grad_data_height RGBA8). Returns 0 on success. */

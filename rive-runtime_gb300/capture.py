@@ -16,7 +16,7 @@ import numpy as np
 CAPTURE_MAGIC = 0x31504352  # "RCP1"
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
-                "grad_spans", "tess_spans")
+                "grad_spans", "tess_spans", "triangles")
 
 # rive_cuda_flush_desc field order (include/rive_cuda.h); 36 u32-sized fields,
 # then the draw_batches pointer (8 bytes, LP64).
@@ -84,9 +84,10 @@ def parse(data: bytes) -> Capture:
 
 
 def serialize(cap: Capture) -> bytes:
-    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC, cap.width, cap.height,
-                                len(BUFFER_NAMES)))
-    for name in BUFFER_NAMES:
+    # Seven kinds, or eight when the frame has interior triangles.
+    kinds = BUFFER_NAMES if cap.buffers.get("triangles") else BUFFER_NAMES[:7]
+    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC, cap.width, cap.height, len(kinds)))
+    for name in kinds:
         b = cap.buffers.get(name, b"")
         out += struct.pack("<Q", len(b)) + b + bytes((8 - (len(b) & 7)) & 7)
     out += struct.pack("<I", len(cap.flushes))

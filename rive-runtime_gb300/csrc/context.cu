@@ -8,7 +8,8 @@
 // 3-deep ring (gpu::kBufferRingSize, gpu.hpp:77) of pinned, write-combined
 // host staging buffers, and unmap enqueues one host->device copy into a
 // device-resident copy of the buffer. flush() then runs, in stream order:
-//   color_ramp_kernel -> tessellate_kernel -> patch_setup_kernel ->
+//   color_ramp_kernel -> tessellate_kernel -> patch_setup_kernel (midpoint fans,
+//   outer curves) + interior_setup_kernel ->
 //   (scan) -> bin_scatter_kernel -> (radix sort by tile) ->
 //   tile_ranges_kernel -> raster_tile_kernel.
 #include "rive_cuda.h"
@@ -29,6 +30,8 @@ namespace rivecuda
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void outer_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void interior_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_fill_kernel(const uint32_t* pairTotal,
                                 uint32_t capacity,
@@ -251,11 +254,29 @@ void stage_end(rive_cuda_context* ctx, cudaStream_t s)
     ctx->openEvent = nullptr;
 }
 
+// The record buffers a flush reads, in buffer-kind order (flush uniforms ..
+// triangle vertices).
+constexpr int kResolvedKinds = 8;
 struct ResolvedBuffers
 {
-    const void* ptr[7];
-    size_t bytes[7];
+    const void* ptr[kResolvedKinds];
+    size_t bytes[kResolvedKinds];
 };
+
+// Caller-owned device buffers: sizes are the caller's; ranges come from desc.
+ResolvedBuffers resolve_device_buffers(const rive_cuda_device_buffers& b)
+{
+    const void* p[kResolvedKinds] = {b.flush_uniforms, b.paths,      b.paints,
+                                     b.paint_aux,      b.contours,   b.grad_spans,
+                                     b.tess_spans,     b.triangle_vertices};
+    ResolvedBuffers rb;
+    for (int k = 0; k < kResolvedKinds; ++k)
+    {
+        rb.ptr[k] = p[k];
+        rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0;
+    }
+    return rb;
+}
 
 // One logical flush of a batch.
 struct FlushInput
@@ -265,16 +286,30 @@ struct FlushInput
     uint32_t* fb;
 };
 
-// Host-side checks of one flush; counts its patch instances.
+// Set-up list of a draw type and the triangles one of its items makes.
+int setup_list(uint32_t drawType)
+{
+    return drawType == DRAW_MIDPOINT_FAN_PATCHES  ? 0
+           : drawType == DRAW_OUTER_CURVE_PATCHES ? 1
+           : drawType == DRAW_INTERIOR_TRIANGULATION ? 2
+                                                     : -1;
+}
+constexpr uint32_t kTrianglesPerItem[kSetupLists] = {kPatchTriangleCount,
+                                                     kOuterPatchTriangleCount, 1};
+
+// Items (patch instances or triangles) of a draw batch.
+uint32_t batch_items(const rive_cuda_draw_batch& b)
+{
+    return b.draw_type == DRAW_INTERIOR_TRIANGULATION ? b.element_count / 3 : b.element_count;
+}
+
+// Host-side checks of one flush; counts its triangle slots.
 int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const ResolvedBuffers& rb,
-                   uint64_t& instances)
+                   uint64_t& slots)
 {
     if (d->interlock_mode != 0)
         return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
                          "interlock mode %u not supported (rasterOrdering only)", d->interlock_mode);
-    if (d->has_triangle_vertices)
-        return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
-                         "interior triangulation draws are not supported");
     if (d->render_target_width == 0 || d->render_target_height == 0)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "empty render target");
     if (d->render_target_width > 16384 || d->render_target_height > 16384)
@@ -303,20 +338,33 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush uniforms out of range");
     if (d->grad_data_height > 65536 || d->tess_data_height > 65536)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "texture height out of range");
-    instances = 0;
+    slots = 0;
     for (uint32_t i = 0; i < d->draw_batch_count; ++i)
     {
         const rive_cuda_draw_batch& b = d->draw_batches[i];
-        if (b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
+        const int list = setup_list(b.draw_type);
+        if (list < 0)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
                              b.draw_type);
         if (b.shader_features & SF_FEATHER)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
-        if (((uint64_t)b.base_element + b.element_count) * kPatchSegmentSpan >
-            (uint64_t)d->tess_data_height * kTessTextureWidth)
-            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
-                             "batch %u reads past the tessellation texture", i);
-        instances += b.element_count;
+        if (list == 2)
+        {
+            if (b.element_count % 3 || !rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE] ||
+                ((uint64_t)b.base_element + b.element_count) * 12 >
+                    rb.bytes[RIVE_CUDA_BUFFER_TRIANGLE])
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "batch %u reads past the triangle vertices", i);
+        }
+        else
+        {
+            const uint64_t span = list == 1 ? kOuterPatchSegmentSpan : kPatchSegmentSpan;
+            if (((uint64_t)b.base_element + b.element_count) * span >
+                (uint64_t)d->tess_data_height * kTessTextureWidth)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "batch %u reads past the tessellation texture", i);
+        }
+        slots += (uint64_t)batch_items(b) * kTrianglesPerItem[list];
     }
     return RIVE_CUDA_OK;
 }
@@ -326,13 +374,14 @@ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 // Host-side layout of a batch of independent logical flushes.
 struct BatchLayout
 {
-    uint32_t n = 0, segCount = 0;
-    uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, instances = 0, slots = 0;
+    uint32_t n = 0;
+    uint32_t segCount[kSetupLists] = {}, items[kSetupLists] = {};
+    uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0;
     uint64_t tessRows = 0, gradRows = 0;
     std::vector<uint64_t> tessRow0, gradRow0;
     // Table blob offsets.
     size_t oScenes = 0, oGradBase = 0, oTessBase = 0, oTileBase = 0, oSceneTiles = 0,
-           oSegments = 0, oSegBase = 0, tableBytes = 0;
+           oSegments[kSetupLists] = {}, oSegBase[kSetupLists] = {}, tableBytes = 0;
     size_t tessBytes() const { return (size_t)kTessTextureWidth * tessRows * 16; }
     size_t gradBytes() const { return (size_t)kGradTextureWidth * gradRows * 4; }
     int endBit() const
@@ -353,11 +402,12 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     L.n = n;
     L.tessRow0.resize(n);
     L.gradRow0.resize(n);
-    uint64_t instances = 0, segs = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
+    uint64_t slots = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
+    uint64_t segs[kSetupLists] = {}, items[kSetupLists] = {};
     for (uint32_t i = 0; i < n; ++i)
     {
-        uint64_t inst = 0;
-        int rc = validate_flush(ctx, in[i].d, in[i].rb, inst);
+        uint64_t fs = 0;
+        int rc = validate_flush(ctx, in[i].d, in[i].rb, fs);
         if (rc)
             return rc;
         if (!in[i].fb)
@@ -365,9 +415,17 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         if (!in[i].rb.ptr[RIVE_CUDA_BUFFER_FLUSH_UNIFORM])
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u has no uniforms", i);
         const rive_cuda_flush_desc* d = in[i].d;
-        instances += inst;
+        slots += fs;
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
-            segs += d->draw_batches[b].element_count ? 1 : 0;
+        {
+            const rive_cuda_draw_batch& db = d->draw_batches[b];
+            const uint32_t k = batch_items(db);
+            if (!k)
+                continue;
+            const int list = setup_list(db.draw_type);
+            segs[list] += 1;
+            items[list] += k;
+        }
         L.tessRow0[i] = L.tessRows;
         L.gradRow0[i] = L.gradRows;
         L.tessRows += std::max(d->tess_data_height, 1u);
@@ -377,8 +435,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         gradSpans += d->grad_span_count;
         tessSpans += d->tess_span_count;
     }
-    if (instances * kPatchTriangleCount > 0xffffffffull || tiles >= 0x7fffffffull ||
-        gradSpans > 0x7fffffffull || tessSpans * 32 > 0xffffffffull)
+    if (slots > 0xffffffffull || tiles >= 0x7fffffffull || gradSpans > 0x7fffffffull ||
+        tessSpans * 32 > 0xffffffffull)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "batch too large");
     if (n > 1)
     {
@@ -391,20 +449,28 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                              "two flushes of one batch share a render target");
     }
-    L.segCount = (uint32_t)segs;
+    for (int l = 0; l < kSetupLists; ++l)
+    {
+        L.segCount[l] = (uint32_t)segs[l];
+        L.items[l] = (uint32_t)items[l];
+    }
     L.gradSpans = (uint32_t)gradSpans;
     L.tessSpans = (uint32_t)tessSpans;
     L.tiles = (uint32_t)tiles;
-    L.instances = (uint32_t)instances;
-    L.slots = (uint32_t)(instances * kPatchTriangleCount);
+    L.slots = (uint32_t)slots;
     L.oScenes = 0;
     L.oGradBase = align16(L.oScenes + sizeof(FlushParams) * n);
     L.oTessBase = align16(L.oGradBase + 4 * (n + 1));
     L.oTileBase = align16(L.oTessBase + 4 * (n + 1));
     L.oSceneTiles = align16(L.oTileBase + 4 * (n + 1));
-    L.oSegments = align16(L.oSceneTiles + 8 * n);
-    L.oSegBase = align16(L.oSegments + sizeof(PatchSegment) * std::max<uint64_t>(segs, 1));
-    L.tableBytes = align16(L.oSegBase + 4 * (segs + 1));
+    size_t o = align16(L.oSceneTiles + 8 * n);
+    for (int l = 0; l < kSetupLists; ++l)
+    {
+        L.oSegments[l] = o;
+        L.oSegBase[l] = align16(o + sizeof(PatchSegment) * std::max<uint64_t>(segs[l], 1));
+        o = align16(L.oSegBase[l] + 4 * (segs[l] + 1));
+    }
+    L.tableBytes = o;
     return RIVE_CUDA_OK;
 }
 
@@ -438,9 +504,15 @@ BatchTables write_tables(rive_cuda_context* ctx,
     auto* tessBase = (uint32_t*)(h + L.oTessBase);
     auto* tileBase = (uint32_t*)(h + L.oTileBase);
     auto* sceneTiles = (uint2*)(h + L.oSceneTiles);
-    auto* segs = (PatchSegment*)(h + L.oSegments);
-    auto* segBase = (uint32_t*)(h + L.oSegBase);
-    uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, segAcc = 0, instAcc = 0, slotAcc = 0;
+    PatchSegment* segs[kSetupLists];
+    uint32_t* segBase[kSetupLists];
+    for (int l = 0; l < kSetupLists; ++l)
+    {
+        segs[l] = (PatchSegment*)(h + L.oSegments[l]);
+        segBase[l] = (uint32_t*)(h + L.oSegBase[l]);
+    }
+    uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, slotAcc = 0;
+    uint32_t segAcc[kSetupLists] = {}, itemAcc[kSetupLists] = {};
     for (uint32_t i = 0; i < L.n; ++i)
     {
         const rive_cuda_flush_desc* d = in[i].d;
@@ -481,6 +553,9 @@ BatchTables write_tables(rive_cuda_context* ctx,
         P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
         P.tess = S.tess + (size_t)L.tessRow0[i] * kTessTextureWidth;
         P.grad = S.grad + (size_t)L.gradRow0[i] * kGradTextureWidth;
+        P.triangleVertices = (const uint32_t*)rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE];
+        P.triangleVertexCount = (uint32_t)std::min<size_t>(rb.bytes[RIVE_CUDA_BUFFER_TRIANGLE] / 12,
+                                                           0xffffffffu);
 
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
@@ -489,22 +564,26 @@ BatchTables write_tables(rive_cuda_context* ctx,
         gAcc += d->grad_span_count;
         tAcc += d->tess_span_count;
         tileAcc += P.tilesX * ((d->render_target_height + kTileSize - 1) / kTileSize);
+        // Slots follow the draw list order across all three set-up lists.
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
         {
             const rive_cuda_draw_batch& db = d->draw_batches[b];
-            if (!db.element_count)
+            const uint32_t k = batch_items(db);
+            if (!k)
                 continue;
-            segs[segAcc] = PatchSegment{i, db.base_element, db.shader_features, slotAcc};
-            segBase[segAcc] = instAcc;
-            ++segAcc;
-            instAcc += db.element_count;
-            slotAcc += db.element_count * kPatchTriangleCount;
+            const int l = setup_list(db.draw_type);
+            segs[l][segAcc[l]] = PatchSegment{i, db.base_element, db.shader_features, slotAcc};
+            segBase[l][segAcc[l]] = itemAcc[l];
+            ++segAcc[l];
+            itemAcc[l] += k;
+            slotAcc += k * kTrianglesPerItem[l];
         }
     }
     gradBase[L.n] = gAcc;
     tessBase[L.n] = tAcc;
     tileBase[L.n] = tileAcc;
-    segBase[segAcc] = instAcc;
+    for (int l = 0; l < kSetupLists; ++l)
+        segBase[l][segAcc[l]] = itemAcc[l];
 
     BatchTables B = {};
     const uint8_t* dT = S.tables;
@@ -513,13 +592,16 @@ BatchTables write_tables(rive_cuda_context* ctx,
     B.tessSpanBase = (const uint32_t*)(dT + L.oTessBase);
     B.tileBase = (const uint32_t*)(dT + L.oTileBase);
     B.sceneTiles = (const uint2*)(dT + L.oSceneTiles);
-    B.segments = (const PatchSegment*)(dT + L.oSegments);
-    B.segInstanceBase = (const uint32_t*)(dT + L.oSegBase);
+    for (int l = 0; l < kSetupLists; ++l)
+    {
+        B.segments[l] = (const PatchSegment*)(dT + L.oSegments[l]);
+        B.segBase[l] = (const uint32_t*)(dT + L.oSegBase[l]);
+        B.segCount[l] = segAcc[l];
+        B.totalItems[l] = itemAcc[l];
+    }
     B.sceneCount = L.n;
-    B.segmentCount = segAcc;
     B.totalGradSpans = gAcc;
     B.totalTessSpans = tAcc;
-    B.totalInstances = instAcc;
     B.totalTiles = tileAcc;
     return B;
 }
@@ -553,7 +635,12 @@ int enqueue_front(rive_cuda_context* ctx,
     if (L.slots)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
-        patch_setup_kernel<<<(L.instances + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
+        if (L.items[0])
+            patch_setup_kernel<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
+        if (L.items[1])
+            outer_setup_kernel<<<(L.items[1] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
+        if (L.items[2])
+            interior_setup_kernel<<<(L.items[2] + 255) / 256, 256, 0, stream>>>(B, S.tris, S.counts);
         stage_end(ctx, stream);
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
         size_t tempBytes = S.scanTempBytes;
@@ -692,7 +779,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     if (rc)
         return rc;
     ctx->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
-    ctx->stats.patches = L.instances;
+    ctx->stats.patches = (uint64_t)L.items[0] + L.items[1];
     ctx->stats.triangles = L.slots;
     ctx->stats.bin_entries = pairs;
     ctx->stats.tiles = L.tiles;
@@ -983,7 +1070,7 @@ int rive_cuda_flush(rive_cuda_context* ctx,
         CK(cudaEventDestroy(ev));
     }
     ResolvedBuffers rb;
-    for (int k = 0; k < 7; ++k)
+    for (int k = 0; k < kResolvedKinds; ++k)
     {
         rb.ptr[k] = ctx->rings[k].device.ptr;
         rb.bytes[k] = ctx->rings[k].deviceValidBytes;
@@ -1000,14 +1087,7 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
     if (!ctx || !desc || !buffers || !target_pixels_device)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "NULL argument to flush_device");
     CK(cudaSetDevice(ctx->device));
-    ResolvedBuffers rb;
-    const void* p[7] = {buffers->flush_uniforms, buffers->paths, buffers->paints, buffers->paint_aux,
-                        buffers->contours, buffers->grad_spans, buffers->tess_spans};
-    for (int k = 0; k < 7; ++k)
-    {
-        rb.ptr[k] = p[k];
-        rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0; // caller-sized; ranges come from desc
-    }
+    const ResolvedBuffers rb = resolve_device_buffers(*buffers);
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     return run_flush(ctx, desc, rb, (uint32_t*)target_pixels_device, s);
 }
@@ -1116,7 +1196,7 @@ int graph_build(rive_cuda_context* ctx,
     CK(e);
     CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
     g->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
-    g->stats.patches = L.instances;
+    g->stats.patches = (uint64_t)L.items[0] + L.items[1];
     g->stats.triangles = L.slots;
     g->stats.bin_entries = g->measured;
     g->stats.tiles = L.tiles;
@@ -1142,15 +1222,8 @@ int rive_cuda_graph_create(rive_cuda_context* ctx,
         if (!f.desc || !f.target_pixels_device)
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u: NULL desc or target",
                              i);
-        const void* p[7] = {f.buffers.flush_uniforms, f.buffers.paths,    f.buffers.paints,
-                            f.buffers.paint_aux,      f.buffers.contours, f.buffers.grad_spans,
-                            f.buffers.tess_spans};
         in[i].d = f.desc;
-        for (int k = 0; k < 7; ++k)
-        {
-            in[i].rb.ptr[k] = p[k];
-            in[i].rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0;
-        }
+        in[i].rb = resolve_device_buffers(f.buffers);
         in[i].fb = (uint32_t*)f.target_pixels_device;
     }
     CK(cudaSetDevice(ctx->device));
@@ -1231,15 +1304,8 @@ int rive_cuda_flush_batch(rive_cuda_context* ctx,
         if (!f.desc || !f.target_pixels_device)
             return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "flush %u: NULL desc or target",
                              i);
-        const void* p[7] = {f.buffers.flush_uniforms, f.buffers.paths,    f.buffers.paints,
-                            f.buffers.paint_aux,      f.buffers.contours, f.buffers.grad_spans,
-                            f.buffers.tess_spans};
         in[i].d = f.desc;
-        for (int k = 0; k < 7; ++k)
-        {
-            in[i].rb.ptr[k] = p[k];
-            in[i].rb.bytes[k] = p[k] ? (size_t)-1 / 2 : 0; // caller-sized
-        }
+        in[i].rb = resolve_device_buffers(f.buffers);
         in[i].fb = (uint32_t*)f.target_pixels_device;
     }
     CK(cudaSetDevice(ctx->device));

@@ -23,6 +23,7 @@ namespace rivecuda
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void outer_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    const uint2* sceneTiles,
@@ -282,13 +283,17 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     B.tessSpanBase = (const uint32_t*)(dTab + kTabPrefix) + 2;
     B.tileBase = (const uint32_t*)(dTab + kTabPrefix) + 4;
     B.sceneTiles = (const uint2*)(dTab + kTabSceneTiles);
-    B.segments = (const PatchSegment*)(dTab + kTabSegments);
-    B.segInstanceBase = (const uint32_t*)(dTab + kTabSegBase);
+    // Midpoint-fan patches only (the other set-up lists stay empty).
+    for (int l = 0; l < kSetupLists; ++l)
+    {
+        B.segments[l] = (const PatchSegment*)(dTab + kTabSegments);
+        B.segBase[l] = (const uint32_t*)(dTab + kTabSegBase);
+    }
+    B.segCount[0] = segCount;
+    B.totalItems[0] = instAcc;
     B.sceneCount = 1;
-    B.segmentCount = segCount;
     B.totalGradSpans = d->grad_span_count;
     B.totalTessSpans = d->tess_span_count;
-    B.totalInstances = instAcc;
     B.totalTiles = tiles;
 
     // What must start at zero on every call: the error word, the tile

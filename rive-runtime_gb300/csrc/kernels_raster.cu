@@ -104,6 +104,105 @@ __device__ __forceinline__ void patch_triangle(int t, int& a, int& b, int& c)
     }
 }
 
+// The outerCurves patch vertex table (gpu.cpp:446-560, PatchType::outerCurves):
+// 17 segments (16 curve segments and a zero-length bowtie join), a centred
+// AA ramp on each side of the curve (coverage 1/2 on the curve), and a fan
+// over the 16 curve segments; no midpoint vertex.
+__device__ __forceinline__ PatchVertexDesc outer_vertex_desc(int v)
+{
+    PatchVertexDesc d;
+    if (v < 2 * 4 * kOuterPatchSegmentSpan)
+    {
+        const bool bottom = v >= 4 * kOuterPatchSegmentSpan;
+        const int u = bottom ? v - 4 * kOuterPatchSegmentSpan : v;
+        const float l = (float)(u >> 2), r = l + 1.f;
+        d.vertexType = STROKE_VERTEX;
+        if (!bottom)
+        {
+            switch (u & 3)
+            {
+                case 0:
+                    d.localVertexID = l; d.outset = 0.f; d.fillCoverage = .5f;
+                    d.mLocalVertexID = r; d.mOutset = 0.f; d.mFillCoverage = .5f;
+                    break;
+                case 1:
+                    d.localVertexID = l; d.outset = 1.f; d.fillCoverage = 0.f;
+                    d.mLocalVertexID = l; d.mOutset = 0.f; d.mFillCoverage = .5f;
+                    break;
+                case 2:
+                    d.localVertexID = r; d.outset = 0.f; d.fillCoverage = .5f;
+                    d.mLocalVertexID = r; d.mOutset = 1.f; d.mFillCoverage = 0.f;
+                    break;
+                default:
+                    d.localVertexID = r; d.outset = 1.f; d.fillCoverage = 0.f;
+                    d.mLocalVertexID = l; d.mOutset = 1.f; d.mFillCoverage = 0.f;
+                    break;
+            }
+        }
+        else
+        {
+            switch (u & 3)
+            {
+                case 0:
+                    d.localVertexID = l; d.outset = -0.f; d.fillCoverage = .5f;
+                    d.mLocalVertexID = r; d.mOutset = -0.f; d.mFillCoverage = .5f;
+                    break;
+                case 1:
+                    d.localVertexID = r; d.outset = -0.f; d.fillCoverage = .5f;
+                    d.mLocalVertexID = r; d.mOutset = -1.f; d.mFillCoverage = 0.f;
+                    break;
+                case 2:
+                    d.localVertexID = l; d.outset = -1.f; d.fillCoverage = 0.f;
+                    d.mLocalVertexID = l; d.mOutset = -0.f; d.mFillCoverage = .5f;
+                    break;
+                default:
+                    d.localVertexID = r; d.outset = -1.f; d.fillCoverage = 0.f;
+                    d.mLocalVertexID = l; d.mOutset = -1.f; d.mFillCoverage = 0.f;
+                    break;
+            }
+        }
+    }
+    else
+    {
+        const float i = (float)(v - 2 * 4 * kOuterPatchSegmentSpan);
+        d.vertexType = FAN_VERTEX;
+        d.localVertexID = i; d.outset = 0.f; d.fillCoverage = 1.f;
+        d.mLocalVertexID = i; d.mOutset = 0.f; d.mFillCoverage = 1.f;
+    }
+    return d;
+}
+
+// The outerCurves index table, by triangle index: the top ramp (pattern
+// 0,1,2 / 2,1,3), the bottom ramp (0,2,1 / 1,2,3), then the middle-out fan.
+__device__ __forceinline__ void outer_triangle(int t, int& a, int& b, int& c)
+{
+    constexpr int kRamp = 2 * kOuterPatchSegmentSpan;
+    if (t < kRamp)
+    {
+        const int e = (t >> 1) * 4;
+        if ((t & 1) == 0) { a = e; b = e + 1; c = e + 2; }
+        else { a = e + 2; b = e + 1; c = e + 3; }
+        return;
+    }
+    if (t < 2 * kRamp)
+    {
+        const int u = t - kRamp;
+        const int e = 4 * kOuterPatchSegmentSpan + (u >> 1) * 4;
+        if ((u & 1) == 0) { a = e; b = e + 2; c = e + 1; }
+        else { a = e + 1; b = e + 2; c = e + 3; }
+        return;
+    }
+    // Middle-out fan over the 17 fan vertices: steps 1, 2, 4, 8.
+    const int fan = 8 * kOuterPatchSegmentSpan;
+    const int u = t - 2 * kRamp;
+    const int step = u < 8 ? 1 : (u < 12 ? 2 : (u < 14 ? 4 : 8));
+    const int first = u < 8 ? 0 : (u < 12 ? 8 : (u < 14 ? 12 : 14));
+    const int i = (u - first) * 2 * step;
+    a = fan + i;
+    b = fan + i + step;
+    c = fan + i + 2 * step;
+}
+
 __device__ __forceinline__ float2 mat_mul(float4 m, float2 v)
 {
     // float2x2 columns (m.x, m.y) and (m.z, m.w).
@@ -146,15 +245,14 @@ __device__ __forceinline__ bool tess_fetch(const FlushParams& P, long long idx, 
 // unpack_tessellated_path_vertex for a midpointFan patch vertex, plus the
 // position math of @drawVertexMain. Returns false on a malformed input.
 __device__ bool shade_patch_vertex(const FlushParams& P,
-                                   int v,
+                                   const PatchVertexDesc& pv,
+                                   int span,
                                    uint32_t instanceID,
                                    VertexOut& o)
 {
-    PatchVertexDesc pv = patch_vertex_desc(v);
     int localVertexID = (int)pv.localVertexID;
     float outset = pv.outset;
     float fillCoverage = pv.fillCoverage;
-    const int span = kPatchSegmentSpan;
     int vertexIDOnContour = min(localVertexID, span - 1);
     long long tessVertexIdx = (long long)instanceID * span + vertexIDOnContour;
     uint4 tv;
@@ -439,35 +537,183 @@ __device__ __forceinline__ int4 unpack_bbox(uint4 meta)
 }
 } // namespace
 
-// Per patch instance of the batch (one warp): shade 42 vertices, assemble and
-// set up 24 triangles, then count the tiles each one touches, the warp
-// striding over each triangle's tile rectangle. Triangle slot order is
-// primitive order (scene, draw batch, instance, triangle-in-patch).
-__global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
-                                                          TriRecord* __restrict__ tris,
-                                                          uint32_t* __restrict__ tileCounts)
+// Sets up one triangle for the tile raster: snaps the vertices to the
+// 1/256-pixel grid, culls counterclockwise and degenerate triangles (exact
+// integer area), clips the pixel box to the target, and builds the edge
+// functions and coverage planes. Returns false for a triangle that draws
+// nothing (bb stays empty).
+__device__ bool setup_triangle(const FlushParams& P,
+                               const VertexOut& A,
+                               const VertexOut& B,
+                               const VertexOut& C,
+                               uint32_t features,
+                               uint32_t scene,
+                               TriRecord& T,
+                               int4& bb)
 {
-    __shared__ VertexOut sv[4][kPatchVertexCount];
-    __shared__ float4 sEdges[4][kPatchTriangleCount][3];
-    __shared__ int4 sBox[4][kPatchTriangleCount];
+    bb = make_int4(0, 0, 0, 0);
+    if (A.discard || B.discard || C.discard)
+        return false;
+    float m = fmaxf(fmaxf(fmaxf(fabsf(A.pos.x), fabsf(A.pos.y)), fmaxf(fabsf(B.pos.x), fabsf(B.pos.y))),
+                    fmaxf(fabsf(C.pos.x), fabsf(C.pos.y)));
+    if (!(m < 32768.f)) // NaN or outside the exact snapping range
+    {
+        if (!isnan(m))
+            atomicOr(P.error, ERR_COORD_RANGE);
+        return false;
+    }
+    const int X0 = __float2int_rn(A.pos.x * 256.f), Y0 = __float2int_rn(A.pos.y * 256.f);
+    const int X1 = __float2int_rn(B.pos.x * 256.f), Y1 = __float2int_rn(B.pos.y * 256.f);
+    const int X2 = __float2int_rn(C.pos.x * 256.f), Y2 = __float2int_rn(C.pos.y * 256.f);
+    // Exact twice-area in 1/65536 px^2: counterclockwise culled, degenerate
+    // dropped.
+    const long long area2 =
+        (long long)(X1 - X0) * (Y2 - Y0) - (long long)(X2 - X0) * (Y1 - Y0);
+    if (area2 <= 0)
+        return false;
+    const int mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
+    const int mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
+    // Pixels k whose centres (256 k + 128) lie in [min, max].
+    const int bx0 = max(-((-(mnx - 128)) >> 8), 0);
+    const int bx1 = min(((mxx - 128) >> 8) + 1, (int)P.width);
+    const int by0 = max(-((-(mny - 128)) >> 8), 0);
+    const int by1 = min(((mxy - 128) >> 8) + 1, (int)P.height);
+    if (bx0 >= bx1 || by0 >= by1)
+        return false;
+    const float s = 1.f / 256.f;
+    const float2 p0 = make_float2(X0 * s, Y0 * s), p1 = make_float2(X1 * s, Y1 * s);
+    const float2 p2 = make_float2(X2 * s, Y2 * s);
+    T.e0 = make_edge(p0, p1);
+    T.e1 = make_edge(p1, p2);
+    T.e2 = make_edge(p2, p0);
+    const float d1x = p1.x - p0.x, d1y = p1.y - p0.y;
+    const float d2x = p2.x - p0.x, d2y = p2.y - p0.y;
+    const float inv = 1.f / ((float)area2 * (s * s));
+    const float ax = T.e0.x - p0.x, ay = T.e0.y - p0.y;
+    const float cxgx = ((B.cov.x - A.cov.x) * d2y - (C.cov.x - A.cov.x) * d1y) * inv;
+    const float cxgy = ((C.cov.x - A.cov.x) * d1x - (B.cov.x - A.cov.x) * d2x) * inv;
+    const float cygx = ((B.cov.y - A.cov.y) * d2y - (C.cov.y - A.cov.y) * d1y) * inv;
+    const float cygy = ((C.cov.y - A.cov.y) * d1x - (B.cov.y - A.cov.y) * d2x) * inv;
+    const uint2 paint = P.paints[P.firstPaint + A.pathID];
+    T.cov0 = make_float4(A.cov.x + cxgx * ax + cxgy * ay, cxgx, cxgy, A.cov.y + cygx * ax + cygy * ay);
+    T.cov1 = make_float4(cygx, cygy, __uint_as_float(paint.x), __uint_as_float(paint.y));
+    // The fp16 coverage key of the path (draw_raster_order_path.frag: pathID
+    // bits, sign bit flipped for even-odd fills).
+    uint32_t key = A.pathID == 0 ? 0u : ((A.pathID + MAX_DENORM_F16) * P.pathIDGranularity) & 0xffffu;
+    if (paint.x & PAINT_FLAG_EVEN_ODD_FILL)
+        key ^= 0x8000u;
+    bb = make_int4(bx0, by0, bx1, by1);
+    T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16), (uint32_t)bx0 | ((uint32_t)bx1 << 16),
+                        (uint32_t)by0 | ((uint32_t)by1 << 16), key | (scene << 16));
+    return true;
+}
+
+// Tiles a set-up triangle touches (the same tile test as the binner's).
+__device__ __forceinline__ void tile_span(int4 bb, int& tx0, int& ty0, int& ntx, int& nty)
+{
+    tx0 = bb.x >> kTileLog2;
+    ty0 = bb.y >> kTileLog2;
+    ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
+    nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+}
+
+constexpr int kLaneTiles = 8;
+
+// Counts the tiles of the warp's triangles: a lane counts its own triangle
+// when its box spans at most kLaneTiles tiles; the whole warp walks larger
+// ones in turn. `has` marks lanes holding a triangle; e/bb its edges and box.
+__device__ __forceinline__ void count_tiles(bool has,
+                                            const float4* e,
+                                            int4 bb,
+                                            uint32_t* __restrict__ countOut,
+                                            const float4 (*warpEdges)[3],
+                                            const int4* warpBoxes,
+                                            uint32_t* const* warpOuts)
+{
+    const int lane = threadIdx.x & 31;
+    bool big = false;
+    if (has)
+    {
+        if (bb.z > bb.x)
+        {
+            int tx0, ty0, ntx, nty;
+            tile_span(bb, tx0, ty0, ntx, nty);
+            if (ntx * nty <= kLaneTiles)
+            {
+                uint32_t count = 0;
+                for (int ty = ty0; ty < ty0 + nty; ++ty)
+                    for (int tx = tx0; tx < tx0 + ntx; ++tx)
+                        count += tile_overlaps(e, bb, tx, ty) ? 1u : 0u;
+                *countOut = count;
+            }
+            else
+            {
+                big = true;
+            }
+        }
+        else
+        {
+            *countOut = 0;
+        }
+    }
+    uint32_t bigs = __ballot_sync(0xffffffffu, big);
+    while (bigs)
+    {
+        const int t = __ffs(bigs) - 1;
+        bigs &= bigs - 1;
+        const int4 tb = warpBoxes[t];
+        const float4 te[3] = {warpEdges[t][0], warpEdges[t][1], warpEdges[t][2]};
+        int tx0, ty0, ntx, nty;
+        tile_span(tb, tx0, ty0, ntx, nty);
+        const int n = ntx * nty;
+        uint32_t count = 0;
+        for (int i = lane; i < n; i += 32)
+            count += tile_overlaps(te, tb, tx0 + i % ntx, ty0 + i / ntx) ? 1u : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            count += __shfl_xor_sync(0xffffffffu, count, o);
+        if (lane == 0)
+            *warpOuts[t] = count;
+    }
+}
+
+// Patch set-up, one warp per patch instance of the batch: shade the patch's
+// vertices, assemble and set up its triangles, then count the tiles each one
+// touches. kOuter selects the outer-curve patch (interior triangulation)
+// instead of the midpoint fan. Triangle slot order is primitive order (flush,
+// draw batch, instance, triangle-in-patch).
+template <bool kOuter>
+__device__ __forceinline__ void patch_setup(const BatchTables& B,
+                                            TriRecord* __restrict__ tris,
+                                            uint32_t* __restrict__ tileCounts)
+{
+    constexpr int kVerts = kOuter ? kOuterPatchVertexCount : kPatchVertexCount;
+    constexpr int kTris = kOuter ? kOuterPatchTriangleCount : kPatchTriangleCount;
+    constexpr int kSpan = kOuter ? kOuterPatchSegmentSpan : kPatchSegmentSpan;
+    constexpr int kList = kOuter ? 1 : 0;
+    constexpr int kTriPasses = (kTris + 31) / 32;
+    __shared__ VertexOut sv[4][kVerts];
+    __shared__ float4 sEdges[4][kTriPasses * 32][3];
+    __shared__ int4 sBox[4][kTriPasses * 32];
+    __shared__ uint32_t* sOut[4][kTriPasses * 32];
     __shared__ bool sok[4];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t gi = blockIdx.x * 4 + w;
-    if (gi >= B.totalInstances)
+    if (gi >= B.totalItems[kList])
         return; // whole warp exits together
-    const uint32_t seg = find_range(B.segInstanceBase, B.segmentCount, gi);
-    const PatchSegment S = B.segments[seg];
+    const uint32_t seg = find_range(B.segBase[kList], B.segCount[kList], gi);
+    const PatchSegment S = B.segments[kList][seg];
     const FlushParams& P = B.scenes[S.scene];
-    const uint32_t local = gi - B.segInstanceBase[seg];
-    const uint32_t instance = S.baseInstance + local;
-    const uint32_t slotBase = S.slotBase, features = S.features;
+    const uint32_t local = gi - B.segBase[kList][seg];
+    const uint32_t instance = S.baseElement + local;
     if (lane == 0)
         sok[w] = true;
     __syncwarp();
-    for (int v = lane; v < kPatchVertexCount; v += 32)
+    for (int v = lane; v < kVerts; v += 32)
     {
         VertexOut o;
-        if (!shade_patch_vertex(P, v, instance, o))
+        const PatchVertexDesc pv = kOuter ? outer_vertex_desc(v) : patch_vertex_desc(v);
+        if (!shade_patch_vertex(P, pv, kSpan, instance, o))
         {
             sok[w] = false;
             o.discard = true;
@@ -475,152 +721,131 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
         sv[w][v] = o;
     }
     __syncwarp();
-    const uint32_t slot0 = slotBase + local * kPatchTriangleCount;
-    if (lane < kPatchTriangleCount)
+    const uint32_t slot0 = S.slotBase + local * kTris;
+    for (int pass = 0; pass < kTriPasses; ++pass)
     {
-        int ia, ib, ic;
-        patch_triangle(lane, ia, ib, ic);
-        const VertexOut& A = sv[w][ia];
-        const VertexOut& B = sv[w][ib];
-        const VertexOut& C = sv[w][ic];
+        const int t = pass * 32 + lane;
+        const bool has = t < kTris;
         int4 bb = make_int4(0, 0, 0, 0);
-        bool valid = sok[w] && !A.discard && !B.discard && !C.discard;
-        // Snap to the rasteriser's 1/256-pixel grid in integers.
-        int X0 = 0, Y0 = 0, X1 = 0, Y1 = 0, X2 = 0, Y2 = 0;
-        if (valid)
+        float4 e[3];
+        if (has)
         {
-            float m = fmaxf(fmaxf(fmaxf(fabsf(A.pos.x), fabsf(A.pos.y)),
-                                  fmaxf(fabsf(B.pos.x), fabsf(B.pos.y))),
-                            fmaxf(fabsf(C.pos.x), fabsf(C.pos.y)));
-            if (!(m < 32768.f)) // NaN or outside the exact snapping range
-            {
-                if (!isnan(m))
-                    atomicOr(P.error, ERR_COORD_RANGE);
-                valid = false;
-            }
+            int ia, ib, ic;
+            if (kOuter)
+                outer_triangle(t, ia, ib, ic);
             else
-            {
-                X0 = __float2int_rn(A.pos.x * 256.f);
-                Y0 = __float2int_rn(A.pos.y * 256.f);
-                X1 = __float2int_rn(B.pos.x * 256.f);
-                Y1 = __float2int_rn(B.pos.y * 256.f);
-                X2 = __float2int_rn(C.pos.x * 256.f);
-                Y2 = __float2int_rn(C.pos.y * 256.f);
-            }
-        }
-        long long area2 = 0;
-        if (valid)
-        {
-            // Exact twice-area in 1/65536 px^2: counterclockwise culled,
-            // degenerate dropped.
-            area2 = (long long)(X1 - X0) * (Y2 - Y0) - (long long)(X2 - X0) * (Y1 - Y0);
-            valid = area2 > 0;
-        }
-        if (valid)
-        {
-            const int mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
-            const int mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
-            // Pixels k whose centres (256 k + 128) lie in [min, max].
-            int bx0 = max(-((-(mnx - 128)) >> 8), 0);
-            int bx1 = min(((mxx - 128) >> 8) + 1, (int)P.width);
-            int by0 = max(-((-(mny - 128)) >> 8), 0);
-            int by1 = min(((mxy - 128) >> 8) + 1, (int)P.height);
-            if (bx0 >= bx1 || by0 >= by1)
-                valid = false;
-            else
-                bb = make_int4(bx0, by0, bx1, by1);
-        }
-        if (valid)
-        {
-            const float s = 1.f / 256.f;
-            const float2 p0 = make_float2(X0 * s, Y0 * s), p1 = make_float2(X1 * s, Y1 * s);
-            const float2 p2 = make_float2(X2 * s, Y2 * s);
+                patch_triangle(t, ia, ib, ic);
             TriRecord T;
-            T.e0 = make_edge(p0, p1);
-            T.e1 = make_edge(p1, p2);
-            T.e2 = make_edge(p2, p0);
-            const float d1x = p1.x - p0.x, d1y = p1.y - p0.y;
-            const float d2x = p2.x - p0.x, d2y = p2.y - p0.y;
-            const float inv = 1.f / ((float)area2 * (s * s));
-            const float ax = T.e0.x - p0.x, ay = T.e0.y - p0.y;
-            const float cxgx = ((B.cov.x - A.cov.x) * d2y - (C.cov.x - A.cov.x) * d1y) * inv;
-            const float cxgy = ((C.cov.x - A.cov.x) * d1x - (B.cov.x - A.cov.x) * d2x) * inv;
-            const float cygx = ((B.cov.y - A.cov.y) * d2y - (C.cov.y - A.cov.y) * d1y) * inv;
-            const float cygy = ((C.cov.y - A.cov.y) * d1x - (B.cov.y - A.cov.y) * d2x) * inv;
-            const uint2 paint = P.paints[P.firstPaint + A.pathID];
-            T.cov0 = make_float4(A.cov.x + cxgx * ax + cxgy * ay, cxgx, cxgy,
-                                 A.cov.y + cygx * ax + cygy * ay);
-            T.cov1 = make_float4(cygx, cygy, __uint_as_float(paint.x), __uint_as_float(paint.y));
-            // The fp16 coverage key of the path (draw_raster_order_path.frag:
-            // pathID bits, sign bit flipped for even-odd fills).
-            uint32_t key = A.pathID == 0 ? 0u
-                                         : ((A.pathID + MAX_DENORM_F16) * P.pathIDGranularity) & 0xffffu;
-            if (paint.x & PAINT_FLAG_EVEN_ODD_FILL)
-                key ^= 0x8000u;
-            T.meta = make_uint4((A.pathID & 0xffffu) | (features << 16),
-                                (uint32_t)bb.x | ((uint32_t)bb.z << 16),
-                                (uint32_t)bb.y | ((uint32_t)bb.w << 16), key | (S.scene << 16));
-            tris[slot0 + lane] = T;
+            if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic], S.features, S.scene,
+                                         T, bb))
+            {
+                tris[slot0 + t] = T;
+                e[0] = T.e0;
+                e[1] = T.e1;
+                e[2] = T.e2;
+                sEdges[w][t][0] = T.e0;
+                sEdges[w][t][1] = T.e1;
+                sEdges[w][t][2] = T.e2;
+            }
+            sBox[w][t] = bb;
+            sOut[w][t] = tileCounts + slot0 + t;
+        }
+        __syncwarp();
+        count_tiles(has, e, bb, tileCounts + slot0 + t, sEdges[w] + pass * 32,
+                    sBox[w] + pass * 32, sOut[w] + pass * 32);
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
+                                                          TriRecord* __restrict__ tris,
+                                                          uint32_t* __restrict__ tileCounts)
+{
+    patch_setup<false>(B, tris, tileCounts);
+}
+
+__global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
+                                                          TriRecord* __restrict__ tris,
+                                                          uint32_t* __restrict__ tileCounts)
+{
+    patch_setup<true>(B, tris, tileCounts);
+}
+
+// Interior triangulation (DrawType::interiorTriangulation): one thread per
+// triangle of the batch's TriangleVertex records. A vertex is the path-space
+// point mapped by the path's matrix, and its coverage is the triangle's
+// winding weight (unpack_interior_triangle_vertex,
+// draw_path_common.glsl:792-819); the raster adds it like a fill's constant
+// coverage.
+__global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
+                                                             TriRecord* __restrict__ tris,
+                                                             uint32_t* __restrict__ tileCounts)
+{
+    __shared__ float4 sEdges[8][32][3];
+    __shared__ int4 sBox[8][32];
+    __shared__ uint32_t* sOut[8][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t first = (blockIdx.x * blockDim.x) & ~31u;
+    if (first >= B.totalItems[2])
+        return; // whole warp exits together
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool has = gi < B.totalItems[2];
+    int4 bb = make_int4(0, 0, 0, 0);
+    float4 e[3];
+    uint32_t slot = 0;
+    if (has)
+    {
+        const uint32_t seg = find_range(B.segBase[2], B.segCount[2], gi);
+        const PatchSegment S = B.segments[2][seg];
+        const FlushParams& P = B.scenes[S.scene];
+        const uint32_t local = gi - B.segBase[2][seg];
+        slot = S.slotBase + local;
+        VertexOut v[3];
+        bool ok = true;
+        for (int k = 0; k < 3; ++k)
+        {
+            const uint32_t vi = S.baseElement + 3 * local + k;
+            if (vi >= P.triangleVertexCount)
+            {
+                atomicOr(P.error, ERR_BAD_TESS_INDEX);
+                ok = false;
+                break;
+            }
+            const uint32_t* r = P.triangleVertices + 3 * (size_t)vi;
+            const uint32_t pathID = r[2] & 0xffffu;
+            if (pathID >= P.pathCount)
+            {
+                atomicOr(P.error, ERR_BAD_PATH);
+                ok = false;
+                break;
+            }
+            const uint4* path = P.paths + 4 * (size_t)(P.firstPath + pathID);
+            const uint4 r0 = path[0], r1 = path[1];
+            const float4 M = make_float4(__uint_as_float(r0.x), __uint_as_float(r0.y),
+                                         __uint_as_float(r0.z), __uint_as_float(r0.w));
+            const float2 p = mat_mul(M, make_float2(__uint_as_float(r[0]), __uint_as_float(r[1])));
+            v[k].pos = make_float2(__fadd_rn(p.x, __uint_as_float(r1.x)),
+                                   __fadd_rn(p.y, __uint_as_float(r1.y)));
+            v[k].cov = make_float2((float)((int32_t)r[2] >> 16), -1.f);
+            v[k].pathID = pathID;
+            v[k].discard = false;
+        }
+        TriRecord T;
+        if (ok && setup_triangle(P, v[0], v[1], v[2], S.features, S.scene, T, bb))
+        {
+            tris[slot] = T;
+            e[0] = T.e0;
+            e[1] = T.e1;
+            e[2] = T.e2;
             sEdges[w][lane][0] = T.e0;
             sEdges[w][lane][1] = T.e1;
             sEdges[w][lane][2] = T.e2;
         }
         sBox[w][lane] = bb;
+        sOut[w][lane] = tileCounts + slot;
     }
     __syncwarp();
-    // Tile counts. A triangle whose box spans few tiles is counted by its own
-    // lane; larger ones are walked by the whole warp, one after another.
-    constexpr int kLaneTiles = 8;
-    uint32_t bigMask = 0;
-    if (lane < kPatchTriangleCount)
-    {
-        const int4 bb = sBox[w][lane];
-        uint32_t count = 0;
-        if (bb.z > bb.x)
-        {
-            const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
-            const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
-            const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
-            if (ntx * nty <= kLaneTiles)
-            {
-                const float4 e[3] = {sEdges[w][lane][0], sEdges[w][lane][1], sEdges[w][lane][2]};
-                for (int ty = ty0; ty < ty0 + nty; ++ty)
-                    for (int tx = tx0; tx < tx0 + ntx; ++tx)
-                        count += tile_overlaps(e, bb, tx, ty) ? 1u : 0u;
-                tileCounts[slot0 + lane] = count;
-            }
-            else
-            {
-                bigMask = 1u;
-            }
-        }
-        else
-        {
-            tileCounts[slot0 + lane] = 0;
-        }
-    }
-    uint32_t big = __ballot_sync(0xffffffffu, bigMask != 0);
-    while (big)
-    {
-        const int t = __ffs(big) - 1;
-        big &= big - 1;
-        const int4 bb = sBox[w][t];
-        const float4 e[3] = {sEdges[w][t][0], sEdges[w][t][1], sEdges[w][t][2]};
-        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
-        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
-        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
-        const int n = ntx * nty;
-        uint32_t count = 0;
-        for (int i = lane; i < n; i += 32)
-            count += tile_overlaps(e, bb, tx0 + i % ntx, ty0 + i / ntx) ? 1u : 0u;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            count += __shfl_xor_sync(0xffffffffu, count, o);
-        if (lane == 0)
-        {
-            tileCounts[slot0 + t] = count;
-        }
-    }
+    count_tiles(has, e, bb, tileCounts + slot, sEdges[w], sBox[w], sOut[w]);
 }
 
 // FlushUniforms fields the passes use (gpu.hpp:1466-1537: pathIDGranularity

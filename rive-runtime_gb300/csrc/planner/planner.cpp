@@ -2402,6 +2402,8 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
         throw PlanError("bad scene magic");
     if (hdr.width == 0 || hdr.height == 0 || hdr.width > 16384 || hdr.height > 16384)
         throw PlanError("bad canvas size");
+    if (hdr.flags & RIVE_SCENE_FLAG_TRIANGULATE)
+        throw PlanError("interior triangulation is not planned here (midpoint fans only)");
     size_t off = sizeof(hdr);
     auto need = [&](size_t n) {
         if (off + n > size)

@@ -19,6 +19,14 @@ constexpr int kPatchSegmentSpan = 8;   // kMidpointFanPatchSegmentSpan
 constexpr int kPatchVertexCount = 42;  // kMidpointFanPatchVertexCount
 constexpr int kPatchIndexCount = 72;   // kMidpointFanPatchIndexCount
 constexpr int kPatchTriangleCount = 24;
+// Outer-curve patches (interior triangulation; gpu.hpp:591-646).
+constexpr int kOuterPatchSegmentSpan = 17;   // OuterCubicPatchSegmentSpanPlusJoin
+constexpr int kOuterPatchVertexCount = 153;  // kOuterCurvePatchVertexCount
+constexpr int kOuterPatchTriangleCount = 83; // kOuterCurvePatchIndexCount / 3
+// gpu::DrawType values (gpu.hpp:657-668).
+constexpr uint32_t DRAW_MIDPOINT_FAN_PATCHES = 0u;
+constexpr uint32_t DRAW_OUTER_CURVE_PATCHES = 2u;
+constexpr uint32_t DRAW_INTERIOR_TRIANGULATION = 3u;
 
 constexpr float kPi = 3.14159265359f;
 constexpr float k2Pi = 6.28318530718f;
@@ -128,17 +136,24 @@ struct FlushParams
     uint32_t* error;
     uint32_t* fb;   // render target, RGBA8, width x height
     uint32_t tilesX;
+    const uint32_t* triangleVertices; // TriangleVertex records (3 words each)
+    uint32_t triangleVertexCount;
     // This flush's FlushUniforms record (device); scene_uniforms_kernel copies
     // pathIDGranularity and the dither terms from it before any other pass.
     const uint8_t* uniforms;
 };
 
-// A run of patch instances of one flush drawn with one set of shader
-// features (one DrawBatch), and where its triangle slots start.
+// One DrawBatch of one flush in a set-up work list: its first element (patch
+// instance, or triangle vertex for interior triangulation), its shader
+// features and where its triangle slots start.
 struct PatchSegment
 {
-    uint32_t scene, baseInstance, features, slotBase;
+    uint32_t scene, baseElement, features, slotBase;
 };
+
+// Set-up work lists: midpoint-fan patches, outer-curve patches, interior
+// triangles (items: instances, instances, triangles).
+constexpr int kSetupLists = 3;
 
 // The work of a batch of independent logical flushes ("scenes"); a single
 // flush is a batch of one. Every kernel maps its global work index to a scene
@@ -150,10 +165,14 @@ struct BatchTables
     const uint32_t* tessSpanBase;    // [sceneCount + 1]
     const uint32_t* tileBase;        // [sceneCount + 1]
     const uint2* sceneTiles;         // [sceneCount]: (tileBase, tilesX)
-    const PatchSegment* segments;    // [segmentCount]
-    const uint32_t* segInstanceBase; // [segmentCount + 1]
-    uint32_t sceneCount, segmentCount;
-    uint32_t totalGradSpans, totalTessSpans, totalInstances, totalTiles;
+    // Per set-up list: segments [segCount] and the prefix of their items
+    // [segCount + 1].
+    const PatchSegment* segments[kSetupLists];
+    const uint32_t* segBase[kSetupLists];
+    uint32_t segCount[kSetupLists];
+    uint32_t totalItems[kSetupLists];
+    uint32_t sceneCount;
+    uint32_t totalGradSpans, totalTessSpans, totalTiles;
 };
 
 // Index j with base[j] <= i < base[j + 1] (empty ranges skipped), n >= 1.

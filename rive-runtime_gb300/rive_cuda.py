@@ -42,9 +42,10 @@ class FlushDesc(ctypes.Structure):
 
 
 class DeviceBuffers(ctypes.Structure):
+    # rive_cuda_device_buffers; the last field is triangle_vertices.
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "flush_uniforms", "paths", "paints", "paint_aux", "contours",
-        "grad_spans", "tess_spans")]
+        "grad_spans", "tess_spans", "triangles")]
 
 
 class BatchFlush(ctypes.Structure):

@@ -50,6 +50,7 @@ BLEND_MODES = [3, 14, 15, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28]
 LOCAL_HALF_EXTENT = 48.0
 
 DITHER_NONE, DITHER_IGN = 0, 1
+FLAG_TRIANGULATE = 1
 
 
 @dataclass
@@ -78,6 +79,7 @@ class Scene:
     height: int
     clear_color: int = 0xFFFFFFFF
     dither_mode: int = DITHER_IGN
+    flags: int = 0  # FLAG_TRIANGULATE: let the front end triangulate large fills
     paths: list = field(default_factory=list)
     paints: list = field(default_factory=list)
     cmds: list = field(default_factory=list)  # (op, a, b, m6)
@@ -117,7 +119,7 @@ class Scene:
         header = struct.pack("<12I", MAGIC, self.width, self.height,
                              self.clear_color & 0xFFFFFFFF, len(self.paths),
                              len(self.paints), len(self.cmds), len(verbs), npts,
-                             len(stops), self.dither_mode, 0)
+                             len(stops), self.dither_mode, self.flags)
         vpad = bytes((4 - len(verbs) % 4) % 4)
         pts_bytes = (np.concatenate(pts).astype("<f4").tobytes()
                      if pts else b"")

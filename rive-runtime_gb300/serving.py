@@ -148,6 +148,8 @@ class RecordArenas:
                 offs[i][name] = (total, n)
                 total += (n + ALIGN - 1) // ALIGN * ALIGN
             if total == 0:
+                for i in range(len(caps)):
+                    offs[i][name] = None
                 continue
             h = self._ensure(self.host[slot], name, total, True)
             d = self._ensure(self.dev[slot], name, total, False)

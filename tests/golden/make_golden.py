@@ -42,11 +42,27 @@ SCENES = {
     "clips_s13": lambda: scene.full_feature(seed=13, width=192, height=192, n_paths=30,
                                             max_cubics=6, p_clip=1.0, p_gradient=0.3,
                                             p_blend=0.2, scale_range=(0.75, 1.5)),
+    # Interior triangulation (the front end's default for large fills): outer
+    # curve patches plus interior triangles, on canvas-wide plain fills.
+    "tri_fills_s21": lambda: _triangulated(scene.plain_canvas(
+        __import__("numpy").random.default_rng(21), 640, 480, 10)),
+    # ... and on scaled-up full-feature paths (even-odd, gradients, blend
+    # modes, triangulated clip paths).
+    "tri_full_s23": lambda: _triangulated(scene.full_feature(
+        seed=23, width=512, height=512, n_paths=24, max_cubics=10, p_fill=0.8, p_clip=0.3,
+        p_blend=0.3, scale_range=(6.0, 9.0))),
 }
 
 
-def main():
+def _triangulated(sc):
+    sc.flags = scene.FLAG_TRIANGULATE
+    return sc
+
+
+def main(only=None):
     for name, make in SCENES.items():
+        if only and name not in only:
+            continue
         sc = make()
         sb = sc.to_bytes()
         cb = oracle.reference_capture(sb)
@@ -58,4 +74,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

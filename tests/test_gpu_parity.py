@@ -88,7 +88,7 @@ def test_flush_rejects_unsupported_draw_type_and_stays_usable(ctx):
     cap, _ = load_golden("plain_small_s1")
     f = cap.flushes[0]
     bad = type(f)(dict(f.desc), f.batches.copy())
-    bad.batches[:, 0] = 2  # gpu::DrawType::outerCurvePatches
+    bad.batches[:, 0] = 5  # gpu::DrawType::imageRect
     t = ctx.render_target(cap.width, cap.height)
     ctx.upload_frame(cap)
     with pytest.raises(rive_cuda.RiveCudaError, match="draw type"):
