@@ -29,9 +29,18 @@ namespace rivecuda
 {
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
-__global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
-__global__ void outer_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
-__global__ void interior_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void patch_setup_kernel(BatchTables B,
+                                   TriRecord* tris,
+                                   uint32_t* tileCounts,
+                                   uint8_t* tileMasks);
+__global__ void outer_setup_kernel(BatchTables B,
+                                   TriRecord* tris,
+                                   uint32_t* tileCounts,
+                                   uint8_t* tileMasks);
+__global__ void interior_setup_kernel(BatchTables B,
+                                      TriRecord* tris,
+                                      uint32_t* tileCounts,
+                                      uint8_t* tileMasks);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_fill_kernel(const uint32_t* pairTotal,
                                 uint32_t capacity,
@@ -41,6 +50,7 @@ __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
+                                   const uint8_t* tileMasks,
                                    const uint32_t* offsets,
                                    uint32_t capacity,
                                    uint32_t* error,
@@ -144,7 +154,7 @@ struct rive_cuda_context
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
     uint32_t tessWidth = 0, tessHeight = 0, gradWidth = 0, gradHeight = 0;
-    DeviceBuffer tris, tileCounts, offsets;
+    DeviceBuffer tris, tileCounts, tileMasks, offsets;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
     DeviceBuffer dTables;  // batch tables (device)
     HostBuffer hTables;    // pinned staging of the tables
@@ -168,8 +178,8 @@ struct rive_cuda_context
 struct rive_cuda_graph
 {
     rive_cuda_context* ctx = nullptr;
-    DeviceBuffer tables, tess, grad, tris, counts, offsets, keys, vals, keysAlt, valsAlt, scanTemp,
-        sortTemp, ranges, error;
+    DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
+        scanTemp, sortTemp, ranges, error;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -482,6 +492,7 @@ struct Scratch
     uchar4* grad = nullptr;
     TriRecord* tris = nullptr;
     uint32_t* counts = nullptr;
+    uint8_t* masks = nullptr;    // per slot: tiles overlapped, for boxes of <= 8 tiles
     uint32_t* offsets = nullptr; // slots + 1 entries
     uint32_t *keys = nullptr, *vals = nullptr, *keysAlt = nullptr, *valsAlt = nullptr;
     void* scanTemp = nullptr;
@@ -636,11 +647,14 @@ int enqueue_front(rive_cuda_context* ctx,
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
         if (L.items[0])
-            patch_setup_kernel<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
+            patch_setup_kernel<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
+                                                                         S.masks);
         if (L.items[1])
-            outer_setup_kernel<<<(L.items[1] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts);
+            outer_setup_kernel<<<(L.items[1] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
+                                                                         S.masks);
         if (L.items[2])
-            interior_setup_kernel<<<(L.items[2] + 255) / 256, 256, 0, stream>>>(B, S.tris, S.counts);
+            interior_setup_kernel<<<(L.items[2] + 255) / 256, 256, 0, stream>>>(B, S.tris, S.counts,
+                                                                                S.masks);
         stage_end(ctx, stream);
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
         size_t tempBytes = S.scanTempBytes;
@@ -671,7 +685,8 @@ int enqueue_back(rive_cuda_context* ctx,
             bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots, entries,
                                                                       L.tiles, S.keys);
         bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
-            L.slots, B.sceneTiles, S.tris, S.counts, S.offsets, entries, S.error, S.keys, S.vals);
+            L.slots, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries, S.error, S.keys,
+            S.vals);
         stage_end(ctx, stream);
         cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
         cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
@@ -728,6 +743,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(ctx->tris.reserve((size_t)std::max(L.slots, 1u) * sizeof(TriRecord)));
     CK(ctx->tileCounts.reserve((size_t)std::max(L.slots, 1u) * 4));
+    CK(ctx->tileMasks.reserve((size_t)std::max(L.slots, 1u)));
     CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
     const size_t scanBytes = scan_temp_bytes(L.slots);
     CK(ctx->scanTemp.reserve(scanBytes));
@@ -740,6 +756,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.grad = (uchar4*)ctx->grad.ptr;
     S.tris = (TriRecord*)ctx->tris.ptr;
     S.counts = (uint32_t*)ctx->tileCounts.ptr;
+    S.masks = (uint8_t*)ctx->tileMasks.ptr;
     S.offsets = (uint32_t*)ctx->offsets.ptr;
     S.scanTemp = ctx->scanTemp.ptr;
     S.scanTempBytes = scanBytes;
@@ -849,7 +866,8 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         }
         r.device.release();
     }
-    for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->offsets,
+    for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->tileMasks,
+                            &ctx->offsets,
                             &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
                             &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables})
         b->release();
@@ -1100,7 +1118,7 @@ void graph_free(rive_cuda_graph* g)
         cudaGraphExecDestroy(g->exec);
     if (g->graph)
         cudaGraphDestroy(g->graph);
-    for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->offsets,
+    for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->masks, &g->offsets,
                             &g->keys, &g->vals, &g->keysAlt, &g->valsAlt, &g->scanTemp,
                             &g->sortTemp, &g->ranges, &g->error})
         b->release();
@@ -1128,6 +1146,7 @@ int graph_build(rive_cuda_context* ctx,
     CK(g->grad.reserve(L.gradBytes()));
     CK(g->tris.reserve((size_t)std::max(L.slots, 1u) * sizeof(TriRecord)));
     CK(g->counts.reserve((size_t)std::max(L.slots, 1u) * 4));
+    CK(g->masks.reserve((size_t)std::max(L.slots, 1u)));
     CK(g->offsets.reserve((size_t)L.slots * 4 + 4));
     CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(g->error.reserve(4));
@@ -1141,6 +1160,7 @@ int graph_build(rive_cuda_context* ctx,
     S.grad = (uchar4*)g->grad.ptr;
     S.tris = (TriRecord*)g->tris.ptr;
     S.counts = (uint32_t*)g->counts.ptr;
+    S.masks = (uint8_t*)g->masks.ptr;
     S.offsets = (uint32_t*)g->offsets.ptr;
     S.scanTemp = g->scanTemp.ptr;
     S.scanTempBytes = scanBytes;

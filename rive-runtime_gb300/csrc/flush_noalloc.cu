@@ -22,13 +22,20 @@ namespace rivecuda
 {
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
-__global__ void patch_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
-__global__ void outer_setup_kernel(BatchTables B, TriRecord* tris, uint32_t* tileCounts);
+__global__ void patch_setup_kernel(BatchTables B,
+                                   TriRecord* tris,
+                                   uint32_t* tileCounts,
+                                   uint8_t* tileMasks);
+__global__ void outer_setup_kernel(BatchTables B,
+                                   TriRecord* tris,
+                                   uint32_t* tileCounts,
+                                   uint8_t* tileMasks);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
+                                   const uint8_t* tileMasks,
                                    const uint32_t* offsets,
                                    uint32_t capacity,
                                    uint32_t* error,
@@ -62,7 +69,8 @@ constexpr size_t kGradBytes = (size_t)kGradTextureWidth * RIVE_CUDA_NOALLOC_MAX_
 constexpr size_t kTrisOff = kGradOff + align256(kGradBytes);
 constexpr size_t kTrisBytes = kMaxSlots * sizeof(TriRecord);
 constexpr size_t kCountsOff = kTrisOff + align256(kTrisBytes);
-constexpr size_t kOffsetsOff = kCountsOff + align256(kMaxSlots * 4);
+constexpr size_t kMasksOff = kCountsOff + align256(kMaxSlots * 4);
+constexpr size_t kOffsetsOff = kMasksOff + align256(kMaxSlots);
 constexpr size_t kKeysOff = kOffsetsOff + align256(kMaxSlots * 4 + 4);
 constexpr size_t kPairBytes = (size_t)RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES * 4;
 constexpr size_t kValsOff = kKeysOff + align256(kPairBytes);
@@ -310,13 +318,14 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         tessellate_kernel<<<(d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(B);
 
     TriRecord* tris = (TriRecord*)(pool + kTrisOff);
+    uint8_t* masks = (uint8_t*)(pool + kMasksOff);
     uint32_t* counts = (uint32_t*)(pool + kCountsOff);
     uint32_t* offs = (uint32_t*)(pool + kOffsetsOff);
     const uint32_t slots = (uint32_t)(instances * kPatchTriangleCount);
     uint32_t pairs = 0;
     if (slots)
     {
-        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, tris, counts);
+        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, tris, counts, masks);
         size_t tempBytes = 0;
         CKN(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
         if (tempBytes > kScanTempBytes)
@@ -340,7 +349,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (pairs)
     {
         bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
-            slots, B.sceneTiles, tris, counts, offs, pairs, dError, keys, vals);
+            slots, B.sceneTiles, tris, counts, masks, offs, pairs, dError, keys, vals);
         int endBit = 1;
         while ((1u << endBit) <= tiles)
             ++endBit;

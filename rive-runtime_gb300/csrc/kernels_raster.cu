@@ -626,6 +626,7 @@ __device__ __forceinline__ void count_tiles(bool has,
                                             const float4* e,
                                             int4 bb,
                                             uint32_t* __restrict__ countOut,
+                                            uint8_t* __restrict__ maskOut,
                                             const float4 (*warpEdges)[3],
                                             const int4* warpBoxes,
                                             uint32_t* const* warpOuts)
@@ -640,11 +641,19 @@ __device__ __forceinline__ void count_tiles(bool has,
             tile_span(bb, tx0, ty0, ntx, nty);
             if (ntx * nty <= kLaneTiles)
             {
-                uint32_t count = 0;
+                // The tiles it overlaps, as bits in row-major order over its
+                // tile box, so the binner need not test them again.
+                uint32_t count = 0, mask = 0;
+                int i = 0;
                 for (int ty = ty0; ty < ty0 + nty; ++ty)
-                    for (int tx = tx0; tx < tx0 + ntx; ++tx)
-                        count += tile_overlaps(e, bb, tx, ty) ? 1u : 0u;
+                    for (int tx = tx0; tx < tx0 + ntx; ++tx, ++i)
+                        if (tile_overlaps(e, bb, tx, ty))
+                        {
+                            ++count;
+                            mask |= 1u << i;
+                        }
                 *countOut = count;
+                *maskOut = (uint8_t)mask;
             }
             else
             {
@@ -685,7 +694,8 @@ __device__ __forceinline__ void count_tiles(bool has,
 template <bool kOuter>
 __device__ __forceinline__ void patch_setup(const BatchTables& B,
                                             TriRecord* __restrict__ tris,
-                                            uint32_t* __restrict__ tileCounts)
+                                            uint32_t* __restrict__ tileCounts,
+                                            uint8_t* __restrict__ tileMasks)
 {
     constexpr int kVerts = kOuter ? kOuterPatchVertexCount : kPatchVertexCount;
     constexpr int kTris = kOuter ? kOuterPatchTriangleCount : kPatchTriangleCount;
@@ -751,7 +761,7 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             sOut[w][t] = tileCounts + slot0 + t;
         }
         __syncwarp();
-        count_tiles(has, e, bb, tileCounts + slot0 + t, sEdges[w] + pass * 32,
+        count_tiles(has, e, bb, tileCounts + slot0 + t, tileMasks + slot0 + t, sEdges[w] + pass * 32,
                     sBox[w] + pass * 32, sOut[w] + pass * 32);
         __syncwarp();
     }
@@ -759,16 +769,18 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
 
 __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
                                                           TriRecord* __restrict__ tris,
-                                                          uint32_t* __restrict__ tileCounts)
+                                                          uint32_t* __restrict__ tileCounts,
+                                                          uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<false>(B, tris, tileCounts);
+    patch_setup<false>(B, tris, tileCounts, tileMasks);
 }
 
 __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
                                                           TriRecord* __restrict__ tris,
-                                                          uint32_t* __restrict__ tileCounts)
+                                                          uint32_t* __restrict__ tileCounts,
+                                                          uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<true>(B, tris, tileCounts);
+    patch_setup<true>(B, tris, tileCounts, tileMasks);
 }
 
 // Interior triangulation (DrawType::interiorTriangulation): one thread per
@@ -779,7 +791,8 @@ __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
 // coverage.
 __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
                                                              TriRecord* __restrict__ tris,
-                                                             uint32_t* __restrict__ tileCounts)
+                                                             uint32_t* __restrict__ tileCounts,
+                                                             uint8_t* __restrict__ tileMasks)
 {
     __shared__ float4 sEdges[8][32][3];
     __shared__ int4 sBox[8][32];
@@ -845,7 +858,7 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
         sOut[w][lane] = tileCounts + slot;
     }
     __syncwarp();
-    count_tiles(has, e, bb, tileCounts + slot, sEdges[w], sBox[w], sOut[w]);
+    count_tiles(has, e, bb, tileCounts + slot, tileMasks + slot, sEdges[w], sBox[w], sOut[w]);
 }
 
 // FlushUniforms fields the passes use (gpu.hpp:1466-1537: pathIDGranularity
@@ -885,6 +898,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
                                                           const uint2* __restrict__ sceneTiles,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ tileCounts,
+                                                          const uint8_t* __restrict__ tileMasks,
                                                           const uint32_t* __restrict__ offsets,
                                                           uint32_t capacity,
                                                           uint32_t* __restrict__ error,
@@ -908,25 +922,26 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
         if (ntx * nty <= kLaneTiles)
         {
-            const TriRecord* T = tris + mySlot;
-            const float4 e[3] = {T->e0, T->e1, T->e2};
-            const uint2 st = sceneTiles[T->meta.w >> 16]; // (tileBase, tilesX)
+            // The set-up already tested these tiles: walk its mask.
+            const uint2 st = sceneTiles[tris[mySlot].meta.w >> 16]; // (tileBase, tilesX)
+            uint32_t mask = tileMasks[mySlot];
             uint32_t o = offsets[mySlot];
-            for (int ty = ty0; ty < ty0 + nty; ++ty)
-                for (int tx = tx0; tx < tx0 + ntx; ++tx)
-                    if (tile_overlaps(e, bb, tx, ty))
-                    {
-                        if (o < capacity)
-                        {
-                            keys[o] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
-                            vals[o] = mySlot;
-                        }
-                        else
-                        {
-                            atomicOr(error, ERR_BIN_OVERFLOW);
-                        }
-                        ++o;
-                    }
+            while (mask)
+            {
+                const int i = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int tx = tx0 + i % ntx, ty = ty0 + i / ntx;
+                if (o < capacity)
+                {
+                    keys[o] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
+                    vals[o] = mySlot;
+                }
+                else
+                {
+                    atomicOr(error, ERR_BIN_OVERFLOW);
+                }
+                ++o;
+            }
         }
         else
         {
