@@ -239,6 +239,9 @@ def run_ours(args, cap, wname, rank, world):
 
     for _ in range(args.warmup):
         frame_device()
+    # Raster configuration: the autotuner times its candidates on this frame
+    # (untimed) and leaves the fastest set, or a fixed "T,C" is used.
+    raster = raster_setup(args, ctx, lambda s: frame_device(), stream)
     # One more untimed frame, flush by flush, for the per-frame bin entries
     # (the pair count is known on the host when a flush call returns).
     frame_entries = 0
@@ -322,7 +325,7 @@ def run_ours(args, cap, wname, rank, world):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": workload_config(cap, wname),
+        "config": dict(workload_config(cap, wname), raster=raster),
         "gpx_per_s": fps * W * H / 1e9,
         "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
                 "d2h_bytes_per_step": W * H * 4},
@@ -337,9 +340,9 @@ def run_ours(args, cap, wname, rank, world):
     del keep, target
     # The batched and serving measurements are single-GPU (rank 0 of N=1).
     if args.batch_scenes > 0 and world == 1:
-        line["batched"] = run_batched(args, dev)
+        line["batched"] = run_batched(args, dev, raster)
     if args.serve_sessions > 0 and world == 1:
-        line["serving"] = run_serving(args, dev)
+        line["serving"] = run_serving(args, dev, raster)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -350,7 +353,7 @@ def run_ours(args, cap, wname, rank, world):
         print(json.dumps(line))
 
 
-def run_serving(args, dev):
+def run_serving(args, dev, raster=None):
     """The serving loop (rive-runtime_gb300/serving.py): sessions with the
     full-feature distributions on a smaller canvas, Poisson arrivals at 50/s,
     each animated for a fixed number of frames at a fixed frame rate."""
@@ -361,6 +364,8 @@ def run_serving(args, dev):
     sessions = serving.poisson_sessions(scs, 50.0, frames=args.serve_frames,
                                         fps=args.serve_fps, seed=7)
     ctx = rive_cuda.Context(dev)
+    if raster:
+        ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
     try:
         server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
@@ -376,7 +381,19 @@ def run_serving(args, dev):
             "hbm_budget_gb": 120, **st}
 
 
-def run_batched(args, dev):
+def raster_setup(args, ctx, run, stream):
+    """Applies --raster-config ("auto" or "tile,ctas_per_sm"); returns what was set."""
+    if args.raster_config == "auto":
+        from rive_runtime_gb300 import autotune
+        best, trials = autotune.autotune(ctx, run, stream=stream, warmup=1, iters=3)
+        return {"tile": best.tile_size, "ctas_per_sm": best.ctas_per_sm, "autotuned": True,
+                "trial_ms": {f"{t.tile_size},{t.ctas_per_sm}": round(t.ms, 3) for t in trials}}
+    t, c = (int(v) for v in args.raster_config.split(","))
+    ctx.set_raster_config(t, c)
+    return {"tile": t, "ctas_per_sm": c, "autotuned": False}
+
+
+def run_batched(args, dev, raster=None):
     """The batched form: N independent scenes of uneven canvas sizes and path
     counts (scene.batched_scenes), rendered (a) one flush at a time, (b) as
     one rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch
@@ -416,14 +433,20 @@ def run_batched(args, dev):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / steps
 
-    ctx = rive_cuda.Context(dev)
+    def configured():
+        c = rive_cuda.Context(dev)
+        if raster:
+            c.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+        return c
+
+    ctx = configured()
     ms_plain = timed(lambda: [ctx.flush_device(f, b, tp, stream.cuda_stream)
                               for w in waves for (f, b, tp) in w])
     ms_batch = timed(lambda: [ctx.flush_batch(w, stream.cuda_stream) for w in waves])
     ctx.sync(stream.cuda_stream)
     entries = ctx.stats()["bin_entries"]
     ctx.close()
-    ctx = rive_cuda.Context(dev)
+    ctx = configured()
     graphs = [ctx.graph(w) for w in waves]
     ms_graph = timed(lambda: [g.launch(stream.cuda_stream) for g in graphs])
     for g in graphs:
@@ -462,6 +485,8 @@ def main():
     ap.add_argument("--serve-paths", type=int, default=300)
     ap.add_argument("--serve-frames", type=int, default=60)
     ap.add_argument("--serve-fps", type=float, default=8.0)
+    ap.add_argument("--raster-config", default="auto",
+                    help='"auto" (autotuned on the workload) or "tile,ctas_per_sm", e.g. "16,0"')
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -351,6 +351,16 @@ int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
 int rive_cuda_graph_stats(const rive_cuda_graph* graph, rive_cuda_flush_stats* out);
 
 /*
+ * Raster configuration of the context's later flushes, batches and graphs
+ * (no counterpart in the reference): the tile size (8, 16 or 32 pixels; 16
+ * by default) and, for 8 and 16, a limit on resident raster CTAs per SM (0:
+ * as many as fit). The results are the same within the image tolerance for
+ * every choice; only the speed differs, so an autotuner may pick per workload.
+ */
+int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_per_sm);
+int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, int* ctas_per_sm);
+
+/*
  * Per-stage device timing with CUDA events recorded on the flush stream
  * (off by default; no counterpart in the reference, whose backends time
  * nothing). Stages of one flush, in launch order:

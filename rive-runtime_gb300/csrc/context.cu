@@ -47,6 +47,7 @@ __global__ void bin_fill_kernel(const uint32_t* pairTotal,
                                 uint32_t sentinel,
                                 uint32_t* keys);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
+                                   int tileLog2,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
@@ -64,6 +65,14 @@ __global__ void raster_tile_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
                                    const uint2* ranges);
+__global__ void raster_tile8_kernel(BatchTables B,
+                                    const TriRecord* tris,
+                                    const uint32_t* sortedSlots,
+                                    const uint2* ranges);
+__global__ void raster_tile32_kernel(BatchTables B,
+                                     const TriRecord* tris,
+                                     const uint32_t* sortedSlots,
+                                     const uint2* ranges);
 } // namespace rivecuda
 
 using namespace rivecuda;
@@ -163,6 +172,12 @@ struct rive_cuda_context
     uint32_t* hError = nullptr;  // pinned
     uint32_t* hPairs = nullptr;  // pinned: scanned pair total
     rive_cuda_flush_stats stats = {};
+    // Raster configuration (rive_cuda_set_raster_config).
+    int tileLog2 = kTileLog2;
+    int rasterCtasPerSm = 0; // 0: as many as fit
+    bool raster32Ready = false;
+    size_t rasterPad[2] = {};         // padding for the 8 and 16 pixel kernels
+    int rasterPadFor[2] = {-1, -1};   // the CTAs-per-SM limit it was found for
     // Stage timing (rive_cuda_set_profiling).
     bool profiling = false;
     std::vector<cudaEvent_t> eventPool;
@@ -385,6 +400,7 @@ size_t align16(size_t n) { return (n + 15) & ~(size_t)15; }
 struct BatchLayout
 {
     uint32_t n = 0;
+    int tileLog2 = kTileLog2;
     uint32_t segCount[kSetupLists] = {}, items[kSetupLists] = {};
     uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0;
     uint64_t tessRows = 0, gradRows = 0;
@@ -410,6 +426,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "a batch holds 1 to 65535 flushes");
     L = BatchLayout();
     L.n = n;
+    L.tileLog2 = ctx->tileLog2;
+    const uint32_t ts = 1u << L.tileLog2;
     L.tessRow0.resize(n);
     L.gradRow0.resize(n);
     uint64_t slots = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
@@ -440,8 +458,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         L.gradRow0[i] = L.gradRows;
         L.tessRows += std::max(d->tess_data_height, 1u);
         L.gradRows += std::max(d->grad_data_height, 1u);
-        tiles += (uint64_t)((d->render_target_width + kTileSize - 1) / kTileSize) *
-                 ((d->render_target_height + kTileSize - 1) / kTileSize);
+        tiles += (uint64_t)((d->render_target_width + ts - 1) / ts) *
+                 ((d->render_target_height + ts - 1) / ts);
         gradSpans += d->grad_span_count;
         tessSpans += d->tess_span_count;
     }
@@ -561,7 +579,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
         P.pathIDGranularity = 1; // replaced on the device by scene_uniforms_kernel
         P.error = S.error;
         P.fb = in[i].fb;
-        P.tilesX = (d->render_target_width + kTileSize - 1) / kTileSize;
+        const uint32_t ts = 1u << L.tileLog2;
+        P.tilesX = (d->render_target_width + ts - 1) / ts;
         P.tess = S.tess + (size_t)L.tessRow0[i] * kTessTextureWidth;
         P.grad = S.grad + (size_t)L.gradRow0[i] * kGradTextureWidth;
         P.triangleVertices = (const uint32_t*)rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE];
@@ -574,7 +593,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
         sceneTiles[i] = make_uint2(tileAcc, P.tilesX);
         gAcc += d->grad_span_count;
         tAcc += d->tess_span_count;
-        tileAcc += P.tilesX * ((d->render_target_height + kTileSize - 1) / kTileSize);
+        tileAcc += P.tilesX * ((d->render_target_height + ts - 1) / ts);
         // Slots follow the draw list order across all three set-up lists.
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
         {
@@ -611,6 +630,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
         B.totalItems[l] = itemAcc[l];
     }
     B.sceneCount = L.n;
+    B.tileLog2 = L.tileLog2;
     B.totalGradSpans = gAcc;
     B.totalTessSpans = tAcc;
     B.totalTiles = tileAcc;
@@ -666,6 +686,75 @@ int enqueue_front(rive_cuda_context* ctx,
     return RIVE_CUDA_OK;
 }
 
+// Dynamic shared memory (unused) that holds a raster kernel to at most
+// `ctas` resident CTAs per SM, found with the occupancy calculator.
+size_t occupancy_pad(const void* fn, int threads, int ctas)
+{
+    constexpr size_t kMaxPad = 160u << 10;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxPad) !=
+        cudaSuccess)
+        return 0;
+    for (size_t dyn = 0; dyn <= kMaxPad; dyn += 256)
+    {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, dyn) != cudaSuccess)
+            return 0;
+        if (occ <= ctas)
+            return dyn;
+    }
+    return 0;
+}
+
+// Sets the kernel attributes and finds the padding the context's raster
+// configuration needs. Called before any stream capture, never inside one.
+int prepare_raster(rive_cuda_context* ctx)
+{
+    if (ctx->tileLog2 == 5 && !ctx->raster32Ready)
+    {
+        CK(cudaFuncSetAttribute(raster_tile32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kRaster32SmemBytes));
+        ctx->raster32Ready = true;
+    }
+    const int slot = ctx->tileLog2 == 3 ? 0 : ctx->tileLog2 == 4 ? 1 : -1;
+    if (slot >= 0 && ctx->rasterCtasPerSm > 0 && ctx->rasterPadFor[slot] != ctx->rasterCtasPerSm)
+    {
+        const void* fn = slot == 0 ? (const void*)raster_tile8_kernel : (const void*)raster_tile_kernel;
+        ctx->rasterPad[slot] = occupancy_pad(fn, slot == 0 ? 64 : 256, ctx->rasterCtasPerSm);
+        cudaGetLastError(); // a failed query only leaves the launch unpadded
+        ctx->rasterPadFor[slot] = ctx->rasterCtasPerSm;
+    }
+    return RIVE_CUDA_OK;
+}
+
+// Launches the raster for the batch's tile size (prepare_raster has run). A
+// CTAs-per-SM limit is applied by asking each CTA for more (unused) dynamic
+// shared memory.
+int launch_raster(rive_cuda_context* ctx,
+                  const BatchLayout& L,
+                  const BatchTables& B,
+                  const TriRecord* tris,
+                  const uint32_t* sortedSlots,
+                  const uint2* ranges,
+                  cudaStream_t stream)
+{
+    if (L.tileLog2 == 3)
+    {
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[0] : 0;
+        raster_tile8_kernel<<<L.tiles, 64, dyn, stream>>>(B, tris, sortedSlots, ranges);
+    }
+    else if (L.tileLog2 == 5)
+    {
+        raster_tile32_kernel<<<L.tiles, 1024, kRaster32SmemBytes, stream>>>(B, tris, sortedSlots,
+                                                                          ranges);
+    }
+    else
+    {
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[1] : 0;
+        raster_tile_kernel<<<L.tiles, 256, dyn, stream>>>(B, tris, sortedSlots, ranges);
+    }
+    return RIVE_CUDA_OK;
+}
+
 // Enqueues binning, sort, ranges and raster over `entries` bin slots. With
 // `padded`, entries is a fixed capacity: the tail past the device's total is
 // filled with the sentinel key and overflow is flagged on the device.
@@ -685,8 +774,8 @@ int enqueue_back(rive_cuda_context* ctx,
             bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots, entries,
                                                                       L.tiles, S.keys);
         bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
-            L.slots, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries, S.error, S.keys,
-            S.vals);
+            L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries, S.error,
+            S.keys, S.vals);
         stage_end(ctx, stream);
         cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
         cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
@@ -700,8 +789,10 @@ int enqueue_back(rive_cuda_context* ctx,
         sortedSlots = v.Current();
     }
     stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
-    raster_tile_kernel<<<L.tiles, 256, 0, stream>>>(B, S.tris, sortedSlots, S.ranges);
+    int rc = launch_raster(ctx, L, B, S.tris, sortedSlots, S.ranges, stream);
     stage_end(ctx, stream);
+    if (rc)
+        return rc;
     CK(cudaGetLastError());
     return RIVE_CUDA_OK;
 }
@@ -731,6 +822,8 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         return RIVE_CUDA_OK;
     BatchLayout L;
     int rc = plan_batch(ctx, in, n, L);
+    if (!rc)
+        rc = prepare_raster(ctx);
     if (rc)
         return rc;
     // The previous batch's tables may still be in flight from the staging.
@@ -1202,6 +1295,12 @@ int graph_build(rive_cuda_context* ctx,
         CK(g->sortTemp.reserve(S.sortTempBytes));
         S.sortTemp = g->sortTemp.ptr;
     }
+    rc = prepare_raster(ctx);
+    if (rc)
+    {
+        ctx->profiling = profiling;
+        return rc;
+    }
     cudaError_t e = cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess)
     {
@@ -1371,6 +1470,30 @@ int rive_cuda_read_grad_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->grad.ptr, std::min(bytes, ctx->lastGradBytes), cudaMemcpyDeviceToHost));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_per_sm)
+{
+    if (!ctx)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    const int log2 = tile_size == 8 ? 3 : tile_size == 16 ? 4 : tile_size == 32 ? 5 : -1;
+    if (log2 < 0)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "tile size %d (8, 16 or 32)",
+                         tile_size);
+    if (ctas_per_sm < 0 || ctas_per_sm > 32)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "ctas_per_sm %d", ctas_per_sm);
+    ctx->tileLog2 = log2;
+    ctx->rasterCtasPerSm = log2 == 5 ? 0 : ctas_per_sm;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, int* ctas_per_sm)
+{
+    if (!ctx || !tile_size || !ctas_per_sm)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *tile_size = 1 << ctx->tileLog2;
+    *ctas_per_sm = ctx->rasterCtasPerSm;
     return RIVE_CUDA_OK;
 }
 

@@ -32,6 +32,7 @@ __global__ void outer_setup_kernel(BatchTables B,
                                    uint8_t* tileMasks);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_scatter_kernel(uint32_t slotCount,
+                                   int tileLog2,
                                    const uint2* sceneTiles,
                                    const TriRecord* tris,
                                    const uint32_t* tileCounts,
@@ -300,6 +301,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     B.segCount[0] = segCount;
     B.totalItems[0] = instAcc;
     B.sceneCount = 1;
+    B.tileLog2 = kTileLog2;
     B.totalGradSpans = d->grad_span_count;
     B.totalTessSpans = d->tess_span_count;
     B.totalTiles = tiles;
@@ -349,7 +351,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (pairs)
     {
         bin_scatter_kernel<<<(slots + 255) / 256, 256, 0, stream>>>(
-            slots, B.sceneTiles, tris, counts, masks, offs, pairs, dError, keys, vals);
+            slots, kTileLog2, B.sceneTiles, tris, counts, masks, offs, pairs, dError, keys, vals);
         int endBit = 1;
         while ((1u << endBit) <= tiles)
             ++endBit;

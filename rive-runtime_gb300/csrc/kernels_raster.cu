@@ -23,6 +23,8 @@
 
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 namespace rivecuda
 {
 namespace
@@ -488,9 +490,9 @@ __device__ __forceinline__ float4 make_edge(float2 P, float2 Q)
 // binning and the raster's block masks all use this same expression; float
 // rounding is monotone in lx and ly, so testing the corner of a rectangle
 // that maximises E never rejects a pixel the raster would accept.
-__device__ __forceinline__ float tile_edge_origin(float4 e, int tx, int ty)
+__device__ __forceinline__ float tile_edge_origin(float4 e, int tx, int ty, int tileLog2)
 {
-    return edge_eval(e, (float)(tx * kTileSize) + .5f, (float)(ty * kTileSize) + .5f);
+    return edge_eval(e, (float)(tx << tileLog2) + .5f, (float)(ty << tileLog2) + .5f);
 }
 
 __device__ __forceinline__ float local_edge(float c, float a, float b, float lx, float ly)
@@ -521,13 +523,16 @@ __device__ __forceinline__ bool local_rect_overlaps(const float* c, const float4
     return true;
 }
 
-__device__ __forceinline__ bool tile_overlaps(const float4* e, int4 bb, int tx, int ty)
+__device__ __forceinline__ bool tile_overlaps(const float4* e, int4 bb, int tx, int ty,
+                                              int tileLog2)
 {
-    const int ox = tx * kTileSize, oy = ty * kTileSize;
-    const float c[3] = {tile_edge_origin(e[0], tx, ty), tile_edge_origin(e[1], tx, ty),
-                        tile_edge_origin(e[2], tx, ty)};
-    return local_rect_overlaps(c, e, max(ox, bb.x) - ox, min(ox + kTileSize, bb.z) - ox,
-                               max(oy, bb.y) - oy, min(oy + kTileSize, bb.w) - oy);
+    const int ts = 1 << tileLog2;
+    const int ox = tx << tileLog2, oy = ty << tileLog2;
+    const float c[3] = {tile_edge_origin(e[0], tx, ty, tileLog2),
+                        tile_edge_origin(e[1], tx, ty, tileLog2),
+                        tile_edge_origin(e[2], tx, ty, tileLog2)};
+    return local_rect_overlaps(c, e, max(ox, bb.x) - ox, min(ox + ts, bb.z) - ox,
+                               max(oy, bb.y) - oy, min(oy + ts, bb.w) - oy);
 }
 
 __device__ __forceinline__ int4 unpack_bbox(uint4 meta)
@@ -609,12 +614,13 @@ __device__ bool setup_triangle(const FlushParams& P,
 }
 
 // Tiles a set-up triangle touches (the same tile test as the binner's).
-__device__ __forceinline__ void tile_span(int4 bb, int& tx0, int& ty0, int& ntx, int& nty)
+__device__ __forceinline__ void tile_span(int4 bb, int tileLog2, int& tx0, int& ty0, int& ntx,
+                                          int& nty)
 {
-    tx0 = bb.x >> kTileLog2;
-    ty0 = bb.y >> kTileLog2;
-    ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
-    nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+    tx0 = bb.x >> tileLog2;
+    ty0 = bb.y >> tileLog2;
+    ntx = ((bb.z - 1) >> tileLog2) - tx0 + 1;
+    nty = ((bb.w - 1) >> tileLog2) - ty0 + 1;
 }
 
 constexpr int kLaneTiles = 8;
@@ -623,6 +629,7 @@ constexpr int kLaneTiles = 8;
 // when its box spans at most kLaneTiles tiles; the whole warp walks larger
 // ones in turn. `has` marks lanes holding a triangle; e/bb its edges and box.
 __device__ __forceinline__ void count_tiles(bool has,
+                                            int tileLog2,
                                             const float4* e,
                                             int4 bb,
                                             uint32_t* __restrict__ countOut,
@@ -638,7 +645,7 @@ __device__ __forceinline__ void count_tiles(bool has,
         if (bb.z > bb.x)
         {
             int tx0, ty0, ntx, nty;
-            tile_span(bb, tx0, ty0, ntx, nty);
+            tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
             if (ntx * nty <= kLaneTiles)
             {
                 // The tiles it overlaps, as bits in row-major order over its
@@ -647,7 +654,7 @@ __device__ __forceinline__ void count_tiles(bool has,
                 int i = 0;
                 for (int ty = ty0; ty < ty0 + nty; ++ty)
                     for (int tx = tx0; tx < tx0 + ntx; ++tx, ++i)
-                        if (tile_overlaps(e, bb, tx, ty))
+                        if (tile_overlaps(e, bb, tx, ty, tileLog2))
                         {
                             ++count;
                             mask |= 1u << i;
@@ -673,11 +680,11 @@ __device__ __forceinline__ void count_tiles(bool has,
         const int4 tb = warpBoxes[t];
         const float4 te[3] = {warpEdges[t][0], warpEdges[t][1], warpEdges[t][2]};
         int tx0, ty0, ntx, nty;
-        tile_span(tb, tx0, ty0, ntx, nty);
+        tile_span(tb, tileLog2, tx0, ty0, ntx, nty);
         const int n = ntx * nty;
         uint32_t count = 0;
         for (int i = lane; i < n; i += 32)
-            count += tile_overlaps(te, tb, tx0 + i % ntx, ty0 + i / ntx) ? 1u : 0u;
+            count += tile_overlaps(te, tb, tx0 + i % ntx, ty0 + i / ntx, tileLog2) ? 1u : 0u;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             count += __shfl_xor_sync(0xffffffffu, count, o);
@@ -761,7 +768,7 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             sOut[w][t] = tileCounts + slot0 + t;
         }
         __syncwarp();
-        count_tiles(has, e, bb, tileCounts + slot0 + t, tileMasks + slot0 + t, sEdges[w] + pass * 32,
+        count_tiles(has, B.tileLog2, e, bb, tileCounts + slot0 + t, tileMasks + slot0 + t, sEdges[w] + pass * 32,
                     sBox[w] + pass * 32, sOut[w] + pass * 32);
         __syncwarp();
     }
@@ -858,7 +865,7 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
         sOut[w][lane] = tileCounts + slot;
     }
     __syncwarp();
-    count_tiles(has, e, bb, tileCounts + slot, tileMasks + slot, sEdges[w], sBox[w], sOut[w]);
+    count_tiles(has, B.tileLog2, e, bb, tileCounts + slot, tileMasks + slot, sEdges[w], sBox[w], sOut[w]);
 }
 
 // FlushUniforms fields the passes use (gpu.hpp:1466-1537: pathIDGranularity
@@ -895,6 +902,7 @@ __global__ void bin_fill_kernel(const uint32_t* __restrict__ pairTotal,
 // a ballot assigning output positions. Pairs at or past `capacity` are
 // dropped and flagged (ERR_BIN_OVERFLOW).
 __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
+                                                          int tileLog2,
                                                           const uint2* __restrict__ sceneTiles,
                                                           const TriRecord* __restrict__ tris,
                                                           const uint32_t* __restrict__ tileCounts,
@@ -917,9 +925,8 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
     if (myCount)
     {
         const int4 bb = unpack_bbox(tris[mySlot].meta);
-        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
-        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
-        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+        int tx0, ty0, ntx, nty;
+        tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
         if (ntx * nty <= kLaneTiles)
         {
             // The set-up already tested these tiles: walk its mask.
@@ -959,9 +966,8 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         const float4 e[3] = {T->e0, T->e1, T->e2};
         const uint2 st = sceneTiles[T->meta.w >> 16];
         uint32_t o = offsets[slot];
-        const int tx0 = bb.x >> kTileLog2, ty0 = bb.y >> kTileLog2;
-        const int ntx = ((bb.z - 1) >> kTileLog2) - tx0 + 1;
-        const int nty = ((bb.w - 1) >> kTileLog2) - ty0 + 1;
+        int tx0, ty0, ntx, nty;
+        tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
         const int n = ntx * nty;
         for (int base = 0; base < n; base += 32)
         {
@@ -972,7 +978,7 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
             {
                 tx = tx0 + i % ntx;
                 ty = ty0 + i / ntx;
-                hit = tile_overlaps(e, bb, tx, ty);
+                hit = tile_overlaps(e, bb, tx, ty, tileLog2);
             }
             const uint32_t mask = __ballot_sync(0xffffffffu, hit);
             if (hit)
@@ -1360,19 +1366,32 @@ struct __align__(16) TileTri
 };
 static_assert(sizeof(TileTri) == 80, "TileTri layout");
 
-// Resident CTAs per SM the register allocation is bounded for.
+// Resident CTAs per SM the register allocation is bounded for (16x16 tiles).
 #ifndef RIVE_RASTER_MIN_BLOCKS
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
 
-__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(
-    BatchTables B,
-    const TriRecord* __restrict__ tris,
-    const uint32_t* __restrict__ sortedSlots,
-    const uint2* __restrict__ ranges)
+// Tile geometry: a CTA of T x T threads, one per pixel; warp w owns the 8x4
+// block at (8 (w % (T/8)), 4 (w / (T/8))).
+template <int TL> struct RasterTile
 {
-    __shared__ TileTri sTris[256];
-    __shared__ uint8_t sMask[256];
+    static constexpr int T = 1 << TL;
+    static constexpr int kThreads = T * T;
+    static constexpr int kWarpCols = T / 8;
+    static constexpr int kBlocks = kThreads / 32;
+    using Mask = typename std::conditional<(kBlocks <= 8), uint8_t, uint32_t>::type;
+};
+
+template <int TL>
+__device__ __forceinline__ void raster_tile(const BatchTables& B,
+                                            const TriRecord* __restrict__ tris,
+                                            const uint32_t* __restrict__ sortedSlots,
+                                            const uint2* __restrict__ ranges,
+                                            TileTri* __restrict__ sTris,
+                                            typename RasterTile<TL>::Mask* __restrict__ sMask)
+{
+    using G = RasterTile<TL>;
+    static_assert(sizeof(FlushParams) / 4 <= G::kThreads, "one word of FlushParams per thread");
     __shared__ FlushParams sP;
     const uint32_t gtile = blockIdx.x;
     const uint2 range = ranges[gtile];
@@ -1387,9 +1406,9 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
     const uint32_t tilesX = P.tilesX;
     const uint32_t tile = gtile - B.tileBase[scene];
     const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
-    const int ox = tx * kTileSize, oy = ty * kTileSize;
+    const int ox = tx * G::T, oy = ty * G::T;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int lxi = (warp & 1) * 8 + (lane & 7), lyi = (warp >> 1) * 4 + (lane >> 3);
+    const int lxi = (warp % G::kWarpCols) * 8 + (lane & 7), lyi = (warp / G::kWarpCols) * 4 + (lane >> 3);
     const int px = ox + lxi, py = oy + lyi;
     const float lx = (float)lxi, ly = (float)lyi;
     const bool inBounds = px < (int)P.width && py < (int)P.height;
@@ -1413,18 +1432,19 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
     const float dither = v2 * P.ditherScale + P.ditherBias;
     uint32_t streamPath = 0xffffffffu; // coverage key of the warp's current path
 
-    for (uint32_t base = range.x; base < range.y; base += 256)
+    for (uint32_t base = range.x; base < range.y; base += G::kThreads)
     {
         // Each thread stages one triangle in tile-local form and marks which
-        // of the eight warp blocks may hold a pixel it covers.
+        // of the warp blocks may hold a pixel it covers.
         const uint32_t k = base + threadIdx.x;
         uint32_t m = 0;
         if (k < range.y)
         {
             const TriRecord T = tris[sortedSlots[k]];
             const float4 e[3] = {T.e0, T.e1, T.e2};
-            const float c[3] = {tile_edge_origin(e[0], tx, ty), tile_edge_origin(e[1], tx, ty),
-                                tile_edge_origin(e[2], tx, ty)};
+            const float c[3] = {tile_edge_origin(e[0], tx, ty, TL),
+                                tile_edge_origin(e[1], tx, ty, TL),
+                                tile_edge_origin(e[2], tx, ty, TL)};
             const float dx0 = (float)ox + .5f - T.e0.x, dy0 = (float)oy + .5f - T.e0.y;
             TileTri L;
             L.v0 = make_float4(__uint_as_float(T.meta.w & 0xffffu), c[0], e[0].z, e[0].w);
@@ -1438,18 +1458,18 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
             const int4 bb = unpack_bbox(T.meta);
             const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;
 #pragma unroll
-            for (int b = 0; b < 8; ++b)
+            for (int b = 0; b < G::kBlocks; ++b)
             {
-                const int qx = (b & 1) * 8, qy = (b >> 1) * 4;
+                const int qx = (b % G::kWarpCols) * 8, qy = (b / G::kWarpCols) * 4;
                 const int x0 = max(bx0, qx), x1 = min(bx1, qx + 8);
                 const int y0 = max(by0, qy), y1 = min(by1, qy + 4);
                 if (x0 < x1 && y0 < y1 && local_rect_overlaps(c, e, x0, x1, y0, y1))
                     m |= 1u << b;
             }
         }
-        sMask[threadIdx.x] = (uint8_t)m;
+        sMask[threadIdx.x] = (typename G::Mask)m;
         __syncthreads();
-        const uint32_t n = min(256u, range.y - base);
+        const uint32_t n = min((uint32_t)G::kThreads, range.y - base);
         for (uint32_t g = 0; g < n; g += 32)
         {
             // Triangles of this group touching this warp's block, in order.
@@ -1526,5 +1546,39 @@ __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kerne
         resolve_path(P, s, fx, fy, dither);
     if (inBounds)
         fb[(size_t)py * P.width + px] = s.color;
+}
+
+__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(
+    BatchTables B,
+    const TriRecord* __restrict__ tris,
+    const uint32_t* __restrict__ sortedSlots,
+    const uint2* __restrict__ ranges)
+{
+    __shared__ TileTri sTris[256];
+    __shared__ uint8_t sMask[256];
+    raster_tile<4>(B, tris, sortedSlots, ranges, sTris, sMask);
+}
+
+__global__ void __launch_bounds__(64) raster_tile8_kernel(BatchTables B,
+                                                         const TriRecord* __restrict__ tris,
+                                                         const uint32_t* __restrict__ sortedSlots,
+                                                         const uint2* __restrict__ ranges)
+{
+    __shared__ TileTri sTris[64];
+    __shared__ uint8_t sMask[64];
+    raster_tile<3>(B, tris, sortedSlots, ranges, sTris, sMask);
+}
+
+// 32x32 tiles: 1,024 threads, the staged records in dynamic shared memory
+// (kRaster32SmemBytes).
+__global__ void __launch_bounds__(1024, 1) raster_tile32_kernel(BatchTables B,
+                                                               const TriRecord* __restrict__ tris,
+                                                               const uint32_t* __restrict__ sortedSlots,
+                                                               const uint2* __restrict__ ranges)
+{
+    extern __shared__ uint4 dyn[];
+    TileTri* sTris = reinterpret_cast<TileTri*>(dyn);
+    uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);
+    raster_tile<5>(B, tris, sortedSlots, ranges, sTris, sMask);
 }
 } // namespace rivecuda

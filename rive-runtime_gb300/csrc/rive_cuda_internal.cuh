@@ -77,10 +77,11 @@ constexpr uint32_t SF_HSL_BLEND_MODES = 1u << 6;
 constexpr uint32_t SF_DITHER = 1u << 7;
 constexpr uint32_t SF_MODULATED_IMAGE = 1u << 8;
 
-// Raster tiles.
+// Raster tiles: 16x16 by default; 8x8 and 32x32 are the autotuner's other
+// choices (rive_cuda_set_raster_config).
 constexpr int kTileSize = 16;
 constexpr int kTileLog2 = 4;
-constexpr int kTilePixels = kTileSize * kTileSize;
+constexpr int kRaster32SmemBytes = 1024 * 80 + 1024 * 4; // staged records + block masks
 
 // Device error word bits (read by rive_cuda_sync).
 constexpr uint32_t ERR_BAD_TESS_INDEX = 1u << 0;
@@ -173,6 +174,7 @@ struct BatchTables
     uint32_t totalItems[kSetupLists];
     uint32_t sceneCount;
     uint32_t totalGradSpans, totalTessSpans, totalTiles;
+    int tileLog2; // raster tile size of this batch (3, 4 or 5)
 };
 
 // Index j with base[j] <= i < base[j + 1] (empty ranges skipped), n >= 1.

@@ -113,6 +113,9 @@ def load():
         "rive_cuda_read_grad_texture": (i32, [vp, vp, sz]),
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
+        "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
+        "rive_cuda_get_raster_config": (i32, [vp, ctypes.POINTER(ctypes.c_int),
+                                              ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_profile_collect": (i32, [vp, ctypes.POINTER(ctypes.c_double),
                                             ctypes.POINTER(ctypes.c_uint64)]),
     }
@@ -313,6 +316,18 @@ class Context:
 
     def set_profiling(self, on: bool):
         self.check(self.lib.rive_cuda_set_profiling(self.h, 1 if on else 0), "set_profiling")
+
+    def set_raster_config(self, tile_size: int = 16, ctas_per_sm: int = 0):
+        """Tile size (8, 16, 32) and resident raster CTAs per SM (0: as many as
+        fit) for later flushes; the image is the same within tolerance."""
+        self.check(self.lib.rive_cuda_set_raster_config(self.h, int(tile_size), int(ctas_per_sm)),
+                   "set_raster_config")
+
+    def raster_config(self):
+        t, c = ctypes.c_int(), ctypes.c_int()
+        self.check(self.lib.rive_cuda_get_raster_config(self.h, ctypes.byref(t), ctypes.byref(c)),
+                   "get_raster_config")
+        return t.value, c.value
 
     def profile_collect(self):
         ms = (ctypes.c_double * len(STAGES))()

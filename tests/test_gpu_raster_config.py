@@ -1,0 +1,126 @@
+"""Raster configurations (rive_cuda_set_raster_config): every tile size and
+CTAs-per-SM limit must meet the same image bar against the oracle as the
+default, in single flushes, in a batch and in a CUDA graph, and the
+autotuner must leave one of its candidates set."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, load_package
+import oracle
+
+load_package()
+
+CONFIGS = [(8, 0), (16, 2), (16, 4), (32, 0)]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from rive_runtime_gb300 import rive_cuda
+    c = rive_cuda.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def oracle_images():
+    return {n: oracle.render(load_golden(n)[0]) for n in golden_names()}
+
+
+def _parity(got, want):
+    d = np.abs(got.astype(np.int16) - want.astype(np.int16)).max(axis=2)
+    return float((d <= 2).mean()), int(d.max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("config", CONFIGS, ids=lambda c: f"tile{c[0]}_ctas{c[1]}")
+def test_every_config_matches_oracle(ctx, oracle_images, config):
+    ctx.set_raster_config(*config)
+    try:
+        assert ctx.raster_config() == (config[0], config[1] if config[0] != 32 else 0)
+        for name in golden_names():
+            cap = load_golden(name)[0]
+            got = ctx.render(cap)
+            frac, worst = _parity(got, oracle_images[name])
+            assert frac >= 0.999 and worst <= 8, (config, name, frac, worst)
+            st = ctx.stats()
+            t = config[0]
+            assert st["tiles"] == ((cap.width + t - 1) // t) * ((cap.height + t - 1) // t)
+    finally:
+        ctx.set_raster_config(16, 0)
+
+
+@pytest.mark.gpu
+def test_rejects_unknown_tile_size(ctx):
+    from rive_runtime_gb300 import rive_cuda
+    with pytest.raises(rive_cuda.RiveCudaError):
+        ctx.set_raster_config(12, 0)
+    with pytest.raises(rive_cuda.RiveCudaError):
+        ctx.set_raster_config(16, -1)
+    assert ctx.raster_config() == (16, 0)
+
+
+def _device_buffers(cap):
+    import torch
+    from rive_runtime_gb300 import rive_cuda
+    from rive_runtime_gb300.capture import BUFFER_NAMES
+    bufs = rive_cuda.DeviceBuffers()
+    keep = []
+    for name in BUFFER_NAMES:
+        b = cap.buffers.get(name, b"")
+        t = torch.from_numpy(np.frombuffer(b, np.uint8).copy()).cuda() if b else None
+        keep.append(t)
+        setattr(bufs, name, t.data_ptr() if t is not None else None)
+    return bufs, keep
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tile", [8, 32])
+def test_batch_and_graph_at_other_tile_sizes_match_oracle(ctx, oracle_images, tile):
+    import torch
+    names = golden_names()
+    caps = [load_golden(n)[0] for n in names]
+    pairs = [_device_buffers(c) for c in caps]
+    stream = torch.cuda.current_stream().cuda_stream
+    ctx.set_raster_config(tile, 0)
+    try:
+        for mode in ("batch", "graph"):
+            targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda")
+                       for c in caps]
+            items = [(c.flushes[0], p[0], t.data_ptr()) for c, p, t in zip(caps, pairs, targets)]
+            if mode == "batch":
+                ctx.flush_batch(items, stream)
+                ctx.sync(stream)
+            else:
+                g = ctx.graph(items)
+                g.launch(stream)
+                g.check(stream)
+                g.close()
+            torch.cuda.synchronize()
+            for name, t in zip(names, targets):
+                frac, worst = _parity(t.cpu().numpy(), oracle_images[name])
+                assert frac >= 0.999 and worst <= 8, (tile, mode, name, frac, worst)
+    finally:
+        ctx.set_raster_config(16, 0)
+
+
+@pytest.mark.gpu
+def test_autotune_leaves_a_candidate_set(ctx):
+    import torch
+    from rive_runtime_gb300 import autotune
+    cap = load_golden("full_small_s7")[0]
+    bufs, keep = _device_buffers(cap)
+    target = torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def run(s):
+        for f in cap.flushes:
+            ctx.flush_device(f, bufs, target.data_ptr(), s.cuda_stream)
+
+    try:
+        best, trials = autotune.autotune(ctx, run, stream=stream, warmup=1, iters=2)
+        assert len(trials) == len(autotune.CANDIDATES)
+        assert all(t.ms > 0 for t in trials)
+        assert ctx.raster_config() == (best.tile_size, best.ctas_per_sm)
+        assert best.ms == min(t.ms for t in trials)
+    finally:
+        ctx.set_raster_config(16, 0)
