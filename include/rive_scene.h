@@ -40,6 +40,7 @@ enum
     RIVE_SCENE_CMD_TRANSFORM = 2, /* m[6] = xx, xy, yx, yy, tx, ty */
     RIVE_SCENE_CMD_DRAW_PATH = 3, /* a = path index, b = paint index */
     RIVE_SCENE_CMD_CLIP_PATH = 4, /* a = path index */
+    RIVE_SCENE_CMD_MODULATE_OPACITY = 5, /* m[0] = opacity (Renderer::modulateOpacity) */
 };
 
 /* rive::RenderPaintStyle / gradient kinds. */
@@ -81,7 +82,7 @@ typedef struct rive_scene_path
     uint32_t verb_count;
     uint32_t point_offset;
     uint32_t point_count;
-    uint32_t fill_rule; /* rive::FillRule: 0 nonZero, 1 evenOdd */
+    uint32_t fill_rule; /* rive::FillRule: 0 nonZero, 1 evenOdd, 2 clockwise */
 } rive_scene_path;
 
 typedef struct rive_scene_paint

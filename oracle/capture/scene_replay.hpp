@@ -172,6 +172,9 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
                 case RIVE_SCENE_CMD_CLIP_PATH:
                     renderer.clipPath(renderPaths[c.a].get());
                     break;
+                case RIVE_SCENE_CMD_MODULATE_OPACITY:
+                    renderer.modulateOpacity(c.m[0]);
+                    break;
                 default:
                     return ("bad command");
             }

@@ -87,6 +87,10 @@
 #define SF_ADVANCED_BLEND (1u << 2)
 #define SF_FEATHER (1u << 3)
 #define SF_EVEN_ODD (1u << 4)
+/* gpu::ShaderMiscFlags::clockwiseFill of a draw batch (gpu.hpp:917), carried
+ * with each triangle's shader features in a bit ShaderFeatures leaves free. */
+#define MISC_CLOCKWISE_FILL (1u << 1)
+#define FEATURE_CLOCKWISE_FILL (1u << 15)
 #define SF_NESTED_CLIPPING (1u << 5)
 #define SF_HSL_BLEND_MODES (1u << 6)
 #define SF_DITHER (1u << 7)
@@ -1391,10 +1395,20 @@ static void fragment(const frag_ctx* fc,
         coverageCount = h2f(storedCount);
     }
 
-    float coverage = fabsf(coverageCount);
-    if ((features & SF_EVEN_ODD) && evenOdd)
-        coverage = 1.f - fabsf(fractf(coverage * .5f) * 2.f + -1.f);
-    coverage = minf(coverage, 1.f);
+    /* draw_raster_order_path.frag:63-82: clockwise fills keep positive
+     * windings only; otherwise nonzero or even-odd. */
+    float coverage;
+    if (features & FEATURE_CLOCKWISE_FILL)
+    {
+        coverage = minf(maxf(coverageCount, 0.f), 1.f);
+    }
+    else
+    {
+        coverage = fabsf(coverageCount);
+        if ((features & SF_EVEN_ODD) && evenOdd)
+            coverage = 1.f - fabsf(fractf(coverage * .5f) * 2.f + -1.f);
+        coverage = minf(coverage, 1.f);
+    }
 
     /* Clip IDs (draw_path.vert:203-220). */
     float clipIDx = 0.f, clipIDy = 0.f;
@@ -1506,7 +1520,10 @@ static void fragment(const frag_ctx* fc,
         float spanB = gradientSpan > .9f ? 2.f : aux[7];
         float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pc.x
                                                           : sqrtf(dot2(pc, pc));
-        t = clampf(t, 0.f, 1.f);
+        /* GLSL clamp() is min(max(t, 0), 1); GPUs evaluate min/max with
+         * IEEE minNum/maxNum, so a NaN coordinate (a degenerate gradient,
+         * whose paint matrix the front end writes as NaN) clamps to 0. */
+        t = fminf(fmaxf(t, 0.f), 1.f);
         float x = spanB > 1.f
                       ? (1.f - 1.f / GRAD_TEXTURE_WIDTH) * t + (.5f / GRAD_TEXTURE_WIDTH)
                       : (1.f / GRAD_TEXTURE_WIDTH) * t + spanB;
@@ -1735,11 +1752,15 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
     {
         const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
-        if (batch->shader_features & SF_FEATHER)
+        if ((batch->shader_features & SF_FEATHER) ||
+            (batch->shader_misc_flags & ~MISC_CLOCKWISE_FILL))
         {
             free(tris);
             return -2;
         }
+        const uint32_t features =
+            batch->shader_features |
+            ((batch->shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u);
         int rc = 0;
         if (batch->draw_type == RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES ||
             batch->draw_type == DRAW_TYPE_OUTER_CURVE_PATCHES)
@@ -1762,7 +1783,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
                     if (rc == 0)
                     {
                         int r = setup_triangle(&vo[idx[k]], &vo[idx[k + 1]], &vo[idx[k + 2]],
-                                               batch->shader_features, W, H, &tris[n]);
+                                               features, W, H, &tris[n]);
                         if (r < 0)
                             rc = r;
                         else
@@ -1806,8 +1827,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
                     rc = grow_tris(&tris, &cap, n);
                 if (rc == 0)
                 {
-                    int r = setup_triangle(&vo[0], &vo[1], &vo[2], batch->shader_features, W, H,
-                                           &tris[n]);
+                    int r = setup_triangle(&vo[0], &vo[1], &vo[2], features, W, H, &tris[n]);
                     if (r < 0)
                         rc = r;
                     else if (r > 0)

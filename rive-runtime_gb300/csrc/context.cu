@@ -373,6 +373,10 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
                              b.draw_type);
         if (b.shader_features & SF_FEATHER)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
+        if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
+            return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
+                             "shader misc flags 0x%x not supported (rasterOrdering: clockwiseFill only)",
+                             b.shader_misc_flags);
         if (list == 2)
         {
             if (b.element_count % 3 || !rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE] ||
@@ -602,7 +606,11 @@ BatchTables write_tables(rive_cuda_context* ctx,
             if (!k)
                 continue;
             const int l = setup_list(db.draw_type);
-            segs[l][segAcc[l]] = PatchSegment{i, db.base_element, db.shader_features, slotAcc};
+            segs[l][segAcc[l]] = PatchSegment{
+                i, db.base_element,
+                db.shader_features |
+                    ((db.shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u),
+                slotAcc};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += k;

@@ -185,6 +185,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                         b.draw_type);
         if (b.shader_features & SF_FEATHER)
             return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
+        if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
+            return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                        "shader misc flags 0x%x not supported", b.shader_misc_flags);
         if (((uint64_t)b.base_element + b.element_count) * kPatchSegmentSpan >
             (uint64_t)d->tess_data_height * kTessTextureWidth)
             return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
@@ -276,7 +279,10 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         const rive_cuda_draw_batch& b = d->draw_batches[i];
         if (!b.element_count)
             continue;
-        segs[segCount] = PatchSegment{0u, b.base_element, b.shader_features,
+        segs[segCount] = PatchSegment{0u, b.base_element,
+                                      b.shader_features | ((b.shader_misc_flags & MISC_CLOCKWISE_FILL)
+                                                               ? FEATURE_CLOCKWISE_FILL
+                                                               : 0u),
                                       instAcc * kPatchTriangleCount};
         segBase[segCount] = instAcc;
         ++segCount;

@@ -1221,10 +1221,20 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
     const uint32_t paintX = s.pendPaintX, paintY = s.pendPaintY;
     const uint32_t paintType = paintX & 0xfu;
     const bool evenOdd = (paintX & PAINT_FLAG_EVEN_ODD_FILL) != 0;
-    float coverage = fabsf(s.count);
-    if ((features & SF_EVEN_ODD) && evenOdd)
-        coverage = 1.f - fabsf((coverage * .5f - floorf(coverage * .5f)) * 2.f + -1.f);
-    coverage = fminf(coverage, 1.f);
+    // draw_raster_order_path.frag:63-82: clockwise fills keep positive
+    // windings only; otherwise nonzero or even-odd.
+    float coverage;
+    if (features & FEATURE_CLOCKWISE_FILL)
+    {
+        coverage = fminf(fmaxf(s.count, 0.f), 1.f);
+    }
+    else
+    {
+        coverage = fabsf(s.count);
+        if ((features & SF_EVEN_ODD) && evenOdd)
+            coverage = 1.f - fabsf((coverage * .5f - floorf(coverage * .5f)) * 2.f + -1.f);
+        coverage = fminf(coverage, 1.f);
+    }
 
     if (features & SF_CLIPPING)
     {

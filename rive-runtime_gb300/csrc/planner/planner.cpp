@@ -59,12 +59,19 @@ constexpr uint32_t PAINT_FLAG_NON_ZERO_FILL = 0x100u;
 constexpr uint32_t PAINT_FLAG_EVEN_ODD_FILL = 0x200u;
 
 // gpu::DrawContents
-constexpr uint32_t DC_OPAQUE = 1u << 0, DC_STROKE = 1u << 2, DC_NONZERO = 1u << 4,
-                   DC_EVENODD = 1u << 5, DC_ACTIVE_CLIP = 1u << 6,
+constexpr uint32_t DC_OPAQUE = 1u << 0, DC_STROKE = 1u << 2, DC_CLOCKWISE = 1u << 3,
+                   DC_NONZERO = 1u << 4, DC_EVENODD = 1u << 5, DC_ACTIVE_CLIP = 1u << 6,
                    DC_ADVANCED_BLEND = 1u << 7, DC_CLIP_UPDATE = 1u << 8;
+constexpr uint32_t DC_ANY_FILL = DC_CLOCKWISE | DC_NONZERO | DC_EVENODD;
 // gpu::ShaderFeatures
-constexpr uint32_t SF_CLIPPING = 1u << 0, SF_ADVANCED_BLEND = 1u << 2, SF_EVEN_ODD = 1u << 4,
-                   SF_NESTED_CLIPPING = 1u << 5, SF_HSL = 1u << 6, SF_DITHER = 1u << 7;
+constexpr uint32_t SF_CLIPPING = 1u << 0, SF_CLIP_RECT = 1u << 1, SF_ADVANCED_BLEND = 1u << 2,
+                   SF_EVEN_ODD = 1u << 4, SF_NESTED_CLIPPING = 1u << 5, SF_HSL = 1u << 6,
+                   SF_DITHER = 1u << 7;
+// gpu::ShaderMiscFlags::clockwiseFill
+constexpr uint32_t MISC_CLOCKWISE_FILL = 1u << 1;
+constexpr uint32_t PAINT_FLAG_HAS_CLIP_RECT = 0x400u;
+constexpr uint32_t NEGATE_PATH_FILL_COVERAGE_FLAG = 1u << 24;
+constexpr uint32_t FILL_RULE_CLOCKWISE = 2; // rive::FillRule::clockwise
 
 enum PaintType : uint32_t
 {
@@ -96,7 +103,8 @@ enum Cap : uint32_t
 enum ContourDirections
 {
     CD_FORWARD,
-    CD_REVERSE_THEN_FORWARD
+    CD_REVERSE_THEN_FORWARD,
+    CD_FORWARD_THEN_REVERSE
 };
 
 struct PlanError : std::runtime_error
@@ -165,7 +173,14 @@ struct FBox
 struct M2
 {
     float v[6] = {1, 0, 0, 1, 0, 0};
-    bool operator==(const M2& o) const { return memcmp(v, o.v, sizeof(v)) == 0; }
+    // operator== (include/rive/math/mat2d.hpp): element-wise float equality.
+    bool operator==(const M2& o) const
+    {
+        for (int i = 0; i < 6; ++i)
+            if (!(v[i] == o.v[i]))
+                return false;
+        return true;
+    }
     // Mat2D::multiply (src/math/mat2d.cpp:45-57)
     M2 operator*(const M2& b) const
     {
@@ -791,6 +806,9 @@ struct PathDraw
     uint32_t contourFlags = 0;
     uint32_t clipID = 0;
     uint32_t pathID = 0;
+    // Draw::setClipRect: the render state's clip rect, if any.
+    bool hasClipRect = false;
+    M2 clipRectInverse; // ClipRectInverseMatrix::inverseMatrix()
 
     // initForMidpointFan
     float strokeMatrixMaxScale = 0;
@@ -1163,7 +1181,7 @@ void PathDraw::initForMidpointFan()
         counts.contourCount = contourCount;
         counts.maxTessellatedSegmentCount = lineCount + unpaddedCurveCount + emptyStrokeCountForCaps;
         counts.midpointFanTessVertexCount =
-            contourDirections == CD_REVERSE_THEN_FORWARD ? tessVertexCount * 2 : tessVertexCount;
+            contourDirections != CD_FORWARD ? tessVertexCount * 2 : tessVertexCount;
     }
 }
 
@@ -1671,6 +1689,8 @@ uint32_t LogicalFlush::pushPath(PathDraw* d)
         local |= PAINT_FLAG_NON_ZERO_FILL;
     else if (d->drawContents & DC_EVENODD)
         local |= PAINT_FLAG_EVEN_ODD_FILL;
+    if (d->hasClipRect)
+        local |= PAINT_FLAG_HAS_CLIP_RECT;
     pd.params = local;
 
     PaintAuxRec& ax = frame->paintAux.push();
@@ -1717,11 +1737,21 @@ uint32_t LogicalFlush::pushPath(PathDraw* d)
         ax.gradSpan[1] = (left + .5f) * (1.f / kGradTextureWidth);
         memcpy(ax.paintMatrix, pm.v, sizeof(pm.v));
     }
-    // No clip rect: ClipRectInverseMatrix::WideOpen() = {0, 0, 0, 0, 1, 1}.
-    ax.clipRectInverse[0] = ax.clipRectInverse[1] = ax.clipRectInverse[2] = 0;
-    ax.clipRectInverse[3] = 0;
-    ax.clipRectInverse[4] = ax.clipRectInverse[5] = 1;
-    ax.inverseFwidth[0] = ax.inverseFwidth[1] = 0;
+    if (d->hasClipRect)
+    {
+        const M2& m = d->clipRectInverse;
+        memcpy(ax.clipRectInverse, m.v, sizeof(m.v));
+        ax.inverseFwidth[0] = -1.f / (fabsf(m.v[0]) + fabsf(m.v[1]));
+        ax.inverseFwidth[1] = -1.f / (fabsf(m.v[2]) + fabsf(m.v[3]));
+    }
+    else
+    {
+        // No clip rect: ClipRectInverseMatrix::WideOpen() = {0, 0, 0, 0, 1, 1}.
+        ax.clipRectInverse[0] = ax.clipRectInverse[1] = ax.clipRectInverse[2] = 0;
+        ax.clipRectInverse[3] = 0;
+        ax.clipRectInverse[4] = ax.clipRectInverse[5] = 1;
+        ax.inverseFwidth[0] = ax.inverseFwidth[1] = 0;
+    }
     return currentPathID;
 }
 
@@ -1976,13 +2006,28 @@ void LogicalFlush::pushDrawBatch(PathDraw* d, uint32_t tessVertexCount, uint32_t
 {
     uint32_t baseInstance = tessLocation / kMidpointFanPatchSegmentSpan;
     uint32_t instanceCount = tessVertexCount / kMidpointFanPatchSegmentSpan;
+    // pushPathDraw (render_context.cpp:3630-3639): clockwise fills get their
+    // own shader variant in rasterOrdering.
+    const uint32_t misc = (d->drawContents & DC_CLOCKWISE) ? MISC_CLOCKWISE_FILL : 0u;
     rive_cuda_draw_batch* batch;
-    if (!batches.empty() &&
-        batches.back().base_element + batches.back().element_count == baseInstance)
+    bool merge = !batches.empty() &&
+                 batches.back().base_element + batches.back().element_count == baseInstance;
+    if (merge)
+    {
+        // can_combine_shader_misc_flags (render_context.cpp:3680-3700):
+        // strokes draw the same in either shader, so the flag only separates
+        // batches when both hold fills.
+        const rive_cuda_draw_batch& tail = batches.back();
+        if ((tail.draw_contents & DC_ANY_FILL) && (d->drawContents & DC_ANY_FILL) &&
+            (tail.shader_misc_flags & MISC_CLOCKWISE_FILL) != misc)
+            merge = false;
+    }
+    if (merge)
     {
         batch = &batches.back();
         batch->element_count += instanceCount;
         batch->draw_contents |= d->drawContents;
+        batch->shader_misc_flags |= misc;
     }
     else
     {
@@ -1992,11 +2037,14 @@ void LogicalFlush::pushDrawBatch(PathDraw* d, uint32_t tessVertexCount, uint32_t
         batch->element_count = instanceCount;
         batch->base_element = baseInstance;
         batch->draw_contents = d->drawContents;
+        batch->shader_misc_flags = misc;
         batch->first_blend_mode = d->blendMode;
     }
     uint32_t features = 0;
     if (d->clipID != 0)
         features |= SF_CLIPPING;
+    if (d->hasClipRect && d->paintType != PT_CLIP_UPDATE)
+        features |= SF_CLIP_RECT;
     if (ctx->ditherMode == 1)
         features |= SF_DITHER;
     if (d->paintType != PT_CLIP_UPDATE)
@@ -2107,10 +2155,18 @@ void LogicalFlush::write()
             fwdLoc = tessLocation;
             mirCount = mirLoc = 0;
         }
-        else
+        else if (d->contourDirections == CD_REVERSE_THEN_FORWARD)
         {
             fwdCount = mirCount = tessVertexCount / 2;
             fwdLoc = mirLoc = tessLocation + tessVertexCount / 2;
+        }
+        else
+        {
+            // forwardThenReverse (draw.cpp:1945-1965): forward from the start,
+            // mirrored growing down from the end.
+            fwdCount = mirCount = tessVertexCount / 2;
+            fwdLoc = tessLocation;
+            mirLoc = tessLocation + tessVertexCount;
         }
         (void)fwdCount;
         (void)mirCount;
@@ -2175,7 +2231,95 @@ struct RenderState
     M2 matrix;
     size_t clipStackHeight = 0;
     IBox overallClipPixelBounds = IBox::maximal();
+    float modulatedOpacity = 1.f;
+    // RiveRenderer clip rect state (rive_renderer.cpp:267-323).
+    bool hasClipRect = false;
+    FBox clipRect{};
+    M2 clipRectMatrix;
+    M2 clipRectInverse; // ClipRectInverseMatrix of (clipRectMatrix, clipRect)
 };
+
+// colorModulateOpacity (src/shapes/paint/color.cpp:36-67): the alpha byte
+// rescaled, rounded to nearest, clamped to [0, 255].
+uint32_t color_modulate_opacity(uint32_t c, float opacity)
+{
+    float o = (float)(c >> 24) / 0xFF * opacity;
+    uint32_t a = (uint32_t)std::lround(255.f * std::max(0.0f, std::min(1.0f, o)));
+    return (c & 0x00ffffffu) | ((a & 0xffu) << 24);
+}
+
+// RiveRenderer::IsAABB (rive_renderer.cpp:16-55): a move and three lines
+// forming an axis-aligned rectangle; any further points must equal p0.
+bool is_aabb(const Path& path, FBox* out)
+{
+    const auto& v = path.verbs;
+    const auto& p = path.pts;
+    if (v.size() < 4 || v[0] != V_MOVE || v[1] != V_LINE || v[2] != V_LINE || v[3] != V_LINE ||
+        p.size() < 4)
+        return false;
+    for (size_t i = 4; i < p.size(); ++i)
+        if (p[i] != p[0])
+            return false;
+    const bool a = p[0].x == p[3].x && p[0].y == p[1].y && p[2].x == p[1].x && p[2].y == p[3].y;
+    const bool b = p[0].x == p[1].x && p[0].y == p[3].y && p[2].x == p[3].x && p[2].y == p[1].y;
+    if (!a && !b)
+        return false;
+    *out = {simd_min(p[0].x, p[2].x), simd_min(p[0].y, p[2].y), simd_max(p[0].x, p[2].x),
+            simd_max(p[0].y, p[2].y)};
+    return true;
+}
+
+// Mat2D::mapPoints (src/math/mat2d.cpp:59-101) for one point.
+V2 map_point(const M2& m, V2 p)
+{
+    if (m.v[1] == 0.f && m.v[2] == 0.f)
+        return {m.v[0] * p.x + m.v[4], m.v[3] * p.y + m.v[5]};
+    float sx = m.v[2] * p.y + m.v[4], sy = m.v[1] * p.x + m.v[5];
+    return {m.v[0] * p.x + sx, m.v[3] * p.y + sy};
+}
+
+// transform_rect_to_new_space (rive_renderer.cpp:230-265).
+bool transform_rect_to_new_space(FBox* rect, const M2& currentMatrix, const M2& newMatrix)
+{
+    if (currentMatrix == newMatrix)
+        return true;
+    M2 currentToNew;
+    if (!newMatrix.invert(&currentToNew))
+        return false;
+    currentToNew = currentToNew * currentMatrix;
+    const float* c = currentToNew.v;
+    float maxSkew = fmaxf(fabsf(c[1]), fabsf(c[2]));
+    float maxScale = fmaxf(fabsf(c[0]), fabsf(c[3]));
+    constexpr float kEpsilon = 1.f / (1 << 12); // math::EPSILON
+    if (maxSkew > kEpsilon && maxScale > kEpsilon)
+        return false;
+    V2 a = map_point(currentToNew, {rect->l, rect->t});
+    V2 b = map_point(currentToNew, {rect->r, rect->b});
+    *rect = {simd_min(a.x, b.x), simd_min(a.y, b.y), simd_max(a.x, b.x), simd_max(a.y, b.y)};
+    return true;
+}
+
+// ClipRectInverseMatrix::reset (gpu.cpp:689-706): pixel space to the clip
+// rect's normalised [-1, +1]^2; all zeros (clip everything) when degenerate.
+M2 clip_rect_inverse(const M2& clipMatrix, const FBox& r)
+{
+    float w = r.width(), h = r.height();
+    M2 box;
+    box.v[0] = w * .5f;
+    box.v[1] = 0;
+    box.v[2] = 0;
+    box.v[3] = h * .5f;
+    box.v[4] = (r.l + r.r) * 0.5f;
+    box.v[5] = (r.t + r.b) * 0.5f;
+    M2 m = clipMatrix * box;
+    M2 inv;
+    if (w <= 0 || h <= 0 || !m.invert(&inv))
+    {
+        for (float& x : inv.v)
+            x = 0;
+    }
+    return inv;
+}
 
 struct Renderer
 {
@@ -2187,7 +2331,7 @@ struct Renderer
     // PathDraw::Make + ctor + initForMidpointFan (draw.cpp:420-757).
     std::unique_ptr<PathDraw> makeDraw(const M2& matrix, const std::shared_ptr<Path>& path,
                                        uint32_t fillRule, const Paint& paint,
-                                       const IBox* precomputed)
+                                       const IBox* precomputed, float modulatedOpacity = 1.f)
     {
         IBox pixelBounds;
         if (precomputed)
@@ -2216,9 +2360,19 @@ struct Renderer
         d->fillRule = fillRule;
         d->paintType = paint.type;
         d->blendMode = paint.blendMode;
+        // RiveRenderPaint::getGradientWithOpacity -> Gradient::getModulated
+        // (gradient.cpp:191-221): every stop colour's alpha scaled.
         d->gradient = paint.gradient;
+        if (paint.gradient && modulatedOpacity != 1.f)
+        {
+            auto g = std::make_shared<Gradient>(*paint.gradient);
+            for (uint32_t& c : g->colors)
+                c = color_modulate_opacity(c, modulatedOpacity);
+            d->gradient = g;
+        }
         if (paint.blendMode != 3)
             d->drawContents |= DC_ADVANCED_BLEND;
+        // The reference tests the paint itself, before opacity modulation.
         if (paint.isOpaque())
             d->drawContents |= DC_OPAQUE;
         if (paint.stroked)
@@ -2227,6 +2381,24 @@ struct Renderer
             d->strokeRadius = fmaxf(d->strokeRadius, std::numeric_limits<float>::min());
             d->drawContents |= DC_STROKE;
             d->contourDirections = CD_FORWARD;
+        }
+        else if (fillRule == FILL_RULE_CLOCKWISE)
+        {
+            // draw.cpp:627-631, 657-680: clockwise fills keep their forward
+            // triangles clockwise; a left-handed matrix reverses the
+            // contours and negates the coverage.
+            d->drawContents |= DC_CLOCKWISE;
+            const M2& m = matrix;
+            float det = m.v[0] * m.v[3] - m.v[2] * m.v[1];
+            if (det < 0)
+            {
+                d->contourDirections = CD_FORWARD_THEN_REVERSE;
+                d->contourFlags |= NEGATE_PATH_FILL_COVERAGE_FLAG;
+            }
+            else
+            {
+                d->contourDirections = CD_REVERSE_THEN_FORWARD;
+            }
         }
         else
         {
@@ -2241,7 +2413,8 @@ struct Renderer
             d->outerClipID = paint.outerClipID;
         }
         if (paint.type == PT_SOLID)
-            d->color = paint.color;
+            d->color = modulatedOpacity != 1.f ? color_modulate_opacity(paint.color, modulatedOpacity)
+                                               : paint.color;
         d->strokeJoin = paint.join;
         d->strokeCap = paint.cap;
         d->initForMidpointFan();
@@ -2259,6 +2432,9 @@ struct Renderer
     ApplyClipResult applyClip(PathDraw* draw)
     {
         RenderState& rs = stack.back();
+        // Draw::setClipRect
+        draw->hasClipRect = rs.hasClipRect;
+        draw->clipRectInverse = rs.clipRectInverse;
         draw->clippedPixelBounds = draw->clippedPixelBounds.intersect(rs.overallClipPixelBounds);
         if (draw->clippedPixelBounds.empty() || ctx->isOutsideCurrentFrame(draw->clippedPixelBounds))
             return CLIP_FULLY_CLIPPED;
@@ -2342,7 +2518,8 @@ struct Renderer
             return;
         if (stack.back().overallClipPixelBounds.empty())
             return;
-        clipAndPushDraw(makeDraw(stack.back().matrix, path, path->fillRule, paint, nullptr));
+        clipAndPushDraw(makeDraw(stack.back().matrix, path, path->fillRule, paint, nullptr,
+                                 stack.back().modulatedOpacity));
     }
 
     void clipPath(const std::shared_ptr<Path>& path)
@@ -2355,12 +2532,50 @@ struct Renderer
             rs.overallClipPixelBounds = {0, 0, 0, 0};
             return;
         }
-        // Axis-aligned rectangle clips become clip rects in the reference
-        // (RiveRenderer::IsAABB); this planner does not model them.
-        if (path->verbs.size() >= 4 && path->verbs[0] == V_MOVE && path->verbs[1] == V_LINE &&
-            path->verbs[2] == V_LINE && path->verbs[3] == V_LINE)
-            throw PlanError("rectangular clip paths (clip rects) are not supported by the planner");
-        // clipPathImpl (rive_renderer.cpp:323-382)
+        // Axis-aligned rectangles become the ENABLE_CLIP_RECT clip rect.
+        FBox rect;
+        if (is_aabb(*path, &rect))
+        {
+            clipRectImpl(rect, path);
+            return;
+        }
+        clipPathImpl(path);
+    }
+
+    // RiveRenderer::clipRectImpl (rive_renderer.cpp:267-323).
+    void clipRectImpl(FBox rect, const std::shared_ptr<Path>& path)
+    {
+        RenderState& rs = stack.back();
+        if (!(rect.width() > 0 && rect.height() > 0)) // AABB::isEmptyOrNaN
+        {
+            rs.overallClipPixelBounds = {0, 0, 0, 0};
+            return;
+        }
+        if (rs.hasClipRect && !transform_rect_to_new_space(&rect, rs.matrix, rs.clipRectMatrix))
+        {
+            clipPathImpl(path);
+            return;
+        }
+        if (!rs.hasClipRect)
+        {
+            rs.clipRect = rect;
+            rs.clipRectMatrix = rs.matrix;
+        }
+        else
+        {
+            rs.clipRect = {simd_max(rs.clipRect.l, rect.l), simd_max(rs.clipRect.t, rect.t),
+                           simd_min(rs.clipRect.r, rect.r), simd_min(rs.clipRect.b, rect.b)};
+        }
+        IBox pixelBounds = rs.clipRectMatrix.mapBoundingBox(rs.clipRect).roundOut();
+        rs.overallClipPixelBounds = rs.overallClipPixelBounds.intersect(pixelBounds);
+        rs.hasClipRect = true;
+        rs.clipRectInverse = clip_rect_inverse(rs.clipRectMatrix, rs.clipRect);
+    }
+
+    // RiveRenderer::clipPathImpl (rive_renderer.cpp:323-382).
+    void clipPathImpl(const std::shared_ptr<Path>& path)
+    {
+        RenderState& rs = stack.back();
         FBox pb = M2{}.mapBoundingBox(path->pts.data(), path->pts.size()); // path bounds
         if (!(pb.r - pb.l > 0 && pb.b - pb.t > 0))
         {
@@ -2545,6 +2760,11 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
                     if (c.a >= paths.size())
                         throw PlanError("clip references a missing path");
                     r.clipPath(paths[c.a]);
+                    break;
+                case RIVE_SCENE_CMD_MODULATE_OPACITY:
+                    // RiveRenderer::modulateOpacity (rive_renderer.cpp:115-119)
+                    r.stack.back().modulatedOpacity =
+                        std::max(0.0f, r.stack.back().modulatedOpacity * c.m[0]);
                     break;
                 default:
                     throw PlanError("bad command");

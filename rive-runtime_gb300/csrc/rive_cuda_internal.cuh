@@ -76,6 +76,11 @@ constexpr uint32_t SF_NESTED_CLIPPING = 1u << 5;
 constexpr uint32_t SF_HSL_BLEND_MODES = 1u << 6;
 constexpr uint32_t SF_DITHER = 1u << 7;
 constexpr uint32_t SF_MODULATED_IMAGE = 1u << 8;
+// gpu::ShaderMiscFlags::clockwiseFill (gpu.hpp:917), the one misc flag a
+// rasterOrdering draw batch carries. It travels with each triangle's shader
+// features in bit 15, which ShaderFeatures leaves free.
+constexpr uint32_t MISC_CLOCKWISE_FILL = 1u << 1;
+constexpr uint32_t FEATURE_CLOCKWISE_FILL = 1u << 15;
 
 // Raster tiles: 16x16 by default; 8x8 and 32x32 are the autotuner's other
 // choices (rive_cuda_set_raster_config).

@@ -37,9 +37,10 @@ MAGIC = 0x31435352  # "RSC1"
 
 VERB_MOVE, VERB_LINE, VERB_QUAD, VERB_CUBIC, VERB_CLOSE = 0, 1, 2, 4, 5
 CMD_SAVE, CMD_RESTORE, CMD_TRANSFORM, CMD_DRAW_PATH, CMD_CLIP_PATH = 0, 1, 2, 3, 4
+CMD_MODULATE_OPACITY = 5  # m[0] = opacity (Renderer::modulateOpacity)
 STYLE_STROKE, STYLE_FILL = 0, 1
 SHADER_NONE, SHADER_LINEAR, SHADER_RADIAL = 0, 1, 2
-FILL_NONZERO, FILL_EVENODD = 0, 1
+FILL_NONZERO, FILL_EVENODD, FILL_CLOCKWISE = 0, 1, 2
 JOIN_MITER, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2
 CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
 

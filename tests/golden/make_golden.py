@@ -4,7 +4,9 @@ Each fixture pair is <name>.scene (a seeded rive_scene.h recording written by
 the scene generator) and <name>.cap: what rive-runtime's own, unmodified CPU
 front end (RiveRenderer -> RenderContext, compiled from its sources by
 oracle/Makefile into oracle/_ref/ref_capture) hands its RenderContextImpl for
-that scene. Needs the reference sources, so it runs only where they exist:
+that scene (for the silver_* fixtures, a frame of one of the reference's
+recorded .sriv animations). Needs the reference sources, so it runs only where
+they exist:
 
     python tests/golden/make_golden.py
 """
@@ -52,6 +54,34 @@ SCENES = {
         seed=23, width=512, height=512, n_paths=24, max_cubics=10, p_fill=0.8, p_clip=0.3,
         p_blend=0.3, scale_range=(6.0, 9.0))),
 }
+
+
+# Frames of real content: the reference's own silver renderer-call streams
+# (tests/unit_tests/silvers/*.sriv, recorded by its SerializingFactory while
+# .riv artboards animate), read by rive_runtime_gb300.sriv. Their fills are
+# mostly clockwise (FillRule::clockwise), with clip rects, nested clips,
+# gradients, blend modes and modulated opacity. Draws with feathered paints and
+# image draws are left out of the scenes (not part of this path).
+SILVERS = {
+    "silver_hunter_x_f0": ("hunter_x_demo", 0),
+    "silver_rewards_f10": ("rewards_demo", 10),
+    "silver_spotify_kids_f31": ("spotify_kids_demo", 31),
+    "silver_echo_show_f0": ("echo_show_demo", 0),
+    "silver_path_opacity_f30": ("script_path_opacity", 30),
+    "silver_artboards_opacity_f30": ("script_artboards_opacity", 30),
+}
+SILVER_DIR = os.path.join(oracle.REFERENCE_SOURCES, "tests", "unit_tests", "silvers")
+
+
+def _silver(stream, frame):
+    from rive_runtime_gb300 import sriv
+    with open(os.path.join(SILVER_DIR, stream + ".sriv"), "rb") as f:
+        st = sriv.read_sriv(f.read())
+    return st.frame_scene(frame)[0]
+
+
+for _name, (_stream, _frame) in SILVERS.items():
+    SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k))
 
 
 def _triangulated(sc):
