@@ -343,6 +343,8 @@ def run_ours(args, cap, wname, rank, world):
         line["batched"] = run_batched(args, dev, raster)
     if args.serve_sessions > 0 and world == 1:
         line["serving"] = run_serving(args, dev, raster)
+    if args.serve_rec_sessions > 0 and world == 1:
+        line["serving_recorded"] = run_serving_recorded(args, dev, raster)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -391,6 +393,37 @@ def raster_setup(args, ctx, run, stream):
     t, c = (int(v) for v in args.raster_config.split(","))
     ctx.set_raster_config(t, c)
     return {"tile": t, "ctas_per_sm": c, "autotuned": False}
+
+
+def run_serving_recorded(args, dev, raster=None):
+    """The serving loop on real content: sessions playing the reference's
+    recorded .riv animations (tests/golden/anim, converted from its .sriv
+    streams), each from a random start frame, Poisson arrivals at 50/s."""
+    import glob
+    from rive_runtime_gb300 import rive_cuda, serving, sriv
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "anim")
+    anims, names = [], []
+    for path in sorted(glob.glob(os.path.join(here, "*.rsa"))):
+        with open(path, "rb") as f:
+            anims.append(sriv.unpack_frames(f.read()))
+        names.append(os.path.basename(path)[:-4])
+    sessions = serving.recorded_sessions(anims, args.serve_rec_sessions, 50.0,
+                                         frames=args.serve_rec_frames, fps=args.serve_rec_fps,
+                                         seed=11)
+    ctx = rive_cuda.Context(dev)
+    if raster:
+        ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+    try:
+        server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
+                                     planner_threads=min(16, os.cpu_count() or 1))
+        st = server.run(sessions, timeout_s=600.0)
+    finally:
+        ctx.close()
+    return {"workload": f"serving_recorded_{args.serve_rec_sessions}x{args.serve_rec_frames}",
+            "content": "recorded .riv animations: " + ", ".join(names),
+            "arrivals_per_s": 50.0, "fps_per_session": args.serve_rec_fps,
+            "offered_frames_per_s_at_full_concurrency":
+                args.serve_rec_sessions * args.serve_rec_fps, **st}
 
 
 def run_batched(args, dev, raster=None):
@@ -485,6 +518,10 @@ def main():
     ap.add_argument("--serve-paths", type=int, default=300)
     ap.add_argument("--serve-frames", type=int, default=60)
     ap.add_argument("--serve-fps", type=float, default=8.0)
+    ap.add_argument("--serve-rec-sessions", type=int, default=128,
+                    help="sessions of the recorded-animation serving run (0 = skip)")
+    ap.add_argument("--serve-rec-frames", type=int, default=120)
+    ap.add_argument("--serve-rec-fps", type=float, default=30.0)
     ap.add_argument("--raster-config", default="auto",
                     help='"auto" (autotuned on the workload) or "tile,ctas_per_sm", e.g. "16,0"')
     args = ap.parse_args()

@@ -1,6 +1,9 @@
 """Serving loop: animated sessions rendered with continuous batching.
 
-Each session is one scene (a rive_scene.h recording) animated on the host:
+A session's content is either real (RecordedAnimation: the frames of one of the
+reference's recorded .riv animations, converted by sriv.py) or synthetic
+(AnimatedScene). A synthetic session is one scene (a rive_scene.h recording)
+animated on the host:
 every transform rotates at its own angular rate and every control point of a
 path moves by amplitude * sin(2 pi f t + phi) along a per-path direction. A
 session asks for frames at a fixed rate from its arrival on (frame k is due
@@ -93,6 +96,26 @@ class AnimatedScene:
                 cm[w:w + 6] = m[j].view("<u4")
             del cm
         return bytes(buf)
+
+
+class RecordedAnimation:
+    """Real content: the frames of a recorded animation (scene recordings, as
+    sriv.unpack_frames returns them), played at `rate` frames per second of
+    session time and looped. Frame t is the recording nearest below t."""
+
+    def __init__(self, frames, rate: float = 60.0, offset: int = 0):
+        if not frames:
+            raise ValueError("an animation needs at least one frame")
+        self.frames = list(frames)
+        self.rate = rate
+        self.offset = offset
+        h = HEADER.unpack_from(self.frames[0], 0)
+        assert h[0] == MAGIC
+        self.width, self.height = h[1], h[2]
+
+    def frame(self, t: float) -> bytes:
+        k = int(math.floor(t * self.rate + 1e-6)) + self.offset
+        return self.frames[k % len(self.frames)]
 
 
 @dataclass
@@ -328,6 +351,22 @@ def poisson_sessions(scenes, rate_per_s: float, frames: int, fps: float = 60.0, 
     for i, sc in enumerate(scenes):
         t += rng.exponential(1.0 / rate_per_s)
         out.append(Session(sid=i, anim=AnimatedScene(sc, rng), frames=frames, fps=fps, arrival=t))
+    return out
+
+
+def recorded_sessions(animations, count: int, rate_per_s: float, frames: int,
+                      fps: float = 60.0, seed: int = 0):
+    """`count` sessions, each playing one of `animations` (lists of frame
+    recordings, in turn) from a random start frame, arriving by a Poisson
+    process of `rate_per_s`."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(count):
+        t += rng.exponential(1.0 / rate_per_s)
+        fr = animations[i % len(animations)]
+        anim = RecordedAnimation(fr, rate=fps, offset=int(rng.integers(len(fr))))
+        out.append(Session(sid=i, anim=anim, frames=frames, fps=fps, arrival=t))
     return out
 
 

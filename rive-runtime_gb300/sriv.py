@@ -205,6 +205,34 @@ class SrivStream:
         return sc, st
 
 
+FRAMES_MAGIC = b"RSA1"
+
+
+def pack_frames(frames) -> bytes:
+    """A sequence of scene recordings (rive_scene.h bytes, one per frame) in
+    one compressed container: "RSA1", u32 count, u32 offsets[count + 1] into
+    the zlib-compressed concatenation that follows."""
+    import zlib
+    offs = [0]
+    for f in frames:
+        offs.append(offs[-1] + len(f))
+    head = FRAMES_MAGIC + struct.pack(f"<{len(offs) + 1}I", len(frames), *offs)
+    return head + zlib.compress(b"".join(frames), 9)
+
+
+def unpack_frames(data: bytes) -> list:
+    """The scene recordings of a pack_frames container."""
+    import zlib
+    if data[:4] != FRAMES_MAGIC:
+        raise SrivError("not a frame container")
+    (n,) = struct.unpack_from("<I", data, 4)
+    offs = struct.unpack_from(f"<{n + 1}I", data, 8)
+    body = zlib.decompress(data[8 + 4 * (n + 1):])
+    if len(body) != offs[-1]:
+        raise SrivError("frame container size mismatch")
+    return [body[offs[i]:offs[i + 1]] for i in range(n)]
+
+
 def read_sriv(data: bytes, default_size=None) -> SrivStream:
     """Parses a whole .sriv stream (utils/serialized_replay.cpp reads the same
     layout); raises SrivError on a malformed or truncated stream. A stream

@@ -68,3 +68,58 @@ def test_server_frames_match_frames_rendered_alone():
             alone_ctx.close()
     finally:
         ctx.close()
+
+
+def _recorded():
+    import glob
+    import os
+    from rive_runtime_gb300 import sriv
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "anim")
+    out = {}
+    for path in sorted(glob.glob(os.path.join(here, "*.rsa"))):
+        with open(path, "rb") as f:
+            out[os.path.basename(path)[:-4]] = sriv.unpack_frames(f.read())
+    return out
+
+
+def test_recorded_animations_load_and_plan():
+    anims = _recorded()
+    assert len(anims) >= 5
+    for name, frames in anims.items():
+        a = serving.RecordedAnimation(frames, rate=60.0)
+        assert a.frame(0.0) == frames[0] and a.frame(1.0 / 60.0) == frames[1 % len(frames)]
+        assert a.frame(len(frames) / 60.0) == frames[0]  # loops
+        cap = planner.plan(a.frame(0.5))
+        assert (cap.width, cap.height) == (a.width, a.height) and cap.flushes, name
+
+
+def test_recorded_sessions_cycle_through_animations():
+    anims = list(_recorded().values())
+    ss = serving.recorded_sessions(anims, 10, 50.0, frames=4, fps=30.0, seed=2)
+    assert [s.anim.frames is anims[i % len(anims)] or s.anim.frames == anims[i % len(anims)]
+            for i, s in enumerate(ss)] == [True] * 10
+    assert [s.arrival for s in ss] == sorted(s.arrival for s in ss)
+
+
+@pytest.mark.gpu
+def test_server_recorded_frames_match_frames_rendered_alone():
+    """Real content in the mix: recorded animations of different canvas sizes
+    and clip/blend/clockwise content, each kept frame equal to itself alone."""
+    from rive_runtime_gb300 import rive_cuda
+    anims = list(_recorded().values())
+    sessions = serving.recorded_sessions(anims, 8, 400.0, frames=4, fps=60.0, seed=5)
+    keep = {(s.sid, k) for s in sessions for k in (0, 3)}
+    ctx = rive_cuda.Context(0)
+    try:
+        server = serving.FrameServer(ctx, keep_frames=keep, planner_threads=4)
+        stats = server.run(sessions, timeout_s=120.0)
+        assert stats["frames"] == 8 * 4
+        alone_ctx = rive_cuda.Context(0)
+        try:
+            for (sid, k), img in server.kept.items():
+                want = serving.render_alone(alone_ctx, sessions[sid], k)
+                assert np.array_equal(img, want), (sid, k)
+        finally:
+            alone_ctx.close()
+    finally:
+        ctx.close()
