@@ -188,6 +188,19 @@ int rive_cuda_render_target_read(rive_cuda_context* ctx,
                                   rive_cuda_render_target* target,
                                   void* dst_host,
                                   void* cuda_stream);
+/*
+ * The same copy, enqueued on the stream (the context's when NULL) after the
+ * flushes already there, without waiting for it: a caller that pipelines
+ * frames writes frame k+1's records into the mapped rings while frame k
+ * renders and reads back. dst_host should be page-locked for the copy to run
+ * asynchronously, and must stay valid until rive_cuda_sync on that stream
+ * returns. Later flushes on the same stream may overwrite the target only
+ * after this copy, in stream order.
+ */
+int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
+                                        rive_cuda_render_target* target,
+                                        void* dst_host,
+                                        void* cuda_stream);
 
 /*
  * RenderContextImpl::flush(const gpu::FlushDescriptor&)

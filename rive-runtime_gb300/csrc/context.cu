@@ -1168,6 +1168,19 @@ int rive_cuda_render_target_read(rive_cuda_context* ctx,
     return RIVE_CUDA_OK;
 }
 
+int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
+                                        rive_cuda_render_target* t,
+                                        void* dst,
+                                        void* cuda_stream)
+{
+    if (!ctx || !t || !dst)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "bad read-back arguments");
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4, cudaMemcpyDeviceToHost, s));
+    return RIVE_CUDA_OK;
+}
+
 int rive_cuda_flush(rive_cuda_context* ctx,
                     const rive_cuda_flush_desc* desc,
                     rive_cuda_render_target* target,

@@ -95,6 +95,7 @@ def load():
         "rive_cuda_render_target_destroy": (None, [vp, vp]),
         "rive_cuda_render_target_device_ptr": (vp, [vp]),
         "rive_cuda_render_target_read": (i32, [vp, vp, vp, vp]),
+        "rive_cuda_render_target_read_async": (i32, [vp, vp, vp, vp]),
         "rive_cuda_flush": (i32, [vp, ctypes.POINTER(FlushDesc), vp, vp]),
         "rive_cuda_flush_device": (i32, [vp, ctypes.POINTER(FlushDesc),
                                          ctypes.POINTER(DeviceBuffers), vp, vp]),
@@ -293,6 +294,12 @@ class Context:
         self.check(self.lib.rive_cuda_render_target_read(
             self.h, target, out.ctypes.data_as(ctypes.c_void_p), None), "render_target_read")
         return out
+
+    def read_target_async(self, target, out_ptr: int, stream=None):
+        """Enqueues the read-back into host memory at out_ptr (page-locked for
+        an asynchronous copy; valid until sync(stream))."""
+        self.check(self.lib.rive_cuda_render_target_read_async(
+            self.h, target, ctypes.c_void_p(out_ptr), stream), "render_target_read_async")
 
     def target_device_ptr(self, target):
         return self.lib.rive_cuda_render_target_device_ptr(target)

@@ -104,3 +104,25 @@ def test_repeated_frames_are_identical(ctx):
     a = ctx.render(cap)
     b = ctx.render(cap)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_async_read_back_equals_sync_read_back(ctx):
+    """rive_cuda_render_target_read_async lands the same pixels as the
+    synchronous read once the stream is synced, even with the next frame's
+    flush already enqueued behind it."""
+    import torch
+    cap, _ = load_golden("full_small_s7")
+    other, _ = load_golden("strokes_s3")  # same 256x256 canvas
+    assert (other.width, other.height) == (cap.width, cap.height)
+    t = ctx.render_target(cap.width, cap.height)
+    want = ctx.render(cap, target=t)
+    out = torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8).pin_memory()
+    ctx.read_target_async(t, out.data_ptr())
+    # A later frame on the same stream overwrites the target after the copy.
+    ctx.upload_frame(other)
+    for f in other.flushes:
+        ctx.flush(f, t)
+    ctx.sync()
+    assert np.array_equal(out.numpy(), want)
+    assert not np.array_equal(ctx.read_target(t, cap.width, cap.height), want)
