@@ -76,13 +76,22 @@ typedef struct rive_scene_header
  * frameBudgetMs = 0 and every fill is a midpoint fan. */
 #define RIVE_SCENE_FLAG_TRIANGULATE 1u
 
+/* In rive_scene_path.fill_rule: the path was built the way a replayed call
+ * stream builds it, Factory::makeEmptyRenderPath + RenderPath::addRawPath,
+ * which keeps empty segments; without it the path is made by
+ * Factory::makeRenderPath, which prunes them (RiveRenderPath's constructor,
+ * renderer/src/rive_render_path.cpp:16-21). */
+#define RIVE_SCENE_PATH_APPENDED 0x100u
+#define RIVE_SCENE_FILL_RULE_MASK 0xffu
+
 typedef struct rive_scene_path
 {
     uint32_t verb_offset;
     uint32_t verb_count;
     uint32_t point_offset;
     uint32_t point_count;
-    uint32_t fill_rule; /* rive::FillRule: 0 nonZero, 1 evenOdd, 2 clockwise */
+    uint32_t fill_rule; /* rive::FillRule: 0 nonZero, 1 evenOdd, 2 clockwise,
+                           | RIVE_SCENE_PATH_APPENDED */
 } rive_scene_path;
 
 typedef struct rive_scene_paint

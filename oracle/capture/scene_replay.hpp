@@ -2,11 +2,14 @@
  * scene_replay.hpp -- TEST INFRASTRUCTURE (oracle). Replays a rive_scene.h
  * recording through rive-runtime's own RiveRenderer into any RenderContext:
  * one frame, cleared, midpoint fans only (frameBudgetMs = 0), then flush.
- * Shared by ref_capture.cpp (recording RenderContextImpl) and
- * adapter_capture.cpp (the product's RenderContextCUDAImpl).
+ * Shared by ref_capture.cpp (recording RenderContextImpl),
+ * adapter_capture.cpp (the product's RenderContextCUDAImpl) and
+ * cmdbuf_capture.cpp (the reference's deferred command recorder).
  */
 #pragma once
 
+#include "rive/factory.hpp"
+#include "rive/renderer.hpp"
 #include "rive/renderer/render_context.hpp"
 #include "rive/renderer/rive_renderer.hpp"
 #include "rive/renderer/gpu.hpp"
@@ -21,48 +24,67 @@
 #include <limits>
 #include <vector>
 
-// Returns nullptr on success, else a message. `makeTarget(width, height)`
-// returns the rcp<RenderTarget> to draw into.
-template <class MakeTarget>
-const char* replay_scene(rive::gpu::RenderContext* ctx,
-                         const std::vector<uint8_t>& scene,
-                         MakeTarget makeTarget,
-                         rive::rcp<rive::gpu::RenderTarget>* outTarget = nullptr)
+// The arrays of a rive_scene.h recording, in place.
+struct SceneView
 {
-    using namespace rive;
-    using namespace rive::gpu;
+    rive_scene_header hdr;
+    const rive_scene_path* paths;
+    const rive_scene_paint* paints;
+    const rive_scene_cmd* cmds;
+    const uint8_t* verbs;
+    const float* points;
+    const rive_scene_stop* stops;
+};
+
+// Returns nullptr on success, else a message.
+inline const char* parse_scene(const std::vector<uint8_t>& scene, SceneView* v)
+{
     if (scene.size() < sizeof(rive_scene_header))
         return "cannot read scene";
-    rive_scene_header hdr;
-    memcpy(&hdr, scene.data(), sizeof(hdr));
+    memcpy(&v->hdr, scene.data(), sizeof(v->hdr));
+    const rive_scene_header& hdr = v->hdr;
     if (hdr.magic != RIVE_SCENE_MAGIC)
-        return ("bad scene magic");
+        return "bad scene magic";
     size_t off = sizeof(hdr);
-    auto* paths = reinterpret_cast<const rive_scene_path*>(scene.data() + off);
+    v->paths = reinterpret_cast<const rive_scene_path*>(scene.data() + off);
     off += sizeof(rive_scene_path) * hdr.path_count;
-    auto* paints = reinterpret_cast<const rive_scene_paint*>(scene.data() + off);
+    v->paints = reinterpret_cast<const rive_scene_paint*>(scene.data() + off);
     off += sizeof(rive_scene_paint) * hdr.paint_count;
-    auto* cmds = reinterpret_cast<const rive_scene_cmd*>(scene.data() + off);
+    v->cmds = reinterpret_cast<const rive_scene_cmd*>(scene.data() + off);
     off += sizeof(rive_scene_cmd) * hdr.cmd_count;
-    const uint8_t* verbs = scene.data() + off;
+    v->verbs = scene.data() + off;
     off += (hdr.verb_count + 3u) & ~3u;
-    auto* points = reinterpret_cast<const float*>(scene.data() + off);
+    v->points = reinterpret_cast<const float*>(scene.data() + off);
     off += sizeof(float) * 2 * hdr.point_count;
-    auto* stops = reinterpret_cast<const rive_scene_stop*>(scene.data() + off);
+    v->stops = reinterpret_cast<const rive_scene_stop*>(scene.data() + off);
     off += sizeof(rive_scene_stop) * hdr.stop_count;
     if (off > scene.size())
-        return ("truncated scene");
+        return "truncated scene";
+    return nullptr;
+}
 
+// The scene's paths and paints, made by `factory` (Factory::makeRenderPath,
+// makeRenderPaint, make*Gradient).
+struct SceneResources
+{
+    std::vector<rive::rcp<rive::RenderPath>> paths;
+    std::vector<rive::rcp<rive::RenderPaint>> paints;
+};
 
-    std::vector<rcp<RenderPath>> renderPaths;
+inline const char* make_scene_resources(rive::Factory* factory,
+                                        const SceneView& v,
+                                        SceneResources* out)
+{
+    using namespace rive;
+    const rive_scene_header& hdr = v.hdr;
     for (uint32_t i = 0; i < hdr.path_count; ++i)
     {
-        const rive_scene_path& p = paths[i];
+        const rive_scene_path& p = v.paths[i];
         RawPath raw;
-        const float* pts = points + 2 * p.point_offset;
-        for (uint32_t v = 0; v < p.verb_count; ++v)
+        const float* pts = v.points + 2 * p.point_offset;
+        for (uint32_t k = 0; k < p.verb_count; ++k)
         {
-            switch (verbs[p.verb_offset + v])
+            switch (v.verbs[p.verb_offset + k])
             {
                 case RIVE_SCENE_VERB_MOVE:
                     raw.move({pts[0], pts[1]});
@@ -77,27 +99,34 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
                     pts += 4;
                     break;
                 case RIVE_SCENE_VERB_CUBIC:
-                    raw.cubic({pts[0], pts[1]},
-                              {pts[2], pts[3]},
-                              {pts[4], pts[5]});
+                    raw.cubic({pts[0], pts[1]}, {pts[2], pts[3]}, {pts[4], pts[5]});
                     pts += 6;
                     break;
                 case RIVE_SCENE_VERB_CLOSE:
                     raw.close();
                     break;
                 default:
-                    return ("bad verb");
+                    return "bad verb";
             }
         }
-        renderPaths.push_back(
-            ctx->makeRenderPath(raw, static_cast<FillRule>(p.fill_rule)));
+        const auto fillRule = static_cast<FillRule>(p.fill_rule & RIVE_SCENE_FILL_RULE_MASK);
+        if (p.fill_rule & RIVE_SCENE_PATH_APPENDED)
+        {
+            // As a replayed call stream builds it: no pruning.
+            rcp<RenderPath> path = factory->makeEmptyRenderPath();
+            path->fillRule(fillRule);
+            path->addRawPath(raw);
+            out->paths.push_back(path);
+        }
+        else
+        {
+            out->paths.push_back(factory->makeRenderPath(raw, fillRule));
+        }
     }
-
-    std::vector<rcp<RenderPaint>> renderPaints;
     for (uint32_t i = 0; i < hdr.paint_count; ++i)
     {
-        const rive_scene_paint& s = paints[i];
-        rcp<RenderPaint> paint = ctx->makeRenderPaint();
+        const rive_scene_paint& s = v.paints[i];
+        rcp<RenderPaint> paint = factory->makeRenderPaint();
         paint->style(s.style == RIVE_SCENE_STYLE_FILL ? RenderPaintStyle::fill
                                                       : RenderPaintStyle::stroke);
         paint->color(s.color);
@@ -111,74 +140,108 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
             std::vector<float> pos(s.stop_count);
             for (uint32_t k = 0; k < s.stop_count; ++k)
             {
-                colors[k] = stops[s.stop_offset + k].color;
-                pos[k] = stops[s.stop_offset + k].position;
+                colors[k] = v.stops[s.stop_offset + k].color;
+                pos[k] = v.stops[s.stop_offset + k].position;
             }
             rcp<RenderShader> shader =
                 s.shader == RIVE_SCENE_SHADER_LINEAR
-                    ? ctx->makeLinearGradient(s.g[0],
-                                              s.g[1],
-                                              s.g[2],
-                                              s.g[3],
-                                              colors.data(),
-                                              pos.data(),
-                                              s.stop_count)
-                    : ctx->makeRadialGradient(s.g[0],
-                                              s.g[1],
-                                              s.g[2],
-                                              colors.data(),
-                                              pos.data(),
-                                              s.stop_count);
+                    ? factory->makeLinearGradient(s.g[0], s.g[1], s.g[2], s.g[3], colors.data(),
+                                                  pos.data(), s.stop_count)
+                    : factory->makeRadialGradient(s.g[0], s.g[1], s.g[2], colors.data(),
+                                                  pos.data(), s.stop_count);
             paint->shader(shader);
         }
-        renderPaints.push_back(paint);
+        out->paints.push_back(paint);
     }
+    return nullptr;
+}
 
-    rcp<RenderTarget> target = makeTarget(hdr.width, hdr.height);
+// The scene's Renderer calls, in order.
+inline const char* issue_scene_commands(rive::Renderer* renderer,
+                                        const SceneView& v,
+                                        const SceneResources& res)
+{
+    using namespace rive;
+    for (uint32_t i = 0; i < v.hdr.cmd_count; ++i)
+    {
+        const rive_scene_cmd& c = v.cmds[i];
+        switch (c.op)
+        {
+            case RIVE_SCENE_CMD_SAVE:
+                renderer->save();
+                break;
+            case RIVE_SCENE_CMD_RESTORE:
+                renderer->restore();
+                break;
+            case RIVE_SCENE_CMD_TRANSFORM:
+                renderer->transform(Mat2D(c.m[0], c.m[1], c.m[2], c.m[3], c.m[4], c.m[5]));
+                break;
+            case RIVE_SCENE_CMD_DRAW_PATH:
+                if (c.a >= res.paths.size() || c.b >= res.paints.size())
+                    return "draw references a missing path or paint";
+                renderer->drawPath(res.paths[c.a].get(), res.paints[c.b].get());
+                break;
+            case RIVE_SCENE_CMD_CLIP_PATH:
+                if (c.a >= res.paths.size())
+                    return "clip references a missing path";
+                renderer->clipPath(res.paths[c.a].get());
+                break;
+            case RIVE_SCENE_CMD_MODULATE_OPACITY:
+                renderer->modulateOpacity(c.m[0]);
+                break;
+            default:
+                return "bad command";
+        }
+    }
+    return nullptr;
+}
+
+// The frame every capture tool renders: cleared to the scene's colour,
+// midpoint fans for every fill, or (flag) every eligible fill triangulated;
+// both are independent of timing.
+inline rive::gpu::RenderContext::FrameDescriptor scene_frame(uint32_t width,
+                                                             uint32_t height,
+                                                             uint32_t clearColor,
+                                                             uint32_t ditherMode,
+                                                             uint32_t flags)
+{
+    using namespace rive::gpu;
+    RenderContext::FrameDescriptor fd;
+    fd.renderTargetWidth = width;
+    fd.renderTargetHeight = height;
+    fd.loadAction = LoadAction::clear;
+    fd.clearColor = clearColor;
+    fd.ditherMode = static_cast<DitherMode>(ditherMode);
+    fd.triangulationThresholds.frameBudgetMs =
+        (flags & RIVE_SCENE_FLAG_TRIANGULATE) ? std::numeric_limits<float>::infinity() : 0.f;
+    return fd;
+}
+
+// Returns nullptr on success, else a message. `makeTarget(width, height)`
+// returns the rcp<RenderTarget> to draw into.
+template <class MakeTarget>
+const char* replay_scene(rive::gpu::RenderContext* ctx,
+                         const std::vector<uint8_t>& scene,
+                         MakeTarget makeTarget,
+                         rive::rcp<rive::gpu::RenderTarget>* outTarget = nullptr)
+{
+    using namespace rive;
+    using namespace rive::gpu;
+    SceneView v;
+    if (const char* err = parse_scene(scene, &v))
+        return err;
+    SceneResources res;
+    if (const char* err = make_scene_resources(ctx, v, &res))
+        return err;
+    rcp<RenderTarget> target = makeTarget(v.hdr.width, v.hdr.height);
     if (!target)
         return "cannot make the render target";
-    RenderContext::FrameDescriptor fd;
-    fd.renderTargetWidth = hdr.width;
-    fd.renderTargetHeight = hdr.height;
-    fd.loadAction = LoadAction::clear;
-    fd.clearColor = hdr.clear_color;
-    fd.ditherMode = static_cast<DitherMode>(hdr.dither_mode);
-    // Midpoint fans for every fill, or (flag) triangulate every eligible fill;
-    // both are independent of timing.
-    fd.triangulationThresholds.frameBudgetMs =
-        (hdr.flags & RIVE_SCENE_FLAG_TRIANGULATE) ? std::numeric_limits<float>::infinity() : 0.f;
-    ctx->beginFrame(fd);
+    ctx->beginFrame(
+        scene_frame(v.hdr.width, v.hdr.height, v.hdr.clear_color, v.hdr.dither_mode, v.hdr.flags));
     {
         RiveRenderer renderer(ctx);
-        for (uint32_t i = 0; i < hdr.cmd_count; ++i)
-        {
-            const rive_scene_cmd& c = cmds[i];
-            switch (c.op)
-            {
-                case RIVE_SCENE_CMD_SAVE:
-                    renderer.save();
-                    break;
-                case RIVE_SCENE_CMD_RESTORE:
-                    renderer.restore();
-                    break;
-                case RIVE_SCENE_CMD_TRANSFORM:
-                    renderer.transform(
-                        Mat2D(c.m[0], c.m[1], c.m[2], c.m[3], c.m[4], c.m[5]));
-                    break;
-                case RIVE_SCENE_CMD_DRAW_PATH:
-                    renderer.drawPath(renderPaths[c.a].get(),
-                                      renderPaints[c.b].get());
-                    break;
-                case RIVE_SCENE_CMD_CLIP_PATH:
-                    renderer.clipPath(renderPaths[c.a].get());
-                    break;
-                case RIVE_SCENE_CMD_MODULATE_OPACITY:
-                    renderer.modulateOpacity(c.m[0]);
-                    break;
-                default:
-                    return ("bad command");
-            }
-        }
+        if (const char* err = issue_scene_commands(&renderer, v, res))
+            return err;
     }
     ctx->flush({.renderTarget = target.get()});
     if (outTarget)

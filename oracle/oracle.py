@@ -181,6 +181,40 @@ def build_reference():
     subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"])
 
 
+CMDBUF_CAPTURE = os.path.join(HERE, "_ref", "cmdbuf_capture")
+
+
+def build_cmdbuf_tool() -> str:
+    """Builds (if needed) the reference's deferred command recorder/replayer
+    tool (oracle/capture/cmdbuf_capture.cpp); returns its path."""
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "cmdbuf"])
+    return CMDBUF_CAPTURE
+
+
+def cmdbuf_record(scene_bytes: bytes) -> bytes:
+    """The reference's DeferredFactory recording of a scene (.rcb bytes)."""
+    tool = build_cmdbuf_tool()
+    with tempfile.TemporaryDirectory() as td:
+        sp, rp = os.path.join(td, "scene.bin"), os.path.join(td, "s.rcb")
+        with open(sp, "wb") as f:
+            f.write(scene_bytes)
+        subprocess.check_call([tool, "record", sp, rp])
+        with open(rp, "rb") as f:
+            return f.read()
+
+
+def cmdbuf_replay(rcb_bytes: bytes) -> bytes:
+    """The reference's replayRenderCommands of a stored stream, captured."""
+    tool = build_cmdbuf_tool()
+    with tempfile.TemporaryDirectory() as td:
+        rp, cp = os.path.join(td, "s.rcb"), os.path.join(td, "capture.bin")
+        with open(rp, "wb") as f:
+            f.write(rcb_bytes)
+        subprocess.check_call([tool, "replay", rp, cp])
+        with open(cp, "rb") as f:
+            return f.read()
+
+
 def _run_capture(tool: str, scene_bytes: bytes) -> bytes:
     with tempfile.TemporaryDirectory() as td:
         sp = os.path.join(td, "scene.bin")

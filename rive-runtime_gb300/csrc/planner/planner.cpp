@@ -2656,7 +2656,7 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
             (size_t)sp.point_offset + sp.point_count > hdr.point_count)
             throw PlanError("path out of range");
         auto p = std::make_shared<Path>();
-        p->fillRule = sp.fill_rule;
+        p->fillRule = sp.fill_rule & RIVE_SCENE_FILL_RULE_MASK;
         p->id = i + 1;
         // RawPath::move/line/cubic/close with implicit moves.
         bool open = false;
@@ -2699,7 +2699,10 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
             }
             pp += adv;
         }
-        prune_empty_segments(*p);
+        // Factory::makeRenderPath prunes; makeEmptyRenderPath + addRawPath
+        // (rive_render_path.cpp:16-21, 115-120) keeps empty segments.
+        if (!(sp.fill_rule & RIVE_SCENE_PATH_APPENDED))
+            prune_empty_segments(*p);
         paths.push_back(p);
     }
     std::vector<Paint> paints;

@@ -41,6 +41,7 @@ CMD_MODULATE_OPACITY = 5  # m[0] = opacity (Renderer::modulateOpacity)
 STYLE_STROKE, STYLE_FILL = 0, 1
 SHADER_NONE, SHADER_LINEAR, SHADER_RADIAL = 0, 1, 2
 FILL_NONZERO, FILL_EVENODD, FILL_CLOCKWISE = 0, 1, 2
+PATH_APPENDED = 0x100  # rive_scene_path.fill_rule flag
 JOIN_MITER, JOIN_ROUND, JOIN_BEVEL = 0, 1, 2
 CAP_BUTT, CAP_ROUND, CAP_SQUARE = 0, 1, 2
 
@@ -59,6 +60,9 @@ class Path:
     verbs: list
     points: np.ndarray  # float32 (n, 2)
     fill_rule: int = FILL_NONZERO
+    # Built by makeEmptyRenderPath + addRawPath (a replayed call stream):
+    # empty segments are kept instead of pruned.
+    appended: bool = False
 
 
 @dataclass
@@ -105,7 +109,7 @@ class Scene:
         for p in self.paths:
             pa = np.asarray(p.points, dtype=np.float32).reshape(-1, 2)
             path_recs.append(struct.pack("<5I", len(verbs), len(p.verbs), npts,
-                                         len(pa), p.fill_rule))
+                                         len(pa), p.fill_rule | (PATH_APPENDED if p.appended else 0)))
             verbs.extend(bytes(p.verbs))
             pts.append(pa)
             npts += len(pa)

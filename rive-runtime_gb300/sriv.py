@@ -165,7 +165,9 @@ class SrivStream:
             key = snap[0]
             if key not in path_ix:
                 _, verbs, pts, fill_rule = snap
-                path_ix[key] = sc.add_path(S.Path(verbs, pts, fill_rule))
+                # The reference's replay builds every path with
+                # makeEmptyRenderPath + addRawPath.
+                path_ix[key] = sc.add_path(S.Path(verbs, pts, fill_rule, appended=True))
             return path_ix[key]
 
         def paint_of(snap):
