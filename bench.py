@@ -340,6 +340,9 @@ def run_ours(args, cap, wname, rank, world):
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": traffic},
         "stage_ms_per_frame": {k: v[0] / args.steps for k, v in prof.items()},
+        # Tessellated vertices per second of the tessellation stage.
+        "tess_vertices_per_s": (counts["tess_vertices"] * args.steps / (prof["tessellate"][0] / 1e3)
+                                if prof["tessellate"][0] > 0 else None),
         "gpu_launches": int(sum(v[1] for v in prof.values())),
         "clocks": clocks,
     }
