@@ -351,6 +351,7 @@ def run_ours(args, cap, wname, rank, world):
     # The batched and serving measurements are single-GPU (rank 0 of N=1).
     if args.batch_scenes > 0 and world == 1:
         line["batched"] = run_batched(args, dev, raster)
+        line["batched_recorded"] = run_batched(args, dev, raster, recorded=True)
     if args.serve_sessions > 0 and world == 1:
         line["serving"] = run_serving(args, dev, raster)
     if args.serve_rec_sessions > 0 and world == 1:
@@ -436,18 +437,40 @@ def run_serving_recorded(args, dev, raster=None):
                 args.serve_rec_sessions * args.serve_rec_fps, **st}
 
 
-def run_batched(args, dev, raster=None):
+def recorded_caps(count):
+    """`count` frames of the recorded .riv animations (tests/golden/anim),
+    taken in turn from each animation, planned."""
+    import glob
+    from rive_runtime_gb300 import planner, sriv
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "anim")
+    anims = []
+    for path in sorted(glob.glob(os.path.join(here, "*.rsa"))):
+        with open(path, "rb") as f:
+            anims.append(sriv.unpack_frames(f.read()))
+    caps = []
+    for i in range(count):
+        fr = anims[i % len(anims)]
+        caps.append(planner.plan(fr[(i // len(anims)) % len(fr)]))
+    return caps
+
+
+def run_batched(args, dev, raster=None, recorded=False):
     """The batched form: N independent scenes of uneven canvas sizes and path
-    counts (scene.batched_scenes), rendered (a) one flush at a time, (b) as
-    one rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch
-    per flush index. Frames/s counts scenes; each pass renders every scene
-    once, with the records resident in HBM."""
+    counts (scene.batched_scenes; or, `recorded`, frames of the recorded .riv
+    animations), rendered (a) one flush at a time, (b) as one
+    rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch per
+    flush index. Frames/s counts scenes; each pass renders every scene once,
+    with the records resident in HBM."""
     import numpy as np
     import torch
     from rive_runtime_gb300 import planner, rive_cuda, scene
     from rive_runtime_gb300.capture import BUFFER_NAMES
 
-    caps = [planner.plan(sc.to_bytes()) for sc in scene.batched_scenes(count=args.batch_scenes)]
+    if recorded:
+        caps = recorded_caps(args.batch_scenes)
+    else:
+        caps = [planner.plan(sc.to_bytes())
+                for sc in scene.batched_scenes(count=args.batch_scenes)]
     stream = torch.cuda.current_stream()
     keep, bufs, targets = [], [], []
     for cap in caps:
@@ -498,7 +521,8 @@ def run_batched(args, dev, raster=None):
     ctx.close()
     n = len(caps)
     px = sum(c.width * c.height for c in caps)
-    return {"workload": f"batched_{n}", "scenes": n, "mpx": px / 1e6,
+    return {"workload": f"batched_{'recorded_' if recorded else ''}{n}", "scenes": n,
+            "mpx": px / 1e6,
             "paths": int(sum(f.desc["path_count"] for c in caps for f in c.flushes)),
             "flushes": int(sum(len(c.flushes) for c in caps)),
             "bin_entries_last_wave": int(entries),

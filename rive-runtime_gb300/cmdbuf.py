@@ -264,8 +264,16 @@ class CommandStreamReader:
             pb = blob_at(po, 8 * npts)
             if vb is None or pb is None:
                 return [], np.zeros((0, 2), np.float32)
+            verbs = list(vb)
+            need = 0
+            for v in verbs:
+                if v not in _VERB_POINTS:
+                    raise CmdbufError(f"bad path verb {v}")
+                need += _VERB_POINTS[v]
+            if need != npts:
+                raise CmdbufError(f"path verbs need {need} points, the stream has {npts}")
             pts = np.frombuffer(pb, "<f4").reshape(-1, 2).astype(np.float32)
-            return list(vb), pts
+            return verbs, pts
 
         def scene_path(p: _Path):
             key = (p.serial, p.mutation)

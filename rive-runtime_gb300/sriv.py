@@ -298,6 +298,8 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
             rule = r.varuint()
             if pid not in paths:
                 raise SrivError(f"unknown path {pid}")
+            if rule > S.FILL_CLOCKWISE:
+                raise SrivError(f"bad fill rule {rule}")
             paths[pid].fill_rule = rule
             bump(paths[pid])
         elif op == OP_ADD_RAW_PATH:
@@ -325,6 +327,8 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
         elif op in (OP_COLOR, OP_STYLE, OP_JOIN, OP_CAP, OP_BLEND_MODE):
             q = paint(r.varuint())
             v = r.varuint()
+            if op in (OP_JOIN, OP_CAP) and v > 2 or op == OP_BLEND_MODE and v > 28:
+                raise SrivError(f"bad paint value {v} for opcode {op}")
             if op == OP_COLOR:
                 q.color = v & 0xFFFFFFFF
             elif op == OP_STYLE:
