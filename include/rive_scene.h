@@ -106,6 +106,7 @@ typedef struct rive_scene_paint
     float g[4];          /* linear: sx, sy, ex, ey; radial: cx, cy, r, 0 */
     uint32_t stop_offset;
     uint32_t stop_count;
+    float feather;       /* RenderPaint::feather (blur width; 0 = none) */
 } rive_scene_paint;
 
 typedef struct rive_scene_cmd

@@ -134,6 +134,8 @@ inline const char* make_scene_resources(rive::Factory* factory,
         paint->join(static_cast<StrokeJoin>(s.join));
         paint->cap(static_cast<StrokeCap>(s.cap));
         paint->blendMode(static_cast<BlendMode>(s.blend_mode));
+        if (s.feather != 0)
+            paint->feather(s.feather);
         if (s.shader != RIVE_SCENE_SHADER_NONE)
         {
             std::vector<ColorInt> colors(s.stop_count);

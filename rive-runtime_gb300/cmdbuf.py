@@ -16,7 +16,8 @@ the same frame gets a new version; draws name the version they saw) and
 destroyed by generation exactly as the replay does. Draws the replay would
 drop (unresolved ids, content between canvas brackets, which needs a host
 canvas) are dropped, and image draws and draws with feathered paints, which
-this path does not render, are left out; all are counted in `CmdbufStats`.
+this path does not render, are left out (feathered ones are kept with
+`keep_feathered`); all are counted in `CmdbufStats`.
 
 The payload layouts are the C structs' natural layouts (little-endian,
 explicit padding); `POD_FORMATS` lists them by opcode.
@@ -231,11 +232,13 @@ class CommandStreamReader:
         self._walk(commands, blobs, None, None)
 
     def frame_scene(self, commands: bytes, blobs: bytes, width: int, height: int,
-                    clear_color: int = 0, dither_mode: int = S.DITHER_IGN, flags: int = 0):
+                    clear_color: int = 0, dither_mode: int = S.DITHER_IGN, flags: int = 0,
+                    keep_feathered: bool = False):
         """One frame's stream as (scene.Scene, CmdbufStats)."""
         sc = S.Scene(width, height, clear_color=clear_color, dither_mode=dither_mode,
                      flags=flags)
         st = CmdbufStats()
+        self.keep_feathered = keep_feathered
         self._walk(commands, blobs, sc, st)
         return sc, st
 
@@ -286,7 +289,8 @@ class CommandStreamReader:
             key = (q.serial, q.mutation)
             if key not in paint_ix:
                 p = S.Paint(style=S.STYLE_FILL if q.style == 1 else S.STYLE_STROKE, color=q.color,
-                            thickness=q.thickness, join=q.join, cap=q.cap, blend_mode=q.blend_mode)
+                            thickness=q.thickness, join=q.join, cap=q.cap, blend_mode=q.blend_mode,
+                            feather=q.feather)
                 if q.shader is not None:
                     kind, stops, g = q.shader
                     p.shader, p.stops, p.g = kind, list(stops), tuple(g)
@@ -454,7 +458,7 @@ class CommandStreamReader:
                 if p is None or q is None:
                     st.dropped_unresolved += 1
                     continue
-                if q.feather != 0:
+                if q.feather != 0 and not getattr(self, "keep_feathered", False):
                     st.dropped_feathered += 1
                     continue
                 st.draws += 1

@@ -2709,6 +2709,8 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
     for (uint32_t i = 0; i < hdr.paint_count; ++i)
     {
         const rive_scene_paint& s = spaints[i];
+        if (s.feather != 0)
+            throw PlanError("feathered paints are not planned here (the reference front end plans them)");
         Paint q;
         q.stroked = s.style == RIVE_SCENE_STYLE_STROKE;
         q.type = PT_SOLID;

@@ -76,6 +76,7 @@ class Paint:
     shader: int = SHADER_NONE
     g: tuple = (0.0, 0.0, 0.0, 0.0)
     stops: list = field(default_factory=list)  # [(pos, color)]
+    feather: float = 0.0  # RenderPaint::feather
 
 
 @dataclass
@@ -116,9 +117,9 @@ class Scene:
         paint_recs = []
         for q in self.paints:
             paint_recs.append(struct.pack(
-                "<IIfIIII4fII", q.style, q.color & 0xFFFFFFFF, q.thickness,
+                "<IIfIIII4fIIf", q.style, q.color & 0xFFFFFFFF, q.thickness,
                 q.join, q.cap, q.blend_mode, q.shader, *[float(v) for v in q.g],
-                len(stops), len(q.stops)))
+                len(stops), len(q.stops), float(q.feather)))
             stops.extend(q.stops)
         cmd_recs = [struct.pack("<3I6f", op, a, b, *m) for (op, a, b, m) in self.cmds]
         header = struct.pack("<12I", MAGIC, self.width, self.height,

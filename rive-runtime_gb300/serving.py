@@ -41,7 +41,7 @@ from .scene import CMD_TRANSFORM, MAGIC, Scene
 
 HEADER = struct.Struct("<12I")
 PATH_REC = 20
-PAINT_REC = 52
+PAINT_REC = 56
 CMD_REC = 36
 ALIGN = 256
 

@@ -17,8 +17,9 @@ per frame, as a test harness that calls Artboard::draw once per frame leaves
 it (every draw is bracketed by save/restore).
 
 What the scene format does not carry is dropped and counted in `FrameStats`:
-image draws and image meshes (no image paints behind this boundary) and draws
-with a feathered paint (feathering is not part of this path).
+image draws and image meshes (no image paints behind this boundary). Draws
+with a feathered paint are dropped and counted too unless `keep_feathered`
+(the backend renders feathered strokes; feathered fills are refused).
 """
 from __future__ import annotations
 
@@ -155,7 +156,7 @@ class SrivStream:
     shaders: dict  # id -> (kind, stops [(pos, color)], g4)
 
     def frame_scene(self, k: int, clear_color: int = 0x00000000,
-                    dither_mode: int = S.DITHER_IGN):
+                    dither_mode: int = S.DITHER_IGN, keep_feathered: bool = False):
         """Frame k as a scene.Scene plus its FrameStats."""
         sc = S.Scene(self.width, self.height, clear_color=clear_color, dither_mode=dither_mode)
         st = FrameStats()
@@ -176,7 +177,7 @@ class SrivStream:
                 q = snap[1]
                 p = S.Paint(style=S.STYLE_STROKE if q.stroked else S.STYLE_FILL,
                             color=q.color, thickness=q.thickness, join=q.join, cap=q.cap,
-                            blend_mode=q.blend_mode)
+                            blend_mode=q.blend_mode, feather=q.feather)
                 sh = self.shaders.get(q.shader) if q.shader is not None else None
                 if sh is not None:
                     kind, stops, g = sh
@@ -197,7 +198,7 @@ class SrivStream:
                 st.clips += 1
                 sc.cmd(S.CMD_CLIP_PATH, path_of(c.a))
             elif c.op == OP_DRAW_PATH:
-                if c.b[1].feather != 0:
+                if c.b[1].feather != 0 and not keep_feathered:
                     st.dropped_feathered += 1
                     continue
                 st.draws += 1
