@@ -364,6 +364,15 @@ int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
 int rive_cuda_graph_stats(const rive_cuda_graph* graph, rive_cuda_flush_stats* out);
 
 /*
+ * The 512 fp16 entries of the feather table the passes sample (the integral of
+ * the normal distribution over -3..+3 standard deviations; the reference ships
+ * the same table as gpu::g_gaussianIntegralTableF16, gpu.hpp:2083-2091).
+ * Feathered strokes (ENABLE_FEATHER in midpoint-fan batches) are rendered;
+ * feathered fills (midpointFanCenterAAPatches, the feather atlas) are not.
+ */
+int rive_cuda_feather_table(uint16_t* out);
+
+/*
  * Raster configuration of the context's later flushes, batches and graphs
  * (no counterpart in the reference): the tile size (8, 16 or 32 pixels; 16
  * by default) and, for 8 and 16, a limit on resident raster CTAs per SM (0:

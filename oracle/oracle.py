@@ -165,6 +165,13 @@ def last_stats():
     return t.value, fr.value
 
 
+def feather_table():
+    """The oracle's 512-entry fp16 feather table (uint16 bits)."""
+    out = np.zeros(512, np.uint16)
+    lib().oracle_feather_table(out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
 def f32_to_f16(x):
     return lib().oracle_f32_to_f16(float(x))
 

@@ -86,6 +86,11 @@
 #define SF_CLIP_RECT (1u << 1)
 #define SF_ADVANCED_BLEND (1u << 2)
 #define SF_FEATHER (1u << 3)
+/* Feathering (constants.glsl:19-43, draw_path_common.glsl:7-13). */
+#define GAUSSIAN_TABLE_SIZE 512
+#define GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS 3.f
+#define FEATHER_COVERAGE_BIAS -2.f
+#define FEATHER_COVERAGE_THRESHOLD -1.5f
 #define SF_EVEN_ODD (1u << 4)
 /* gpu::ShaderMiscFlags::clockwiseFill of a draw batch (gpu.hpp:917), carried
  * with each triangle's shader features in a bit ShaderFeatures leaves free. */
@@ -946,8 +951,8 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     f2 translate = {path[4], path[5]};
     float strokeRadius = path[6];
     float featherRadius = path[7];
-    if (featherRadius != 0.f)
-        return -2;
+    if (featherRadius != 0.f && strokeRadius == 0.f)
+        return -2; /* feathered fills: midpointFanCenterAA patches, not built */
     uint32_t mirroredContourFlag =
         contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG;
     if (mirroredContourFlag)
@@ -990,6 +995,15 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     float cov[2] = {0.f, 0.f};
     o->discard = 0;
 
+    if (featherRadius != 0.f)
+    {
+        /* draw_path_common.glsl:474-485: never feather harder than 1.5
+         * standard deviations across half a pixel. */
+        f2 mn = mat_mul(M, norm);
+        featherRadius = maxf(featherRadius, (GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS / 3.f) /
+                                                sqrtf(dot2(mn, mn)));
+    }
+
     if (strokeRadius != 0.f)
     {
         float detM = M[0] * M[3] - M[2] * M[1];
@@ -998,9 +1012,10 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
             outset = minf(outset, 0.f);
         if (contourIDWithFlags & RIGHT_JOIN_CONTOUR_FLAG)
             outset = maxf(outset, 0.f);
-        float aaRadius = manhattan_pixel_width(M, norm) * AA_RADIUS;
+        float aaRadius = featherRadius != 0.f ? featherRadius
+                                              : manhattan_pixel_width(M, norm) * AA_RADIUS;
         float globalCoverage = 1.f;
-        if (aaRadius > strokeRadius)
+        if (aaRadius > strokeRadius && featherRadius == 0.f)
         {
             globalCoverage = strokeRadius / aaRadius;
             strokeRadius = aaRadius;
@@ -1083,6 +1098,8 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
         cov[0] *= globalCoverage;
         cov[1] *= globalCoverage;
         cov[1] = maxf(cov[1], 1e-4f);
+        if (featherRadius != 0.f)
+            cov[0] = FEATHER_COVERAGE_BIAS - cov[0]; /* marks a feathered stroke */
         postTransformVertexOffset = mat_mul(M, mul2(vertexOffset, outset));
         if (vertexType != STROKE_VERTEX)
             o->discard = 1;
@@ -1150,6 +1167,104 @@ static inline uint16_t id_bits_to_f16(uint32_t idBits, uint32_t granularity)
     return idBits == 0 ? 0 : (uint16_t)((idBits + MAX_DENORM_F16) * granularity);
 }
 static inline float h2f(uint16_t h) { return oracle_f16_to_f32(h); }
+
+/* ---- Feather lookup table ------------------------------------------------
+ * The integral of the normal distribution over -3..+3 standard deviations in
+ * 512 fp16 entries, the R16F texture the feather passes sample with a linear
+ * filter (constants.glsl:19-26, gpu.hpp:2083-2091). Restated from its
+ * generator (renderer/src/gpu.cpp:1983-2062): 7 samples per entry of the
+ * normal distribution, shifted so the middle is exactly 1/2, made monotonic
+ * and clamped to [0, 1], with an 8-entry ease to 0 and 1 at the ends. */
+static uint16_t g_feather16[GAUSSIAN_TABLE_SIZE];
+static float g_feather[GAUSSIAN_TABLE_SIZE];
+static int g_featherReady;
+
+static float eval_normal_distribution(float x, float mu, float inverseSigma)
+{
+    const float ONE_OVER_SQRT_2_PI = 0.398942280401433f;
+    float y = (x - mu) * inverseSigma;
+    return expf(-.5 * y * y) * inverseSigma * ONE_OVER_SQRT_2_PI;
+}
+
+static void build_feather_table(void)
+{
+    if (g_featherReady)
+        return;
+    float table[GAUSSIAN_TABLE_SIZE];
+    float sigma = GAUSSIAN_TABLE_SIZE / (GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS * 2);
+    float inverseSigma = 1 / sigma;
+    float mu = GAUSSIAN_TABLE_SIZE * .5f;
+    float integral = 0;
+    for (int i = 0; i < GAUSSIAN_TABLE_SIZE; ++i)
+    {
+        const int SAMPLES = 7;
+        float barCenterX = (float)i;
+        for (int sample = 0; sample < SAMPLES; ++sample)
+        {
+            float dx = (float)(sample - (SAMPLES >> 1)) / SAMPLES;
+            integral += eval_normal_distribution(barCenterX + dx, mu, inverseSigma) / SAMPLES;
+        }
+        table[i] = integral;
+    }
+    float shift = .5 - (table[GAUSSIAN_TABLE_SIZE / 2 - 1] + table[GAUSSIAN_TABLE_SIZE / 2]) / 2;
+    table[0] = fminf(fmaxf(0, table[0] + shift), 1);
+    for (int i = 1; i < GAUSSIAN_TABLE_SIZE; ++i)
+        table[i] = fminf(fmaxf(table[i - 1], table[i] + shift), 1);
+    const int EASE = 8;
+    for (int i = 0; i < GAUSSIAN_TABLE_SIZE; ++i)
+    {
+        if (i < EASE)
+            table[i] *= (float)i / (float)EASE;
+        if (i > (GAUSSIAN_TABLE_SIZE - EASE) - 1)
+        {
+            float diffToOne = 1.0 - table[i];
+            float fi = (float)(i - (GAUSSIAN_TABLE_SIZE - EASE) + 1) / (float)EASE;
+            table[i] = table[i] + (diffToOne * fi);
+        }
+    }
+    for (int i = 0; i < GAUSSIAN_TABLE_SIZE; ++i)
+    {
+        g_feather16[i] = oracle_f32_to_f16(table[i]);
+        g_feather[i] = oracle_f16_to_f32(g_feather16[i]);
+    }
+    g_featherReady = 1;
+}
+
+void oracle_feather_table(uint16_t* out)
+{
+    build_feather_table();
+    memcpy(out, g_feather16, sizeof(g_feather16));
+}
+
+
+/* FEATHER(x) (common.glsl:53-60): the table sampled at normalised x with a
+ * linear filter and clamp-to-edge addressing. */
+static float feather_lut(float x)
+{
+    float t = x * GAUSSIAN_TABLE_SIZE - .5f;
+    if (!(t == t))
+        return g_feather[0];
+    float f = floorf(t);
+    float w = t - f;
+    float fc = fminf(fmaxf(f, -1.f), (float)GAUSSIAN_TABLE_SIZE);
+    int i0 = (int)fc;
+    int a = i0 < 0 ? 0 : (i0 > GAUSSIAN_TABLE_SIZE - 1 ? GAUSSIAN_TABLE_SIZE - 1 : i0);
+    int b = i0 + 1 < 0 ? 0 : (i0 + 1 > GAUSSIAN_TABLE_SIZE - 1 ? GAUSSIAN_TABLE_SIZE - 1 : i0 + 1);
+    return g_feather[a] + (g_feather[b] - g_feather[a]) * w;
+}
+
+/* eval_feathered_stroke (draw_path_common.glsl:242-258):
+ * 1 - feather(1 - leftCoverage) - feather(1 - rightCoverage), with the left
+ * coverage carried biased by FEATHER_COVERAGE_BIAS. */
+static float eval_feathered_stroke(float covx, float covy)
+{
+    float featherCoverage = 1.f;
+    float leftOutsideCoverage = (1.f - FEATHER_COVERAGE_BIAS) + covx;
+    featherCoverage -= feather_lut(leftOutsideCoverage);
+    float rightOutsideCoverage = 1.f - covy;
+    featherCoverage -= feather_lut(rightOutsideCoverage);
+    return featherCoverage;
+}
 
 /* advanced_blend.glsl:94-154 */
 static float lum_from_rgb(const float c[3])
@@ -1387,7 +1502,13 @@ static void fragment(const frag_ctx* fc,
     else
     {
         if (covy >= 0.f) /* stroke */
-            coverageCount = maxf(minf(covx, covy), coverageCount);
+        {
+            /* find_stroke_coverage (draw_path.vert:501-509) */
+            float frag = ((features & SF_FEATHER) && covx < FEATHER_COVERAGE_THRESHOLD)
+                             ? eval_feathered_stroke(covx, covy)
+                             : minf(covx, covy);
+            coverageCount = maxf(frag, coverageCount);
+        }
         else
             coverageCount = coverageCount + covx;
         uint16_t storedCount = oracle_f32_to_f16(coverageCount);
@@ -1744,6 +1865,8 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     memcpy(&ditherScale, uni + 88, 4);
     memcpy(&ditherBias, uni + 92, 4);
 
+    build_feather_table(); /* before any parallel region reads it */
+
     /* Vertex processing + primitive assembly, in primitive order. */
     size_t cap = 1024, n = 0;
     tri_rec* tris = (tri_rec*)malloc(cap * sizeof(tri_rec));
@@ -1752,7 +1875,10 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
     {
         const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
-        if ((batch->shader_features & SF_FEATHER) ||
+        /* ENABLE_FEATHER is built for midpoint-fan batches (feathered
+         * strokes; a feathered fill's vertices still refuse). */
+        if (((batch->shader_features & SF_FEATHER) &&
+             batch->draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES) ||
             (batch->shader_misc_flags & ~MISC_CLOCKWISE_FILL))
         {
             free(tris);

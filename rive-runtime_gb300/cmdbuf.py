@@ -503,10 +503,11 @@ def read_rcb(data: bytes):
             dict(width=w, height=h, clear_color=clear, dither_mode=dither, flags=flags))
 
 
-def rcb_scene(data: bytes):
+def rcb_scene(data: bytes, keep_feathered: bool = False):
     """A stored stream as (scene.Scene, CmdbufStats)."""
     commands, blobs, hdr = read_rcb(data)
-    return command_buffer_scene(commands, blobs, **hdr)
+    return CommandStreamReader().frame_scene(commands, blobs, keep_feathered=keep_feathered,
+                                             **hdr)
 
 
 def read_rcs(data: bytes):

@@ -371,8 +371,11 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         if (list < 0)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
                              b.draw_type);
-        if (b.shader_features & SF_FEATHER)
-            return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
+        // ENABLE_FEATHER is built for midpoint-fan batches: feathered
+        // strokes (a feathered fill's vertices report ERR_FEATHER).
+        if ((b.shader_features & SF_FEATHER) && b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
+            return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
+                             "feathered fills (draw type %u) not supported", b.draw_type);
         if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
                              "shader misc flags 0x%x not supported (rasterOrdering: clockwiseFill only)",
@@ -939,6 +942,8 @@ int rive_cuda_context_create(int device, rive_cuda_context** out_ctx)
         e = cudaMallocHost(&ctx->hError, 4);
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->hPairs, 4);
+    if (e == cudaSuccess)
+        e = ensure_feather_lut(device);
     if (e != cudaSuccess)
     {
         fprintf(stderr, "rive_cuda_context_create: %s\n", cudaGetErrorString(e));
@@ -1491,6 +1496,14 @@ int rive_cuda_read_grad_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->grad.ptr, std::min(bytes, ctx->lastGradBytes), cudaMemcpyDeviceToHost));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_feather_table(uint16_t* out)
+{
+    if (!out)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    feather_table_f16(out);
     return RIVE_CUDA_OK;
 }
 

@@ -183,8 +183,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         if (b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
             return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
                         b.draw_type);
-        if (b.shader_features & SF_FEATHER)
-            return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "feathered draws not supported");
+        // Only midpoint-fan batches reach here; their feathered strokes are
+        // built (a feathered fill's vertices report ERR_FEATHER).
         if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
             return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                         "shader misc flags 0x%x not supported", b.shader_misc_flags);
@@ -215,6 +215,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         {
             void* p = nullptr;
             CKN(cudaGetSymbolAddress(&p, gNoAllocScratch));
+            // The feather table (a copy into a file-scope symbol, no
+            // allocation) also goes up on the first call.
+            CKN(ensure_feather_lut(dev));
             gPool[dev] = (uint8_t*)p;
         }
         pool = gPool[dev];

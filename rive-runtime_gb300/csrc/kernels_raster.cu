@@ -23,6 +23,7 @@
 
 #include <cuda_fp16.h>
 
+#include <mutex>
 #include <type_traits>
 
 namespace rivecuda
@@ -283,8 +284,9 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     float2 translate = make_float2(__uint_as_float(r1.x), __uint_as_float(r1.y));
     float strokeRadius = __uint_as_float(r1.z);
     float featherRadius = __uint_as_float(r1.w);
-    if (featherRadius != 0.f)
+    if (featherRadius != 0.f && strokeRadius == 0.f)
     {
+        // Feathered fills draw as midpointFanCenterAA patches (not built).
         atomicOr(P.error, ERR_FEATHER);
         return false;
     }
@@ -327,6 +329,14 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     float2 offset = make_float2(0.f, 0.f);
     float2 cov;
     o.discard = false;
+    if (featherRadius != 0.f)
+    {
+        // draw_path_common.glsl:474-485: never feather harder than 1.5
+        // standard deviations across half a pixel.
+        const float2 mn = mat_mul(M, norm);
+        const float len = __fsqrt_rn(__fadd_rn(__fmul_rn(mn.x, mn.x), __fmul_rn(mn.y, mn.y)));
+        featherRadius = fmaxf(featherRadius, __fdiv_rn(kGaussianStddevs / 3.f, len));
+    }
     if (strokeRadius != 0.f)
     {
         float detM = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
@@ -335,9 +345,10 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
             outset = fminf(outset, 0.f);
         if (flags & RIGHT_JOIN_CONTOUR_FLAG)
             outset = fmaxf(outset, 0.f);
-        float aaRadius = __fmul_rn(manhattan_pixel_width(M, norm), kAARadius);
+        float aaRadius = featherRadius != 0.f ? featherRadius
+                                              : __fmul_rn(manhattan_pixel_width(M, norm), kAARadius);
         float globalCoverage = 1.f;
-        if (aaRadius > strokeRadius)
+        if (aaRadius > strokeRadius && featherRadius == 0.f)
         {
             globalCoverage = __fdiv_rn(strokeRadius, aaRadius);
             strokeRadius = aaRadius;
@@ -427,6 +438,8 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
         cov.x = __fmul_rn(cov.x, globalCoverage);
         cov.y = __fmul_rn(cov.y, globalCoverage);
         cov.y = fmaxf(cov.y, 1e-4f);
+        if (featherRadius != 0.f)
+            cov.x = __fsub_rn(kFeatherCoverageBias, cov.x); // marks a feathered stroke
         offset = mat_mul(M, make_float2(__fmul_rn(vertexOffset.x, outset),
                                         __fmul_rn(vertexOffset.y, outset)));
         if (pv.vertexType != STROKE_VERTEX)
@@ -1377,6 +1390,39 @@ struct __align__(16) TileTri
 static_assert(sizeof(TileTri) == 80, "TileTri layout");
 
 // Resident CTAs per SM the register allocation is bounded for (16x16 tiles).
+// The 512-entry feather table (the integral of the normal distribution over
+// -3..+3 standard deviations, fp16 values widened to float), written by the
+// host once per device (feather_table.cpp) before any flush.
+__device__ float g_featherLUT[kGaussianTableSize];
+
+// FEATHER(x) (common.glsl:53-60): the table sampled at normalised x with a
+// linear filter and clamp-to-edge addressing.
+__device__ __noinline__ float feather_lut(float x)
+{
+    const float t = __fsub_rn(__fmul_rn(x, (float)kGaussianTableSize), .5f);
+    if (!(t == t))
+        return g_featherLUT[0];
+    const float f = floorf(t);
+    const float w = __fsub_rn(t, f);
+    const float fc = fminf(fmaxf(f, -1.f), (float)kGaussianTableSize);
+    const int i0 = (int)fc;
+    const int a = min(max(i0, 0), kGaussianTableSize - 1);
+    const int b = min(max(i0 + 1, 0), kGaussianTableSize - 1);
+    const float va = g_featherLUT[a], vb = g_featherLUT[b];
+    return __fadd_rn(va, __fmul_rn(__fsub_rn(vb, va), w));
+}
+
+// eval_feathered_stroke (draw_path_common.glsl:242-258):
+// 1 - feather(1 - leftCoverage) - feather(1 - rightCoverage), the left
+// coverage carried biased by the feather bias.
+__device__ __forceinline__ float eval_feathered_stroke(float covx, float covy)
+{
+    float c = 1.f;
+    c = __fsub_rn(c, feather_lut(__fadd_rn(1.f - kFeatherCoverageBias, covx)));
+    c = __fsub_rn(c, feather_lut(__fsub_rn(1.f, covy)));
+    return c;
+}
+
 #ifndef RIVE_RASTER_MIN_BLOCKS
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
@@ -1543,10 +1589,18 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                         s.pendPaintY = v4.y;
                     }
                 }
-                if (covy >= 0.f)
-                    count = fmaxf(fminf(covx, covy), count); // stroke
+                if (covy >= 0.f) // stroke (find_stroke_coverage, draw_path.vert:501-509)
+                {
+                    const float frag =
+                        covx < kFeatherCoverageThreshold && ((T.v4.z >> 16) & SF_FEATHER)
+                            ? eval_feathered_stroke(covx, covy)
+                            : fminf(covx, covy);
+                    count = fmaxf(frag, count);
+                }
                 else
+                {
                     count = count + covx; // fill
+                }
                 s.count = h2f(f2h(count)); // the plane stores fp16
             }
         }
@@ -1590,5 +1644,86 @@ __global__ void __launch_bounds__(1024, 1) raster_tile32_kernel(BatchTables B,
     TileTri* sTris = reinterpret_cast<TileTri*>(dyn);
     uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);
     raster_tile<5>(B, tris, sortedSlots, ranges, sTris, sMask);
+}
+} // namespace rivecuda
+
+namespace rivecuda
+{
+namespace
+{
+// Generator of the feather table (renderer/src/gpu.cpp:1983-2062, restated):
+// 7 samples per entry of the normal distribution, shifted so the middle entry
+// pair averages 1/2, made monotonic and clamped to [0, 1], eased to 0 and 1
+// over the 8 entries at each end, then rounded to fp16 as the R16F texture
+// holds it.
+float eval_normal_distribution(float x, float mu, float inverseSigma)
+{
+    const float kOneOverSqrt2Pi = 0.398942280401433f;
+    float y = (x - mu) * inverseSigma;
+    return expf(-.5 * y * y) * inverseSigma * kOneOverSqrt2Pi;
+}
+
+void build_feather_table(float out[kGaussianTableSize])
+{
+    float table[kGaussianTableSize];
+    const float sigma = kGaussianTableSize / (kGaussianStddevs * 2);
+    const float inverseSigma = 1 / sigma;
+    const float mu = kGaussianTableSize * .5f;
+    float integral = 0;
+    for (int i = 0; i < kGaussianTableSize; ++i)
+    {
+        const int kSamples = 7;
+        for (int sample = 0; sample < kSamples; ++sample)
+        {
+            float dx = (float)(sample - (kSamples >> 1)) / kSamples;
+            integral += eval_normal_distribution((float)i + dx, mu, inverseSigma) / kSamples;
+        }
+        table[i] = integral;
+    }
+    const float shift =
+        .5 - (table[kGaussianTableSize / 2 - 1] + table[kGaussianTableSize / 2]) / 2;
+    table[0] = fminf(fmaxf(0, table[0] + shift), 1);
+    for (int i = 1; i < kGaussianTableSize; ++i)
+        table[i] = fminf(fmaxf(table[i - 1], table[i] + shift), 1);
+    const int kEase = 8;
+    for (int i = 0; i < kGaussianTableSize; ++i)
+    {
+        if (i < kEase)
+            table[i] *= (float)i / (float)kEase;
+        if (i > (kGaussianTableSize - kEase) - 1)
+        {
+            float diffToOne = 1.0 - table[i];
+            float fi = (float)(i - (kGaussianTableSize - kEase) + 1) / (float)kEase;
+            table[i] = table[i] + (diffToOne * fi);
+        }
+    }
+    for (int i = 0; i < kGaussianTableSize; ++i)
+        out[i] = __half2float(__float2half_rn(table[i]));
+}
+} // namespace
+
+// Uploads the feather table to the current device (once per device).
+cudaError_t ensure_feather_lut(int device)
+{
+    static std::mutex m;
+    static bool done[64] = {};
+    std::lock_guard<std::mutex> lock(m);
+    if (device >= 0 && device < 64 && done[device])
+        return cudaSuccess;
+    float table[kGaussianTableSize];
+    build_feather_table(table);
+    cudaError_t e = cudaMemcpyToSymbol(g_featherLUT, table, sizeof(table));
+    if (e == cudaSuccess && device >= 0 && device < 64)
+        done[device] = true;
+    return e;
+}
+
+// The fp16 bits of the feather table, for the C ABI.
+void feather_table_f16(uint16_t out[kGaussianTableSize])
+{
+    float table[kGaussianTableSize];
+    build_feather_table(table);
+    for (int i = 0; i < kGaussianTableSize; ++i)
+        out[i] = __half_as_ushort(__float2half_rn(table[i]));
 }
 } // namespace rivecuda

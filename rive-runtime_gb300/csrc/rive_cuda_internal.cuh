@@ -80,6 +80,14 @@ constexpr uint32_t SF_MODULATED_IMAGE = 1u << 8;
 // rasterOrdering draw batch carries. It travels with each triangle's shader
 // features in bit 15, which ShaderFeatures leaves free.
 constexpr uint32_t MISC_CLOCKWISE_FILL = 1u << 1;
+// Feathering (constants.glsl:19-43, draw_path_common.glsl:7-13).
+constexpr int kGaussianTableSize = 512;
+constexpr float kGaussianStddevs = 3.f;
+constexpr float kFeatherCoverageBias = -2.f;
+constexpr float kFeatherCoverageThreshold = -1.5f;
+// Uploads the feather table to a device once (kernels_raster.cu).
+cudaError_t ensure_feather_lut(int device);
+void feather_table_f16(uint16_t out[kGaussianTableSize]);
 constexpr uint32_t FEATURE_CLOCKWISE_FILL = 1u << 15;
 
 // Raster tiles: 16x16 by default; 8x8 and 32x32 are the autotuner's other

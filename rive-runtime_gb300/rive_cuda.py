@@ -115,6 +115,7 @@ def load():
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
+        "rive_cuda_feather_table": (i32, [vp]),
         "rive_cuda_get_raster_config": (i32, [vp, ctypes.POINTER(ctypes.c_int),
                                               ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_profile_collect": (i32, [vp, ctypes.POINTER(ctypes.c_double),
@@ -139,6 +140,15 @@ def make_desc(flush):
     d.draw_batch_count = len(batches)
     d.draw_batches = batches.ctypes.data if len(batches) else None
     return d, batches
+
+
+def feather_table():
+    """The fp16 bits of the library's feather table (512 entries)."""
+    out = np.zeros(512, np.uint16)
+    rc = load().rive_cuda_feather_table(out.ctypes.data_as(ctypes.c_void_p))
+    if rc != OK:
+        raise RiveCudaError(f"feather_table: status {rc}")
+    return out
 
 
 def flush_device_noalloc(flush, bufs: DeviceBuffers, target_ptr: int, stream=None):

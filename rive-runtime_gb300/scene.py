@@ -347,3 +347,18 @@ def stroke_stress(seed: int = 4, width: int = 1024, height: int = 1024,
                                 thickness=width_px, join=JOIN_ROUND, cap=CAP_ROUND))
         sc.cmd(CMD_DRAW_PATH, pi, qi)
     return sc
+
+
+def feathered_strokes(seed: int = 31, width: int = 320, height: int = 256, n_paths: int = 40,
+                      p_feather: float = 0.6, feather_range=(0.5, 8.0)) -> Scene:
+    """The full-feature distributions with a share of the strokes feathered
+    (RenderPaint::feather uniform in `feather_range`). Transforms scale by at
+    most 2, so every feather stays below the 32-pixel radius at which the
+    reference switches to its feather atlas: radius = 1.5 x feather x scale."""
+    sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=10,
+                      p_fill=0.4, p_clip=0.15, scale_range=(0.5, 2.0))
+    rng = np.random.default_rng(seed + 1)
+    for p in sc.paints:
+        if p.style == STYLE_STROKE and rng.uniform() < p_feather:
+            p.feather = float(rng.uniform(*feather_range))
+    return sc

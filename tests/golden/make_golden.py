@@ -56,6 +56,10 @@ SCENES = {
 }
 
 
+# Feathered strokes (RenderPaint::feather on strokes, radius x scale below the
+# reference's 32-pixel feather-atlas threshold): ENABLE_FEATHER batches.
+SCENES["feather_strokes_s31"] = lambda: scene.feathered_strokes(seed=31)
+
 # Frames of real content: the reference's own silver renderer-call streams
 # (tests/unit_tests/silvers/*.sriv, recorded by its SerializingFactory while
 # .riv artboards animate), read by rive_runtime_gb300.sriv. Their fills are

@@ -37,3 +37,11 @@ def test_null_arguments_are_rejected_without_a_gpu_call():
     assert lib.rive_cuda_context_create(0, None) == 1  # RIVE_CUDA_ERR_INVALID_ARGUMENT
     assert lib.rive_cuda_last_error(None, None, 0) == 1
     assert lib.rive_cuda_map_buffer(None, 0, 16) is None
+
+
+def test_feather_table_is_the_oracles():
+    """The library's feather table (host code, no GPU needed) equals the
+    oracle's, which is pinned to the reference's shipped table."""
+    from rive_runtime_gb300 import rive_cuda
+    import oracle
+    assert (rive_cuda.feather_table() == oracle.feather_table()).all()

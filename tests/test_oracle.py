@@ -171,3 +171,22 @@ def test_golden_captures_reproduce_from_reference(name):
     cap_bytes = open(os.path.join(GOLDEN, name + ".cap"), "rb").read()
     scene_bytes = open(os.path.join(GOLDEN, name + ".scene"), "rb").read()
     assert oracle.reference_capture(scene_bytes) == cap_bytes
+
+
+def test_feather_table_matches_the_reference_table():
+    """The oracle's Gaussian-integral table, built from the published
+    generator, equals the fp16 table the reference ships."""
+    import os
+    import re
+    import pytest
+    src = os.path.join(oracle.REFERENCE_SOURCES, "renderer", "src", "gpu.cpp")
+    if not os.path.exists(src):
+        pytest.skip("reference sources absent")
+    text = open(src).read()
+    body = text[text.index("const uint16_t g_gaussianIntegralTableF16[GAUSSIAN_TABLE_SIZE] = {"):]
+    body = body[body.index("{") + 1:body.index("};")]
+    want = [int(v, 16) for v in re.findall(r"0x[0-9a-fA-F]+", body)]
+    got = oracle.feather_table().tolist()
+    assert len(want) == 512
+    diff = [i for i in range(512) if got[i] != want[i]]
+    assert diff == [], (diff[:8], [(got[i], want[i]) for i in diff[:8]])

@@ -19,12 +19,25 @@ def _triangulated(scene_bytes):
     return struct.unpack_from("<12I", scene_bytes, 0)[11] & scene.FLAG_TRIANGULATE
 
 
+def _feathered(scene_bytes):
+    import struct
+    h = struct.unpack_from("<12I", scene_bytes, 0)
+    off = 48 + 20 * h[4]
+    return any(struct.unpack_from("<f", scene_bytes, off + 56 * i + 52)[0] != 0
+               for i in range(h[5]))
+
+
 @pytest.mark.parametrize("name", golden_names())
 def test_planner_matches_golden_capture(name):
     cap, scene_bytes = load_golden(name)
     if _triangulated(scene_bytes):
         # Interior triangulation stays with the reference front end.
         with pytest.raises(RuntimeError, match="triangulation"):
+            planner.plan(scene_bytes)
+        return
+    if _feathered(scene_bytes):
+        # So do feathered paints.
+        with pytest.raises(RuntimeError, match="feathered"):
             planner.plan(scene_bytes)
         return
     got = planner.plan(scene_bytes)
