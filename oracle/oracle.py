@@ -172,6 +172,13 @@ def feather_table():
     return out
 
 
+def inverse_feather_table():
+    """The oracle's 512-entry fp16 inverse feather table (uint16 bits)."""
+    out = np.zeros(512, np.uint16)
+    lib().oracle_inverse_feather_table(out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
 def f32_to_f16(x):
     return lib().oracle_f32_to_f16(float(x))
 

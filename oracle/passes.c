@@ -91,6 +91,19 @@
 #define GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS 3.f
 #define FEATHER_COVERAGE_BIAS -2.f
 #define FEATHER_COVERAGE_THRESHOLD -1.5f
+#define FEATHER_X_COORD_BIAS .25f
+#define HORIZONTAL_COTANGENT_THRESHOLD 1e3f
+#define HORIZONTAL_COTANGENT_VALUE (HORIZONTAL_COTANGENT_THRESHOLD * HORIZONTAL_COTANGENT_THRESHOLD)
+#define FEATHER_JOIN_HELPER_VERTEX_COUNT 3.f
+/* midpointFanCenterAAPatches (gpu.hpp:591-640): both AA ramps of an 8-segment
+ * span, a middle-out fan and the midpoint triangle. */
+#define CENTER_VERTEX_COUNT (PATCH_SEGMENT_SPAN * 8 + PATCH_SEGMENT_SPAN + 2)
+#define CENTER_INDEX_COUNT (PATCH_SEGMENT_SPAN * 12 + 7 * 3 + 3)
+#define DRAW_TYPE_MIDPOINT_FAN_CENTER_AA_PATCHES 1u
+static float feather_lut(float x);
+static float inverse_feather_lut(float x);
+static void build_feather_table(void);
+static void build_inverse_feather_table(void);
 #define SF_EVEN_ODD (1u << 4)
 /* gpu::ShaderMiscFlags::clockwiseFill of a draw batch (gpu.hpp:917), carried
  * with each triangle's shader features in a bit ShaderFeatures leaves free. */
@@ -366,6 +379,104 @@ static const uint32_t* contour_record(const rive_cuda_flush_desc* d,
     return (const uint32_t*)b->contours + idx * 4;
 }
 
+/* GLSL mix(): x * (1 - a) + y * a. */
+static inline f2 glsl_mix2(f2 x, f2 y, float a)
+{
+    return (f2){x.x * (1.f - a) + y.x * a, x.y * (1.f - a) + y.y * a};
+}
+
+/* clamped_divide (bezier_utils.glsl:164-169): clamp(a/b, 0, 1). */
+static float clamped_divide(float a, float b)
+{
+    a = b < 0.f ? -a : a;
+    b = fabsf(b);
+    return a > 0.f ? (a < b ? a / b : 1.f) : 0.f;
+}
+
+/* find_cubic_max_height (bezier_utils.glsl:173-245): three Newton steps from
+ * t = 1/2 on the height above the chord. */
+static float find_cubic_max_height(f2 p0, f2 p1, f2 p2, f2 p3, float* outT)
+{
+    f2 base = sub2(p3, p0);
+    float lengthBase = sqrtf(dot2(base, base));
+    if (lengthBase == 0.f)
+    {
+        *outT = .5f;
+        return 0.f;
+    }
+    f2 norm = {-base.y / lengthBase, base.x / lengthBase};
+    float h2 = dot2(norm, sub2(p2, p0));
+    float h1 = dot2(norm, sub2(p1, p0));
+    float dh = h1 - h2;
+    float _3A = 3.f * dh;
+    float B = -h1 - dh;
+    float C = h1;
+    float t = .5f;
+    for (int i = 0; i < 3; ++i)
+    {
+        float _3At = _3A * t;
+        t = clamped_divide(_3At * t - C, 2.f * (_3At + B));
+    }
+    *outT = t;
+    return fabsf(t * (t * (t * _3A + 3.f * B) + 3.f * C));
+}
+
+/* measure_cubic_local_curvature (bezier_utils.glsl:77-153): the turn, in
+ * radians, across a spread of `desiredSpread` centred at T. */
+static float measure_cubic_local_curvature(f2 p0, f2 p1, f2 p2, f2 p3, float T,
+                                           float desiredSpread)
+{
+    f2 C = sub2(p1, p0);
+    f2 D = sub2(p2, p1);
+    f2 E = sub2(p3, p0);
+    f2 B = sub2(D, C);
+    f2 A = add2(mul2(D, -3.f), E);
+    f2 tangent = mul2(add2(mul2(add2(mul2(A, T), mul2(B, 2.f)), T), C), 3.f);
+    float lengthTan = sqrtf(dot2(tangent, tangent));
+    if (lengthTan == 0.f)
+        return 0.f;
+    tangent = mul2(tangent, 1.f / lengthTan);
+    float A_ = 2.f * dot2(A, tangent);
+    float C_ = 3.f * (A_ * T + 4.f * dot2(B, tangent)) * T + 6.f * dot2(C, tangent);
+    float maxDT = minf(T, 1.f - T);
+    float maxSpread = (A_ * maxDT * maxDT + C_) * maxDT;
+    float targetSpread = minf(desiredSpread, maxSpread * .9999f);
+    float dt;
+    if (A_ == 0.f)
+    {
+        dt = targetSpread / C_;
+    }
+    else
+    {
+        float r = 1.f / A_;
+        float b = C_ * r, c = -targetSpread * r;
+        float Q = (-1.f / 3.f) * b, R = .5f * c;
+        float discr = R * R - Q * Q * Q;
+        if (discr < 0.f)
+        {
+            float sqrtQ = sqrtf(Q);
+            float th = acosf(R / (sqrtQ * sqrtQ * sqrtQ));
+            dt = -2.f * sqrtQ * cosf(th * (1.f / 3.f) + (-PI_F * 2.f / 3.f));
+        }
+        else
+        {
+            float Aq = powf(fabsf(R) + sqrtf(discr), 1.f / 3.f);
+            if (R < 0.f)
+                Aq = -Aq;
+            dt = Aq != 0.f ? Aq + Q / Aq : 0.f;
+        }
+    }
+    dt = fabsf(dt);
+    float t0 = T - dt, t1 = T + dt;
+    f2 dir0 = add2(mul2(add2(mul2(A, t0), mul2(B, 2.f)), t0), C);
+    f2 dir1 = add2(mul2(add2(mul2(A, t1), mul2(B, 2.f)), t1), C);
+    f2 e0, e1;
+    find_cubic_tangents(p0, p1, p2, p3, &e0, &e1);
+    f2 tan0 = t0 < 1e-3f ? e0 : dir0;
+    f2 tan1 = t1 > 1.f - 1e-3f ? e1 : dir1;
+    return acosf(cosine_between_vectors(tan0, tan1));
+}
+
 /* Vertex-shader half of pass 2, evaluated once per span rectangle. */
 static int tess_setup(const rive_cuda_flush_desc* d,
                       const oracle_buffers* b,
@@ -408,7 +519,27 @@ static int tess_setup(const rive_cuda_flush_desc* d,
         featherRadius = path[7];
     }
     if (featherRadius != 0.f && strokeRadius == 0.f)
-        return -2; /* feathered fills: not supported */
+    {
+        /* tessellate.glsl:141-190: a cubic of a feathered fill is flattened
+         * toward its chord, more where it curves, to mimic the softening a
+         * feather gets from curvature. */
+        float maxHeightT;
+        float height = find_cubic_max_height(p0, p1, p2, p3, &maxHeightT);
+        float oneStddev = featherRadius * (1.f / GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS);
+        float curvature = measure_cubic_local_curvature(p0, p1, p2, p3, maxHeightT, oneStddev);
+        float dimming = 1.f - curvature * (1.f / PI_F);
+        f2 base = sub2(p3, p0);
+        float stddevsPow2 = dot2(base, base) / (oneStddev * oneStddev);
+        float dimmingByStddevs = (stddevsPow2 - 1.f) * .5f;
+        dimming = minf(dimming, dimmingByStddevs);
+        dimming = minf(dimming, .99f);
+        float desiredOpacityOnCenter = .5f * dimming;
+        float x = inverse_feather_lut(desiredOpacityOnCenter) * -2.f + 1.f;
+        float softness = clamped_divide(x * featherRadius, height);
+        f2 flat1 = glsl_mix2(p0, p3, 1.f / 3.f), flat2 = glsl_mix2(p0, p3, 2.f / 3.f);
+        p1 = glsl_mix2(p1, flat1, softness);
+        p2 = glsl_mix2(p2, flat2, softness);
+    }
     if (contourIDWithFlags & CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG)
     {
         if (!path)
@@ -628,7 +759,16 @@ static void tess_fragment_t(const tess_varyings* v,
     }
     out[0] = f2u(tessCoord.x);
     out[1] = f2u(tessCoord.y);
-    out[2] = f2u(glsl_mod(theta, TWO_PI_F));
+    if ((contourIDWithFlags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG)
+    {
+        /* tessellate.glsl:551-559: feather joins hand their stepping to the
+         * draw pass. */
+        out[2] = ((uint32_t)mergedSegmentCount << 16) | (uint32_t)mergedVertexID;
+    }
+    else
+    {
+        out[2] = f2u(glsl_mod(theta, TWO_PI_F));
+    }
     out[3] = contourIDWithFlags;
 }
 
@@ -764,6 +904,8 @@ typedef struct
 static patch_vertex g_patch[PATCH_VERTEX_COUNT];
 static uint16_t g_patch_idx[PATCH_INDEX_COUNT];
 static patch_vertex g_outer[OUTER_VERTEX_COUNT];
+static patch_vertex g_center[CENTER_VERTEX_COUNT];
+static uint16_t g_center_idx[CENTER_INDEX_COUNT];
 static uint16_t g_outer_idx[OUTER_INDEX_COUNT];
 static int g_patch_ready = 0;
 
@@ -888,6 +1030,70 @@ static void build_patch_tables(void)
             g_outer_idx[k++] = (uint16_t)(ofan + i + step);
             g_outer_idx[k++] = (uint16_t)(ofan + i + step * 2);
         }
+
+    /* Center-AA midpoint fan (gpu.cpp:446-687, PatchType::midpointFanCenterAA):
+     * the AA ramp centred on the curve (both sides), the middle-out fan and
+     * the midpoint triangle; feathered fills draw with it. */
+    n = 0;
+    for (int i = 0; i < span; ++i) /* top side */
+    {
+        float l = (float)i, r = l + 1.f;
+        pv_set(&g_center[n + 0], l, 0.f, .5f, strokeParams);
+        pv_set(&g_center[n + 1], l, 1.f, 0.f, strokeParams);
+        pv_set(&g_center[n + 2], r, 0.f, .5f, strokeParams);
+        pv_set(&g_center[n + 3], r, 1.f, 0.f, strokeParams);
+        pv_mirror(&g_center[n + 0], r - 1.f, 0.f, .5f);
+        pv_mirror(&g_center[n + 1], l - 1.f, 0.f, .5f);
+        pv_mirror(&g_center[n + 2], r - 1.f, 1.f, 0.f);
+        pv_mirror(&g_center[n + 3], l - 1.f, 1.f, 0.f);
+        n += 4;
+    }
+    for (int i = 0; i < span; ++i) /* bottom (negative coverage) side */
+    {
+        float l = (float)i, r = l + 1.f;
+        pv_set(&g_center[n + 0], l, -0.f, .5f, strokeParams);
+        pv_set(&g_center[n + 1], r, -0.f, .5f, strokeParams);
+        pv_set(&g_center[n + 2], l, -1.f, 0.f, strokeParams);
+        pv_set(&g_center[n + 3], r, -1.f, 0.f, strokeParams);
+        pv_mirror(&g_center[n + 0], r - 1.f, -0.f, .5f);
+        pv_mirror(&g_center[n + 1], r - 1.f, -1.f, 0.f);
+        pv_mirror(&g_center[n + 2], l - 1.f, -0.f, .5f);
+        pv_mirror(&g_center[n + 3], l - 1.f, -1.f, 0.f);
+        n += 4;
+    }
+    const int cfan = n;
+    for (int i = 0; i <= span; ++i)
+    {
+        pv_set(&g_center[n], (float)i, 0.f, 1.f, (span << 2) | FAN_VERTEX);
+        pv_mirror(&g_center[n], (float)i - 1.f, 0.f, 1.f);
+        ++n;
+    }
+    const int cmid = n;
+    pv_set(&g_center[n++], 0.f, 0.f, 1.f, (span << 2) | FAN_MIDPOINT_VERTEX);
+    k = 0;
+    e = 0;
+    for (int sgm = 0; sgm < span; ++sgm)
+    {
+        for (int i = 0; i < 6; ++i)
+            g_center_idx[k++] = (uint16_t)(e + border[i]);
+        e += 4;
+    }
+    for (int sgm = 0; sgm < span; ++sgm)
+    {
+        for (int i = 0; i < 6; ++i)
+            g_center_idx[k++] = (uint16_t)(e + negBorder[i]);
+        e += 4;
+    }
+    for (int step = 1; step < span; step <<= 1)
+        for (int i = 0; i < span; i += step * 2)
+        {
+            g_center_idx[k++] = (uint16_t)(cfan + i);
+            g_center_idx[k++] = (uint16_t)(cfan + i + step);
+            g_center_idx[k++] = (uint16_t)(cfan + i + step * 2);
+        }
+    g_center_idx[k++] = (uint16_t)cfan;
+    g_center_idx[k++] = (uint16_t)(cfan + span);
+    g_center_idx[k++] = (uint16_t)cmid;
     g_patch_ready = 1;
 }
 
@@ -907,13 +1113,39 @@ static float manhattan_pixel_width(const float M[4], f2 normalized)
 typedef struct
 {
     f2 pos;
-    float cov[2];
+    float cov[4];
     uint32_t pathID;
     int discard;
 } vtx_out;
 
 /* unpack_tessellated_path_vertex (draw_path_common.glsl:275-789), for
  * midpointFan patches without feathering, rasterOrdering mode. */
+/* pack_feathered_fill_coverages (draw_path_common.glsl:107-149). */
+static void pack_feathered_fill_coverages(float cornerTheta, f2 spokeNorm, float outset,
+                                          float cov[4])
+{
+    f2 cornerLocalCoord = {(1.f - spokeNorm.x * fabsf(outset)) * .5f,
+                           (1.f - spokeNorm.y * fabsf(outset)) * .5f};
+    float cotTheta, y0;
+    if (fabsf(cornerTheta - PI_F * .5f) < 1.f / HORIZONTAL_COTANGENT_THRESHOLD)
+    {
+        cotTheta = 0.f;
+        y0 = 0.f;
+    }
+    else
+    {
+        float tanTheta = tanf(cornerTheta);
+        cotTheta = signf(PI_F * .5f - cornerTheta) /
+                   maxf(fabsf(tanTheta), 1.f / HORIZONTAL_COTANGENT_VALUE);
+        y0 = cotTheta >= 0.f ? cornerLocalCoord.y - (1.f - cornerLocalCoord.x) * tanTheta
+                             : cornerLocalCoord.y + cornerLocalCoord.x * tanTheta;
+    }
+    cov[0] = maxf(cornerLocalCoord.x, 0.f) + FEATHER_X_COORD_BIAS;
+    cov[1] = -cornerLocalCoord.y + FEATHER_COVERAGE_BIAS;
+    cov[2] = cotTheta;
+    cov[3] = y0;
+}
+
 static int patch_vertex_shader(const rive_cuda_flush_desc* d,
                                const oracle_buffers* b,
                                const uint32_t* tess,
@@ -951,8 +1183,6 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     f2 translate = {path[4], path[5]};
     float strokeRadius = path[6];
     float featherRadius = path[7];
-    if (featherRadius != 0.f && strokeRadius == 0.f)
-        return -2; /* feathered fills: midpointFanCenterAA patches, not built */
     uint32_t mirroredContourFlag =
         contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG;
     if (mirroredContourFlag)
@@ -988,11 +1218,80 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
         contourIDWithFlags =
             (tv[3] & ~MIRRORED_CONTOUR_CONTOUR_FLAG) | mirroredContourFlag;
     }
-    float theta = u2f(tv[2]);
+    float theta;
+    float featherJoinEdge0Theta = 0.f, featherJoinCornerTheta = 0.f;
+    if ((contourIDWithFlags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG &&
+        vertexType == STROKE_VERTEX)
+    {
+        /* draw_path_common.glsl:372-468: a feather join steps between the
+         * tangents of the tessellation vertices just before and after it,
+         * backward segments first (to erase coverage outside the corner),
+         * then forward ones. */
+        uint32_t joinDataPacked = tv[2];
+        float joinVertexID = (float)(joinDataPacked & 0xffffu);
+        float joinSegmentCount = (float)(joinDataPacked >> 16);
+        int off0 = (int)(-joinVertexID - 1.f), off1 = (int)(joinSegmentCount - joinVertexID + 1.f);
+        if (contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG)
+        {
+            off0 = -off0;
+            off1 = -off1;
+        }
+        int64_t ib = tessVertexIdx + off0, ia = tessVertexIdx + off1;
+        if (ib < 0 || (size_t)ib >= tessTexels || ia < 0 || (size_t)ia >= tessTexels)
+            return -1;
+        const uint32_t* before = tess + (size_t)ib * 4;
+        const uint32_t* after = tess + (size_t)ia * 4;
+        if ((after[3] & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)) !=
+            (before[3] & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)))
+        {
+            if ((size_t)vertexIndex0 >= tessTexels)
+                return -1;
+            after = tess + (size_t)vertexIndex0 * 4;
+        }
+        featherJoinEdge0Theta = u2f(before[2]);
+        float featherJoinEdge1Theta = u2f(after[2]);
+        featherJoinCornerTheta = featherJoinEdge1Theta - featherJoinEdge0Theta;
+        if (fabsf(featherJoinCornerTheta) > PI_F)
+            featherJoinCornerTheta -= TWO_PI_F * signf(featherJoinCornerTheta);
+        float nonHelperSegmentCount =
+            joinSegmentCount + 1.f - FEATHER_JOIN_HELPER_VERTEX_COUNT;
+        float forwardSegmentCount =
+            clampf(rintf(fabsf(featherJoinCornerTheta) / PI_F * nonHelperSegmentCount), 1.f,
+                   nonHelperSegmentCount - 1.f);
+        float backwardSegmentCount = nonHelperSegmentCount - forwardSegmentCount;
+        if (joinVertexID <= backwardSegmentCount)
+        {
+            featherJoinCornerTheta =
+                -(PI_F * signf(featherJoinCornerTheta) - featherJoinCornerTheta);
+            joinSegmentCount = backwardSegmentCount;
+            if (joinVertexID == backwardSegmentCount)
+                outset = -outset;
+        }
+        else if (joinVertexID == backwardSegmentCount + 1.f)
+        {
+            joinVertexID = 0.f;
+            joinSegmentCount = 0.f;
+            outset = 0.f;
+        }
+        else
+        {
+            joinVertexID -= backwardSegmentCount + 2.f;
+            joinSegmentCount = forwardSegmentCount;
+        }
+        if (joinVertexID == joinSegmentCount)
+            theta = featherJoinEdge1Theta;
+        else
+            theta = featherJoinEdge0Theta +
+                    featherJoinCornerTheta * (joinVertexID / joinSegmentCount);
+    }
+    else
+    {
+        theta = u2f(tv[2]);
+    }
     f2 norm = {sinf(theta), -cosf(theta)};
     f2 origin = {u2f(tv[0]), u2f(tv[1])};
     f2 postTransformVertexOffset = {0.f, 0.f};
-    float cov[2] = {0.f, 0.f};
+    float cov[4] = {0.f, 0.f, 0.f, 0.f};
     o->discard = 0;
 
     if (featherRadius != 0.f)
@@ -1108,14 +1407,42 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     {
         cov[0] = fillCoverage;
         cov[1] = -1.f;
-        /* sign(MUL(outset * norm, inverse(M))) * AA_RADIUS: row vector times
-         * the inverse matrix. */
-        f2 on = mul2(norm, outset);
-        float det = M[0] * M[3] - M[2] * M[1];
-        float i00 = M[3] / det, i01 = -M[1] / det; /* column 0 of inverse */
-        float i10 = -M[2] / det, i11 = M[0] / det; /* column 1 of inverse */
-        f2 r = {on.x * i00 + on.y * i01, on.x * i10 + on.y * i11};
-        postTransformVertexOffset = (f2){signf(r.x) * AA_RADIUS, signf(r.y) * AA_RADIUS};
+        if (featherRadius != 0.f)
+        {
+            /* draw_path_common.glsl:659-741: a feathered edge; the spokes of
+             * a feather join carry their corner. */
+            cov[1] = FEATHER_COVERAGE_BIAS;
+            cov[2] = HORIZONTAL_COTANGENT_VALUE;
+            cov[3] = fillCoverage;
+            if ((contourIDWithFlags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG &&
+                vertexType == STROKE_VERTEX)
+            {
+                if (featherJoinCornerTheta < 0.f)
+                {
+                    featherJoinEdge0Theta += featherJoinCornerTheta;
+                    featherJoinCornerTheta = -featherJoinCornerTheta;
+                }
+                float spokeTheta = theta - featherJoinEdge0Theta;
+                spokeTheta = glsl_mod(spokeTheta + PI_F * .5f, TWO_PI_F) - PI_F * .5f;
+                spokeTheta = clampf(spokeTheta, 0.f, featherJoinCornerTheta);
+                if (spokeTheta > featherJoinCornerTheta * .5f)
+                    spokeTheta = featherJoinCornerTheta - spokeTheta;
+                f2 spokeNorm = {sinf(spokeTheta), cosf(spokeTheta)};
+                pack_feathered_fill_coverages(featherJoinCornerTheta, spokeNorm, outset, cov);
+            }
+            postTransformVertexOffset = mat_mul(M, mul2(norm, outset * featherRadius));
+        }
+        else
+        {
+            /* sign(MUL(outset * norm, inverse(M))) * AA_RADIUS: row vector
+             * times the inverse matrix. */
+            f2 on = mul2(norm, outset);
+            float det = M[0] * M[3] - M[2] * M[1];
+            float i00 = M[3] / det, i01 = -M[1] / det; /* column 0 of inverse */
+            float i10 = -M[2] / det, i11 = M[0] / det; /* column 1 of inverse */
+            f2 r = {on.x * i00 + on.y * i01, on.x * i10 + on.y * i11};
+            postTransformVertexOffset = (f2){signf(r.x) * AA_RADIUS, signf(r.y) * AA_RADIUS};
+        }
         if (((contourIDWithFlags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
             ((contourIDWithFlags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
             cov[0] = -cov[0];
@@ -1134,6 +1461,8 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     o->pos = add2(add2(mo, postTransformVertexOffset), translate);
     o->cov[0] = cov[0];
     o->cov[1] = cov[1];
+    o->cov[2] = cov[2];
+    o->cov[3] = cov[3];
     o->pathID = pathID;
     return 0;
 }
@@ -1141,7 +1470,7 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
 typedef struct
 {
     int64_t x[3], y[3]; /* fixed point, SUBPIXEL_BITS */
-    float cov[3][2];
+    float cov[3][4];
     uint32_t pathID;
     uint32_t features;
     int32_t bx0, by0, bx1, by1; /* pixel bbox, inclusive-exclusive */
@@ -1227,6 +1556,7 @@ static void build_feather_table(void)
         g_feather16[i] = oracle_f32_to_f16(table[i]);
         g_feather[i] = oracle_f16_to_f32(g_feather16[i]);
     }
+    build_inverse_feather_table();
     g_featherReady = 1;
 }
 
@@ -1256,6 +1586,110 @@ static float feather_lut(float x)
 /* eval_feathered_stroke (draw_path_common.glsl:242-258):
  * 1 - feather(1 - leftCoverage) - feather(1 - rightCoverage), with the left
  * coverage carried biased by FEATHER_COVERAGE_BIAS. */
+static uint16_t g_inverse16[GAUSSIAN_TABLE_SIZE];
+static float g_inverse[GAUSSIAN_TABLE_SIZE];
+
+/* The inverse table (renderer/src/gpu.cpp:2125-2190, restated): 32 samples per
+ * entry of the running integral; each cell holds the height at which the
+ * integral crosses the cell's centre, the middle cell exactly 1/2. */
+static void build_inverse_feather_table(void)
+{
+    float table[GAUSSIAN_TABLE_SIZE];
+    memset(table, 0, sizeof(table));
+    const size_t MULTIPLIER = 32;
+    float sigma = GAUSSIAN_TABLE_SIZE / (GAUSSIAN_INTEGRAL_TEXTURE_STDDEVS * 2);
+    float inverseSigma = 1 / sigma;
+    float mu = GAUSSIAN_TABLE_SIZE * .5f;
+    size_t samples = GAUSSIAN_TABLE_SIZE * MULTIPLIER;
+    float integral = 0;
+    for (size_t i = 0; i < (samples + 1) / 2; ++i)
+    {
+        float barCenterX = (float)i / MULTIPLIER;
+        integral += eval_normal_distribution(barCenterX, mu, inverseSigma) / MULTIPLIER;
+    }
+    integral = .5 - integral;
+    float lastInverseX = NAN, lastInverseY = 0;
+    table[0] = 0;
+    table[GAUSSIAN_TABLE_SIZE - 1] = 1;
+    for (size_t i = 0; i < samples; ++i)
+    {
+        float barCenterX = (float)i / MULTIPLIER;
+        integral += eval_normal_distribution(barCenterX, mu, inverseSigma) / MULTIPLIER;
+        float inverseX = fminf(fmaxf(0, integral), 1) * GAUSSIAN_TABLE_SIZE;
+        float inverseY = (i + .5f) / samples;
+        size_t cell = (size_t)inverseX;
+        float cellCenterX = cell + .5f;
+        if (cellCenterX == mu)
+        {
+            table[cell] = .5f;
+        }
+        else if (lastInverseX <= cellCenterX && inverseX >= cellCenterX)
+        {
+            float t = (cellCenterX - lastInverseX) / (inverseX - lastInverseX);
+            float y = lastInverseY + (inverseY - lastInverseY) * t;
+            if (cell < GAUSSIAN_TABLE_SIZE)
+                table[cell] = y;
+        }
+        lastInverseX = inverseX;
+        lastInverseY = inverseY;
+    }
+    for (int i = 0; i < GAUSSIAN_TABLE_SIZE; ++i)
+    {
+        g_inverse16[i] = oracle_f32_to_f16(table[i]);
+        g_inverse[i] = oracle_f16_to_f32(g_inverse16[i]);
+    }
+}
+
+void oracle_inverse_feather_table(uint16_t* out)
+{
+    build_feather_table();
+    memcpy(out, g_inverse16, sizeof(g_inverse16));
+}
+
+/* INVERSE_FEATHER(x) (common.glsl:61-68): layer 1 of the same 1D array
+ * texture, sampled the same way. */
+static float inverse_feather_lut(float x)
+{
+    float t = x * GAUSSIAN_TABLE_SIZE - .5f;
+    if (!(t == t))
+        return g_inverse[0];
+    float f = floorf(t);
+    float w = t - f;
+    float fc = fminf(fmaxf(f, -1.f), (float)GAUSSIAN_TABLE_SIZE);
+    int i0 = (int)fc;
+    int a = i0 < 0 ? 0 : (i0 > GAUSSIAN_TABLE_SIZE - 1 ? GAUSSIAN_TABLE_SIZE - 1 : i0);
+    int b = i0 + 1 < 0 ? 0 : (i0 + 1 > GAUSSIAN_TABLE_SIZE - 1 ? GAUSSIAN_TABLE_SIZE - 1 : i0 + 1);
+    return g_inverse[a] + (g_inverse[b] - g_inverse[a]) * w;
+}
+
+/* eval_feathered_fill (draw_path_common.glsl:152-240): the feather of a flat
+ * edge, or of a corner through a 4-sample integral of the second edge. */
+static float eval_feathered_fill(float cx, float cy, float cz, float cw)
+{
+    float cotTheta = cz;
+    float y0 = maxf(cw, 0.f);
+    float featherCoverage = cotTheta >= 0.f ? feather_lut(y0) : 0.f;
+    if (fabsf(cotTheta) < HORIZONTAL_COTANGENT_THRESHOLD)
+    {
+        float x = fabsf(cx) - FEATHER_X_COORD_BIAS;
+        float y = -cy + FEATHER_COVERAGE_BIAS;
+        float dt = (y - y0) * 0.5984134206f;
+        static const float k[4] = {0.20888568955f, 0.62665706865f, 1.04442844776f,
+                                   1.46219982687f};
+        float sum = 0.f;
+        for (int i = 0; i < 4; ++i)
+        {
+            float t = y0 + dt * k[i];
+            float u = t * -cotTheta + (y * cotTheta + x);
+            float t_ = t * 5.09593080173f + -2.54796540086f;
+            float ddt = exp2f(-t_ * t_);
+            sum += feather_lut(u) * ddt;
+        }
+        featherCoverage += sum * dt;
+    }
+    return featherCoverage * signf(cx);
+}
+
 static float eval_feathered_stroke(float covx, float covy)
 {
     float featherCoverage = 1.f;
@@ -1472,6 +1906,8 @@ static void fragment(const frag_ctx* fc,
                      const tri_rec* t,
                      float covx,
                      float covy,
+                     float covz,
+                     float covw,
                      int px,
                      int py,
                      pls_pixel* pls)
@@ -1510,7 +1946,13 @@ static void fragment(const frag_ctx* fc,
             coverageCount = maxf(frag, coverageCount);
         }
         else
-            coverageCount = coverageCount + covx;
+        {
+            /* find_fill_coverage (draw_path.vert:511-519) */
+            float frag = ((features & SF_FEATHER) && covy < FEATHER_COVERAGE_THRESHOLD)
+                             ? eval_feathered_fill(covx, covy, covz, covw)
+                             : covx;
+            coverageCount = coverageCount + frag;
+        }
         uint16_t storedCount = oracle_f32_to_f16(coverageCount);
         pls->coverage = ((uint32_t)vPathID << 16) | storedCount;
         coverageCount = h2f(storedCount);
@@ -1741,6 +2183,8 @@ static int setup_triangle(const vtx_out* a,
         t->y[i] = snap(v[i]->pos.y);
         t->cov[i][0] = v[i]->cov[0];
         t->cov[i][1] = v[i]->cov[1];
+        t->cov[i][2] = v[i]->cov[2];
+        t->cov[i][3] = v[i]->cov[3];
     }
     int64_t area2 = (t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
                     (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]);
@@ -1823,7 +2267,13 @@ static void raster_triangle_rows(const frag_ctx* fc,
             float l2 = (float)((double)e2 / area2);
             float covx = l0 * t->cov[0][0] + l1 * t->cov[1][0] + l2 * t->cov[2][0];
             float covy = l0 * t->cov[0][1] + l1 * t->cov[1][1] + l2 * t->cov[2][1];
-            fragment(fc, t, covx, covy, px, py, pls + (size_t)py * W + px);
+            float covz = 0.f, covw = 0.f;
+            if (covy < FEATHER_COVERAGE_THRESHOLD) /* a feathered fill needs all four */
+            {
+                covz = l0 * t->cov[0][2] + l1 * t->cov[1][2] + l2 * t->cov[2][2];
+                covw = l0 * t->cov[0][3] + l1 * t->cov[1][3] + l2 * t->cov[2][3];
+            }
+            fragment(fc, t, covx, covy, covz, covw, px, py, pls + (size_t)py * W + px);
             ++*frags;
         }
     }
@@ -1875,10 +2325,11 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
     {
         const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
-        /* ENABLE_FEATHER is built for midpoint-fan batches (feathered
-         * strokes; a feathered fill's vertices still refuse). */
+        /* ENABLE_FEATHER: feathered strokes (midpoint-fan batches) and
+         * feathered fills (center-AA batches). */
         if (((batch->shader_features & SF_FEATHER) &&
-             batch->draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES) ||
+             batch->draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES &&
+             batch->draw_type != DRAW_TYPE_MIDPOINT_FAN_CENTER_AA_PATCHES) ||
             (batch->shader_misc_flags & ~MISC_CLOCKWISE_FILL))
         {
             free(tris);
@@ -1889,13 +2340,17 @@ int oracle_draw(const rive_cuda_flush_desc* d,
             ((batch->shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u);
         int rc = 0;
         if (batch->draw_type == RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES ||
+            batch->draw_type == DRAW_TYPE_MIDPOINT_FAN_CENTER_AA_PATCHES ||
             batch->draw_type == DRAW_TYPE_OUTER_CURVE_PATCHES)
         {
             const int outer = batch->draw_type == DRAW_TYPE_OUTER_CURVE_PATCHES;
-            const patch_vertex* table = outer ? g_outer : g_patch;
-            const uint16_t* idx = outer ? g_outer_idx : g_patch_idx;
-            const int nv = outer ? OUTER_VERTEX_COUNT : PATCH_VERTEX_COUNT;
-            const int ni = outer ? OUTER_INDEX_COUNT : PATCH_INDEX_COUNT;
+            const int center = batch->draw_type == DRAW_TYPE_MIDPOINT_FAN_CENTER_AA_PATCHES;
+            const patch_vertex* table = outer ? g_outer : center ? g_center : g_patch;
+            const uint16_t* idx = outer ? g_outer_idx : center ? g_center_idx : g_patch_idx;
+            const int nv = outer ? OUTER_VERTEX_COUNT : center ? CENTER_VERTEX_COUNT
+                                                                : PATCH_VERTEX_COUNT;
+            const int ni = outer ? OUTER_INDEX_COUNT : center ? CENTER_INDEX_COUNT
+                                                               : PATCH_INDEX_COUNT;
             for (uint32_t inst = batch->base_element;
                  inst < batch->base_element + batch->element_count && rc == 0;
                  ++inst)
@@ -1946,6 +2401,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
                     vo[k].pos = (f2){p.x + path[4], p.y + path[5]};
                     vo[k].cov[0] = (float)((int32_t)r[2] >> 16);
                     vo[k].cov[1] = -1.f;
+                    vo[k].cov[2] = vo[k].cov[3] = 0.f;
                     vo[k].pathID = pathID;
                     vo[k].discard = 0;
                 }

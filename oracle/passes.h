@@ -95,6 +95,8 @@ void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
 uint16_t oracle_f32_to_f16(float f);
 /* The 512-entry fp16 feather (Gaussian integral) table. */
 void oracle_feather_table(uint16_t* out);
+/* Its 512-entry fp16 inverse (the height at which the integral reaches x). */
+void oracle_inverse_feather_table(uint16_t* out);
 float oracle_f16_to_f32(uint16_t h);
 
 /* Blend coefficients of one mode (advanced_blend.glsl:156-301). */

@@ -362,3 +362,24 @@ def feathered_strokes(seed: int = 31, width: int = 320, height: int = 256, n_pat
         if p.style == STYLE_STROKE and rng.uniform() < p_feather:
             p.feather = float(rng.uniform(*feather_range))
     return sc
+
+
+def feathered(seed: int = 33, width: int = 320, height: int = 256, n_paths: int = 40,
+              p_feather: float = 0.6, feather_range=(0.5, 8.0)) -> Scene:
+    """The full-feature distributions with a share of the fills and strokes
+    feathered. The reference draws feathered fills only with the clockwise fill
+    rule, so the feathered fills' paths are clockwise. Transforms scale by at
+    most 2, keeping every feather below the 32-pixel radius of the feather
+    atlas (radius = 1.5 x feather x scale)."""
+    sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=10,
+                      p_fill=0.7, p_clip=0.15, scale_range=(0.5, 2.0))
+    rng = np.random.default_rng(seed + 1)
+    for op, a, b, _ in sc.cmds:
+        if op != CMD_DRAW_PATH:
+            continue
+        paint = sc.paints[b]
+        if rng.uniform() < p_feather:
+            paint.feather = float(rng.uniform(*feather_range))
+            if paint.style == STYLE_FILL:
+                sc.paths[a].fill_rule = FILL_CLOCKWISE
+    return sc

@@ -59,6 +59,9 @@ SCENES = {
 # Feathered strokes (RenderPaint::feather on strokes, radius x scale below the
 # reference's 32-pixel feather-atlas threshold): ENABLE_FEATHER batches.
 SCENES["feather_strokes_s31"] = lambda: scene.feathered_strokes(seed=31)
+# Feathered fills and strokes (clockwise feathered fills, radius x scale below
+# the atlas threshold): midpointFanCenterAAPatches batches beside the fans.
+SCENES["feathered_s33"] = lambda: scene.feathered(seed=33)
 
 # Frames of real content: the reference's own silver renderer-call streams
 # (tests/unit_tests/silvers/*.sriv, recorded by its SerializingFactory while

@@ -173,9 +173,7 @@ def test_golden_captures_reproduce_from_reference(name):
     assert oracle.reference_capture(scene_bytes) == cap_bytes
 
 
-def test_feather_table_matches_the_reference_table():
-    """The oracle's Gaussian-integral table, built from the published
-    generator, equals the fp16 table the reference ships."""
+def _reference_f16_table(name):
     import os
     import re
     import pytest
@@ -183,10 +181,26 @@ def test_feather_table_matches_the_reference_table():
     if not os.path.exists(src):
         pytest.skip("reference sources absent")
     text = open(src).read()
-    body = text[text.index("const uint16_t g_gaussianIntegralTableF16[GAUSSIAN_TABLE_SIZE] = {"):]
+    body = text[text.index(f"const uint16_t {name}[GAUSSIAN_TABLE_SIZE] = {{"):]
     body = body[body.index("{") + 1:body.index("};")]
-    want = [int(v, 16) for v in re.findall(r"0x[0-9a-fA-F]+", body)]
+    return [int(v, 16) for v in re.findall(r"0x[0-9a-fA-F]+", body)]
+
+
+def test_feather_table_matches_the_reference_table():
+    """The oracle's Gaussian-integral table, built from the published
+    generator, equals the fp16 table the reference ships."""
+    want = _reference_f16_table("g_gaussianIntegralTableF16")
     got = oracle.feather_table().tolist()
+    assert len(want) == 512
+    diff = [i for i in range(512) if got[i] != want[i]]
+    assert diff == [], (diff[:8], [(got[i], want[i]) for i in diff[:8]])
+
+
+def test_inverse_feather_table_matches_the_reference_table():
+    """The inverse table feathered-fill tessellation softens curves with
+    equals the reference's shipped fp16 inverse table."""
+    want = _reference_f16_table("g_inverseGaussianIntegralTableF16")
+    got = oracle.inverse_feather_table().tolist()
     assert len(want) == 512
     diff = [i for i in range(512) if got[i] != want[i]]
     assert diff == [], (diff[:8], [(got[i], want[i]) for i in diff[:8]])
