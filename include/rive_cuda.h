@@ -69,6 +69,7 @@ enum
 enum
 {
     RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES = 0,
+    RIVE_CUDA_DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES = 1, /* feathered fills */
     RIVE_CUDA_DRAW_OUTER_CURVE_PATCHES = 2,   /* interior triangulation: the curves */
     RIVE_CUDA_DRAW_INTERIOR_TRIANGULATION = 3, /* ... and the interior triangles  */
 };
@@ -367,8 +368,10 @@ int rive_cuda_graph_stats(const rive_cuda_graph* graph, rive_cuda_flush_stats* o
  * The 512 fp16 entries of the feather table the passes sample (the integral of
  * the normal distribution over -3..+3 standard deviations; the reference ships
  * the same table as gpu::g_gaussianIntegralTableF16, gpu.hpp:2083-2091).
- * Feathered strokes (ENABLE_FEATHER in midpoint-fan batches) are rendered;
- * feathered fills (midpointFanCenterAAPatches, the feather atlas) are not.
+ * Feathers below the feather atlas's 32-pixel radius are rendered: strokes
+ * in midpoint-fan batches and fills in midpointFanCenterAAPatches batches
+ * (draw type 1), both with ENABLE_FEATHER. The feather atlas (larger
+ * feathers) is not built.
  */
 int rive_cuda_feather_table(uint16_t* out);
 

@@ -22,7 +22,9 @@ SOURCES = ["context.cu", "kernels_tess.cu", "kernels_raster.cu", "flush_noalloc.
 HEADERS = ["rive_cuda_internal.cuh"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+# Host code unfused (-ffp-contract=off): the feather tables it generates must
+# round the same on x86 and Arm.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
 
 

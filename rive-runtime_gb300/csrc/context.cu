@@ -41,6 +41,10 @@ __global__ void interior_setup_kernel(BatchTables B,
                                       TriRecord* tris,
                                       uint32_t* tileCounts,
                                       uint8_t* tileMasks);
+__global__ void center_setup_kernel(BatchTables B,
+                                    TriRecord* tris,
+                                    uint32_t* tileCounts,
+                                    uint8_t* tileMasks);
 __global__ void scene_uniforms_kernel(FlushParams* scenes, uint32_t sceneCount);
 __global__ void bin_fill_kernel(const uint32_t* pairTotal,
                                 uint32_t capacity,
@@ -163,7 +167,7 @@ struct rive_cuda_context
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
     uint32_t tessWidth = 0, tessHeight = 0, gradWidth = 0, gradHeight = 0;
-    DeviceBuffer tris, tileCounts, tileMasks, offsets;
+    DeviceBuffer tris, tileCounts, tileMasks, offsets, featherPlanes;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
     DeviceBuffer dTables;  // batch tables (device)
     HostBuffer hTables;    // pinned staging of the tables
@@ -194,7 +198,7 @@ struct rive_cuda_graph
 {
     rive_cuda_context* ctx = nullptr;
     DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
-        scanTemp, sortTemp, ranges, error;
+        scanTemp, sortTemp, ranges, error, featherPlanes;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -317,10 +321,11 @@ int setup_list(uint32_t drawType)
     return drawType == DRAW_MIDPOINT_FAN_PATCHES  ? 0
            : drawType == DRAW_OUTER_CURVE_PATCHES ? 1
            : drawType == DRAW_INTERIOR_TRIANGULATION ? 2
-                                                     : -1;
+           : drawType == DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES ? 3
+                                                             : -1;
 }
-constexpr uint32_t kTrianglesPerItem[kSetupLists] = {kPatchTriangleCount,
-                                                     kOuterPatchTriangleCount, 1};
+constexpr uint32_t kTrianglesPerItem[kSetupLists] = {
+    kPatchTriangleCount, kOuterPatchTriangleCount, 1, kCenterPatchTriangleCount};
 
 // Items (patch instances or triangles) of a draw batch.
 uint32_t batch_items(const rive_cuda_draw_batch& b)
@@ -371,11 +376,12 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         if (list < 0)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
                              b.draw_type);
-        // ENABLE_FEATHER is built for midpoint-fan batches: feathered
-        // strokes (a feathered fill's vertices report ERR_FEATHER).
-        if ((b.shader_features & SF_FEATHER) && b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
+        // ENABLE_FEATHER: feathered strokes draw in midpoint-fan batches,
+        // feathered fills in center-AA midpoint-fan batches.
+        if ((b.shader_features & SF_FEATHER) && b.draw_type != DRAW_MIDPOINT_FAN_PATCHES &&
+            b.draw_type != DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
-                             "feathered fills (draw type %u) not supported", b.draw_type);
+                             "feathered draws of draw type %u not supported", b.draw_type);
         if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
                              "shader misc flags 0x%x not supported (rasterOrdering: clockwiseFill only)",
@@ -526,6 +532,7 @@ struct Scratch
     size_t sortTempBytes = 0;
     uint2* ranges = nullptr;
     uint32_t* error = nullptr;
+    float4* featherPlanes = nullptr; // 2 per slot, only with center-AA patches
 };
 
 // Fills the table blob (host memory) and returns the device view of it.
@@ -601,7 +608,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
         gAcc += d->grad_span_count;
         tAcc += d->tess_span_count;
         tileAcc += P.tilesX * ((d->render_target_height + ts - 1) / ts);
-        // Slots follow the draw list order across all three set-up lists.
+        // Slots follow the draw list order across all the set-up lists.
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
         {
             const rive_cuda_draw_batch& db = d->draw_batches[b];
@@ -642,6 +649,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
     }
     B.sceneCount = L.n;
     B.tileLog2 = L.tileLog2;
+    B.featherPlanes = S.featherPlanes;
     B.totalGradSpans = gAcc;
     B.totalTessSpans = tAcc;
     B.totalTiles = tileAcc;
@@ -686,6 +694,9 @@ int enqueue_front(rive_cuda_context* ctx,
         if (L.items[2])
             interior_setup_kernel<<<(L.items[2] + 255) / 256, 256, 0, stream>>>(B, S.tris, S.counts,
                                                                                 S.masks);
+        if (L.items[3])
+            center_setup_kernel<<<(L.items[3] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
+                                                                          S.masks);
         stage_end(ctx, stream);
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
         size_t tempBytes = S.scanTempBytes;
@@ -849,6 +860,8 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->tileCounts.reserve((size_t)std::max(L.slots, 1u) * 4));
     CK(ctx->tileMasks.reserve((size_t)std::max(L.slots, 1u)));
     CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
+    if (L.items[3])
+        CK(ctx->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     const size_t scanBytes = scan_temp_bytes(L.slots);
     CK(ctx->scanTemp.reserve(scanBytes));
     ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
@@ -859,6 +872,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.tess = (uint4*)ctx->tess.ptr;
     S.grad = (uchar4*)ctx->grad.ptr;
     S.tris = (TriRecord*)ctx->tris.ptr;
+    S.featherPlanes = L.items[3] ? (float4*)ctx->featherPlanes.ptr : nullptr;
     S.counts = (uint32_t*)ctx->tileCounts.ptr;
     S.masks = (uint8_t*)ctx->tileMasks.ptr;
     S.offsets = (uint32_t*)ctx->offsets.ptr;
@@ -900,7 +914,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     if (rc)
         return rc;
     ctx->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
-    ctx->stats.patches = (uint64_t)L.items[0] + L.items[1];
+    ctx->stats.patches = (uint64_t)L.items[0] + L.items[1] + L.items[3];
     ctx->stats.triangles = L.slots;
     ctx->stats.bin_entries = pairs;
     ctx->stats.tiles = L.tiles;
@@ -973,7 +987,7 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         r.device.release();
     }
     for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->tileMasks,
-                            &ctx->offsets,
+                            &ctx->offsets, &ctx->featherPlanes,
                             &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
                             &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables})
         b->release();
@@ -1239,7 +1253,7 @@ void graph_free(rive_cuda_graph* g)
         cudaGraphDestroy(g->graph);
     for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->masks, &g->offsets,
                             &g->keys, &g->vals, &g->keysAlt, &g->valsAlt, &g->scanTemp,
-                            &g->sortTemp, &g->ranges, &g->error})
+                            &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes})
         b->release();
     if (g->hError)
         cudaFreeHost(g->hError);
@@ -1267,6 +1281,8 @@ int graph_build(rive_cuda_context* ctx,
     CK(g->counts.reserve((size_t)std::max(L.slots, 1u) * 4));
     CK(g->masks.reserve((size_t)std::max(L.slots, 1u)));
     CK(g->offsets.reserve((size_t)L.slots * 4 + 4));
+    if (L.items[3])
+        CK(g->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(g->error.reserve(4));
     const size_t scanBytes = scan_temp_bytes(L.slots);
@@ -1278,6 +1294,7 @@ int graph_build(rive_cuda_context* ctx,
     S.tess = (uint4*)g->tess.ptr;
     S.grad = (uchar4*)g->grad.ptr;
     S.tris = (TriRecord*)g->tris.ptr;
+    S.featherPlanes = L.items[3] ? (float4*)g->featherPlanes.ptr : nullptr;
     S.counts = (uint32_t*)g->counts.ptr;
     S.masks = (uint8_t*)g->masks.ptr;
     S.offsets = (uint32_t*)g->offsets.ptr;
@@ -1341,7 +1358,7 @@ int graph_build(rive_cuda_context* ctx,
     CK(e);
     CK(cudaGraphInstantiate(&g->exec, g->graph, 0));
     g->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
-    g->stats.patches = (uint64_t)L.items[0] + L.items[1];
+    g->stats.patches = (uint64_t)L.items[0] + L.items[1] + L.items[3];
     g->stats.triangles = L.slots;
     g->stats.bin_entries = g->measured;
     g->stats.tiles = L.tiles;

@@ -206,6 +206,97 @@ __device__ __forceinline__ void outer_triangle(int t, int& a, int& b, int& c)
     c = fan + i + 2 * step;
 }
 
+// The midpointFanCenterAA patch vertex table (gpu.cpp:446-560,
+// PatchType::midpointFanCenterAA), by vertex index: an AA ramp centred on the
+// curve on each side (coverage 1/2 on the curve), the 9-vertex fan and the
+// contour midpoint. Feathered fills draw with it.
+__device__ __forceinline__ PatchVertexDesc center_vertex_desc(int v)
+{
+    constexpr int kRampVerts = 4 * kPatchSegmentSpan;
+    PatchVertexDesc d;
+    auto set = [&d](float l, float o, float c, float ml, float mo, float mc) {
+        d.localVertexID = l; d.outset = o; d.fillCoverage = c;
+        d.mLocalVertexID = ml; d.mOutset = mo; d.mFillCoverage = mc;
+    };
+    if (v < 2 * kRampVerts)
+    {
+        const bool bottom = v >= kRampVerts;
+        const int u = bottom ? v - kRampVerts : v;
+        const float l = (float)(u >> 2), r = l + 1.f;
+        d.vertexType = STROKE_VERTEX;
+        if (!bottom)
+        {
+            switch (u & 3)
+            {
+                case 0: set(l, 0.f, .5f, r - 1.f, 0.f, .5f); break;
+                case 1: set(l, 1.f, 0.f, l - 1.f, 0.f, .5f); break;
+                case 2: set(r, 0.f, .5f, r - 1.f, 1.f, 0.f); break;
+                default: set(r, 1.f, 0.f, l - 1.f, 1.f, 0.f); break;
+            }
+        }
+        else
+        {
+            switch (u & 3)
+            {
+                case 0: set(l, -0.f, .5f, r - 1.f, -0.f, .5f); break;
+                case 1: set(r, -0.f, .5f, r - 1.f, -1.f, 0.f); break;
+                case 2: set(l, -1.f, 0.f, l - 1.f, -0.f, .5f); break;
+                default: set(r, -1.f, 0.f, l - 1.f, -1.f, 0.f); break;
+            }
+        }
+    }
+    else if (v < 2 * kRampVerts + kPatchSegmentSpan + 1)
+    {
+        const float i = (float)(v - 2 * kRampVerts);
+        d.vertexType = FAN_VERTEX;
+        set(i, 0.f, 1.f, i - 1.f, 0.f, 1.f);
+    }
+    else
+    {
+        d.vertexType = FAN_MIDPOINT_VERTEX;
+        set(0.f, 0.f, 1.f, 0.f, 0.f, 1.f);
+    }
+    return d;
+}
+
+// The midpointFanCenterAA index table, by triangle index: the top ramp
+// (0,1,2 / 2,1,3 per segment), the bottom ramp (0,2,1 / 1,2,3), the
+// middle-out fan (steps 1, 2, 4) and the triangle to the midpoint.
+__device__ __forceinline__ void center_triangle(int t, int& a, int& b, int& c)
+{
+    constexpr int kRamp = 2 * kPatchSegmentSpan;
+    if (t < kRamp)
+    {
+        const int e = (t >> 1) * 4;
+        if ((t & 1) == 0) { a = e; b = e + 1; c = e + 2; }
+        else { a = e + 2; b = e + 1; c = e + 3; }
+        return;
+    }
+    if (t < 2 * kRamp)
+    {
+        const int u = t - kRamp;
+        const int e = 4 * kPatchSegmentSpan + (u >> 1) * 4;
+        if ((u & 1) == 0) { a = e; b = e + 2; c = e + 1; }
+        else { a = e + 1; b = e + 2; c = e + 3; }
+        return;
+    }
+    const int fan = 8 * kPatchSegmentSpan;
+    const int u = t - 2 * kRamp;
+    if (u == 7)
+    {
+        a = fan;
+        b = fan + kPatchSegmentSpan;
+        c = fan + kPatchSegmentSpan + 1;
+        return;
+    }
+    const int step = u < 4 ? 1 : (u < 6 ? 2 : 4);
+    const int first = u < 4 ? 0 : (u < 6 ? 4 : 6);
+    const int i = (u - first) * 2 * step;
+    a = fan + i;
+    b = fan + i + step;
+    c = fan + i + 2 * step;
+}
+
 __device__ __forceinline__ float2 mat_mul(float4 m, float2 v)
 {
     // float2x2 columns (m.x, m.y) and (m.z, m.w).
@@ -230,9 +321,39 @@ struct VertexOut
 {
     float2 pos;
     float2 cov;
+    float2 cov2; // feathered fills: cotTheta and y0 of the corner
     uint32_t pathID;
     bool discard;
 };
+
+// GLSL mod(x, y) = x - y * floor(x / y)
+__device__ __forceinline__ float glsl_mod(float x, float y)
+{
+    return __fsub_rn(x, __fmul_rn(y, floorf(__fdiv_rn(x, y))));
+}
+
+// pack_feathered_fill_coverages (draw_path_common.glsl:107-149): a spoke of a
+// feather join carries the corner's angle as (cotTheta, y0) and its position
+// in the corner's local frame as (x, y).
+__device__ void pack_feathered_fill_coverages(float cornerTheta, float2 spokeNorm, float outset,
+                                              float2& cov, float2& cov2)
+{
+    const float ao = fabsf(outset);
+    const float cx = __fmul_rn(__fsub_rn(1.f, __fmul_rn(spokeNorm.x, ao)), .5f);
+    const float cy = __fmul_rn(__fsub_rn(1.f, __fmul_rn(spokeNorm.y, ao)), .5f);
+    float cotTheta = 0.f, y0 = 0.f;
+    if (!(fabsf(__fsub_rn(cornerTheta, kPi * .5f)) < 1.f / kHorizontalCotangentThreshold))
+    {
+        const float tanTheta = tanf(cornerTheta);
+        cotTheta = __fdiv_rn(signf(__fsub_rn(kPi * .5f, cornerTheta)),
+                             fmaxf(fabsf(tanTheta), 1.f / kHorizontalCotangentValue));
+        y0 = cotTheta >= 0.f ? __fsub_rn(cy, __fmul_rn(__fsub_rn(1.f, cx), tanTheta))
+                             : __fadd_rn(cy, __fmul_rn(cx, tanTheta));
+    }
+    cov = make_float2(__fadd_rn(fmaxf(cx, 0.f), kFeatherXCoordBias),
+                      __fadd_rn(-cy, kFeatherCoverageBias));
+    cov2 = make_float2(cotTheta, y0);
+}
 
 __device__ __forceinline__ bool tess_fetch(const FlushParams& P, long long idx, uint4& out)
 {
@@ -284,12 +405,6 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     float2 translate = make_float2(__uint_as_float(r1.x), __uint_as_float(r1.y));
     float strokeRadius = __uint_as_float(r1.z);
     float featherRadius = __uint_as_float(r1.w);
-    if (featherRadius != 0.f && strokeRadius == 0.f)
-    {
-        // Feathered fills draw as midpointFanCenterAA patches (not built).
-        atomicOr(P.error, ERR_FEATHER);
-        return false;
-    }
     uint32_t mirrored = flags & MIRRORED_CONTOUR_CONTOUR_FLAG;
     if (mirrored)
     {
@@ -321,13 +436,79 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
         }
         flags = (tv.w & ~MIRRORED_CONTOUR_CONTOUR_FLAG) | mirrored;
     }
-    float theta = __uint_as_float(tv.z);
+    float theta;
+    float joinEdge0Theta = 0.f, joinCornerTheta = 0.f;
+    const bool featherJoin =
+        (flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG && pv.vertexType == STROKE_VERTEX;
+    if (featherJoin)
+    {
+        // draw_path_common.glsl:372-468: a feather join steps between the
+        // tangents of the tessellation vertices just before and after it:
+        // backward segments first (erasing coverage outside the corner), one
+        // zero-width helper, then forward segments.
+        float joinVertexID = (float)(tv.z & 0xffffu);
+        float joinSegmentCount = (float)(tv.z >> 16);
+        int off0 = (int)(-joinVertexID - 1.f);
+        int off1 = (int)(__fadd_rn(__fsub_rn(joinSegmentCount, joinVertexID), 1.f));
+        if (flags & MIRRORED_CONTOUR_CONTOUR_FLAG)
+        {
+            off0 = -off0;
+            off1 = -off1;
+        }
+        uint4 before, after;
+        if (!tess_fetch(P, tessVertexIdx + off0, before) ||
+            !tess_fetch(P, tessVertexIdx + off1, after))
+            return false;
+        if ((after.w & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)) !=
+            (before.w & (MIRRORED_CONTOUR_CONTOUR_FLAG | 0xffffu)))
+        {
+            if (!tess_fetch(P, vertexIndex0, after))
+                return false;
+        }
+        joinEdge0Theta = __uint_as_float(before.z);
+        const float joinEdge1Theta = __uint_as_float(after.z);
+        joinCornerTheta = __fsub_rn(joinEdge1Theta, joinEdge0Theta);
+        if (fabsf(joinCornerTheta) > kPi)
+            joinCornerTheta = __fsub_rn(joinCornerTheta, __fmul_rn(k2Pi, signf(joinCornerTheta)));
+        const float nonHelper =
+            __fsub_rn(__fadd_rn(joinSegmentCount, 1.f), kFeatherJoinHelperVertexCount);
+        const float forward =
+            fminf(fmaxf(rintf(__fmul_rn(__fdiv_rn(fabsf(joinCornerTheta), kPi), nonHelper)), 1.f),
+                  __fsub_rn(nonHelper, 1.f));
+        const float backward = __fsub_rn(nonHelper, forward);
+        if (joinVertexID <= backward)
+        {
+            joinCornerTheta = -__fsub_rn(__fmul_rn(kPi, signf(joinCornerTheta)), joinCornerTheta);
+            joinSegmentCount = backward;
+            if (joinVertexID == backward)
+                outset = -outset;
+        }
+        else if (joinVertexID == __fadd_rn(backward, 1.f))
+        {
+            joinVertexID = 0.f;
+            joinSegmentCount = 0.f;
+            outset = 0.f;
+        }
+        else
+        {
+            joinVertexID = __fsub_rn(joinVertexID, __fadd_rn(backward, 2.f));
+            joinSegmentCount = forward;
+        }
+        theta = joinVertexID == joinSegmentCount
+                    ? joinEdge1Theta
+                    : __fadd_rn(joinEdge0Theta,
+                                __fmul_rn(joinCornerTheta, __fdiv_rn(joinVertexID, joinSegmentCount)));
+    }
+    else
+    {
+        theta = __uint_as_float(tv.z);
+    }
     float sn, cs;
     sincosf(theta, &sn, &cs);
     float2 norm = make_float2(sn, -cs);
     float2 origin = make_float2(__uint_as_float(tv.x), __uint_as_float(tv.y));
     float2 offset = make_float2(0.f, 0.f);
-    float2 cov;
+    float2 cov, cov2 = make_float2(0.f, 0.f);
     o.discard = false;
     if (featherRadius != 0.f)
     {
@@ -448,14 +629,43 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     else
     {
         cov = make_float2(fillCoverage, -1.f);
-        // sign(MUL(outset * norm, inverse(M))): the row vector times the
-        // adjugate, signed by the determinant (no division needed).
-        float2 on = make_float2(__fmul_rn(norm.x, outset), __fmul_rn(norm.y, outset));
-        float det = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
-        float sd = signf(det);
-        float rx = __fsub_rn(__fmul_rn(on.x, M.w), __fmul_rn(on.y, M.y));
-        float ry = __fsub_rn(__fmul_rn(on.y, M.x), __fmul_rn(on.x, M.z));
-        offset = make_float2(signf(rx) * sd * kAARadius, signf(ry) * sd * kAARadius);
+        if (featherRadius != 0.f)
+        {
+            // draw_path_common.glsl:659-741: a feathered edge; the spokes of a
+            // feather join carry their corner.
+            cov.y = kFeatherCoverageBias;
+            cov2 = make_float2(kHorizontalCotangentValue, fillCoverage);
+            if (featherJoin)
+            {
+                if (joinCornerTheta < 0.f)
+                {
+                    joinEdge0Theta = __fadd_rn(joinEdge0Theta, joinCornerTheta);
+                    joinCornerTheta = -joinCornerTheta;
+                }
+                float spoke = __fsub_rn(theta, joinEdge0Theta);
+                spoke = __fsub_rn(glsl_mod(__fadd_rn(spoke, kPi * .5f), k2Pi), kPi * .5f);
+                spoke = fminf(fmaxf(spoke, 0.f), joinCornerTheta);
+                if (spoke > __fmul_rn(joinCornerTheta, .5f))
+                    spoke = __fsub_rn(joinCornerTheta, spoke);
+                float ss, sc;
+                sincosf(spoke, &ss, &sc);
+                pack_feathered_fill_coverages(joinCornerTheta, make_float2(ss, sc), outset, cov,
+                                              cov2);
+            }
+            const float r = __fmul_rn(outset, featherRadius);
+            offset = mat_mul(M, make_float2(__fmul_rn(norm.x, r), __fmul_rn(norm.y, r)));
+        }
+        else
+        {
+            // sign(MUL(outset * norm, inverse(M))): the row vector times the
+            // adjugate, signed by the determinant (no division needed).
+            float2 on = make_float2(__fmul_rn(norm.x, outset), __fmul_rn(norm.y, outset));
+            float det = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
+            float sd = signf(det);
+            float rx = __fsub_rn(__fmul_rn(on.x, M.w), __fmul_rn(on.y, M.y));
+            float ry = __fsub_rn(__fmul_rn(on.y, M.x), __fmul_rn(on.x, M.z));
+            offset = make_float2(signf(rx) * sd * kAARadius, signf(ry) * sd * kAARadius);
+        }
         if (((flags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
             ((flags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
             cov.x = -cov.x;
@@ -470,6 +680,7 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     o.pos = make_float2(__fadd_rn(__fadd_rn(mo.x, offset.x), translate.x),
                         __fadd_rn(__fadd_rn(mo.y, offset.y), translate.y));
     o.cov = cov;
+    o.cov2 = cov2;
     o.pathID = pathID;
     return true;
 }
@@ -567,7 +778,8 @@ __device__ bool setup_triangle(const FlushParams& P,
                                uint32_t features,
                                uint32_t scene,
                                TriRecord& T,
-                               int4& bb)
+                               int4& bb,
+                               float4* featherPlanes = nullptr)
 {
     bb = make_int4(0, 0, 0, 0);
     if (A.discard || B.discard || C.discard)
@@ -615,6 +827,17 @@ __device__ bool setup_triangle(const FlushParams& P,
     const uint2 paint = P.paints[P.firstPaint + A.pathID];
     T.cov0 = make_float4(A.cov.x + cxgx * ax + cxgy * ay, cxgx, cxgy, A.cov.y + cygx * ax + cygy * ay);
     T.cov1 = make_float4(cygx, cygy, __uint_as_float(paint.x), __uint_as_float(paint.y));
+    if (featherPlanes)
+    {
+        // The third and fourth coverage components of a feathered fill, as
+        // planes anchored at the first (snapped) vertex.
+        const float zgx = ((B.cov2.x - A.cov2.x) * d2y - (C.cov2.x - A.cov2.x) * d1y) * inv;
+        const float zgy = ((C.cov2.x - A.cov2.x) * d1x - (B.cov2.x - A.cov2.x) * d2x) * inv;
+        const float wgx = ((B.cov2.y - A.cov2.y) * d2y - (C.cov2.y - A.cov2.y) * d1y) * inv;
+        const float wgy = ((C.cov2.y - A.cov2.y) * d1x - (B.cov2.y - A.cov2.y) * d2x) * inv;
+        featherPlanes[0] = make_float4(A.cov2.x, zgx, zgy, A.cov2.y);
+        featherPlanes[1] = make_float4(wgx, wgy, p0.x, p0.y);
+    }
     // The fp16 coverage key of the path (draw_raster_order_path.frag: pathID
     // bits, sign bit flipped for even-odd fills).
     uint32_t key = A.pathID == 0 ? 0u : ((A.pathID + MAX_DENORM_F16) * P.pathIDGranularity) & 0xffffu;
@@ -708,19 +931,22 @@ __device__ __forceinline__ void count_tiles(bool has,
 
 // Patch set-up, one warp per patch instance of the batch: shade the patch's
 // vertices, assemble and set up its triangles, then count the tiles each one
-// touches. kOuter selects the outer-curve patch (interior triangulation)
-// instead of the midpoint fan. Triangle slot order is primitive order (flush,
-// draw batch, instance, triangle-in-patch).
-template <bool kOuter>
+// touches. kList selects the patch: 0 the midpoint fan, 1 the outer-curve
+// patch (interior triangulation), 3 the center-AA midpoint fan (feathered
+// fills). Triangle slot order is primitive order (flush, draw batch,
+// instance, triangle-in-patch).
+template <int kList>
 __device__ __forceinline__ void patch_setup(const BatchTables& B,
                                             TriRecord* __restrict__ tris,
                                             uint32_t* __restrict__ tileCounts,
                                             uint8_t* __restrict__ tileMasks)
 {
-    constexpr int kVerts = kOuter ? kOuterPatchVertexCount : kPatchVertexCount;
-    constexpr int kTris = kOuter ? kOuterPatchTriangleCount : kPatchTriangleCount;
+    constexpr bool kOuter = kList == 1, kCenter = kList == 3;
+    constexpr int kVerts =
+        kOuter ? kOuterPatchVertexCount : (kCenter ? kCenterPatchVertexCount : kPatchVertexCount);
+    constexpr int kTris = kOuter ? kOuterPatchTriangleCount
+                                 : (kCenter ? kCenterPatchTriangleCount : kPatchTriangleCount);
     constexpr int kSpan = kOuter ? kOuterPatchSegmentSpan : kPatchSegmentSpan;
-    constexpr int kList = kOuter ? 1 : 0;
     constexpr int kTriPasses = (kTris + 31) / 32;
     __shared__ VertexOut sv[4][kVerts];
     __shared__ float4 sEdges[4][kTriPasses * 32][3];
@@ -742,7 +968,9 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     for (int v = lane; v < kVerts; v += 32)
     {
         VertexOut o;
-        const PatchVertexDesc pv = kOuter ? outer_vertex_desc(v) : patch_vertex_desc(v);
+        const PatchVertexDesc pv = kOuter    ? outer_vertex_desc(v)
+                                   : kCenter ? center_vertex_desc(v)
+                                             : patch_vertex_desc(v);
         if (!shade_patch_vertex(P, pv, kSpan, instance, o))
         {
             sok[w] = false;
@@ -752,6 +980,8 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     }
     __syncwarp();
     const uint32_t slot0 = S.slotBase + local * kTris;
+    // Feathered draws keep their fills' extra coverage planes per slot.
+    float4* const planes = (S.features & SF_FEATHER) ? B.featherPlanes : nullptr;
     for (int pass = 0; pass < kTriPasses; ++pass)
     {
         const int t = pass * 32 + lane;
@@ -763,11 +993,14 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             int ia, ib, ic;
             if (kOuter)
                 outer_triangle(t, ia, ib, ic);
+            else if (kCenter)
+                center_triangle(t, ia, ib, ic);
             else
                 patch_triangle(t, ia, ib, ic);
             TriRecord T;
             if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic], S.features, S.scene,
-                                         T, bb))
+                                         T, bb,
+                                         planes ? planes + 2 * (size_t)(slot0 + t) : nullptr))
             {
                 tris[slot0 + t] = T;
                 e[0] = T.e0;
@@ -792,7 +1025,7 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
                                                           uint32_t* __restrict__ tileCounts,
                                                           uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<false>(B, tris, tileCounts, tileMasks);
+    patch_setup<0>(B, tris, tileCounts, tileMasks);
 }
 
 __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
@@ -800,7 +1033,15 @@ __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
                                                           uint32_t* __restrict__ tileCounts,
                                                           uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<true>(B, tris, tileCounts, tileMasks);
+    patch_setup<1>(B, tris, tileCounts, tileMasks);
+}
+
+__global__ void __launch_bounds__(128) center_setup_kernel(BatchTables B,
+                                                           TriRecord* __restrict__ tris,
+                                                           uint32_t* __restrict__ tileCounts,
+                                                           uint8_t* __restrict__ tileMasks)
+{
+    patch_setup<3>(B, tris, tileCounts, tileMasks);
 }
 
 // Interior triangulation (DrawType::interiorTriangulation): one thread per
@@ -1385,7 +1626,7 @@ struct __align__(16) TileTri
     float4 v1; // C1, A1, B1, C2
     float4 v2; // A2, B2, covx at the tile origin, d covx/dx
     float4 v3; // d covx/dy, covy at the tile origin, d covy/dx, d covy/dy
-    uint4 v4;  // paint.x, paint.y, pathAndFeatures, unused
+    uint4 v4;  // paint.x, paint.y, pathAndFeatures, triangle slot
 };
 static_assert(sizeof(TileTri) == 80, "TileTri layout");
 
@@ -1421,6 +1662,47 @@ __device__ __forceinline__ float eval_feathered_stroke(float covx, float covy)
     c = __fsub_rn(c, feather_lut(__fadd_rn(1.f - kFeatherCoverageBias, covx)));
     c = __fsub_rn(c, feather_lut(__fsub_rn(1.f, covy)));
     return c;
+}
+
+// eval_feathered_fill (draw_path_common.glsl:152-240): the feather of a flat
+// edge, or, at a feather join, of a corner: the coverage of the first edge
+// plus a 4-sample Gaussian quadrature of the second edge's integral.
+__device__ float eval_feathered_fill(float cx, float cy, float cotTheta, float y0)
+{
+    y0 = fmaxf(y0, 0.f);
+    float featherCoverage = cotTheta >= 0.f ? feather_lut(y0) : 0.f;
+    if (fabsf(cotTheta) < kHorizontalCotangentThreshold)
+    {
+        const float x = __fsub_rn(fabsf(cx), kFeatherXCoordBias);
+        const float y = __fadd_rn(-cy, kFeatherCoverageBias);
+        const float dt = __fmul_rn(__fsub_rn(y, y0), 0.5984134206f);
+        const float k[4] = {0.20888568955f, 0.62665706865f, 1.04442844776f, 1.46219982687f};
+        const float c = __fadd_rn(__fmul_rn(y, cotTheta), x);
+        float sum = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            const float t = __fadd_rn(y0, __fmul_rn(dt, k[i]));
+            const float u = __fadd_rn(__fmul_rn(t, -cotTheta), c);
+            const float tt = __fadd_rn(__fmul_rn(t, 5.09593080173f), -2.54796540086f);
+            sum = __fadd_rn(sum, __fmul_rn(feather_lut(u), exp2f(-__fmul_rn(tt, tt))));
+        }
+        featherCoverage = __fadd_rn(featherCoverage, __fmul_rn(sum, dt));
+    }
+    return __fmul_rn(featherCoverage, signf(cx));
+}
+
+// A feathered fill's fragment: its third and fourth coverage components from
+// the slot's planes, then the feather.
+__device__ __noinline__ float feathered_fill_fragment(const float4* __restrict__ planes,
+                                                      uint32_t slot, float fx, float fy, float covx,
+                                                      float covy)
+{
+    const float4 f0 = planes[2 * (size_t)slot], f1 = planes[2 * (size_t)slot + 1];
+    const float dx = fx - f1.z, dy = fy - f1.w;
+    const float covz = f0.x + f0.y * dx + f0.z * dy;
+    const float covw = f0.w + f1.x * dx + f1.y * dy;
+    return eval_feathered_fill(covx, covy, covz, covw);
 }
 
 #ifndef RIVE_RASTER_MIN_BLOCKS
@@ -1509,7 +1791,8 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                                T.cov0.y);
             L.v3 = make_float4(T.cov0.z, T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x,
                                T.cov1.y);
-            L.v4 = make_uint4(__float_as_uint(T.cov1.z), __float_as_uint(T.cov1.w), T.meta.x, 0u);
+            L.v4 = make_uint4(__float_as_uint(T.cov1.z), __float_as_uint(T.cov1.w), T.meta.x,
+                              sortedSlots[k]);
             sTris[threadIdx.x] = L;
             const int4 bb = unpack_bbox(T.meta);
             const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;
@@ -1596,6 +1879,13 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                             ? eval_feathered_stroke(covx, covy)
                             : fminf(covx, covy);
                     count = fmaxf(frag, count);
+                }
+                else if (covy < kFeatherCoverageThreshold && ((T.v4.z >> 16) & SF_FEATHER) &&
+                         B.featherPlanes)
+                {
+                    // feathered fill (find_fill_coverage, draw_path.vert:511-519)
+                    count = count + feathered_fill_fragment(B.featherPlanes, T.v4.w, fx, fy,
+                                                            covx, covy);
                 }
                 else
                 {
@@ -1702,7 +1992,45 @@ void build_feather_table(float out[kGaussianTableSize])
 }
 } // namespace
 
-// Uploads the feather table to the current device (once per device).
+// Generator of the inverse feather table (renderer/src/gpu.cpp:2125-2190,
+// restated): the running integral of the normal distribution sampled 32 times
+// per entry; every cell whose centre the integral crosses gets the sample
+// height interpolated at the crossing, the middle cell exactly 1/2, the end
+// cells 0 and 1; then rounded to fp16.
+void build_inverse_feather_table(float out[kGaussianTableSize])
+{
+    constexpr int kPerEntry = 32;
+    constexpr int kSamples = kGaussianTableSize * kPerEntry;
+    float table[kGaussianTableSize] = {};
+    const float inverseSigma = 1 / (float)(kGaussianTableSize / (kGaussianStddevs * 2));
+    const float mu = kGaussianTableSize * .5f;
+    // Start the integral at -1/2 minus the left half, so it reaches 1/2 at mu.
+    float integral = 0;
+    for (int i = 0; i < (kSamples + 1) / 2; ++i)
+        integral += eval_normal_distribution((float)i / kPerEntry, mu, inverseSigma) / kPerEntry;
+    integral = .5 - integral;
+    table[0] = 0;
+    table[kGaussianTableSize - 1] = 1;
+    float prevX = NAN, prevY = 0;
+    for (int i = 0; i < kSamples; ++i)
+    {
+        integral += eval_normal_distribution((float)i / kPerEntry, mu, inverseSigma) / kPerEntry;
+        const float x = fminf(fmaxf(0, integral), 1) * kGaussianTableSize;
+        const float y = (i + .5f) / kSamples;
+        const size_t cell = (size_t)x;
+        const float centre = cell + .5f;
+        if (centre == mu)
+            table[cell] = .5f;
+        else if (prevX <= centre && x >= centre && cell < kGaussianTableSize)
+            table[cell] = prevY + (y - prevY) * ((centre - prevX) / (x - prevX));
+        prevX = x;
+        prevY = y;
+    }
+    for (int i = 0; i < kGaussianTableSize; ++i)
+        out[i] = __half2float(__float2half_rn(table[i]));
+}
+
+// Uploads the feather tables to the current device (once per device).
 cudaError_t ensure_feather_lut(int device)
 {
     static std::mutex m;
@@ -1713,6 +2041,11 @@ cudaError_t ensure_feather_lut(int device)
     float table[kGaussianTableSize];
     build_feather_table(table);
     cudaError_t e = cudaMemcpyToSymbol(g_featherLUT, table, sizeof(table));
+    if (e == cudaSuccess)
+    {
+        build_inverse_feather_table(table);
+        e = upload_inverse_feather_lut(table);
+    }
     if (e == cudaSuccess && device >= 0 && device < 64)
         done[device] = true;
     return e;

@@ -87,6 +87,137 @@ __device__ __forceinline__ float rive_atan2(float2 v)
     return v.y >= 0.f ? theta : -theta;
 }
 
+// The inverse feather table (the height at which the Gaussian integral
+// reaches x), fp16 values widened to float, written once per device by the
+// host before any flush.
+__device__ float g_inverseFeatherLUT[kGaussianTableSize];
+
+// INVERSE_FEATHER(x) (common.glsl:61-68): linear filter, clamp to edge.
+__device__ float inverse_feather_lut(float x)
+{
+    const float t = __fsub_rn(__fmul_rn(x, (float)kGaussianTableSize), .5f);
+    if (!(t == t))
+        return g_inverseFeatherLUT[0];
+    const float f = floorf(t);
+    const float w = __fsub_rn(t, f);
+    const int i0 = (int)fminf(fmaxf(f, -1.f), (float)kGaussianTableSize);
+    const int a = min(max(i0, 0), kGaussianTableSize - 1);
+    const int b = min(max(i0 + 1, 0), kGaussianTableSize - 1);
+    const float va = g_inverseFeatherLUT[a], vb = g_inverseFeatherLUT[b];
+    return __fadd_rn(va, __fmul_rn(__fsub_rn(vb, va), w));
+}
+
+// mix(x, y, a) = x * (1 - a) + y * a
+__device__ __forceinline__ float2 f2mix(float2 x, float2 y, float a)
+{
+    const float r = __fsub_rn(1.f, a);
+    return make_float2(__fadd_rn(__fmul_rn(x.x, r), __fmul_rn(y.x, a)),
+                       __fadd_rn(__fmul_rn(x.y, r), __fmul_rn(y.y, a)));
+}
+
+// clamp(a / b, 0, 1) without dividing when the result saturates
+// (bezier_utils.glsl:164-169).
+__device__ __forceinline__ float clamped_divide(float a, float b)
+{
+    if (b < 0.f)
+        a = -a;
+    b = fabsf(b);
+    return a > 0.f ? (a < b ? __fdiv_rn(a, b) : 1.f) : 0.f;
+}
+
+// The height of a cubic above its chord at its highest point, found with three
+// Newton steps from t = 1/2 (bezier_utils.glsl:173-245).
+__device__ float cubic_max_height(float2 p0, float2 p1, float2 p2, float2 p3, float& outT)
+{
+    const float2 base = f2sub(p3, p0);
+    const float lengthBase = __fsqrt_rn(f2dot(base, base));
+    if (lengthBase == 0.f)
+    {
+        outT = .5f;
+        return 0.f;
+    }
+    const float2 norm =
+        make_float2(__fdiv_rn(-base.y, lengthBase), __fdiv_rn(base.x, lengthBase));
+    const float h2 = f2dot(norm, f2sub(p2, p0));
+    const float h1 = f2dot(norm, f2sub(p1, p0));
+    const float dh = __fsub_rn(h1, h2);
+    const float a3 = __fmul_rn(3.f, dh);
+    const float b = __fsub_rn(-h1, dh);
+    const float c = h1;
+    float t = .5f;
+    for (int i = 0; i < 3; ++i)
+    {
+        const float a3t = __fmul_rn(a3, t);
+        t = clamped_divide(__fsub_rn(__fmul_rn(a3t, t), c), __fmul_rn(2.f, __fadd_rn(a3t, b)));
+    }
+    outT = t;
+    return fabsf(__fmul_rn(
+        t, __fadd_rn(__fmul_rn(t, __fadd_rn(__fmul_rn(t, a3), __fmul_rn(3.f, b))),
+                     __fmul_rn(3.f, c))));
+}
+
+// The turn, in radians, of a cubic's tangent across an arc length of about
+// 2 * desiredSpread centred at T (bezier_utils.glsl:77-153).
+__device__ float cubic_local_curvature(float2 p0, float2 p1, float2 p2, float2 p3, float T,
+                                       float desiredSpread)
+{
+    const float2 C = f2sub(p1, p0);
+    const float2 D = f2sub(p2, p1);
+    const float2 E = f2sub(p3, p0);
+    const float2 B = f2sub(D, C);
+    const float2 A = f2add(f2scale(D, -3.f), E);
+    float2 tangent =
+        f2scale(f2add(f2scale(f2add(f2scale(A, T), f2scale(B, 2.f)), T), C), 3.f);
+    const float lengthTan = __fsqrt_rn(f2dot(tangent, tangent));
+    if (lengthTan == 0.f)
+        return 0.f;
+    tangent = f2scale(tangent, __fdiv_rn(1.f, lengthTan));
+    const float a = __fmul_rn(2.f, f2dot(A, tangent));
+    const float c = __fadd_rn(
+        __fmul_rn(__fmul_rn(3.f, __fadd_rn(__fmul_rn(a, T), __fmul_rn(4.f, f2dot(B, tangent)))),
+                  T),
+        __fmul_rn(6.f, f2dot(C, tangent)));
+    const float maxDT = fminf(T, __fsub_rn(1.f, T));
+    const float maxSpread = __fmul_rn(__fadd_rn(__fmul_rn(__fmul_rn(a, maxDT), maxDT), c), maxDT);
+    const float targetSpread = fminf(desiredSpread, __fmul_rn(maxSpread, .9999f));
+    float dt;
+    if (a == 0.f)
+    {
+        dt = __fdiv_rn(targetSpread, c);
+    }
+    else
+    {
+        // The real root of a t^3 + c t - targetSpread (Cardano).
+        const float r = __fdiv_rn(1.f, a);
+        const float bb = __fmul_rn(c, r), cc = __fmul_rn(-targetSpread, r);
+        const float Q = __fmul_rn(-1.f / 3.f, bb), R = __fmul_rn(.5f, cc);
+        const float discr = __fsub_rn(__fmul_rn(R, R), __fmul_rn(__fmul_rn(Q, Q), Q));
+        if (discr < 0.f)
+        {
+            const float sqrtQ = __fsqrt_rn(Q);
+            const float th = acosf(__fdiv_rn(R, __fmul_rn(__fmul_rn(sqrtQ, sqrtQ), sqrtQ)));
+            dt = __fmul_rn(__fmul_rn(-2.f, sqrtQ),
+                           cosf(__fadd_rn(__fmul_rn(th, 1.f / 3.f), -kPi * 2.f / 3.f)));
+        }
+        else
+        {
+            float Aq = powf(__fadd_rn(fabsf(R), __fsqrt_rn(discr)), 1.f / 3.f);
+            if (R < 0.f)
+                Aq = -Aq;
+            dt = Aq != 0.f ? __fadd_rn(Aq, __fdiv_rn(Q, Aq)) : 0.f;
+        }
+    }
+    dt = fabsf(dt);
+    const float t0 = __fsub_rn(T, dt), t1 = __fadd_rn(T, dt);
+    const float2 dir0 = f2add(f2scale(f2add(f2scale(A, t0), f2scale(B, 2.f)), t0), C);
+    const float2 dir1 = f2add(f2scale(f2add(f2scale(A, t1), f2scale(B, 2.f)), t1), C);
+    float2 e0, e1;
+    cubic_tangents(p0, p1, p2, p3, e0, e1);
+    const float2 tan0 = t0 < 1e-3f ? e0 : dir0;
+    const float2 tan1 = t1 > 1.f - 1e-3f ? e1 : dir1;
+    return acosf(cos_between(tan0, tan1));
+}
+
 struct SpanSetup
 {
     float2 p0, p1, p2, p3;
@@ -146,9 +277,24 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
     }
     if (featherRadius != 0.f && strokeRadius == 0.f)
     {
-        atomicOr(P.error, ERR_FEATHER);
-        s.valid = false;
-        return s;
+        // tessellate.glsl:141-190: a feathered fill's cubic is pulled toward
+        // its chord, the more the more it curves within one standard
+        // deviation, mimicking the softening the feather gives a curve.
+        float maxHeightT;
+        const float height = cubic_max_height(s.p0, s.p1, s.p2, s.p3, maxHeightT);
+        const float oneStddev = __fmul_rn(featherRadius, 1.f / kGaussianStddevs);
+        const float curvature =
+            cubic_local_curvature(s.p0, s.p1, s.p2, s.p3, maxHeightT, oneStddev);
+        float dimming = __fsub_rn(1.f, __fmul_rn(curvature, 1.f / kPi));
+        const float2 base = f2sub(s.p3, s.p0);
+        const float stddevsPow2 = __fdiv_rn(f2dot(base, base), __fmul_rn(oneStddev, oneStddev));
+        dimming = fminf(dimming, __fmul_rn(__fsub_rn(stddevsPow2, 1.f), .5f));
+        dimming = fminf(dimming, .99f);
+        const float x =
+            __fadd_rn(__fmul_rn(inverse_feather_lut(__fmul_rn(.5f, dimming)), -2.f), 1.f);
+        const float softness = clamped_divide(__fmul_rn(x, featherRadius), height);
+        s.p1 = f2mix(s.p1, f2mix(s.p0, s.p3, 1.f / 3.f), softness);
+        s.p2 = f2mix(s.p2, f2mix(s.p0, s.p3, 2.f / 3.f), softness);
     }
     if (flags & CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG)
     {
@@ -338,9 +484,19 @@ __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flag
             theta = rive_atan2(f2sub(bcd, abc));
     }
     // GLSL mod(theta, 2pi) = theta - 2pi * floor(theta / 2pi)
-    float m = __fsub_rn(theta, __fmul_rn(k2Pi, floorf(__fdiv_rn(theta, k2Pi))));
-    return make_uint4(__float_as_uint(coord.x), __float_as_uint(coord.y),
-                      __float_as_uint(m), flags);
+    uint32_t z;
+    if ((flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG)
+    {
+        // tessellate.glsl:551-559: a feather join leaves its stepping to the
+        // draw pass, which needs the join's vertex and segment counts.
+        z = ((uint32_t)mergedSegmentCount << 16) | (uint32_t)mergedVertexID;
+    }
+    else
+    {
+        z = __float_as_uint(
+            __fsub_rn(theta, __fmul_rn(k2Pi, floorf(__fdiv_rn(theta, k2Pi)))));
+    }
+    return make_uint4(__float_as_uint(coord.x), __float_as_uint(coord.y), z, flags);
 }
 } // namespace
 
@@ -436,5 +592,9 @@ __global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
             row[px] = tess_vertex(s, vertexIdx, flags);
         }
     }
+}
+cudaError_t upload_inverse_feather_lut(const float table[kGaussianTableSize])
+{
+    return cudaMemcpyToSymbol(g_inverseFeatherLUT, table, sizeof(float) * kGaussianTableSize);
 }
 } // namespace rivecuda

@@ -23,8 +23,13 @@ constexpr int kPatchTriangleCount = 24;
 constexpr int kOuterPatchSegmentSpan = 17;   // OuterCubicPatchSegmentSpanPlusJoin
 constexpr int kOuterPatchVertexCount = 153;  // kOuterCurvePatchVertexCount
 constexpr int kOuterPatchTriangleCount = 83; // kOuterCurvePatchIndexCount / 3
+// Center-AA midpoint-fan patches (feathered fills; gpu.hpp:591-646): both AA
+// ramps of an 8-segment span, the 9-vertex fan and the midpoint vertex.
+constexpr int kCenterPatchVertexCount = 8 * 8 + 8 + 2;           // 74
+constexpr int kCenterPatchTriangleCount = (8 * 12 + 7 * 3 + 3) / 3; // 40
 // gpu::DrawType values (gpu.hpp:657-668).
 constexpr uint32_t DRAW_MIDPOINT_FAN_PATCHES = 0u;
+constexpr uint32_t DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES = 1u;
 constexpr uint32_t DRAW_OUTER_CURVE_PATCHES = 2u;
 constexpr uint32_t DRAW_INTERIOR_TRIANGULATION = 3u;
 
@@ -85,6 +90,13 @@ constexpr int kGaussianTableSize = 512;
 constexpr float kGaussianStddevs = 3.f;
 constexpr float kFeatherCoverageBias = -2.f;
 constexpr float kFeatherCoverageThreshold = -1.5f;
+constexpr float kFeatherXCoordBias = .25f;
+constexpr float kHorizontalCotangentThreshold = 1e3f;
+constexpr float kHorizontalCotangentValue = 1e6f;
+constexpr float kFeatherJoinHelperVertexCount = 3.f;
+// The inverse feather table for tessellation softening (kernels_tess.cu).
+cudaError_t upload_inverse_feather_lut(const float table[kGaussianTableSize]);
+void build_inverse_feather_table(float out[kGaussianTableSize]);
 // Uploads the feather table to a device once (kernels_raster.cu).
 cudaError_t ensure_feather_lut(int device);
 void feather_table_f16(uint16_t out[kGaussianTableSize]);
@@ -166,8 +178,9 @@ struct PatchSegment
 };
 
 // Set-up work lists: midpoint-fan patches, outer-curve patches, interior
-// triangles (items: instances, instances, triangles).
-constexpr int kSetupLists = 3;
+// triangles, center-AA midpoint-fan patches (items: instances, instances,
+// triangles, instances).
+constexpr int kSetupLists = 4;
 
 // The work of a batch of independent logical flushes ("scenes"); a single
 // flush is a batch of one. Every kernel maps its global work index to a scene
@@ -188,6 +201,10 @@ struct BatchTables
     uint32_t sceneCount;
     uint32_t totalGradSpans, totalTessSpans, totalTiles;
     int tileLog2; // raster tile size of this batch (3, 4 or 5)
+    // Per triangle slot, when the batch holds feathered fills: the planes of
+    // the feather coverage's third and fourth components (cotTheta, y0) as
+    // (z0, dz/dx, dz/dy, w0), (dw/dx, dw/dy, anchor x, anchor y).
+    float4* featherPlanes;
 };
 
 // Index j with base[j] <= i < base[j + 1] (empty ranges skipped), n >= 1.

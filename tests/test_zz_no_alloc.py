@@ -25,8 +25,10 @@ def _fits(cap):
 
 
 def _fans_only(cap):
-    # The no-allocation path draws midpoint fans only (no interior triangulation).
-    return not any(f.desc["has_triangle_vertices"] for f in cap.flushes)
+    # The no-allocation path draws midpoint-fan batches only (no interior
+    # triangulation, no center-AA fans of feathered fills).
+    return not any(f.desc["has_triangle_vertices"] or (f.batches[:, 0] != 0).any()
+                   for f in cap.flushes)
 
 
 def _device_buffers(cap):
