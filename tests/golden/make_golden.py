@@ -67,8 +67,9 @@ SCENES["feathered_s33"] = lambda: scene.feathered(seed=33)
 # (tests/unit_tests/silvers/*.sriv, recorded by its SerializingFactory while
 # .riv artboards animate), read by rive_runtime_gb300.sriv. Their fills are
 # mostly clockwise (FillRule::clockwise), with clip rects, nested clips,
-# gradients, blend modes and modulated opacity. Draws with feathered paints and
-# image draws are left out of the scenes (not part of this path).
+# gradients, blend modes and modulated opacity. Image draws are left out of the
+# scenes (not part of this path), and so are feathered draws except in the
+# FEATHERED_SILVERS frames below.
 SILVERS = {
     "silver_hunter_x_f0": ("hunter_x_demo", 0),
     "silver_rewards_f10": ("rewards_demo", 10),
@@ -80,15 +81,27 @@ SILVERS = {
 SILVER_DIR = os.path.join(oracle.REFERENCE_SOURCES, "tests", "unit_tests", "silvers")
 
 
-def _silver(stream, frame):
+# Real frames whose feathered draws all stay below the feather atlas
+# threshold, feathered draws kept: the reference front end draws their
+# feathered fills as midpointFanCenterAAPatches batches.
+FEATHERED_SILVERS = {
+    "silver_path_effect_feathers_f30": ("path_effect_with_feathers", 30),
+    "silver_text_feather_falloff_f30": ("text_feather_falloff", 30),
+    "silver_police_files_f60": ("game_menu_ad_police_files", 60),
+}
+
+
+def _silver(stream, frame, keep_feathered=False):
     from rive_runtime_gb300 import sriv
     with open(os.path.join(SILVER_DIR, stream + ".sriv"), "rb") as f:
         st = sriv.read_sriv(f.read())
-    return st.frame_scene(frame)[0]
+    return st.frame_scene(frame, keep_feathered=keep_feathered)[0]
 
 
 for _name, (_stream, _frame) in SILVERS.items():
     SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k))
+for _name, (_stream, _frame) in FEATHERED_SILVERS.items():
+    SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True))
 
 
 def _triangulated(sc):
