@@ -41,6 +41,10 @@ __global__ void interior_setup_kernel(BatchTables B,
                                       TriRecord* tris,
                                       uint32_t* tileCounts,
                                       uint8_t* tileMasks);
+__global__ void patch_setup_feather_kernel(BatchTables B,
+                                           TriRecord* tris,
+                                           uint32_t* tileCounts,
+                                           uint8_t* tileMasks);
 __global__ void center_setup_kernel(BatchTables B,
                                     TriRecord* tris,
                                     uint32_t* tileCounts,
@@ -65,18 +69,17 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    uint32_t tileCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
-__global__ void raster_tile_kernel(BatchTables B,
-                                   const TriRecord* tris,
-                                   const uint32_t* sortedSlots,
-                                   const uint2* ranges);
-__global__ void raster_tile8_kernel(BatchTables B,
-                                    const TriRecord* tris,
-                                    const uint32_t* sortedSlots,
-                                    const uint2* ranges);
-__global__ void raster_tile32_kernel(BatchTables B,
-                                     const TriRecord* tris,
-                                     const uint32_t* sortedSlots,
-                                     const uint2* ranges);
+// The raster kernels without and with the feather paths.
+#define RIVE_DECLARE_RASTER(NAME)                                                                  \
+    __global__ void NAME(BatchTables B, const TriRecord* tris, const uint32_t* sortedSlots,        \
+                         const uint2* ranges);
+RIVE_DECLARE_RASTER(raster_tile_kernel)
+RIVE_DECLARE_RASTER(raster_tile_feather_kernel)
+RIVE_DECLARE_RASTER(raster_tile8_kernel)
+RIVE_DECLARE_RASTER(raster_tile8_feather_kernel)
+RIVE_DECLARE_RASTER(raster_tile32_kernel)
+RIVE_DECLARE_RASTER(raster_tile32_feather_kernel)
+#undef RIVE_DECLARE_RASTER
 } // namespace rivecuda
 
 using namespace rivecuda;
@@ -180,7 +183,7 @@ struct rive_cuda_context
     int tileLog2 = kTileLog2;
     int rasterCtasPerSm = 0; // 0: as many as fit
     bool raster32Ready = false;
-    size_t rasterPad[2] = {};         // padding for the 8 and 16 pixel kernels
+    size_t rasterPad[2][2] = {};      // [feather variant][8 or 16 pixel kernel]: padding
     int rasterPadFor[2] = {-1, -1};   // the CTAs-per-SM limit it was found for
     // Stage timing (rive_cuda_set_profiling).
     bool profiling = false;
@@ -416,6 +419,7 @@ struct BatchLayout
     int tileLog2 = kTileLog2;
     uint32_t segCount[kSetupLists] = {}, items[kSetupLists] = {};
     uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0;
+    bool feather = false; // some batch draws with ENABLE_FEATHER
     uint64_t tessRows = 0, gradRows = 0;
     std::vector<uint64_t> tessRow0, gradRow0;
     // Table blob offsets.
@@ -466,6 +470,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             const int list = setup_list(db.draw_type);
             segs[list] += 1;
             items[list] += k;
+            if (db.shader_features & SF_FEATHER)
+                L.feather = true;
         }
         L.tessRow0[i] = L.tessRows;
         L.gradRow0[i] = L.gradRows;
@@ -686,7 +692,7 @@ int enqueue_front(rive_cuda_context* ctx,
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
         if (L.items[0])
-            patch_setup_kernel<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
+            (L.feather ? patch_setup_feather_kernel : patch_setup_kernel)<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
                                                                          S.masks);
         if (L.items[1])
             outer_setup_kernel<<<(L.items[1] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
@@ -735,13 +741,19 @@ int prepare_raster(rive_cuda_context* ctx)
     {
         CK(cudaFuncSetAttribute(raster_tile32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kRaster32SmemBytes));
+        CK(cudaFuncSetAttribute(raster_tile32_feather_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kRaster32SmemBytes));
         ctx->raster32Ready = true;
     }
     const int slot = ctx->tileLog2 == 3 ? 0 : ctx->tileLog2 == 4 ? 1 : -1;
     if (slot >= 0 && ctx->rasterCtasPerSm > 0 && ctx->rasterPadFor[slot] != ctx->rasterCtasPerSm)
     {
-        const void* fn = slot == 0 ? (const void*)raster_tile8_kernel : (const void*)raster_tile_kernel;
-        ctx->rasterPad[slot] = occupancy_pad(fn, slot == 0 ? 64 : 256, ctx->rasterCtasPerSm);
+        const void* fns[2][2] = {
+            {(const void*)raster_tile8_kernel, (const void*)raster_tile_kernel},
+            {(const void*)raster_tile8_feather_kernel, (const void*)raster_tile_feather_kernel}};
+        for (int f = 0; f < 2; ++f)
+            ctx->rasterPad[f][slot] =
+                occupancy_pad(fns[f][slot], slot == 0 ? 64 : 256, ctx->rasterCtasPerSm);
         cudaGetLastError(); // a failed query only leaves the launch unpadded
         ctx->rasterPadFor[slot] = ctx->rasterCtasPerSm;
     }
@@ -761,18 +773,20 @@ int launch_raster(rive_cuda_context* ctx,
 {
     if (L.tileLog2 == 3)
     {
-        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[0] : 0;
-        raster_tile8_kernel<<<L.tiles, 64, dyn, stream>>>(B, tris, sortedSlots, ranges);
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][0] : 0;
+        (L.feather ? raster_tile8_feather_kernel : raster_tile8_kernel)<<<L.tiles, 64, dyn, stream>>>(
+            B, tris, sortedSlots, ranges);
     }
     else if (L.tileLog2 == 5)
     {
-        raster_tile32_kernel<<<L.tiles, 1024, kRaster32SmemBytes, stream>>>(B, tris, sortedSlots,
-                                                                          ranges);
+        (L.feather ? raster_tile32_feather_kernel : raster_tile32_kernel)<<<
+            L.tiles, 1024, kRaster32SmemBytes, stream>>>(B, tris, sortedSlots, ranges);
     }
     else
     {
-        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[1] : 0;
-        raster_tile_kernel<<<L.tiles, 256, dyn, stream>>>(B, tris, sortedSlots, ranges);
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][1] : 0;
+        (L.feather ? raster_tile_feather_kernel : raster_tile_kernel)<<<L.tiles, 256, dyn, stream>>>(
+            B, tris, sortedSlots, ranges);
     }
     return RIVE_CUDA_OK;
 }

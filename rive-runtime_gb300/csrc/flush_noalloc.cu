@@ -26,6 +26,10 @@ __global__ void patch_setup_kernel(BatchTables B,
                                    TriRecord* tris,
                                    uint32_t* tileCounts,
                                    uint8_t* tileMasks);
+__global__ void patch_setup_feather_kernel(BatchTables B,
+                                           TriRecord* tris,
+                                           uint32_t* tileCounts,
+                                           uint8_t* tileMasks);
 __global__ void outer_setup_kernel(BatchTables B,
                                    TriRecord* tris,
                                    uint32_t* tileCounts,
@@ -47,6 +51,10 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
 __global__ void raster_tile_kernel(BatchTables B,
+                                   const TriRecord* tris,
+                                   const uint32_t* sortedSlots,
+                                   const uint2* ranges);
+__global__ void raster_tile_feather_kernel(BatchTables B,
                                    const TriRecord* tris,
                                    const uint32_t* sortedSlots,
                                    const uint2* ranges);
@@ -177,14 +185,17 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                     "gradient texture height %u exceeds the no-allocation limit %u rows",
                     d->grad_data_height, RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS);
     uint64_t instances = 0;
+    bool feather = false; // some batch draws with ENABLE_FEATHER
     for (uint32_t i = 0; i < d->draw_batch_count; ++i)
     {
         const rive_cuda_draw_batch& b = d->draw_batches[i];
+        feather = feather || (b.shader_features & SF_FEATHER) != 0;
         if (b.draw_type != RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES)
             return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "draw type %u not supported",
                         b.draw_type);
-        // Only midpoint-fan batches reach here; their feathered strokes are
-        // built (a feathered fill's vertices report ERR_FEATHER).
+        // Only midpoint-fan batches reach here, feathered strokes included
+        // (feathered fills draw in center-AA batches, which need the
+        // allocating path's per-slot coverage planes).
         if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
             return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                         "shader misc flags 0x%x not supported", b.shader_misc_flags);
@@ -336,7 +347,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     uint32_t pairs = 0;
     if (slots)
     {
-        patch_setup_kernel<<<(instAcc + 3) / 4, 128, 0, stream>>>(B, tris, counts, masks);
+        (feather ? patch_setup_feather_kernel : patch_setup_kernel)<<<(instAcc + 3) / 4, 128, 0,
+                                                                     stream>>>(B, tris, counts,
+                                                                               masks);
         size_t tempBytes = 0;
         CKN(cub::DeviceScan::InclusiveSum(nullptr, tempBytes, counts, offs + 1, slots, stream));
         if (tempBytes > kScanTempBytes)
@@ -378,7 +391,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                                                                   ranges);
         sortedSlots = v.Current();
     }
-    raster_tile_kernel<<<tiles, 256, 0, stream>>>(B, tris, sortedSlots, ranges);
+    (feather ? raster_tile_feather_kernel : raster_tile_kernel)<<<tiles, 256, 0, stream>>>(
+        B, tris, sortedSlots, ranges);
     CKN(cudaGetLastError());
 
     // Device status of this flush (overflow and range flags of the kernels).

@@ -321,7 +321,6 @@ struct VertexOut
 {
     float2 pos;
     float2 cov;
-    float2 cov2; // feathered fills: cotTheta and y0 of the corner
     uint32_t pathID;
     bool discard;
 };
@@ -368,11 +367,15 @@ __device__ __forceinline__ bool tess_fetch(const FlushParams& P, long long idx, 
 
 // unpack_tessellated_path_vertex for a midpointFan patch vertex, plus the
 // position math of @drawVertexMain. Returns false on a malformed input.
+// kFeather: compiled with the feather paths (ENABLE_FEATHER); without it a
+// path's feather radius is ignored.
+template <bool kFeather>
 __device__ bool shade_patch_vertex(const FlushParams& P,
                                    const PatchVertexDesc& pv,
                                    int span,
                                    uint32_t instanceID,
-                                   VertexOut& o)
+                                   VertexOut& o,
+                                   float2& cov2) // feathered fills: the corner's cotTheta, y0
 {
     int localVertexID = (int)pv.localVertexID;
     float outset = pv.outset;
@@ -404,7 +407,7 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
                            __uint_as_float(r0.z), __uint_as_float(r0.w));
     float2 translate = make_float2(__uint_as_float(r1.x), __uint_as_float(r1.y));
     float strokeRadius = __uint_as_float(r1.z);
-    float featherRadius = __uint_as_float(r1.w);
+    float featherRadius = kFeather ? __uint_as_float(r1.w) : 0.f;
     uint32_t mirrored = flags & MIRRORED_CONTOUR_CONTOUR_FLAG;
     if (mirrored)
     {
@@ -438,8 +441,8 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     }
     float theta;
     float joinEdge0Theta = 0.f, joinCornerTheta = 0.f;
-    const bool featherJoin =
-        (flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG && pv.vertexType == STROKE_VERTEX;
+    const bool featherJoin = kFeather && (flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG &&
+                             pv.vertexType == STROKE_VERTEX;
     if (featherJoin)
     {
         // draw_path_common.glsl:372-468: a feather join steps between the
@@ -508,7 +511,8 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     float2 norm = make_float2(sn, -cs);
     float2 origin = make_float2(__uint_as_float(tv.x), __uint_as_float(tv.y));
     float2 offset = make_float2(0.f, 0.f);
-    float2 cov, cov2 = make_float2(0.f, 0.f);
+    float2 cov;
+    cov2 = make_float2(0.f, 0.f);
     o.discard = false;
     if (featherRadius != 0.f)
     {
@@ -680,7 +684,6 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     o.pos = make_float2(__fadd_rn(__fadd_rn(mo.x, offset.x), translate.x),
                         __fadd_rn(__fadd_rn(mo.y, offset.y), translate.y));
     o.cov = cov;
-    o.cov2 = cov2;
     o.pathID = pathID;
     return true;
 }
@@ -779,7 +782,8 @@ __device__ bool setup_triangle(const FlushParams& P,
                                uint32_t scene,
                                TriRecord& T,
                                int4& bb,
-                               float4* featherPlanes = nullptr)
+                               float4* featherPlanes = nullptr,
+                               float2 zwA = {}, float2 zwB = {}, float2 zwC = {})
 {
     bb = make_int4(0, 0, 0, 0);
     if (A.discard || B.discard || C.discard)
@@ -831,11 +835,11 @@ __device__ bool setup_triangle(const FlushParams& P,
     {
         // The third and fourth coverage components of a feathered fill, as
         // planes anchored at the first (snapped) vertex.
-        const float zgx = ((B.cov2.x - A.cov2.x) * d2y - (C.cov2.x - A.cov2.x) * d1y) * inv;
-        const float zgy = ((C.cov2.x - A.cov2.x) * d1x - (B.cov2.x - A.cov2.x) * d2x) * inv;
-        const float wgx = ((B.cov2.y - A.cov2.y) * d2y - (C.cov2.y - A.cov2.y) * d1y) * inv;
-        const float wgy = ((C.cov2.y - A.cov2.y) * d1x - (B.cov2.y - A.cov2.y) * d2x) * inv;
-        featherPlanes[0] = make_float4(A.cov2.x, zgx, zgy, A.cov2.y);
+        const float zgx = ((zwB.x - zwA.x) * d2y - (zwC.x - zwA.x) * d1y) * inv;
+        const float zgy = ((zwC.x - zwA.x) * d1x - (zwB.x - zwA.x) * d2x) * inv;
+        const float wgx = ((zwB.y - zwA.y) * d2y - (zwC.y - zwA.y) * d1y) * inv;
+        const float wgy = ((zwC.y - zwA.y) * d1x - (zwB.y - zwA.y) * d2x) * inv;
+        featherPlanes[0] = make_float4(zwA.x, zgx, zgy, zwA.y);
         featherPlanes[1] = make_float4(wgx, wgy, p0.x, p0.y);
     }
     // The fp16 coverage key of the path (draw_raster_order_path.frag: pathID
@@ -935,7 +939,7 @@ __device__ __forceinline__ void count_tiles(bool has,
 // patch (interior triangulation), 3 the center-AA midpoint fan (feathered
 // fills). Triangle slot order is primitive order (flush, draw batch,
 // instance, triangle-in-patch).
-template <int kList>
+template <int kList, bool kFeather>
 __device__ __forceinline__ void patch_setup(const BatchTables& B,
                                             TriRecord* __restrict__ tris,
                                             uint32_t* __restrict__ tileCounts,
@@ -949,6 +953,8 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     constexpr int kSpan = kOuter ? kOuterPatchSegmentSpan : kPatchSegmentSpan;
     constexpr int kTriPasses = (kTris + 31) / 32;
     __shared__ VertexOut sv[4][kVerts];
+    // The feathered-fill coverage components, kept only for feathered draws.
+    __shared__ float2 sZW[4][kFeather ? kVerts : 1];
     __shared__ float4 sEdges[4][kTriPasses * 32][3];
     __shared__ int4 sBox[4][kTriPasses * 32];
     __shared__ uint32_t* sOut[4][kTriPasses * 32];
@@ -962,6 +968,8 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     const FlushParams& P = B.scenes[S.scene];
     const uint32_t local = gi - B.segBase[kList][seg];
     const uint32_t instance = S.baseElement + local;
+    // Feathered draws keep their fills' extra coverage planes per slot.
+    float4* const planes = (kFeather && (S.features & SF_FEATHER)) ? B.featherPlanes : nullptr;
     if (lane == 0)
         sok[w] = true;
     __syncwarp();
@@ -971,17 +979,18 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
         const PatchVertexDesc pv = kOuter    ? outer_vertex_desc(v)
                                    : kCenter ? center_vertex_desc(v)
                                              : patch_vertex_desc(v);
-        if (!shade_patch_vertex(P, pv, kSpan, instance, o))
+        float2 zw;
+        if (!shade_patch_vertex<kFeather>(P, pv, kSpan, instance, o, zw))
         {
             sok[w] = false;
             o.discard = true;
         }
         sv[w][v] = o;
+        if (kFeather && planes)
+            sZW[w][v] = zw;
     }
     __syncwarp();
     const uint32_t slot0 = S.slotBase + local * kTris;
-    // Feathered draws keep their fills' extra coverage planes per slot.
-    float4* const planes = (S.features & SF_FEATHER) ? B.featherPlanes : nullptr;
     for (int pass = 0; pass < kTriPasses; ++pass)
     {
         const int t = pass * 32 + lane;
@@ -999,8 +1008,10 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
                 patch_triangle(t, ia, ib, ic);
             TriRecord T;
             if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic], S.features, S.scene,
-                                         T, bb,
-                                         planes ? planes + 2 * (size_t)(slot0 + t) : nullptr))
+                                         T, bb, planes ? planes + 2 * (size_t)(slot0 + t) : nullptr,
+                                         planes ? sZW[w][kFeather ? ia : 0] : float2{},
+                                         planes ? sZW[w][kFeather ? ib : 0] : float2{},
+                                         planes ? sZW[w][kFeather ? ic : 0] : float2{}))
             {
                 tris[slot0 + t] = T;
                 e[0] = T.e0;
@@ -1025,7 +1036,16 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
                                                           uint32_t* __restrict__ tileCounts,
                                                           uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<0>(B, tris, tileCounts, tileMasks);
+    patch_setup<0, false>(B, tris, tileCounts, tileMasks);
+}
+
+// Midpoint-fan set-up with the feather paths, for batches that feather.
+__global__ void __launch_bounds__(128) patch_setup_feather_kernel(BatchTables B,
+                                                                  TriRecord* __restrict__ tris,
+                                                                  uint32_t* __restrict__ tileCounts,
+                                                                  uint8_t* __restrict__ tileMasks)
+{
+    patch_setup<0, true>(B, tris, tileCounts, tileMasks);
 }
 
 __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
@@ -1033,7 +1053,7 @@ __global__ void __launch_bounds__(128) outer_setup_kernel(BatchTables B,
                                                           uint32_t* __restrict__ tileCounts,
                                                           uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<1>(B, tris, tileCounts, tileMasks);
+    patch_setup<1, false>(B, tris, tileCounts, tileMasks);
 }
 
 __global__ void __launch_bounds__(128) center_setup_kernel(BatchTables B,
@@ -1041,7 +1061,7 @@ __global__ void __launch_bounds__(128) center_setup_kernel(BatchTables B,
                                                            uint32_t* __restrict__ tileCounts,
                                                            uint8_t* __restrict__ tileMasks)
 {
-    patch_setup<3>(B, tris, tileCounts, tileMasks);
+    patch_setup<3, true>(B, tris, tileCounts, tileMasks);
 }
 
 // Interior triangulation (DrawType::interiorTriangulation): one thread per
@@ -1692,12 +1712,17 @@ __device__ float eval_feathered_fill(float cx, float cy, float cotTheta, float y
     return __fmul_rn(featherCoverage, signf(cx));
 }
 
-// A feathered fill's fragment: its third and fourth coverage components from
-// the slot's planes, then the feather.
-__device__ __noinline__ float feathered_fill_fragment(const float4* __restrict__ planes,
-                                                      uint32_t slot, float fx, float fy, float covx,
-                                                      float covy)
+// A feathered fragment: a stroke's (covy >= 0), or a fill's, whose third and
+// fourth coverage components come from the slot's planes. One out-of-line
+// call site keeps the raster loop's register allocation as it is without
+// feathers.
+__device__ __noinline__ float feathered_fragment(const float4* __restrict__ planes, uint32_t slot,
+                                                 float fx, float fy, float covx, float covy)
 {
+    if (covy >= 0.f)
+        return eval_feathered_stroke(covx, covy);
+    if (!planes)
+        return covx;
     const float4 f0 = planes[2 * (size_t)slot], f1 = planes[2 * (size_t)slot + 1];
     const float dx = fx - f1.z, dy = fy - f1.w;
     const float covz = f0.x + f0.y * dx + f0.z * dy;
@@ -1720,7 +1745,7 @@ template <int TL> struct RasterTile
     using Mask = typename std::conditional<(kBlocks <= 8), uint8_t, uint32_t>::type;
 };
 
-template <int TL>
+template <int TL, bool kFeather>
 __device__ __forceinline__ void raster_tile(const BatchTables& B,
                                             const TriRecord* __restrict__ tris,
                                             const uint32_t* __restrict__ sortedSlots,
@@ -1872,25 +1897,17 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                         s.pendPaintY = v4.y;
                     }
                 }
-                if (covy >= 0.f) // stroke (find_stroke_coverage, draw_path.vert:501-509)
-                {
-                    const float frag =
-                        covx < kFeatherCoverageThreshold && ((T.v4.z >> 16) & SF_FEATHER)
-                            ? eval_feathered_stroke(covx, covy)
-                            : fminf(covx, covy);
-                    count = fmaxf(frag, count);
-                }
-                else if (covy < kFeatherCoverageThreshold && ((T.v4.z >> 16) & SF_FEATHER) &&
-                         B.featherPlanes)
-                {
-                    // feathered fill (find_fill_coverage, draw_path.vert:511-519)
-                    count = count + feathered_fill_fragment(B.featherPlanes, T.v4.w, fx, fy,
-                                                            covx, covy);
-                }
-                else
-                {
-                    count = count + covx; // fill
-                }
+                // Strokes (covy >= 0) keep the maximum coverage, fills add
+                // (find_stroke_coverage / find_fill_coverage,
+                // draw_path.vert:501-519); feathered ones are marked by a
+                // coverage below the feather threshold.
+                const bool stroke = covy >= 0.f;
+                float frag = stroke ? fminf(covx, covy) : covx;
+                // (s.pendMeta is this triangle's pathAndFeatures here.)
+                if (kFeather && (stroke ? covx : covy) < kFeatherCoverageThreshold &&
+                    ((s.pendMeta >> 16) & SF_FEATHER))
+                    frag = feathered_fragment(B.featherPlanes, T.v4.w, fx, fy, covx, covy);
+                count = stroke ? fmaxf(frag, count) : count + frag;
                 s.count = h2f(f2h(count)); // the plane stores fp16
             }
         }
@@ -1902,39 +1919,49 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
         fb[(size_t)py * P.width + px] = s.color;
 }
 
-__global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) raster_tile_kernel(
-    BatchTables B,
-    const TriRecord* __restrict__ tris,
-    const uint32_t* __restrict__ sortedSlots,
-    const uint2* __restrict__ ranges)
-{
-    __shared__ TileTri sTris[256];
-    __shared__ uint8_t sMask[256];
-    raster_tile<4>(B, tris, sortedSlots, ranges, sTris, sMask);
-}
+// The raster kernels, each without and with the feather paths (the host
+// launches the feather variant only for batches with ENABLE_FEATHER draws).
+#define RIVE_RASTER_KERNELS(NAME, FEATHER)                                                        \
+    __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) NAME(                           \
+        BatchTables B, const TriRecord* __restrict__ tris,                                        \
+        const uint32_t* __restrict__ sortedSlots, const uint2* __restrict__ ranges)               \
+    {                                                                                             \
+        __shared__ TileTri sTris[256];                                                            \
+        __shared__ uint8_t sMask[256];                                                            \
+        raster_tile<4, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+    }
+RIVE_RASTER_KERNELS(raster_tile_kernel, false)
+RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
+#undef RIVE_RASTER_KERNELS
 
-__global__ void __launch_bounds__(64) raster_tile8_kernel(BatchTables B,
-                                                         const TriRecord* __restrict__ tris,
-                                                         const uint32_t* __restrict__ sortedSlots,
-                                                         const uint2* __restrict__ ranges)
-{
-    __shared__ TileTri sTris[64];
-    __shared__ uint8_t sMask[64];
-    raster_tile<3>(B, tris, sortedSlots, ranges, sTris, sMask);
-}
+#define RIVE_RASTER8_KERNELS(NAME, FEATHER)                                                       \
+    __global__ void __launch_bounds__(64) NAME(BatchTables B, const TriRecord* __restrict__ tris, \
+                                               const uint32_t* __restrict__ sortedSlots,         \
+                                               const uint2* __restrict__ ranges)                 \
+    {                                                                                             \
+        __shared__ TileTri sTris[64];                                                             \
+        __shared__ uint8_t sMask[64];                                                             \
+        raster_tile<3, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+    }
+RIVE_RASTER8_KERNELS(raster_tile8_kernel, false)
+RIVE_RASTER8_KERNELS(raster_tile8_feather_kernel, true)
+#undef RIVE_RASTER8_KERNELS
 
 // 32x32 tiles: 1,024 threads, the staged records in dynamic shared memory
 // (kRaster32SmemBytes).
-__global__ void __launch_bounds__(1024, 1) raster_tile32_kernel(BatchTables B,
-                                                               const TriRecord* __restrict__ tris,
-                                                               const uint32_t* __restrict__ sortedSlots,
-                                                               const uint2* __restrict__ ranges)
-{
-    extern __shared__ uint4 dyn[];
-    TileTri* sTris = reinterpret_cast<TileTri*>(dyn);
-    uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);
-    raster_tile<5>(B, tris, sortedSlots, ranges, sTris, sMask);
-}
+#define RIVE_RASTER32_KERNELS(NAME, FEATHER)                                                      \
+    __global__ void __launch_bounds__(1024, 1) NAME(                                              \
+        BatchTables B, const TriRecord* __restrict__ tris,                                        \
+        const uint32_t* __restrict__ sortedSlots, const uint2* __restrict__ ranges)               \
+    {                                                                                             \
+        extern __shared__ uint4 dyn[];                                                            \
+        TileTri* sTris = reinterpret_cast<TileTri*>(dyn);                                         \
+        uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);                              \
+        raster_tile<5, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+    }
+RIVE_RASTER32_KERNELS(raster_tile32_kernel, false)
+RIVE_RASTER32_KERNELS(raster_tile32_feather_kernel, true)
+#undef RIVE_RASTER32_KERNELS
 } // namespace rivecuda
 
 namespace rivecuda
