@@ -356,6 +356,8 @@ def run_ours(args, cap, wname, rank, world):
         line["serving"] = run_serving(args, dev, raster)
     if args.serve_rec_sessions > 0 and world == 1:
         line["serving_recorded"] = run_serving_recorded(args, dev, raster)
+    if args.feather_steps > 0 and world == 1:
+        line["feathered"] = run_feathered(args, dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -364,6 +366,60 @@ def run_ours(args, cap, wname, rank, world):
                                 "sample": f"1 whole frame of {wname} through the oracle"}
     if rank == 0:
         print(json.dumps(line))
+
+
+FEATHERED_CAPTURE = ("silver_police_files_f60",
+                     "recorded frame 60 of game_menu_ad_police_files (1080x1080) with feathered "
+                     "fills and strokes below the atlas threshold, planned by the reference front end")
+
+
+def run_feathered(args, dev):
+    """Frames/s of a recorded frame with feathered draws (the feather kernel
+    variants and the center-AA fans), records resident in HBM, timed with CUDA
+    events on the flush stream."""
+    import numpy as np
+    import torch
+    from rive_runtime_gb300 import capture, rive_cuda
+    from rive_runtime_gb300.capture import BUFFER_NAMES
+    name, what = FEATHERED_CAPTURE
+    with open(os.path.join(REPO, "tests", "golden", name + ".cap"), "rb") as f:
+        cap = capture.parse(f.read())
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = rive_cuda.Context(dev)
+    dbufs = rive_cuda.DeviceBuffers()
+    keep = []
+    for n in BUFFER_NAMES:
+        b = cap.buffers.get(n, b"")
+        t = torch.from_numpy(np.frombuffer(b, np.uint8).copy()).cuda() if b else None
+        keep.append(t)
+        setattr(dbufs, n, t.data_ptr() if t is not None else None)
+    target = torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8, device="cuda")
+
+    def frame():
+        for fl in cap.flushes:
+            ctx.flush_device(fl, dbufs, target.data_ptr(), stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        frame()
+    ctx.sync(stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.feather_steps):
+        frame()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    ctx.sync(stream.cuda_stream)
+    ctx.close()
+    center = sum(int((fl.batches[:, 0] == 1).sum()) for fl in cap.flushes)
+    return {"workload": name, "content": what, "width": cap.width, "height": cap.height,
+            "center_aa_batches": center, "steps": args.feather_steps,
+            "frames_per_s": args.feather_steps / (ms / 1e3),
+            "ms_per_frame": ms / args.feather_steps,
+            "raster": "16x16 tiles, full occupancy (not autotuned)"}
 
 
 def run_serving(args, dev, raster=None):
@@ -556,6 +612,8 @@ def main():
                     help="sessions of the recorded-animation serving run (0 = skip)")
     ap.add_argument("--serve-rec-frames", type=int, default=120)
     ap.add_argument("--serve-rec-fps", type=float, default=30.0)
+    ap.add_argument("--feather-steps", type=int, default=200,
+                    help="frames of the recorded feathered-frame measurement (0 skips it)")
     ap.add_argument("--raster-config", default="auto",
                     help='"auto" (autotuned on the workload) or "tile,ctas_per_sm", e.g. "16,0"')
     args = ap.parse_args()
