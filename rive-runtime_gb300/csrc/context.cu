@@ -29,6 +29,7 @@ namespace rivecuda
 {
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
+__global__ void tessellate_feather_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B,
                                    TriRecord* tris,
                                    uint32_t* tileCounts,
@@ -685,7 +686,8 @@ int enqueue_front(rive_cuda_context* ctx,
     if (L.tessSpans)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_TESSELLATE, stream);
-        tessellate_kernel<<<(L.tessSpans * 32u + 255u) / 256u, 256, 0, stream>>>(B);
+        (L.feather ? tessellate_feather_kernel : tessellate_kernel)<<<(L.tessSpans * 32u + 255u) / 256u,
+                                                                     256, 0, stream>>>(B);
         stage_end(ctx, stream);
     }
     if (L.slots)
@@ -1503,7 +1505,7 @@ int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)
         CK(cudaMemsetAsync(ctx->dError, 0, 4, s));
         CK(cudaStreamSynchronize(s));
         return set_error(ctx, RIVE_CUDA_ERR_DEVICE_STATUS,
-                         "device status 0x%x (1 tess index, 2 contour, 4 path, 8 feather, "
+                         "device status 0x%x (1 tess index, 2 contour, 4 path, "
                          "16 coordinate range, 32 bin overflow)",
                          err);
     }

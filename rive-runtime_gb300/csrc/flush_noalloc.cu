@@ -22,6 +22,7 @@ namespace rivecuda
 {
 __global__ void color_ramp_kernel(BatchTables B);
 __global__ void tessellate_kernel(BatchTables B);
+__global__ void tessellate_feather_kernel(BatchTables B);
 __global__ void patch_setup_kernel(BatchTables B,
                                    TriRecord* tris,
                                    uint32_t* tileCounts,
@@ -337,7 +338,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (d->grad_span_count)
         color_ramp_kernel<<<d->grad_span_count, 128, 0, stream>>>(B);
     if (d->tess_span_count)
-        tessellate_kernel<<<(d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(B);
+        (feather ? tessellate_feather_kernel : tessellate_kernel)<<<
+            (d->tess_span_count * 32u + 255u) / 256u, 256, 0, stream>>>(B);
 
     TriRecord* tris = (TriRecord*)(pool + kTrisOff);
     uint8_t* masks = (uint8_t*)(pool + kMasksOff);
@@ -401,7 +403,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     CKN(cudaStreamSynchronize(stream));
     if (status)
         return fail(err, err_len, RIVE_CUDA_ERR_DEVICE_STATUS,
-                    "device status 0x%x (1 tess index, 2 contour, 4 path, 8 feather, "
+                    "device status 0x%x (1 tess index, 2 contour, 4 path, "
                     "16 coordinate range, 32 bin overflow)",
                     status);
     return RIVE_CUDA_OK;

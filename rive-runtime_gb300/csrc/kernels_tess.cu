@@ -232,6 +232,8 @@ struct SpanSetup
 };
 
 // Per-span half of tessellate.glsl (the vertex shader, 61-287).
+// kFeather: compiled with feathered-fill softening (ENABLE_FEATHER batches).
+template <bool kFeather>
 __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
 {
     SpanSetup s;
@@ -275,7 +277,7 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
         strokeRadius = __uint_as_float(row1.z);
         featherRadius = __uint_as_float(row1.w);
     }
-    if (featherRadius != 0.f && strokeRadius == 0.f)
+    if (kFeather && featherRadius != 0.f && strokeRadius == 0.f)
     {
         // tessellate.glsl:141-190: a feathered fill's cubic is pulled toward
         // its chord, the more the more it curves within one standard
@@ -343,6 +345,7 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
 }
 
 // Per-texel half of tessellate.glsl (the fragment shader, 294-567).
+template <bool kFeather>
 __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flagsIn)
 {
     float2 p0 = s.p0, p1 = s.p1, p2 = s.p2, p3 = s.p3;
@@ -485,7 +488,7 @@ __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flag
     }
     // GLSL mod(theta, 2pi) = theta - 2pi * floor(theta / 2pi)
     uint32_t z;
-    if ((flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG)
+    if (kFeather && (flags & JOIN_TYPE_MASK) == FEATHER_JOIN_CONTOUR_FLAG)
     {
         // tessellate.glsl:551-559: a feather join leaves its stepping to the
         // draw pass, which needs the join's vertex and segment counts.
@@ -557,7 +560,8 @@ __global__ void __launch_bounds__(128) color_ramp_kernel(BatchTables B)
 
 // One warp per TessVertexSpan of the batch (both its forward and mirrored
 // rectangles).
-__global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
+template <bool kFeather>
+__device__ __forceinline__ void tessellate(const BatchTables& B)
 {
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
@@ -567,7 +571,7 @@ __global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
     const FlushParams& P = B.scenes[scene];
     const uint32_t warp = gw - B.tessSpanBase[scene];
     const uint4* sp = P.tessSpans + 4 * (size_t)(P.firstTessSpan + warp);
-    SpanSetup s = span_setup(P, sp);
+    SpanSetup s = span_setup<kFeather>(P, sp);
     if (!s.valid)
         return;
     uint4 q2 = sp[2], q3 = sp[3];
@@ -589,9 +593,20 @@ __global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
         {
             float vertexIdx = __fsub_rn(s.totalVertexCount,
                                         fabsf(__fsub_rn((float)x1, __fadd_rn((float)px, .5f))));
-            row[px] = tess_vertex(s, vertexIdx, flags);
+            row[px] = tess_vertex<kFeather>(s, vertexIdx, flags);
         }
     }
+}
+
+__global__ void __launch_bounds__(256) tessellate_kernel(BatchTables B)
+{
+    tessellate<false>(B);
+}
+
+// With feathered-fill softening and feather-join texels.
+__global__ void __launch_bounds__(256) tessellate_feather_kernel(BatchTables B)
+{
+    tessellate<true>(B);
 }
 cudaError_t upload_inverse_feather_lut(const float table[kGaussianTableSize])
 {

@@ -112,7 +112,7 @@ constexpr int kRaster32SmemBytes = 1024 * 80 + 1024 * 4; // staged records + blo
 constexpr uint32_t ERR_BAD_TESS_INDEX = 1u << 0;
 constexpr uint32_t ERR_BAD_CONTOUR = 1u << 1;
 constexpr uint32_t ERR_BAD_PATH = 1u << 2;
-constexpr uint32_t ERR_FEATHER = 1u << 3;
+constexpr uint32_t ERR_RESERVED_8 = 1u << 3; // no longer raised (feathers are drawn)
 constexpr uint32_t ERR_COORD_RANGE = 1u << 4;
 constexpr uint32_t ERR_BIN_OVERFLOW = 1u << 5;
 
