@@ -295,7 +295,10 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
  * reserved when the library's module loads, so the call never allocates or
  * frees memory. It is for callers that may not allocate while they render: a
  * render thread with a frame deadline (cudaFree waits for the whole device),
- * or an embedder whose device memory budget is fixed up front.
+ * or an embedder whose device memory budget is fixed up front. It draws
+ * midpoint-fan batches only, feathered strokes included; flushes with other
+ * draw types (interior triangulation, the center-AA fans of feathered fills)
+ * return RIVE_CUDA_ERR_UNSUPPORTED.
  *
  * Limits (larger flushes return RIVE_CUDA_ERR_INVALID_ARGUMENT with a message
  * naming the limit, before anything is launched or written): render target
