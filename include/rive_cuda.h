@@ -377,6 +377,9 @@ int rive_cuda_graph_stats(const rive_cuda_graph* graph, rive_cuda_flush_stats* o
  * feathers) is not built.
  */
 int rive_cuda_feather_table(uint16_t* out);
+/* Its 512-entry fp16 inverse (gpu::g_inverseGaussianIntegralTableF16,
+ * gpu.hpp:2090), which feathered-fill tessellation samples. */
+int rive_cuda_inverse_feather_table(uint16_t* out);
 
 /*
  * Raster configuration of the context's later flushes, batches and graphs

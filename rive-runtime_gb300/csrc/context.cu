@@ -15,6 +15,8 @@
 #include "rive_cuda.h"
 #include "rive_cuda_internal.cuh"
 
+#include <cuda_fp16.h>
+
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -1537,6 +1539,17 @@ int rive_cuda_feather_table(uint16_t* out)
     if (!out)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
     feather_table_f16(out);
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_inverse_feather_table(uint16_t* out)
+{
+    if (!out)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    float table[kGaussianTableSize];
+    build_inverse_feather_table(table);
+    for (int i = 0; i < kGaussianTableSize; ++i)
+        out[i] = __half_as_ushort(__float2half_rn(table[i]));
     return RIVE_CUDA_OK;
 }
 

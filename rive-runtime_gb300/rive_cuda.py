@@ -116,6 +116,7 @@ def load():
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
         "rive_cuda_feather_table": (i32, [vp]),
+        "rive_cuda_inverse_feather_table": (i32, [vp]),
         "rive_cuda_get_raster_config": (i32, [vp, ctypes.POINTER(ctypes.c_int),
                                               ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_profile_collect": (i32, [vp, ctypes.POINTER(ctypes.c_double),
@@ -148,6 +149,15 @@ def feather_table():
     rc = load().rive_cuda_feather_table(out.ctypes.data_as(ctypes.c_void_p))
     if rc != OK:
         raise RiveCudaError(f"feather_table: status {rc}")
+    return out
+
+
+def inverse_feather_table():
+    """The fp16 bits of the library's inverse feather table (512 entries)."""
+    out = np.zeros(512, np.uint16)
+    rc = load().rive_cuda_inverse_feather_table(out.ctypes.data_as(ctypes.c_void_p))
+    if rc != OK:
+        raise RiveCudaError(f"inverse_feather_table: status {rc}")
     return out
 
 

@@ -45,3 +45,11 @@ def test_feather_table_is_the_oracles():
     from rive_runtime_gb300 import rive_cuda
     import oracle
     assert (rive_cuda.feather_table() == oracle.feather_table()).all()
+
+
+def test_inverse_feather_table_is_the_oracles():
+    """The library's inverse feather table (host code, no GPU needed) equals the
+    oracle's, which equals the reference's shipped table."""
+    from rive_runtime_gb300 import rive_cuda
+    import oracle
+    assert (rive_cuda.inverse_feather_table() == oracle.inverse_feather_table()).all()
