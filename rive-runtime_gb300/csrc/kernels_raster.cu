@@ -1650,10 +1650,9 @@ struct __align__(16) TileTri
 };
 static_assert(sizeof(TileTri) == 80, "TileTri layout");
 
-// Resident CTAs per SM the register allocation is bounded for (16x16 tiles).
 // The 512-entry feather table (the integral of the normal distribution over
 // -3..+3 standard deviations, fp16 values widened to float), written by the
-// host once per device (feather_table.cpp) before any flush.
+// host once per device (ensure_feather_lut, end of this file) before any flush.
 __device__ float g_featherLUT[kGaussianTableSize];
 
 // FEATHER(x) (common.glsl:53-60): the table sampled at normalised x with a
@@ -1730,6 +1729,7 @@ __device__ __noinline__ float feathered_fragment(const float4* __restrict__ plan
     return eval_feathered_fill(covx, covy, covz, covw);
 }
 
+// Resident CTAs per SM the register allocation is bounded for (16x16 tiles).
 #ifndef RIVE_RASTER_MIN_BLOCKS
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
