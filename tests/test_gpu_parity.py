@@ -83,12 +83,13 @@ def test_gradient_ramps_match_oracle(ctx, name):
 
 
 @pytest.mark.gpu
-def test_flush_rejects_unsupported_draw_type_and_stays_usable(ctx):
+@pytest.mark.parametrize("draw_type", [4, 5, 6])  # featherAtlasBlit, imageRect, imageMesh
+def test_flush_rejects_unsupported_draw_type_and_stays_usable(ctx, draw_type):
     from rive_runtime_gb300 import rive_cuda
     cap, _ = load_golden("plain_small_s1")
     f = cap.flushes[0]
     bad = type(f)(dict(f.desc), f.batches.copy())
-    bad.batches[:, 0] = 5  # gpu::DrawType::imageRect
+    bad.batches[:, 0] = draw_type
     t = ctx.render_target(cap.width, cap.height)
     ctx.upload_frame(cap)
     with pytest.raises(rive_cuda.RiveCudaError, match="draw type"):
