@@ -53,6 +53,14 @@ SCENES = {
     "tri_full_s23": lambda: _triangulated(scene.full_feature(
         seed=23, width=512, height=512, n_paths=24, max_cubics=10, p_fill=0.8, p_clip=0.3,
         p_blend=0.3, scale_range=(6.0, 9.0))),
+    # More complex gradients than the gradient texture has rows (2,048): the
+    # front end splits the frame into two logical flushes
+    # (LogicalFlush::pushDraws, render_context.cpp:509-586), and the second
+    # loads the target the first wrote (render_context.cpp:1218-1222).
+    "multiflush_s41": lambda: scene.full_feature(
+        seed=41, width=256, height=256, n_paths=2450, max_contours=1, min_cubics=2,
+        max_cubics=2, p_fill=0.85, p_gradient=1.0, p_clip=0.05, p_blend=0.1,
+        scale_range=(0.15, 0.5)),
 }
 
 

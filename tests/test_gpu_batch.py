@@ -1,26 +1,15 @@
 """The batched form (rive_cuda_flush_batch): independent flushes of different
 canvases and path counts rendered by one sequence of launches must give every
-target exactly the image the one-flush-at-a-time path gives it."""
+target exactly the image the one-flush-at-a-time path gives it. Frames of
+several logical flushes run as waves: wave i batches logical flush i of every
+frame, so a frame's later flushes load what its earlier ones wrote."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, load_package
+from conftest import (device_buffers, flush_waves, golden_names, load_golden, load_package,
+                      render_one_by_one)
 
 load_package()
-
-
-def _device_buffers(cap):
-    import torch
-    from rive_runtime_gb300 import rive_cuda
-    from rive_runtime_gb300.capture import BUFFER_NAMES
-    bufs = rive_cuda.DeviceBuffers()
-    keep = []
-    for name in BUFFER_NAMES:
-        b = cap.buffers.get(name, b"")
-        t = torch.from_numpy(np.frombuffer(b, np.uint8).copy()).cuda() if b else None
-        keep.append(t)
-        setattr(bufs, name, t.data_ptr() if t is not None else None)
-    return bufs, keep
 
 
 @pytest.fixture(scope="module")
@@ -31,37 +20,27 @@ def ctx():
     c.close()
 
 
-def _one_by_one(ctx, caps, bufs, stream):
-    import torch
-    out = []
-    for cap, b in zip(caps, bufs):
-        t = torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8, device="cuda")
-        for f in cap.flushes:
-            ctx.flush_device(f, b, t.data_ptr(), stream)
-        out.append(t)
-    ctx.sync(stream)
-    torch.cuda.synchronize()
-    return [t.cpu().numpy() for t in out]
-
-
 @pytest.mark.gpu
 def test_batch_of_all_goldens_matches_single_flushes(ctx):
     import torch
-    caps = [load_golden(n)[0] for n in golden_names()]
-    assert all(len(c.flushes) == 1 for c in caps)
-    pairs = [_device_buffers(c) for c in caps]
+    names = golden_names()
+    caps = [load_golden(n)[0] for n in names]
+    assert any(len(c.flushes) > 1 for c in caps), "a multi-flush golden is expected"
+    pairs = [device_buffers(c) for c in caps]
     bufs = [p[0] for p in pairs]
     stream = torch.cuda.current_stream().cuda_stream
-    want = _one_by_one(ctx, caps, bufs, stream)
+    want = render_one_by_one(ctx, caps, bufs, stream)
     targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda") for c in caps]
-    ctx.flush_batch([(c.flushes[0], b, t.data_ptr()) for c, b, t in zip(caps, bufs, targets)],
-                    stream)
+    waves = flush_waves(caps, bufs, targets)
+    for wave in waves:
+        ctx.flush_batch(wave, stream)
     ctx.sync(stream)
     torch.cuda.synchronize()
-    for name, t, w in zip(golden_names(), targets, want):
+    for name, t, w in zip(names, targets, want):
         assert np.array_equal(t.cpu().numpy(), w), name
     st = ctx.stats()
-    assert st["tiles"] == sum(((c.width + 15) // 16) * ((c.height + 15) // 16) for c in caps)
+    last = [c for c in caps if len(c.flushes) == len(waves)]
+    assert st["tiles"] == sum(((c.width + 15) // 16) * ((c.height + 15) // 16) for c in last)
 
 
 @pytest.mark.gpu
@@ -71,9 +50,9 @@ def test_batch_repeats_and_reorders_consistently(ctx):
     import torch
     a = load_golden("full_small_s7")[0]
     b = load_golden("strokes_s3")[0]
-    (ba, ka), (bb, kb) = _device_buffers(a), _device_buffers(b)
+    (ba, ka), (bb, kb) = device_buffers(a), device_buffers(b)
     stream = torch.cuda.current_stream().cuda_stream
-    want_a, want_b = _one_by_one(ctx, [a, b], [ba, bb], stream)
+    want_a, want_b = render_one_by_one(ctx, [a, b], [ba, bb], stream)
     ts = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda") for c in (a, b, a)]
     ctx.flush_batch([(a.flushes[0], ba, ts[0].data_ptr()), (b.flushes[0], bb, ts[1].data_ptr()),
                      (a.flushes[0], ba, ts[2].data_ptr())], stream)
@@ -89,7 +68,7 @@ def test_batch_refuses_a_shared_target(ctx):
     import torch
     from rive_runtime_gb300 import rive_cuda
     a = load_golden("strokes_s3")[0]
-    ba, ka = _device_buffers(a)
+    ba, ka = device_buffers(a)
     t = torch.zeros((a.height, a.width, 4), dtype=torch.uint8, device="cuda")
     with pytest.raises(rive_cuda.RiveCudaError, match="share a render target"):
         ctx.flush_batch([(a.flushes[0], ba, t.data_ptr()), (a.flushes[0], ba, t.data_ptr())])
@@ -98,29 +77,37 @@ def test_batch_refuses_a_shared_target(ctx):
 
 @pytest.mark.gpu
 def test_graph_replays_match_single_flushes(ctx):
-    """A batch captured as a CUDA graph: every launch gives every target the
-    one-by-one image, and the device status stays clean."""
+    """Each wave captured as a CUDA graph: every replay of the waves, in
+    order, gives every target the one-by-one image, and the device status
+    stays clean."""
     import torch
-    caps = [load_golden(n)[0] for n in golden_names()]
-    pairs = [_device_buffers(c) for c in caps]
+    names = golden_names()
+    caps = [load_golden(n)[0] for n in names]
+    pairs = [device_buffers(c) for c in caps]
     bufs = [p[0] for p in pairs]
     stream = torch.cuda.current_stream().cuda_stream
-    want = _one_by_one(ctx, caps, bufs, stream)
+    want = render_one_by_one(ctx, caps, bufs, stream)
     targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda") for c in caps]
-    g = ctx.graph([(c.flushes[0], b, t.data_ptr()) for c, b, t in zip(caps, bufs, targets)])
+    graphs = [ctx.graph(wave) for wave in flush_waves(caps, bufs, targets)]
+    # One stream orders the waves (a NULL stream would run each graph on its
+    # own stream).
+    order = torch.cuda.Stream().cuda_stream
     try:
         for _ in range(2):
             for t in targets:
                 t.zero_()
             torch.cuda.synchronize()
-            g.launch()
-            g.check()
+            for g in graphs:
+                g.launch(order)
+            for g in graphs:
+                g.check(order)
             torch.cuda.synchronize()
-            for name, t, w in zip(golden_names(), targets, want):
+            for name, t, w in zip(names, targets, want):
                 assert np.array_equal(t.cpu().numpy(), w), name
-        assert g.stats()["bin_entries"] > 0
+        assert all(g.stats()["bin_entries"] > 0 for g in graphs)
     finally:
-        g.close()
+        for g in graphs:
+            g.close()
 
 
 @pytest.mark.gpu
@@ -130,7 +117,7 @@ def test_graph_reports_a_bin_capacity_overflow(ctx):
     import torch
     from rive_runtime_gb300 import rive_cuda
     a = load_golden("strokes_s3")[0]
-    ba, ka = _device_buffers(a)
+    ba, ka = device_buffers(a)
     t = torch.zeros((a.height, a.width, 4), dtype=torch.uint8, device="cuda")
     g = ctx.graph([(a.flushes[0], ba, t.data_ptr())], bin_capacity=64)
     try:
@@ -141,5 +128,5 @@ def test_graph_reports_a_bin_capacity_overflow(ctx):
     finally:
         g.close()
     stream = torch.cuda.current_stream().cuda_stream
-    (want,) = _one_by_one(ctx, [a], [ba], stream)
+    (want,) = render_one_by_one(ctx, [a], [ba], stream)
     assert want.any()

@@ -5,7 +5,7 @@ autotuner must leave one of its candidates set."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, load_package
+from conftest import device_buffers, flush_waves, golden_names, load_golden, load_package
 import oracle
 
 load_package()
@@ -59,42 +59,30 @@ def test_rejects_unknown_tile_size(ctx):
     assert ctx.raster_config() == (16, 0)
 
 
-def _device_buffers(cap):
-    import torch
-    from rive_runtime_gb300 import rive_cuda
-    from rive_runtime_gb300.capture import BUFFER_NAMES
-    bufs = rive_cuda.DeviceBuffers()
-    keep = []
-    for name in BUFFER_NAMES:
-        b = cap.buffers.get(name, b"")
-        t = torch.from_numpy(np.frombuffer(b, np.uint8).copy()).cuda() if b else None
-        keep.append(t)
-        setattr(bufs, name, t.data_ptr() if t is not None else None)
-    return bufs, keep
-
-
 @pytest.mark.gpu
 @pytest.mark.parametrize("tile", [8, 32])
 def test_batch_and_graph_at_other_tile_sizes_match_oracle(ctx, oracle_images, tile):
     import torch
     names = golden_names()
     caps = [load_golden(n)[0] for n in names]
-    pairs = [_device_buffers(c) for c in caps]
-    stream = torch.cuda.current_stream().cuda_stream
+    pairs = [device_buffers(c) for c in caps]
+    # A stream of its own (graphs launched on a NULL stream run on theirs).
+    stream = torch.cuda.Stream().cuda_stream
     ctx.set_raster_config(tile, 0)
     try:
         for mode in ("batch", "graph"):
             targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda")
                        for c in caps]
-            items = [(c.flushes[0], p[0], t.data_ptr()) for c, p, t in zip(caps, pairs, targets)]
-            if mode == "batch":
-                ctx.flush_batch(items, stream)
-                ctx.sync(stream)
-            else:
-                g = ctx.graph(items)
-                g.launch(stream)
-                g.check(stream)
-                g.close()
+            torch.cuda.synchronize()
+            for items in flush_waves(caps, [p[0] for p in pairs], targets):
+                if mode == "batch":
+                    ctx.flush_batch(items, stream)
+                    ctx.sync(stream)
+                else:
+                    g = ctx.graph(items)
+                    g.launch(stream)
+                    g.check(stream)
+                    g.close()
             torch.cuda.synchronize()
             for name, t in zip(names, targets):
                 frac, worst = _parity(t.cpu().numpy(), oracle_images[name])
@@ -108,7 +96,7 @@ def test_autotune_leaves_a_candidate_set(ctx):
     import torch
     from rive_runtime_gb300 import autotune
     cap = load_golden("full_small_s7")[0]
-    bufs, keep = _device_buffers(cap)
+    bufs, keep = device_buffers(cap)
     target = torch.zeros((cap.height, cap.width, 4), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
 
