@@ -5,7 +5,10 @@
  * the checker. See passes.h for what each function restates.
  *
  * Arithmetic follows the GLSL statement by statement in fp32 (built with
- * -ffp-contract=off), with libm for acos/sin/cos/sqrt. `half` values of the
+ * -ffp-contract=off). The tessellation pass takes acos, sin, cos and the cube
+ * root from rive_fp32_math.h, the same correctly-rounded-operation
+ * implementations the tessellation kernel compiles, so the two agree bit for
+ * bit; the other passes use libm. `half` values of the
  * shaders are computed in fp32 (desktop mediump) and rounded to fp16 exactly
  * where the shaders pack them into pixel local storage (packHalf2x16).
  *
@@ -19,6 +22,7 @@
  * on provides): for the final images this oracle is "parity unpinned".
  */
 #include "passes.h"
+#include "rive_fp32_math.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -261,7 +265,7 @@ static void find_cubic_tangents(f2 p0, f2 p1, f2 p2, f2 p3, f2* t0, f2* t1)
 static float rive_atan2(f2 v)
 {
     v = normalize2(v);
-    float theta = acosf(clampf(v.x, -1.f, 1.f));
+    float theta = rc_acosf(clampf(v.x, -1.f, 1.f));
     return v.y >= 0.f ? theta : -theta;
 }
 
@@ -455,12 +459,12 @@ static float measure_cubic_local_curvature(f2 p0, f2 p1, f2 p2, f2 p3, float T,
         if (discr < 0.f)
         {
             float sqrtQ = sqrtf(Q);
-            float th = acosf(R / (sqrtQ * sqrtQ * sqrtQ));
-            dt = -2.f * sqrtQ * cosf(th * (1.f / 3.f) + (-PI_F * 2.f / 3.f));
+            float th = rc_acosf(R / (sqrtQ * sqrtQ * sqrtQ));
+            dt = -2.f * sqrtQ * rc_cosf(th * (1.f / 3.f) + (-PI_F * 2.f / 3.f));
         }
         else
         {
-            float Aq = powf(fabsf(R) + sqrtf(discr), 1.f / 3.f);
+            float Aq = rc_cbrtf(fabsf(R) + sqrtf(discr));
             if (R < 0.f)
                 Aq = -Aq;
             dt = Aq != 0.f ? Aq + Q / Aq : 0.f;
@@ -474,7 +478,7 @@ static float measure_cubic_local_curvature(f2 p0, f2 p1, f2 p2, f2 p3, float T,
     find_cubic_tangents(p0, p1, p2, p3, &e0, &e1);
     f2 tan0 = t0 < 1e-3f ? e0 : dir0;
     f2 tan1 = t1 > 1.f - 1e-3f ? e1 : dir1;
-    return acosf(cosine_between_vectors(tan0, tan1));
+    return rc_acosf(cosine_between_vectors(tan0, tan1));
 }
 
 /* Vertex-shader half of pass 2, evaluated once per span rectangle. */
@@ -561,7 +565,7 @@ static int tess_setup(const rive_cuda_flush_desc* d,
         parametricSegmentCount + polarSegmentCount + joinSegmentCount - 1u;
     f2 t0, t1;
     find_cubic_tangents(p0, p1, p2, p3, &t0, &t1);
-    float theta = acosf(cosine_between_vectors(t0, t1));
+    float theta = rc_acosf(cosine_between_vectors(t0, t1));
     float radsPerPolarSegment = theta / (float)polarSegmentCount;
     float turn = det2(sub2(p2, p0), sub2(p3, p1));
     if (turn == 0.f)
@@ -581,7 +585,7 @@ static int tess_setup(const rive_cuda_flush_desc* d,
     if (joinSegmentCount > 1u)
     {
         f2 jt = v->joinTangent;
-        float joinTheta = acosf(cosine_between_vectors(t1, jt));
+        float joinTheta = rc_acosf(cosine_between_vectors(t1, jt));
         float joinSpan = (float)joinSegmentCount;
         if ((contourIDWithFlags &
              (JOIN_TYPE_MASK | EMULATED_STROKE_CAP_CONTOUR_FLAG)) ==
@@ -705,16 +709,18 @@ static void tess_fragment_t(const tess_varyings* v,
                     float maxRotation =
                         testParametricID * negAbsRadsPerSegment + maxRotation0;
                     maxRotation = minf(maxRotation, PI_F);
-                    if (cosRotation >= cosf(maxRotation))
+                    if (cosRotation >= rc_cosf(maxRotation))
                         lastParametricVertexID = testParametricID;
                 }
             }
             float parametricT = lastParametricVertexID / parametricSegmentCount;
             float lastPolarVertexID = mergedVertexID - lastParametricVertexID;
-            float theta0 = acosf(clampf(tan0norm.x, -1.f, 1.f));
+            float theta0 = rc_acosf(clampf(tan0norm.x, -1.f, 1.f));
             theta0 = tan0norm.y >= 0.f ? theta0 : -theta0;
             theta = lastPolarVertexID * radsPerPolarSegment + theta0;
-            f2 norm = {sinf(theta), -cosf(theta)};
+            float sn, cs;
+            rc_sincosf(theta, &sn, &cs);
+            f2 norm = {sn, -cs};
             float a = dot2(norm, A), b_over_2 = dot2(norm, B), c = dot2(norm, C);
             float discr_over_4 = maxf(b_over_2 * b_over_2 - a * c, 0.f);
             float q = sqrtf(discr_over_4);
@@ -2510,4 +2516,22 @@ int oracle_flush(const rive_cuda_flush_desc* d,
     free(grad);
     free(tess);
     return rc;
+}
+
+/* ---- the shared fp32 elementary functions, for their accuracy test -------- */
+/* fn: 0 sin, 1 cos, 2 acos, 3 cube root. */
+int oracle_math_eval(int fn, const float* x, float* out, size_t n)
+{
+    for (size_t i = 0; i < n; ++i)
+    {
+        switch (fn)
+        {
+            case 0: out[i] = rc_sinf(x[i]); break;
+            case 1: out[i] = rc_cosf(x[i]); break;
+            case 2: out[i] = rc_acosf(x[i]); break;
+            case 3: out[i] = rc_cbrtf(x[i]); break;
+            default: return -1;
+        }
+    }
+    return 0;
 }

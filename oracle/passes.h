@@ -91,6 +91,11 @@ int oracle_flush(const rive_cuda_flush_desc* d,
 /* Counters of the last oracle_draw (triangles after culling, fragments). */
 void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
 
+/* The fp32 elementary functions the tessellation pass and kernel share
+ * (rive-runtime_gb300/csrc/rive_fp32_math.h) over n inputs: fn 0 sin, 1 cos,
+ * 2 acos, 3 cube root. Returns -1 for an unknown fn. */
+int oracle_math_eval(int fn, const float* x, float* out, size_t n);
+
 /* Half-float helpers exposed for known-answer tests. */
 uint16_t oracle_f32_to_f16(float f);
 /* The 512-entry fp16 feather (Gaussian integral) table. */

@@ -19,7 +19,7 @@ PLANNER_LIB = os.path.join(OUT, "librive_planner.so")
 PLANNER_SOURCES = [os.path.join(CSRC, "planner", "planner.cpp")]
 CXX = os.environ.get("CXX", "g++")
 SOURCES = ["context.cu", "kernels_tess.cu", "kernels_raster.cu", "flush_noalloc.cu"]
-HEADERS = ["rive_cuda_internal.cuh"]
+HEADERS = ["rive_cuda_internal.cuh", "rive_fp32_math.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code unfused (-ffp-contract=off): the feather tables it generates must

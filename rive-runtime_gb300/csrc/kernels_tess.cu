@@ -17,6 +17,7 @@
 // (row-major, 2048 texels per row), so the draw kernels read it with ordinary
 // 128-bit loads.
 #include "rive_cuda_internal.cuh"
+#include "rive_fp32_math.h"
 
 namespace rivecuda
 {
@@ -79,11 +80,13 @@ __device__ __forceinline__ void cubic_tangents(float2 p0,
     t1 = f2sub(p3, f2ne(p3, p2) ? p2 : (f2ne(p2, p1) ? p1 : p0));
 }
 
-// common.glsl atan2(): acos of the normalized x, signed by y.
+// common.glsl atan2(): acos of the normalized x, signed by y. The elementary
+// functions of this file come from rive_fp32_math.h, which the oracle's
+// tessellation shares, so its texels equal the oracle's bit for bit.
 __device__ __forceinline__ float rive_atan2(float2 v)
 {
     v = f2normalize(v);
-    float theta = acosf(fminf(fmaxf(v.x, -1.f), 1.f));
+    float theta = rc_acosf(fminf(fmaxf(v.x, -1.f), 1.f));
     return v.y >= 0.f ? theta : -theta;
 }
 
@@ -195,13 +198,13 @@ __device__ float cubic_local_curvature(float2 p0, float2 p1, float2 p2, float2 p
         if (discr < 0.f)
         {
             const float sqrtQ = __fsqrt_rn(Q);
-            const float th = acosf(__fdiv_rn(R, __fmul_rn(__fmul_rn(sqrtQ, sqrtQ), sqrtQ)));
+            const float th = rc_acosf(__fdiv_rn(R, __fmul_rn(__fmul_rn(sqrtQ, sqrtQ), sqrtQ)));
             dt = __fmul_rn(__fmul_rn(-2.f, sqrtQ),
-                           cosf(__fadd_rn(__fmul_rn(th, 1.f / 3.f), -kPi * 2.f / 3.f)));
+                           rc_cosf(__fadd_rn(__fmul_rn(th, 1.f / 3.f), -kPi * 2.f / 3.f)));
         }
         else
         {
-            float Aq = powf(__fadd_rn(fabsf(R), __fsqrt_rn(discr)), 1.f / 3.f);
+            float Aq = rc_cbrtf(__fadd_rn(fabsf(R), __fsqrt_rn(discr)));
             if (R < 0.f)
                 Aq = -Aq;
             dt = Aq != 0.f ? __fadd_rn(Aq, __fdiv_rn(Q, Aq)) : 0.f;
@@ -215,7 +218,7 @@ __device__ float cubic_local_curvature(float2 p0, float2 p1, float2 p2, float2 p
     cubic_tangents(p0, p1, p2, p3, e0, e1);
     const float2 tan0 = t0 < 1e-3f ? e0 : dir0;
     const float2 tan1 = t1 > 1.f - 1e-3f ? e1 : dir1;
-    return acosf(cos_between(tan0, tan1));
+    return rc_acosf(cos_between(tan0, tan1));
 }
 
 struct SpanSetup
@@ -316,7 +319,7 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
     uint32_t total = parametric + polar + join - 1u;
     float2 t0, t1;
     cubic_tangents(s.p0, s.p1, s.p2, s.p3, t0, t1);
-    float theta = acosf(cos_between(t0, t1));
+    float theta = rc_acosf(cos_between(t0, t1));
     float rpp = __fdiv_rn(theta, (float)polar);
     float turn = f2cross(f2sub(s.p2, s.p0), f2sub(s.p3, s.p1));
     if (turn == 0.f)
@@ -330,7 +333,7 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
     s.radsPerJoinSegment = 0.f;
     if (join > 1u)
     {
-        float joinTheta = acosf(cos_between(t1, s.joinTangent));
+        float joinTheta = rc_acosf(cos_between(t1, s.joinTangent));
         float joinSpan = (float)join;
         if ((flags & (JOIN_TYPE_MASK | EMULATED_STROKE_CAP_CONTOUR_FLAG)) ==
             (ROUND_JOIN_CONTOUR_FLAG | EMULATED_STROKE_CAP_CONTOUR_FLAG))
@@ -441,17 +444,17 @@ __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flag
                     float maxRotation =
                         __fadd_rn(__fmul_rn(testID, -absRads), maxRotation0);
                     maxRotation = fminf(maxRotation, kPi);
-                    if (cosRotation >= cosf(maxRotation))
+                    if (cosRotation >= rc_cosf(maxRotation))
                         lastParametricID = testID;
                 }
             }
             float parametricT = __fdiv_rn(lastParametricID, parametricSegmentCount);
             float lastPolarID = __fsub_rn(mergedVertexID, lastParametricID);
-            float theta0 = acosf(fminf(fmaxf(tan0norm.x, -1.f), 1.f));
+            float theta0 = rc_acosf(fminf(fmaxf(tan0norm.x, -1.f), 1.f));
             theta0 = tan0norm.y >= 0.f ? theta0 : -theta0;
             theta = __fadd_rn(__fmul_rn(lastPolarID, radsPerPolarSegment), theta0);
             float sn, cs;
-            sincosf(theta, &sn, &cs);
+            rc_sincosf(theta, &sn, &cs);
             float2 norm = make_float2(sn, -cs);
             float a = f2dot(norm, A), bHalf = f2dot(norm, B), c = f2dot(norm, C);
             float disc = fmaxf(__fsub_rn(__fmul_rn(bHalf, bHalf), __fmul_rn(a, c)), 0.f);
