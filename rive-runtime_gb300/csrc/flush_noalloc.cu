@@ -107,7 +107,7 @@ static_assert(kPoolBytes == RIVE_CUDA_NOALLOC_POOL_BYTES,
 
 constexpr int kMaxDevices = 64;
 std::mutex gPoolMutex;
-uint8_t* gPool[kMaxDevices] = {};
+bool gTablesUp[kMaxDevices] = {};
 
 int fail(char* err, size_t len, int code, const char* fmt, ...)
 {
@@ -221,18 +221,19 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
     uint8_t* pool = nullptr;
     {
-        // The pool's address is looked up once per device, on the first call.
+        // The pool's address in the current CUDA context, looked up on every
+        // call (cheap), so no address from an earlier context is reused. The
+        // feather tables (copies into file-scope symbols, no allocation) go up
+        // on the first call on each device.
         std::lock_guard<std::mutex> lock(gPoolMutex);
-        if (!gPool[dev])
+        void* p = nullptr;
+        CKN(cudaGetSymbolAddress(&p, gNoAllocScratch));
+        if (!gTablesUp[dev])
         {
-            void* p = nullptr;
-            CKN(cudaGetSymbolAddress(&p, gNoAllocScratch));
-            // The feather table (a copy into a file-scope symbol, no
-            // allocation) also goes up on the first call.
             CKN(ensure_feather_lut(dev));
-            gPool[dev] = (uint8_t*)p;
+            gTablesUp[dev] = true;
         }
-        pool = gPool[dev];
+        pool = (uint8_t*)p;
     }
     cudaStream_t stream = (cudaStream_t)cuda_stream;
     uint32_t* dError = (uint32_t*)(pool + kStatusOff);
