@@ -292,8 +292,12 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
  * No-allocation flush (no counterpart in the reference). Same inputs and
  * result as rive_cuda_flush_device, without a context: every intermediate
  * lives in one fixed device pool of RIVE_CUDA_NOALLOC_POOL_BYTES per device,
- * reserved when the library's module loads, so the call never allocates or
- * frees memory. It is for callers that may not allocate while they render: a
+ * a file-scope __device__ array that exists while the library's module is
+ * loaded, so the call itself never allocates or frees memory. With CUDA's
+ * lazy module loading (the default) the module, and with it the pool, is
+ * loaded on the first call on each device: that first call is where the
+ * pool's memory is reserved, and it can fail if the device has no room for
+ * it. A caller with a fixed budget makes one small call at start-up. It is for callers that may not allocate while they render: a
  * render thread with a frame deadline (cudaFree waits for the whole device),
  * or an embedder whose device memory budget is fixed up front. It draws
  * midpoint-fan batches only, feathered strokes included; flushes with other
@@ -314,8 +318,11 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
  * default stream) twice, to read the bin total and at the end, and
  * returns after the whole flush has run, with the device status checked
  * (RIVE_CUDA_ERR_DEVICE_STATUS as rive_cuda_sync reports it). The first call
- * on each device looks up the pool's address (cudaGetSymbolAddress); make
- * that first call before any stream capture begins. There is one pool per
+ * on each device also uploads the feather tables; make it before any stream
+ * capture begins. Every call looks up the pool's address
+ * (cudaGetSymbolAddress), so a pointer cached from an earlier CUDA context
+ * is never used; the feather tables, though, are uploaded once per device
+ * and process, so a cudaDeviceReset after the first call is not supported. There is one pool per
  * device and process: calls that overlap in time, from two threads or on two
  * streams of one device, race on it and must be serialised by the caller.
  * `err` (may be NULL) receives a message on failure.
@@ -361,6 +368,7 @@ typedef struct rive_cuda_flush_stats
     uint64_t bin_entries;
     uint64_t tiles;
     uint64_t kernel_launches;
+    uint64_t winding_entries; /* bin entries that are interior-tile windings */
 } rive_cuda_flush_stats;
 int rive_cuda_last_flush_stats(const rive_cuda_context* ctx,
                                rive_cuda_flush_stats* out);
@@ -390,6 +398,19 @@ int rive_cuda_inverse_feather_table(uint16_t* out);
  */
 int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_per_sm);
 int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, int* ctas_per_sm);
+
+/*
+ * Interior tiles as winding records (no counterpart in the reference; on by
+ * default). Inside a fill, every midpoint-fan triangle has coverage +1 or -1,
+ * so on a tile that no contour edge, AA ramp or contour midpoint comes within
+ * 2 px of, the path's coverage count is the same integer at every pixel: the
+ * winding number of the fan's boundary. With this on, such tiles get one
+ * winding entry per path instead of every fan triangle that crosses them
+ * (fills that are not nested clip updates, in batches without feathers). The
+ * image is bit-identical either way; off is the plain fan, for comparison.
+ */
+int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled);
+int rive_cuda_get_winding_tiles(const rive_cuda_context* ctx, int* enabled);
 
 /*
  * Per-stage device timing with CUDA events recorded on the flush stream

@@ -72,6 +72,25 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    uint32_t tileCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
+// Interior tiles as winding records (kernels_raster.cu).
+__global__ void path_init_kernel(BatchTables B);
+__global__ void path_bounds_kernel(BatchTables B);
+__global__ void path_alloc_kernel(BatchTables B);
+__global__ void path_winding_kernel(BatchTables B, uint32_t* tileCounts);
+__global__ void fan_filter_kernel(BatchTables B,
+                                  const TriRecord* tris,
+                                  uint32_t* tileCounts,
+                                  uint8_t* tileMasks);
+__global__ void bin_scatter_winding_kernel(BatchTables B,
+                                           const TriRecord* tris,
+                                           const uint32_t* tileCounts,
+                                           const uint8_t* tileMasks,
+                                           const uint32_t* offsets,
+                                           uint32_t slotCount,
+                                           uint32_t capacity,
+                                           uint32_t* error,
+                                           uint32_t* keys,
+                                           uint32_t* vals);
 // The raster kernels without and with the feather paths.
 #define RIVE_DECLARE_RASTER(NAME)                                                                  \
     __global__ void NAME(BatchTables B, const TriRecord* tris, const uint32_t* sortedSlots,        \
@@ -181,6 +200,12 @@ struct rive_cuda_context
     uint32_t* dError = nullptr;
     uint32_t* hError = nullptr;  // pinned
     uint32_t* hPairs = nullptr;  // pinned: scanned pair total
+    // Interior tiles as winding records (rive_cuda_set_winding_tiles): per-path
+    // grids and the cell pool, grown when a flush asked for more cells.
+    bool windingTiles = true;
+    DeviceBuffer pathGrids, gridWinding, gridEdge, gridCounters;
+    uint32_t gridCapacity = 0;
+    uint32_t* hGridCounters = nullptr; // pinned: cells asked, winding entries
     rive_cuda_flush_stats stats = {};
     // Raster configuration (rive_cuda_set_raster_config).
     int tileLog2 = kTileLog2;
@@ -204,11 +229,12 @@ struct rive_cuda_graph
 {
     rive_cuda_context* ctx = nullptr;
     DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
-        scanTemp, sortTemp, ranges, error, featherPlanes;
+        scanTemp, sortTemp, ranges, error, featherPlanes, pathGrids, gridWinding, gridEdge,
+        gridCounters;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    uint32_t* hError = nullptr; // pinned
+    uint32_t* hError = nullptr; // pinned, 2 words
     uint32_t capacity = 0, measured = 0;
     rive_cuda_flush_stats stats = {};
 };
@@ -421,13 +447,17 @@ struct BatchLayout
     uint32_t n = 0;
     int tileLog2 = kTileLog2;
     uint32_t segCount[kSetupLists] = {}, items[kSetupLists] = {};
-    uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0;
+    uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0, paths = 0;
     bool feather = false; // some batch draws with ENABLE_FEATHER
+    // Interior tiles as winding records for this batch: midpoint-fan patches
+    // then take fanStride slots (their 24 triangles and a winding slot).
+    bool winding = false;
+    uint32_t fanStride = kPatchTriangleCount;
     uint64_t tessRows = 0, gradRows = 0;
     std::vector<uint64_t> tessRow0, gradRow0;
     // Table blob offsets.
     size_t oScenes = 0, oGradBase = 0, oTessBase = 0, oTileBase = 0, oSceneTiles = 0,
-           oSegments[kSetupLists] = {}, oSegBase[kSetupLists] = {}, tableBytes = 0;
+           oPathBase = 0, oSegments[kSetupLists] = {}, oSegBase[kSetupLists] = {}, tableBytes = 0;
     size_t tessBytes() const { return (size_t)kTessTextureWidth * tessRows * 16; }
     size_t gradBytes() const { return (size_t)kGradTextureWidth * gradRows * 4; }
     int endBit() const
@@ -450,7 +480,7 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     const uint32_t ts = 1u << L.tileLog2;
     L.tessRow0.resize(n);
     L.gradRow0.resize(n);
-    uint64_t slots = 0, tiles = 0, gradSpans = 0, tessSpans = 0;
+    uint64_t slots = 0, tiles = 0, gradSpans = 0, tessSpans = 0, paths = 0;
     uint64_t segs[kSetupLists] = {}, items[kSetupLists] = {};
     for (uint32_t i = 0; i < n; ++i)
     {
@@ -484,10 +514,20 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
                  ((d->render_target_height + ts - 1) / ts);
         gradSpans += d->grad_span_count;
         tessSpans += d->tess_span_count;
+        paths += d->path_count;
+    }
+    // Winding records for the interior tiles of fills: on unless turned off
+    // or the batch feathers (feathered batches keep their fans).
+    L.winding = ctx->windingTiles && !L.feather && items[0] > 0;
+    if (L.winding)
+    {
+        L.fanStride = kPatchTriangleCount + 1;
+        slots += items[0]; // one winding slot per midpoint-fan patch
     }
     if (slots > 0xffffffffull || tiles >= 0x7fffffffull || gradSpans > 0x7fffffffull ||
-        tessSpans * 32 > 0xffffffffull)
+        tessSpans * 32 > 0xffffffffull || paths > 0x7fffffffull)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "batch too large");
+    L.paths = (uint32_t)paths;
     if (n > 1)
     {
         // The flushes of one batch run concurrently: each needs its own target.
@@ -513,7 +553,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     L.oTessBase = align16(L.oGradBase + 4 * (n + 1));
     L.oTileBase = align16(L.oTessBase + 4 * (n + 1));
     L.oSceneTiles = align16(L.oTileBase + 4 * (n + 1));
-    size_t o = align16(L.oSceneTiles + 8 * n);
+    L.oPathBase = align16(L.oSceneTiles + 8 * n);
+    size_t o = align16(L.oPathBase + 4 * (n + 1));
     for (int l = 0; l < kSetupLists; ++l)
     {
         L.oSegments[l] = o;
@@ -542,6 +583,13 @@ struct Scratch
     uint2* ranges = nullptr;
     uint32_t* error = nullptr;
     float4* featherPlanes = nullptr; // 2 per slot, only with center-AA patches
+    // Winding grids (only when the batch draws interior tiles as winding
+    // records).
+    PathGrid* pathGrids = nullptr;
+    int32_t* gridWinding = nullptr;
+    uint8_t* gridEdge = nullptr;
+    uint32_t* gridCounters = nullptr;
+    uint32_t gridCapacity = 0;
 };
 
 // Fills the table blob (host memory) and returns the device view of it.
@@ -556,6 +604,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
     auto* tessBase = (uint32_t*)(h + L.oTessBase);
     auto* tileBase = (uint32_t*)(h + L.oTileBase);
     auto* sceneTiles = (uint2*)(h + L.oSceneTiles);
+    auto* pathBase = (uint32_t*)(h + L.oPathBase);
     PatchSegment* segs[kSetupLists];
     uint32_t* segBase[kSetupLists];
     for (int l = 0; l < kSetupLists; ++l)
@@ -563,7 +612,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
         segs[l] = (PatchSegment*)(h + L.oSegments[l]);
         segBase[l] = (uint32_t*)(h + L.oSegBase[l]);
     }
-    uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, slotAcc = 0;
+    uint32_t gAcc = 0, tAcc = 0, tileAcc = 0, slotAcc = 0, pathAcc = 0;
     uint32_t segAcc[kSetupLists] = {}, itemAcc[kSetupLists] = {};
     for (uint32_t i = 0; i < L.n; ++i)
     {
@@ -613,6 +662,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
         tileBase[i] = tileAcc;
+        pathBase[i] = pathAcc;
+        pathAcc += d->path_count;
         sceneTiles[i] = make_uint2(tileAcc, P.tilesX);
         gAcc += d->grad_span_count;
         tAcc += d->tess_span_count;
@@ -633,12 +684,13 @@ BatchTables write_tables(rive_cuda_context* ctx,
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += k;
-            slotAcc += k * kTrianglesPerItem[l];
+            slotAcc += k * (l == 0 ? L.fanStride : kTrianglesPerItem[l]);
         }
     }
     gradBase[L.n] = gAcc;
     tessBase[L.n] = tAcc;
     tileBase[L.n] = tileAcc;
+    pathBase[L.n] = pathAcc;
     for (int l = 0; l < kSetupLists; ++l)
         segBase[l][segAcc[l]] = itemAcc[l];
 
@@ -659,6 +711,16 @@ BatchTables write_tables(rive_cuda_context* ctx,
     B.sceneCount = L.n;
     B.tileLog2 = L.tileLog2;
     B.featherPlanes = S.featherPlanes;
+    B.fanSlotStride = L.fanStride;
+    B.pathBase = (const uint32_t*)(dT + L.oPathBase);
+    if (L.winding)
+    {
+        B.grids = S.pathGrids;
+        B.gridWinding = S.gridWinding;
+        B.gridEdge = S.gridEdge;
+        B.gridCapacity = S.gridCapacity;
+        B.gridCounters = S.gridCounters;
+    }
     B.totalGradSpans = gAcc;
     B.totalTessSpans = tAcc;
     B.totalTiles = tileAcc;
@@ -679,6 +741,18 @@ int enqueue_front(rive_cuda_context* ctx,
     // texture is deterministic.
     CK(cudaMemsetAsync(S.grad, 0, L.gradBytes(), stream));
     CK(cudaMemsetAsync(S.ranges, 0, (size_t)L.tiles * sizeof(uint2), stream));
+    if (L.winding)
+    {
+        // Winding grids: every path's box and eligibility, its box from the
+        // spans' control points, then its place in the (zeroed) cell pool.
+        CK(cudaMemsetAsync(S.gridWinding, 0, (size_t)S.gridCapacity * 4, stream));
+        CK(cudaMemsetAsync(S.gridEdge, 0, S.gridCapacity, stream));
+        CK(cudaMemsetAsync(S.gridCounters, 0, 8, stream));
+        path_init_kernel<<<(L.paths + 255) / 256, 256, 0, stream>>>(B);
+        if (L.tessSpans)
+            path_bounds_kernel<<<(L.tessSpans + 255) / 256, 256, 0, stream>>>(B);
+        path_alloc_kernel<<<(L.paths + 255) / 256, 256, 0, stream>>>(B);
+    }
     if (L.gradSpans)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_COLOR_RAMP, stream);
@@ -707,6 +781,14 @@ int enqueue_front(rive_cuda_context* ctx,
         if (L.items[3])
             center_setup_kernel<<<(L.items[3] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
                                                                           S.masks);
+        if (L.winding)
+        {
+            // The deferred fan triangles' winding deltas and edge tiles, then
+            // the windings of every path's grid.
+            fan_filter_kernel<<<(L.items[0] * 8u + 255u) / 256u, 256, 0, stream>>>(B, S.tris,
+                                                                                   S.counts, S.masks);
+            path_winding_kernel<<<(L.paths + 7) / 8, 256, 0, stream>>>(B, S.counts);
+        }
         stage_end(ctx, stream);
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
         size_t tempBytes = S.scanTempBytes;
@@ -813,9 +895,13 @@ int enqueue_back(rive_cuda_context* ctx,
         if (padded)
             bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots, entries,
                                                                       L.tiles, S.keys);
-        bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
-            L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries, S.error,
-            S.keys, S.vals);
+        if (L.winding)
+            bin_scatter_winding_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+                B, S.tris, S.counts, S.masks, S.offsets, L.slots, entries, S.error, S.keys, S.vals);
+        else
+            bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+                L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries,
+                S.error, S.keys, S.vals);
         stage_end(ctx, stream);
         cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
         cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
@@ -880,6 +966,18 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
     if (L.items[3])
         CK(ctx->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
+    if (L.winding)
+    {
+        // The cell pool starts at four cells per tile of the batch and grows
+        // to what the last flush asked for (cells past it leave those paths
+        // on their fans).
+        if (ctx->gridCapacity < L.tiles * 4u)
+            ctx->gridCapacity = std::max(L.tiles * 4u, 1u << 16);
+        CK(ctx->pathGrids.reserve((size_t)std::max(L.paths, 1u) * sizeof(PathGrid)));
+        CK(ctx->gridWinding.reserve((size_t)ctx->gridCapacity * 4));
+        CK(ctx->gridEdge.reserve(ctx->gridCapacity));
+        CK(ctx->gridCounters.reserve(8));
+    }
     const size_t scanBytes = scan_temp_bytes(L.slots);
     CK(ctx->scanTemp.reserve(scanBytes));
     ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
@@ -898,6 +996,14 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.scanTempBytes = scanBytes;
     S.ranges = (uint2*)ctx->ranges.ptr;
     S.error = ctx->dError;
+    if (L.winding)
+    {
+        S.pathGrids = (PathGrid*)ctx->pathGrids.ptr;
+        S.gridWinding = (int32_t*)ctx->gridWinding.ptr;
+        S.gridEdge = (uint8_t*)ctx->gridEdge.ptr;
+        S.gridCounters = (uint32_t*)ctx->gridCounters.ptr;
+        S.gridCapacity = ctx->gridCapacity;
+    }
     BatchTables B = write_tables(ctx, in, L, S, (uint8_t*)ctx->hTables.ptr);
     CK(cudaMemcpyAsync(S.tables, ctx->hTables.ptr, L.tableBytes, cudaMemcpyHostToDevice, stream));
     if (!ctx->tablesCopied)
@@ -907,12 +1013,22 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     rc = enqueue_front(ctx, L, B, S, stream);
     if (rc)
         return rc;
-    uint32_t pairs = 0;
+    uint32_t pairs = 0, windingEntries = 0;
     if (L.slots)
     {
         CK(cudaMemcpyAsync(ctx->hPairs, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost, stream));
+        if (L.winding)
+            CK(cudaMemcpyAsync(ctx->hGridCounters, S.gridCounters, 8, cudaMemcpyDeviceToHost,
+                               stream));
         CK(cudaStreamSynchronize(stream));
         pairs = *ctx->hPairs;
+        if (L.winding)
+        {
+            windingEntries = ctx->hGridCounters[1];
+            const uint32_t asked = ctx->hGridCounters[0];
+            if (asked > ctx->gridCapacity)
+                ctx->gridCapacity = asked + asked / 4; // for the next flush
+        }
     }
     if (pairs)
     {
@@ -935,9 +1051,11 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     ctx->stats.patches = (uint64_t)L.items[0] + L.items[1] + L.items[3];
     ctx->stats.triangles = L.slots;
     ctx->stats.bin_entries = pairs;
+    ctx->stats.winding_entries = windingEntries;
     ctx->stats.tiles = L.tiles;
     ctx->stats.kernel_launches = 1 + (L.gradSpans ? 1 : 0) + (L.tessSpans ? 1 : 0) +
-                                 (L.slots ? 1 : 0) + (pairs ? 3 : 0) + 1;
+                                 (L.slots ? 1 : 0) + (pairs ? 3 : 0) + 1 +
+                                 (L.winding ? 3 + (L.tessSpans ? 1 : 0) + 1 : 0);
     return RIVE_CUDA_OK;
 }
 
@@ -975,6 +1093,8 @@ int rive_cuda_context_create(int device, rive_cuda_context** out_ctx)
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->hPairs, 4);
     if (e == cudaSuccess)
+        e = cudaMallocHost(&ctx->hGridCounters, 8);
+    if (e == cudaSuccess)
         e = ensure_feather_lut(device);
     if (e != cudaSuccess)
     {
@@ -1007,9 +1127,13 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
     for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->tileMasks,
                             &ctx->offsets, &ctx->featherPlanes,
                             &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
-                            &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables})
+                            &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables,
+                            &ctx->pathGrids, &ctx->gridWinding, &ctx->gridEdge,
+                            &ctx->gridCounters})
         b->release();
     ctx->hTables.release();
+    if (ctx->hGridCounters)
+        cudaFreeHost(ctx->hGridCounters);
     if (ctx->tablesCopied)
         cudaEventDestroy(ctx->tablesCopied);
     if (ctx->dError)
@@ -1271,7 +1395,8 @@ void graph_free(rive_cuda_graph* g)
         cudaGraphDestroy(g->graph);
     for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->masks, &g->offsets,
                             &g->keys, &g->vals, &g->keysAlt, &g->valsAlt, &g->scanTemp,
-                            &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes})
+                            &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes,
+                            &g->pathGrids, &g->gridWinding, &g->gridEdge, &g->gridCounters})
         b->release();
     if (g->hError)
         cudaFreeHost(g->hError);
@@ -1291,7 +1416,7 @@ int graph_build(rive_cuda_context* ctx,
     if (rc)
         return rc;
     CK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
-    CK(cudaMallocHost(&g->hError, 4));
+    CK(cudaMallocHost(&g->hError, 8)); // status word; cells the grids asked for
     CK(g->tables.reserve(L.tableBytes));
     CK(g->tess.reserve(L.tessBytes()));
     CK(g->grad.reserve(L.gradBytes()));
@@ -1321,6 +1446,27 @@ int graph_build(rive_cuda_context* ctx,
     S.ranges = (uint2*)g->ranges.ptr;
     S.error = (uint32_t*)g->error.ptr;
     std::vector<uint8_t> h(L.tableBytes);
+    // The graph's winding grids: a cell pool sized like the context's, grown
+    // below if the measuring run asks for more.
+    uint32_t gridCap = L.winding ? std::max({ctx->gridCapacity, L.tiles * 4u, 1u << 16}) : 0u;
+    auto placeGrids = [&]() -> cudaError_t {
+        if (!L.winding)
+            return cudaSuccess;
+        cudaError_t e = g->pathGrids.reserve((size_t)std::max(L.paths, 1u) * sizeof(PathGrid));
+        if (e == cudaSuccess)
+            e = g->gridWinding.reserve((size_t)gridCap * 4);
+        if (e == cudaSuccess)
+            e = g->gridEdge.reserve(gridCap);
+        if (e == cudaSuccess)
+            e = g->gridCounters.reserve(8);
+        S.pathGrids = (PathGrid*)g->pathGrids.ptr;
+        S.gridWinding = (int32_t*)g->gridWinding.ptr;
+        S.gridEdge = (uint8_t*)g->gridEdge.ptr;
+        S.gridCounters = (uint32_t*)g->gridCounters.ptr;
+        S.gridCapacity = gridCap;
+        return e;
+    };
+    CK(placeGrids());
     BatchTables B = write_tables(ctx, in, L, S, h.data());
     CK(cudaMemcpy(S.tables, h.data(), L.tableBytes, cudaMemcpyHostToDevice));
 
@@ -1330,15 +1476,31 @@ int graph_build(rive_cuda_context* ctx,
     {
         // Size the bins from one run of the front half: the exact total plus
         // an eighth of headroom for records that change between launches.
-        rc = enqueue_front(ctx, L, B, S, g->stream);
-        if (rc)
+        // (The grids' cells too, with one more run if the pool was short.)
+        for (int pass = 0; pass < 2; ++pass)
         {
-            ctx->profiling = profiling;
-            return rc;
+            rc = enqueue_front(ctx, L, B, S, g->stream);
+            if (rc)
+            {
+                ctx->profiling = profiling;
+                return rc;
+            }
+            CK(cudaMemcpyAsync(g->hError, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost,
+                               g->stream));
+            g->hError[1] = 0;
+            if (L.winding)
+                CK(cudaMemcpyAsync(g->hError + 1, S.gridCounters, 4, cudaMemcpyDeviceToHost,
+                                   g->stream));
+            CK(cudaStreamSynchronize(g->stream));
+            g->measured = g->hError[0];
+            const uint32_t asked = g->hError[1];
+            if (asked <= gridCap)
+                break;
+            gridCap = asked + asked / 8;
+            CK(placeGrids());
+            B = write_tables(ctx, in, L, S, h.data());
+            CK(cudaMemcpy(S.tables, h.data(), L.tableBytes, cudaMemcpyHostToDevice));
         }
-        CK(cudaMemcpyAsync(g->hError, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost, g->stream));
-        CK(cudaStreamSynchronize(g->stream));
-        g->measured = *g->hError;
         capacity = g->measured + g->measured / 8 + 4096;
     }
     if (!L.slots)
@@ -1574,6 +1736,22 @@ int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, in
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
     *tile_size = 1 << ctx->tileLog2;
     *ctas_per_sm = ctx->rasterCtasPerSm;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled)
+{
+    if (!ctx)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    ctx->windingTiles = enabled != 0;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_get_winding_tiles(const rive_cuda_context* ctx, int* enabled)
+{
+    if (!ctx || !enabled)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *enabled = ctx->windingTiles ? 1 : 0;
     return RIVE_CUDA_OK;
 }
 

@@ -933,6 +933,172 @@ __device__ __forceinline__ void count_tiles(bool has,
     }
 }
 
+// ---- Interior tiles as winding records -----------------------------------
+//
+// Inside a fill, the midpoint fan's triangles overlap a tile many times, yet
+// every one of them has coverage +1 or -1, so at a pixel the path's count is
+// their signed sum: the winding number of the fan's boundary (the contour
+// polygon inset by the AA ramp) around the pixel. On a tile that no contour
+// edge, AA ramp or contour midpoint comes near, that sum is one integer for
+// every pixel, and the raster can add it once instead of walking the fan.
+//
+//  * patch_setup marks the path's edge tiles (within kWindingEdgeMargin of a
+//    contour edge or midpoint) and defers the counting of its fan triangles;
+//  * fan_filter_kernel adds each deferred fan triangle's coverage, row by
+//    row, into the path's grid of winding deltas and counts its tiles,
+//    keeping edge tiles only;
+//  * path_winding_kernel turns each grid row's deltas into windings and
+//    counts the interior tiles whose winding is not zero;
+//  * bin_scatter writes one winding entry per counted interior tile, at the
+//    path's place in primitive order (its first patch's winding slot);
+//  * the raster stages a winding entry as a tile-wide "triangle" of constant
+//    coverage W.
+// Integers are exact in the fp16 coverage plane, and integer sums do not
+// depend on their order, so the image is the one the fan gives.
+
+// clamp(floor(n / d), qmin, qmax) for d > 0 (|n| < 2^50, d < 2^38,
+// |qmin|, |qmax| < 2^13), without a 64-bit division: exact products decide
+// the clamped cases; inside the range a float estimate is off by at most one
+// and is corrected with exact products.
+__device__ __forceinline__ long long floor_div_clamped(long long n, long long d, long long qmin,
+                                                       long long qmax)
+{
+    if (n < qmin * d)
+        return qmin;
+    if (n >= (qmax + 1) * d)
+        return qmax;
+    long long q = (long long)floorf(__fdiv_rn((float)n, (float)d));
+    q = min(max(q, qmin), qmax);
+    while (q > qmin && q * d > n)
+        --q;
+    while (q < qmax && (q + 1) * d <= n)
+        ++q;
+    return q;
+}
+
+// The grid of a path whose interior tiles are winding records, or null.
+__device__ __forceinline__ PathGrid* winding_grid(const BatchTables& B, uint32_t scene,
+                                                  uint32_t pathID)
+{
+    if (!B.grids)
+        return nullptr;
+    PathGrid* g = B.grids + B.pathBase[scene] + pathID;
+    const uint32_t f = g->flags;
+    return (f & (PATH_GRID_ELIGIBLE | PATH_GRID_PLACED | PATH_GRID_UNSAFE)) ==
+                   (PATH_GRID_ELIGIBLE | PATH_GRID_PLACED)
+               ? g
+               : nullptr;
+}
+
+// Whether a deferred fan triangle keeps tile (tx, ty): every tile when its
+// path has no usable grid, else the edge tiles (and, defensively, tiles
+// outside the grid box, which the box's margin keeps from happening).
+__device__ __forceinline__ bool keep_fan_tile(const PathGrid* g, const uint8_t* __restrict__ edge,
+                                              int tx, int ty)
+{
+    if (!g || tx < g->tx0 || tx >= g->tx1 || ty < g->ty0 || ty >= g->ty1)
+        return true;
+    return edge[g->offset + (size_t)(ty - g->ty0) * (g->tx1 - g->tx0) + (tx - g->tx0)] != 0;
+}
+
+// Adds a kept fan triangle's coverage (+-1) into its path's winding deltas.
+// A tile's winding is evaluated at its reference pixel, its first pixel
+// centre (ox + 1/2, oy + 1/2): for each tile row whose reference line the
+// triangle crosses, the columns whose reference pixel lies inside it are
+// found exactly, in 64-bit integers of 1/256 px, from the snapped edges with
+// the raster's tie rule, and the row's deltas get +c at the first and -c
+// past the last.
+__device__ void fan_winding_deltas(const TriRecord& T, int4 bb, int c, const PathGrid& G,
+                                   int32_t* __restrict__ W, int tileLog2)
+{
+    const int ts = 1 << tileLog2;
+    int r0 = (bb.y + ts - 1) >> tileLog2, r1 = (bb.w - 1) >> tileLog2;
+    r0 = max(r0, G.ty0);
+    r1 = min(r1, G.ty1 - 1);
+    if (r0 > r1)
+        return;
+    const float4 e[3] = {T.e0, T.e1, T.e2};
+    long long A[3], Bc[3], AX[3], AY[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+        // Snapped coordinates and their differences are exact multiples of
+        // 1/256 below 2^16 px: exact integers after scaling.
+        AX[k] = (long long)__fmul_rn(e[k].x, 256.f);
+        AY[k] = (long long)__fmul_rn(e[k].y, 256.f);
+        A[k] = (long long)__fmul_rn(e[k].z, 256.f);
+        Bc[k] = (long long)__fmul_rn(e[k].w, 256.f);
+    }
+    const int gw = G.tx1 - G.tx0;
+    for (int r = r0; r <= r1; ++r)
+    {
+        const long long PY = (long long)(r << tileLog2) * 256 + 128;
+        long long lo = G.tx0, hi = G.tx1 - 1;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+        {
+            // E(col) = alpha * col + beta, in (1/256 px)^2.
+            const long long alpha = A[k] * (long long)(ts * 256);
+            const long long beta = A[k] * (128 - AX[k]) + Bc[k] * (PY - AY[k]);
+            if (A[k] > 0) // inside where E >= 0 (ties belong to this edge): col >= -beta/alpha
+                lo = max(lo, -floor_div_clamped(beta, alpha, -hi - 1, -lo));
+            else if (A[k] < 0) // inside where E > 0: col <= floor((beta - 1) / -alpha)
+                hi = min(hi, floor_div_clamped(beta - 1, -alpha, lo - 1, hi));
+            else if (!(beta > 0 || (beta == 0 && Bc[k] > 0)))
+                hi = lo - 1;
+            if (lo > hi)
+                break;
+        }
+        if (lo > hi)
+            continue;
+        int32_t* row = W + G.offset + (size_t)(r - G.ty0) * gw;
+        atomicAdd(row + (lo - G.tx0), c);
+        if (hi + 1 < G.tx1)
+            atomicAdd(row + (hi + 1 - G.tx0), -c);
+    }
+}
+
+// Marks the grid's tiles whose pixel centres, widened by kWindingEdgeMargin
+// px, meet the segment a-b (a point when a == b). Finite inputs.
+__device__ void mark_edge_tiles(float2 a, float2 b, const PathGrid& G, uint8_t* __restrict__ edge,
+                                int tileLog2)
+{
+    const float ts = (float)(1 << tileLog2);
+    const float m = kWindingEdgeMargin - .5f; // tile t's widened span: [t ts - m, (t+1) ts + m]
+    const float y0 = fminf(a.y, b.y), y1 = fmaxf(a.y, b.y);
+    const int gw = G.tx1 - G.tx0;
+    int t0 = (int)ceilf((y0 - m) / ts - 1.f), t1 = (int)floorf((y1 + m) / ts);
+    t0 = max(t0, G.ty0);
+    t1 = min(t1, G.ty1 - 1);
+    const float dy = b.y - a.y, dx = b.x - a.x;
+    for (int ty = t0; ty <= t1; ++ty)
+    {
+        // The part of the segment inside the row's widened band.
+        const float ylo = fmaxf((float)ty * ts - m, y0), yhi = fminf((float)(ty + 1) * ts + m, y1);
+        float xa, xb;
+        if (fabsf(dy) < 1e-6f)
+        {
+            xa = fminf(a.x, b.x);
+            xb = fmaxf(a.x, b.x);
+        }
+        else
+        {
+            const float u0 = fminf(fmaxf((ylo - a.y) / dy, 0.f), 1.f);
+            const float u1 = fminf(fmaxf((yhi - a.y) / dy, 0.f), 1.f);
+            const float xu0 = a.x + dx * u0, xu1 = a.x + dx * u1;
+            // A little slack for the rounding of the clip.
+            xa = fminf(xu0, xu1) - 1e-2f;
+            xb = fmaxf(xu0, xu1) + 1e-2f;
+        }
+        int c0 = (int)ceilf((xa - m) / ts - 1.f), c1 = (int)floorf((xb + m) / ts);
+        c0 = max(c0, G.tx0);
+        c1 = min(c1, G.tx1 - 1);
+        uint8_t* row = edge + G.offset + (size_t)(ty - G.ty0) * gw;
+        for (int tx = c0; tx <= c1; ++tx)
+            row[tx - G.tx0] = 1;
+    }
+}
+
 // Patch set-up, one warp per patch instance of the batch: shade the patch's
 // vertices, assemble and set up its triangles, then count the tiles each one
 // touches. kList selects the patch: 0 the midpoint fan, 1 the outer-curve
@@ -990,11 +1156,83 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             sZW[w][v] = zw;
     }
     __syncwarp();
-    const uint32_t slot0 = S.slotBase + local * kTris;
+    // With interior tiles as winding records, each midpoint-fan patch also
+    // owns a winding slot after its triangles.
+    const uint32_t stride = (kList == 0 && B.fanSlotStride) ? B.fanSlotStride : (uint32_t)kTris;
+    const uint32_t slot0 = S.slotBase + local * stride;
+    PathGrid* wg = nullptr; // the path's winding grid, when this patch feeds it
+    if (kList == 0 && !kFeather && B.grids)
+    {
+        if (lane == 0)
+        {
+            tileCounts[slot0 + kTris] = 0; // path_winding_kernel fills the path's anchor
+            tileMasks[slot0 + kTris] = 0;
+        }
+        if (sok[w])
+        {
+            const uint32_t pid = sv[w][kVerts - 1].pathID;
+            PathGrid* g = pid < P.pathCount ? winding_grid(B, S.scene, pid) : nullptr;
+            if (g)
+            {
+                // A discarded or non-finite vertex would leave a hole in the
+                // fan: such a path keeps its fan triangles everywhere.
+                bool bad = false;
+                for (int v = lane; v < kVerts; v += 32)
+                {
+                    const VertexOut& o = sv[w][v];
+                    bad = bad || o.discard ||
+                          !(fabsf(o.pos.x) < 32768.f && fabsf(o.pos.y) < 32768.f);
+                }
+                if (__any_sync(0xffffffffu, bad))
+                {
+                    if (lane == 0)
+                        atomicOr(&g->flags, PATH_GRID_UNSAFE);
+                }
+                else
+                {
+                    wg = g;
+                }
+            }
+        }
+        if (wg)
+        {
+            const PathGrid G = *wg;
+            // Edge tiles: near the inset contour's edges (fan vertices 32..40,
+            // shared by the AA ramps) or its midpoint (vertex 41).
+            if (lane < kPatchSegmentSpan)
+                mark_edge_tiles(sv[w][32 + lane].pos, sv[w][33 + lane].pos, G, B.gridEdge,
+                                B.tileLog2);
+            else if (lane == kPatchSegmentSpan)
+                mark_edge_tiles(sv[w][41].pos, sv[w][41].pos, G, B.gridEdge, B.tileLog2);
+            if (lane == 0)
+            {
+                // The winding slot's record: the path's paint, coverage key
+                // and grid, for the raster to stage a winding entry from.
+                const uint32_t pid = sv[w][kVerts - 1].pathID;
+                atomicMin(&wg->anchor, slot0 + kTris);
+                const uint2 paint = P.paints[P.firstPaint + pid];
+                uint32_t key = pid == 0 ? 0u
+                                        : ((pid + MAX_DENORM_F16) * P.pathIDGranularity) & 0xffffu;
+                if (paint.x & PAINT_FLAG_EVEN_ODD_FILL)
+                    key ^= 0x8000u;
+                TriRecord R;
+                R.e0 = make_float4(__uint_as_float(G.offset), __int_as_float(G.tx0),
+                                   __int_as_float(G.ty0), __int_as_float(G.tx1 - G.tx0));
+                R.e1 = make_float4(__int_as_float(G.ty1 - G.ty0), 0.f, 0.f, 0.f);
+                R.e2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                R.cov0 = make_float4(0.f, 0.f, 0.f, 0.f);
+                R.cov1 = make_float4(0.f, 0.f, __uint_as_float(paint.x), __uint_as_float(paint.y));
+                R.meta = make_uint4((pid & 0xffffu) | ((S.features | FEATURE_WINDING_SLOT) << 16), 0u,
+                                    0u, key | (S.scene << 16));
+                tris[slot0 + kTris] = R;
+            }
+        }
+    }
     for (int pass = 0; pass < kTriPasses; ++pass)
     {
         const int t = pass * 32 + lane;
         const bool has = t < kTris;
+        bool deferred = false;
         int4 bb = make_int4(0, 0, 0, 0);
         float4 e[3];
         if (has)
@@ -1006,8 +1244,12 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
                 center_triangle(t, ia, ib, ic);
             else
                 patch_triangle(t, ia, ib, ic);
+            // Fan triangles (16..23) of a path with a winding grid: their
+            // tiles are counted once the grid knows its edge tiles.
+            const bool fan = kList == 0 && wg && t >= 16;
             TriRecord T;
-            if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic], S.features, S.scene,
+            if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic],
+                                         S.features | (fan ? FEATURE_FAN_DEFERRED : 0u), S.scene,
                                          T, bb, planes ? planes + 2 * (size_t)(slot0 + t) : nullptr,
                                          planes ? sZW[w][kFeather ? ia : 0] : float2{},
                                          planes ? sZW[w][kFeather ? ib : 0] : float2{},
@@ -1020,13 +1262,17 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
                 sEdges[w][t][0] = T.e0;
                 sEdges[w][t][1] = T.e1;
                 sEdges[w][t][2] = T.e2;
+                deferred = fan;
             }
             sBox[w][t] = bb;
             sOut[w][t] = tileCounts + slot0 + t;
         }
         __syncwarp();
-        count_tiles(has, B.tileLog2, e, bb, tileCounts + slot0 + t, tileMasks + slot0 + t, sEdges[w] + pass * 32,
-                    sBox[w] + pass * 32, sOut[w] + pass * 32);
+        count_tiles(has && !deferred, B.tileLog2, e, bb, tileCounts + slot0 + t,
+                    tileMasks + slot0 + t, sEdges[w] + pass * 32, sBox[w] + pass * 32,
+                    sOut[w] + pass * 32);
+        if (deferred)
+            tileCounts[slot0 + t] = kDeferredCount;
         __syncwarp();
     }
 }
@@ -1142,6 +1388,286 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
     count_tiles(has, B.tileLog2, e, bb, tileCounts + slot, tileMasks + slot, sEdges[w], sBox[w], sOut[w]);
 }
 
+// ---- Winding grids: the per-path passes ------------------------------------
+
+// One thread per path of the batch: an empty grid box, and whether the path's
+// interior tiles may become winding records. Eligible: a fill (no stroke
+// radius) without a feather, not the clear colour's path 0, not drawn as
+// wireframe, and not a nested clip update (its stash of the outer clip keeps
+// an RGBA8 rounding when a pixel saw more than one fragment of it, which a
+// single winding entry cannot reproduce).
+__global__ void __launch_bounds__(256) path_init_kernel(BatchTables B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.pathBase[B.sceneCount])
+        return;
+    const uint32_t scene = find_range(B.pathBase, B.sceneCount, i);
+    const FlushParams& P = B.scenes[scene];
+    const uint32_t pid = i - B.pathBase[scene];
+    PathGrid g;
+    g.tx0 = g.ty0 = 0x7fffffff;
+    g.tx1 = g.ty1 = -0x7fffffff;
+    g.offset = 0;
+    g.anchor = 0xffffffffu;
+    g.entries = 0;
+    g.flags = 0;
+    g.length = 0.f;
+    if (pid != 0 && !P.wireframe)
+    {
+        const uint4 r1 = P.paths[4 * (size_t)(P.firstPath + pid) + 1];
+        const uint2 paint = P.paints[P.firstPaint + pid];
+        const bool nestedClip = (paint.x & 0xfu) == CLIP_UPDATE_PAINT_TYPE && (paint.x >> 16) != 0;
+        if (__uint_as_float(r1.z) == 0.f && __uint_as_float(r1.w) == 0.f && !nestedClip)
+            g.flags = PATH_GRID_ELIGIBLE;
+    }
+    B.grids[i] = g;
+}
+
+// One thread per tessellation span of the batch: grows its path's grid box by
+// the span's control points and its contour's midpoint, mapped to pixels by
+// the path's matrix (curves stay inside their control points' hull), widened
+// by the AA offset (1/2 px) and the edge margin, in tiles clipped to the
+// canvas.
+__global__ void __launch_bounds__(256) path_bounds_kernel(BatchTables B)
+{
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= B.totalTessSpans)
+        return;
+    const uint32_t scene = find_range(B.tessSpanBase, B.sceneCount, gi);
+    const FlushParams& P = B.scenes[scene];
+    const uint4* sp = P.tessSpans + 4 * (size_t)(P.firstTessSpan + gi - B.tessSpanBase[scene]);
+    const uint32_t contourID = sp[3].w & CONTOUR_ID_MASK;
+    if (contourID == 0 || contourID > P.contourCount)
+        return;
+    const uint4 cd = P.contours[P.firstContour + contourID - 1];
+    const uint32_t pid = cd.z & 0xffffu;
+    if (pid >= P.pathCount)
+        return;
+    PathGrid* g = B.grids + B.pathBase[scene] + pid;
+    if (!(g->flags & PATH_GRID_ELIGIBLE))
+        return;
+    const uint4* path = P.paths + 4 * (size_t)(P.firstPath + pid);
+    const uint4 r0 = path[0], r1 = path[1];
+    const float4 M = make_float4(__uint_as_float(r0.x), __uint_as_float(r0.y),
+                                 __uint_as_float(r0.z), __uint_as_float(r0.w));
+    const float2 tr = make_float2(__uint_as_float(r1.x), __uint_as_float(r1.y));
+    const uint4 q0 = sp[0], q1 = sp[1];
+    const float2 pts[5] = {make_float2(__uint_as_float(q0.x), __uint_as_float(q0.y)),
+                           make_float2(__uint_as_float(q0.z), __uint_as_float(q0.w)),
+                           make_float2(__uint_as_float(q1.x), __uint_as_float(q1.y)),
+                           make_float2(__uint_as_float(q1.z), __uint_as_float(q1.w)),
+                           make_float2(__uint_as_float(cd.x), __uint_as_float(cd.y))};
+    float x0 = 3e38f, y0 = 3e38f, x1 = -3e38f, y1 = -3e38f, len = 0.f;
+    float2 prev = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+    {
+        const float2 q = mat_mul(M, pts[k]);
+        const float x = q.x + tr.x, y = q.y + tr.y;
+        if (!(fabsf(x) < 1e9f && fabsf(y) < 1e9f))
+            return; // non-finite: the set-up marks the path unsafe
+        x0 = fminf(x0, x);
+        x1 = fmaxf(x1, x);
+        y0 = fminf(y0, y);
+        y1 = fmaxf(y1, y);
+        if (k > 0 && k < 4) // the control polygon p0-p1-p2-p3
+            len += sqrtf((x - prev.x) * (x - prev.x) + (y - prev.y) * (y - prev.y));
+        prev = make_float2(x, y);
+    }
+    atomicAdd(&g->length, len);
+    const float pad = kAARadius + kWindingEdgeMargin + 1.f;
+    const float ts = (float)(1 << B.tileLog2);
+    const int tilesY = (int)((P.height + (1u << B.tileLog2) - 1) >> B.tileLog2);
+    const int tx0 = max((int)floorf((x0 - pad) / ts), 0);
+    const int ty0 = max((int)floorf((y0 - pad) / ts), 0);
+    const int tx1 = min((int)floorf((x1 + pad) / ts), (int)P.tilesX - 1) + 1;
+    const int ty1 = min((int)floorf((y1 + pad) / ts), tilesY - 1) + 1;
+    if (tx0 >= tx1 || ty0 >= ty1)
+        return;
+    atomicMin(&g->tx0, tx0);
+    atomicMin(&g->ty0, ty0);
+    atomicMax(&g->tx1, tx1);
+    atomicMax(&g->ty1, ty1);
+}
+
+// One thread per path: places an eligible path's grid in the pool (one cell
+// per tile of its box), unless its contour is long enough to make most of
+// those tiles edge tiles. gridCounters[0] ends as the cells the batch asked
+// for; a grid past the pool's capacity is not placed, and that path keeps its
+// fan triangles on every tile.
+__global__ void __launch_bounds__(256) path_alloc_kernel(BatchTables B)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B.pathBase[B.sceneCount])
+        return;
+    PathGrid& g = B.grids[i];
+    if (!(g.flags & PATH_GRID_ELIGIBLE) || g.tx0 >= g.tx1 || g.ty0 >= g.ty1)
+        return;
+    const uint32_t cells = (uint32_t)(g.tx1 - g.tx0) * (uint32_t)(g.ty1 - g.ty0);
+    // Too little interior to pay for the grid: keep the plain fan.
+    if (1.5f * g.length * (1.f / (float)(1 << B.tileLog2)) >= kWindingMaxEdgeShare * (float)cells)
+        return;
+    const uint32_t off = atomicAdd(&B.gridCounters[0], cells);
+    if ((uint64_t)off + cells <= B.gridCapacity)
+    {
+        g.offset = off;
+        g.flags |= PATH_GRID_PLACED;
+    }
+}
+
+// One warp per path, after fan_filter_kernel: each grid row's deltas become the
+// windings of its tiles (a warp scan, 32 columns at a time), and the path's
+// interior tiles with a nonzero winding are counted into its anchor slot.
+__global__ void __launch_bounds__(256) path_winding_kernel(BatchTables B,
+                                                           uint32_t* __restrict__ tileCounts)
+{
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= B.pathBase[B.sceneCount])
+        return;
+    PathGrid* g = B.grids + i;
+    const uint32_t flags = g->flags;
+    if ((flags & (PATH_GRID_ELIGIBLE | PATH_GRID_PLACED)) != (PATH_GRID_ELIGIBLE | PATH_GRID_PLACED))
+        return;
+    const int gw = g->tx1 - g->tx0, gh = g->ty1 - g->ty0;
+    const uint32_t anchor = g->anchor;
+    const bool counted = !(flags & PATH_GRID_UNSAFE) && anchor != 0xffffffffu;
+    uint32_t n = 0;
+    for (int r = 0; r < gh; ++r)
+    {
+        int32_t* row = B.gridWinding + g->offset + (size_t)r * gw;
+        const uint8_t* edge = B.gridEdge + g->offset + (size_t)r * gw;
+        int32_t carry = 0;
+        for (int c0 = 0; c0 < gw; c0 += 32)
+        {
+            const int c = c0 + lane;
+            int32_t v = c < gw ? row[c] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int32_t y = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o)
+                    v += y;
+            }
+            v += carry;
+            if (c < gw)
+            {
+                row[c] = v;
+                n += (counted && !edge[c] && v != 0) ? 1u : 0u;
+            }
+            carry = __shfl_sync(0xffffffffu, v, 31);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        n += __shfl_xor_sync(0xffffffffu, n, o);
+    if (lane == 0)
+    {
+        g->entries = counted ? n : 0u;
+        if (counted && n)
+        {
+            tileCounts[anchor] = n;
+            atomicAdd(&B.gridCounters[1], n);
+        }
+    }
+}
+
+// One thread per fan triangle (16..23) of every midpoint-fan patch, after the
+// set-up: a deferred one adds its coverage into its path's winding deltas and
+// counts its tiles, now that the path's edge tiles are known (only edge
+// tiles, when the path's grid is usable), with the per-slot tile mask for
+// small boxes, as count_tiles does.
+__global__ void __launch_bounds__(256) fan_filter_kernel(BatchTables B,
+                                                         const TriRecord* __restrict__ tris,
+                                                         uint32_t* __restrict__ tileCounts,
+                                                         uint8_t* __restrict__ tileMasks)
+{
+    __shared__ float4 sEdges[8][32][3];
+    __shared__ int4 sBox[8][32];
+    __shared__ const PathGrid* sGrid[8][32];
+    __shared__ uint32_t sSlot[8][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t total = B.totalItems[0] * 8u;
+    const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((gi & ~31u) >= total)
+        return; // whole warp exits together
+    const int tileLog2 = B.tileLog2;
+    bool big = false;
+    if (gi < total)
+    {
+        const uint32_t patch = gi >> 3;
+        const uint32_t seg = find_range(B.segBase[0], B.segCount[0], patch);
+        const PatchSegment S = B.segments[0][seg];
+        const uint32_t slot =
+            S.slotBase + (patch - B.segBase[0][seg]) * B.fanSlotStride + 16u + (gi & 7u);
+        if (tileCounts[slot] == kDeferredCount)
+        {
+            const TriRecord& T = tris[slot];
+            const uint4 meta = T.meta;
+            const int4 bb = unpack_bbox(meta);
+            const float4 e[3] = {T.e0, T.e1, T.e2};
+            const PathGrid* g = winding_grid(B, meta.w >> 16, meta.x & 0xffffu);
+            // A fan triangle's coverage is +-1 everywhere (its three vertices
+            // carry the same fill coverage): its share of the path's windings.
+            if (g)
+                fan_winding_deltas(T, bb, T.cov0.x > 0.f ? 1 : -1, *g, B.gridWinding, tileLog2);
+            int tx0, ty0, ntx, nty;
+            tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
+            if (ntx * nty <= kLaneTiles)
+            {
+                uint32_t count = 0, mask = 0;
+                int k = 0;
+                for (int ty = ty0; ty < ty0 + nty; ++ty)
+                    for (int tx = tx0; tx < tx0 + ntx; ++tx, ++k)
+                        if (tile_overlaps(e, bb, tx, ty, tileLog2) &&
+                            keep_fan_tile(g, B.gridEdge, tx, ty))
+                        {
+                            ++count;
+                            mask |= 1u << k;
+                        }
+                tileCounts[slot] = count;
+                tileMasks[slot] = (uint8_t)mask;
+            }
+            else
+            {
+                big = true;
+                sEdges[w][lane][0] = e[0];
+                sEdges[w][lane][1] = e[1];
+                sEdges[w][lane][2] = e[2];
+                sBox[w][lane] = bb;
+                sGrid[w][lane] = g;
+                sSlot[w][lane] = slot;
+            }
+        }
+    }
+    __syncwarp();
+    uint32_t bigs = __ballot_sync(0xffffffffu, big);
+    while (bigs)
+    {
+        const int t = __ffs(bigs) - 1;
+        bigs &= bigs - 1;
+        const int4 tb = sBox[w][t];
+        const float4 te[3] = {sEdges[w][t][0], sEdges[w][t][1], sEdges[w][t][2]};
+        const PathGrid* tg = sGrid[w][t];
+        int tx0, ty0, ntx, nty;
+        tile_span(tb, tileLog2, tx0, ty0, ntx, nty);
+        const int n = ntx * nty;
+        uint32_t count = 0;
+        for (int i = lane; i < n; i += 32)
+        {
+            const int tx = tx0 + i % ntx, ty = ty0 + i / ntx;
+            count += (tile_overlaps(te, tb, tx, ty, tileLog2) && keep_fan_tile(tg, B.gridEdge, tx, ty))
+                         ? 1u
+                         : 0u;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            count += __shfl_xor_sync(0xffffffffu, count, o);
+        if (lane == 0)
+            tileCounts[sSlot[w][t]] = count;
+    }
+}
+
 // FlushUniforms fields the passes use (gpu.hpp:1466-1537: pathIDGranularity
 // at byte 72, ditherScale at 88, ditherBias at 92), read on the device so no
 // pass waits for the host. One thread per flush of the batch.
@@ -1174,18 +1700,23 @@ __global__ void bin_fill_kernel(const uint32_t* __restrict__ pairTotal,
 // warp per 32 consecutive slots: a lane writes its own triangle's pairs when
 // its box spans few tiles; larger triangles are walked by the whole warp with
 // a ballot assigning output positions. Pairs at or past `capacity` are
-// dropped and flagged (ERR_BIN_OVERFLOW).
-__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
-                                                          int tileLog2,
-                                                          const uint2* __restrict__ sceneTiles,
-                                                          const TriRecord* __restrict__ tris,
-                                                          const uint32_t* __restrict__ tileCounts,
-                                                          const uint8_t* __restrict__ tileMasks,
-                                                          const uint32_t* __restrict__ offsets,
-                                                          uint32_t capacity,
-                                                          uint32_t* __restrict__ error,
-                                                          uint32_t* __restrict__ keys,
-                                                          uint32_t* __restrict__ vals)
+// dropped and flagged (ERR_BIN_OVERFLOW). With kWinding (interior tiles as
+// winding records), a deferred fan triangle's large box keeps its path's
+// edge tiles only, and an anchor winding slot writes one entry per interior
+// tile of its path with a nonzero winding.
+template <bool kWinding>
+__device__ __forceinline__ void bin_scatter(const BatchTables* __restrict__ Bw,
+                                            uint32_t slotCount,
+                                            int tileLog2,
+                                            const uint2* __restrict__ sceneTiles,
+                                            const TriRecord* __restrict__ tris,
+                                            const uint32_t* __restrict__ tileCounts,
+                                            const uint8_t* __restrict__ tileMasks,
+                                            const uint32_t* __restrict__ offsets,
+                                            uint32_t capacity,
+                                            uint32_t* __restrict__ error,
+                                            uint32_t* __restrict__ keys,
+                                            uint32_t* __restrict__ vals)
 {
     constexpr int kLaneTiles = 8;
     const uint32_t warpId = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1198,13 +1729,18 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
     bool isBig = false;
     if (myCount)
     {
-        const int4 bb = unpack_bbox(tris[mySlot].meta);
+        const uint4 meta = tris[mySlot].meta;
+        const int4 bb = unpack_bbox(meta);
         int tx0, ty0, ntx, nty;
         tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
-        if (ntx * nty <= kLaneTiles)
+        if (kWinding && (meta.x & (FEATURE_WINDING_SLOT << 16)))
+        {
+            isBig = true; // the warp writes a path's winding entries
+        }
+        else if (ntx * nty <= kLaneTiles)
         {
             // The set-up already tested these tiles: walk its mask.
-            const uint2 st = sceneTiles[tris[mySlot].meta.w >> 16]; // (tileBase, tilesX)
+            const uint2 st = sceneTiles[meta.w >> 16]; // (tileBase, tilesX)
             uint32_t mask = tileMasks[mySlot];
             uint32_t o = offsets[mySlot];
             while (mask)
@@ -1235,11 +1771,46 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
         const int t = __ffs(pending) - 1;
         pending &= pending - 1;
         const uint32_t slot = first + t;
-        const int4 bb = unpack_bbox(tris[slot].meta);
         const TriRecord* T = tris + slot;
-        const float4 e[3] = {T->e0, T->e1, T->e2};
-        const uint2 st = sceneTiles[T->meta.w >> 16];
+        const uint4 meta = T->meta;
+        const uint2 st = sceneTiles[meta.w >> 16];
         uint32_t o = offsets[slot];
+        if (kWinding && (meta.x & (FEATURE_WINDING_SLOT << 16)))
+        {
+            // The path's grid, from its winding slot's record.
+            const uint32_t goff = __float_as_uint(T->e0.x);
+            const int gx0 = __float_as_int(T->e0.y), gy0 = __float_as_int(T->e0.z);
+            const int gw = __float_as_int(T->e0.w), gh = __float_as_int(T->e1.x);
+            const uint32_t cells = (uint32_t)gw * (uint32_t)gh;
+            for (uint32_t base = 0; base < cells; base += 32)
+            {
+                const uint32_t c = base + lane;
+                const bool hit =
+                    c < cells && !Bw->gridEdge[goff + c] && Bw->gridWinding[goff + c] != 0;
+                const uint32_t mask = __ballot_sync(0xffffffffu, hit);
+                if (hit)
+                {
+                    const uint32_t pos = o + __popc(mask & ((1u << lane) - 1u));
+                    const int tx = gx0 + (int)(c % (uint32_t)gw), ty = gy0 + (int)(c / (uint32_t)gw);
+                    if (pos < capacity)
+                    {
+                        keys[pos] = st.x + (uint32_t)ty * st.y + (uint32_t)tx;
+                        vals[pos] = BIN_WINDING_ENTRY | slot;
+                    }
+                    else
+                    {
+                        atomicOr(error, ERR_BIN_OVERFLOW);
+                    }
+                }
+                o += __popc(mask);
+            }
+            continue;
+        }
+        const int4 bb = unpack_bbox(meta);
+        const float4 e[3] = {T->e0, T->e1, T->e2};
+        const PathGrid* g = (kWinding && (meta.x & (FEATURE_FAN_DEFERRED << 16)))
+                                ? winding_grid(*Bw, meta.w >> 16, meta.x & 0xffffu)
+                                : nullptr;
         int tx0, ty0, ntx, nty;
         tile_span(bb, tileLog2, tx0, ty0, ntx, nty);
         const int n = ntx * nty;
@@ -1252,7 +1823,8 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
             {
                 tx = tx0 + i % ntx;
                 ty = ty0 + i / ntx;
-                hit = tile_overlaps(e, bb, tx, ty, tileLog2);
+                hit = tile_overlaps(e, bb, tx, ty, tileLog2) &&
+                      (!kWinding || keep_fan_tile(g, kWinding ? Bw->gridEdge : nullptr, tx, ty));
             }
             const uint32_t mask = __ballot_sync(0xffffffffu, hit);
             if (hit)
@@ -1271,6 +1843,38 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
             o += __popc(mask);
         }
     }
+}
+
+__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
+                                                          int tileLog2,
+                                                          const uint2* __restrict__ sceneTiles,
+                                                          const TriRecord* __restrict__ tris,
+                                                          const uint32_t* __restrict__ tileCounts,
+                                                          const uint8_t* __restrict__ tileMasks,
+                                                          const uint32_t* __restrict__ offsets,
+                                                          uint32_t capacity,
+                                                          uint32_t* __restrict__ error,
+                                                          uint32_t* __restrict__ keys,
+                                                          uint32_t* __restrict__ vals)
+{
+    bin_scatter<false>(nullptr, slotCount, tileLog2, sceneTiles, tris, tileCounts, tileMasks,
+                       offsets, capacity, error, keys, vals);
+}
+
+// The same, for batches that draw interior tiles as winding records.
+__global__ void __launch_bounds__(256) bin_scatter_winding_kernel(BatchTables B,
+                                                                  const TriRecord* __restrict__ tris,
+                                                                  const uint32_t* __restrict__ tileCounts,
+                                                                  const uint8_t* __restrict__ tileMasks,
+                                                                  const uint32_t* __restrict__ offsets,
+                                                                  uint32_t slotCount,
+                                                                  uint32_t capacity,
+                                                                  uint32_t* __restrict__ error,
+                                                                  uint32_t* __restrict__ keys,
+                                                                  uint32_t* __restrict__ vals)
+{
+    bin_scatter<true>(&B, slotCount, B.tileLog2, B.sceneTiles, tris, tileCounts, tileMasks,
+                      offsets, capacity, error, keys, vals);
 }
 
 __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
@@ -1733,6 +2337,11 @@ __device__ __noinline__ float feathered_fragment(const float4* __restrict__ plan
 #ifndef RIVE_RASTER_MIN_BLOCKS
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
+// Bin entries each thread stages per chunk (8x8 and 16x16 tiles): a chunk of
+// kStage x threads entries between two CTA barriers.
+#ifndef RIVE_RASTER_STAGE
+#define RIVE_RASTER_STAGE 1
+#endif
 
 // Tile geometry: a CTA of T x T threads, one per pixel; warp w owns the 8x4
 // block at (8 (w % (T/8)), 4 (w / (T/8))).
@@ -1745,7 +2354,7 @@ template <int TL> struct RasterTile
     using Mask = typename std::conditional<(kBlocks <= 8), uint8_t, uint32_t>::type;
 };
 
-template <int TL, bool kFeather>
+template <int TL, bool kFeather, int kStage>
 __device__ __forceinline__ void raster_tile(const BatchTables& B,
                                             const TriRecord* __restrict__ tris,
                                             const uint32_t* __restrict__ sortedSlots,
@@ -1795,15 +2404,43 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
     const float dither = v2 * P.ditherScale + P.ditherBias;
     uint32_t streamPath = 0xffffffffu; // coverage key of the warp's current path
 
-    for (uint32_t base = range.x; base < range.y; base += G::kThreads)
+    constexpr uint32_t kChunk = (uint32_t)G::kThreads * kStage;
+    for (uint32_t base = range.x; base < range.y; base += kChunk)
     {
-        // Each thread stages one triangle in tile-local form and marks which
-        // of the warp blocks may hold a pixel it covers.
-        const uint32_t k = base + threadIdx.x;
-        uint32_t m = 0;
-        if (k < range.y)
+        // Each thread stages kStage triangles in tile-local form and marks
+        // which of the warp blocks may hold a pixel each covers.
+#pragma unroll
+        for (int j = 0; j < kStage; ++j)
         {
-            const TriRecord T = tris[sortedSlots[k]];
+        const uint32_t si = (uint32_t)j * G::kThreads + threadIdx.x;
+        const uint32_t k = base + si;
+        uint32_t m = 0;
+        const uint32_t entry = k < range.y ? sortedSlots[k] : 0u;
+        if (k < range.y && (entry & BIN_WINDING_ENTRY))
+        {
+            // A winding entry: the path's winding W on this interior tile, as
+            // a "triangle" covering every pixel with constant fill coverage W
+            // (edge functions 1, coverage planes flat).
+            const TriRecord& R = tris[entry & ~BIN_WINDING_ENTRY];
+            const float4 ge = R.e0;
+            const uint32_t cell = __float_as_uint(ge.x) +
+                                  (uint32_t)(ty - __float_as_int(ge.z)) * (uint32_t)__float_as_int(ge.w) +
+                                  (uint32_t)(tx - __float_as_int(ge.y));
+            const float W = (float)B.gridWinding[cell];
+            const uint4 meta = R.meta;
+            const float4 cv = R.cov1;
+            TileTri L;
+            L.v0 = make_float4(__uint_as_float(meta.w & 0xffffu), 1.f, 0.f, 0.f);
+            L.v1 = make_float4(1.f, 0.f, 0.f, 1.f);
+            L.v2 = make_float4(0.f, 0.f, W, 0.f);
+            L.v3 = make_float4(0.f, -1.f, 0.f, 0.f);
+            L.v4 = make_uint4(__float_as_uint(cv.z), __float_as_uint(cv.w), meta.x, 0u);
+            sTris[si] = L;
+            m = G::kBlocks >= 32 ? 0xffffffffu : ((1u << (G::kBlocks & 31)) - 1u);
+        }
+        else if (k < range.y)
+        {
+            const TriRecord T = tris[entry];
             const float4 e[3] = {T.e0, T.e1, T.e2};
             const float c[3] = {tile_edge_origin(e[0], tx, ty, TL),
                                 tile_edge_origin(e[1], tx, ty, TL),
@@ -1817,8 +2454,8 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
             L.v3 = make_float4(T.cov0.z, T.cov0.w + T.cov1.x * dx0 + T.cov1.y * dy0, T.cov1.x,
                                T.cov1.y);
             L.v4 = make_uint4(__float_as_uint(T.cov1.z), __float_as_uint(T.cov1.w), T.meta.x,
-                              sortedSlots[k]);
-            sTris[threadIdx.x] = L;
+                              entry);
+            sTris[si] = L;
             const int4 bb = unpack_bbox(T.meta);
             const int bx0 = bb.x - ox, bx1 = bb.z - ox, by0 = bb.y - oy, by1 = bb.w - oy;
 #pragma unroll
@@ -1831,9 +2468,10 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                     m |= 1u << b;
             }
         }
-        sMask[threadIdx.x] = (typename G::Mask)m;
+        sMask[si] = (typename G::Mask)m;
+        }
         __syncthreads();
-        const uint32_t n = min((uint32_t)G::kThreads, range.y - base);
+        const uint32_t n = min(kChunk, range.y - base);
         for (uint32_t g = 0; g < n; g += 32)
         {
             // Triangles of this group touching this warp's block, in order.
@@ -1926,9 +2564,9 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
         BatchTables B, const TriRecord* __restrict__ tris,                                        \
         const uint32_t* __restrict__ sortedSlots, const uint2* __restrict__ ranges)               \
     {                                                                                             \
-        __shared__ TileTri sTris[256];                                                            \
-        __shared__ uint8_t sMask[256];                                                            \
-        raster_tile<4, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+        __shared__ TileTri sTris[256 * RIVE_RASTER_STAGE];                                        \
+        __shared__ uint8_t sMask[256 * RIVE_RASTER_STAGE];                                        \
+        raster_tile<4, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask);   \
     }
 RIVE_RASTER_KERNELS(raster_tile_kernel, false)
 RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
@@ -1939,9 +2577,9 @@ RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
                                                const uint32_t* __restrict__ sortedSlots,         \
                                                const uint2* __restrict__ ranges)                 \
     {                                                                                             \
-        __shared__ TileTri sTris[64];                                                             \
-        __shared__ uint8_t sMask[64];                                                             \
-        raster_tile<3, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+        __shared__ TileTri sTris[64 * RIVE_RASTER_STAGE];                                         \
+        __shared__ uint8_t sMask[64 * RIVE_RASTER_STAGE];                                         \
+        raster_tile<3, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask);   \
     }
 RIVE_RASTER8_KERNELS(raster_tile8_kernel, false)
 RIVE_RASTER8_KERNELS(raster_tile8_feather_kernel, true)
@@ -1957,7 +2595,7 @@ RIVE_RASTER8_KERNELS(raster_tile8_feather_kernel, true)
         extern __shared__ uint4 dyn[];                                                            \
         TileTri* sTris = reinterpret_cast<TileTri*>(dyn);                                         \
         uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);                              \
-        raster_tile<5, FEATHER>(B, tris, sortedSlots, ranges, sTris, sMask);                      \
+        raster_tile<5, FEATHER, 1>(B, tris, sortedSlots, ranges, sTris, sMask);                   \
     }
 RIVE_RASTER32_KERNELS(raster_tile32_kernel, false)
 RIVE_RASTER32_KERNELS(raster_tile32_feather_kernel, true)

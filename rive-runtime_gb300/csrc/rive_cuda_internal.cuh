@@ -101,6 +101,42 @@ void build_inverse_feather_table(float out[kGaussianTableSize]);
 cudaError_t ensure_feather_lut(int device);
 void feather_table_f16(uint16_t out[kGaussianTableSize]);
 constexpr uint32_t FEATURE_CLOCKWISE_FILL = 1u << 15;
+// Two more bits of a triangle record's feature half-word, set only when the
+// batch draws interior tiles as winding records: a fan triangle whose tiles
+// are counted after its path's winding grid is complete, and the record of a
+// patch's winding slot (one per midpoint-fan patch, after its 24 triangles).
+constexpr uint32_t FEATURE_FAN_DEFERRED = 1u << 14;
+constexpr uint32_t FEATURE_WINDING_SLOT = 1u << 13;
+// A bin entry's value with this bit set names a winding slot, not a triangle.
+constexpr uint32_t BIN_WINDING_ENTRY = 1u << 31;
+// tileCounts value of a deferred fan triangle until its tiles are counted.
+constexpr uint32_t kDeferredCount = 0xffffffffu;
+
+// Per path of a batch, for drawing interior tiles as winding records: the
+// path's tile box (clipped to the canvas), its place in the grid pool (one
+// int32 winding and one edge byte per tile of the box), and the slot that
+// carries its winding entries.
+struct PathGrid
+{
+    int tx0, ty0, tx1, ty1; // tiles [tx0, tx1) x [ty0, ty1)
+    uint32_t offset;        // first cell in the pool
+    uint32_t flags;         // PATH_GRID_* bits
+    uint32_t anchor;        // winding slot of the path's first patch
+    uint32_t entries;       // winding entries (interior tiles with a nonzero winding)
+    float length;           // pixels of control polygon (bounds the contour's length)
+};
+constexpr uint32_t PATH_GRID_ELIGIBLE = 1u; // a fill whose interior tiles may be winding records
+constexpr uint32_t PATH_GRID_UNSAFE = 2u;   // a patch was discarded or non-finite: no winding records
+constexpr uint32_t PATH_GRID_PLACED = 4u;   // the grid fits the pool (offset valid)
+// Pixels of margin around a tile's pixel centres within which a contour edge
+// or midpoint makes the tile an edge tile: an AA ramp lies within 1 px
+// (max norm) of its contour edge, plus snapping and float rounding.
+constexpr float kWindingEdgeMargin = 2.f;
+// A path gets a winding grid only when its contour cannot mark more than
+// this share of its box's tiles as edge tiles (a contour of length L crosses
+// at most about 1.5 L / T tiles of size T, margins included): scribbles whose
+// contour passes through nearly every tile keep their plain fans.
+constexpr float kWindingMaxEdgeShare = .75f;
 
 // Raster tiles: 16x16 by default; 8x8 and 32x32 are the autotuner's other
 // choices (rive_cuda_set_raster_config).
@@ -205,6 +241,16 @@ struct BatchTables
     // the feather coverage's third and fourth components (cotTheta, y0) as
     // (z0, dz/dx, dz/dy, w0), (dw/dx, dw/dy, anchor x, anchor y).
     float4* featherPlanes;
+    // Interior tiles as winding records (null grids: off). Midpoint-fan
+    // patches then take fanSlotStride = 25 slots (24 triangles and the
+    // winding slot), otherwise 24.
+    uint32_t fanSlotStride;
+    const uint32_t* pathBase;  // [sceneCount + 1]: first path of each scene
+    PathGrid* grids;           // [pathBase[sceneCount]]
+    int32_t* gridWinding;      // pool: per cell, deltas, then the winding
+    uint8_t* gridEdge;         // pool: per cell, nonzero for an edge tile
+    uint32_t gridCapacity;     // cells in the pool
+    uint32_t* gridCounters;    // [0] cells asked for, [1] winding entries
 };
 
 // Index j with base[j] <= i < base[j + 1] (empty ranges skipped), n >= 1.

@@ -56,7 +56,7 @@ class BatchFlush(ctypes.Structure):
 class FlushStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "tess_vertices", "patches", "triangles", "bin_entries", "tiles",
-        "kernel_launches")]
+        "kernel_launches", "winding_entries")]
 
 
 class RiveCudaError(RuntimeError):
@@ -115,6 +115,8 @@ def load():
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
+        "rive_cuda_set_winding_tiles": (i32, [vp, i32]),
+        "rive_cuda_get_winding_tiles": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_feather_table": (i32, [vp]),
         "rive_cuda_inverse_feather_table": (i32, [vp]),
         "rive_cuda_get_raster_config": (i32, [vp, ctypes.POINTER(ctypes.c_int),
@@ -349,6 +351,18 @@ class Context:
         fit) for later flushes; the image is the same within tolerance."""
         self.check(self.lib.rive_cuda_set_raster_config(self.h, int(tile_size), int(ctas_per_sm)),
                    "set_raster_config")
+
+    def set_winding_tiles(self, on: bool):
+        """Interior tiles of fills as one winding record per path (on by
+        default) or as the plain midpoint fan; the image is the same."""
+        self.check(self.lib.rive_cuda_set_winding_tiles(self.h, 1 if on else 0),
+                   "set_winding_tiles")
+
+    def winding_tiles(self):
+        v = ctypes.c_int()
+        self.check(self.lib.rive_cuda_get_winding_tiles(self.h, ctypes.byref(v)),
+                   "get_winding_tiles")
+        return bool(v.value)
 
     def raster_config(self):
         t, c = ctypes.c_int(), ctypes.c_int()
