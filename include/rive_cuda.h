@@ -359,6 +359,19 @@ int rive_cuda_read_grad_texture(rive_cuda_context* ctx,
                                 void* dst_host,
                                 size_t bytes);
 
+/*
+ * The tessellation pass's device functions evaluated on n host items (no
+ * counterpart in the reference; for parity tests of the kernel's building
+ * blocks against the oracle and the reference's unit-test properties). By fn,
+ * floats in / out per item:
+ *   0 clamped_divide(a, b) 2/1; 1 cubic max height (p0..p3) 8/2 (height, T);
+ *   2 local curvature (p0..p3, T, spread) 10/1; 3 De Casteljau point at T
+ *   9/2; 4 Wang's segment count under a 2x2 matrix 12/1; 5 end tangents 8/4;
+ *   10 sin, 11 cos, 12 acos, 13 cube root 1/1.
+ * Synchronous on the current device; allocates its own temporaries.
+ */
+int rive_cuda_eval_tessellation_math(int fn, const float* in, float* out, size_t n);
+
 /* Counters of the last flush (triangles set up, tile bin entries, ...). */
 typedef struct rive_cuda_flush_stats
 {

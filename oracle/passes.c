@@ -481,6 +481,33 @@ static float measure_cubic_local_curvature(f2 p0, f2 p1, f2 p2, f2 p3, float T,
     return rc_acosf(cosine_between_vectors(tan0, tan1));
 }
 
+/* The tessellated point at T by De Casteljau with unchecked_mix(a, b, t) =
+ * (b - a) * t + a (tessellate.glsl:535-540); *abc and *bcd are the last
+ * level's pair, whose difference is the tangent. */
+static f2 eval_cubic_mix(f2 p0, f2 p1, f2 p2, f2 p3, float T, f2* abc, f2* bcd)
+{
+    f2 ab = add2(mul2(sub2(p1, p0), T), p0);
+    f2 bc = add2(mul2(sub2(p2, p1), T), p1);
+    f2 cd = add2(mul2(sub2(p3, p2), T), p2);
+    *abc = add2(mul2(sub2(bc, ab), T), ab);
+    *bcd = add2(mul2(sub2(cd, bc), T), bc);
+    return add2(mul2(sub2(*bcd, *abc), T), *abc);
+}
+
+/* The parametric segment count of a cubic in pixel space under the path's
+ * 2x2 matrix m (columns (m0, m1), (m2, m3)): Wang's formula at precision 4,
+ * as the CULL_EXCESS_TESSELLATION_SEGMENTS recount (tessellate.glsl:195-211)
+ * evaluates it. */
+static float wang_cubic_segments(f2 p0, f2 p1, f2 p2, f2 p3, const float* m)
+{
+    f2 a = {-2.f * p1.x + p2.x + p0.x, -2.f * p1.y + p2.y + p0.y};
+    f2 c = {-2.f * p2.x + p3.x + p1.x, -2.f * p2.y + p3.y + p1.y};
+    f2 d0 = {m[0] * a.x + m[2] * a.y, m[1] * a.x + m[3] * a.y};
+    f2 d1 = {m[0] * c.x + m[2] * c.y, m[1] * c.x + m[3] * c.y};
+    float mm = maxf(dot2(d0, d0), dot2(d1, d1));
+    return maxf(ceilf(sqrtf(.75f * 4.f * sqrtf(mm))), 1.f);
+}
+
 /* Vertex-shader half of pass 2, evaluated once per span rectangle. */
 static int tess_setup(const rive_cuda_flush_desc* d,
                       const oracle_buffers* b,
@@ -551,13 +578,7 @@ static int tess_setup(const rive_cuda_flush_desc* d,
         if (!path)
             return -1;
         /* mat = [[m0, m1], [m2, m3]] columns; MUL(mat, v). */
-        f2 a = {-2.f * p1.x + p2.x + p0.x, -2.f * p1.y + p2.y + p0.y};
-        f2 c = {-2.f * p2.x + p3.x + p1.x, -2.f * p2.y + p3.y + p1.y};
-        f2 d0 = {path[0] * a.x + path[2] * a.y, path[1] * a.x + path[3] * a.y};
-        f2 d1 = {path[0] * c.x + path[2] * c.y, path[1] * c.x + path[3] * c.y};
-        float m = maxf(dot2(d0, d0), dot2(d1, d1));
-        float n = maxf(ceilf(sqrtf(.75f * 4.f * sqrtf(m))), 1.f);
-        uint32_t un = (uint32_t)n;
+        uint32_t un = (uint32_t)wang_cubic_segments(p0, p1, p2, p3, path);
         parametricSegmentCount =
             un < parametricSegmentCount ? un : parametricSegmentCount;
     }
@@ -745,13 +766,8 @@ static void tess_fragment_t(const tess_varyings* v,
                 polarT = 0.f;
             T = maxf(parametricT, polarT);
         }
-        /* unchecked_mix(a, b, t) = (b - a) * t + a */
-        f2 ab = add2(mul2(sub2(p1, p0), T), p0);
-        f2 bc = add2(mul2(sub2(p2, p1), T), p1);
-        f2 cd = add2(mul2(sub2(p3, p2), T), p2);
-        f2 abc = add2(mul2(sub2(bc, ab), T), ab);
-        f2 bcd = add2(mul2(sub2(cd, bc), T), bc);
-        tessCoord = add2(mul2(sub2(bcd, abc), T), abc);
+        f2 abc, bcd;
+        tessCoord = eval_cubic_mix(p0, p1, p2, p3, T, &abc, &bcd);
         if (T != polarT)
             theta = rive_atan2(sub2(bcd, abc));
         if (outT)
@@ -2531,6 +2547,53 @@ int oracle_math_eval(int fn, const float* x, float* out, size_t n)
             case 2: out[i] = rc_acosf(x[i]); break;
             case 3: out[i] = rc_cbrtf(x[i]); break;
             default: return -1;
+        }
+    }
+    return 0;
+}
+
+/* Shader functions of the tessellation pass on n inputs, for the tests that
+ * hold them to the reference's bezier and Wang's-formula unit tests and to
+ * the kernel's device functions. Per item, by fn:
+ *   0 clamped_divide(a, b)                       in 2, out 1
+ *   1 find_cubic_max_height(p0..p3)              in 8, out 2 (height, T)
+ *   2 measure_cubic_local_curvature(p0..p3, T, spread)  in 10, out 1
+ *   3 the De Casteljau point at T                in 9, out 2
+ *   4 Wang's segment count under matrix m0..m3   in 12, out 1
+ *   5 find_cubic_tangents(p0..p3)                in 8, out 4 */
+int oracle_cubic_eval(int fn, const float* in, float* out, size_t n)
+{
+    static const int kIn[6] = {2, 8, 10, 9, 12, 8}, kOut[6] = {1, 2, 1, 2, 1, 4};
+    if (fn < 0 || fn > 5)
+        return -1;
+    for (size_t i = 0; i < n; ++i)
+    {
+        const float* x = in + i * kIn[fn];
+        float* y = out + i * kOut[fn];
+        f2 p0 = {x[0], x[1]}, p1 = {x[2], x[3]}, p2 = {x[4], x[5]}, p3 = {x[6], x[7]};
+        switch (fn)
+        {
+            case 0: y[0] = clamped_divide(x[0], x[1]); break;
+            case 1: y[0] = find_cubic_max_height(p0, p1, p2, p3, &y[1]); break;
+            case 2: y[0] = measure_cubic_local_curvature(p0, p1, p2, p3, x[8], x[9]); break;
+            case 3:
+            {
+                f2 abc, bcd, q = eval_cubic_mix(p0, p1, p2, p3, x[8], &abc, &bcd);
+                y[0] = q.x;
+                y[1] = q.y;
+                break;
+            }
+            case 4: y[0] = wang_cubic_segments(p0, p1, p2, p3, x + 8); break;
+            default:
+            {
+                f2 t0, t1;
+                find_cubic_tangents(p0, p1, p2, p3, &t0, &t1);
+                y[0] = t0.x;
+                y[1] = t0.y;
+                y[2] = t1.x;
+                y[3] = t1.y;
+                break;
+            }
         }
     }
     return 0;

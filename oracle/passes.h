@@ -96,6 +96,11 @@ void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
  * 2 acos, 3 cube root. Returns -1 for an unknown fn. */
 int oracle_math_eval(int fn, const float* x, float* out, size_t n);
 
+/* The tessellation pass's cubic functions on n items (fn 0 clamped_divide,
+ * 1 max height, 2 local curvature, 3 De Casteljau point, 4 Wang's segment
+ * count, 5 end tangents; see passes.c for the layouts). -1 for an unknown fn. */
+int oracle_cubic_eval(int fn, const float* in, float* out, size_t n);
+
 /* Half-float helpers exposed for known-answer tests. */
 uint16_t oracle_f32_to_f16(float f);
 /* The 512-entry fp16 feather (Gaussian integral) table. */

@@ -1739,6 +1739,13 @@ int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, in
     return RIVE_CUDA_OK;
 }
 
+int rive_cuda_eval_tessellation_math(int fn, const float* in, float* out, size_t n)
+{
+    if (!((fn >= 0 && fn <= 5) || (fn >= 10 && fn <= 13)) || (n && (!in || !out)))
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    return run_tess_math(fn, in, out, n) == cudaSuccess ? RIVE_CUDA_OK : RIVE_CUDA_ERR_CUDA;
+}
+
 int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled)
 {
     if (!ctx)

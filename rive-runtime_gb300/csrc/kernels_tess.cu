@@ -90,6 +90,36 @@ __device__ __forceinline__ float rive_atan2(float2 v)
     return v.y >= 0.f ? theta : -theta;
 }
 
+// The tessellated point at T by De Casteljau with unchecked_mix(a, b, t) =
+// (b - a) * t + a (tessellate.glsl:535-540); abc and bcd are the last
+// level's pair, whose difference is the tangent.
+__device__ __forceinline__ float2 eval_cubic_mix(float2 p0, float2 p1, float2 p2, float2 p3,
+                                                 float T, float2& abc, float2& bcd)
+{
+    const float2 ab = f2lerp(p0, p1, T);
+    const float2 bc = f2lerp(p1, p2, T);
+    const float2 cd = f2lerp(p2, p3, T);
+    abc = f2lerp(ab, bc, T);
+    bcd = f2lerp(bc, cd, T);
+    return f2lerp(abc, bcd, T);
+}
+
+// Wang's formula at precision 4 in pixel space under the path's 2x2 matrix m
+// (columns (m.x, m.y), (m.z, m.w)): the CULL_EXCESS_TESSELLATION_SEGMENTS
+// recount of the parametric segments (tessellate.glsl:195-211).
+__device__ __forceinline__ float wang_cubic_segments(float2 p0, float2 p1, float2 p2, float2 p3,
+                                                     float4 m)
+{
+    const float2 a = f2add(f2add(f2scale(p1, -2.f), p2), p0);
+    const float2 c = f2add(f2add(f2scale(p2, -2.f), p3), p1);
+    const float2 d0 = make_float2(__fadd_rn(__fmul_rn(m.x, a.x), __fmul_rn(m.z, a.y)),
+                                  __fadd_rn(__fmul_rn(m.y, a.x), __fmul_rn(m.w, a.y)));
+    const float2 d1 = make_float2(__fadd_rn(__fmul_rn(m.x, c.x), __fmul_rn(m.z, c.y)),
+                                  __fadd_rn(__fmul_rn(m.y, c.x), __fmul_rn(m.w, c.y)));
+    const float mm = fmaxf(f2dot(d0, d0), f2dot(d1, d1));
+    return fmaxf(ceilf(__fsqrt_rn(__fmul_rn(.75f * 4.f, __fsqrt_rn(mm)))), 1.f);
+}
+
 // The inverse feather table (the height at which the Gaussian integral
 // reaches x), fp16 values widened to float, written once per device by the
 // host before any flush.
@@ -303,17 +333,9 @@ __device__ SpanSetup span_setup(const FlushParams& P, const uint4* sp)
     }
     if (flags & CULL_EXCESS_TESSELLATION_SEGMENTS_CONTOUR_FLAG)
     {
-        float m0 = __uint_as_float(pathRow0.x), m1 = __uint_as_float(pathRow0.y);
-        float m2 = __uint_as_float(pathRow0.z), m3 = __uint_as_float(pathRow0.w);
-        float2 a = f2add(f2add(f2scale(s.p1, -2.f), s.p2), s.p0);
-        float2 c = f2add(f2add(f2scale(s.p2, -2.f), s.p3), s.p1);
-        float2 d0 = make_float2(__fadd_rn(__fmul_rn(m0, a.x), __fmul_rn(m2, a.y)),
-                                __fadd_rn(__fmul_rn(m1, a.x), __fmul_rn(m3, a.y)));
-        float2 d1 = make_float2(__fadd_rn(__fmul_rn(m0, c.x), __fmul_rn(m2, c.y)),
-                                __fadd_rn(__fmul_rn(m1, c.x), __fmul_rn(m3, c.y)));
-        float m = fmaxf(f2dot(d0, d0), f2dot(d1, d1));
-        float n = fmaxf(ceilf(__fsqrt_rn(__fmul_rn(.75f * 4.f, __fsqrt_rn(m)))), 1.f);
-        uint32_t un = (uint32_t)n;
+        const float4 m = make_float4(__uint_as_float(pathRow0.x), __uint_as_float(pathRow0.y),
+                                     __uint_as_float(pathRow0.z), __uint_as_float(pathRow0.w));
+        const uint32_t un = (uint32_t)wang_cubic_segments(s.p0, s.p1, s.p2, s.p3, m);
         parametric = min(un, parametric);
     }
     uint32_t total = parametric + polar + join - 1u;
@@ -480,12 +502,8 @@ __device__ uint4 tess_vertex(const SpanSetup& s, float vertexIdxF, uint32_t flag
                 polarT = 0.f;
             T = fmaxf(parametricT, polarT);
         }
-        float2 ab = f2lerp(p0, p1, T);
-        float2 bc = f2lerp(p1, p2, T);
-        float2 cd = f2lerp(p2, p3, T);
-        float2 abc = f2lerp(ab, bc, T);
-        float2 bcd = f2lerp(bc, cd, T);
-        coord = f2lerp(abc, bcd, T);
+        float2 abc, bcd;
+        coord = eval_cubic_mix(p0, p1, p2, p3, T, abc, bcd);
         if (T != polarT)
             theta = rive_atan2(f2sub(bcd, abc));
     }
@@ -611,6 +629,78 @@ __global__ void __launch_bounds__(256) tessellate_feather_kernel(BatchTables B)
 {
     tessellate<true>(B);
 }
+// The tessellation pass's device functions on n items, for the parity tests
+// (the layouts of oracle_cubic_eval and oracle_math_eval): fn 0..5 the cubic
+// functions, 10..13 sin, cos, acos and the cube root.
+__global__ void __launch_bounds__(128) tess_math_kernel(int fn, const float* __restrict__ in,
+                                                        float* __restrict__ out, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    constexpr int kIn[6] = {2, 8, 10, 9, 12, 8}, kOut[6] = {1, 2, 1, 2, 1, 4};
+    if (fn >= 10)
+    {
+        const float v = in[i];
+        out[i] = fn == 10 ? rc_sinf(v) : fn == 11 ? rc_cosf(v) : fn == 12 ? rc_acosf(v)
+                                                                         : rc_cbrtf(v);
+        return;
+    }
+    const float* x = in + (size_t)i * kIn[fn];
+    float* y = out + (size_t)i * kOut[fn];
+    const float2 p0 = make_float2(x[0], x[1]), p1 = make_float2(x[2], x[3]);
+    const float2 p2 = make_float2(x[4], x[5]), p3 = make_float2(x[6], x[7]);
+    switch (fn)
+    {
+        case 0: y[0] = clamped_divide(x[0], x[1]); break;
+        case 1: y[0] = cubic_max_height(p0, p1, p2, p3, y[1]); break;
+        case 2: y[0] = cubic_local_curvature(p0, p1, p2, p3, x[8], x[9]); break;
+        case 3:
+        {
+            float2 abc, bcd;
+            const float2 q = eval_cubic_mix(p0, p1, p2, p3, x[8], abc, bcd);
+            y[0] = q.x;
+            y[1] = q.y;
+            break;
+        }
+        case 4: y[0] = wang_cubic_segments(p0, p1, p2, p3, make_float4(x[8], x[9], x[10], x[11])); break;
+        default:
+        {
+            float2 t0, t1;
+            cubic_tangents(p0, p1, p2, p3, t0, t1);
+            y[0] = t0.x;
+            y[1] = t0.y;
+            y[2] = t1.x;
+            y[3] = t1.y;
+            break;
+        }
+    }
+}
+
+cudaError_t run_tess_math(int fn, const float* in, float* out, size_t n)
+{
+    static const int kIn[6] = {2, 8, 10, 9, 12, 8}, kOut[6] = {1, 2, 1, 2, 1, 4};
+    if (n == 0)
+        return cudaSuccess;
+    const size_t inN = n * (fn >= 10 ? 1 : kIn[fn]), outN = n * (fn >= 10 ? 1 : kOut[fn]);
+    float *dIn = nullptr, *dOut = nullptr;
+    cudaError_t e = cudaMalloc(&dIn, inN * 4);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&dOut, outN * 4);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(dIn, in, inN * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+    {
+        tess_math_kernel<<<(unsigned)((n + 127) / 128), 128>>>(fn, dIn, dOut, (uint32_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, dOut, outN * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dIn);
+    cudaFree(dOut);
+    return e;
+}
+
 cudaError_t upload_inverse_feather_lut(const float table[kGaussianTableSize])
 {
     return cudaMemcpyToSymbol(g_inverseFeatherLUT, table, sizeof(float) * kGaussianTableSize);

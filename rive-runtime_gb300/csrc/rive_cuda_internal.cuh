@@ -97,6 +97,9 @@ constexpr float kFeatherJoinHelperVertexCount = 3.f;
 // The inverse feather table for tessellation softening (kernels_tess.cu).
 cudaError_t upload_inverse_feather_lut(const float table[kGaussianTableSize]);
 void build_inverse_feather_table(float out[kGaussianTableSize]);
+// The tessellation pass's device functions on n host items (kernels_tess.cu;
+// rive_cuda_eval_tessellation_math).
+cudaError_t run_tess_math(int fn, const float* in, float* out, size_t n);
 // Uploads the feather table to a device once (kernels_raster.cu).
 cudaError_t ensure_feather_lut(int device);
 void feather_table_f16(uint16_t out[kGaussianTableSize]);

@@ -116,6 +116,7 @@ def load():
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
         "rive_cuda_set_winding_tiles": (i32, [vp, i32]),
+        "rive_cuda_eval_tessellation_math": (i32, [i32, vp, vp, sz]),
         "rive_cuda_get_winding_tiles": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_feather_table": (i32, [vp]),
         "rive_cuda_inverse_feather_table": (i32, [vp]),
@@ -175,6 +176,23 @@ def flush_device_noalloc(flush, bufs: DeviceBuffers, target_ptr: int, stream=Non
     del keep
     if rc != OK:
         raise RiveCudaError(f"flush_device_noalloc: status {rc}: {err.value.decode()}")
+
+
+TESS_MATH_LAYOUT = {0: (2, 1), 1: (8, 2), 2: (10, 1), 3: (9, 2), 4: (12, 1), 5: (8, 4),
+                    10: (1, 1), 11: (1, 1), 12: (1, 1), 13: (1, 1)}
+
+
+def eval_tessellation_math(fn, items):
+    """rive_cuda_eval_tessellation_math: the tessellation kernel's device
+    function `fn` on an (n, k_in) float32 array; returns (n, k_out)."""
+    k_in, k_out = TESS_MATH_LAYOUT[fn]
+    x = np.ascontiguousarray(items, np.float32).reshape(-1, k_in)
+    out = np.zeros((len(x), k_out), np.float32)
+    rc = load().rive_cuda_eval_tessellation_math(fn, x.ctypes.data_as(ctypes.c_void_p),
+                                                 out.ctypes.data_as(ctypes.c_void_p), len(x))
+    if rc != OK:
+        raise RiveCudaError(f"eval_tessellation_math({fn}): status {rc}")
+    return out
 
 
 class Graph:
