@@ -218,12 +218,16 @@ static inline uint32_t f2u(float f)
     memcpy(&u, &f, 4);
     return u;
 }
+/* GLSL clamp as GPUs evaluate it, min(max(x, lo), hi) with IEEE minNum and
+ * maxNum: a NaN x gives lo (the kernels' fminf(fmaxf(x, lo), hi)). */
 static inline float clampf(float x, float lo, float hi)
 {
-    return x < lo ? lo : (x > hi ? hi : x);
+    return fminf(fmaxf(x, lo), hi);
 }
-static inline float minf(float a, float b) { return a < b ? a : b; }
-static inline float maxf(float a, float b) { return a > b ? a : b; }
+/* min and max as the kernels take them (IEEE minNum/maxNum: a NaN operand
+ * yields the other one). */
+static inline float minf(float a, float b) { return fminf(a, b); }
+static inline float maxf(float a, float b) { return fmaxf(a, b); }
 static inline float signf(float x)
 {
     return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);
@@ -803,6 +807,7 @@ int oracle_tessellate(const rive_cuda_flush_desc* d,
                       const oracle_buffers* b,
                       uint32_t* tess)
 {
+    build_feather_table(); /* feathered fills soften through the inverse table */
     const uint32_t H = d->tess_data_height;
     memset(tess, 0, (size_t)TESS_TEXTURE_WIDTH * H * 16);
     if ((size_t)(d->first_tess_span + d->tess_span_count) * 64 >
@@ -853,6 +858,7 @@ int oracle_tessellate_f64(const rive_cuda_flush_desc* d,
                           double* xy,
                           uint32_t* tess_flags)
 {
+    build_feather_table(); /* feathered fills soften through the inverse table */
     const uint32_t H = d->tess_data_height;
     const size_t N = (size_t)TESS_TEXTURE_WIDTH * H;
     memset(xy, 0, N * 2 * sizeof(double));
