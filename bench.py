@@ -358,6 +358,8 @@ def run_ours(args, cap, wname, rank, world):
         line["serving_recorded"] = run_serving_recorded(args, dev, raster)
     if args.feather_steps > 0 and world == 1:
         line["feathered"] = run_feathered(args, dev)
+    if args.stress_canvases > 0 and world == 1:
+        line["stroke_stress"] = run_stress(args, dev, raster)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         dt = cpu_baseline(cap, threads)
@@ -435,6 +437,7 @@ def run_serving(args, dev, raster=None):
     ctx = rive_cuda.Context(dev)
     if raster:
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+        ctx.set_winding_tiles(raster.get("winding", False))
     try:
         server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
@@ -455,11 +458,16 @@ def raster_setup(args, ctx, run, stream):
     if args.raster_config == "auto":
         from rive_runtime_gb300 import autotune
         best, trials = autotune.autotune(ctx, run, stream=stream, warmup=1, iters=3)
-        return {"tile": best.tile_size, "ctas_per_sm": best.ctas_per_sm, "autotuned": True,
-                "trial_ms": {f"{t.tile_size},{t.ctas_per_sm}": round(t.ms, 3) for t in trials}}
-    t, c = (int(v) for v in args.raster_config.split(","))
+        return {"tile": best.tile_size, "ctas_per_sm": best.ctas_per_sm,
+                "winding": best.winding, "autotuned": True,
+                "trial_ms": {f"{t.tile_size},{t.ctas_per_sm},{'w' if t.winding else 'f'}":
+                             round(t.ms, 3) for t in trials}}
+    parts = args.raster_config.split(",")
+    t, c = int(parts[0]), int(parts[1])
+    w = len(parts) > 2 and parts[2] == "w"
     ctx.set_raster_config(t, c)
-    return {"tile": t, "ctas_per_sm": c, "autotuned": False}
+    ctx.set_winding_tiles(w)
+    return {"tile": t, "ctas_per_sm": c, "winding": w, "autotuned": False}
 
 
 def run_serving_recorded(args, dev, raster=None):
@@ -480,6 +488,7 @@ def run_serving_recorded(args, dev, raster=None):
     ctx = rive_cuda.Context(dev)
     if raster:
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+        ctx.set_winding_tiles(raster.get("winding", False))
     try:
         server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
@@ -517,16 +526,65 @@ def run_batched(args, dev, raster=None, recorded=False):
     rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch per
     flush index. Frames/s counts scenes; each pass renders every scene once,
     with the records resident in HBM."""
-    import numpy as np
-    import torch
-    from rive_runtime_gb300 import planner, rive_cuda, scene
-    from rive_runtime_gb300.capture import BUFFER_NAMES
+    from rive_runtime_gb300 import planner, scene
 
     if recorded:
         caps = recorded_caps(args.batch_scenes)
     else:
         caps = [planner.plan(sc.to_bytes())
                 for sc in scene.batched_scenes(count=args.batch_scenes)]
+    out = time_batch(caps, args, dev, raster)
+    out["workload"] = f"batched_{'recorded_' if recorded else ''}{len(caps)}"
+    return out
+
+
+def _stress_scene_bytes(job):
+    # One canvas of the tessellation-heavy stress (a worker of a spawned
+    # process pool: scene generation is plain Python).
+    seed, size, strokes = job
+    from conftest import load_package
+    load_package()
+    from rive_runtime_gb300 import scene
+    return scene.stroke_stress(seed=seed, width=size, height=size, n_strokes=strokes).to_bytes()
+
+
+def run_stress(args, dev, raster=None):
+    """The tessellation-heavy stress at its stated size: one 4096x4096 canvas
+    of 100,000 strokes and 64 1024x1024 canvases of 5,000 strokes each (1-16
+    cubics, 20% cusp or near-degenerate, width log-uniform in [0.5, 64] px,
+    round joins and caps, alpha 0.8), rendered together as batches: wave i
+    batches logical flush i of every canvas. A frame is all 65 canvases."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from rive_runtime_gb300 import planner
+    jobs = [(4000, 4096, args.stress_big)] + [(4001 + i, 1024, args.stress_small)
+                                               for i in range(args.stress_canvases)]
+    sys.path.insert(0, os.path.join(REPO, "tests"))
+    # Spawned workers (never forked from a process that has used the GPU).
+    with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
+                                mp_context=mp.get_context("spawn")) as ex:
+        scenes = list(ex.map(_stress_scene_bytes, jobs))
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        caps = list(ex.map(planner.plan, scenes))
+    out = time_batch(caps, args, dev, raster, modes=("batch", "graph"))
+    verts = sum(int(f.batches[:, 1].sum()) * 8 for c in caps for f in c.flushes
+                if len(f.batches))
+    out["workload"] = (f"stroke_stress: 1 x 4096^2 with {args.stress_big} strokes + "
+                       f"{args.stress_canvases} x 1024^2 with {args.stress_small} strokes")
+    out["tess_vertices_per_frame"] = verts
+    out["graph_tess_vertices_per_s"] = verts * out["graph_frames_per_s"] / len(caps)
+    return out
+
+
+def time_batch(caps, args, dev, raster=None, modes=("plain", "batch", "graph")):
+    """Times rendering every capture once, with the records resident in HBM:
+    one flush at a time, as one rive_cuda_flush_batch per wave of logical
+    flushes, and as one CUDA graph per wave; frames/s counts captures."""
+    import numpy as np
+    import torch
+    from rive_runtime_gb300 import rive_cuda
+    from rive_runtime_gb300.capture import BUFFER_NAMES
+
     stream = torch.cuda.current_stream()
     keep, bufs, targets = [], [], []
     for cap in caps:
@@ -559,35 +617,39 @@ def run_batched(args, dev, raster=None, recorded=False):
         c = rive_cuda.Context(dev)
         if raster:
             c.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+            c.set_winding_tiles(raster.get("winding", False))
         return c
 
-    ctx = configured()
-    ms_plain = timed(lambda: [ctx.flush_device(f, b, tp, stream.cuda_stream)
-                              for w in waves for (f, b, tp) in w])
-    ms_batch = timed(lambda: [ctx.flush_batch(w, stream.cuda_stream) for w in waves])
-    ctx.sync(stream.cuda_stream)
-    entries = ctx.stats()["bin_entries"]
-    ctx.close()
-    ctx = configured()
-    graphs = [ctx.graph(w) for w in waves]
-    ms_graph = timed(lambda: [g.launch(stream.cuda_stream) for g in graphs])
-    for g in graphs:
-        g.check(stream.cuda_stream)
-        g.close()
-    ctx.close()
     n = len(caps)
     px = sum(c.width * c.height for c in caps)
-    return {"workload": f"batched_{'recorded_' if recorded else ''}{n}", "scenes": n,
-            "mpx": px / 1e6,
-            "paths": int(sum(f.desc["path_count"] for c in caps for f in c.flushes)),
-            "flushes": int(sum(len(c.flushes) for c in caps)),
-            "bin_entries_last_wave": int(entries),
-            "plain_frames_per_s": n * 1e3 / ms_plain,
-            "batch_frames_per_s": n * 1e3 / ms_batch,
-            "graph_frames_per_s": n * 1e3 / ms_graph,
-            "graph_gpx_per_s": px / (ms_graph * 1e6),
-            "speedup_vs_plain": ms_plain / ms_graph,
-            "steps": steps}
+    out = {"scenes": n, "mpx": px / 1e6,
+           "paths": int(sum(f.desc["path_count"] for c in caps for f in c.flushes)),
+           "flushes": int(sum(len(c.flushes) for c in caps)), "waves": len(waves),
+           "steps": steps}
+    ctx = configured()
+    if "plain" in modes:
+        ms_plain = timed(lambda: [ctx.flush_device(f, b, tp, stream.cuda_stream)
+                                  for w in waves for (f, b, tp) in w])
+        out["plain_frames_per_s"] = n * 1e3 / ms_plain
+    if "batch" in modes:
+        ms_batch = timed(lambda: [ctx.flush_batch(w, stream.cuda_stream) for w in waves])
+        ctx.sync(stream.cuda_stream)
+        out["bin_entries_last_wave"] = int(ctx.stats()["bin_entries"])
+        out["batch_frames_per_s"] = n * 1e3 / ms_batch
+    ctx.close()
+    if "graph" in modes:
+        ctx = configured()
+        graphs = [ctx.graph(w) for w in waves]
+        ms_graph = timed(lambda: [g.launch(stream.cuda_stream) for g in graphs])
+        for g in graphs:
+            g.check(stream.cuda_stream)
+            g.close()
+        ctx.close()
+        out["graph_frames_per_s"] = n * 1e3 / ms_graph
+        out["graph_gpx_per_s"] = px / (ms_graph * 1e6)
+        if "plain" in modes:
+            out["speedup_vs_plain"] = ms_plain / ms_graph
+    return out
 
 
 def main():
@@ -614,8 +676,14 @@ def main():
     ap.add_argument("--serve-rec-fps", type=float, default=30.0)
     ap.add_argument("--feather-steps", type=int, default=200,
                     help="frames of the recorded feathered-frame measurement (0 skips it)")
+    ap.add_argument("--stress-canvases", type=int, default=64,
+                    help="1024x1024 canvases of the stroke stress beside its 4096x4096 one "
+                         "(0 skips the stress measurement)")
+    ap.add_argument("--stress-small", type=int, default=5000)
+    ap.add_argument("--stress-big", type=int, default=100000)
     ap.add_argument("--raster-config", default="auto",
-                    help='"auto" (autotuned on the workload) or "tile,ctas_per_sm", e.g. "16,0"')
+                    help='"auto" (autotuned on the workload) or "tile,ctas_per_sm[,w]", e.g. '
+                         '"16,0" (",w": interior tiles as winding records)')
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

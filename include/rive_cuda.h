@@ -413,14 +413,17 @@ int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_
 int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, int* ctas_per_sm);
 
 /*
- * Interior tiles as winding records (no counterpart in the reference; on by
- * default). Inside a fill, every midpoint-fan triangle has coverage +1 or -1,
- * so on a tile that no contour edge, AA ramp or contour midpoint comes within
- * 2 px of, the path's coverage count is the same integer at every pixel: the
- * winding number of the fan's boundary. With this on, such tiles get one
- * winding entry per path instead of every fan triangle that crosses them
- * (fills that are not nested clip updates, in batches without feathers). The
- * image is bit-identical either way; off is the plain fan, for comparison.
+ * Interior tiles as winding records (no counterpart in the reference; off by
+ * default, an autotuner knob). Inside a fill, every midpoint-fan triangle has
+ * coverage +1 or -1, so on a tile that no contour edge, AA ramp or contour
+ * midpoint comes within 2 px of, the path's coverage count is the same
+ * integer at every pixel: the winding number of the fan's boundary. With this
+ * on, such tiles get one winding entry per path instead of every fan
+ * triangle that crosses them (fills that are not nested clip updates, whose
+ * contour is short enough for their box to have interior tiles, in batches
+ * without feathers). It pays on large filled shapes; on scribbles and small
+ * flushes its extra passes cost more than they save. The image is
+ * bit-identical either way.
  */
 int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled);
 int rive_cuda_get_winding_tiles(const rive_cuda_context* ctx, int* enabled);

@@ -1,12 +1,19 @@
 """Raster autotuner for a rive_cuda context.
 
-The raster's speed depends on the workload's shape: small tiles cut the
+The flush's speed depends on the workload's shape: small tiles cut the
 triangles each tile walks but raise the bin entries and the per-tile fixed
-cost; more resident CTAs per SM hide latency but share the SM's issue slots
-and L1. Every configuration gives the same image within the parity tolerance,
-so the choice is free: this module times each candidate on the caller's own
-work with CUDA events on the caller's stream and leaves the fastest set on the
-context.
+cost; more resident raster CTAs per SM hide latency but share the SM's issue
+slots and L1; interior tiles as winding records pay on large filled shapes
+and cost extra passes elsewhere. Every configuration gives the same image (bit
+for bit for the winding records, within the parity tolerance across tile
+sizes), so the choice is free: this module times each candidate on the
+caller's own work with CUDA events on the caller's stream and leaves the
+fastest set on the context.
+
+The search space is tile size {8, 16, 32} x resident raster CTAs per SM
+{1, 2, 4, as many as fit} x winding records {off, on}; 32-pixel tiles run one
+1,024-thread CTA per SM at most, so only their "as many as fit" entry
+differs.
 """
 from __future__ import annotations
 
@@ -14,20 +21,40 @@ from dataclasses import dataclass
 
 import torch
 
-# (tile size in pixels, resident raster CTAs per SM; 0 = as many as fit)
-CANDIDATES = ((16, 0), (16, 4), (16, 3), (8, 0), (32, 0))
+TILES = (8, 16, 32)
+CTAS_PER_SM = (1, 2, 4, 0)  # 0 = as many as fit
+WINDING = (False, True)
+
+
+def _candidates():
+    out = []
+    for w in WINDING:
+        for t in TILES:
+            for c in (CTAS_PER_SM if t != 32 else (0,)):
+                out.append((t, c, w))
+    return tuple(out)
+
+
+# (tile size in pixels, resident raster CTAs per SM or 0, winding records)
+CANDIDATES = _candidates()
 
 
 @dataclass
 class Trial:
     tile_size: int
     ctas_per_sm: int
+    winding: bool
     ms: float
 
 
-def time_config(ctx, run, tile_size, ctas_per_sm, stream, warmup=2, iters=5):
-    """Mean device milliseconds of `run(stream)` under one raster config."""
+def apply(ctx, tile_size, ctas_per_sm, winding):
     ctx.set_raster_config(tile_size, ctas_per_sm)
+    ctx.set_winding_tiles(winding)
+
+
+def time_config(ctx, run, tile_size, ctas_per_sm, winding, stream, warmup=2, iters=5):
+    """Mean device milliseconds of `run(stream)` under one configuration."""
+    apply(ctx, tile_size, ctas_per_sm, winding)
     with torch.cuda.stream(stream):
         for _ in range(warmup):
             run(stream)
@@ -44,15 +71,19 @@ def time_config(ctx, run, tile_size, ctas_per_sm, stream, warmup=2, iters=5):
 
 def autotune(ctx, run, candidates=CANDIDATES, stream=None, warmup=2, iters=5):
     """Times `run(stream)` (one frame or one batch, enqueued on `stream`) under
-    each candidate and leaves the fastest configured on `ctx`.
+    each candidate (tile size, CTAs per SM, winding records) and leaves the
+    fastest configured on `ctx`.
 
     Returns (best Trial, all Trials). `run` must enqueue the same work each
     call; a CUDA graph built before the call keeps the configuration it was
     built with, so pass a `run` that builds nothing or rebuilds its graph.
     """
     stream = stream or torch.cuda.current_stream()
-    trials = [Trial(t, c, time_config(ctx, run, t, c, stream, warmup, iters))
-              for t, c in candidates]
+    trials = []
+    for cand in candidates:
+        t, c = cand[0], cand[1]
+        w = cand[2] if len(cand) > 2 else False
+        trials.append(Trial(t, c, w, time_config(ctx, run, t, c, w, stream, warmup, iters)))
     best = min(trials, key=lambda r: r.ms)
-    ctx.set_raster_config(best.tile_size, best.ctas_per_sm)
+    apply(ctx, best.tile_size, best.ctas_per_sm, best.winding)
     return best, trials

@@ -48,6 +48,10 @@ __global__ void patch_setup_feather_kernel(BatchTables B,
                                            TriRecord* tris,
                                            uint32_t* tileCounts,
                                            uint8_t* tileMasks);
+__global__ void patch_setup_winding_kernel(BatchTables B,
+                                           TriRecord* tris,
+                                           uint32_t* tileCounts,
+                                           uint8_t* tileMasks);
 __global__ void center_setup_kernel(BatchTables B,
                                     TriRecord* tris,
                                     uint32_t* tileCounts,
@@ -202,7 +206,7 @@ struct rive_cuda_context
     uint32_t* hPairs = nullptr;  // pinned: scanned pair total
     // Interior tiles as winding records (rive_cuda_set_winding_tiles): per-path
     // grids and the cell pool, grown when a flush asked for more cells.
-    bool windingTiles = true;
+    bool windingTiles = false;
     DeviceBuffer pathGrids, gridWinding, gridEdge, gridCounters;
     uint32_t gridCapacity = 0;
     uint32_t* hGridCounters = nullptr; // pinned: cells asked, winding entries
@@ -770,8 +774,10 @@ int enqueue_front(rive_cuda_context* ctx,
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_PATCH_SETUP, stream);
         if (L.items[0])
-            (L.feather ? patch_setup_feather_kernel : patch_setup_kernel)<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
-                                                                         S.masks);
+            (L.feather   ? patch_setup_feather_kernel
+             : L.winding ? patch_setup_winding_kernel
+                         : patch_setup_kernel)<<<(L.items[0] + 3) / 4, 128, 0, stream>>>(
+                B, S.tris, S.counts, S.masks);
         if (L.items[1])
             outer_setup_kernel<<<(L.items[1] + 3) / 4, 128, 0, stream>>>(B, S.tris, S.counts,
                                                                          S.masks);

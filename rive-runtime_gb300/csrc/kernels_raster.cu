@@ -1105,7 +1105,7 @@ __device__ void mark_edge_tiles(float2 a, float2 b, const PathGrid& G, uint8_t* 
 // patch (interior triangulation), 3 the center-AA midpoint fan (feathered
 // fills). Triangle slot order is primitive order (flush, draw batch,
 // instance, triangle-in-patch).
-template <int kList, bool kFeather>
+template <int kList, bool kFeather, bool kWinding = false>
 __device__ __forceinline__ void patch_setup(const BatchTables& B,
                                             TriRecord* __restrict__ tris,
                                             uint32_t* __restrict__ tileCounts,
@@ -1161,7 +1161,7 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     const uint32_t stride = (kList == 0 && B.fanSlotStride) ? B.fanSlotStride : (uint32_t)kTris;
     const uint32_t slot0 = S.slotBase + local * stride;
     PathGrid* wg = nullptr; // the path's winding grid, when this patch feeds it
-    if (kList == 0 && !kFeather && B.grids)
+    if (kWinding && kList == 0 && !kFeather && B.grids)
     {
         if (lane == 0)
         {
@@ -1246,7 +1246,7 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
                 patch_triangle(t, ia, ib, ic);
             // Fan triangles (16..23) of a path with a winding grid: their
             // tiles are counted once the grid knows its edge tiles.
-            const bool fan = kList == 0 && wg && t >= 16;
+            const bool fan = kWinding && kList == 0 && wg && t >= 16;
             TriRecord T;
             if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic],
                                          S.features | (fan ? FEATURE_FAN_DEFERRED : 0u), S.scene,
@@ -1283,6 +1283,16 @@ __global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
                                                           uint8_t* __restrict__ tileMasks)
 {
     patch_setup<0, false>(B, tris, tileCounts, tileMasks);
+}
+
+// Midpoint-fan set-up for batches that draw interior tiles as winding records
+// (its own kernel, so the plain one keeps its register budget).
+__global__ void __launch_bounds__(128) patch_setup_winding_kernel(BatchTables B,
+                                                                  TriRecord* __restrict__ tris,
+                                                                  uint32_t* __restrict__ tileCounts,
+                                                                  uint8_t* __restrict__ tileMasks)
+{
+    patch_setup<0, false, true>(B, tris, tileCounts, tileMasks);
 }
 
 // Midpoint-fan set-up with the feather paths, for batches that feather.

@@ -10,7 +10,7 @@ import oracle
 
 load_package()
 
-CONFIGS = [(8, 0), (16, 2), (16, 4), (32, 0)]
+CONFIGS = [(8, 0), (8, 1), (16, 1), (16, 2), (16, 4), (32, 0)]
 
 
 @pytest.fixture(scope="module")
@@ -107,8 +107,12 @@ def test_autotune_leaves_a_candidate_set(ctx):
     try:
         best, trials = autotune.autotune(ctx, run, stream=stream, warmup=1, iters=2)
         assert len(trials) == len(autotune.CANDIDATES)
+        assert {(t.tile_size, t.ctas_per_sm) for t in trials} >= {
+            (t, c) for t in (8, 16) for c in (1, 2, 4)}
         assert all(t.ms > 0 for t in trials)
         assert ctx.raster_config() == (best.tile_size, best.ctas_per_sm)
+        assert ctx.winding_tiles() == best.winding
         assert best.ms == min(t.ms for t in trials)
     finally:
         ctx.set_raster_config(16, 0)
+        ctx.set_winding_tiles(False)
