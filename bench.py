@@ -52,7 +52,7 @@ def build_workload(args):
     if args.capture:
         with open(args.capture, "rb") as f:
             return capture.parse(f.read()), f"capture:{os.path.basename(args.capture)}"
-    from rive_runtime_gb300 import planner
+    from inputgen import planner
     if args.workload == "full_feature":
         sc = scene.full_feature(seed=2)
     elif args.workload == "full_feature_1024":
@@ -439,7 +439,7 @@ def run_serving(args, dev, raster=None):
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
         ctx.set_winding_tiles(raster.get("winding", False))
     try:
-        server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
+        server = serving.FrameServer(ctx, planner.plan, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
         st = server.run(sessions, timeout_s=600.0)
     finally:
@@ -490,7 +490,7 @@ def run_serving_recorded(args, dev, raster=None):
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
         ctx.set_winding_tiles(raster.get("winding", False))
     try:
-        server = serving.FrameServer(ctx, device=dev, hbm_budget_bytes=120 << 30,
+        server = serving.FrameServer(ctx, planner.plan, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
         st = server.run(sessions, timeout_s=600.0)
     finally:
@@ -506,7 +506,8 @@ def recorded_caps(count):
     """`count` frames of the recorded .riv animations (tests/golden/anim),
     taken in turn from each animation, planned."""
     import glob
-    from rive_runtime_gb300 import planner, sriv
+    from inputgen import planner
+    from rive_runtime_gb300 import sriv
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "anim")
     anims = []
     for path in sorted(glob.glob(os.path.join(here, "*.rsa"))):
@@ -526,7 +527,8 @@ def run_batched(args, dev, raster=None, recorded=False):
     rive_cuda_flush_batch per flush index, (c) as one CUDA graph launch per
     flush index. Frames/s counts scenes; each pass renders every scene once,
     with the records resident in HBM."""
-    from rive_runtime_gb300 import planner, scene
+    from inputgen import planner
+    from rive_runtime_gb300 import scene
 
     if recorded:
         caps = recorded_caps(args.batch_scenes)
@@ -556,7 +558,7 @@ def run_stress(args, dev, raster=None):
     batches logical flush i of every canvas. A frame is all 65 canvases."""
     import concurrent.futures as cf
     import multiprocessing as mp
-    from rive_runtime_gb300 import planner
+    from inputgen import planner
     jobs = [(4000, 4096, args.stress_big)] + [(4001 + i, 1024, args.stress_small)
                                                for i in range(args.stress_canvases)]
     sys.path.insert(0, os.path.join(REPO, "tests"))

@@ -18,7 +18,9 @@ REPO = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "_build", "liboracle_passes.so")
 REF_CAPTURE = os.path.join(HERE, "_ref", "ref_capture")
 ADAPTER_CAPTURE = os.path.join(HERE, "_ref", "adapter_capture")
-REFERENCE_SOURCES = "/root/reference"
+# The reference sources, where they exist (this build machine only):
+# RIVE_REFERENCE_DIR, or the default checkout location.
+REFERENCE_SOURCES = os.environ.get("RIVE_REFERENCE_DIR", "/root/reference")
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
                 "grad_spans", "tess_spans", "triangles")
@@ -191,8 +193,12 @@ def reference_available():
     return os.path.isdir(REFERENCE_SOURCES)
 
 
+def _make_env():
+    return dict(os.environ, REF=REFERENCE_SOURCES)
+
+
 def build_reference():
-    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"])
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "ref"], env=_make_env())
 
 
 CMDBUF_CAPTURE = os.path.join(HERE, "_ref", "cmdbuf_capture")
@@ -201,7 +207,7 @@ CMDBUF_CAPTURE = os.path.join(HERE, "_ref", "cmdbuf_capture")
 def build_cmdbuf_tool() -> str:
     """Builds (if needed) the reference's deferred command recorder/replayer
     tool (oracle/capture/cmdbuf_capture.cpp); returns its path."""
-    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "cmdbuf"])
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "cmdbuf"], env=_make_env())
     return CMDBUF_CAPTURE
 
 
@@ -250,5 +256,5 @@ def reference_capture(scene_bytes: bytes) -> bytes:
 def adapter_capture(scene_bytes: bytes) -> bytes:
     """Runs the reference front end into the product's RenderContextCUDAImpl
     over the recording C ABI; returns what reached the ABI as a capture."""
-    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "adapter"])
+    subprocess.check_call(["make", "-s", "-j8", "-C", HERE, "adapter"], env=_make_env())
     return _run_capture(ADAPTER_CAPTURE, scene_bytes)

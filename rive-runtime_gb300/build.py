@@ -15,9 +15,6 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "librive_cuda.so")
-PLANNER_LIB = os.path.join(OUT, "librive_planner.so")
-PLANNER_SOURCES = [os.path.join(CSRC, "planner", "planner.cpp")]
-CXX = os.environ.get("CXX", "g++")
 SOURCES = ["context.cu", "kernels_tess.cu", "kernels_raster.cu", "flush_noalloc.cu"]
 HEADERS = ["rive_cuda_internal.cuh", "rive_fp32_math.h"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
@@ -35,26 +32,8 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build_planner(verbose=False):
-    """The host front end: plain C++17, no CUDA. -ffp-contract=off keeps its
-    float arithmetic identical across x86-64 and aarch64."""
-    os.makedirs(OUT, exist_ok=True)
-    deps = PLANNER_SOURCES + [os.path.join(REPO, "include", h)
-                              for h in ("rive_planner.h", "rive_scene.h", "rive_cuda.h")]
-    if _stale(PLANNER_LIB, deps):
-        cmd = [CXX, "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
-               "-I" + os.path.join(REPO, "include"), *PLANNER_SOURCES, "-o", PLANNER_LIB]
-        res = subprocess.run(cmd, capture_output=True, text=True)
-        if verbose or res.returncode:
-            sys.stderr.write(res.stdout + res.stderr)
-        if res.returncode:
-            raise RuntimeError("planner build failed")
-    return PLANNER_LIB
-
-
 def build(verbose=False, extra_flags=()):
     os.makedirs(OUT, exist_ok=True)
-    build_planner(verbose)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(REPO, "include", "rive_cuda.h")]
     objs = []
     jobs = []

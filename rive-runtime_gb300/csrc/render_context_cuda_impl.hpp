@@ -16,13 +16,15 @@
 //   ctx->flush({.renderTarget = target.get()});
 //   target->readPixels(rgba);   // or target->devicePixels() for zero-copy
 //
-// Supported: InterlockMode::rasterOrdering with midpoint-fan patches and,
-// for large fills the front end triangulates, outer-curve patches plus
-// interior triangles; i.e. fills (nonzero, even-odd), strokes with every join
-// and cap, linear and radial gradients, clip paths (nested), clip rects, all
-// blend modes, dither. A flush that needs anything else (feathers, images,
-// atomic/MSAA/clockwise modes) is not rendered: flush() records
-// RIVE_CUDA_ERR_UNSUPPORTED in lastStatus().
+// Supported: InterlockMode::rasterOrdering with midpoint-fan patches, the
+// center-AA midpoint fans of feathered fills and, for large fills the front
+// end triangulates, outer-curve patches plus interior triangles; i.e. fills
+// (nonzero, even-odd, clockwise), strokes with every join and cap, feathers
+// below the feather atlas's 32-pixel threshold (fills and strokes), linear and
+// radial gradients, clip paths (nested), clip rects, all blend modes, dither.
+// A flush that needs anything else (the feather atlas for larger feathers,
+// images, atomic/MSAA/clockwise interlock modes) is not rendered: flush()
+// records RIVE_CUDA_ERR_UNSUPPORTED in lastStatus().
 #pragma once
 
 // texture.hpp first: render_context_impl.hpp destroys rcp<Texture> inline.

@@ -7,8 +7,11 @@ animated on the host:
 every transform rotates at its own angular rate and every control point of a
 path moves by amplitude * sin(2 pi f t + phi) along a per-path direction. A
 session asks for frames at a fixed rate from its arrival on (frame k is due
-at arrival + k / fps). For each frame the host re-plans the recording with the
-C++ front end (planner.plan), and the frame joins the next batch.
+at arrival + k / fps). For each frame the host turns the session's frame
+recording into flush records with the front end the caller supplies (in a
+deployment, rive-runtime's own RiveRenderer -> RenderContext through
+RenderContextCUDAImpl; in the benchmark and the tests, a stand-in), and the
+frame joins the next batch.
 
 Continuous batching: each batch takes every frame that is due (one per
 session at most, up to max_batch), so sessions join and leave the batch
@@ -35,7 +38,6 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import planner
 from .capture import BUFFER_NAMES
 from .scene import CMD_TRANSFORM, MAGIC, Scene
 
@@ -191,12 +193,17 @@ class RecordArenas:
 
 
 class FrameServer:
-    """Continuous-batching frame server on one rive_cuda context."""
+    """Continuous-batching frame server on one rive_cuda context.
 
-    def __init__(self, ctx, device: int = 0, hbm_budget_bytes: int = 120 << 30,
+    `front_end(frame_bytes) -> capture.Capture` turns one frame recording of a
+    session into its flush records; it runs on `planner_threads` host threads
+    (it must release the GIL to overlap)."""
+
+    def __init__(self, ctx, front_end, device: int = 0, hbm_budget_bytes: int = 120 << 30,
                  max_batch: int = 256, planner_threads: int = 8, keep_frames=()):
         import torch
         self.torch = torch
+        self.front_end = front_end
         self.ctx = ctx
         self.device = device
         self.budget = hbm_budget_bytes
@@ -226,7 +233,7 @@ class FrameServer:
                    + slots * 4 * 16)
 
     def _plan(self, s: Session, k: int):
-        return planner.plan(s.anim.frame(k / s.fps))
+        return self.front_end(s.anim.frame(k / s.fps))
 
     def _admit(self, now):
         still = []
@@ -370,12 +377,12 @@ def recorded_sessions(animations, count: int, rate_per_s: float, frames: int,
     return out
 
 
-def render_alone(ctx, s: Session, k: int, stream=None):
+def render_alone(ctx, front_end, s: Session, k: int, stream=None):
     """Frame k of session s rendered by itself (one flush at a time), for the
     alone-versus-in-the-mix check."""
     import torch
     from .rive_cuda import DeviceBuffers
-    cap = planner.plan(s.anim.frame(k / s.fps))
+    cap = front_end(s.anim.frame(k / s.fps))
     keep = []
     b = DeviceBuffers()
     for name in BUFFER_NAMES:

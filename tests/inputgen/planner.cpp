@@ -1,11 +1,20 @@
-// Host front end: rive_scene.h recording -> flush records (see
-// include/rive_planner.h). A restatement, in this project's own code, of the
-// CPU half of rive-runtime's gpu::RenderContext flush for rasterOrdering with
-// midpoint-fan tessellation. Floating-point expressions keep the reference's
-// operation order so results are bit-identical when both are built without
-// FMA contraction (-ffp-contract=off).
+// TEST AND BENCH INFRASTRUCTURE -- not part of the product. A stand-in for
+// rive-runtime's own CPU front end (RiveRenderer -> RenderContext), used to
+// produce flush records from rive_scene.h recordings on machines where the
+// reference sources cannot be built (the GPU machines the benchmark and the
+// GPU tests run on). In a deployment the reference's front end produces the
+// records and hands them to RenderContextCUDAImpl; where the reference is
+// compiled (oracle/_ref), the goldens come from it and this stand-in is tested
+// byte for byte against it (tests/test_planner.py, tests/test_sriv.py).
+//
+// It follows the reference's algorithms (Wang's formula, chops, polar counts,
+// span layout, gradient allocation, logical-flush limits) step by step,
+// because its output must be byte-identical to the reference's: for
+// rasterOrdering with midpoint-fan tessellation. Floating-point expressions
+// keep the reference's operation order so results are bit-identical when both
+// are built without FMA contraction (-ffp-contract=off).
 #include "rive_cuda.h"
-#include "rive_planner.h"
+#include "rive_planner.h" // this directory
 #include "rive_scene.h"
 
 #include <algorithm>

@@ -1,6 +1,7 @@
 /*
- * rive_planner.h -- host-side front end that turns a rive_scene.h recording
- * into the records a RenderContextImpl receives for one frame.
+ * rive_planner.h -- TEST AND BENCH INFRASTRUCTURE (not part of the product):
+ * a host-side stand-in for the reference front end that turns a rive_scene.h
+ * recording into the records a RenderContextImpl receives for one frame.
  *
  * It restates, for InterlockMode::rasterOrdering with midpoint-fan
  * tessellation (no feathers, images or interior triangulation), the CPU work

@@ -26,7 +26,8 @@ from planner_compare import diff_captures
 import oracle
 
 load_package()
-from rive_runtime_gb300 import capture, cmdbuf, planner, scene  # noqa: E402
+from rive_runtime_gb300 import capture, cmdbuf, scene  # noqa: E402
+from inputgen import planner  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SESSIONS = os.path.join(HERE, "golden", "cmdbuf")

@@ -21,7 +21,8 @@ load_package()
 
 @pytest.fixture(scope="module")
 def frame():
-    from rive_runtime_gb300 import planner, scene
+    from rive_runtime_gb300 import scene
+    from inputgen import planner
     cap = planner.plan(scene.full_feature(seed=2).to_bytes())
     assert (cap.width, cap.height) == (2048, 2048)
     assert len(cap.flushes) == 4

@@ -54,7 +54,8 @@ def test_winding_tiles_match_the_fan_bit_for_bit(ctx, name, tile):
 
 @pytest.mark.gpu
 def test_full_feature_frame_winding_matches_the_fan(ctx):
-    from rive_runtime_gb300 import planner, scene
+    from rive_runtime_gb300 import scene
+    from inputgen import planner
     cap = planner.plan(scene.full_feature(seed=2).to_bytes())
     fan, sf = _render(ctx, cap, False)
     wind, sw = _render(ctx, cap, True)

@@ -11,7 +11,8 @@ from planner_compare import diff_captures
 import oracle
 
 load_package()
-from rive_runtime_gb300 import planner, scene  # noqa: E402
+from rive_runtime_gb300 import scene  # noqa: E402
+from inputgen import planner  # noqa: E402
 
 
 def _triangulated(scene_bytes):

@@ -9,7 +9,8 @@ import pytest
 from conftest import load_package
 
 load_package()
-from rive_runtime_gb300 import planner, scene, serving  # noqa: E402
+from rive_runtime_gb300 import scene, serving  # noqa: E402
+from inputgen import planner  # noqa: E402
 
 
 def _anim(seed=5):
@@ -55,14 +56,14 @@ def test_server_frames_match_frames_rendered_alone():
     keep = {(s.sid, k) for s in sessions for k in (0, 4)}
     ctx = rive_cuda.Context(0)
     try:
-        server = serving.FrameServer(ctx, keep_frames=keep, planner_threads=4)
+        server = serving.FrameServer(ctx, planner.plan, keep_frames=keep, planner_threads=4)
         stats = server.run(sessions, timeout_s=120.0)
         assert stats["frames"] == 6 * 5 and stats["sessions"] == 6
         assert stats["mean_batch"] > 1.0  # frames of several sessions shared batches
         alone_ctx = rive_cuda.Context(0)
         try:
             for (sid, k), img in server.kept.items():
-                want = serving.render_alone(alone_ctx, sessions[sid], k)
+                want = serving.render_alone(alone_ctx, planner.plan, sessions[sid], k)
                 assert np.array_equal(img, want), (sid, k)
         finally:
             alone_ctx.close()
@@ -111,13 +112,13 @@ def test_server_recorded_frames_match_frames_rendered_alone():
     keep = {(s.sid, k) for s in sessions for k in (0, 3)}
     ctx = rive_cuda.Context(0)
     try:
-        server = serving.FrameServer(ctx, keep_frames=keep, planner_threads=4)
+        server = serving.FrameServer(ctx, planner.plan, keep_frames=keep, planner_threads=4)
         stats = server.run(sessions, timeout_s=120.0)
         assert stats["frames"] == 8 * 4
         alone_ctx = rive_cuda.Context(0)
         try:
             for (sid, k), img in server.kept.items():
-                want = serving.render_alone(alone_ctx, sessions[sid], k)
+                want = serving.render_alone(alone_ctx, planner.plan, sessions[sid], k)
                 assert np.array_equal(img, want), (sid, k)
         finally:
             alone_ctx.close()

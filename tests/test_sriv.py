@@ -14,7 +14,8 @@ from planner_compare import diff_captures
 import oracle
 
 load_package()
-from rive_runtime_gb300 import capture, planner, scene, sriv  # noqa: E402
+from rive_runtime_gb300 import capture, scene, sriv  # noqa: E402
+from inputgen import planner  # noqa: E402
 
 
 class _Writer:

@@ -127,7 +127,8 @@ def test_noalloc_refuses_a_bin_overflow_after_setup():
     overlap more than 2^20 (tile, triangle) pairs: the call stops after
     set-up and leaves the target untouched."""
     import torch
-    from rive_runtime_gb300 import planner, rive_cuda
+    from rive_runtime_gb300 import rive_cuda
+    from inputgen import planner
     cap = planner.plan(_star_scene(200).to_bytes())
     assert _fits(cap) and _fans_only(cap) and len(cap.flushes) == 1
     bufs, keep = device_buffers(cap)
