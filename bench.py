@@ -47,11 +47,12 @@ def _package():
 
 
 def build_workload(args):
+    """(capture, workload name, scene recording or None)."""
     _package()
     from rive_runtime_gb300 import capture, scene
     if args.capture:
         with open(args.capture, "rb") as f:
-            return capture.parse(f.read()), f"capture:{os.path.basename(args.capture)}"
+            return capture.parse(f.read()), f"capture:{os.path.basename(args.capture)}", None
     from inputgen import planner
     if args.workload == "full_feature":
         sc = scene.full_feature(seed=2)
@@ -65,7 +66,8 @@ def build_workload(args):
         sc = scene.stroke_stress(seed=4, width=1024, height=1024, n_strokes=5000)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
-    return planner.plan(sc.to_bytes()), args.workload
+    sb = sc.to_bytes()
+    return planner.plan(sb), args.workload, sb
 
 
 def max_over_ranks(value, device):
@@ -208,7 +210,7 @@ def workload_config(cap, wname):
             **workload_counts(cap)}
 
 
-def run_ours(args, cap, wname, rank, world):
+def run_ours(args, cap, wname, rank, world, scene_bytes=None):
     import numpy as np
     import torch
     from rive_runtime_gb300 import rive_cuda
@@ -366,6 +368,22 @@ def run_ours(args, cap, wname, rank, world):
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "frames/s", "cores": threads,
                                 "kind": "port",
                                 "sample": f"1 whole frame of {wname} through the oracle"}
+        if scene_bytes is not None:
+            # The CPU front end beside the passes: RiveRenderer -> RenderContext
+            # turning the scene into flush records, single-threaded as the
+            # reference's RenderContext is. On this machine it is the stand-in
+            # (tests/inputgen), whose records equal the reference's byte for byte.
+            from inputgen import planner
+            t0 = time.perf_counter()
+            planner.plan_bytes(scene_bytes)
+            fe = time.perf_counter() - t0
+            line["cpu_baseline"]["front_end"] = {
+                "value": 1.0 / fe, "unit": "frames/s", "cores": 1,
+                "kind": "stand-in for the reference front end (records byte-identical)",
+                "ms_per_frame": fe * 1e3}
+            line["cpu_baseline"]["front_end_plus_passes"] = {
+                "value": 1.0 / (fe + dt), "unit": "frames/s",
+                "ms_per_frame": (fe + dt) * 1e3}
     if rank == 0:
         print(json.dumps(line))
 
@@ -438,6 +456,7 @@ def run_serving(args, dev, raster=None):
     if raster:
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
         ctx.set_winding_tiles(raster.get("winding", False))
+        ctx.set_raster_queue(raster.get("queue", False))
     try:
         server = serving.FrameServer(ctx, planner.plan, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
@@ -459,15 +478,16 @@ def raster_setup(args, ctx, run, stream):
         from rive_runtime_gb300 import autotune
         best, trials = autotune.autotune(ctx, run, stream=stream, warmup=1, iters=3)
         return {"tile": best.tile_size, "ctas_per_sm": best.ctas_per_sm,
-                "winding": best.winding, "autotuned": True,
-                "trial_ms": {f"{t.tile_size},{t.ctas_per_sm},{'w' if t.winding else 'f'}":
-                             round(t.ms, 3) for t in trials}}
+                "winding": best.winding, "queue": best.queue, "autotuned": True,
+                "trial_ms": {f"{t.tile_size},{t.ctas_per_sm}{',w' if t.winding else ''}"
+                             f"{',q' if t.queue else ''}": round(t.ms, 3) for t in trials}}
     parts = args.raster_config.split(",")
     t, c = int(parts[0]), int(parts[1])
-    w = len(parts) > 2 and parts[2] == "w"
+    w, q = "w" in parts[2:], "q" in parts[2:]
     ctx.set_raster_config(t, c)
     ctx.set_winding_tiles(w)
-    return {"tile": t, "ctas_per_sm": c, "winding": w, "autotuned": False}
+    ctx.set_raster_queue(q)
+    return {"tile": t, "ctas_per_sm": c, "winding": w, "queue": q, "autotuned": False}
 
 
 def run_serving_recorded(args, dev, raster=None):
@@ -489,6 +509,7 @@ def run_serving_recorded(args, dev, raster=None):
     if raster:
         ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
         ctx.set_winding_tiles(raster.get("winding", False))
+        ctx.set_raster_queue(raster.get("queue", False))
     try:
         server = serving.FrameServer(ctx, planner.plan, device=dev, hbm_budget_bytes=120 << 30,
                                      planner_threads=min(16, os.cpu_count() or 1))
@@ -620,6 +641,7 @@ def time_batch(caps, args, dev, raster=None, modes=("plain", "batch", "graph")):
         if raster:
             c.set_raster_config(raster["tile"], raster["ctas_per_sm"])
             c.set_winding_tiles(raster.get("winding", False))
+            c.set_raster_queue(raster.get("queue", False))
         return c
 
     n = len(caps)
@@ -684,8 +706,9 @@ def main():
     ap.add_argument("--stress-small", type=int, default=5000)
     ap.add_argument("--stress-big", type=int, default=100000)
     ap.add_argument("--raster-config", default="auto",
-                    help='"auto" (autotuned on the workload) or "tile,ctas_per_sm[,w]", e.g. '
-                         '"16,0" (",w": interior tiles as winding records)')
+                    help='"auto" (autotuned on the workload) or "tile,ctas_per_sm[,w][,q]", e.g. '
+                         '"16,0" (",w": interior tiles as winding records; ",q": work-queue '
+                         'raster)')
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -696,11 +719,11 @@ def main():
         if args.impl == "ours":
             torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group(backend)
-    cap, wname = build_workload(args)
+    cap, wname, scene_bytes = build_workload(args)
     if args.impl == "reference":
         run_reference(args, cap, wname, rank, world)
     else:
-        run_ours(args, cap, wname, rank, world)
+        run_ours(args, cap, wname, rank, world, scene_bytes)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

@@ -413,6 +413,16 @@ int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_
 int rive_cuda_get_raster_config(const rive_cuda_context* ctx, int* tile_size, int* ctas_per_sm);
 
 /*
+ * Raster schedule (no counterpart in the reference; off by default, an
+ * autotuner knob; 16-pixel tiles): with it on, the raster runs as a
+ * persistent grid of resident CTAs that take tiles from an atomic cursor over
+ * the batch's tiles sorted by bin entries, heaviest first, instead of one CTA
+ * launched per tile. The image is the same either way.
+ */
+int rive_cuda_set_raster_queue(rive_cuda_context* ctx, int enabled);
+int rive_cuda_get_raster_queue(const rive_cuda_context* ctx, int* enabled);
+
+/*
  * Interior tiles as winding records (no counterpart in the reference; off by
  * default, an autotuner knob). Inside a fill, every midpoint-fan triangle has
  * coverage +1 or -1, so on a tile that no contour edge, AA ramp or contour

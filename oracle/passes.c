@@ -485,17 +485,56 @@ static float measure_cubic_local_curvature(f2 p0, f2 p1, f2 p2, f2 p3, float T,
     return rc_acosf(cosine_between_vectors(tan0, tan1));
 }
 
-/* The tessellated point at T by De Casteljau with unchecked_mix(a, b, t) =
- * (b - a) * t + a (tessellate.glsl:535-540); *abc and *bcd are the last
- * level's pair, whose difference is the tangent. */
+/* Compensated De Casteljau (Graillat, Langlois and Louvet's compensated
+ * evaluation): every mix (b - a) * t + a is computed with its exact rounding
+ * errors (TwoSum for the sums, a fused multiply-subtract for the product),
+ * the errors are carried through the levels with the values, and the point
+ * is value + error rounded once: as if evaluated in twice the precision, so
+ * the fp32 point is within about half an ulp of the exact point at T. */
+static inline float two_sum_err(float a, float b, float s)
+{
+    const float bb = s - a;
+    return (a - (s - bb)) + (b - bb);
+}
+
+typedef struct
+{
+    float v, e; /* value and its (first-order) error term */
+} cfloat;
+
+static inline cfloat cmix(cfloat a, cfloat b, float t)
+{
+    const float d = b.v - a.v;
+    const float ed = two_sum_err(b.v, -a.v, d);
+    const float p = d * t;
+    const float ep = fmaf(d, t, -p);
+    const float r = a.v + p;
+    const float er = two_sum_err(a.v, p, r);
+    /* a + (b - a) t = r + er + ep + ed t, plus the inputs' errors mixed. */
+    const float e = ((er + ep) + ed * t) + fmaf(b.e - a.e, t, a.e);
+    return (cfloat){r, e};
+}
+
+static float eval_cubic_c(float a0, float a1, float a2, float a3, float t, float* t0, float* t1)
+{
+    const cfloat p0 = {a0, 0.f}, p1 = {a1, 0.f}, p2 = {a2, 0.f}, p3 = {a3, 0.f};
+    const cfloat ab = cmix(p0, p1, t), bc = cmix(p1, p2, t), cd = cmix(p2, p3, t);
+    const cfloat abc = cmix(ab, bc, t), bcd = cmix(bc, cd, t);
+    const cfloat r = cmix(abc, bcd, t);
+    *t0 = abc.v;
+    *t1 = bcd.v;
+    return r.v + r.e;
+}
+
+/* The tessellated point at T by De Casteljau (tessellate.glsl:535-540),
+ * compensated as above. *abc and *bcd are the last level's pair, whose
+ * difference is the tangent. */
 static f2 eval_cubic_mix(f2 p0, f2 p1, f2 p2, f2 p3, float T, f2* abc, f2* bcd)
 {
-    f2 ab = add2(mul2(sub2(p1, p0), T), p0);
-    f2 bc = add2(mul2(sub2(p2, p1), T), p1);
-    f2 cd = add2(mul2(sub2(p3, p2), T), p2);
-    *abc = add2(mul2(sub2(bc, ab), T), ab);
-    *bcd = add2(mul2(sub2(cd, bc), T), bc);
-    return add2(mul2(sub2(*bcd, *abc), T), *abc);
+    f2 q;
+    q.x = eval_cubic_c(p0.x, p1.x, p2.x, p3.x, T, &abc->x, &bcd->x);
+    q.y = eval_cubic_c(p0.y, p1.y, p2.y, p3.y, T, &abc->y, &bcd->y);
+    return q;
 }
 
 /* The parametric segment count of a cubic in pixel space under the path's

@@ -11,9 +11,10 @@ caller's own work with CUDA events on the caller's stream and leaves the
 fastest set on the context.
 
 The search space is tile size {8, 16, 32} x resident raster CTAs per SM
-{1, 2, 4, as many as fit} x winding records {off, on}; 32-pixel tiles run one
-1,024-thread CTA per SM at most, so only their "as many as fit" entry
-differs.
+{1, 2, 4, as many as fit} x winding records {off, on}, and for 16-pixel
+tiles the raster schedule {one CTA per tile, persistent work queue}; 32-pixel
+tiles run one 1,024-thread CTA per SM at most, so only their "as many as fit"
+entry differs.
 """
 from __future__ import annotations
 
@@ -31,11 +32,13 @@ def _candidates():
     for w in WINDING:
         for t in TILES:
             for c in (CTAS_PER_SM if t != 32 else (0,)):
-                out.append((t, c, w))
+                for q in ((False, True) if t == 16 else (False,)):
+                    out.append((t, c, w, q))
     return tuple(out)
 
 
-# (tile size in pixels, resident raster CTAs per SM or 0, winding records)
+# (tile size in pixels, resident raster CTAs per SM or 0, winding records,
+# work-queue raster)
 CANDIDATES = _candidates()
 
 
@@ -44,17 +47,20 @@ class Trial:
     tile_size: int
     ctas_per_sm: int
     winding: bool
+    queue: bool
     ms: float
 
 
-def apply(ctx, tile_size, ctas_per_sm, winding):
+def apply(ctx, tile_size, ctas_per_sm, winding, queue=False):
     ctx.set_raster_config(tile_size, ctas_per_sm)
     ctx.set_winding_tiles(winding)
+    ctx.set_raster_queue(queue)
 
 
-def time_config(ctx, run, tile_size, ctas_per_sm, winding, stream, warmup=2, iters=5):
+def time_config(ctx, run, tile_size, ctas_per_sm, winding, stream, warmup=2, iters=5,
+                queue=False):
     """Mean device milliseconds of `run(stream)` under one configuration."""
-    apply(ctx, tile_size, ctas_per_sm, winding)
+    apply(ctx, tile_size, ctas_per_sm, winding, queue)
     with torch.cuda.stream(stream):
         for _ in range(warmup):
             run(stream)
@@ -71,7 +77,7 @@ def time_config(ctx, run, tile_size, ctas_per_sm, winding, stream, warmup=2, ite
 
 def autotune(ctx, run, candidates=CANDIDATES, stream=None, warmup=2, iters=5):
     """Times `run(stream)` (one frame or one batch, enqueued on `stream`) under
-    each candidate (tile size, CTAs per SM, winding records) and leaves the
+    each candidate (tile size, CTAs per SM, winding records, queue) and leaves the
     fastest configured on `ctx`.
 
     Returns (best Trial, all Trials). `run` must enqueue the same work each
@@ -83,7 +89,8 @@ def autotune(ctx, run, candidates=CANDIDATES, stream=None, warmup=2, iters=5):
     for cand in candidates:
         t, c = cand[0], cand[1]
         w = cand[2] if len(cand) > 2 else False
-        trials.append(Trial(t, c, w, time_config(ctx, run, t, c, w, stream, warmup, iters)))
+        q = cand[3] if len(cand) > 3 else False
+        trials.append(Trial(t, c, w, q, time_config(ctx, run, t, c, w, stream, warmup, iters, q)))
     best = min(trials, key=lambda r: r.ms)
-    apply(ctx, best.tile_size, best.ctas_per_sm, best.winding)
+    apply(ctx, best.tile_size, best.ctas_per_sm, best.winding, best.queue)
     return best, trials

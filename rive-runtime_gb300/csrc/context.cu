@@ -76,6 +76,25 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    uint32_t tileCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
+// The work-queue raster (kernels_raster.cu).
+__global__ void raster_queue_kernel(BatchTables B,
+                                    const TriRecord* tris,
+                                    const uint32_t* sortedSlots,
+                                    const uint2* ranges,
+                                    const uint32_t* order,
+                                    uint32_t* cursor,
+                                    uint32_t tiles);
+__global__ void raster_queue_feather_kernel(BatchTables B,
+                                            const TriRecord* tris,
+                                            const uint32_t* sortedSlots,
+                                            const uint2* ranges,
+                                            const uint32_t* order,
+                                            uint32_t* cursor,
+                                            uint32_t tiles);
+__global__ void tile_order_keys_kernel(uint32_t tiles,
+                                       const uint2* ranges,
+                                       uint32_t* keys,
+                                       uint32_t* vals);
 // Interior tiles as winding records (kernels_raster.cu).
 __global__ void path_init_kernel(BatchTables B);
 __global__ void path_bounds_kernel(BatchTables B);
@@ -207,6 +226,12 @@ struct rive_cuda_context
     // Interior tiles as winding records (rive_cuda_set_winding_tiles): per-path
     // grids and the cell pool, grown when a flush asked for more cells.
     bool windingTiles = false;
+    // Raster as a persistent work queue over heaviest-first tiles
+    // (rive_cuda_set_raster_queue; 16-pixel tiles).
+    bool rasterQueue = false;
+    int queueCtas[2] = {0, 0}; // resident queue CTAs per SM [feather variant]
+    int smCount = 0;
+    DeviceBuffer queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor;
     DeviceBuffer pathGrids, gridWinding, gridEdge, gridCounters;
     uint32_t gridCapacity = 0;
     uint32_t* hGridCounters = nullptr; // pinned: cells asked, winding entries
@@ -234,7 +259,7 @@ struct rive_cuda_graph
     rive_cuda_context* ctx = nullptr;
     DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
         scanTemp, sortTemp, ranges, error, featherPlanes, pathGrids, gridWinding, gridEdge,
-        gridCounters;
+        gridCounters, queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -594,6 +619,12 @@ struct Scratch
     uint8_t* gridEdge = nullptr;
     uint32_t* gridCounters = nullptr;
     uint32_t gridCapacity = 0;
+    // Work-queue raster: the tile order (sorted keys/values and their
+    // alternates), the sort's temporaries and the cursor.
+    uint32_t *qKeys = nullptr, *qVals = nullptr, *qKeysAlt = nullptr, *qValsAlt = nullptr;
+    uint32_t* qCursor = nullptr;
+    void* qTemp = nullptr;
+    size_t qTempBytes = 0;
 };
 
 // Fills the table blob (host memory) and returns the device view of it.
@@ -837,6 +868,14 @@ int prepare_raster(rive_cuda_context* ctx)
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kRaster32SmemBytes));
         ctx->raster32Ready = true;
     }
+    if (ctx->rasterQueue && ctx->smCount == 0)
+    {
+        CK(cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device));
+        const void* q[2] = {(const void*)raster_queue_kernel,
+                            (const void*)raster_queue_feather_kernel};
+        for (int f = 0; f < 2; ++f)
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctx->queueCtas[f], q[f], 256, 0));
+    }
     const int slot = ctx->tileLog2 == 3 ? 0 : ctx->tileLog2 == 4 ? 1 : -1;
     if (slot >= 0 && ctx->rasterCtasPerSm > 0 && ctx->rasterPadFor[slot] != ctx->rasterCtasPerSm)
     {
@@ -858,11 +897,30 @@ int prepare_raster(rive_cuda_context* ctx)
 int launch_raster(rive_cuda_context* ctx,
                   const BatchLayout& L,
                   const BatchTables& B,
+                  const Scratch& S,
                   const TriRecord* tris,
                   const uint32_t* sortedSlots,
                   const uint2* ranges,
                   cudaStream_t stream)
 {
+    if (L.tileLog2 == 4 && S.qCursor)
+    {
+        // The work queue: tiles sorted by bin entries, heaviest first, taken
+        // in turn by a persistent grid of resident CTAs.
+        tile_order_keys_kernel<<<(L.tiles + 255) / 256, 256, 0, stream>>>(L.tiles, ranges, S.qKeys,
+                                                                        S.qVals);
+        cub::DoubleBuffer<uint32_t> k(S.qKeys, S.qKeysAlt), v(S.qVals, S.qValsAlt);
+        size_t tb = S.qTempBytes;
+        CK(cub::DeviceRadixSort::SortPairs(S.qTemp, tb, k, v, (int)L.tiles, 0, 32, stream));
+        CK(cudaMemsetAsync(S.qCursor, 0, 4, stream));
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][1] : 0;
+        const int per = ctx->rasterCtasPerSm > 0 ? ctx->rasterCtasPerSm : ctx->queueCtas[L.feather];
+        const uint32_t grid =
+            std::min<uint32_t>(L.tiles, (uint32_t)std::max(per * ctx->smCount, 1));
+        (L.feather ? raster_queue_feather_kernel : raster_queue_kernel)<<<grid, 256, dyn, stream>>>(
+            B, tris, sortedSlots, ranges, v.Current(), S.qCursor, L.tiles);
+        return RIVE_CUDA_OK;
+    }
     if (L.tileLog2 == 3)
     {
         const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][0] : 0;
@@ -921,7 +979,7 @@ int enqueue_back(rive_cuda_context* ctx,
         sortedSlots = v.Current();
     }
     stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
-    int rc = launch_raster(ctx, L, B, S.tris, sortedSlots, S.ranges, stream);
+    int rc = launch_raster(ctx, L, B, S, S.tris, sortedSlots, S.ranges, stream);
     stage_end(ctx, stream);
     if (rc)
         return rc;
@@ -934,6 +992,15 @@ size_t scan_temp_bytes(uint32_t slots)
     size_t b = 0;
     cub::DeviceScan::InclusiveSum(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
                                   std::max(slots, 1u));
+    return b;
+}
+
+// Temporary bytes of the work queue's sort of `tiles` tile indices.
+size_t queue_temp_bytes(uint32_t tiles)
+{
+    size_t b = 0;
+    cub::DoubleBuffer<uint32_t> k(nullptr, nullptr), v(nullptr, nullptr);
+    cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, (int)std::max(tiles, 1u), 0, 32);
     return b;
 }
 
@@ -984,6 +1051,17 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         CK(ctx->gridEdge.reserve(ctx->gridCapacity));
         CK(ctx->gridCounters.reserve(8));
     }
+    const bool queue = ctx->rasterQueue && L.tileLog2 == 4;
+    size_t queueBytes = 0;
+    if (queue)
+    {
+        queueBytes = queue_temp_bytes(L.tiles);
+        for (DeviceBuffer* b : {&ctx->queueKeys, &ctx->queueVals, &ctx->queueKeysAlt,
+                                &ctx->queueValsAlt})
+            CK(b->reserve((size_t)L.tiles * 4));
+        CK(ctx->queueTemp.reserve(queueBytes));
+        CK(ctx->queueCursor.reserve(4));
+    }
     const size_t scanBytes = scan_temp_bytes(L.slots);
     CK(ctx->scanTemp.reserve(scanBytes));
     ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
@@ -1009,6 +1087,16 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         S.gridEdge = (uint8_t*)ctx->gridEdge.ptr;
         S.gridCounters = (uint32_t*)ctx->gridCounters.ptr;
         S.gridCapacity = ctx->gridCapacity;
+    }
+    if (queue)
+    {
+        S.qKeys = (uint32_t*)ctx->queueKeys.ptr;
+        S.qVals = (uint32_t*)ctx->queueVals.ptr;
+        S.qKeysAlt = (uint32_t*)ctx->queueKeysAlt.ptr;
+        S.qValsAlt = (uint32_t*)ctx->queueValsAlt.ptr;
+        S.qTemp = ctx->queueTemp.ptr;
+        S.qTempBytes = queueBytes;
+        S.qCursor = (uint32_t*)ctx->queueCursor.ptr;
     }
     BatchTables B = write_tables(ctx, in, L, S, (uint8_t*)ctx->hTables.ptr);
     CK(cudaMemcpyAsync(S.tables, ctx->hTables.ptr, L.tableBytes, cudaMemcpyHostToDevice, stream));
@@ -1135,7 +1223,9 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
                             &ctx->keys, &ctx->vals, &ctx->keysAlt, &ctx->valsAlt,
                             &ctx->sortTemp, &ctx->scanTemp, &ctx->ranges, &ctx->dTables,
                             &ctx->pathGrids, &ctx->gridWinding, &ctx->gridEdge,
-                            &ctx->gridCounters})
+                            &ctx->gridCounters, &ctx->queueKeys, &ctx->queueVals,
+                            &ctx->queueKeysAlt, &ctx->queueValsAlt, &ctx->queueTemp,
+                            &ctx->queueCursor})
         b->release();
     ctx->hTables.release();
     if (ctx->hGridCounters)
@@ -1402,7 +1492,9 @@ void graph_free(rive_cuda_graph* g)
     for (DeviceBuffer* b : {&g->tables, &g->tess, &g->grad, &g->tris, &g->counts, &g->masks, &g->offsets,
                             &g->keys, &g->vals, &g->keysAlt, &g->valsAlt, &g->scanTemp,
                             &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes,
-                            &g->pathGrids, &g->gridWinding, &g->gridEdge, &g->gridCounters})
+                            &g->pathGrids, &g->gridWinding, &g->gridEdge, &g->gridCounters,
+                            &g->queueKeys, &g->queueVals, &g->queueKeysAlt, &g->queueValsAlt,
+                            &g->queueTemp, &g->queueCursor})
         b->release();
     if (g->hError)
         cudaFreeHost(g->hError);
@@ -1434,6 +1526,16 @@ int graph_build(rive_cuda_context* ctx,
         CK(g->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(g->error.reserve(4));
+    const bool queue = ctx->rasterQueue && L.tileLog2 == 4;
+    size_t queueBytes = 0;
+    if (queue)
+    {
+        queueBytes = queue_temp_bytes(L.tiles);
+        for (DeviceBuffer* b : {&g->queueKeys, &g->queueVals, &g->queueKeysAlt, &g->queueValsAlt})
+            CK(b->reserve((size_t)L.tiles * 4));
+        CK(g->queueTemp.reserve(queueBytes));
+        CK(g->queueCursor.reserve(4));
+    }
     const size_t scanBytes = scan_temp_bytes(L.slots);
     CK(g->scanTemp.reserve(scanBytes));
     CK(cudaMemset(g->error.ptr, 0, 4));
@@ -1451,6 +1553,16 @@ int graph_build(rive_cuda_context* ctx,
     S.scanTempBytes = scanBytes;
     S.ranges = (uint2*)g->ranges.ptr;
     S.error = (uint32_t*)g->error.ptr;
+    if (queue)
+    {
+        S.qKeys = (uint32_t*)g->queueKeys.ptr;
+        S.qVals = (uint32_t*)g->queueVals.ptr;
+        S.qKeysAlt = (uint32_t*)g->queueKeysAlt.ptr;
+        S.qValsAlt = (uint32_t*)g->queueValsAlt.ptr;
+        S.qTemp = g->queueTemp.ptr;
+        S.qTempBytes = queueBytes;
+        S.qCursor = (uint32_t*)g->queueCursor.ptr;
+    }
     std::vector<uint8_t> h(L.tableBytes);
     // The graph's winding grids: a cell pool sized like the context's, grown
     // below if the measuring run asks for more.
@@ -1750,6 +1862,22 @@ int rive_cuda_eval_tessellation_math(int fn, const float* in, float* out, size_t
     if (!((fn >= 0 && fn <= 5) || (fn >= 10 && fn <= 13)) || (n && (!in || !out)))
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
     return run_tess_math(fn, in, out, n) == cudaSuccess ? RIVE_CUDA_OK : RIVE_CUDA_ERR_CUDA;
+}
+
+int rive_cuda_set_raster_queue(rive_cuda_context* ctx, int enabled)
+{
+    if (!ctx)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    ctx->rasterQueue = enabled != 0;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_get_raster_queue(const rive_cuda_context* ctx, int* enabled)
+{
+    if (!ctx || !enabled)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *enabled = ctx->rasterQueue ? 1 : 0;
+    return RIVE_CUDA_OK;
 }
 
 int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled)

@@ -2370,12 +2370,12 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                                             const uint32_t* __restrict__ sortedSlots,
                                             const uint2* __restrict__ ranges,
                                             TileTri* __restrict__ sTris,
-                                            typename RasterTile<TL>::Mask* __restrict__ sMask)
+                                            typename RasterTile<TL>::Mask* __restrict__ sMask,
+                                            uint32_t gtile)
 {
     using G = RasterTile<TL>;
     static_assert(sizeof(FlushParams) / 4 <= G::kThreads, "one word of FlushParams per thread");
     __shared__ FlushParams sP;
-    const uint32_t gtile = blockIdx.x;
     const uint2 range = ranges[gtile];
     // The tile's scene: its parameters are staged once for the whole CTA.
     const uint32_t scene = find_range(B.tileBase, B.sceneCount, gtile);
@@ -2576,11 +2576,57 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
     {                                                                                             \
         __shared__ TileTri sTris[256 * RIVE_RASTER_STAGE];                                        \
         __shared__ uint8_t sMask[256 * RIVE_RASTER_STAGE];                                        \
-        raster_tile<4, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask);   \
+        raster_tile<4, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask,   \
+                                                    blockIdx.x);                                  \
     }
 RIVE_RASTER_KERNELS(raster_tile_kernel, false)
 RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
 #undef RIVE_RASTER_KERNELS
+
+// The work-queue form of the 16x16 raster: a persistent grid (as many CTAs
+// as stay resident) in which each CTA takes its next tile from an atomic
+// cursor over `order`, the batch's tiles sorted by bin entries, heaviest
+// first, so the longest tiles start first and the last wave has no straggler
+// behind it. The cursor starts at zero on every launch.
+#define RIVE_RASTER_QUEUE_KERNELS(NAME, FEATHER)                                                  \
+    __global__ void __launch_bounds__(256, RIVE_RASTER_MIN_BLOCKS) NAME(                           \
+        BatchTables B, const TriRecord* __restrict__ tris,                                        \
+        const uint32_t* __restrict__ sortedSlots, const uint2* __restrict__ ranges,               \
+        const uint32_t* __restrict__ order, uint32_t* __restrict__ cursor, uint32_t tiles)        \
+    {                                                                                             \
+        __shared__ TileTri sTris[256];                                                            \
+        __shared__ uint8_t sMask[256];                                                            \
+        __shared__ uint32_t sNext;                                                                \
+        for (;;)                                                                                  \
+        {                                                                                         \
+            __syncthreads(); /* the last tile is done with the shared state */                    \
+            if (threadIdx.x == 0)                                                                 \
+                sNext = atomicAdd(cursor, 1u);                                                    \
+            __syncthreads();                                                                      \
+            const uint32_t t = sNext;                                                             \
+            if (t >= tiles)                                                                       \
+                break;                                                                            \
+            raster_tile<4, FEATHER, 1>(B, tris, sortedSlots, ranges, sTris, sMask, order[t]);     \
+        }                                                                                         \
+    }
+RIVE_RASTER_QUEUE_KERNELS(raster_queue_kernel, false)
+RIVE_RASTER_QUEUE_KERNELS(raster_queue_feather_kernel, true)
+#undef RIVE_RASTER_QUEUE_KERNELS
+
+// Sort keys of the work queue: per tile, its bin entries inverted (a plain
+// ascending sort then puts the heaviest tile first), and its index.
+__global__ void __launch_bounds__(256) tile_order_keys_kernel(uint32_t tiles,
+                                                              const uint2* __restrict__ ranges,
+                                                              uint32_t* __restrict__ keys,
+                                                              uint32_t* __restrict__ vals)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tiles)
+        return;
+    const uint2 r = ranges[i];
+    keys[i] = 0xffffffffu - (r.y > r.x ? r.y - r.x : 0u);
+    vals[i] = i;
+}
 
 #define RIVE_RASTER8_KERNELS(NAME, FEATHER)                                                       \
     __global__ void __launch_bounds__(64) NAME(BatchTables B, const TriRecord* __restrict__ tris, \
@@ -2589,7 +2635,8 @@ RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
     {                                                                                             \
         __shared__ TileTri sTris[64 * RIVE_RASTER_STAGE];                                         \
         __shared__ uint8_t sMask[64 * RIVE_RASTER_STAGE];                                         \
-        raster_tile<3, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask);   \
+        raster_tile<3, FEATHER, RIVE_RASTER_STAGE>(B, tris, sortedSlots, ranges, sTris, sMask,   \
+                                                    blockIdx.x);                                  \
     }
 RIVE_RASTER8_KERNELS(raster_tile8_kernel, false)
 RIVE_RASTER8_KERNELS(raster_tile8_feather_kernel, true)
@@ -2605,7 +2652,7 @@ RIVE_RASTER8_KERNELS(raster_tile8_feather_kernel, true)
         extern __shared__ uint4 dyn[];                                                            \
         TileTri* sTris = reinterpret_cast<TileTri*>(dyn);                                         \
         uint32_t* sMask = reinterpret_cast<uint32_t*>(sTris + 1024);                              \
-        raster_tile<5, FEATHER, 1>(B, tris, sortedSlots, ranges, sTris, sMask);                   \
+        raster_tile<5, FEATHER, 1>(B, tris, sortedSlots, ranges, sTris, sMask, blockIdx.x);       \
     }
 RIVE_RASTER32_KERNELS(raster_tile32_kernel, false)
 RIVE_RASTER32_KERNELS(raster_tile32_feather_kernel, true)

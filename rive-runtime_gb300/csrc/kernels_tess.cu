@@ -90,18 +90,59 @@ __device__ __forceinline__ float rive_atan2(float2 v)
     return v.y >= 0.f ? theta : -theta;
 }
 
-// The tessellated point at T by De Casteljau with unchecked_mix(a, b, t) =
-// (b - a) * t + a (tessellate.glsl:535-540); abc and bcd are the last
-// level's pair, whose difference is the tangent.
+// Compensated De Casteljau (Graillat, Langlois and Louvet's compensated
+// evaluation): every mix (b - a) * t + a is computed with its exact rounding
+// errors (TwoSum for the sums, a fused multiply-subtract for the product),
+// the errors are carried through the levels with the values, and the point
+// is value + error rounded once: as if evaluated in twice the precision, so
+// the fp32 point is within about half an ulp of the exact point at T.
+__device__ __forceinline__ float two_sum_err(float a, float b, float s)
+{
+    const float bb = __fsub_rn(s, a);
+    return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+struct CFloat
+{
+    float v, e; // value and its (first-order) error term
+};
+
+__device__ __forceinline__ CFloat cmix(CFloat a, CFloat b, float t)
+{
+    const float d = __fsub_rn(b.v, a.v);
+    const float ed = two_sum_err(b.v, -a.v, d);
+    const float p = __fmul_rn(d, t);
+    const float ep = __fmaf_rn(d, t, -p);
+    const float r = __fadd_rn(a.v, p);
+    const float er = two_sum_err(a.v, p, r);
+    // a + (b - a) t = r + er + ep + ed t, plus the inputs' errors mixed.
+    const float e = __fadd_rn(__fadd_rn(__fadd_rn(er, ep), __fmul_rn(ed, t)),
+                              __fmaf_rn(__fsub_rn(b.e, a.e), t, a.e));
+    return CFloat{r, e};
+}
+
+__device__ __forceinline__ float eval_cubic_c(float a0, float a1, float a2, float a3, float t,
+                                              float& t0, float& t1)
+{
+    const CFloat p0{a0, 0.f}, p1{a1, 0.f}, p2{a2, 0.f}, p3{a3, 0.f};
+    const CFloat ab = cmix(p0, p1, t), bc = cmix(p1, p2, t), cd = cmix(p2, p3, t);
+    const CFloat abc = cmix(ab, bc, t), bcd = cmix(bc, cd, t);
+    const CFloat r = cmix(abc, bcd, t);
+    t0 = abc.v;
+    t1 = bcd.v;
+    return __fadd_rn(r.v, r.e);
+}
+
+// The tessellated point at T by De Casteljau (tessellate.glsl:535-540),
+// compensated as above. abc and bcd are the last level's pair, whose
+// difference is the tangent.
 __device__ __forceinline__ float2 eval_cubic_mix(float2 p0, float2 p1, float2 p2, float2 p3,
                                                  float T, float2& abc, float2& bcd)
 {
-    const float2 ab = f2lerp(p0, p1, T);
-    const float2 bc = f2lerp(p1, p2, T);
-    const float2 cd = f2lerp(p2, p3, T);
-    abc = f2lerp(ab, bc, T);
-    bcd = f2lerp(bc, cd, T);
-    return f2lerp(abc, bcd, T);
+    float2 q;
+    q.x = eval_cubic_c(p0.x, p1.x, p2.x, p3.x, T, abc.x, bcd.x);
+    q.y = eval_cubic_c(p0.y, p1.y, p2.y, p3.y, T, abc.y, bcd.y);
+    return q;
 }
 
 // Wang's formula at precision 4 in pixel space under the path's 2x2 matrix m

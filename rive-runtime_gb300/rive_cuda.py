@@ -116,6 +116,8 @@ def load():
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
         "rive_cuda_set_winding_tiles": (i32, [vp, i32]),
+        "rive_cuda_set_raster_queue": (i32, [vp, i32]),
+        "rive_cuda_get_raster_queue": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_eval_tessellation_math": (i32, [i32, vp, vp, sz]),
         "rive_cuda_get_winding_tiles": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_feather_table": (i32, [vp]),
@@ -375,6 +377,18 @@ class Context:
         default) or as the plain midpoint fan; the image is the same."""
         self.check(self.lib.rive_cuda_set_winding_tiles(self.h, 1 if on else 0),
                    "set_winding_tiles")
+
+    def set_raster_queue(self, on: bool):
+        """The raster as a persistent work queue over heaviest-first tiles
+        (16-pixel tiles), or one CTA per tile (default); same image."""
+        self.check(self.lib.rive_cuda_set_raster_queue(self.h, 1 if on else 0),
+                   "set_raster_queue")
+
+    def raster_queue(self):
+        v = ctypes.c_int()
+        self.check(self.lib.rive_cuda_get_raster_queue(self.h, ctypes.byref(v)),
+                   "get_raster_queue")
+        return bool(v.value)
 
     def winding_tiles(self):
         v = ctypes.c_int()

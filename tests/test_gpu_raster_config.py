@@ -112,7 +112,50 @@ def test_autotune_leaves_a_candidate_set(ctx):
         assert all(t.ms > 0 for t in trials)
         assert ctx.raster_config() == (best.tile_size, best.ctas_per_sm)
         assert ctx.winding_tiles() == best.winding
+        assert ctx.raster_queue() == best.queue
         assert best.ms == min(t.ms for t in trials)
     finally:
         ctx.set_raster_config(16, 0)
         ctx.set_winding_tiles(False)
+        ctx.set_raster_queue(False)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ctas", [0, 2])
+def test_work_queue_raster_matches_the_grid_bit_for_bit(ctx, ctas):
+    """The persistent work-queue raster (heaviest tiles first) renders every
+    tile as the one-CTA-per-tile grid does: identical images on every golden,
+    one by one, in batches and in graphs."""
+    import torch
+    names = golden_names()
+    caps = [load_golden(n)[0] for n in names]
+    ctx.set_raster_config(16, ctas)
+    try:
+        want = {}
+        for queue in (False, True):
+            ctx.set_raster_queue(queue)
+            assert ctx.raster_queue() == queue
+            want[queue] = [ctx.render(c) for c in caps]
+        for n, a, b in zip(names, want[False], want[True]):
+            assert np.array_equal(a, b), n
+        pairs = [device_buffers(c) for c in caps]
+        stream = torch.cuda.Stream().cuda_stream
+        for mode in ("batch", "graph"):
+            targets = [torch.zeros((c.height, c.width, 4), dtype=torch.uint8, device="cuda")
+                       for c in caps]
+            torch.cuda.synchronize()
+            for items in flush_waves(caps, [p[0] for p in pairs], targets):
+                if mode == "batch":
+                    ctx.flush_batch(items, stream)
+                    ctx.sync(stream)
+                else:
+                    g = ctx.graph(items)
+                    g.launch(stream)
+                    g.check(stream)
+                    g.close()
+            torch.cuda.synchronize()
+            for n, t, w in zip(names, targets, want[False]):
+                assert np.array_equal(t.cpu().numpy(), w), (mode, n)
+    finally:
+        ctx.set_raster_queue(False)
+        ctx.set_raster_config(16, 0)

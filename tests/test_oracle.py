@@ -149,7 +149,7 @@ def test_oracle_renders_golden(name):
 @pytest.mark.parametrize("name", golden_names())
 def test_oracle_tessellation_within_fp64(name):
     """fp32 tessellated vertices vs the FP64 evaluation of the same segment
-    parameters: every vertex within 1e-4 px, or within 2 ulp of its coordinate
+    parameters: every vertex within 1e-4 px, or within 1 ulp of its coordinate
     where fp32 spacing itself exceeds that (coordinates beyond 1024 px)."""
     cap, _ = load_golden(name)
     for fi in range(len(cap.flushes)):
@@ -159,8 +159,8 @@ def test_oracle_tessellation_within_fp64(name):
         assert np.array_equal(t32[used, 3], flags64[used])
         xy32 = t32[used, :2].view(np.float32).astype(np.float64)
         err = np.abs(xy32 - xy64[used])
-        ulp2 = 2 * np.spacing(np.abs(xy64[used]).astype(np.float32)).astype(np.float64)
-        ok = err <= np.maximum(1e-4, ulp2)
+        ulp = np.spacing(np.abs(xy64[used]).astype(np.float32)).astype(np.float64)
+        ok = err <= np.maximum(1e-4, ulp)
         assert ok.all(), (name, float(ok.mean()), float(err.max()))
 
 
