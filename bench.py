@@ -356,6 +356,8 @@ def run_ours(args, cap, wname, rank, world, scene_bytes=None):
         line["batched_recorded"] = run_batched(args, dev, raster, recorded=True)
     if args.serve_sessions > 0 and world == 1:
         line["serving"] = run_serving(args, dev, raster)
+    if args.serve_curve and world == 1:
+        line["serving_curve"] = run_serving_curve(args, dev, raster)
     if args.serve_rec_sessions > 0 and world == 1:
         line["serving_recorded"] = run_serving_recorded(args, dev, raster)
     if args.feather_steps > 0 and world == 1:
@@ -446,7 +448,7 @@ def run_serving(args, dev, raster=None):
     """The serving loop (rive-runtime_gb300/serving.py): sessions with the
     full-feature distributions on a smaller canvas, Poisson arrivals at 50/s,
     each animated for a fixed number of frames at a fixed frame rate."""
-    import numpy as np
+    from inputgen import planner
     from rive_runtime_gb300 import rive_cuda, scene, serving
     scs = [scene.full_feature(seed=1000 + i, width=args.serve_size, height=args.serve_size,
                               n_paths=args.serve_paths) for i in range(args.serve_sessions)]
@@ -472,6 +474,67 @@ def run_serving(args, dev, raster=None):
             "hbm_budget_gb": 120, **st}
 
 
+def _serve(ctx, dev, raster, scenes, frames, fps, seed):
+    """One serving-loop run over `scenes` (Poisson arrivals at 50/s)."""
+    from inputgen import planner
+    from rive_runtime_gb300 import serving
+    sessions = serving.poisson_sessions(scenes, 50.0, frames=frames, fps=fps, seed=seed)
+    server = serving.FrameServer(ctx, planner.plan, device=dev, hbm_budget_bytes=120 << 30,
+                                 planner_threads=min(16, os.cpu_count() or 1))
+    return server.run(sessions, timeout_s=600.0)
+
+
+def run_serving_curve(args, dev, raster=None):
+    """Frame latency against session count.
+
+    (1) The serving scene (full-feature distributions at --serve-size with
+    --serve-paths paths) at each count of --serve-curve, --serve-curve-frames
+    frames per session at --serve-fps; the largest count whose p99 stays
+    within 8 ms is the capacity at that bound. (2) Sessions of the
+    full-feature single scene itself (2048x2048, 5,000 paths) at one and two
+    sessions: one such frame alone occupies the whole GPU for longer than
+    8 ms, so no session count of that scene holds p99 within 8 ms on one GPU
+    (1,000 of them would need 1,000 x 60 frames/s)."""
+    from rive_runtime_gb300 import rive_cuda, scene
+    counts = [int(x) for x in args.serve_curve.split(",") if x.strip()]
+    ctx = rive_cuda.Context(dev)
+    if raster:
+        ctx.set_raster_config(raster["tile"], raster["ctas_per_sm"])
+        ctx.set_winding_tiles(raster.get("winding", False))
+        ctx.set_raster_queue(raster.get("queue", False))
+    keys = ("sessions", "frames", "frames_per_s", "p50_ms", "p99_ms", "mean_batch",
+            "max_concurrent", "peak_reserved_gb", "wall_s")
+    curve, full = [], []
+    try:
+        for n in counts:
+            scs = [scene.full_feature(seed=3000 + i, width=args.serve_size,
+                                      height=args.serve_size, n_paths=args.serve_paths)
+                   for i in range(n)]
+            st = _serve(ctx, dev, raster, scs, args.serve_curve_frames, args.serve_fps, seed=n)
+            curve.append({"offered_frames_per_s": n * args.serve_fps,
+                          **{k: st[k] for k in keys}})
+        if args.serve_full_frames > 0:
+            for n in (1, 2):
+                scs = [scene.full_feature(seed=5000 + i) for i in range(n)]
+                st = _serve(ctx, dev, raster, scs, args.serve_full_frames, 4.0, seed=50 + n)
+                full.append({"offered_frames_per_s": n * 4.0, **{k: st[k] for k in keys}})
+    finally:
+        ctx.close()
+    within = [c["sessions"] for c in curve if c["p99_ms"] is not None and c["p99_ms"] <= 8.0]
+    return {
+        "scene": f"full_feature distributions, {args.serve_size}x{args.serve_size}, "
+                 f"{args.serve_paths} paths",
+        "fps_per_session": args.serve_fps, "frames_per_session": args.serve_curve_frames,
+        "arrivals_per_s": 50.0, "curve": curve,
+        "max_sessions_p99_within_8ms": max(within) if within else 0,
+        "full_scale": {"scene": "full_feature 2048x2048, 5,000 paths",
+                       "fps_per_session": 4.0, "frames_per_session": args.serve_full_frames,
+                       "runs": full,
+                       "sessions_p99_within_8ms": 0 if full and all(
+                           r["p99_ms"] > 8.0 for r in full) else None},
+    }
+
+
 def raster_setup(args, ctx, run, stream):
     """Applies --raster-config ("auto" or "tile,ctas_per_sm"); returns what was set."""
     if args.raster_config == "auto":
@@ -495,6 +558,7 @@ def run_serving_recorded(args, dev, raster=None):
     recorded .riv animations (tests/golden/anim, converted from its .sriv
     streams), each from a random start frame, Poisson arrivals at 50/s."""
     import glob
+    from inputgen import planner
     from rive_runtime_gb300 import rive_cuda, serving, sriv
     here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "anim")
     anims, names = [], []
@@ -694,6 +758,11 @@ def main():
     ap.add_argument("--serve-paths", type=int, default=300)
     ap.add_argument("--serve-frames", type=int, default=60)
     ap.add_argument("--serve-fps", type=float, default=8.0)
+    ap.add_argument("--serve-curve", default="4,16,64,128",
+                    help="session counts of the latency-against-sessions curve (empty skips it)")
+    ap.add_argument("--serve-curve-frames", type=int, default=40)
+    ap.add_argument("--serve-full-frames", type=int, default=6,
+                    help="frames per session of the full-scale serving runs (0 skips them)")
     ap.add_argument("--serve-rec-sessions", type=int, default=128,
                     help="sessions of the recorded-animation serving run (0 = skip)")
     ap.add_argument("--serve-rec-frames", type=int, default=120)
