@@ -242,6 +242,8 @@ struct rive_cuda_context
     bool raster32Ready = false;
     size_t rasterPad[2][2] = {};      // [feather variant][8 or 16 pixel kernel]: padding
     int rasterPadFor[2] = {-1, -1};   // the CTAs-per-SM limit it was found for
+    size_t queuePad[2] = {};          // [feather variant]: the work-queue kernel's padding
+    int queuePadFor = -1;             // the CTAs-per-SM limit it was found for
     // Stage timing (rive_cuda_set_profiling).
     bool profiling = false;
     std::vector<cudaEvent_t> eventPool;
@@ -888,6 +890,17 @@ int prepare_raster(rive_cuda_context* ctx)
         cudaGetLastError(); // a failed query only leaves the launch unpadded
         ctx->rasterPadFor[slot] = ctx->rasterCtasPerSm;
     }
+    if (ctx->rasterQueue && ctx->rasterCtasPerSm > 0 && ctx->queuePadFor != ctx->rasterCtasPerSm)
+    {
+        // The queue kernels have their own static shared memory, so their own
+        // padding (and their own dynamic shared memory limit, set there).
+        const void* q[2] = {(const void*)raster_queue_kernel,
+                            (const void*)raster_queue_feather_kernel};
+        for (int f = 0; f < 2; ++f)
+            ctx->queuePad[f] = occupancy_pad(q[f], 256, ctx->rasterCtasPerSm);
+        cudaGetLastError();
+        ctx->queuePadFor = ctx->rasterCtasPerSm;
+    }
     return RIVE_CUDA_OK;
 }
 
@@ -913,7 +926,7 @@ int launch_raster(rive_cuda_context* ctx,
         size_t tb = S.qTempBytes;
         CK(cub::DeviceRadixSort::SortPairs(S.qTemp, tb, k, v, (int)L.tiles, 0, 32, stream));
         CK(cudaMemsetAsync(S.qCursor, 0, 4, stream));
-        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][1] : 0;
+        const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->queuePad[L.feather] : 0;
         const int per = ctx->rasterCtasPerSm > 0 ? ctx->rasterCtasPerSm : ctx->queueCtas[L.feather];
         const uint32_t grid =
             std::min<uint32_t>(L.tiles, (uint32_t)std::max(per * ctx->smCount, 1));
