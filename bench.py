@@ -38,7 +38,10 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "tests"))
 
 
-RASTER_DRAM_BYTES_PER_ENTRY = 696.4e6 / 9.766e6
+# DRAM bytes per bin entry of the raster, from one ncu capture of each raster
+# form on the 1024x1024 full-feature frame (9.766 M entries): the one-CTA-per-
+# tile grid read and wrote 696.4 MB, the work queue 993.6 MB (profiles/).
+RASTER_DRAM_BYTES_PER_ENTRY = {"grid": 696.4e6 / 9.766e6, "queue": 993.6e6 / 9.766e6}
 
 
 def _package():
@@ -321,9 +324,10 @@ def run_ours(args, cap, wname, rank, world, scene_bytes=None):
         frame_bytes_raster = frame_entries * 100 + 4 * W * H * (len(cap.flushes) + preserve)
         alg_bytes = frame_bytes_raster / len(cap.flushes)
         # DRAM bytes (read + write) per launch, scaled by bin entries from one
-        # ncu capture of this kernel on the 1024x1024 full-feature frame
-        # (696.4 MB for 9.77 M entries); the full frame is too large to capture.
-        traffic = RASTER_DRAM_BYTES_PER_ENTRY * frame_entries / len(cap.flushes)
+        # ncu capture of this raster form on the 1024x1024 full-feature frame;
+        # the full frame is too large to capture.
+        form = "queue" if raster.get("queue") and raster.get("tile") == 16 else "grid"
+        traffic = RASTER_DRAM_BYTES_PER_ENTRY[form] * frame_entries / len(cap.flushes)
     elif dominant == "tessellate":
         alg_bytes = 64 * counts["spans"] / counts["flushes"] + 16 * counts["tess_vertices"] / counts["flushes"]
     else:

@@ -72,7 +72,21 @@ enum
     RIVE_CUDA_DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES = 1, /* feathered fills */
     RIVE_CUDA_DRAW_OUTER_CURVE_PATCHES = 2,   /* interior triangulation: the curves */
     RIVE_CUDA_DRAW_INTERIOR_TRIANGULATION = 3, /* ... and the interior triangles  */
+    RIVE_CUDA_DRAW_FEATHER_ATLAS_BLIT = 4,     /* a path's coverage from the atlas */
 };
+
+/*
+ * One gpu::AtlasDrawBatch (gpu.hpp:827-833): `patch_count` patch instances
+ * from `base_patch`, drawn into the feather atlas within the scissor
+ * [left, right) x [top, bottom) (atlas pixels). Fill batches draw center-AA
+ * midpoint-fan patches, stroke batches the border of midpoint-fan patches.
+ */
+typedef struct rive_cuda_atlas_batch
+{
+    uint16_t scissor[4]; /* left, top, right, bottom */
+    uint32_t patch_count;
+    uint32_t base_patch;
+} rive_cuda_atlas_batch;
 
 /*
  * One gpu::DrawBatch (gpu.hpp:1219-1282), flattened. The reference keeps the
@@ -130,6 +144,18 @@ typedef struct rive_cuda_flush_desc
     uint32_t has_triangle_vertices;
     uint32_t draw_batch_count;
     const rive_cuda_draw_batch* draw_batches; /* host array, list order */
+    /* The feather atlas (gpu.hpp:1361-1368, 1418-1426): feathered paths whose
+     * blur is wide enough render their coverage into an offscreen fp16
+     * texture first (fills add, strokes take the maximum), and a
+     * featherAtlasBlit draw of each then samples it. All zero when the flush
+     * has no atlas draws. */
+    uint32_t atlas_texture_width;  /* featherAtlasTextureWidth/Height */
+    uint32_t atlas_texture_height;
+    uint32_t atlas_content_width;  /* featherAtlasContentWidth/Height */
+    uint32_t atlas_content_height;
+    uint32_t atlas_fill_batch_count;
+    uint32_t atlas_stroke_batch_count;
+    const rive_cuda_atlas_batch* atlas_batches; /* fill batches, then stroke batches */
 } rive_cuda_flush_desc;
 
 typedef struct rive_cuda_context rive_cuda_context;

@@ -76,6 +76,12 @@ typedef struct rive_scene_header
  * frameBudgetMs = 0 and every fill is a midpoint fan. */
 #define RIVE_SCENE_FLAG_TRIANGULATE 1u
 
+/* Draw every feathered path through the feather atlas, whatever its radius:
+ * the frame is recorded with PlatformFeatures::alwaysFeatherToAtlas
+ * (gpu.hpp:156-158). Without it only blurs the front end scales to half
+ * resolution or less go to the atlas (radius x scale >= 32 px). */
+#define RIVE_SCENE_FLAG_FEATHER_ATLAS 2u
+
 /* In rive_scene_path.fill_rule: the path was built the way a replayed call
  * stream builds it, Factory::makeEmptyRenderPath + RenderPath::addRawPath,
  * which keeps empty segments; without it the path is made by

@@ -8,6 +8,7 @@
  * C ABI exactly what the reference's RenderContext produced.
  */
 #include "rive_cuda.h"
+#include "capture_format.h"
 
 #include <stdio.h>
 #include <stdlib.h>
@@ -26,6 +27,7 @@ struct rive_cuda_context
     uint32_t flush_count;
     rive_cuda_flush_desc descs[MAX_FLUSHES];
     rive_cuda_draw_batch* batches[MAX_FLUSHES];
+    rive_cuda_atlas_batch* atlas[MAX_FLUSHES];
     uint32_t width, height;
     int failed;
 };
@@ -57,7 +59,10 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         free(ctx->data[k]);
     }
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
+    {
         free(ctx->batches[i]);
+        free(ctx->atlas[i]);
+    }
     if (g_last == ctx)
         g_last = NULL;
     free(ctx);
@@ -165,6 +170,11 @@ int rive_cuda_flush(rive_cuda_context* ctx,
     ctx->batches[i] = (rive_cuda_draw_batch*)malloc(n ? n * sizeof(rive_cuda_draw_batch) : 1);
     if (n)
         memcpy(ctx->batches[i], desc->draw_batches, n * sizeof(rive_cuda_draw_batch));
+    size_t na = (size_t)desc->atlas_fill_batch_count + desc->atlas_stroke_batch_count;
+    ctx->descs[i].atlas_batches = NULL;
+    ctx->atlas[i] = (rive_cuda_atlas_batch*)malloc(na ? na * sizeof(rive_cuda_atlas_batch) : 1);
+    if (na)
+        memcpy(ctx->atlas[i], desc->atlas_batches, na * sizeof(rive_cuda_atlas_batch));
     return RIVE_CUDA_OK;
 }
 
@@ -185,7 +195,11 @@ int abi_recorder_write(const char* path)
         return 1;
     /* Seven kinds, or eight when the frame has interior triangles. */
     const uint32_t kinds = ctx->bytes[CAPTURED_KINDS] ? CAPTURED_KINDS + 1 : CAPTURED_KINDS;
-    uint32_t head[4] = {0x31504352u /* RCP1 */, ctx->width, ctx->height, kinds};
+    int v2 = 0;
+    for (uint32_t i = 0; i < ctx->flush_count; ++i)
+        v2 = v2 || rive_capture_flush_has_atlas(&ctx->descs[i]);
+    uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, ctx->width,
+                        ctx->height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const unsigned char zeros[8] = {0};
     for (uint32_t k = 0; k < kinds; ++k)
@@ -198,12 +212,7 @@ int abi_recorder_write(const char* path)
     }
     fwrite(&ctx->flush_count, sizeof(uint32_t), 1, f);
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
-    {
-        fwrite(&ctx->descs[i], sizeof(rive_cuda_flush_desc), 1, f);
-        if (ctx->descs[i].draw_batch_count)
-            fwrite(ctx->batches[i], sizeof(rive_cuda_draw_batch), ctx->descs[i].draw_batch_count,
-                   f);
-    }
+        rive_capture_write_flush(f, &ctx->descs[i], ctx->batches[i], ctx->atlas[i], v2);
     fclose(f);
     return 0;
 }

@@ -11,6 +11,7 @@
 #include "scene_replay.hpp"
 
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 extern "C" int abi_recorder_write(const char* path);
@@ -36,6 +37,12 @@ int main(int argc, char** argv)
     if (!ctx)
         return 1;
     auto* impl = ctx->static_impl_cast<rive::gpu::RenderContextCUDAImpl>();
+    if (scene.size() >= sizeof(rive_scene_header))
+    {
+        rive_scene_header hdr;
+        memcpy(&hdr, scene.data(), sizeof(hdr));
+        impl->setAlwaysFeatherToAtlas((hdr.flags & RIVE_SCENE_FLAG_FEATHER_ATLAS) != 0);
+    }
     const char* err = replay_scene(ctx.get(), scene, [&](uint32_t w, uint32_t h) {
         return rive::rcp<rive::gpu::RenderTarget>(impl->makeRenderTarget(w, h));
     });

@@ -1,0 +1,63 @@
+/*
+ * capture_format.h -- TEST INFRASTRUCTURE (oracle). The flush part of the
+ * capture layout, shared by ref_capture / cmdbuf_capture (capture_impl.hpp)
+ * and the product-adapter recorder (abi_recorder.c), so that both write the
+ * same bytes for the same flushes.
+ *
+ * Per flush:
+ *   the rive_cuda_flush_desc fields up to and including draw_batches
+ *   (RIVE_CAPTURE_DESC_BYTES, the pointer written as 0),
+ *   rive_cuda_draw_batch[draw_batch_count],
+ * and, in an 'RCP2' capture (one whose frame renders into the feather atlas):
+ *   u32 atlas_texture_width, atlas_texture_height, atlas_content_width,
+ *   atlas_content_height, atlas_fill_batch_count, atlas_stroke_batch_count,
+ *   rive_cuda_atlas_batch[fill + stroke].
+ * A frame without atlas draws keeps the 'RCP1' layout byte for byte.
+ */
+#ifndef RIVE_CAPTURE_FORMAT_H
+#define RIVE_CAPTURE_FORMAT_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "rive_cuda.h"
+
+#define RIVE_CAPTURE_MAGIC_V1 0x31504352u /* "RCP1" */
+#define RIVE_CAPTURE_MAGIC_V2 0x32504352u /* "RCP2": with feather atlas batches */
+#define RIVE_CAPTURE_DESC_BYTES offsetof(rive_cuda_flush_desc, atlas_texture_width)
+
+static inline int rive_capture_flush_has_atlas(const rive_cuda_flush_desc* d)
+{
+    return d->atlas_fill_batch_count != 0 || d->atlas_stroke_batch_count != 0 ||
+           d->atlas_content_width != 0 || d->atlas_content_height != 0;
+}
+
+/* Writes one flush (`d`'s pointers are ignored; the arrays come separately). */
+static inline void rive_capture_write_flush(FILE* f,
+                                            const rive_cuda_flush_desc* d,
+                                            const rive_cuda_draw_batch* batches,
+                                            const rive_cuda_atlas_batch* atlas,
+                                            int v2)
+{
+    rive_cuda_flush_desc o;
+    memcpy(&o, d, sizeof(o));
+    o.draw_batches = NULL;
+    o.atlas_batches = NULL;
+    fwrite(&o, RIVE_CAPTURE_DESC_BYTES, 1, f);
+    if (d->draw_batch_count)
+        fwrite(batches, sizeof(rive_cuda_draw_batch), d->draw_batch_count, f);
+    if (v2)
+    {
+        const uint32_t a[6] = {d->atlas_texture_width,   d->atlas_texture_height,
+                               d->atlas_content_width,   d->atlas_content_height,
+                               d->atlas_fill_batch_count, d->atlas_stroke_batch_count};
+        fwrite(a, sizeof(a), 1, f);
+        const uint32_t na = d->atlas_fill_batch_count + d->atlas_stroke_batch_count;
+        if (na)
+            fwrite(atlas, sizeof(rive_cuda_atlas_batch), na, f);
+    }
+}
+
+#endif /* RIVE_CAPTURE_FORMAT_H */

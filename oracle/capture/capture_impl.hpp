@@ -13,6 +13,7 @@
 #include "rive/renderer/gpu.hpp"
 
 #include "rive_cuda.h"
+#include "capture_format.h"
 
 #include <cstdio>
 #include <cstdlib>
@@ -51,6 +52,7 @@ struct FlushRecord
 {
     rive_cuda_flush_desc desc;
     std::vector<rive_cuda_draw_batch> batches;
+    std::vector<rive_cuda_atlas_batch> atlasBatches; // fills, then strokes
 };
 
 class CaptureImpl : public RenderContextNULL
@@ -134,6 +136,10 @@ public:
         m_gradTextureHeight = height;
     }
 
+    // PlatformFeatures::alwaysFeatherToAtlas (gpu.hpp:156-158): every
+    // feathered draw renders through the feather atlas, whatever its radius.
+    void setAlwaysFeatherToAtlas(bool on) { m_platformFeatures.alwaysFeatherToAtlas = on; }
+
     void flush(const FlushDescriptor& d) override
     {
         FlushRecord rec;
@@ -187,6 +193,27 @@ public:
             }
         }
         o.draw_batch_count = static_cast<uint32_t>(rec.batches.size());
+        o.atlas_texture_width = d.featherAtlasTextureWidth;
+        o.atlas_texture_height = d.featherAtlasTextureHeight;
+        o.atlas_content_width = d.featherAtlasContentWidth;
+        o.atlas_content_height = d.featherAtlasContentHeight;
+        o.atlas_fill_batch_count = static_cast<uint32_t>(d.featherAtlasFillBatchCount);
+        o.atlas_stroke_batch_count = static_cast<uint32_t>(d.featherAtlasStrokeBatchCount);
+        auto add_atlas = [&](const AtlasDrawBatch* b, size_t n) {
+            for (size_t i = 0; i < n; ++i)
+            {
+                rive_cuda_atlas_batch a;
+                a.scissor[0] = b[i].scissor.left;
+                a.scissor[1] = b[i].scissor.top;
+                a.scissor[2] = b[i].scissor.right;
+                a.scissor[3] = b[i].scissor.bottom;
+                a.patch_count = b[i].patchCount;
+                a.base_patch = b[i].basePatch;
+                rec.atlasBatches.push_back(a);
+            }
+        };
+        add_atlas(d.featherAtlasFillBatches, d.featherAtlasFillBatchCount);
+        add_atlas(d.featherAtlasStrokeBatches, d.featherAtlasStrokeBatchCount);
         flushes.push_back(std::move(rec));
     }
 
@@ -224,7 +251,10 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
         return false;
     // Seven buffer kinds, or eight when the frame has interior triangles.
     const uint32_t kinds = impl.buffers[7].empty() ? 7u : 8u;
-    uint32_t head[4] = {0x31504352u /*RCP1*/, width, height, kinds};
+    bool v2 = false;
+    for (const FlushRecord& r : impl.flushes)
+        v2 = v2 || rive_capture_flush_has_atlas(&r.desc);
+    uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, width, height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const uint8_t zeros[8] = {};
     for (uint32_t k = 0; k < kinds; ++k)
@@ -238,11 +268,7 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
     uint32_t nf = static_cast<uint32_t>(impl.flushes.size());
     fwrite(&nf, sizeof(nf), 1, f);
     for (const FlushRecord& r : impl.flushes)
-    {
-        fwrite(&r.desc, sizeof(r.desc), 1, f);
-        if (!r.batches.empty())
-            fwrite(r.batches.data(), sizeof(rive_cuda_draw_batch), r.batches.size(), f);
-    }
+        rive_capture_write_flush(f, &r.desc, r.batches.data(), r.atlasBatches.data(), v2);
     fclose(f);
     return true;
 }

@@ -100,6 +100,7 @@ int replay(const char* rcbPath, const char* outPath)
     Span<const uint8_t> blobs(data.data() + sizeof(h) + h.commandBytes, h.blobBytes);
     CaptureImpl* impl = nullptr;
     std::unique_ptr<RenderContext> ctx = CaptureImpl::Make(&impl);
+    impl->setAlwaysFeatherToAtlas((h.flags & RIVE_SCENE_FLAG_FEATHER_ATLAS) != 0);
     rcp<RenderTarget> target(impl->makeRenderTarget(h.width, h.height));
     ctx->beginFrame(scene_frame(h.width, h.height, h.clearColor, h.ditherMode, h.flags));
     {
@@ -194,6 +195,7 @@ int replay_frame(const char* rcsPath, const char* kArg, const char* outPath)
     }
     CaptureImpl* impl = nullptr;
     std::unique_ptr<RenderContext> ctx = CaptureImpl::Make(&impl);
+    impl->setAlwaysFeatherToAtlas((head[5] & RIVE_SCENE_FLAG_FEATHER_ATLAS) != 0);
     rcp<RenderTarget> target(impl->makeRenderTarget(head[1], head[2]));
     cmd::ResourceTable table;
     ctx->beginFrame(scene_frame(head[1], head[2], head[3], head[4], head[5]));

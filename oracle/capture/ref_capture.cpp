@@ -14,12 +14,12 @@
  * Usage: ref_capture <scene.bin> <capture.bin>
  *
  * Capture file layout (little-endian):
- *   u32 magic 'RCP1', u32 width, u32 height, u32 buffer_kinds (7, or 8 when
- *   the frame has interior triangles)
+ *   u32 magic 'RCP1' ('RCP2' when the frame renders into the feather atlas),
+ *   u32 width, u32 height, u32 buffer_kinds (7, or 8 when the frame has
+ *   interior triangles or atlas blits)
  *   buffer_kinds x { u64 bytes, bytes of data, zero pad to 8 }  in rive_cuda.h order
  *   u32 flush_count
- *   flush_count x { rive_cuda_flush_desc (draw_batches = 0),
- *                   rive_cuda_draw_batch[draw_batch_count] }
+ *   flush_count x { the flush (capture_format.h) }
  */
 #include "capture_impl.hpp"
 #include "scene_replay.hpp"
@@ -44,13 +44,14 @@ int main(int argc, char** argv)
         return fail("cannot read scene");
     CaptureImpl* impl = nullptr;
     std::unique_ptr<RenderContext> ctx = CaptureImpl::Make(&impl);
+    rive_scene_header hdr;
+    memcpy(&hdr, scene.data(), sizeof(hdr));
+    impl->setAlwaysFeatherToAtlas((hdr.flags & RIVE_SCENE_FLAG_FEATHER_ATLAS) != 0);
     const char* err = replay_scene(ctx.get(), scene, [&](uint32_t w, uint32_t h) {
         return rcp<RenderTarget>(impl->makeRenderTarget(w, h));
     });
     if (err)
         return fail(err);
-    rive_scene_header hdr;
-    memcpy(&hdr, scene.data(), sizeof(hdr));
 
     if (!write_capture(argv[2], *impl, hdr.width, hdr.height))
         return fail("cannot open output");

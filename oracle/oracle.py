@@ -39,7 +39,11 @@ class FlushDesc(ctypes.Structure):
             "first_tess_span", "grad_data_height", "tess_data_height",
             "grad_texture_height", "wireframe", "clockwise_fill_override",
             "has_triangle_vertices",
-            "draw_batch_count")] + [("draw_batches", ctypes.c_void_p)]
+            "draw_batch_count")] + [("draw_batches", ctypes.c_void_p)] + [
+        (n, ctypes.c_uint32) for n in (
+            "atlas_texture_width", "atlas_texture_height", "atlas_content_width",
+            "atlas_content_height", "atlas_fill_batch_count",
+            "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p)]
 
 
 class OracleBuffers(ctypes.Structure):
@@ -82,7 +86,12 @@ def make_desc(flush):
     batches = np.ascontiguousarray(flush.batches, dtype=np.uint32)
     d.draw_batch_count = len(batches)
     d.draw_batches = batches.ctypes.data if len(batches) else None
-    return d, batches
+    # rive_cuda_atlas_batch: u16 scissor[4], u32 patch_count, u32 base_patch
+    # (the capture's (n, 4) uint32 rows have the same bytes).
+    atlas = np.ascontiguousarray(getattr(flush, "atlas", np.zeros((0, 4), np.uint32)),
+                                 dtype=np.uint32).reshape(-1, 4)
+    d.atlas_batches = atlas.ctypes.data if len(atlas) else None
+    return d, (batches, atlas)
 
 
 def make_buffers(cap):

@@ -129,6 +129,7 @@ static void build_inverse_feather_table(void);
 #define OUTER_INDEX_COUNT (OUTER_SEGMENT_SPAN * 12 + 15 * 3)
 #define DRAW_TYPE_OUTER_CURVE_PATCHES 2u
 #define DRAW_TYPE_INTERIOR_TRIANGULATION 3u
+#define DRAW_TYPE_FEATHER_ATLAS_BLIT 4u
 
 /* Sub-pixel precision of the rasteriser (Vulkan minimum is 4 bits; desktop
  * parts use 8). */
@@ -1542,6 +1543,8 @@ typedef struct
     uint32_t features;
     int32_t bx0, by0, bx1, by1; /* pixel bbox, inclusive-exclusive */
     int interior; /* an interior-triangulation triangle (DRAW_INTERIOR_TRIANGLES) */
+    int blit;     /* a featherAtlasBlit triangle: coverage sampled from the atlas */
+    int negate;   /* an atlas fill triangle that faced away: coverage negated */
 } tri_rec;
 
 static inline int64_t snap(float v)
@@ -1966,7 +1969,209 @@ typedef struct
     const uint8_t* grad;
     uint32_t granularity;
     float ditherScale, ditherBias;
+    /* The feather atlas the flush rendered first (fp16 values held as
+     * floats), atlasW x atlasH texels; NULL without atlas draws. */
+    const float* atlas;
+    int atlasW, atlasH;
 } frag_ctx;
+
+/* find_paint_color (draw_path.vert:431-496, evaluated per fragment): the
+ * paint's colour at the pixel centre with its alpha multiplied by `coverage`,
+ * premultiplied unless advanced blending wants it straight. */
+static void paint_color(const frag_ctx* fc,
+                        uint32_t paintType,
+                        const uint32_t* paint,
+                        const float* aux,
+                        float fragX,
+                        float fragY,
+                        float coverage,
+                        int unmultiplied,
+                        float color[4])
+{
+    if (paintType == SOLID_COLOR_PAINT_TYPE)
+    {
+        uint32_t c = paint[1];
+        color[0] = (float)(c & 0xffu) / 255.f;
+        color[1] = (float)((c >> 8) & 0xffu) / 255.f;
+        color[2] = (float)((c >> 16) & 0xffu) / 255.f;
+        color[3] = (float)(c >> 24) / 255.f;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+            for (int k = 0; k < 4; ++k)
+                color[k] *= coverage;
+        }
+        else
+            color[3] *= coverage;
+    }
+    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE ||
+             paintType == RADIAL_GRADIENT_PAINT_TYPE)
+    {
+        float pm[4] = {aux[0], aux[1], aux[2], aux[3]};
+        f2 pc = add2(mat_mul(pm, (f2){fragX, fragY}), (f2){aux[4], aux[5]});
+        float gradientSpan = aux[6];
+        float spanB = gradientSpan > .9f ? 2.f : aux[7];
+        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pc.x
+                                                          : sqrtf(dot2(pc, pc));
+        /* GLSL clamp() is min(max(t, 0), 1); GPUs evaluate min/max with
+         * IEEE minNum/maxNum, so a NaN coordinate (a degenerate gradient,
+         * whose paint matrix the front end writes as NaN) clamps to 0. */
+        t = fminf(fmaxf(t, 0.f), 1.f);
+        float x = spanB > 1.f
+                      ? (1.f - 1.f / GRAD_TEXTURE_WIDTH) * t + (.5f / GRAD_TEXTURE_WIDTH)
+                      : (1.f / GRAD_TEXTURE_WIDTH) * t + spanB;
+        float row = u2f(paint[1]);
+        sample_grad(fc->grad, fc->d->grad_data_height,
+                    fc->d->grad_texture_height ? fc->d->grad_texture_height
+                                               : fc->d->grad_data_height,
+                    x, row, color);
+        color[3] *= coverage;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+        }
+    }
+    else
+    {
+        /* Clip-update paint outside ENABLE_CLIPPING draws nothing sensible;
+         * the reference leaves v_paint zero. */
+        color[0] = color[1] = color[2] = color[3] = 0.f;
+    }
+}
+
+/* min_component of find_clip_rect_coverage_distances (common.glsl:376-400)
+ * at the pixel centre. */
+static float clip_rect_distance(const float* aux, float fragX, float fragY)
+{
+    float cm[4] = {aux[8], aux[9], aux[10], aux[11]};
+    f2 ct = {aux[12], aux[13]};
+    f2 aaw = {fabsf(cm[0]) + fabsf(cm[2]), fabsf(cm[1]) + fabsf(cm[3])};
+    float cr[4];
+    if (aaw.x != 0.f && aaw.y != 0.f)
+    {
+        f2 r = {1.f / aaw.x, 1.f / aaw.y};
+        f2 cc = add2(mat_mul(cm, (f2){fragX, fragY}), ct);
+        cr[0] = cc.x * r.x + r.x + .5f;
+        cr[1] = cc.y * r.y + r.y + .5f;
+        cr[2] = -cc.x * r.x + r.x + .5f;
+        cr[3] = -cc.y * r.y + r.y + .5f;
+    }
+    else
+    {
+        cr[0] = cr[2] = ct.x;
+        cr[1] = cr[3] = ct.y;
+    }
+    return minf(minf(cr[0], cr[1]), minf(cr[2], cr[3]));
+}
+
+/* The feather atlas sampled at atlas pixel coordinates (x, y): the linear
+ * filter with clamp-to-edge addressing of the atlas sampler
+ * (draw_mesh.frag:89-97), texel centres at half-integers. Addresses clamp to
+ * the atlas content, the texels the atlas pass wrote. */
+static float atlas_sample(const frag_ctx* fc, float x, float y)
+{
+    if (!fc->atlas || fc->atlasW <= 0 || fc->atlasH <= 0)
+        return 0.f;
+    const float u = x - .5f, v = y - .5f;
+    if (!(u == u) || !(v == v))
+        return 0.f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float wu = u - fu, wv = v - fv;
+    const float cu = fminf(fmaxf(fu, -1.f), (float)fc->atlasW);
+    const float cv = fminf(fmaxf(fv, -1.f), (float)fc->atlasH);
+    const int iu = (int)cu, iv = (int)cv;
+    const int u0 = iu < 0 ? 0 : (iu > fc->atlasW - 1 ? fc->atlasW - 1 : iu);
+    const int u1 = iu + 1 < 0 ? 0 : (iu + 1 > fc->atlasW - 1 ? fc->atlasW - 1 : iu + 1);
+    const int v0 = iv < 0 ? 0 : (iv > fc->atlasH - 1 ? fc->atlasH - 1 : iv);
+    const int v1 = iv + 1 < 0 ? 0 : (iv + 1 > fc->atlasH - 1 ? fc->atlasH - 1 : iv + 1);
+    const float* a = fc->atlas;
+    const size_t W = (size_t)fc->atlasW;
+    const float t00 = a[v0 * W + u0], t10 = a[v0 * W + u1];
+    const float t01 = a[v1 * W + u0], t11 = a[v1 * W + u1];
+    const float top = t00 + (t10 - t00) * wu;
+    const float bot = t01 + (t11 - t01) * wu;
+    return top + (bot - top) * wv;
+}
+
+/* One fragment of a featherAtlasBlit draw (draw_mesh.frag:60-225 with
+ * FEATHER_ATLAS_BLIT): the coverage is the atlas texel the pixel maps to,
+ * clamped to [0, 1], cut by the clip rect and the clip; the paint is blended
+ * straight into the colour plane (the coverage plane is left as it is). */
+static void blit_fragment(const frag_ctx* fc,
+                          const tri_rec* t,
+                          float atlasX,
+                          float atlasY,
+                          int px,
+                          int py,
+                          pls_pixel* pls)
+{
+    const uint32_t features = t->features;
+    const uint32_t pathID = t->pathID;
+    const uint32_t* paint =
+        (const uint32_t*)fc->b->paints + 2 * ((size_t)fc->d->first_paint + pathID);
+    const float* aux =
+        (const float*)fc->b->paint_aux + 32 * ((size_t)fc->d->first_paint_aux + pathID);
+    const uint32_t paintType = paint[0] & 0xfu;
+    const float fragX = (float)px + .5f, fragY = (float)py + .5f;
+    float coverage = clampf(atlas_sample(fc, atlasX, atlasY), 0.f, 1.f);
+    if (features & SF_CLIP_RECT)
+        coverage = minf(maxf(clip_rect_distance(aux, fragX, fragY), 0.f), coverage);
+    if (features & SF_CLIPPING)
+    {
+        uint32_t clipIDBits = (paintType == CLIP_UPDATE_PAINT_TYPE ? paint[1] : paint[0]) >> 16;
+        uint16_t clipID = id_bits_to_f16(clipIDBits, fc->granularity);
+        if (clipID != 0)
+        {
+            uint16_t clipContentID = (uint16_t)(pls->clip >> 16);
+            float clipCoverage = clipContentID == clipID ? h2f((uint16_t)(pls->clip & 0xffffu))
+                                                         : 0.f;
+            clipCoverage = maxf(clipCoverage, 0.f);
+            coverage = minf(coverage, clipCoverage);
+        }
+    }
+    const int unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
+    float color[4];
+    paint_color(fc, paintType, paint, aux, fragX, fragY, 1.f, unmultiplied, color);
+    float dst[4];
+    for (int k = 0; k < 4; ++k)
+        dst[k] = (float)pls->color[k] / 255.f;
+    if (unmultiplied)
+    {
+        uint32_t blendMode = (paint[0] >> 4) & 0xfu;
+        if (blendMode != BLEND_SRC_OVER &&
+            ((int)blendMode < BLEND_MODE_HUE || (features & SF_HSL_BLEND_MODES)))
+        {
+            float rgb[3];
+            oracle_advanced_blend(color, dst, (int)blendMode, rgb);
+            color[0] = rgb[0];
+            color[1] = rgb[1];
+            color[2] = rgb[2];
+        }
+        color[3] *= coverage;
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    else
+    {
+        for (int k = 0; k < 4; ++k)
+            color[k] *= coverage;
+    }
+    if ((features & SF_DITHER) && color[3] != 0.f)
+    {
+        float n = ign(fragX, fragY, fc->ditherScale, fc->ditherBias);
+        color[0] += n;
+        color[1] += n;
+        color[2] += n;
+    }
+    const float a = color[3];
+    for (int k = 0; k < 4; ++k)
+        pls->color[k] = unorm8(dst[k] * (1.f - a) + color[k]);
+}
 
 /* One fragment of draw_raster_order_path.frag:14-238. */
 static void fragment(const frag_ctx* fc,
@@ -2096,86 +2301,11 @@ static void fragment(const frag_ctx* fc,
         }
     }
     if ((features & SF_CLIP_RECT))
-    {
-        /* find_clip_rect_coverage_distances (common.glsl:376-400) at the
-         * pixel centre. */
-        float cm[4] = {aux[8], aux[9], aux[10], aux[11]};
-        f2 ct = {aux[12], aux[13]};
-        f2 aaw = {fabsf(cm[0]) + fabsf(cm[2]), fabsf(cm[1]) + fabsf(cm[3])};
-        float cr[4];
-        if (aaw.x != 0.f && aaw.y != 0.f)
-        {
-            f2 r = {1.f / aaw.x, 1.f / aaw.y};
-            f2 cc = add2(mat_mul(cm, (f2){fragX, fragY}), ct);
-            cr[0] = cc.x * r.x + r.x + .5f;
-            cr[1] = cc.y * r.y + r.y + .5f;
-            cr[2] = -cc.x * r.x + r.x + .5f;
-            cr[3] = -cc.y * r.y + r.y + .5f;
-        }
-        else
-        {
-            cr[0] = cr[2] = ct.x;
-            cr[1] = cr[3] = ct.y;
-        }
-        float m = minf(minf(cr[0], cr[1]), minf(cr[2], cr[3]));
-        coverage = clampf(m, 0.f, coverage);
-    }
+        coverage = clampf(clip_rect_distance(aux, fragX, fragY), 0.f, coverage);
 
     int unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    if (paintType == SOLID_COLOR_PAINT_TYPE)
-    {
-        uint32_t c = paint[1];
-        color[0] = (float)(c & 0xffu) / 255.f;
-        color[1] = (float)((c >> 8) & 0xffu) / 255.f;
-        color[2] = (float)((c >> 16) & 0xffu) / 255.f;
-        color[3] = (float)(c >> 24) / 255.f;
-        if (!unmultiplied)
-        {
-            color[0] *= color[3];
-            color[1] *= color[3];
-            color[2] *= color[3];
-            for (int k = 0; k < 4; ++k)
-                color[k] *= coverage;
-        }
-        else
-            color[3] *= coverage;
-    }
-    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE ||
-             paintType == RADIAL_GRADIENT_PAINT_TYPE)
-    {
-        float pm[4] = {aux[0], aux[1], aux[2], aux[3]};
-        f2 pc = add2(mat_mul(pm, (f2){fragX, fragY}), (f2){aux[4], aux[5]});
-        float gradientSpan = aux[6];
-        float spanB = gradientSpan > .9f ? 2.f : aux[7];
-        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pc.x
-                                                          : sqrtf(dot2(pc, pc));
-        /* GLSL clamp() is min(max(t, 0), 1); GPUs evaluate min/max with
-         * IEEE minNum/maxNum, so a NaN coordinate (a degenerate gradient,
-         * whose paint matrix the front end writes as NaN) clamps to 0. */
-        t = fminf(fmaxf(t, 0.f), 1.f);
-        float x = spanB > 1.f
-                      ? (1.f - 1.f / GRAD_TEXTURE_WIDTH) * t + (.5f / GRAD_TEXTURE_WIDTH)
-                      : (1.f / GRAD_TEXTURE_WIDTH) * t + spanB;
-        float row = u2f(paint[1]);
-        sample_grad(fc->grad, fc->d->grad_data_height,
-                    fc->d->grad_texture_height ? fc->d->grad_texture_height
-                                               : fc->d->grad_data_height,
-                    x, row, color);
-        color[3] *= coverage;
-        if (!unmultiplied)
-        {
-            color[0] *= color[3];
-            color[1] *= color[3];
-            color[2] *= color[3];
-        }
-    }
-    else
-    {
-        /* Clip-update paint outside ENABLE_CLIPPING draws nothing sensible;
-         * the reference leaves v_paint zero. */
-        color[0] = color[1] = color[2] = color[3] = 0.f;
-    }
+    paint_color(fc, paintType, paint, aux, fragX, fragY, coverage, unmultiplied, color);
 
     float dst[4];
     if (covBufferID != vPathID)
@@ -2229,13 +2359,21 @@ static void fragment(const frag_ctx* fc,
         pls->color[k] = unorm8(color[k]);
 }
 
-static int setup_triangle(const vtx_out* a,
-                          const vtx_out* bb,
-                          const vtx_out* c,
-                          uint32_t features,
-                          int W,
-                          int H,
-                          tri_rec* t)
+/* Primitive assembly of one triangle into the pixel rectangle [x0, x1) x
+ * [y0, y1) (the viewport, or an atlas batch's scissor). Counterclockwise
+ * triangles are culled, except with `twoSided` (the atlas fill pipeline,
+ * CullFace::none, gpu.hpp:2076-2077): they are turned clockwise and marked
+ * `negate`, since a back-facing atlas fill subtracts its coverage. */
+static int setup_triangle_rect(const vtx_out* a,
+                               const vtx_out* bb,
+                               const vtx_out* c,
+                               uint32_t features,
+                               int x0,
+                               int y0,
+                               int x1,
+                               int y1,
+                               int twoSided,
+                               tri_rec* t)
 {
     if (a->discard || bb->discard || c->discard)
         return 0;
@@ -2255,6 +2393,23 @@ static int setup_triangle(const vtx_out* a,
     }
     int64_t area2 = (t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
                     (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]);
+    t->negate = 0;
+    if (area2 < 0 && twoSided)
+    {
+        int64_t tx = t->x[1], ty = t->y[1];
+        t->x[1] = t->x[2];
+        t->y[1] = t->y[2];
+        t->x[2] = tx;
+        t->y[2] = ty;
+        for (int k = 0; k < 4; ++k)
+        {
+            float tc = t->cov[1][k];
+            t->cov[1][k] = t->cov[2][k];
+            t->cov[2][k] = tc;
+        }
+        area2 = -area2;
+        t->negate = 1;
+    }
     if (area2 <= 0) /* counterclockwise faces are culled; degenerate drop */
         return 0;
     int64_t minx = t->x[0], maxx = t->x[0], miny = t->y[0], maxy = t->y[0];
@@ -2270,10 +2425,10 @@ static int setup_triangle(const vtx_out* a,
     int64_t bx1 = ((maxx - SUBPIXEL_ONE / 2) >> SUBPIXEL_BITS) + 1;
     int64_t by0 = (miny - SUBPIXEL_ONE / 2 + SUBPIXEL_ONE - 1) >> SUBPIXEL_BITS;
     int64_t by1 = ((maxy - SUBPIXEL_ONE / 2) >> SUBPIXEL_BITS) + 1;
-    if (bx0 < 0) bx0 = 0;
-    if (by0 < 0) by0 = 0;
-    if (bx1 > W) bx1 = W;
-    if (by1 > H) by1 = H;
+    if (bx0 < x0) bx0 = x0;
+    if (by0 < y0) by0 = y0;
+    if (bx1 > x1) bx1 = x1;
+    if (by1 > y1) by1 = y1;
     if (bx0 >= bx1 || by0 >= by1)
         return 0;
     t->bx0 = (int32_t)bx0;
@@ -2283,7 +2438,19 @@ static int setup_triangle(const vtx_out* a,
     t->pathID = v[0]->pathID;
     t->features = features;
     t->interior = 0;
+    t->blit = 0;
     return 1;
+}
+
+static int setup_triangle(const vtx_out* a,
+                          const vtx_out* bb,
+                          const vtx_out* c,
+                          uint32_t features,
+                          int W,
+                          int H,
+                          tri_rec* t)
+{
+    return setup_triangle_rect(a, bb, c, features, 0, 0, W, H, 0, t);
 }
 
 /* Edge function of edge a->b at point p, with the top-left tie rule for
@@ -2340,8 +2507,65 @@ static void raster_triangle_rows(const frag_ctx* fc,
                 covz = l0 * t->cov[0][2] + l1 * t->cov[1][2] + l2 * t->cov[2][2];
                 covw = l0 * t->cov[0][3] + l1 * t->cov[1][3] + l2 * t->cov[2][3];
             }
-            fragment(fc, t, covx, covy, covz, covw, px, py, pls + (size_t)py * W + px);
+            if (t->blit)
+                blit_fragment(fc, t, covx, covy, px, py, pls + (size_t)py * W + px);
+            else
+                fragment(fc, t, covx, covy, covz, covw, px, py, pls + (size_t)py * W + px);
             ++*frags;
+        }
+    }
+}
+
+/* The atlas pass's fragments of one triangle on rows [row0, row1)
+ * (render_atlas.glsl:58-77, the floating-point render target with fixed
+ * function blending): a fill adds its feathered coverage, negated when the
+ * triangle faced away, a stroke keeps the maximum; the R16F target rounds
+ * every blend result to fp16. */
+static void raster_atlas_rows(const tri_rec* t, int row0, int row1, float* atlas, int W)
+{
+    int y0 = t->by0 > row0 ? t->by0 : row0;
+    int y1 = t->by1 < row1 ? t->by1 : row1;
+    if (y0 >= y1)
+        return;
+    double area2 = (double)((t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
+                            (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]));
+    for (int py = y0; py < y1; ++py)
+    {
+        int64_t cy = ((int64_t)py << SUBPIXEL_BITS) + SUBPIXEL_ONE / 2;
+        for (int px = t->bx0; px < t->bx1; ++px)
+        {
+            int64_t cx = ((int64_t)px << SUBPIXEL_BITS) + SUBPIXEL_ONE / 2;
+            int64_t e0, e1, e2;
+            if (!edge_inside(t->x[1], t->y[1], t->x[2], t->y[2], cx, cy, &e0))
+                continue;
+            if (!edge_inside(t->x[2], t->y[2], t->x[0], t->y[0], cx, cy, &e1))
+                continue;
+            if (!edge_inside(t->x[0], t->y[0], t->x[1], t->y[1], cx, cy, &e2))
+                continue;
+            float l0 = (float)((double)e0 / area2);
+            float l1 = (float)((double)e1 / area2);
+            float l2 = (float)((double)e2 / area2);
+            float covx = l0 * t->cov[0][0] + l1 * t->cov[1][0] + l2 * t->cov[2][0];
+            float covy = l0 * t->cov[0][1] + l1 * t->cov[1][1] + l2 * t->cov[2][1];
+            float* texel = atlas + (size_t)py * W + px;
+            if (covy >= 0.f)
+            {
+                float c = eval_feathered_stroke(covx, covy);
+                *texel = h2f(oracle_f32_to_f16(maxf(*texel, c)));
+            }
+            else
+            {
+                float c = covx;
+                if (covy < FEATHER_COVERAGE_THRESHOLD)
+                {
+                    float covz = l0 * t->cov[0][2] + l1 * t->cov[1][2] + l2 * t->cov[2][2];
+                    float covw = l0 * t->cov[0][3] + l1 * t->cov[1][3] + l2 * t->cov[2][3];
+                    c = eval_feathered_fill(covx, covy, covz, covw);
+                }
+                if (t->negate)
+                    c = -c;
+                *texel = h2f(oracle_f32_to_f16(*texel + c));
+            }
         }
     }
 }
@@ -2356,6 +2580,112 @@ static int grow_tris(tri_rec** tris, size_t* cap, size_t n)
         return -4;
     *tris = nt;
     *cap = nc;
+    return 0;
+}
+
+/* The feather atlas pass (RenderContextGLImpl's atlas fill and stroke
+ * draws, render_context_gl_impl.cpp:2545-2590; render_atlas.glsl): every
+ * atlas batch's patches -- center-AA midpoint fans for fills, the border
+ * triangles of midpoint fans for strokes -- shaded as in the main pass, moved
+ * into the atlas by their path's atlas transform (PathData words 9-11,
+ * render_atlas.glsl:30-35), scissored, and rasterised into a cleared
+ * atlasContentWidth x atlasContentHeight fp16 target: fill batches first,
+ * then stroke batches, each in patch order. */
+static int render_atlas(const rive_cuda_flush_desc* d,
+                        const oracle_buffers* b,
+                        const uint32_t* tess,
+                        size_t tessTexels,
+                        float** out,
+                        int threads)
+{
+    *out = NULL;
+    const uint32_t nb = d->atlas_fill_batch_count + d->atlas_stroke_batch_count;
+    const int W = (int)d->atlas_content_width, H = (int)d->atlas_content_height;
+    if (W <= 0 || H <= 0)
+        return nb ? -1 : 0;
+    if (W > 16384 || H > 16384 || (nb && !d->atlas_batches))
+        return -1;
+    float* atlas = (float*)calloc((size_t)W * H, sizeof(float));
+    if (!atlas)
+        return -4;
+    size_t cap = 1024, n = 0;
+    tri_rec* tris = (tri_rec*)malloc(cap * sizeof(tri_rec));
+    if (!tris)
+    {
+        free(atlas);
+        return -4;
+    }
+    int rc = 0;
+    for (uint32_t bi = 0; bi < nb && rc == 0; ++bi)
+    {
+        const rive_cuda_atlas_batch* ab = &d->atlas_batches[bi];
+        const int fill = bi < d->atlas_fill_batch_count;
+        const patch_vertex* table = fill ? g_center : g_patch;
+        const uint16_t* idx = fill ? g_center_idx : g_patch_idx;
+        const int nv = fill ? CENTER_VERTEX_COUNT : PATCH_VERTEX_COUNT;
+        /* kMidpointFanCenterAAPatchIndexCount, kMidpointFanPatchBorderIndexCount */
+        const int ni = fill ? CENTER_INDEX_COUNT : 8 * 6;
+        int sx0 = ab->scissor[0], sy0 = ab->scissor[1];
+        int sx1 = ab->scissor[2] < W ? ab->scissor[2] : W;
+        int sy1 = ab->scissor[3] < H ? ab->scissor[3] : H;
+        for (uint32_t inst = ab->base_patch; inst < ab->base_patch + ab->patch_count && rc == 0;
+             ++inst)
+        {
+            vtx_out vo[OUTER_VERTEX_COUNT];
+            for (int k = 0; k < nv && rc == 0; ++k)
+            {
+                rc = patch_vertex_shader(d, b, tess, tessTexels, &table[k], inst, &vo[k]);
+                if (rc == 0 && !vo[k].discard)
+                {
+                    const float* path = path_record(d, b, vo[k].pathID);
+                    if (!path)
+                    {
+                        rc = -1;
+                        break;
+                    }
+                    /* vertexPosition * atlasTransform.x + atlasTransform.yz */
+                    vo[k].pos.x = vo[k].pos.x * path[9] + path[10];
+                    vo[k].pos.y = vo[k].pos.y * path[9] + path[11];
+                }
+            }
+            for (int k = 0; k < ni && rc == 0; k += 3)
+            {
+                rc = grow_tris(&tris, &cap, n);
+                if (rc == 0)
+                {
+                    int r = setup_triangle_rect(&vo[idx[k]], &vo[idx[k + 1]], &vo[idx[k + 2]], 0,
+                                                sx0, sy0, sx1, sy1, fill, &tris[n]);
+                    if (r < 0)
+                        rc = r;
+                    else
+                        n += (size_t)r;
+                }
+            }
+        }
+    }
+    if (rc == 0)
+    {
+        const int band = 8;
+        const int nbands = (H + band - 1) / band;
+#ifdef _OPENMP
+        if (threads > 0)
+            omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+        for (int bnd = 0; bnd < nbands; ++bnd)
+        {
+            int r0 = bnd * band, r1 = r0 + band < H ? r0 + band : H;
+            for (size_t i = 0; i < n; ++i)
+                raster_atlas_rows(&tris[i], r0, r1, atlas, W);
+        }
+    }
+    free(tris);
+    if (rc != 0)
+    {
+        free(atlas);
+        return rc;
+    }
+    *out = atlas;
     return 0;
 }
 
@@ -2384,11 +2714,22 @@ int oracle_draw(const rive_cuda_flush_desc* d,
 
     build_feather_table(); /* before any parallel region reads it */
 
+    /* The feather atlas first: the main pass's blits sample it. */
+    float* atlas = NULL;
+    {
+        int arc = render_atlas(d, b, tess, tessTexels, &atlas, threads);
+        if (arc != 0)
+            return arc;
+    }
+
     /* Vertex processing + primitive assembly, in primitive order. */
     size_t cap = 1024, n = 0;
     tri_rec* tris = (tri_rec*)malloc(cap * sizeof(tri_rec));
     if (!tris)
+    {
+        free(atlas);
         return -4;
+    }
     for (uint32_t bi = 0; bi < d->draw_batch_count; ++bi)
     {
         const rive_cuda_draw_batch* batch = &d->draw_batches[bi];
@@ -2484,6 +2825,49 @@ int oracle_draw(const rive_cuda_flush_desc* d,
                 }
             }
         }
+        else if (batch->draw_type == DRAW_TYPE_FEATHER_ATLAS_BLIT)
+        {
+            /* unpack_atlas_coverage_vertex (draw_path_common.glsl:822-844):
+             * the rectangle's TriangleVertex records are screen positions;
+             * each carries its atlas position, screen * scale + translate
+             * by the path's atlas transform, for the fragment to sample. */
+            if (batch->element_count % 3 ||
+                ((size_t)batch->base_element + batch->element_count) * 12 > b->triangles_bytes)
+                rc = -1;
+            const uint32_t* tv = (const uint32_t*)b->triangles;
+            for (uint32_t v = batch->base_element;
+                 v < batch->base_element + batch->element_count && rc == 0; v += 3)
+            {
+                vtx_out vo[3];
+                for (int k = 0; k < 3 && rc == 0; ++k)
+                {
+                    const uint32_t* r = tv + 3 * ((size_t)v + k);
+                    uint32_t pathID = r[2] & 0xffffu;
+                    const float* path = path_record(d, b, pathID);
+                    if (!path)
+                    {
+                        rc = -1;
+                        break;
+                    }
+                    vo[k].pos = (f2){u2f(r[0]), u2f(r[1])};
+                    vo[k].cov[0] = vo[k].pos.x * path[9] + path[10];
+                    vo[k].cov[1] = vo[k].pos.y * path[9] + path[11];
+                    vo[k].cov[2] = vo[k].cov[3] = 0.f;
+                    vo[k].pathID = pathID;
+                    vo[k].discard = 0;
+                }
+                if (rc == 0)
+                    rc = grow_tris(&tris, &cap, n);
+                if (rc == 0)
+                {
+                    int r = setup_triangle(&vo[0], &vo[1], &vo[2], features, W, H, &tris[n]);
+                    if (r < 0)
+                        rc = r;
+                    else if (r > 0)
+                        tris[n++].blit = 1;
+                }
+            }
+        }
         else
         {
             rc = -2;
@@ -2491,6 +2875,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
         if (rc != 0)
         {
             free(tris);
+            free(atlas);
             return rc;
         }
     }
@@ -2500,6 +2885,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     if (!pls)
     {
         free(tris);
+        free(atlas);
         return -4;
     }
     uint8_t clear[4];
@@ -2522,7 +2908,8 @@ int oracle_draw(const rive_cuda_flush_desc* d,
         memset(pls[i].scratch, 0, 4);
     }
 
-    frag_ctx fc = {d, b, grad, granularity, ditherScale, ditherBias};
+    frag_ctx fc = {d,          b,    grad, granularity, ditherScale, ditherBias, atlas,
+                   (int)d->atlas_content_width, (int)d->atlas_content_height};
     const int band = 8;
     const int nbands = (H + band - 1) / band;
     uint64_t frags = 0;
@@ -2545,6 +2932,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     g_stat_fragments = frags;
     free(pls);
     free(tris);
+    free(atlas);
     return 0;
 }
 

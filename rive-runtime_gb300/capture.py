@@ -4,7 +4,9 @@ of logical flushes (rive_cuda_flush_desc + rive_cuda_draw_batch[]).
 A capture is exactly what rive::gpu::RenderContext hands its RenderContextImpl
 for one frame (render_context.cpp:970-1010): the bytes written into the mapped
 path/paint/paintAux/contour/gradSpan/tessVertexSpan/flushUniform buffers, and
-one gpu::FlushDescriptor per logical flush.
+one gpu::FlushDescriptor per logical flush. A frame that renders into the
+feather atlas is an "RCP2" capture: each flush also carries the atlas sizes
+and its gpu::AtlasDrawBatch lists (gpu.hpp:827-833, 1361-1426).
 """
 from __future__ import annotations
 
@@ -14,6 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 CAPTURE_MAGIC = 0x31504352  # "RCP1"
+CAPTURE_MAGIC_V2 = 0x32504352  # "RCP2": with feather atlas batches
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
                 "grad_spans", "tess_spans", "triangles")
@@ -36,12 +39,23 @@ BATCH_FIELDS = ("draw_type", "element_count", "base_element", "shader_features",
                 "draw_contents", "shader_misc_flags", "first_blend_mode",
                 "barriers")
 BATCH_SIZE = 32
+# The atlas part of an RCP2 flush: these six u32 fields, then the atlas
+# batches (fill batches first), 16 bytes each: u16 scissor left, top, right,
+# bottom, u32 patch_count, u32 base_patch. Held per flush as an (n, 4) uint32
+# array: [left | top << 16, right | bottom << 16, patch_count, base_patch].
+ATLAS_FIELDS = ("atlas_texture_width", "atlas_texture_height", "atlas_content_width",
+                "atlas_content_height", "atlas_fill_batch_count", "atlas_stroke_batch_count")
 
 
 @dataclass
 class Flush:
     desc: dict
     batches: np.ndarray  # (n, 8) uint32
+    atlas: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.uint32))
+
+    @property
+    def has_atlas(self) -> bool:
+        return any(self.desc.get(k, 0) for k in ATLAS_FIELDS)
 
 
 @dataclass
@@ -61,8 +75,9 @@ class Capture:
 
 def parse(data: bytes) -> Capture:
     magic, w, h, nk = struct.unpack_from("<4I", data, 0)
-    if magic != CAPTURE_MAGIC:
+    if magic not in (CAPTURE_MAGIC, CAPTURE_MAGIC_V2):
         raise ValueError("not a flush capture")
+    v2 = magic == CAPTURE_MAGIC_V2
     off = 16
     cap = Capture(w, h)
     for k in range(nk):
@@ -79,14 +94,26 @@ def parse(data: bytes) -> Capture:
         nb = desc["draw_batch_count"]
         batches = np.frombuffer(data, dtype="<u4", count=nb * 8, offset=off).reshape(nb, 8).copy()
         off += nb * BATCH_SIZE
-        cap.flushes.append(Flush(desc, batches))
+        atlas = np.zeros((0, 4), np.uint32)
+        for k in ATLAS_FIELDS:
+            desc[k] = 0
+        if v2:
+            vals = struct.unpack_from("<6I", data, off)
+            off += 24
+            desc.update(zip(ATLAS_FIELDS, vals))
+            na = vals[4] + vals[5]
+            atlas = np.frombuffer(data, dtype="<u4", count=na * 4, offset=off).reshape(na, 4).copy()
+            off += na * 16
+        cap.flushes.append(Flush(desc, batches, atlas))
     return cap
 
 
 def serialize(cap: Capture) -> bytes:
     # Seven kinds, or eight when the frame has interior triangles.
     kinds = BUFFER_NAMES if cap.buffers.get("triangles") else BUFFER_NAMES[:7]
-    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC, cap.width, cap.height, len(kinds)))
+    v2 = any(f.has_atlas for f in cap.flushes)
+    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC_V2 if v2 else CAPTURE_MAGIC, cap.width,
+                                cap.height, len(kinds)))
     for name in kinds:
         b = cap.buffers.get(name, b"")
         out += struct.pack("<Q", len(b)) + b + bytes((8 - (len(b) & 7)) & 7)
@@ -97,4 +124,7 @@ def serialize(cap: Capture) -> bytes:
         out += DESC_STRUCT.pack(*[d[k] for k in DESC_FIELDS])
         out += bytes(DESC_SIZE - DESC_STRUCT.size)
         out += np.asarray(f.batches, dtype="<u4").tobytes()
+        if v2:
+            out += struct.pack("<6I", *[d.get(k, 0) for k in ATLAS_FIELDS])
+            out += np.asarray(f.atlas, dtype="<u4").reshape(-1, 4).tobytes()
     return bytes(out)

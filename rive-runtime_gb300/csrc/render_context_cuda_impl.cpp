@@ -195,6 +195,10 @@ void RenderContextCUDAImpl::resizeTessellationTexture(uint32_t width, uint32_t h
     note(rive_cuda_resize_tessellation_texture(m_ctx, width, height));
 }
 
+// The atlas lives in the flush's intermediates, sized per flush from
+// FlushDescriptor::featherAtlasContentWidth/Height; nothing to allocate here.
+void RenderContextCUDAImpl::resizeFeatherAtlasTexture(uint32_t, uint32_t) {}
+
 void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
 {
     rive_cuda_flush_desc o;
@@ -247,6 +251,31 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
     }
     o.draw_batch_count = static_cast<uint32_t>(batches.size());
     o.draw_batches = batches.empty() ? nullptr : batches.data();
+
+    // The feather atlas batches: fills, then strokes.
+    std::vector<rive_cuda_atlas_batch> atlas;
+    auto add_atlas = [&](const AtlasDrawBatch* b, size_t n) {
+        for (size_t i = 0; i < n; ++i)
+        {
+            rive_cuda_atlas_batch a;
+            a.scissor[0] = b[i].scissor.left;
+            a.scissor[1] = b[i].scissor.top;
+            a.scissor[2] = b[i].scissor.right;
+            a.scissor[3] = b[i].scissor.bottom;
+            a.patch_count = b[i].patchCount;
+            a.base_patch = b[i].basePatch;
+            atlas.push_back(a);
+        }
+    };
+    add_atlas(d.featherAtlasFillBatches, d.featherAtlasFillBatchCount);
+    add_atlas(d.featherAtlasStrokeBatches, d.featherAtlasStrokeBatchCount);
+    o.atlas_texture_width = d.featherAtlasTextureWidth;
+    o.atlas_texture_height = d.featherAtlasTextureHeight;
+    o.atlas_content_width = d.featherAtlasContentWidth;
+    o.atlas_content_height = d.featherAtlasContentHeight;
+    o.atlas_fill_batch_count = static_cast<uint32_t>(d.featherAtlasFillBatchCount);
+    o.atlas_stroke_batch_count = static_cast<uint32_t>(d.featherAtlasStrokeBatchCount);
+    o.atlas_batches = atlas.empty() ? nullptr : atlas.data();
 
     auto* target = static_cast<RenderTargetCUDA*>(d.renderTarget);
     note(rive_cuda_flush(m_ctx, &o, target->handle(), d.externalCommandBuffer));

@@ -17,14 +17,14 @@
 //   target->readPixels(rgba);   // or target->devicePixels() for zero-copy
 //
 // Supported: InterlockMode::rasterOrdering with midpoint-fan patches, the
-// center-AA midpoint fans of feathered fills and, for large fills the front
-// end triangulates, outer-curve patches plus interior triangles; i.e. fills
-// (nonzero, even-odd, clockwise), strokes with every join and cap, feathers
-// below the feather atlas's 32-pixel threshold (fills and strokes), linear and
-// radial gradients, clip paths (nested), clip rects, all blend modes, dither.
-// A flush that needs anything else (the feather atlas for larger feathers,
-// images, atomic/MSAA/clockwise interlock modes) is not rendered: flush()
-// records RIVE_CUDA_ERR_UNSUPPORTED in lastStatus().
+// center-AA midpoint fans of feathered fills, the feather atlas with its
+// blits and, for large fills the front end triangulates, outer-curve patches
+// plus interior triangles; i.e. fills (nonzero, even-odd, clockwise), strokes
+// with every join and cap, feathers of any radius (fills and strokes), linear
+// and radial gradients, clip paths (nested), clip rects, all blend modes,
+// dither. A flush that needs anything else (images, atomic/MSAA/clockwise
+// interlock modes) is not rendered: flush() records RIVE_CUDA_ERR_UNSUPPORTED
+// in lastStatus().
 #pragma once
 
 // texture.hpp first: render_context_impl.hpp destroys rcp<Texture> inline.
@@ -123,6 +123,12 @@ public:
 
     void resizeGradientTexture(uint32_t width, uint32_t height) override;
     void resizeTessellationTexture(uint32_t width, uint32_t height) override;
+    void resizeFeatherAtlasTexture(uint32_t width, uint32_t height) override;
+
+    // PlatformFeatures::alwaysFeatherToAtlas (gpu.hpp:156-158): render every
+    // feathered draw through the feather atlas (off by default: only blurs
+    // the front end scales to half resolution or less go there).
+    void setAlwaysFeatherToAtlas(bool on) { m_platformFeatures.alwaysFeatherToAtlas = on; }
 
     // FlushDescriptor::externalCommandBuffer, when set, is the cudaStream_t
     // to enqueue on; otherwise the context's own stream is used.

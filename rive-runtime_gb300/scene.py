@@ -53,6 +53,7 @@ LOCAL_HALF_EXTENT = 48.0
 
 DITHER_NONE, DITHER_IGN = 0, 1
 FLAG_TRIANGULATE = 1
+FLAG_FEATHER_ATLAS = 2  # every feather through the feather atlas (alwaysFeatherToAtlas)
 
 
 @dataclass
@@ -373,6 +374,28 @@ def feathered(seed: int = 33, width: int = 320, height: int = 256, n_paths: int 
     atlas (radius = 1.5 x feather x scale)."""
     sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=10,
                       p_fill=0.7, p_clip=0.15, scale_range=(0.5, 2.0))
+    rng = np.random.default_rng(seed + 1)
+    for op, a, b, _ in sc.cmds:
+        if op != CMD_DRAW_PATH:
+            continue
+        paint = sc.paints[b]
+        if rng.uniform() < p_feather:
+            paint.feather = float(rng.uniform(*feather_range))
+            if paint.style == STYLE_FILL:
+                sc.paths[a].fill_rule = FILL_CLOCKWISE
+    return sc
+
+
+def feathered_atlas(seed: int = 35, width: int = 384, height: int = 320, n_paths: int = 36,
+                    p_feather: float = 0.7, feather_range=(4.0, 40.0)) -> Scene:
+    """Wide feathers: the full-feature distributions with a share of the fills
+    and strokes feathered by up to 40 (radius = 1.5 x feather x scale, scale
+    0.5..2), so many reach the 32-pixel radius at which the reference renders
+    them through its feather atlas at half resolution or less
+    (draw.cpp:387-404), beside feathers drawn directly. Feathered fills are
+    clockwise, as the reference draws them."""
+    sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=10,
+                      p_fill=0.65, p_clip=0.15, scale_range=(0.5, 2.0))
     rng = np.random.default_rng(seed + 1)
     for op, a, b, _ in sc.cmds:
         if op != CMD_DRAW_PATH:

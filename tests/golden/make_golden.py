@@ -99,6 +99,29 @@ FEATHERED_SILVERS = {
 }
 
 
+# Wide feathers through the feather atlas (radius x scale >= 32 px; the
+# reference renders their coverage offscreen and blits it,
+# render_context.cpp:676-744, 2255-2345, 3515-3534), beside direct feathers.
+SCENES["feather_atlas_s35"] = lambda: scene.feathered_atlas(seed=35)
+# feathered_s33 again, every feather through the atlas
+# (PlatformFeatures::alwaysFeatherToAtlas): renders the same image as the
+# direct feathers of feathered_s33, within the image tolerance.
+SCENES["feathered_atlas_s33"] = lambda: _atlas_always(scene.feathered(seed=33))
+
+# Real frames whose wide feathers the reference front end sends through the
+# feather atlas (feathered draws kept).
+ATLAS_SILVERS = {
+    "silver_data_viz_f6": ("data_viz_demo", 6),
+    "silver_bankcard_f10": ("bankcard", 10),
+    "silver_rewards_atlas_f10": ("rewards_demo", 10),
+}
+
+
+def _atlas_always(sc):
+    sc.flags = scene.FLAG_FEATHER_ATLAS
+    return sc
+
+
 def _silver(stream, frame, keep_feathered=False):
     from rive_runtime_gb300 import sriv
     with open(os.path.join(SILVER_DIR, stream + ".sriv"), "rb") as f:
@@ -109,6 +132,8 @@ def _silver(stream, frame, keep_feathered=False):
 for _name, (_stream, _frame) in SILVERS.items():
     SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k))
 for _name, (_stream, _frame) in FEATHERED_SILVERS.items():
+    SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True))
+for _name, (_stream, _frame) in ATLAS_SILVERS.items():
     SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True))
 
 

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -2829,7 +2830,9 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
     {
         rive_cuda_flush_desc d = f->desc;
         d.draw_batches = nullptr;
-        put(&d, sizeof(d));
+        // The RCP1 flush record: the descriptor up to its draw_batches
+        // pointer (this front end plans no feather atlas).
+        put(&d, offsetof(rive_cuda_flush_desc, atlas_texture_width));
         if (!f->batches.empty())
             put(f->batches.data(), f->batches.size() * sizeof(rive_cuda_draw_batch));
     }
