@@ -359,7 +359,7 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
 #define RIVE_CUDA_NOALLOC_MAX_PATCHES 8192u /* 32 rows x 2048 vertices / 8 */
 #define RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS 64u
 #define RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES 1048576u
-#define RIVE_CUDA_NOALLOC_POOL_BYTES 42899456u /* about 40.9 MiB */
+#define RIVE_CUDA_NOALLOC_POOL_BYTES 42901504u /* about 40.9 MiB */
 int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* desc,
                                    const rive_cuda_device_buffers* buffers,
                                    void* target_pixels_device,
@@ -384,6 +384,11 @@ int rive_cuda_read_tess_texture(rive_cuda_context* ctx,
 int rive_cuda_read_grad_texture(rive_cuda_context* ctx,
                                 void* dst_host,
                                 size_t bytes);
+/* ... and the feather atlas the last flush rendered (fp16 texels,
+ * atlas_content_width per row). */
+int rive_cuda_read_atlas_texture(rive_cuda_context* ctx,
+                                 void* dst_host,
+                                 size_t bytes);
 
 /*
  * The tessellation pass's device functions evaluated on n host items (no

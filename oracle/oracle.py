@@ -66,7 +66,7 @@ def lib():
             build()
         _lib = ctypes.CDLL(LIB_PATH)
         for name in ("oracle_color_ramps", "oracle_tessellate", "oracle_draw",
-                     "oracle_flush", "oracle_tessellate_f64"):
+                     "oracle_flush", "oracle_tessellate_f64", "oracle_atlas"):
             getattr(_lib, name).restype = ctypes.c_int
         _lib.oracle_f32_to_f16.restype = ctypes.c_uint16
         _lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
@@ -145,6 +145,19 @@ def tessellate_f64(cap, fi=0):
                                        flags.ctypes.data_as(ctypes.c_void_p)),
            "tessellate_f64")
     return xy, flags
+
+
+def atlas(cap, fi=0, threads=0):
+    """The feather atlas logical flush `fi` renders (fp16 texels as float32,
+    atlas_content_height x atlas_content_width)."""
+    f = cap.flushes[fi]
+    d, _k1 = make_desc(f)
+    b, _k2 = make_buffers(cap)
+    h, w = int(f.desc["atlas_content_height"]), int(f.desc["atlas_content_width"])
+    out = np.zeros((max(h, 1), max(w, 1)), np.uint16)
+    _check(lib().oracle_atlas(ctypes.byref(d), ctypes.byref(b),
+                              out.ctypes.data_as(ctypes.c_void_p), int(threads)), "atlas")
+    return out[:h, :w].view(np.float16).astype(np.float32)
 
 
 def render(cap, threads=0, fb=None):

@@ -2967,6 +2967,35 @@ int oracle_flush(const rive_cuda_flush_desc* d,
     return rc;
 }
 
+/* The feather atlas of one logical flush (its tessellation, then the atlas
+ * pass) as fp16 texels, atlas_content_width x atlas_content_height. */
+int oracle_atlas(const rive_cuda_flush_desc* d,
+                 const oracle_buffers* b,
+                 uint16_t* out,
+                 int threads)
+{
+    build_patch_tables();
+    build_feather_table();
+    size_t tessTexels = (size_t)TESS_TEXTURE_WIDTH * (d->tess_data_height ? d->tess_data_height : 1);
+    uint32_t* tess = (uint32_t*)calloc(1, tessTexels * 16);
+    if (!tess)
+        return -4;
+    int rc = oracle_tessellate(d, b, tess);
+    float* atlas = NULL;
+    if (rc == 0)
+        rc = render_atlas(d, b, tess, (size_t)TESS_TEXTURE_WIDTH * d->tess_data_height, &atlas,
+                          threads);
+    if (rc == 0 && atlas)
+    {
+        const size_t n = (size_t)d->atlas_content_width * d->atlas_content_height;
+        for (size_t i = 0; i < n; ++i)
+            out[i] = oracle_f32_to_f16(atlas[i]);
+    }
+    free(atlas);
+    free(tess);
+    return rc;
+}
+
 /* ---- the shared fp32 elementary functions, for their accuracy test -------- */
 /* fn: 0 sin, 1 cos, 2 acos, 3 cube root. */
 int oracle_math_eval(int fn, const float* x, float* out, size_t n)

@@ -88,6 +88,13 @@ int oracle_flush(const rive_cuda_flush_desc* d,
                  uint8_t* fb,
                  int threads);
 
+/* The feather atlas pass of one logical flush (tessellation included) into
+ * out, atlas_content_width x atlas_content_height fp16 texels, row-major. */
+int oracle_atlas(const rive_cuda_flush_desc* d,
+                 const oracle_buffers* b,
+                 uint16_t* out,
+                 int threads);
+
 /* Counters of the last oracle_draw (triangles after culling, fragments). */
 void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);
 

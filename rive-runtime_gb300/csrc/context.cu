@@ -91,6 +91,16 @@ __global__ void raster_queue_feather_kernel(BatchTables B,
                                             const uint32_t* order,
                                             uint32_t* cursor,
                                             uint32_t tiles);
+// The feather atlas pass at 8, 16 and 32 pixel tiles (kernels_raster.cu).
+__global__ void raster_atlas8_kernel(BatchTables B, const TriRecord* tris,
+                                     const uint32_t* sortedSlots, const uint2* ranges,
+                                     uint32_t firstTile);
+__global__ void raster_atlas_kernel(BatchTables B, const TriRecord* tris,
+                                    const uint32_t* sortedSlots, const uint2* ranges,
+                                    uint32_t firstTile);
+__global__ void raster_atlas32_kernel(BatchTables B, const TriRecord* tris,
+                                      const uint32_t* sortedSlots, const uint2* ranges,
+                                      uint32_t firstTile);
 __global__ void tile_order_keys_kernel(uint32_t tiles,
                                        const uint2* ranges,
                                        uint32_t* keys,
@@ -233,6 +243,7 @@ struct rive_cuda_context
     int smCount = 0;
     DeviceBuffer queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor;
     DeviceBuffer pathGrids, gridWinding, gridEdge, gridCounters;
+    DeviceBuffer atlas; // the batch's feather atlases (fp16 texels)
     uint32_t gridCapacity = 0;
     uint32_t* hGridCounters = nullptr; // pinned: cells asked, winding entries
     rive_cuda_flush_stats stats = {};
@@ -251,7 +262,7 @@ struct rive_cuda_context
     cudaEvent_t openEvent = nullptr;
     int openStage = -1;
     // Last flush's texture extents (for debug read-backs).
-    size_t lastTessBytes = 0, lastGradBytes = 0;
+    size_t lastTessBytes = 0, lastGradBytes = 0, lastAtlasBytes = 0;
 };
 
 // A batch captured as a CUDA graph (rive_cuda_graph_*): it owns every
@@ -261,7 +272,8 @@ struct rive_cuda_graph
     rive_cuda_context* ctx = nullptr;
     DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
         scanTemp, sortTemp, ranges, error, featherPlanes, pathGrids, gridWinding, gridEdge,
-        gridCounters, queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor;
+        gridCounters, queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor,
+        atlas;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -385,6 +397,7 @@ int setup_list(uint32_t drawType)
            : drawType == DRAW_OUTER_CURVE_PATCHES ? 1
            : drawType == DRAW_INTERIOR_TRIANGULATION ? 2
            : drawType == DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES ? 3
+           : drawType == DRAW_FEATHER_ATLAS_BLIT ? 2 // a rectangle of triangle vertices
                                                              : -1;
 }
 constexpr uint32_t kTrianglesPerItem[kSetupLists] = {
@@ -393,7 +406,22 @@ constexpr uint32_t kTrianglesPerItem[kSetupLists] = {
 // Items (patch instances or triangles) of a draw batch.
 uint32_t batch_items(const rive_cuda_draw_batch& b)
 {
-    return b.draw_type == DRAW_INTERIOR_TRIANGULATION ? b.element_count / 3 : b.element_count;
+    return b.draw_type == DRAW_INTERIOR_TRIANGULATION || b.draw_type == DRAW_FEATHER_ATLAS_BLIT
+               ? b.element_count / 3
+               : b.element_count;
+}
+
+// Atlas batch i of a flush: fill batches come first.
+bool atlas_is_fill(const rive_cuda_flush_desc* d, uint32_t i) { return i < d->atlas_fill_batch_count; }
+uint32_t atlas_batch_count(const rive_cuda_flush_desc* d)
+{
+    return d->atlas_fill_batch_count + d->atlas_stroke_batch_count;
+}
+// Whether the flush renders a feather atlas (content and batches).
+bool has_atlas(const rive_cuda_flush_desc* d)
+{
+    return atlas_batch_count(d) != 0 && d->atlas_content_width != 0 &&
+           d->atlas_content_height != 0;
 }
 
 // Host-side checks of one flush; counts its triangle slots.
@@ -442,7 +470,8 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         // ENABLE_FEATHER: feathered strokes draw in midpoint-fan batches,
         // feathered fills in center-AA midpoint-fan batches.
         if ((b.shader_features & SF_FEATHER) && b.draw_type != DRAW_MIDPOINT_FAN_PATCHES &&
-            b.draw_type != DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES)
+            b.draw_type != DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES &&
+            b.draw_type != DRAW_FEATHER_ATLAS_BLIT)
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
                              "feathered draws of draw type %u not supported", b.draw_type);
         if (b.shader_misc_flags & ~MISC_CLOCKWISE_FILL)
@@ -467,6 +496,29 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         }
         slots += (uint64_t)batch_items(b) * kTrianglesPerItem[list];
     }
+    // The feather atlas: its size, and every batch within the tessellation
+    // texture and the atlas.
+    const uint32_t na = atlas_batch_count(d);
+    if (na)
+    {
+        if (!d->atlas_batches)
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "atlas_batches is NULL");
+        if (d->atlas_content_width > 16384 || d->atlas_content_height > 16384)
+            return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "feather atlas too large");
+        for (uint32_t i = 0; i < na; ++i)
+        {
+            const rive_cuda_atlas_batch& a = d->atlas_batches[i];
+            if (((uint64_t)a.base_patch + a.patch_count) * kPatchSegmentSpan >
+                (uint64_t)d->tess_data_height * kTessTextureWidth)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "atlas batch %u reads past the tessellation texture", i);
+            if (a.scissor[0] > a.scissor[2] || a.scissor[1] > a.scissor[3])
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "atlas batch %u has an inverted scissor", i);
+            slots += (uint64_t)a.patch_count *
+                     (atlas_is_fill(d, i) ? kCenterPatchTriangleCount : kPatchTriangleCount);
+        }
+    }
     return RIVE_CUDA_OK;
 }
 
@@ -479,6 +531,13 @@ struct BatchLayout
     int tileLog2 = kTileLog2;
     uint32_t segCount[kSetupLists] = {}, items[kSetupLists] = {};
     uint32_t gradSpans = 0, tessSpans = 0, tiles = 0, slots = 0, paths = 0;
+    // Feather atlases: one more scene per flush that renders one (after the
+    // n main scenes), with its tiles after all the main ones.
+    uint32_t atlasScenes = 0, mainTiles = 0;
+    uint64_t atlasTexels = 0;
+    std::vector<uint32_t> atlasScene; // per flush: its atlas scene, or ~0u
+    std::vector<uint64_t> atlasTexel0; // per flush: its first atlas texel
+    uint32_t scenes() const { return n + atlasScenes; }
     bool feather = false; // some batch draws with ENABLE_FEATHER
     // Interior tiles as winding records for this batch: midpoint-fan patches
     // then take fanStride slots (their 24 triangles and a winding slot).
@@ -511,6 +570,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     const uint32_t ts = 1u << L.tileLog2;
     L.tessRow0.resize(n);
     L.gradRow0.resize(n);
+    L.atlasScene.assign(n, ~0u);
+    L.atlasTexel0.assign(n, 0);
     uint64_t slots = 0, tiles = 0, gradSpans = 0, tessSpans = 0, paths = 0;
     uint64_t segs[kSetupLists] = {}, items[kSetupLists] = {};
     for (uint32_t i = 0; i < n; ++i)
@@ -534,7 +595,7 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             const int list = setup_list(db.draw_type);
             segs[list] += 1;
             items[list] += k;
-            if (db.shader_features & SF_FEATHER)
+            if ((db.shader_features & SF_FEATHER) || db.draw_type == DRAW_FEATHER_ATLAS_BLIT)
                 L.feather = true;
         }
         L.tessRow0[i] = L.tessRows;
@@ -547,6 +608,31 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         tessSpans += d->tess_span_count;
         paths += d->path_count;
     }
+    L.mainTiles = (uint32_t)std::min<uint64_t>(tiles, 0xffffffffu);
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const rive_cuda_flush_desc* d = in[i].d;
+        if (!has_atlas(d))
+            continue;
+        L.atlasScene[i] = n + L.atlasScenes++;
+        L.atlasTexel0[i] = L.atlasTexels;
+        L.atlasTexels += (uint64_t)d->atlas_content_width * d->atlas_content_height;
+        tiles += (uint64_t)((d->atlas_content_width + ts - 1) / ts) *
+                 ((d->atlas_content_height + ts - 1) / ts);
+        L.feather = true;
+        for (uint32_t b = 0; b < atlas_batch_count(d); ++b)
+        {
+            const uint32_t k = d->atlas_batches[b].patch_count;
+            if (!k)
+                continue;
+            const int list = atlas_is_fill(d, b) ? 3 : 0;
+            segs[list] += 1;
+            items[list] += k;
+        }
+    }
+    if (L.scenes() > 65535)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                         "a batch holds at most 65535 flushes and feather atlases");
     // Winding records for the interior tiles of fills: on unless turned off
     // or the batch feathers (feathered batches keep their fans).
     L.winding = ctx->windingTiles && !L.feather && items[0] > 0;
@@ -579,13 +665,14 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     L.tessSpans = (uint32_t)tessSpans;
     L.tiles = (uint32_t)tiles;
     L.slots = (uint32_t)slots;
+    const uint32_t ns = L.scenes();
     L.oScenes = 0;
-    L.oGradBase = align16(L.oScenes + sizeof(FlushParams) * n);
-    L.oTessBase = align16(L.oGradBase + 4 * (n + 1));
-    L.oTileBase = align16(L.oTessBase + 4 * (n + 1));
-    L.oSceneTiles = align16(L.oTileBase + 4 * (n + 1));
-    L.oPathBase = align16(L.oSceneTiles + 8 * n);
-    size_t o = align16(L.oPathBase + 4 * (n + 1));
+    L.oGradBase = align16(L.oScenes + sizeof(FlushParams) * ns);
+    L.oTessBase = align16(L.oGradBase + 4 * (ns + 1));
+    L.oTileBase = align16(L.oTessBase + 4 * (ns + 1));
+    L.oSceneTiles = align16(L.oTileBase + 4 * (ns + 1));
+    L.oPathBase = align16(L.oSceneTiles + 8 * ns);
+    size_t o = align16(L.oPathBase + 4 * (ns + 1));
     for (int l = 0; l < kSetupLists; ++l)
     {
         L.oSegments[l] = o;
@@ -614,6 +701,7 @@ struct Scratch
     uint2* ranges = nullptr;
     uint32_t* error = nullptr;
     float4* featherPlanes = nullptr; // 2 per slot, only with center-AA patches
+    uint16_t* atlas = nullptr;       // the batch's feather atlases, fp16 texels
     // Winding grids (only when the batch draws interior tiles as winding
     // records).
     PathGrid* pathGrids = nullptr;
@@ -695,6 +783,12 @@ BatchTables write_tables(rive_cuda_context* ctx,
         P.triangleVertices = (const uint32_t*)rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE];
         P.triangleVertexCount = (uint32_t)std::min<size_t>(rb.bytes[RIVE_CUDA_BUFFER_TRIANGLE] / 12,
                                                            0xffffffffu);
+        if (L.atlasScene[i] != ~0u)
+        {
+            P.atlas = S.atlas + L.atlasTexel0[i];
+            P.atlasW = d->atlas_content_width;
+            P.atlasH = d->atlas_content_height;
+        }
 
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
@@ -716,18 +810,63 @@ BatchTables write_tables(rive_cuda_context* ctx,
             segs[l][segAcc[l]] = PatchSegment{
                 i, db.base_element,
                 db.shader_features |
-                    ((db.shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u),
-                slotAcc};
+                    ((db.shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u) |
+                    (db.draw_type == DRAW_FEATHER_ATLAS_BLIT ? FEATURE_ATLAS_BLIT : 0u),
+                slotAcc, 0u, 0xffffffffu};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += k;
             slotAcc += k * (l == 0 ? L.fanStride : kTrianglesPerItem[l]);
         }
     }
-    gradBase[L.n] = gAcc;
-    tessBase[L.n] = tAcc;
-    tileBase[L.n] = tileAcc;
-    pathBase[L.n] = pathAcc;
+    // The feather atlases: per flush that renders one, a scene whose canvas
+    // is the atlas content and whose set-up segments are the atlas batches
+    // (center-AA fans for fills, midpoint fans for strokes; fills first),
+    // each clipped to its scissor. Its slots follow all the main ones.
+    for (uint32_t i = 0; i < L.n; ++i)
+    {
+        const uint32_t j = L.atlasScene[i];
+        if (j == ~0u)
+            continue;
+        const rive_cuda_flush_desc* d = in[i].d;
+        FlushParams& A = scenes[j];
+        A = scenes[i];
+        A.width = d->atlas_content_width;
+        A.height = d->atlas_content_height;
+        A.fb = nullptr;
+        A.loadClear = 0;
+        A.gradSpanCount = 0;
+        A.tessSpanCount = 0;
+        A.atlasMode = 1;
+        const uint32_t ts = 1u << L.tileLog2;
+        A.tilesX = (A.width + ts - 1) / ts;
+        gradBase[j] = gAcc;
+        tessBase[j] = tAcc;
+        tileBase[j] = tileAcc;
+        pathBase[j] = pathAcc;
+        sceneTiles[j] = make_uint2(tileAcc, A.tilesX);
+        tileAcc += A.tilesX * ((A.height + ts - 1) / ts);
+        for (uint32_t b = 0; b < atlas_batch_count(d); ++b)
+        {
+            const rive_cuda_atlas_batch& ab = d->atlas_batches[b];
+            if (!ab.patch_count)
+                continue;
+            const int l = atlas_is_fill(d, b) ? 3 : 0;
+            segs[l][segAcc[l]] = PatchSegment{
+                j, ab.base_patch, SF_FEATHER, slotAcc,
+                (uint32_t)ab.scissor[0] | ((uint32_t)ab.scissor[1] << 16),
+                (uint32_t)ab.scissor[2] | ((uint32_t)ab.scissor[3] << 16)};
+            segBase[l][segAcc[l]] = itemAcc[l];
+            ++segAcc[l];
+            itemAcc[l] += ab.patch_count;
+            slotAcc += ab.patch_count * (l == 0 ? L.fanStride : kTrianglesPerItem[l]);
+        }
+    }
+    const uint32_t ns = L.scenes();
+    gradBase[ns] = gAcc;
+    tessBase[ns] = tAcc;
+    tileBase[ns] = tileAcc;
+    pathBase[ns] = pathAcc;
     for (int l = 0; l < kSetupLists; ++l)
         segBase[l][segAcc[l]] = itemAcc[l];
 
@@ -745,7 +884,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
         B.segCount[l] = segAcc[l];
         B.totalItems[l] = itemAcc[l];
     }
-    B.sceneCount = L.n;
+    B.sceneCount = ns;
+    B.mainTiles = L.mainTiles;
     B.tileLog2 = L.tileLog2;
     B.featherPlanes = S.featherPlanes;
     B.fanSlotStride = L.fanStride;
@@ -772,8 +912,8 @@ int enqueue_front(rive_cuda_context* ctx,
                   const Scratch& S,
                   cudaStream_t stream)
 {
-    scene_uniforms_kernel<<<(L.n + 127) / 128, 128, 0, stream>>>(
-        const_cast<FlushParams*>(B.scenes), L.n);
+    scene_uniforms_kernel<<<(L.scenes() + 127) / 128, 128, 0, stream>>>(
+        const_cast<FlushParams*>(B.scenes), L.scenes());
     // Texels no span covers are never sampled; zero them so the gradient
     // texture is deterministic.
     CK(cudaMemsetAsync(S.grad, 0, L.gradBytes(), stream));
@@ -920,35 +1060,37 @@ int launch_raster(rive_cuda_context* ctx,
     {
         // The work queue: tiles sorted by bin entries, heaviest first, taken
         // in turn by a persistent grid of resident CTAs.
-        tile_order_keys_kernel<<<(L.tiles + 255) / 256, 256, 0, stream>>>(L.tiles, ranges, S.qKeys,
-                                                                        S.qVals);
+        tile_order_keys_kernel<<<(L.mainTiles + 255) / 256, 256, 0, stream>>>(L.mainTiles, ranges,
+                                                                            S.qKeys, S.qVals);
         cub::DoubleBuffer<uint32_t> k(S.qKeys, S.qKeysAlt), v(S.qVals, S.qValsAlt);
         size_t tb = S.qTempBytes;
-        CK(cub::DeviceRadixSort::SortPairs(S.qTemp, tb, k, v, (int)L.tiles, 0, 32, stream));
+        CK(cub::DeviceRadixSort::SortPairs(S.qTemp, tb, k, v, (int)L.mainTiles, 0, 32, stream));
         CK(cudaMemsetAsync(S.qCursor, 0, 4, stream));
         const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->queuePad[L.feather] : 0;
         const int per = ctx->rasterCtasPerSm > 0 ? ctx->rasterCtasPerSm : ctx->queueCtas[L.feather];
         const uint32_t grid =
-            std::min<uint32_t>(L.tiles, (uint32_t)std::max(per * ctx->smCount, 1));
+            std::min<uint32_t>(L.mainTiles, (uint32_t)std::max(per * ctx->smCount, 1));
         (L.feather ? raster_queue_feather_kernel : raster_queue_kernel)<<<grid, 256, dyn, stream>>>(
-            B, tris, sortedSlots, ranges, v.Current(), S.qCursor, L.tiles);
+            B, tris, sortedSlots, ranges, v.Current(), S.qCursor, L.mainTiles);
         return RIVE_CUDA_OK;
     }
     if (L.tileLog2 == 3)
     {
         const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][0] : 0;
-        (L.feather ? raster_tile8_feather_kernel : raster_tile8_kernel)<<<L.tiles, 64, dyn, stream>>>(
+        (L.feather ? raster_tile8_feather_kernel : raster_tile8_kernel)<<<L.mainTiles, 64, dyn,
+                                                                           stream>>>(
             B, tris, sortedSlots, ranges);
     }
     else if (L.tileLog2 == 5)
     {
         (L.feather ? raster_tile32_feather_kernel : raster_tile32_kernel)<<<
-            L.tiles, 1024, kRaster32SmemBytes, stream>>>(B, tris, sortedSlots, ranges);
+            L.mainTiles, 1024, kRaster32SmemBytes, stream>>>(B, tris, sortedSlots, ranges);
     }
     else
     {
         const size_t dyn = ctx->rasterCtasPerSm > 0 ? ctx->rasterPad[L.feather][1] : 0;
-        (L.feather ? raster_tile_feather_kernel : raster_tile_kernel)<<<L.tiles, 256, dyn, stream>>>(
+        (L.feather ? raster_tile_feather_kernel : raster_tile_kernel)<<<L.mainTiles, 256, dyn,
+                                                                         stream>>>(
             B, tris, sortedSlots, ranges);
     }
     return RIVE_CUDA_OK;
@@ -992,6 +1134,20 @@ int enqueue_back(rive_cuda_context* ctx,
         sortedSlots = v.Current();
     }
     stage_begin(ctx, RIVE_CUDA_STAGE_RASTER, stream);
+    if (L.tiles > L.mainTiles)
+    {
+        // The feather atlases first: the main raster's blits sample them.
+        const uint32_t atlasTiles = L.tiles - L.mainTiles;
+        if (L.tileLog2 == 3)
+            raster_atlas8_kernel<<<atlasTiles, 64, 0, stream>>>(B, S.tris, sortedSlots, S.ranges,
+                                                                L.mainTiles);
+        else if (L.tileLog2 == 5)
+            raster_atlas32_kernel<<<atlasTiles, 1024, 0, stream>>>(B, S.tris, sortedSlots,
+                                                                   S.ranges, L.mainTiles);
+        else
+            raster_atlas_kernel<<<atlasTiles, 256, 0, stream>>>(B, S.tris, sortedSlots, S.ranges,
+                                                                L.mainTiles);
+    }
     int rc = launch_raster(ctx, L, B, S, S.tris, sortedSlots, S.ranges, stream);
     stage_end(ctx, stream);
     if (rc)
@@ -1052,6 +1208,8 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
     if (L.items[3])
         CK(ctx->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
+    if (L.atlasTexels)
+        CK(ctx->atlas.reserve((size_t)L.atlasTexels * 2));
     if (L.winding)
     {
         // The cell pool starts at four cells per tile of the batch and grows
@@ -1079,6 +1237,9 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->scanTemp.reserve(scanBytes));
     ctx->lastTessBytes = (size_t)kTessTextureWidth * std::max(in[0].d->tess_data_height, 1u) * 16;
     ctx->lastGradBytes = (size_t)kGradTextureWidth * std::max(in[0].d->grad_data_height, 1u) * 4;
+    ctx->lastAtlasBytes = L.atlasScene[0] != ~0u ? (size_t)in[0].d->atlas_content_width *
+                                                       in[0].d->atlas_content_height * 2
+                                                 : 0;
 
     Scratch S;
     S.tables = (uint8_t*)ctx->dTables.ptr;
@@ -1086,6 +1247,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.grad = (uchar4*)ctx->grad.ptr;
     S.tris = (TriRecord*)ctx->tris.ptr;
     S.featherPlanes = L.items[3] ? (float4*)ctx->featherPlanes.ptr : nullptr;
+    S.atlas = L.atlasTexels ? (uint16_t*)ctx->atlas.ptr : nullptr;
     S.counts = (uint32_t*)ctx->tileCounts.ptr;
     S.masks = (uint8_t*)ctx->tileMasks.ptr;
     S.offsets = (uint32_t*)ctx->offsets.ptr;
@@ -1162,6 +1324,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     ctx->stats.tiles = L.tiles;
     ctx->stats.kernel_launches = 1 + (L.gradSpans ? 1 : 0) + (L.tessSpans ? 1 : 0) +
                                  (L.slots ? 1 : 0) + (pairs ? 3 : 0) + 1 +
+                                 (L.tiles > L.mainTiles ? 1 : 0) +
                                  (L.winding ? 3 + (L.tessSpans ? 1 : 0) + 1 : 0);
     return RIVE_CUDA_OK;
 }
@@ -1238,7 +1401,7 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
                             &ctx->pathGrids, &ctx->gridWinding, &ctx->gridEdge,
                             &ctx->gridCounters, &ctx->queueKeys, &ctx->queueVals,
                             &ctx->queueKeysAlt, &ctx->queueValsAlt, &ctx->queueTemp,
-                            &ctx->queueCursor})
+                            &ctx->queueCursor, &ctx->atlas})
         b->release();
     ctx->hTables.release();
     if (ctx->hGridCounters)
@@ -1507,7 +1670,7 @@ void graph_free(rive_cuda_graph* g)
                             &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes,
                             &g->pathGrids, &g->gridWinding, &g->gridEdge, &g->gridCounters,
                             &g->queueKeys, &g->queueVals, &g->queueKeysAlt, &g->queueValsAlt,
-                            &g->queueTemp, &g->queueCursor})
+                            &g->queueTemp, &g->queueCursor, &g->atlas})
         b->release();
     if (g->hError)
         cudaFreeHost(g->hError);
@@ -1537,6 +1700,8 @@ int graph_build(rive_cuda_context* ctx,
     CK(g->offsets.reserve((size_t)L.slots * 4 + 4));
     if (L.items[3])
         CK(g->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
+    if (L.atlasTexels)
+        CK(g->atlas.reserve((size_t)L.atlasTexels * 2));
     CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(g->error.reserve(4));
     const bool queue = ctx->rasterQueue && L.tileLog2 == 4;
@@ -1559,6 +1724,7 @@ int graph_build(rive_cuda_context* ctx,
     S.grad = (uchar4*)g->grad.ptr;
     S.tris = (TriRecord*)g->tris.ptr;
     S.featherPlanes = L.items[3] ? (float4*)g->featherPlanes.ptr : nullptr;
+    S.atlas = L.atlasTexels ? (uint16_t*)g->atlas.ptr : nullptr;
     S.counts = (uint32_t*)g->counts.ptr;
     S.masks = (uint8_t*)g->masks.ptr;
     S.offsets = (uint32_t*)g->offsets.ptr;
@@ -1814,6 +1980,18 @@ int rive_cuda_read_tess_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->tess.ptr, std::min(bytes, ctx->lastTessBytes), cudaMemcpyDeviceToHost));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_read_atlas_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
+{
+    if (!ctx || !dst)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const size_t n = std::min(bytes, ctx->lastAtlasBytes);
+    if (n)
+        CK(cudaMemcpy(dst, ctx->atlas.ptr, n, cudaMemcpyDeviceToHost));
     return RIVE_CUDA_OK;
 }
 

@@ -185,6 +185,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                     "gradient texture height %u exceeds the no-allocation limit %u rows",
                     d->grad_data_height, RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS);
+    if (d->atlas_fill_batch_count || d->atlas_stroke_batch_count)
+        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                    "the feather atlas needs the allocating path (rive_cuda_flush_device)");
     uint64_t instances = 0;
     bool feather = false; // some batch draws with ENABLE_FEATHER
     for (uint32_t i = 0; i < d->draw_batch_count; ++i)
@@ -299,7 +302,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                                       b.shader_features | ((b.shader_misc_flags & MISC_CLOCKWISE_FILL)
                                                                ? FEATURE_CLOCKWISE_FILL
                                                                : 0u),
-                                      instAcc * kPatchTriangleCount};
+                                      instAcc * kPatchTriangleCount, 0u, 0xffffffffu};
         segBase[segCount] = instAcc;
         ++segCount;
         instAcc += b.element_count;
@@ -323,6 +326,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     B.segCount[0] = segCount;
     B.totalItems[0] = instAcc;
     B.sceneCount = 1;
+    B.mainTiles = tiles;
     B.tileLog2 = kTileLog2;
     B.totalGradSpans = d->grad_span_count;
     B.totalTessSpans = d->tess_span_count;

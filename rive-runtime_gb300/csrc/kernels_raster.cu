@@ -683,6 +683,15 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
     float2 mo = mat_mul(M, origin);
     o.pos = make_float2(__fadd_rn(__fadd_rn(mo.x, offset.x), translate.x),
                         __fadd_rn(__fadd_rn(mo.y, offset.y), translate.y));
+    if (kFeather && P.atlasMode)
+    {
+        // render_atlas.glsl:30-35: into the feather atlas by the path's atlas
+        // transform (PathData words 9-11: scale, translate x, translate y).
+        const uint4 r2 = path[2];
+        const float sc = __uint_as_float(r2.y);
+        o.pos = make_float2(__fadd_rn(__fmul_rn(o.pos.x, sc), __uint_as_float(r2.z)),
+                            __fadd_rn(__fmul_rn(o.pos.y, sc), __uint_as_float(r2.w)));
+    }
     o.cov = cov;
     o.pathID = pathID;
     return true;
@@ -774,44 +783,69 @@ __device__ __forceinline__ int4 unpack_bbox(uint4 meta)
 // integer area), clips the pixel box to the target, and builds the edge
 // functions and coverage planes. Returns false for a triangle that draws
 // nothing (bb stays empty).
+// `clip` bounds the pixels (an atlas batch's scissor; the canvas always).
+// `twoSided` keeps counterclockwise triangles (the atlas fill pipeline culls
+// nothing, gpu.hpp:2076-2077): they are turned clockwise and marked
+// FEATURE_ATLAS_NEGATE, since a back-facing atlas fill subtracts coverage.
 __device__ bool setup_triangle(const FlushParams& P,
                                const VertexOut& A,
-                               const VertexOut& B,
-                               const VertexOut& C,
+                               const VertexOut& Bv,
+                               const VertexOut& Cv,
                                uint32_t features,
                                uint32_t scene,
                                TriRecord& T,
                                int4& bb,
                                float4* featherPlanes = nullptr,
-                               float2 zwA = {}, float2 zwB = {}, float2 zwC = {})
+                               float2 zwA = {}, float2 zwB = {}, float2 zwC = {},
+                               int4 clip = make_int4(0, 0, 0x7fffffff, 0x7fffffff),
+                               bool twoSided = false)
 {
     bb = make_int4(0, 0, 0, 0);
-    if (A.discard || B.discard || C.discard)
+    if (A.discard || Bv.discard || Cv.discard)
         return false;
-    float m = fmaxf(fmaxf(fmaxf(fabsf(A.pos.x), fabsf(A.pos.y)), fmaxf(fabsf(B.pos.x), fabsf(B.pos.y))),
-                    fmaxf(fabsf(C.pos.x), fabsf(C.pos.y)));
+    float m = fmaxf(fmaxf(fmaxf(fabsf(A.pos.x), fabsf(A.pos.y)), fmaxf(fabsf(Bv.pos.x), fabsf(Bv.pos.y))),
+                    fmaxf(fabsf(Cv.pos.x), fabsf(Cv.pos.y)));
     if (!(m < 32768.f)) // NaN or outside the exact snapping range
     {
         if (!isnan(m))
             atomicOr(P.error, ERR_COORD_RANGE);
         return false;
     }
+    const VertexOut* pB = &Bv;
+    const VertexOut* pC = &Cv;
+    int X1 = __float2int_rn(Bv.pos.x * 256.f), Y1 = __float2int_rn(Bv.pos.y * 256.f);
+    int X2 = __float2int_rn(Cv.pos.x * 256.f), Y2 = __float2int_rn(Cv.pos.y * 256.f);
     const int X0 = __float2int_rn(A.pos.x * 256.f), Y0 = __float2int_rn(A.pos.y * 256.f);
-    const int X1 = __float2int_rn(B.pos.x * 256.f), Y1 = __float2int_rn(B.pos.y * 256.f);
-    const int X2 = __float2int_rn(C.pos.x * 256.f), Y2 = __float2int_rn(C.pos.y * 256.f);
-    // Exact twice-area in 1/65536 px^2: counterclockwise culled, degenerate
-    // dropped.
-    const long long area2 =
-        (long long)(X1 - X0) * (Y2 - Y0) - (long long)(X2 - X0) * (Y1 - Y0);
+    // Exact twice-area in 1/65536 px^2: counterclockwise culled (or turned,
+    // when two-sided), degenerate dropped.
+    long long area2 = (long long)(X1 - X0) * (Y2 - Y0) - (long long)(X2 - X0) * (Y1 - Y0);
+    if (area2 < 0 && twoSided)
+    {
+        int t = X1;
+        X1 = X2;
+        X2 = t;
+        t = Y1;
+        Y1 = Y2;
+        Y2 = t;
+        pB = &Cv;
+        pC = &Bv;
+        const float2 z = zwB;
+        zwB = zwC;
+        zwC = z;
+        area2 = -area2;
+        features |= FEATURE_ATLAS_NEGATE;
+    }
     if (area2 <= 0)
         return false;
+    const VertexOut& B = *pB;
+    const VertexOut& C = *pC;
     const int mnx = min(min(X0, X1), X2), mxx = max(max(X0, X1), X2);
     const int mny = min(min(Y0, Y1), Y2), mxy = max(max(Y0, Y1), Y2);
     // Pixels k whose centres (256 k + 128) lie in [min, max].
-    const int bx0 = max(-((-(mnx - 128)) >> 8), 0);
-    const int bx1 = min(((mxx - 128) >> 8) + 1, (int)P.width);
-    const int by0 = max(-((-(mny - 128)) >> 8), 0);
-    const int by1 = min(((mxy - 128) >> 8) + 1, (int)P.height);
+    const int bx0 = max(max(-((-(mnx - 128)) >> 8), 0), clip.x);
+    const int bx1 = min(min(((mxx - 128) >> 8) + 1, (int)P.width), clip.z);
+    const int by0 = max(max(-((-(mny - 128)) >> 8), 0), clip.y);
+    const int by1 = min(min(((mxy - 128) >> 8) + 1, (int)P.height), clip.w);
     if (bx0 >= bx1 || by0 >= by1)
         return false;
     const float s = 1.f / 256.f;
@@ -1248,12 +1282,15 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             // tiles are counted once the grid knows its edge tiles.
             const bool fan = kWinding && kList == 0 && wg && t >= 16;
             TriRecord T;
+            const int4 clip = make_int4((int)(S.scissorLT & 0xffffu), (int)(S.scissorLT >> 16),
+                                        (int)(S.scissorRB & 0xffffu), (int)(S.scissorRB >> 16));
             if (sok[w] && setup_triangle(P, sv[w][ia], sv[w][ib], sv[w][ic],
                                          S.features | (fan ? FEATURE_FAN_DEFERRED : 0u), S.scene,
                                          T, bb, planes ? planes + 2 * (size_t)(slot0 + t) : nullptr,
                                          planes ? sZW[w][kFeather ? ia : 0] : float2{},
                                          planes ? sZW[w][kFeather ? ib : 0] : float2{},
-                                         planes ? sZW[w][kFeather ? ic : 0] : float2{}))
+                                         planes ? sZW[w][kFeather ? ic : 0] : float2{}, clip,
+                                         kCenter && P.atlasMode))
             {
                 tris[slot0 + t] = T;
                 e[0] = T.e0;
@@ -1370,6 +1407,22 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
                 break;
             }
             const uint4* path = P.paths + 4 * (size_t)(P.firstPath + pathID);
+            if (S.features & FEATURE_ATLAS_BLIT)
+            {
+                // unpack_atlas_coverage_vertex (draw_path_common.glsl:822-844):
+                // a screen-space rectangle corner, carrying its atlas position
+                // (screen * scale + translate by the path's atlas transform)
+                // for the raster to sample.
+                const uint4 r2 = path[2];
+                const float sc = __uint_as_float(r2.y);
+                const float x = __uint_as_float(r[0]), y = __uint_as_float(r[1]);
+                v[k].pos = make_float2(x, y);
+                v[k].cov = make_float2(__fadd_rn(__fmul_rn(x, sc), __uint_as_float(r2.z)),
+                                       __fadd_rn(__fmul_rn(y, sc), __uint_as_float(r2.w)));
+                v[k].pathID = pathID;
+                v[k].discard = false;
+                continue;
+            }
             const uint4 r0 = path[0], r1 = path[1];
             const float4 M = make_float4(__uint_as_float(r0.x), __uint_as_float(r0.y),
                                          __uint_as_float(r0.z), __uint_as_float(r0.w));
@@ -2092,6 +2145,81 @@ struct Pixel
     uint32_t pendFrags; // fragments of the pending path so far (saturating)
 };
 
+// min_component of find_clip_rect_coverage_distances (common.glsl:376-400)
+// at the pixel centre.
+__device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32_t pathID, float fx,
+                                                    float fy)
+{
+    const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+    float4 cm = aux[2], ct = aux[3];
+    float awx = fabsf(cm.x) + fabsf(cm.z), awy = fabsf(cm.y) + fabsf(cm.w);
+    float d0, d1, d2, d3;
+    if (awx != 0.f && awy != 0.f)
+    {
+        float rx = 1.f / awx, ry = 1.f / awy;
+        float cx = cm.x * fx + cm.z * fy + ct.x;
+        float cy = cm.y * fx + cm.w * fy + ct.y;
+        d0 = cx * rx + rx + .5f;
+        d1 = cy * ry + ry + .5f;
+        d2 = -cx * rx + rx + .5f;
+        d3 = -cy * ry + ry + .5f;
+    }
+    else
+    {
+        d0 = d2 = ct.x;
+        d1 = d3 = ct.y;
+    }
+    return fminf(fminf(d0, d1), fminf(d2, d3));
+}
+
+// find_paint_color (draw_path.vert:431-496, evaluated at the pixel): the
+// paint's colour with its alpha multiplied by `coverage`, premultiplied
+// unless advanced blending wants it straight.
+__device__ __forceinline__ void paint_color(const FlushParams& P, uint32_t paintX, uint32_t paintY,
+                                            uint32_t pathID, float fx, float fy, float coverage,
+                                            bool unmultiplied, float color[4])
+{
+    const uint32_t paintType = paintX & 0xfu;
+    if (paintType == SOLID_COLOR_PAINT_TYPE)
+    {
+        unpack_rgba8(paintY, color);
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+            for (int k = 0; k < 4; ++k)
+                color[k] *= coverage;
+        }
+        else
+            color[3] *= coverage;
+    }
+    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE || paintType == RADIAL_GRADIENT_PAINT_TYPE)
+    {
+        const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+        float4 pm = aux[0], pt = aux[1];
+        float pcx = pm.x * fx + pm.z * fy + pt.x;
+        float pcy = pm.y * fx + pm.w * fy + pt.y;
+        float spanB = pt.z > .9f ? 2.f : pt.w;
+        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pcx : sqrtf(pcx * pcx + pcy * pcy);
+        t = clamp01(t);
+        float x = spanB > 1.f ? (1.f - 1.f / kGradTextureWidth) * t + (.5f / kGradTextureWidth)
+                              : (1.f / kGradTextureWidth) * t + spanB;
+        sample_grad(P, x, __uint_as_float(paintY), color);
+        color[3] *= coverage;
+        if (!unmultiplied)
+        {
+            color[0] *= color[3];
+            color[1] *= color[3];
+            color[2] *= color[3];
+        }
+    }
+    else
+    {
+        color[0] = color[1] = color[2] = color[3] = 0.f;
+    }
+}
+
 // The colour / clip write of the last fragment of a path at this pixel.
 //
 // draw_raster_order_path.frag writes the colour (or clip) plane on every
@@ -2159,70 +2287,11 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
             coverage = (s.clip >> 16) == clipBits ? fminf(h2f(s.clip & 0xffffu), coverage) : 0.f;
     }
     if (features & SF_CLIP_RECT)
-    {
-        const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
-        float4 cm = aux[2], ct = aux[3];
-        float awx = fabsf(cm.x) + fabsf(cm.z), awy = fabsf(cm.y) + fabsf(cm.w);
-        float d0, d1, d2, d3;
-        if (awx != 0.f && awy != 0.f)
-        {
-            float rx = 1.f / awx, ry = 1.f / awy;
-            float cx = cm.x * fx + cm.z * fy + ct.x;
-            float cy = cm.y * fx + cm.w * fy + ct.y;
-            d0 = cx * rx + rx + .5f;
-            d1 = cy * ry + ry + .5f;
-            d2 = -cx * rx + rx + .5f;
-            d3 = -cy * ry + ry + .5f;
-        }
-        else
-        {
-            d0 = d2 = ct.x;
-            d1 = d3 = ct.y;
-        }
-        float m = fminf(fminf(d0, d1), fminf(d2, d3));
-        coverage = fminf(fmaxf(m, 0.f), coverage);
-    }
+        coverage = fminf(fmaxf(clip_rect_distance(P, pathID, fx, fy), 0.f), coverage);
 
     const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    if (paintType == SOLID_COLOR_PAINT_TYPE)
-    {
-        unpack_rgba8(paintY, color);
-        if (!unmultiplied)
-        {
-            color[0] *= color[3];
-            color[1] *= color[3];
-            color[2] *= color[3];
-            for (int k = 0; k < 4; ++k)
-                color[k] *= coverage;
-        }
-        else
-            color[3] *= coverage;
-    }
-    else if (paintType == LINEAR_GRADIENT_PAINT_TYPE || paintType == RADIAL_GRADIENT_PAINT_TYPE)
-    {
-        const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
-        float4 pm = aux[0], pt = aux[1];
-        float pcx = pm.x * fx + pm.z * fy + pt.x;
-        float pcy = pm.y * fx + pm.w * fy + pt.y;
-        float spanB = pt.z > .9f ? 2.f : pt.w;
-        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pcx : sqrtf(pcx * pcx + pcy * pcy);
-        t = clamp01(t);
-        float x = spanB > 1.f ? (1.f - 1.f / kGradTextureWidth) * t + (.5f / kGradTextureWidth)
-                              : (1.f / kGradTextureWidth) * t + spanB;
-        sample_grad(P, x, __uint_as_float(paintY), color);
-        color[3] *= coverage;
-        if (!unmultiplied)
-        {
-            color[0] *= color[3];
-            color[1] *= color[3];
-            color[2] *= color[3];
-        }
-    }
-    else
-    {
-        color[0] = color[1] = color[2] = color[3] = 0.f;
-    }
+    paint_color(P, paintX, paintY, pathID, fx, fy, coverage, unmultiplied, color);
 
     float dst[4];
     unpack_rgba8(s.color, dst);
@@ -2245,6 +2314,89 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
         color[1] += dither;
         color[2] += dither;
     }
+    s.color = pack_rgba8(color);
+}
+
+// The feather atlas at atlas pixel coordinates (x, y): the atlas sampler's
+// linear filter with clamp-to-edge addressing (draw_mesh.frag:89-97), texel
+// centres at half-integers, addresses clamped to the atlas content; then
+// clamped to [0, 1].
+__device__ __noinline__ float atlas_coverage(const FlushParams& P, float x, float y)
+{
+    const uint16_t* __restrict__ a = P.atlas;
+    const int W = (int)P.atlasW, H = (int)P.atlasH;
+    if (!a || W <= 0 || H <= 0)
+        return 0.f;
+    const float u = __fsub_rn(x, .5f), v = __fsub_rn(y, .5f);
+    if (!(u == u) || !(v == v))
+        return 0.f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float wu = __fsub_rn(u, fu), wv = __fsub_rn(v, fv);
+    const int iu = (int)fminf(fmaxf(fu, -1.f), (float)W), iv = (int)fminf(fmaxf(fv, -1.f), (float)H);
+    const int u0 = min(max(iu, 0), W - 1), u1 = min(max(iu + 1, 0), W - 1);
+    const int v0 = min(max(iv, 0), H - 1), v1 = min(max(iv + 1, 0), H - 1);
+    const float t00 = h2f(a[(size_t)v0 * W + u0]), t10 = h2f(a[(size_t)v0 * W + u1]);
+    const float t01 = h2f(a[(size_t)v1 * W + u0]), t11 = h2f(a[(size_t)v1 * W + u1]);
+    const float top = __fadd_rn(t00, __fmul_rn(__fsub_rn(t10, t00), wu));
+    const float bot = __fadd_rn(t01, __fmul_rn(__fsub_rn(t11, t01), wu));
+    const float c = __fadd_rn(top, __fmul_rn(__fsub_rn(bot, top), wv));
+    return fminf(fmaxf(c, 0.f), 1.f);
+}
+
+// One fragment of a featherAtlasBlit draw (draw_mesh.frag:60-225 with
+// FEATHER_ATLAS_BLIT), written at once: the blit's two triangles never
+// overlap, so it is the path's only fragment at the pixel. The coverage is
+// the atlas sample, cut by the clip rect and the clip; the paint blends
+// straight into the colour (dither before the blend, as that shader does);
+// the coverage plane keeps what it held.
+__device__ __noinline__ void resolve_blit(const FlushParams& P, Pixel& s, uint32_t meta,
+                                          uint32_t paintX, uint32_t paintY, float ax, float ay,
+                                          float fx, float fy, float dither)
+{
+    const uint32_t pathID = meta & 0xffffu, features = meta >> 16;
+    const uint32_t paintType = paintX & 0xfu;
+    float coverage = atlas_coverage(P, ax, ay);
+    if (features & SF_CLIP_RECT)
+        coverage = fminf(fmaxf(clip_rect_distance(P, pathID, fx, fy), 0.f), coverage);
+    if (features & SF_CLIPPING)
+    {
+        const uint32_t clipBits = id_bits_to_f16(
+            (paintType == CLIP_UPDATE_PAINT_TYPE ? paintY : paintX) >> 16, P.pathIDGranularity);
+        if (clipBits != 0)
+        {
+            float clipCoverage = (s.clip >> 16) == clipBits ? h2f(s.clip & 0xffffu) : 0.f;
+            coverage = fminf(coverage, fmaxf(clipCoverage, 0.f));
+        }
+    }
+    const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
+    float color[4];
+    paint_color(P, paintX, paintY, pathID, fx, fy, 1.f, unmultiplied, color);
+    float dst[4];
+    unpack_rgba8(s.color, dst);
+    if (unmultiplied)
+    {
+        uint32_t mode = (paintX >> 4) & 0xfu;
+        if (mode != 0 && (mode < 12 || (features & SF_HSL_BLEND_MODES)))
+            advanced_blend(color, dst, mode);
+        color[3] *= coverage;
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    else
+    {
+        for (int k = 0; k < 4; ++k)
+            color[k] *= coverage;
+    }
+    if ((features & SF_DITHER) && color[3] != 0.f)
+    {
+        color[0] += dither;
+        color[1] += dither;
+        color[2] += dither;
+    }
+    const float a = color[3];
+    for (int k = 0; k < 4; ++k)
+        color[k] = dst[k] * (1.f - a) + color[k];
     s.color = pack_rgba8(color);
 }
 } // namespace
@@ -2520,6 +2672,20 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                 const float4 v3 = T.v3;
                 const float covx = __fmaf_rn(v2.w, lx, __fmaf_rn(v3.x, ly, v2.z));
                 const float covy = __fmaf_rn(v3.z, lx, __fmaf_rn(v3.w, ly, v3.y));
+                if (kFeather && ((T.v4.z >> 16) & FEATURE_ATLAS_BLIT))
+                {
+                    // A blit: the pending path is complete here; the blit
+                    // writes its colour at once and leaves the coverage plane
+                    // (key and count) to whichever path owns it.
+                    if (s.pendMeta)
+                    {
+                        resolve_path(P, s, fx, fy, dither);
+                        s.pendMeta = 0;
+                    }
+                    const uint4 v4 = T.v4;
+                    resolve_blit(P, s, v4.z, v4.x, v4.y, covx, covy, fx, fy, dither);
+                    continue;
+                }
                 float count;
                 if (s.key != vPathID)
                 {
@@ -2612,6 +2778,89 @@ RIVE_RASTER_KERNELS(raster_tile_feather_kernel, true)
 RIVE_RASTER_QUEUE_KERNELS(raster_queue_kernel, false)
 RIVE_RASTER_QUEUE_KERNELS(raster_queue_feather_kernel, true)
 #undef RIVE_RASTER_QUEUE_KERNELS
+
+// The feather atlas pass (render_atlas.glsl with the floating-point target
+// and fixed-function blending; the atlas pipelines of gpu.hpp:2076-2080):
+// one CTA of T x T threads per atlas tile, one thread per texel, walking the
+// tile's bin entries in primitive order (fill batches, then stroke batches).
+// A fill adds its feathered coverage, subtracted when the triangle faced
+// away; a stroke keeps the maximum; every blend result rounds to fp16, as
+// the R16F target stores it. Each texel is written, covered or not (the
+// atlas starts cleared). Triangles arrive clipped to their batch's scissor
+// through their pixel box, which the texel test applies exactly.
+template <int TL>
+__device__ __forceinline__ void raster_atlas_tile(const BatchTables& B,
+                                                  const TriRecord* __restrict__ tris,
+                                                  const uint32_t* __restrict__ sortedSlots,
+                                                  const uint2* __restrict__ ranges,
+                                                  uint32_t gtile)
+{
+    constexpr int T = 1 << TL;
+    const uint32_t scene = find_range(B.tileBase, B.sceneCount, gtile);
+    const FlushParams& P = B.scenes[scene];
+    const uint32_t tilesX = P.tilesX;
+    const uint32_t tile = gtile - B.tileBase[scene];
+    const int tx = (int)(tile % tilesX), ty = (int)(tile / tilesX);
+    const int ox = tx * T, oy = ty * T;
+    const int lxi = (int)threadIdx.x & (T - 1), lyi = (int)threadIdx.x >> TL;
+    const int px = ox + lxi, py = oy + lyi;
+    const float lx = (float)lxi, ly = (float)lyi;
+    const float fx = (float)px + .5f, fy = (float)py + .5f;
+    const uint2 range = ranges[gtile];
+    float acc = 0.f;
+    for (uint32_t k = range.x; k < range.y; ++k)
+    {
+        const uint32_t slot = __ldg(sortedSlots + k);
+        const TriRecord& R = tris[slot];
+        const uint4 meta = R.meta;
+        const int4 bb = unpack_bbox(meta);
+        if (px < bb.x || px >= bb.z || py < bb.y || py >= bb.w)
+            continue;
+        const float4 e0 = R.e0, e1 = R.e1, e2 = R.e2;
+        const float c0 = tile_edge_origin(e0, tx, ty, TL), c1 = tile_edge_origin(e1, tx, ty, TL),
+                    c2 = tile_edge_origin(e2, tx, ty, TL);
+        const float E0 = local_edge(c0, e0.z, e0.w, lx, ly);
+        const float E1 = local_edge(c1, e1.z, e1.w, lx, ly);
+        const float E2 = local_edge(c2, e2.z, e2.w, lx, ly);
+        const float emin = fminf(fminf(E0, E1), E2);
+        if (!(emin > 0.f) &&
+            !(emin == 0.f && local_inside(e0.z, e0.w, E0) && local_inside(e1.z, e1.w, E1) &&
+              local_inside(e2.z, e2.w, E2)))
+            continue;
+        const float4 cv0 = R.cov0, cv1 = R.cov1;
+        const float dx0 = (float)ox + .5f - e0.x, dy0 = (float)oy + .5f - e0.y;
+        const float cx0 = cv0.x + cv0.y * dx0 + cv0.z * dy0;
+        const float cy0 = cv0.w + cv1.x * dx0 + cv1.y * dy0;
+        const float covx = __fmaf_rn(cv0.y, lx, __fmaf_rn(cv0.z, ly, cx0));
+        const float covy = __fmaf_rn(cv1.x, lx, __fmaf_rn(cv1.y, ly, cy0));
+        float frag = feathered_fragment(B.featherPlanes, slot, fx, fy, covx, covy);
+        if (covy >= 0.f)
+        {
+            acc = h2f(f2h(fmaxf(acc, frag)));
+        }
+        else
+        {
+            if ((meta.x >> 16) & FEATURE_ATLAS_NEGATE)
+                frag = -frag;
+            acc = h2f(f2h(acc + frag));
+        }
+    }
+    if (px < (int)P.width && py < (int)P.height)
+        P.atlas[(size_t)py * P.atlasW + px] = (uint16_t)f2h(acc);
+}
+
+#define RIVE_ATLAS_KERNEL(NAME, TL)                                                                \
+    __global__ void __launch_bounds__(1 << (2 * TL)) NAME(                                          \
+        BatchTables B, const TriRecord* __restrict__ tris,                                        \
+        const uint32_t* __restrict__ sortedSlots, const uint2* __restrict__ ranges,               \
+        uint32_t firstTile)                                                                       \
+    {                                                                                             \
+        raster_atlas_tile<TL>(B, tris, sortedSlots, ranges, firstTile + blockIdx.x);              \
+    }
+RIVE_ATLAS_KERNEL(raster_atlas8_kernel, 3)
+RIVE_ATLAS_KERNEL(raster_atlas_kernel, 4)
+RIVE_ATLAS_KERNEL(raster_atlas32_kernel, 5)
+#undef RIVE_ATLAS_KERNEL
 
 // Sort keys of the work queue: per tile, its bin entries inverted (a plain
 // ascending sort then puts the heaviest tile first), and its index.

@@ -32,6 +32,7 @@ constexpr uint32_t DRAW_MIDPOINT_FAN_PATCHES = 0u;
 constexpr uint32_t DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES = 1u;
 constexpr uint32_t DRAW_OUTER_CURVE_PATCHES = 2u;
 constexpr uint32_t DRAW_INTERIOR_TRIANGULATION = 3u;
+constexpr uint32_t DRAW_FEATHER_ATLAS_BLIT = 4u;
 
 constexpr float kPi = 3.14159265359f;
 constexpr float k2Pi = 6.28318530718f;
@@ -104,6 +105,12 @@ cudaError_t run_tess_math(int fn, const float* in, float* out, size_t n);
 cudaError_t ensure_feather_lut(int device);
 void feather_table_f16(uint16_t out[kGaussianTableSize]);
 constexpr uint32_t FEATURE_CLOCKWISE_FILL = 1u << 15;
+// A featherAtlasBlit triangle (main scenes): its coverage is the feather
+// atlas sampled at the pixel, its coverage planes carry atlas coordinates.
+constexpr uint32_t FEATURE_ATLAS_BLIT = 1u << 12;
+// An atlas fill triangle that faced away (the atlas fill pipeline culls
+// nothing): turned clockwise, its coverage is subtracted.
+constexpr uint32_t FEATURE_ATLAS_NEGATE = 1u << 11;
 // Two more bits of a triangle record's feature half-word, set only when the
 // batch draws interior tiles as winding records: a fan triangle whose tiles
 // are counted after its path's winding grid is complete, and the record of a
@@ -206,6 +213,13 @@ struct FlushParams
     // This flush's FlushUniforms record (device); scene_uniforms_kernel copies
     // pathIDGranularity and the dither terms from it before any other pass.
     const uint8_t* uniforms;
+    // The flush's feather atlas: atlasW x atlasH fp16 texels, row-major. A
+    // main scene samples it for its featherAtlasBlit draws; the flush's atlas
+    // scene (atlasMode = 1: width x height = the atlas content, no target)
+    // renders it.
+    uint16_t* atlas;
+    uint32_t atlasW, atlasH;
+    uint32_t atlasMode;
 };
 
 // One DrawBatch of one flush in a set-up work list: its first element (patch
@@ -214,6 +228,10 @@ struct FlushParams
 struct PatchSegment
 {
     uint32_t scene, baseElement, features, slotBase;
+    // Pixel rectangle the segment's triangles are clipped to, as
+    // left | top << 16 and right | bottom << 16: an atlas batch's scissor, or
+    // everything (0, 0xffffffff) for the draw batches of a main scene.
+    uint32_t scissorLT, scissorRB;
 };
 
 // Set-up work lists: midpoint-fan patches, outer-curve patches, interior
@@ -239,6 +257,9 @@ struct BatchTables
     uint32_t totalItems[kSetupLists];
     uint32_t sceneCount;
     uint32_t totalGradSpans, totalTessSpans, totalTiles;
+    // Tiles [0, mainTiles) belong to the flushes' targets, the rest to their
+    // feather atlases (scenes after the main ones).
+    uint32_t mainTiles;
     int tileLog2; // raster tile size of this batch (3, 4 or 5)
     // Per triangle slot, when the batch holds feathered fills: the planes of
     // the feather coverage's third and fourth components (cotTheta, y0) as

@@ -116,6 +116,7 @@ def load():
         "rive_cuda_sync": (i32, [vp, vp]),
         "rive_cuda_read_tess_texture": (i32, [vp, vp, sz]),
         "rive_cuda_read_grad_texture": (i32, [vp, vp, sz]),
+        "rive_cuda_read_atlas_texture": (i32, [vp, vp, sz]),
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
@@ -360,6 +361,13 @@ class Context:
         self.check(self.lib.rive_cuda_read_tess_texture(
             self.h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes), "read_tess_texture")
         return out
+
+    def read_atlas(self, width, height):
+        """The feather atlas of the last flush, as float32 (from fp16)."""
+        out = np.zeros((height, width), np.uint16)
+        self.check(self.lib.rive_cuda_read_atlas_texture(
+            self.h, out.ctypes.data_as(ctypes.c_void_p), out.nbytes), "read_atlas_texture")
+        return out.view(np.float16).astype(np.float32)
 
     def read_grad(self, height):
         out = np.empty((height, 512, 4), np.uint8)

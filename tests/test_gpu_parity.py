@@ -110,7 +110,7 @@ def test_gradient_ramps_match_oracle(ctx, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("draw_type", [4, 5, 6])  # featherAtlasBlit, imageRect, imageMesh
+@pytest.mark.parametrize("draw_type", [5, 6])  # imageRect, imageMesh
 def test_flush_rejects_unsupported_draw_type_and_stays_usable(ctx, draw_type):
     from rive_runtime_gb300 import rive_cuda
     cap, _ = load_golden("plain_small_s1")
