@@ -2105,14 +2105,19 @@ __device__ __noinline__ void advanced_blend(float src[3], const float dp[4], uin
         src[i] = src[i] * (1.f - a) + co[i] * a;
 }
 
+// Coordinate arithmetic here and in paint_color / clip_rect_distance is
+// written with explicit round-to-nearest operations (no contraction into
+// fused multiply-adds), in the oracle's order: a gradient coordinate is a
+// difference of large terms, and a contracted evaluation lands on the other
+// side of a hard colour step at a few pixels.
 __device__ __noinline__ void sample_grad(const FlushParams& P, float u, float v, float out[4])
 {
-    float fx = u * kGradTextureWidth - .5f;
+    float fx = __fsub_rn(__fmul_rn(u, (float)kGradTextureWidth), .5f);
     // The gradient texture always has at least one row allocated.
     const int H = max((int)P.gradDataHeight, 1);
-    float fy = v * (float)P.gradTextureHeight - .5f;
+    float fy = __fsub_rn(__fmul_rn(v, (float)P.gradTextureHeight), .5f);
     float x0f = floorf(fx), y0f = floorf(fy);
-    float ax = fx - x0f, ay = fy - y0f;
+    float ax = __fsub_rn(fx, x0f), ay = __fsub_rn(fy, y0f);
     int x0 = (int)x0f, y0 = (int)y0f;
     out[0] = out[1] = out[2] = out[3] = 0.f;
 #pragma unroll
@@ -2122,12 +2127,12 @@ __device__ __noinline__ void sample_grad(const FlushParams& P, float u, float v,
         {
             int xi = min(max(x0 + i, 0), kGradTextureWidth - 1);
             int yj = min(max(y0 + j, 0), H - 1);
-            float wgt = (i ? ax : 1.f - ax) * (j ? ay : 1.f - ay);
+            float wgt = __fmul_rn(i ? ax : __fsub_rn(1.f, ax), j ? ay : __fsub_rn(1.f, ay));
             uchar4 t = P.grad[(size_t)yj * kGradTextureWidth + xi];
-            out[0] += wgt * ((float)t.x / 255.f);
-            out[1] += wgt * ((float)t.y / 255.f);
-            out[2] += wgt * ((float)t.z / 255.f);
-            out[3] += wgt * ((float)t.w / 255.f);
+            out[0] = __fadd_rn(out[0], __fmul_rn(wgt, __fdiv_rn((float)t.x, 255.f)));
+            out[1] = __fadd_rn(out[1], __fmul_rn(wgt, __fdiv_rn((float)t.y, 255.f)));
+            out[2] = __fadd_rn(out[2], __fmul_rn(wgt, __fdiv_rn((float)t.z, 255.f)));
+            out[3] = __fadd_rn(out[3], __fmul_rn(wgt, __fdiv_rn((float)t.w, 255.f)));
         }
 }
 
@@ -2156,13 +2161,13 @@ __device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32
     float d0, d1, d2, d3;
     if (awx != 0.f && awy != 0.f)
     {
-        float rx = 1.f / awx, ry = 1.f / awy;
-        float cx = cm.x * fx + cm.z * fy + ct.x;
-        float cy = cm.y * fx + cm.w * fy + ct.y;
-        d0 = cx * rx + rx + .5f;
-        d1 = cy * ry + ry + .5f;
-        d2 = -cx * rx + rx + .5f;
-        d3 = -cy * ry + ry + .5f;
+        float rx = __fdiv_rn(1.f, awx), ry = __fdiv_rn(1.f, awy);
+        float cx = __fadd_rn(__fadd_rn(__fmul_rn(cm.x, fx), __fmul_rn(cm.z, fy)), ct.x);
+        float cy = __fadd_rn(__fadd_rn(__fmul_rn(cm.y, fx), __fmul_rn(cm.w, fy)), ct.y);
+        d0 = __fadd_rn(__fadd_rn(__fmul_rn(cx, rx), rx), .5f);
+        d1 = __fadd_rn(__fadd_rn(__fmul_rn(cy, ry), ry), .5f);
+        d2 = __fadd_rn(__fadd_rn(__fmul_rn(-cx, rx), rx), .5f);
+        d3 = __fadd_rn(__fadd_rn(__fmul_rn(-cy, ry), ry), .5f);
     }
     else
     {
@@ -2198,13 +2203,16 @@ __device__ __forceinline__ void paint_color(const FlushParams& P, uint32_t paint
     {
         const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
         float4 pm = aux[0], pt = aux[1];
-        float pcx = pm.x * fx + pm.z * fy + pt.x;
-        float pcy = pm.y * fx + pm.w * fy + pt.y;
+        float pcx = __fadd_rn(__fadd_rn(__fmul_rn(pm.x, fx), __fmul_rn(pm.z, fy)), pt.x);
+        float pcy = __fadd_rn(__fadd_rn(__fmul_rn(pm.y, fx), __fmul_rn(pm.w, fy)), pt.y);
         float spanB = pt.z > .9f ? 2.f : pt.w;
-        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE ? pcx : sqrtf(pcx * pcx + pcy * pcy);
+        float t = paintType == LINEAR_GRADIENT_PAINT_TYPE
+                      ? pcx
+                      : __fsqrt_rn(__fadd_rn(__fmul_rn(pcx, pcx), __fmul_rn(pcy, pcy)));
         t = clamp01(t);
-        float x = spanB > 1.f ? (1.f - 1.f / kGradTextureWidth) * t + (.5f / kGradTextureWidth)
-                              : (1.f / kGradTextureWidth) * t + spanB;
+        float x = spanB > 1.f ? __fadd_rn(__fmul_rn(1.f - 1.f / kGradTextureWidth, t),
+                                          .5f / kGradTextureWidth)
+                              : __fadd_rn(__fmul_rn(1.f / kGradTextureWidth, t), spanB);
         sample_grad(P, x, __uint_as_float(paintY), color);
         color[3] *= coverage;
         if (!unmultiplied)

@@ -44,7 +44,14 @@ def test_every_config_matches_oracle(ctx, oracle_images, config):
             assert frac >= 0.999 and worst <= 8, (config, name, frac, worst)
             st = ctx.stats()
             t = config[0]
-            assert st["tiles"] == ((cap.width + t - 1) // t) * ((cap.height + t - 1) // t)
+            # The target's tiles, plus the feather atlas's when the (last)
+            # flush renders one.
+            d = cap.flushes[-1].desc
+            want = ((cap.width + t - 1) // t) * ((cap.height + t - 1) // t)
+            if cap.flushes[-1].has_atlas:
+                want += (((d["atlas_content_width"] + t - 1) // t) *
+                         ((d["atlas_content_height"] + t - 1) // t))
+            assert st["tiles"] == want
     finally:
         ctx.set_raster_config(16, 0)
 

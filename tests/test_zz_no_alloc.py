@@ -97,6 +97,24 @@ def test_noalloc_refuses_flushes_beyond_its_limits():
     del keep
 
 
+@pytest.mark.gpu
+def test_noalloc_refuses_the_feather_atlas():
+    """The atlas's intermediates have no room in the fixed pool: a flush that
+    renders one is refused before launch, the target untouched."""
+    import torch
+    from rive_runtime_gb300 import rive_cuda
+    cap, _ = load_golden("feather_atlas_s35")
+    assert cap.flushes[0].has_atlas
+    bufs, keep = device_buffers(cap)
+    target = torch.full((cap.height, cap.width, 4), 7, dtype=torch.uint8, device="cuda")
+    with pytest.raises(rive_cuda.RiveCudaError, match="feather atlas"):
+        rive_cuda.flush_device_noalloc(cap.flushes[0], bufs, target.data_ptr(),
+                                       torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert bool((target == 7).all())
+    del keep
+
+
 def _star_scene(n_paths):
     """n_paths star polygons {40/17} of radius 380-500 px around the middle
     of a 1024x1024 canvas: few tessellation vertices (one segment per
