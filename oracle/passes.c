@@ -1356,7 +1356,11 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
     {
         theta = u2f(tv[2]);
     }
-    f2 norm = {sinf(theta), -cosf(theta)};
+    /* sin and cos here, as everywhere in the passes, are the shared
+     * correctly-rounded-operation forms (rive_fp32_math.h) the kernel uses. */
+    float normS, normC;
+    rc_sincosf(theta, &normS, &normC);
+    f2 norm = {normS, -normC};
     f2 origin = {u2f(tv[0]), u2f(tv[1])};
     f2 postTransformVertexOffset = {0.f, 0.f};
     float cov[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1411,9 +1415,11 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
             int isLeftJoin = (contourIDWithFlags & LEFT_JOIN_CONTOUR_FLAG) != 0;
             float bisectTheta =
                 joinAngle * (isTan0 == isLeftJoin ? -.5f : .5f) + theta;
-            f2 bisector = {sinf(bisectTheta), -cosf(bisectTheta)};
+            float bisS, bisC;
+            rc_sincosf(bisectTheta, &bisS, &bisC);
+            f2 bisector = {bisS, -bisC};
             float bisectPixelWidth = manhattan_pixel_width(M, bisector);
-            float miterRatio = cosf(joinAngle * .5f);
+            float miterRatio = rc_cosf(joinAngle * .5f);
             float clipRadius;
             if (joinType == MITER_CLIP_JOIN_CONTOUR_FLAG ||
                 (joinType == MITER_REVERT_JOIN_CONTOUR_FLAG && miterRatio >= .25f))
@@ -1495,7 +1501,9 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
                 spokeTheta = clampf(spokeTheta, 0.f, featherJoinCornerTheta);
                 if (spokeTheta > featherJoinCornerTheta * .5f)
                     spokeTheta = featherJoinCornerTheta - spokeTheta;
-                f2 spokeNorm = {sinf(spokeTheta), cosf(spokeTheta)};
+                float spokeS, spokeC;
+                rc_sincosf(spokeTheta, &spokeS, &spokeC);
+                f2 spokeNorm = {spokeS, spokeC};
                 pack_feathered_fill_coverages(featherJoinCornerTheta, spokeNorm, outset, cov);
             }
             postTransformVertexOffset = mat_mul(M, mul2(norm, outset * featherRadius));

@@ -11,15 +11,20 @@
 //  * resolve: draw_raster_order_path.frag:14-238 (fp16 coverage keyed by
 //    path ID, nonzero/even-odd, nested clip, clip rect, paint colour,
 //    advanced blend, src-over, dither).
+// The vertex shading takes sin and cos from rive_fp32_math.h, as the
+// tessellation does: the sign of an AA outset depends on the last bit of a
+// near-zero normal component, so the C restatement of these passes and this
+// kernel must evaluate them to the same bits to place the same triangles.
 //
 // GB300 design: instead of a hardware rasteriser with fragment interlock, the
 // flush is tiled. Each triangle is set up once (edge functions with canonical
-// anchors, coverage planes) into an 80-byte record; (tile, triangle) pairs are
+// anchors, coverage planes) into a 96-byte record; (tile, triangle) pairs are
 // radix-sorted by tile, which keeps primitive order inside each tile; then one
 // 256-thread CTA per 16x16 tile walks its triangles in order with each thread
 // owning one pixel and its pixel-local-storage planes in registers. Raster
 // order therefore holds by construction, with no interlock and no atomics.
 #include "rive_cuda_internal.cuh"
+#include "rive_fp32_math.h"
 
 #include <cuda_fp16.h>
 
@@ -507,7 +512,7 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
         theta = __uint_as_float(tv.z);
     }
     float sn, cs;
-    sincosf(theta, &sn, &cs);
+    rc_sincosf(theta, &sn, &cs);
     float2 norm = make_float2(sn, -cs);
     float2 origin = make_float2(__uint_as_float(tv.x), __uint_as_float(tv.y));
     float2 offset = make_float2(0.f, 0.f);
@@ -564,10 +569,10 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
             float bisectTheta =
                 __fadd_rn(__fmul_rn(joinAngle, isTan0 == isLeft ? -.5f : .5f), theta);
             float bs, bc;
-            sincosf(bisectTheta, &bs, &bc);
+            rc_sincosf(bisectTheta, &bs, &bc);
             float2 bisector = make_float2(bs, -bc);
             float bisectPixelWidth = manhattan_pixel_width(M, bisector);
-            float miterRatio = cosf(__fmul_rn(joinAngle, .5f));
+            float miterRatio = rc_cosf(__fmul_rn(joinAngle, .5f));
             float clipRadius;
             if (joinType == MITER_CLIP_JOIN_CONTOUR_FLAG ||
                 (joinType == MITER_REVERT_JOIN_CONTOUR_FLAG && miterRatio >= .25f))
@@ -652,7 +657,7 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
                 if (spoke > __fmul_rn(joinCornerTheta, .5f))
                     spoke = __fsub_rn(joinCornerTheta, spoke);
                 float ss, sc;
-                sincosf(spoke, &ss, &sc);
+                rc_sincosf(spoke, &ss, &sc);
                 pack_feathered_fill_coverages(joinCornerTheta, make_float2(ss, sc), outset, cov,
                                               cov2);
             }
