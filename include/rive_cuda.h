@@ -89,6 +89,26 @@ typedef struct rive_cuda_atlas_batch
 } rive_cuda_atlas_batch;
 
 /*
+ * An image texture (RenderContextImpl::makeImageTexture,
+ * render_context_impl.hpp:60-70): RGBA8 premultiplied texels in device
+ * memory with their mip chain. Created and destroyed with
+ * rive_cuda_texture_create / rive_cuda_texture_destroy.
+ */
+typedef struct rive_cuda_texture rive_cuda_texture;
+
+/*
+ * The image a draw batch samples (gpu::DrawBatch::imageTexture and
+ * imageSampler, gpu.hpp:1257-1259): a texture and an ImageSampler key
+ * (wrapX + 3 wrapY + 9 filter; include/rive/shapes/paint/image_sampler.hpp).
+ */
+typedef struct rive_cuda_batch_image
+{
+    const rive_cuda_texture* texture; /* NULL: the batch draws no image */
+    uint32_t sampler_key;
+    uint32_t reserved;
+} rive_cuda_batch_image;
+
+/*
  * One gpu::DrawBatch (gpu.hpp:1219-1282), flattened. The reference keeps the
  * batches in a linked list owned by a per-frame allocator; the caller flattens
  * it into an array in list order.
@@ -156,6 +176,9 @@ typedef struct rive_cuda_flush_desc
     uint32_t atlas_fill_batch_count;
     uint32_t atlas_stroke_batch_count;
     const rive_cuda_atlas_batch* atlas_batches; /* fill batches, then stroke batches */
+    /* Images: NULL, or one entry per draw batch (the batch's texture and
+     * sampler; paths with an image paint, ENABLE_MODULATED_IMAGE). */
+    const rive_cuda_batch_image* batch_images;
 } rive_cuda_flush_desc;
 
 typedef struct rive_cuda_context rive_cuda_context;
@@ -196,6 +219,28 @@ int rive_cuda_resize_gradient_texture(rive_cuda_context* ctx,
 int rive_cuda_resize_tessellation_texture(rive_cuda_context* ctx,
                                           uint32_t width,
                                           uint32_t height);
+
+/*
+ * RenderContextImpl::makeImageTexture (render_context_impl.hpp:60-70) for an
+ * RGBA8 premultiplied image: uploads level 0 (width * height * 4 bytes, row 0
+ * at the top) and, with mip_levels > 1, makes the other levels on the device
+ * (each texel the rounded mean of the 2x2 texels above it; edges clamp).
+ * mip_levels is at most the full chain's length. The texture belongs to the
+ * context and is valid until destroyed or the context is.
+ */
+int rive_cuda_texture_create(rive_cuda_context* ctx,
+                             uint32_t width,
+                             uint32_t height,
+                             uint32_t mip_levels,
+                             const void* rgba_host,
+                             rive_cuda_texture** out_texture);
+void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* texture);
+/* Copies mip level `level` of the texture to host memory (debug/parity). */
+int rive_cuda_texture_read(rive_cuda_context* ctx,
+                           const rive_cuda_texture* texture,
+                           uint32_t level,
+                           void* dst_host,
+                           size_t bytes);
 
 /*
  * Render targets (gpu::RenderTarget, render_target.hpp): an RGBA8 image in

@@ -14,6 +14,9 @@
  *   uint8_t verbs[verb_count]          (padded to a multiple of 4 bytes)
  *   float   points[point_count * 2]
  *   rive_scene_stop stops[stop_count]
+ * and, only when the frame draws images:
+ *   rive_scene_images { magic "RSI1", count }
+ *   count x { rive_scene_image, uint8_t rgba[width * height * 4] }
  */
 #ifndef RIVE_SCENE_H
 #define RIVE_SCENE_H
@@ -41,6 +44,10 @@ enum
     RIVE_SCENE_CMD_DRAW_PATH = 3, /* a = path index, b = paint index */
     RIVE_SCENE_CMD_CLIP_PATH = 4, /* a = path index */
     RIVE_SCENE_CMD_MODULATE_OPACITY = 5, /* m[0] = opacity (Renderer::modulateOpacity) */
+    /* Renderer::drawImage (renderer.hpp:216-219): a = image index, b = blend
+     * mode | ImageSampler key << 8, m[0] = opacity. The image covers the unit
+     * square scaled to its size under the current transform. */
+    RIVE_SCENE_CMD_DRAW_IMAGE = 6,
 };
 
 /* rive::RenderPaintStyle / gradient kinds. */
@@ -128,5 +135,22 @@ typedef struct rive_scene_stop
     float position;
     uint32_t color; /* rive::ColorInt */
 } rive_scene_stop;
+
+#define RIVE_SCENE_IMAGES_MAGIC 0x31495352u /* "RSI1" */
+
+typedef struct rive_scene_images
+{
+    uint32_t magic;
+    uint32_t count;
+} rive_scene_images;
+
+/* An image: RGBA8 premultiplied texels, row 0 at the top, handed to
+ * RenderContextImpl::makeImageTexture as one level; the backend makes the
+ * other mip levels (generateRemainingMips). */
+typedef struct rive_scene_image
+{
+    uint32_t width;
+    uint32_t height;
+} rive_scene_image;
 
 #endif /* RIVE_SCENE_H */

@@ -17,6 +17,12 @@
 #define KINDS RIVE_CUDA_BUFFER_KIND_COUNT
 #define CAPTURED_KINDS 7 /* flush uniforms .. tess spans (+ triangle vertices) */
 #define MAX_FLUSHES 256
+#define MAX_TEXTURES 4096
+
+struct rive_cuda_texture
+{
+    uint32_t index; /* in the context's texture table */
+};
 
 struct rive_cuda_context
 {
@@ -28,6 +34,11 @@ struct rive_cuda_context
     rive_cuda_flush_desc descs[MAX_FLUSHES];
     rive_cuda_draw_batch* batches[MAX_FLUSHES];
     rive_cuda_atlas_batch* atlas[MAX_FLUSHES];
+    uint32_t* images[MAX_FLUSHES]; /* 2 per batch, or NULL */
+    uint32_t texture_count;
+    uint32_t texture_dims[3 * MAX_TEXTURES];
+    unsigned char* texture_texels[MAX_TEXTURES];
+    rive_cuda_texture* textures[MAX_TEXTURES];
     uint32_t width, height;
     int failed;
 };
@@ -62,10 +73,63 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
     {
         free(ctx->batches[i]);
         free(ctx->atlas[i]);
+        free(ctx->images[i]);
+    }
+    for (uint32_t i = 0; i < ctx->texture_count; ++i)
+    {
+        free(ctx->texture_texels[i]);
+        free(ctx->textures[i]);
     }
     if (g_last == ctx)
         g_last = NULL;
     free(ctx);
+}
+
+int rive_cuda_texture_create(rive_cuda_context* ctx,
+                             uint32_t width,
+                             uint32_t height,
+                             uint32_t mip_levels,
+                             const void* rgba_host,
+                             rive_cuda_texture** out)
+{
+    if (!ctx || !out || !rgba_host || ctx->texture_count >= MAX_TEXTURES)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    const uint32_t i = ctx->texture_count;
+    const size_t bytes = (size_t)width * height * 4;
+    rive_cuda_texture* t = (rive_cuda_texture*)malloc(sizeof(rive_cuda_texture));
+    unsigned char* texels = (unsigned char*)malloc(bytes ? bytes : 1);
+    if (!t || !texels)
+    {
+        free(t);
+        free(texels);
+        return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+    }
+    memcpy(texels, rgba_host, bytes);
+    t->index = i;
+    ctx->texture_dims[3 * i] = width;
+    ctx->texture_dims[3 * i + 1] = height;
+    ctx->texture_dims[3 * i + 2] = mip_levels;
+    ctx->texture_texels[i] = texels;
+    ctx->textures[i] = t;
+    ctx->texture_count = i + 1;
+    *out = t;
+    return RIVE_CUDA_OK;
+}
+
+/* Textures stay recorded until the context goes (the capture lists them). */
+void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* texture)
+{
+    (void)ctx, (void)texture;
+}
+
+int rive_cuda_texture_read(rive_cuda_context* ctx,
+                           const rive_cuda_texture* texture,
+                           uint32_t level,
+                           void* dst_host,
+                           size_t bytes)
+{
+    (void)ctx, (void)texture, (void)level, (void)dst_host, (void)bytes;
+    return RIVE_CUDA_ERR_UNSUPPORTED;
 }
 
 int rive_cuda_last_error(const rive_cuda_context* ctx, char* buf, size_t len)
@@ -175,6 +239,26 @@ int rive_cuda_flush(rive_cuda_context* ctx,
     ctx->atlas[i] = (rive_cuda_atlas_batch*)malloc(na ? na * sizeof(rive_cuda_atlas_batch) : 1);
     if (na)
         memcpy(ctx->atlas[i], desc->atlas_batches, na * sizeof(rive_cuda_atlas_batch));
+    ctx->descs[i].batch_images = NULL;
+    ctx->images[i] = NULL;
+    if (desc->batch_images && n)
+    {
+        int any = 0;
+        uint32_t* im = (uint32_t*)malloc(n * 8);
+        if (!im)
+            return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+        for (size_t b = 0; b < n; ++b)
+        {
+            const rive_cuda_texture* t = desc->batch_images[b].texture;
+            im[2 * b] = t ? t->index : 0xffffffffu;
+            im[2 * b + 1] = desc->batch_images[b].sampler_key;
+            any = any || t != NULL;
+        }
+        if (any)
+            ctx->images[i] = im;
+        else
+            free(im);
+    }
     return RIVE_CUDA_OK;
 }
 
@@ -195,9 +279,9 @@ int abi_recorder_write(const char* path)
         return 1;
     /* Seven kinds, or eight when the frame has interior triangles. */
     const uint32_t kinds = ctx->bytes[CAPTURED_KINDS] ? CAPTURED_KINDS + 1 : CAPTURED_KINDS;
-    int v2 = 0;
+    int v2 = ctx->texture_count != 0;
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
-        v2 = v2 || rive_capture_flush_has_atlas(&ctx->descs[i]);
+        v2 = v2 || rive_capture_flush_has_atlas(&ctx->descs[i]) || ctx->images[i] != NULL;
     uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, ctx->width,
                         ctx->height, kinds};
     fwrite(head, sizeof(head), 1, f);
@@ -212,7 +296,11 @@ int abi_recorder_write(const char* path)
     }
     fwrite(&ctx->flush_count, sizeof(uint32_t), 1, f);
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
-        rive_capture_write_flush(f, &ctx->descs[i], ctx->batches[i], ctx->atlas[i], v2);
+        rive_capture_write_flush(f, &ctx->descs[i], ctx->batches[i], ctx->atlas[i], ctx->images[i],
+                                 v2);
+    if (v2)
+        rive_capture_write_textures(f, ctx->texture_count, ctx->texture_dims,
+                                    (const uint8_t* const*)ctx->texture_texels);
     fclose(f);
     return 0;
 }

@@ -8,11 +8,18 @@
  *   the rive_cuda_flush_desc fields up to and including draw_batches
  *   (RIVE_CAPTURE_DESC_BYTES, the pointer written as 0),
  *   rive_cuda_draw_batch[draw_batch_count],
- * and, in an 'RCP2' capture (one whose frame renders into the feather atlas):
+ * and, in an 'RCP2' capture (one whose frame renders into the feather atlas
+ * or draws images):
  *   u32 atlas_texture_width, atlas_texture_height, atlas_content_width,
  *   atlas_content_height, atlas_fill_batch_count, atlas_stroke_batch_count,
- *   rive_cuda_atlas_batch[fill + stroke].
- * A frame without atlas draws keeps the 'RCP1' layout byte for byte.
+ *   rive_cuda_atlas_batch[fill + stroke],
+ *   u32 image_count (draw_batch_count, or 0 when no batch draws an image),
+ *   image_count x { u32 texture index (0xffffffff: none), u32 sampler key }.
+ * After the flushes an RCP2 capture lists its textures:
+ *   u32 texture_count,
+ *   texture_count x { u32 width, u32 height, u32 mip_levels,
+ *                     uint8_t rgba[width * height * 4] (level 0) }.
+ * A frame without atlas draws or images keeps the 'RCP1' layout byte for byte.
  */
 #ifndef RIVE_CAPTURE_FORMAT_H
 #define RIVE_CAPTURE_FORMAT_H
@@ -39,12 +46,14 @@ static inline void rive_capture_write_flush(FILE* f,
                                             const rive_cuda_flush_desc* d,
                                             const rive_cuda_draw_batch* batches,
                                             const rive_cuda_atlas_batch* atlas,
+                                            const uint32_t* images, /* 2 per batch, or NULL */
                                             int v2)
 {
     rive_cuda_flush_desc o;
     memcpy(&o, d, sizeof(o));
     o.draw_batches = NULL;
     o.atlas_batches = NULL;
+    o.batch_images = NULL;
     fwrite(&o, RIVE_CAPTURE_DESC_BYTES, 1, f);
     if (d->draw_batch_count)
         fwrite(batches, sizeof(rive_cuda_draw_batch), d->draw_batch_count, f);
@@ -57,6 +66,24 @@ static inline void rive_capture_write_flush(FILE* f,
         const uint32_t na = d->atlas_fill_batch_count + d->atlas_stroke_batch_count;
         if (na)
             fwrite(atlas, sizeof(rive_cuda_atlas_batch), na, f);
+        const uint32_t ni = images ? d->draw_batch_count : 0u;
+        fwrite(&ni, 4, 1, f);
+        if (ni)
+            fwrite(images, 8, ni, f);
+    }
+}
+
+/* The texture table at the end of an RCP2 capture. */
+static inline void rive_capture_write_textures(FILE* f,
+                                               uint32_t count,
+                                               const uint32_t* dims, /* w, h, levels per texture */
+                                               const uint8_t* const* texels)
+{
+    fwrite(&count, 4, 1, f);
+    for (uint32_t i = 0; i < count; ++i)
+    {
+        fwrite(dims + 3 * i, 4, 3, f);
+        fwrite(texels[i], 1, (size_t)dims[3 * i] * dims[3 * i + 1] * 4, f);
     }
 }
 

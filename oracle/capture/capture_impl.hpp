@@ -53,6 +53,16 @@ struct FlushRecord
     rive_cuda_flush_desc desc;
     std::vector<rive_cuda_draw_batch> batches;
     std::vector<rive_cuda_atlas_batch> atlasBatches; // fills, then strokes
+    std::vector<uint32_t> images; // per batch: texture index (~0u: none), sampler key
+};
+
+// An image texture the front end asked for (makeImageTexture): its index in
+// the capture's texture table.
+class CaptureTexture : public Texture
+{
+public:
+    CaptureTexture(uint32_t w, uint32_t h, uint32_t index) : Texture(w, h), index(index) {}
+    uint32_t index;
 };
 
 class CaptureImpl : public RenderContextNULL
@@ -61,6 +71,27 @@ public:
     // Buffers in rive_cuda.h kind order 0..7.
     std::vector<uint8_t> buffers[8];
     std::vector<FlushRecord> flushes;
+    // Image textures: width, height, mip levels and level-0 texels.
+    std::vector<uint32_t> textureDims;
+    std::vector<std::vector<uint8_t>> textureTexels;
+
+    rcp<Texture> makeImageTexture(uint32_t width,
+                                  uint32_t height,
+                                  uint32_t mipLevelCount,
+                                  GPUTextureFormat format,
+                                  const uint8_t imageData[],
+                                  uint8_t,
+                                  uint8_t,
+                                  bool,
+                                  bool) override
+    {
+        if (format != GPUTextureFormat::rgba32 || imageData == nullptr)
+            return nullptr; // only uncompressed RGBA is recorded
+        const uint32_t index = static_cast<uint32_t>(textureTexels.size());
+        textureDims.insert(textureDims.end(), {width, height, mipLevelCount});
+        textureTexels.emplace_back(imageData, imageData + (size_t)width * height * 4);
+        return make_rcp<CaptureTexture>(width, height, index);
+    }
 
     static std::unique_ptr<RenderContext> Make(CaptureImpl** out)
     {
@@ -190,8 +221,16 @@ public:
                 ob.first_blend_mode = static_cast<uint32_t>(b.firstBlendMode);
                 ob.barriers = static_cast<uint32_t>(b.barriers);
                 rec.batches.push_back(ob);
+                const auto* tex = static_cast<const CaptureTexture*>(b.imageTexture);
+                rec.images.push_back(tex ? tex->index : ~0u);
+                rec.images.push_back(b.imageSampler.asKey());
             }
         }
+        bool anyImage = false;
+        for (size_t i = 0; i < rec.images.size(); i += 2)
+            anyImage = anyImage || rec.images[i] != ~0u;
+        if (!anyImage)
+            rec.images.clear();
         o.draw_batch_count = static_cast<uint32_t>(rec.batches.size());
         o.atlas_texture_width = d.featherAtlasTextureWidth;
         o.atlas_texture_height = d.featherAtlasTextureHeight;
@@ -251,9 +290,9 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
         return false;
     // Seven buffer kinds, or eight when the frame has interior triangles.
     const uint32_t kinds = impl.buffers[7].empty() ? 7u : 8u;
-    bool v2 = false;
+    bool v2 = !impl.textureTexels.empty();
     for (const FlushRecord& r : impl.flushes)
-        v2 = v2 || rive_capture_flush_has_atlas(&r.desc);
+        v2 = v2 || rive_capture_flush_has_atlas(&r.desc) || !r.images.empty();
     uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, width, height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const uint8_t zeros[8] = {};
@@ -268,7 +307,16 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
     uint32_t nf = static_cast<uint32_t>(impl.flushes.size());
     fwrite(&nf, sizeof(nf), 1, f);
     for (const FlushRecord& r : impl.flushes)
-        rive_capture_write_flush(f, &r.desc, r.batches.data(), r.atlasBatches.data(), v2);
+        rive_capture_write_flush(f, &r.desc, r.batches.data(), r.atlasBatches.data(),
+                                 r.images.empty() ? nullptr : r.images.data(), v2);
+    if (v2)
+    {
+        std::vector<const uint8_t*> texels;
+        for (const auto& t : impl.textureTexels)
+            texels.push_back(t.data());
+        rive_capture_write_textures(f, static_cast<uint32_t>(texels.size()),
+                                    impl.textureDims.data(), texels.data());
+    }
     fclose(f);
     return true;
 }

@@ -12,6 +12,8 @@
 #include "rive/renderer.hpp"
 #include "rive/renderer/render_context.hpp"
 #include "rive/renderer/rive_renderer.hpp"
+#include "rive/renderer/rive_render_image.hpp"
+#include "rive/renderer/render_context_impl.hpp"
 #include "rive/renderer/gpu.hpp"
 #include "rive/math/raw_path.hpp"
 #include "rive/shapes/paint/blend_mode.hpp"
@@ -34,6 +36,9 @@ struct SceneView
     const uint8_t* verbs;
     const float* points;
     const rive_scene_stop* stops;
+    // Images (only when the recording has an images section).
+    std::vector<rive_scene_image> images;
+    std::vector<const uint8_t*> imageTexels;
 };
 
 // Returns nullptr on success, else a message.
@@ -60,7 +65,41 @@ inline const char* parse_scene(const std::vector<uint8_t>& scene, SceneView* v)
     off += sizeof(rive_scene_stop) * hdr.stop_count;
     if (off > scene.size())
         return "truncated scene";
+    if (off + sizeof(rive_scene_images) <= scene.size())
+    {
+        rive_scene_images ih;
+        memcpy(&ih, scene.data() + off, sizeof(ih));
+        if (ih.magic != RIVE_SCENE_IMAGES_MAGIC)
+            return "bad images magic";
+        off += sizeof(ih);
+        for (uint32_t i = 0; i < ih.count; ++i)
+        {
+            rive_scene_image im;
+            if (off + sizeof(im) > scene.size())
+                return "truncated images";
+            memcpy(&im, scene.data() + off, sizeof(im));
+            off += sizeof(im);
+            const size_t bytes = (size_t)im.width * im.height * 4;
+            if (im.width == 0 || im.height == 0 || off + bytes > scene.size())
+                return "truncated image";
+            v->images.push_back(im);
+            v->imageTexels.push_back(scene.data() + off);
+            off += bytes;
+        }
+    }
     return nullptr;
+}
+
+// Mip levels of a full chain for an image of the given size: the index of
+// the highest set bit of (height | width), counted from 1, as the
+// reference's own image decoding asks makeImageTexture for
+// (render_context.cpp:251).
+inline uint32_t scene_image_mip_count(uint32_t w, uint32_t h)
+{
+    uint32_t n = 0;
+    for (uint32_t m = w | h; m; m >>= 1)
+        ++n;
+    return n;
 }
 
 // The scene's paths and paints, made by `factory` (Factory::makeRenderPath,
@@ -69,7 +108,29 @@ struct SceneResources
 {
     std::vector<rive::rcp<rive::RenderPath>> paths;
     std::vector<rive::rcp<rive::RenderPaint>> paints;
+    std::vector<rive::rcp<rive::RenderImage>> images;
 };
+
+// The scene's images as textures of `impl` (RenderContextImpl::makeImageTexture
+// with one level of RGBA8 texels and the rest generated), wrapped as the
+// renderer's images.
+inline const char* make_scene_images(rive::gpu::RenderContextImpl* impl,
+                                     const SceneView& v,
+                                     SceneResources* out)
+{
+    using namespace rive;
+    for (size_t i = 0; i < v.images.size(); ++i)
+    {
+        const rive_scene_image& im = v.images[i];
+        rcp<gpu::Texture> tex =
+            impl->makeImageTexture(im.width, im.height, scene_image_mip_count(im.width, im.height),
+                                   GPUTextureFormat::rgba32, v.imageTexels[i], 1, 1, false, true);
+        if (!tex)
+            return "cannot make an image texture";
+        out->images.push_back(make_rcp<RiveRenderImage>(std::move(tex)));
+    }
+    return nullptr;
+}
 
 inline const char* make_scene_resources(rive::Factory* factory,
                                         const SceneView& v,
@@ -191,6 +252,13 @@ inline const char* issue_scene_commands(rive::Renderer* renderer,
             case RIVE_SCENE_CMD_MODULATE_OPACITY:
                 renderer->modulateOpacity(c.m[0]);
                 break;
+            case RIVE_SCENE_CMD_DRAW_IMAGE:
+                if (c.a >= res.images.size())
+                    return "draw references a missing image";
+                renderer->drawImage(res.images[c.a].get(),
+                                    ImageSampler::SamplerFromKey(static_cast<uint8_t>(c.b >> 8)),
+                                    static_cast<BlendMode>(c.b & 0xffu), c.m[0]);
+                break;
             default:
                 return "bad command";
         }
@@ -234,6 +302,8 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
         return err;
     SceneResources res;
     if (const char* err = make_scene_resources(ctx, v, &res))
+        return err;
+    if (const char* err = make_scene_images(ctx->impl(), v, &res))
         return err;
     rcp<RenderTarget> target = makeTarget(v.hdr.width, v.hdr.height);
     if (!target)

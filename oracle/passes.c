@@ -1453,9 +1453,13 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
                      * columns are vertexOffset and bisectAAOffset. */
                     float a = vertexOffset.x, bb = vertexOffset.y;
                     float c = bisectAAOffset.x, dd = bisectAAOffset.y;
+                    /* inverse() as the reference's own polyfills define it:
+                     * the adjoint times 1 / determinant (hlsl.glsl:378-382,
+                     * metal.glsl:509-514). */
                     float det = a * dd - c * bb;
-                    float inv00 = dd / det, inv01 = -bb / det; /* column 0 */
-                    float inv10 = -c / det, inv11 = a / det;   /* column 1 */
+                    float invDet = 1.f / det;
+                    float inv00 = dd * invDet, inv01 = -bb * invDet; /* column 0 */
+                    float inv10 = -c * invDet, inv11 = a * invDet;   /* column 1 */
                     vertexOffset.x = kk.x * inv00 + kk.y * inv01;
                     vertexOffset.y = kk.x * inv10 + kk.y * inv11;
                 }
@@ -1514,8 +1518,9 @@ static int patch_vertex_shader(const rive_cuda_flush_desc* d,
              * times the inverse matrix. */
             f2 on = mul2(norm, outset);
             float det = M[0] * M[3] - M[2] * M[1];
-            float i00 = M[3] / det, i01 = -M[1] / det; /* column 0 of inverse */
-            float i10 = -M[2] / det, i11 = M[0] / det; /* column 1 of inverse */
+            float invDet = 1.f / det; /* inverse() = adjoint * (1 / det) */
+            float i00 = M[3] * invDet, i01 = -M[1] * invDet; /* column 0 of inverse */
+            float i10 = -M[2] * invDet, i11 = M[0] * invDet; /* column 1 of inverse */
             f2 r = {on.x * i00 + on.y * i01, on.x * i10 + on.y * i11};
             postTransformVertexOffset = (f2){signf(r.x) * AA_RADIUS, signf(r.y) * AA_RADIUS};
         }

@@ -23,6 +23,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # round the same on x86 and Arm.
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
+# The draw pass is compiled without contracting multiplies and adds into fused
+# multiply-adds: its colour arithmetic (blend formulas, dither noise, the
+# final blend) then rounds as the C restatement of the pass rounds it, so the
+# few pixels where a last bit decides a unorm8 step, and chains of advanced
+# blends amplify it, agree too. The hot loops use explicit fma intrinsics,
+# which this leaves alone.
+PER_SOURCE_FLAGS = {"kernels_raster.cu": ["--fmad=false"]}
 
 
 def _stale(target, deps):
@@ -41,8 +48,9 @@ def build(verbose=False, extra_flags=()):
         s = os.path.join(CSRC, src)
         o = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(o)
-        if _stale(o, [s] + hdrs):
-            jobs.append([NVCC, *ARCH, *FLAGS, *extra_flags, "-c", s, "-o", o])
+        if _stale(o, [s] + hdrs + [os.path.abspath(__file__)]):
+            jobs.append([NVCC, *ARCH, *FLAGS, *PER_SOURCE_FLAGS.get(src, []), *extra_flags, "-c", s,
+                         "-o", o])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         for cmd, res in zip(jobs, ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), jobs)):
             if verbose or res.returncode:

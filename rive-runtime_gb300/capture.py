@@ -5,8 +5,11 @@ A capture is exactly what rive::gpu::RenderContext hands its RenderContextImpl
 for one frame (render_context.cpp:970-1010): the bytes written into the mapped
 path/paint/paintAux/contour/gradSpan/tessVertexSpan/flushUniform buffers, and
 one gpu::FlushDescriptor per logical flush. A frame that renders into the
-feather atlas is an "RCP2" capture: each flush also carries the atlas sizes
-and its gpu::AtlasDrawBatch lists (gpu.hpp:827-833, 1361-1426).
+feather atlas or draws images is an "RCP2" capture: each flush also carries
+the atlas sizes, its gpu::AtlasDrawBatch lists (gpu.hpp:827-833, 1361-1426)
+and each draw batch's image (texture index and ImageSampler key), and the
+capture ends with the image textures the front end created
+(RenderContextImpl::makeImageTexture: size, mip levels, level-0 RGBA).
 """
 from __future__ import annotations
 
@@ -48,14 +51,29 @@ ATLAS_FIELDS = ("atlas_texture_width", "atlas_texture_height", "atlas_content_wi
 
 
 @dataclass
+class Texture:
+    width: int
+    height: int
+    mip_levels: int
+    rgba: bytes  # level 0, premultiplied RGBA8, row 0 at the top
+
+
+@dataclass
 class Flush:
     desc: dict
     batches: np.ndarray  # (n, 8) uint32
     atlas: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.uint32))
+    # Per draw batch: (texture index or 0xffffffff, sampler key); empty when
+    # no batch draws an image.
+    images: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.uint32))
 
     @property
     def has_atlas(self) -> bool:
         return any(self.desc.get(k, 0) for k in ATLAS_FIELDS)
+
+    @property
+    def has_images(self) -> bool:
+        return bool(len(self.images)) and bool((self.images[:, 0] != 0xFFFFFFFF).any())
 
 
 @dataclass
@@ -64,6 +82,7 @@ class Capture:
     height: int
     buffers: dict = field(default_factory=dict)  # name -> bytes
     flushes: list = field(default_factory=list)
+    textures: list = field(default_factory=list)  # Texture
 
     def buffer_array(self, name, dtype=np.uint32):
         return np.frombuffer(self.buffers[name], dtype=dtype)
@@ -104,14 +123,28 @@ def parse(data: bytes) -> Capture:
             na = vals[4] + vals[5]
             atlas = np.frombuffer(data, dtype="<u4", count=na * 4, offset=off).reshape(na, 4).copy()
             off += na * 16
-        cap.flushes.append(Flush(desc, batches, atlas))
+            (ni,) = struct.unpack_from("<I", data, off)
+            off += 4
+            images = np.frombuffer(data, dtype="<u4", count=ni * 2, offset=off).reshape(ni, 2).copy()
+            off += ni * 8
+        else:
+            images = np.zeros((0, 2), np.uint32)
+        cap.flushes.append(Flush(desc, batches, atlas, images))
+    if v2:
+        (nt,) = struct.unpack_from("<I", data, off)
+        off += 4
+        for _ in range(nt):
+            w, h, levels = struct.unpack_from("<3I", data, off)
+            off += 12
+            cap.textures.append(Texture(w, h, levels, bytes(data[off:off + w * h * 4])))
+            off += w * h * 4
     return cap
 
 
 def serialize(cap: Capture) -> bytes:
     # Seven kinds, or eight when the frame has interior triangles.
     kinds = BUFFER_NAMES if cap.buffers.get("triangles") else BUFFER_NAMES[:7]
-    v2 = any(f.has_atlas for f in cap.flushes)
+    v2 = any(f.has_atlas or f.has_images for f in cap.flushes) or bool(cap.textures)
     out = bytearray(struct.pack("<4I", CAPTURE_MAGIC_V2 if v2 else CAPTURE_MAGIC, cap.width,
                                 cap.height, len(kinds)))
     for name in kinds:
@@ -127,4 +160,11 @@ def serialize(cap: Capture) -> bytes:
         if v2:
             out += struct.pack("<6I", *[d.get(k, 0) for k in ATLAS_FIELDS])
             out += np.asarray(f.atlas, dtype="<u4").reshape(-1, 4).tobytes()
+            im = np.asarray(f.images, dtype="<u4").reshape(-1, 2) if f.has_images else \
+                np.zeros((0, 2), "<u4")
+            out += struct.pack("<I", len(im)) + im.tobytes()
+    if v2:
+        out += struct.pack("<I", len(cap.textures))
+        for t in cap.textures:
+            out += struct.pack("<3I", t.width, t.height, t.mip_levels) + bytes(t.rgba)
     return bytes(out)

@@ -163,6 +163,9 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (d->interlock_mode != 0)
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                     "interlock mode %u not supported (rasterOrdering only)", d->interlock_mode);
+    if (d->atlas_fill_batch_count || d->atlas_stroke_batch_count)
+        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                    "the feather atlas needs the allocating path (rive_cuda_flush_device)");
     if (d->has_triangle_vertices)
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                     "interior triangulation draws are not supported");
@@ -185,9 +188,6 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
         return fail(err, err_len, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                     "gradient texture height %u exceeds the no-allocation limit %u rows",
                     d->grad_data_height, RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS);
-    if (d->atlas_fill_batch_count || d->atlas_stroke_batch_count)
-        return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
-                    "the feather atlas needs the allocating path (rive_cuda_flush_device)");
     uint64_t instances = 0;
     bool feather = false; // some batch draws with ENABLE_FEATHER
     for (uint32_t i = 0; i < d->draw_batch_count; ++i)

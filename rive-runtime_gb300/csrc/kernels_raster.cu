@@ -605,11 +605,13 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
                                          __fmul_rn(vertexOffset.y, vertexOffset.y));
                     float ky = __fadd_rn(__fmul_rn(bo.x, bo.x), __fmul_rn(bo.y, bo.y));
                     // Row vector k times inverse of the matrix with columns
-                    // vertexOffset and bo.
+                    // vertexOffset and bo; inverse() as the reference's own
+                    // polyfills define it, the adjoint times 1 / determinant.
                     float det = __fsub_rn(__fmul_rn(vertexOffset.x, bo.y),
                                           __fmul_rn(bo.x, vertexOffset.y));
-                    float i00 = __fdiv_rn(bo.y, det), i01 = __fdiv_rn(-vertexOffset.y, det);
-                    float i10 = __fdiv_rn(-bo.x, det), i11 = __fdiv_rn(vertexOffset.x, det);
+                    float invDet = __fdiv_rn(1.f, det);
+                    float i00 = __fmul_rn(bo.y, invDet), i01 = __fmul_rn(-vertexOffset.y, invDet);
+                    float i10 = __fmul_rn(-bo.x, invDet), i11 = __fmul_rn(vertexOffset.x, invDet);
                     vertexOffset = make_float2(__fadd_rn(__fmul_rn(kx, i00), __fmul_rn(ky, i01)),
                                                __fadd_rn(__fmul_rn(kx, i10), __fmul_rn(ky, i11)));
                 }
@@ -666,14 +668,20 @@ __device__ bool shade_patch_vertex(const FlushParams& P,
         }
         else
         {
-            // sign(MUL(outset * norm, inverse(M))): the row vector times the
-            // adjugate, signed by the determinant (no division needed).
+            // sign(MUL(outset * norm, inverse(M))) with inverse() as the
+            // reference's own polyfills define it, the adjoint times
+            // 1 / determinant: where the product cancels to within a
+            // rounding step, the form decides the sign (and so which side of
+            // the vertex the AA ramp goes), so it is the same form, rounded
+            // the same way, as the C restatement of this pass.
             float2 on = make_float2(__fmul_rn(norm.x, outset), __fmul_rn(norm.y, outset));
             float det = __fsub_rn(__fmul_rn(M.x, M.w), __fmul_rn(M.z, M.y));
-            float sd = signf(det);
-            float rx = __fsub_rn(__fmul_rn(on.x, M.w), __fmul_rn(on.y, M.y));
-            float ry = __fsub_rn(__fmul_rn(on.y, M.x), __fmul_rn(on.x, M.z));
-            offset = make_float2(signf(rx) * sd * kAARadius, signf(ry) * sd * kAARadius);
+            float invDet = __fdiv_rn(1.f, det);
+            float i00 = __fmul_rn(M.w, invDet), i01 = __fmul_rn(-M.y, invDet);
+            float i10 = __fmul_rn(-M.z, invDet), i11 = __fmul_rn(M.x, invDet);
+            float rx = __fadd_rn(__fmul_rn(on.x, i00), __fmul_rn(on.y, i01));
+            float ry = __fadd_rn(__fmul_rn(on.x, i10), __fmul_rn(on.y, i11));
+            offset = make_float2(signf(rx) * kAARadius, signf(ry) * kAARadius);
         }
         if (((flags & MIRRORED_CONTOUR_CONTOUR_FLAG) != 0) !=
             ((flags & NEGATE_PATH_FILL_COVERAGE_FLAG) != 0))
@@ -2571,12 +2579,15 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
     s.pendPaintX = s.pendPaintY = 0;
     s.pendFrags = 0;
     const float fx = (float)px + .5f, fy = (float)py + .5f;
-    // common.glsl:269-274 interleaved gradient noise (depends on the pixel only).
-    float v1 = 0.06711056f * fx + 0.00583715f * fy;
-    v1 = v1 - floorf(v1);
-    float v2 = 52.9829189f * v1;
-    v2 = v2 - floorf(v2);
-    const float dither = v2 * P.ditherScale + P.ditherBias;
+    // common.glsl:269-274 interleaved gradient noise (depends on the pixel
+    // only). Rounded step by step as the C restatement rounds it: the noise
+    // wraps at fract(), where a fused multiply-add's last bit moves a pixel's
+    // dither by a whole step, and chains of advanced blends amplify it.
+    float v1 = __fadd_rn(__fmul_rn(0.06711056f, fx), __fmul_rn(0.00583715f, fy));
+    v1 = __fsub_rn(v1, floorf(v1));
+    float v2 = __fmul_rn(52.9829189f, v1);
+    v2 = __fsub_rn(v2, floorf(v2));
+    const float dither = __fadd_rn(__fmul_rn(v2, P.ditherScale), P.ditherBias);
     uint32_t streamPath = 0xffffffffu; // coverage key of the warp's current path
 
     constexpr uint32_t kChunk = (uint32_t)G::kThreads * kStage;

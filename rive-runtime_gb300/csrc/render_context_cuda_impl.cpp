@@ -118,19 +118,47 @@ rcp<RenderBuffer> RenderContextCUDAImpl::makeRenderBuffer(RenderBufferType type,
     return make_rcp<HostRenderBuffer>(type, flags, bytes);
 }
 
+// A texture in device memory with its mip chain (rive_cuda_texture_create).
+class TextureCUDA : public Texture
+{
+public:
+    TextureCUDA(rive_cuda_context* ctx, rive_cuda_texture* tex, uint32_t w, uint32_t h) :
+        Texture(w, h), m_ctx(ctx), m_tex(tex)
+    {}
+    ~TextureCUDA() override { rive_cuda_texture_destroy(m_ctx, m_tex); }
+    const rive_cuda_texture* handle() const { return m_tex; }
+    void* nativeHandle() const override { return m_tex; }
+
+private:
+    rive_cuda_context* m_ctx;
+    rive_cuda_texture* m_tex;
+};
+
 rcp<Texture> RenderContextCUDAImpl::makeImageTexture(uint32_t width,
                                                      uint32_t height,
-                                                     uint32_t,
-                                                     GPUTextureFormat,
-                                                     const uint8_t[],
+                                                     uint32_t mipLevelCount,
+                                                     GPUTextureFormat format,
+                                                     const uint8_t imageData[],
                                                      uint8_t,
                                                      uint8_t,
                                                      bool,
-                                                     bool)
+                                                     bool generateRemainingMips)
 {
-    // Image paints are not drawn by this backend; the texture object only
-    // carries its size so RenderImage bookkeeping works.
-    return make_rcp<Texture>(width, height);
+    // Uncompressed RGBA (premultiplied, as the front end hands it over) only;
+    // the other mip levels are made on the device.
+    if (format != GPUTextureFormat::rgba32 || imageData == nullptr)
+    {
+        note(RIVE_CUDA_ERR_UNSUPPORTED);
+        return nullptr;
+    }
+    rive_cuda_texture* tex = nullptr;
+    int rc = rive_cuda_texture_create(m_ctx, width, height,
+                                      generateRemainingMips ? mipLevelCount : 1u, imageData,
+                                      &tex);
+    note(rc);
+    if (rc != RIVE_CUDA_OK)
+        return nullptr;
+    return make_rcp<TextureCUDA>(m_ctx, tex, width, height);
 }
 
 // RenderContextImpl::resize* "cannot fail" (render_context_impl.hpp:99-107):
@@ -233,10 +261,20 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
     o.has_triangle_vertices = d.hasTriangleVertices ? 1u : 0u;
 
     std::vector<rive_cuda_draw_batch> batches;
+    std::vector<rive_cuda_batch_image> images;
+    bool anyImage = false;
     if (d.drawList != nullptr)
     {
         for (const DrawBatch& b : *d.drawList)
         {
+            rive_cuda_batch_image im = {};
+            if (b.imageTexture != nullptr)
+            {
+                im.texture = static_cast<const TextureCUDA*>(b.imageTexture)->handle();
+                im.sampler_key = b.imageSampler.asKey();
+                anyImage = true;
+            }
+            images.push_back(im);
             rive_cuda_draw_batch ob;
             ob.draw_type = static_cast<uint32_t>(b.drawType);
             ob.element_count = b.elementCount;
@@ -251,6 +289,7 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
     }
     o.draw_batch_count = static_cast<uint32_t>(batches.size());
     o.draw_batches = batches.empty() ? nullptr : batches.data();
+    o.batch_images = anyImage ? images.data() : nullptr;
 
     // The feather atlas batches: fills, then strokes.
     std::vector<rive_cuda_atlas_batch> atlas;

@@ -38,6 +38,19 @@ MAGIC = 0x31435352  # "RSC1"
 VERB_MOVE, VERB_LINE, VERB_QUAD, VERB_CUBIC, VERB_CLOSE = 0, 1, 2, 4, 5
 CMD_SAVE, CMD_RESTORE, CMD_TRANSFORM, CMD_DRAW_PATH, CMD_CLIP_PATH = 0, 1, 2, 3, 4
 CMD_MODULATE_OPACITY = 5  # m[0] = opacity (Renderer::modulateOpacity)
+# Renderer::drawImage: a = image index, b = blend mode | sampler key << 8,
+# m[0] = opacity.
+CMD_DRAW_IMAGE = 6
+IMAGES_MAGIC = 0x31495352  # "RSI1"
+# ImageSampler (include/rive/shapes/paint/image_sampler.hpp): key =
+# wrapX + 3 wrapY + 9 filter; wrap 0 clamp, 1 repeat, 2 mirror; filter 0
+# bilinear, 1 nearest.
+WRAP_CLAMP, WRAP_REPEAT, WRAP_MIRROR = 0, 1, 2
+FILTER_BILINEAR, FILTER_NEAREST = 0, 1
+
+
+def sampler_key(wrap_x=WRAP_CLAMP, wrap_y=WRAP_CLAMP, filt=FILTER_BILINEAR) -> int:
+    return wrap_x + 3 * wrap_y + 9 * filt
 STYLE_STROKE, STYLE_FILL = 0, 1
 SHADER_NONE, SHADER_LINEAR, SHADER_RADIAL = 0, 1, 2
 FILL_NONZERO, FILL_EVENODD, FILL_CLOCKWISE = 0, 1, 2
@@ -81,6 +94,12 @@ class Paint:
 
 
 @dataclass
+class Image:
+    """RGBA8 premultiplied texels, (height, width, 4) uint8, row 0 at the top."""
+    rgba: np.ndarray
+
+
+@dataclass
 class Scene:
     width: int
     height: int
@@ -90,6 +109,7 @@ class Scene:
     paths: list = field(default_factory=list)
     paints: list = field(default_factory=list)
     cmds: list = field(default_factory=list)  # (op, a, b, m6)
+    images: list = field(default_factory=list)  # Image
 
     def add_path(self, p: Path) -> int:
         self.paths.append(p)
@@ -98,6 +118,14 @@ class Scene:
     def add_paint(self, p: Paint) -> int:
         self.paints.append(p)
         return len(self.paints) - 1
+
+    def add_image(self, im: Image) -> int:
+        self.images.append(im)
+        return len(self.images) - 1
+
+    def draw_image(self, image: int, opacity: float = 1.0, blend_mode: int = BLEND_SRC_OVER,
+                   sampler: int = 0):
+        self.cmd(CMD_DRAW_IMAGE, image, blend_mode | (sampler << 8), (opacity, 0, 0, 0, 0, 0))
 
     def cmd(self, op, a=0, b=0, m=(0, 0, 0, 0, 0, 0)):
         self.cmds.append((op, a, b, tuple(float(v) for v in m)))
@@ -132,8 +160,15 @@ class Scene:
                      if pts else b"")
         stop_bytes = b"".join(struct.pack("<fI", float(s), c & 0xFFFFFFFF)
                               for s, c in stops)
+        image_bytes = b""
+        if self.images:
+            image_bytes = struct.pack("<2I", IMAGES_MAGIC, len(self.images))
+            for im in self.images:
+                a = np.ascontiguousarray(im.rgba, dtype=np.uint8)
+                image_bytes += struct.pack("<2I", a.shape[1], a.shape[0]) + a.tobytes()
         return (header + b"".join(path_recs) + b"".join(paint_recs)
-                + b"".join(cmd_recs) + bytes(verbs) + vpad + pts_bytes + stop_bytes)
+                + b"".join(cmd_recs) + bytes(verbs) + vpad + pts_bytes + stop_bytes
+                + image_bytes)
 
     @property
     def draw_count(self):
