@@ -404,7 +404,7 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
 #define RIVE_CUDA_NOALLOC_MAX_PATCHES 8192u /* 32 rows x 2048 vertices / 8 */
 #define RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS 64u
 #define RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES 1048576u
-#define RIVE_CUDA_NOALLOC_POOL_BYTES 42901504u /* about 40.9 MiB */
+#define RIVE_CUDA_NOALLOC_POOL_BYTES 42902528u /* about 40.9 MiB */
 int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* desc,
                                    const rive_cuda_device_buffers* buffers,
                                    void* target_pixels_device,

@@ -43,7 +43,21 @@ class FlushDesc(ctypes.Structure):
         (n, ctypes.c_uint32) for n in (
             "atlas_texture_width", "atlas_texture_height", "atlas_content_width",
             "atlas_content_height", "atlas_fill_batch_count",
-            "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p)]
+            "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p),
+                                            ("batch_images", ctypes.c_void_p)]
+
+
+class OracleTexture(ctypes.Structure):
+    """oracle_texture (passes.h)."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("levels", ctypes.c_uint32), ("rgba", ctypes.c_void_p),
+                ("mips", ctypes.c_void_p), ("off", ctypes.c_uint32 * 16)]
+
+
+class BatchImage(ctypes.Structure):
+    """rive_cuda_batch_image, its texture pointing at an OracleTexture."""
+    _fields_ = [("texture", ctypes.c_void_p), ("sampler_key", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class OracleBuffers(ctypes.Structure):
@@ -66,7 +80,8 @@ def lib():
             build()
         _lib = ctypes.CDLL(LIB_PATH)
         for name in ("oracle_color_ramps", "oracle_tessellate", "oracle_draw",
-                     "oracle_flush", "oracle_tessellate_f64", "oracle_atlas"):
+                     "oracle_flush", "oracle_tessellate_f64", "oracle_atlas",
+                     "oracle_texture_prepare"):
             getattr(_lib, name).restype = ctypes.c_int
         _lib.oracle_f32_to_f16.restype = ctypes.c_uint16
         _lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
@@ -91,7 +106,35 @@ def make_desc(flush):
     atlas = np.ascontiguousarray(getattr(flush, "atlas", np.zeros((0, 4), np.uint32)),
                                  dtype=np.uint32).reshape(-1, 4)
     d.atlas_batches = atlas.ctypes.data if len(atlas) else None
-    return d, (batches, atlas)
+    images = textures = None
+    if getattr(flush, "has_images", False):
+        textures = _textures(flush.textures)
+        images = (BatchImage * len(batches))()
+        for i, (tex, key) in enumerate(np.asarray(flush.images, dtype=np.uint32)):
+            if tex != 0xFFFFFFFF:
+                images[i].texture = ctypes.addressof(textures[int(tex)][0])
+                images[i].sampler_key = int(key)
+        d.batch_images = ctypes.addressof(images)
+    return d, (batches, atlas, images, textures)
+
+
+# Prepared oracle textures (mip chains made by oracle_texture_prepare), kept
+# per capture.Texture object.
+_TEXTURES = {}
+
+
+def _textures(texs):
+    out = []
+    for t in texs:
+        key = id(t)
+        if key not in _TEXTURES:
+            data = np.frombuffer(t.rgba, np.uint8).copy()
+            ot = OracleTexture(t.width, t.height, t.mip_levels,
+                               data.ctypes.data_as(ctypes.c_void_p).value, None)
+            _check(lib().oracle_texture_prepare(ctypes.byref(ot)), "texture_prepare")
+            _TEXTURES[key] = (ot, data, t)
+        out.append(_TEXTURES[key])
+    return out
 
 
 def make_buffers(cap):

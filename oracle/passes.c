@@ -116,6 +116,8 @@ static void build_inverse_feather_table(void);
 #define SF_NESTED_CLIPPING (1u << 5)
 #define SF_HSL_BLEND_MODES (1u << 6)
 #define SF_DITHER (1u << 7)
+#define SF_MODULATED_IMAGE (1u << 8)
+#define PAINT_FLAG_HAS_IMAGE 0x800u
 
 /* Patch geometry (gpu.hpp:591-640). */
 #define PATCH_SEGMENT_SPAN 8
@@ -1558,6 +1560,8 @@ typedef struct
     int interior; /* an interior-triangulation triangle (DRAW_INTERIOR_TRIANGLES) */
     int blit;     /* a featherAtlasBlit triangle: coverage sampled from the atlas */
     int negate;   /* an atlas fill triangle that faced away: coverage negated */
+    const oracle_texture* image; /* the batch's image (NULL: none) */
+    uint32_t sampler;            /* its ImageSampler key */
 } tri_rec;
 
 static inline int64_t snap(float v)
@@ -1988,10 +1992,156 @@ typedef struct
     int atlasW, atlasH;
 } frag_ctx;
 
+/* ---- Images ----------------------------------------------------------- */
+
+int oracle_texture_prepare(oracle_texture* t)
+{
+    if (!t || !t->rgba || t->width == 0 || t->height == 0 || t->levels == 0 || t->levels > 16)
+        return -1;
+    uint32_t total = 0;
+    for (uint32_t l = 0; l < t->levels; ++l)
+    {
+        uint32_t w = t->width >> l, h = t->height >> l;
+        t->off[l] = total;
+        total += (w ? w : 1) * (h ? h : 1);
+    }
+    t->mips = (uint8_t*)malloc((size_t)total * 4);
+    if (!t->mips)
+        return -4;
+    memcpy(t->mips, t->rgba, (size_t)t->width * t->height * 4);
+    for (uint32_t l = 1; l < t->levels; ++l)
+    {
+        uint32_t sw = t->width >> (l - 1), sh = t->height >> (l - 1);
+        uint32_t dw = t->width >> l, dh = t->height >> l;
+        sw = sw ? sw : 1;
+        sh = sh ? sh : 1;
+        dw = dw ? dw : 1;
+        dh = dh ? dh : 1;
+        const uint8_t* src = t->mips + (size_t)t->off[l - 1] * 4;
+        uint8_t* dst = t->mips + (size_t)t->off[l] * 4;
+        for (uint32_t y = 0; y < dh; ++y)
+            for (uint32_t x = 0; x < dw; ++x)
+            {
+                uint32_t x0 = 2 * x < sw - 1 ? 2 * x : sw - 1;
+                uint32_t x1 = 2 * x + 1 < sw - 1 ? 2 * x + 1 : sw - 1;
+                uint32_t y0 = 2 * y < sh - 1 ? 2 * y : sh - 1;
+                uint32_t y1 = 2 * y + 1 < sh - 1 ? 2 * y + 1 : sh - 1;
+                for (int k = 0; k < 4; ++k)
+                {
+                    uint32_t sum = src[((size_t)y0 * sw + x0) * 4 + k] +
+                                   src[((size_t)y0 * sw + x1) * 4 + k] +
+                                   src[((size_t)y1 * sw + x0) * 4 + k] +
+                                   src[((size_t)y1 * sw + x1) * 4 + k];
+                    dst[((size_t)y * dw + x) * 4 + k] = (uint8_t)((sum + 2) >> 2);
+                }
+            }
+    }
+    return 0;
+}
+
+void oracle_texture_release(oracle_texture* t)
+{
+    if (t)
+    {
+        free(t->mips);
+        t->mips = NULL;
+    }
+}
+
+/* A texel address under a wrap mode: the Vulkan sampler address modes the
+ * reference maps ImageWrap to (pipeline_manager_vulkan.cpp:25-38). */
+static int wrap_texel(int i, int n, uint32_t wrap)
+{
+    if (wrap == 1) /* repeat */
+    {
+        i %= n;
+        return i < 0 ? i + n : i;
+    }
+    if (wrap == 2) /* mirrored repeat */
+    {
+        int m = i % (2 * n);
+        if (m < 0)
+            m += 2 * n;
+        int a = m - n;
+        return (n - 1) - (a >= 0 ? a : -(1 + a));
+    }
+    return i < 0 ? 0 : (i > n - 1 ? n - 1 : i); /* clamp to edge */
+}
+
+/* The image at normalised (u, v) with an explicit level of detail: nearest
+ * mip selection (VK_SAMPLER_MIPMAP_MODE_NEAREST: level ceil(lod + 1/2) - 1
+ * above 1/2, else 0), the sampler's filter within the level. */
+static void sample_image(const oracle_texture* t, uint32_t sampler, float u, float v, float lod,
+                         float out[4])
+{
+    const uint32_t wrapX = sampler % 3u, wrapY = (sampler / 3u) % 3u;
+    const int nearest = sampler >= 9u;
+    int level = 0;
+    if (lod > .5f)
+    {
+        level = (int)ceilf(lod + .5f) - 1;
+        if (level > (int)t->levels - 1)
+            level = (int)t->levels - 1;
+    }
+    int w = (int)(t->width >> level), h = (int)(t->height >> level);
+    w = w ? w : 1;
+    h = h ? h : 1;
+    const uint8_t* tex = t->mips + (size_t)t->off[level] * 4;
+    if (nearest)
+    {
+        int x = wrap_texel((int)floorf(u * (float)w), w, wrapX);
+        int y = wrap_texel((int)floorf(v * (float)h), h, wrapY);
+        for (int k = 0; k < 4; ++k)
+            out[k] = (float)tex[((size_t)y * w + x) * 4 + k] / 255.f;
+        return;
+    }
+    float fx = u * (float)w - .5f, fy = v * (float)h - .5f;
+    float x0f = floorf(fx), y0f = floorf(fy);
+    float ax = fx - x0f, ay = fy - y0f;
+    int x0 = (int)x0f, y0 = (int)y0f;
+    for (int k = 0; k < 4; ++k)
+        out[k] = 0.f;
+    for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i)
+        {
+            int xi = wrap_texel(x0 + i, w, wrapX), yj = wrap_texel(y0 + j, h, wrapY);
+            float wgt = (i ? ax : 1.f - ax) * (j ? ay : 1.f - ay);
+            for (int k = 0; k < 4; ++k)
+                out[k] += wgt * ((float)tex[((size_t)yj * w + xi) * 4 + k] / 255.f);
+        }
+}
+
+/* ENABLE_MODULATED_IMAGE (draw_path.vert:343-361, 478-493): the paint's
+ * colour times its batch's image, sampled at the image matrix applied to the
+ * pixel centre at the front end's level of detail (PaintAuxData words 16-22).
+ * Texels are premultiplied; advanced blending wants them straight. */
+static void image_modulate(const tri_rec* t,
+                           const float* aux,
+                           float fragX,
+                           float fragY,
+                           int unmultiplied,
+                           float color[4])
+{
+    float m[4] = {aux[16], aux[17], aux[18], aux[19]};
+    f2 uv = add2(mat_mul(m, (f2){fragX, fragY}), (f2){aux[20], aux[21]});
+    float lod = (1.f + aux[22]) - 1.f; /* v_image.z = 1 + lod, then - 1 */
+    float img[4];
+    sample_image(t->image, t->sampler, uv.x, uv.y, lod, img);
+    if (unmultiplied && img[3] != 0.f)
+    {
+        img[0] /= img[3];
+        img[1] /= img[3];
+        img[2] /= img[3];
+    }
+    for (int k = 0; k < 4; ++k)
+        color[k] *= img[k];
+}
+
 /* find_paint_color (draw_path.vert:431-496, evaluated per fragment): the
  * paint's colour at the pixel centre with its alpha multiplied by `coverage`,
  * premultiplied unless advanced blending wants it straight. */
 static void paint_color(const frag_ctx* fc,
+                        const tri_rec* t,
                         uint32_t paintType,
                         const uint32_t* paint,
                         const float* aux,
@@ -2054,6 +2204,9 @@ static void paint_color(const frag_ctx* fc,
          * the reference leaves v_paint zero. */
         color[0] = color[1] = color[2] = color[3] = 0.f;
     }
+    if ((t->features & SF_MODULATED_IMAGE) && (paint[0] & PAINT_FLAG_HAS_IMAGE) && t->image &&
+        t->image->mips)
+        image_modulate(t, aux, fragX, fragY, unmultiplied, color);
 }
 
 /* min_component of find_clip_rect_coverage_distances (common.glsl:376-400)
@@ -2148,7 +2301,7 @@ static void blit_fragment(const frag_ctx* fc,
     }
     const int unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    paint_color(fc, paintType, paint, aux, fragX, fragY, 1.f, unmultiplied, color);
+    paint_color(fc, t, paintType, paint, aux, fragX, fragY, 1.f, unmultiplied, color);
     float dst[4];
     for (int k = 0; k < 4; ++k)
         dst[k] = (float)pls->color[k] / 255.f;
@@ -2318,7 +2471,7 @@ static void fragment(const frag_ctx* fc,
 
     int unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    paint_color(fc, paintType, paint, aux, fragX, fragY, coverage, unmultiplied, color);
+    paint_color(fc, t, paintType, paint, aux, fragX, fragY, coverage, unmultiplied, color);
 
     float dst[4];
     if (covBufferID != vPathID)
@@ -2452,6 +2605,8 @@ static int setup_triangle_rect(const vtx_out* a,
     t->features = features;
     t->interior = 0;
     t->blit = 0;
+    t->image = NULL;
+    t->sampler = 0;
     return 1;
 }
 
@@ -2759,6 +2914,7 @@ int oracle_draw(const rive_cuda_flush_desc* d,
         const uint32_t features =
             batch->shader_features |
             ((batch->shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u);
+        const size_t batchFirstTri = n;
         int rc = 0;
         if (batch->draw_type == RIVE_CUDA_DRAW_MIDPOINT_FAN_PATCHES ||
             batch->draw_type == DRAW_TYPE_MIDPOINT_FAN_CENTER_AA_PATCHES ||
@@ -2890,6 +3046,13 @@ int oracle_draw(const rive_cuda_flush_desc* d,
             free(tris);
             free(atlas);
             return rc;
+        }
+        const oracle_texture* image =
+            d->batch_images ? (const oracle_texture*)d->batch_images[bi].texture : NULL;
+        for (size_t k = batchFirstTri; k < n; ++k)
+        {
+            tris[k].image = image;
+            tris[k].sampler = image ? d->batch_images[bi].sampler_key : 0u;
         }
     }
 

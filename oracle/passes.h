@@ -88,6 +88,23 @@ int oracle_flush(const rive_cuda_flush_desc* d,
                  uint8_t* fb,
                  int threads);
 
+/* An image texture for the passes: level-0 RGBA8 premultiplied texels (row 0
+ * at the top) and, after oracle_texture_prepare, its whole mip chain. A
+ * flush's rive_cuda_batch_image entries point at these (in place of the
+ * library's rive_cuda_texture). */
+typedef struct oracle_texture
+{
+    uint32_t width, height, levels;
+    const uint8_t* rgba;
+    uint8_t* mips;      /* every level; owned, freed by oracle_texture_release */
+    uint32_t off[16];   /* texel offset of each level in mips */
+} oracle_texture;
+
+/* Makes the mip chain: each texel of level l the rounded mean of the (up to)
+ * 2x2 texels of level l - 1 it covers, edges clamped. */
+int oracle_texture_prepare(oracle_texture* t);
+void oracle_texture_release(oracle_texture* t);
+
 /* The feather atlas pass of one logical flush (tessellation included) into
  * out, atlas_content_width x atlas_content_height fp16 texels, row-major. */
 int oracle_atlas(const rive_cuda_flush_desc* d,

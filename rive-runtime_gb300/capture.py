@@ -66,6 +66,8 @@ class Flush:
     # Per draw batch: (texture index or 0xffffffff, sampler key); empty when
     # no batch draws an image.
     images: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.uint32))
+    # The capture's textures (the indices above refer to them).
+    textures: list = field(default_factory=list)
 
     @property
     def has_atlas(self) -> bool:
@@ -138,6 +140,8 @@ def parse(data: bytes) -> Capture:
             off += 12
             cap.textures.append(Texture(w, h, levels, bytes(data[off:off + w * h * 4])))
             off += w * h * 4
+    for f in cap.flushes:
+        f.textures = cap.textures
     return cap
 
 

@@ -91,6 +91,9 @@ __global__ void raster_queue_feather_kernel(BatchTables B,
                                             const uint32_t* order,
                                             uint32_t* cursor,
                                             uint32_t tiles);
+// One mip level of an image from the level above (kernels_raster.cu).
+__global__ void mip_level_kernel(const uchar4* src, uint32_t sw, uint32_t sh, uchar4* dst,
+                                 uint32_t dw, uint32_t dh);
 // The feather atlas pass at 8, 16 and 32 pixel tiles (kernels_raster.cu).
 __global__ void raster_atlas8_kernel(BatchTables B, const TriRecord* tris,
                                      const uint32_t* sortedSlots, const uint2* ranges,
@@ -211,6 +214,15 @@ struct RecordRing
 };
 } // namespace
 
+// An image texture (rive_cuda_texture_create): one device allocation with
+// every mip level, and its descriptor for the kernels.
+struct rive_cuda_texture
+{
+    void* mem = nullptr;
+    rivecuda::ImageTex desc = {};
+    uint32_t texels = 0;
+};
+
 struct rive_cuda_render_target
 {
     uint32_t width = 0, height = 0;
@@ -244,6 +256,7 @@ struct rive_cuda_context
     DeviceBuffer queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor;
     DeviceBuffer pathGrids, gridWinding, gridEdge, gridCounters;
     DeviceBuffer atlas; // the batch's feather atlases (fp16 texels)
+    DeviceBuffer pathImage; // per path of the batch: the slot of its image
     uint32_t gridCapacity = 0;
     uint32_t* hGridCounters = nullptr; // pinned: cells asked, winding entries
     rive_cuda_flush_stats stats = {};
@@ -273,7 +286,7 @@ struct rive_cuda_graph
     DeviceBuffer tables, tess, grad, tris, counts, masks, offsets, keys, vals, keysAlt, valsAlt,
         scanTemp, sortTemp, ranges, error, featherPlanes, pathGrids, gridWinding, gridEdge,
         gridCounters, queueKeys, queueVals, queueKeysAlt, queueValsAlt, queueTemp, queueCursor,
-        atlas;
+        atlas, pathImage;
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -496,6 +509,13 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
         }
         slots += (uint64_t)batch_items(b) * kTrianglesPerItem[list];
     }
+    // Images: a known sampler for every batch that samples a texture.
+    if (d->batch_images)
+        for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+            if (d->batch_images[i].texture && d->batch_images[i].sampler_key >= 18)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "batch %u has an unknown image sampler key %u", i,
+                                 d->batch_images[i].sampler_key);
     // The feather atlas: its size, and every batch within the tessellation
     // texture and the atlas.
     const uint32_t na = atlas_batch_count(d);
@@ -538,6 +558,10 @@ struct BatchLayout
     std::vector<uint32_t> atlasScene; // per flush: its atlas scene, or ~0u
     std::vector<uint64_t> atlasTexel0; // per flush: its first atlas texel
     uint32_t scenes() const { return n + atlasScenes; }
+    // Images: draw batches that sample a texture (slots of the batch's image
+    // table), and the per-path image slots of every main scene.
+    uint32_t imageSlots = 0;
+    size_t oImages = 0;
     bool feather = false; // some batch draws with ENABLE_FEATHER
     // Interior tiles as winding records for this batch: midpoint-fan patches
     // then take fanStride slots (their 24 triangles and a winding slot).
@@ -597,6 +621,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             items[list] += k;
             if ((db.shader_features & SF_FEATHER) || db.draw_type == DRAW_FEATHER_ATLAS_BLIT)
                 L.feather = true;
+            if (d->batch_images && d->batch_images[b].texture)
+                ++L.imageSlots;
         }
         L.tessRow0[i] = L.tessRows;
         L.gradRow0[i] = L.gradRows;
@@ -672,7 +698,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     L.oTileBase = align16(L.oTessBase + 4 * (ns + 1));
     L.oSceneTiles = align16(L.oTileBase + 4 * (ns + 1));
     L.oPathBase = align16(L.oSceneTiles + 8 * ns);
-    size_t o = align16(L.oPathBase + 4 * (ns + 1));
+    L.oImages = align16(L.oPathBase + 4 * (ns + 1));
+    size_t o = align16(L.oImages + sizeof(ImageTex) * std::max(L.imageSlots, 1u));
     for (int l = 0; l < kSetupLists; ++l)
     {
         L.oSegments[l] = o;
@@ -702,6 +729,7 @@ struct Scratch
     uint32_t* error = nullptr;
     float4* featherPlanes = nullptr; // 2 per slot, only with center-AA patches
     uint16_t* atlas = nullptr;       // the batch's feather atlases, fp16 texels
+    uint32_t* pathImage = nullptr;   // per path of the batch: its image slot
     // Winding grids (only when the batch draws interior tiles as winding
     // records).
     PathGrid* pathGrids = nullptr;
@@ -730,6 +758,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
     auto* tileBase = (uint32_t*)(h + L.oTileBase);
     auto* sceneTiles = (uint2*)(h + L.oSceneTiles);
     auto* pathBase = (uint32_t*)(h + L.oPathBase);
+    auto* images = (ImageTex*)(h + L.oImages);
+    uint32_t imageAcc = 0;
     PatchSegment* segs[kSetupLists];
     uint32_t* segBase[kSetupLists];
     for (int l = 0; l < kSetupLists; ++l)
@@ -789,6 +819,11 @@ BatchTables write_tables(rive_cuda_context* ctx,
             P.atlasW = d->atlas_content_width;
             P.atlasH = d->atlas_content_height;
         }
+        if (L.imageSlots)
+        {
+            P.images = (const ImageTex*)(S.tables + L.oImages);
+            P.pathImage = S.pathImage + pathAcc;
+        }
 
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
@@ -807,12 +842,19 @@ BatchTables write_tables(rive_cuda_context* ctx,
             if (!k)
                 continue;
             const int l = setup_list(db.draw_type);
+            uint32_t image = kNoImage;
+            if (d->batch_images && d->batch_images[b].texture)
+            {
+                image = imageAcc++;
+                images[image] = d->batch_images[b].texture->desc;
+                images[image].sampler = d->batch_images[b].sampler_key;
+            }
             segs[l][segAcc[l]] = PatchSegment{
                 i, db.base_element,
                 db.shader_features |
                     ((db.shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u) |
                     (db.draw_type == DRAW_FEATHER_ATLAS_BLIT ? FEATURE_ATLAS_BLIT : 0u),
-                slotAcc, 0u, 0xffffffffu};
+                slotAcc, 0u, 0xffffffffu, image};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += k;
@@ -838,6 +880,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
         A.gradSpanCount = 0;
         A.tessSpanCount = 0;
         A.atlasMode = 1;
+        A.images = nullptr;
+        A.pathImage = nullptr;
         const uint32_t ts = 1u << L.tileLog2;
         A.tilesX = (A.width + ts - 1) / ts;
         gradBase[j] = gAcc;
@@ -855,7 +899,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
             segs[l][segAcc[l]] = PatchSegment{
                 j, ab.base_patch, SF_FEATHER, slotAcc,
                 (uint32_t)ab.scissor[0] | ((uint32_t)ab.scissor[1] << 16),
-                (uint32_t)ab.scissor[2] | ((uint32_t)ab.scissor[3] << 16)};
+                (uint32_t)ab.scissor[2] | ((uint32_t)ab.scissor[3] << 16), kNoImage};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += ab.patch_count;
@@ -918,6 +962,8 @@ int enqueue_front(rive_cuda_context* ctx,
     // texture is deterministic.
     CK(cudaMemsetAsync(S.grad, 0, L.gradBytes(), stream));
     CK(cudaMemsetAsync(S.ranges, 0, (size_t)L.tiles * sizeof(uint2), stream));
+    if (L.imageSlots)
+        CK(cudaMemsetAsync(S.pathImage, 0xff, (size_t)std::max(L.paths, 1u) * 4, stream));
     if (L.winding)
     {
         // Winding grids: every path's box and eligibility, its box from the
@@ -1210,6 +1256,8 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         CK(ctx->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     if (L.atlasTexels)
         CK(ctx->atlas.reserve((size_t)L.atlasTexels * 2));
+    if (L.imageSlots)
+        CK(ctx->pathImage.reserve((size_t)std::max(L.paths, 1u) * 4));
     if (L.winding)
     {
         // The cell pool starts at four cells per tile of the batch and grows
@@ -1248,6 +1296,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.tris = (TriRecord*)ctx->tris.ptr;
     S.featherPlanes = L.items[3] ? (float4*)ctx->featherPlanes.ptr : nullptr;
     S.atlas = L.atlasTexels ? (uint16_t*)ctx->atlas.ptr : nullptr;
+    S.pathImage = L.imageSlots ? (uint32_t*)ctx->pathImage.ptr : nullptr;
     S.counts = (uint32_t*)ctx->tileCounts.ptr;
     S.masks = (uint8_t*)ctx->tileMasks.ptr;
     S.offsets = (uint32_t*)ctx->offsets.ptr;
@@ -1401,7 +1450,7 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
                             &ctx->pathGrids, &ctx->gridWinding, &ctx->gridEdge,
                             &ctx->gridCounters, &ctx->queueKeys, &ctx->queueVals,
                             &ctx->queueKeysAlt, &ctx->queueValsAlt, &ctx->queueTemp,
-                            &ctx->queueCursor, &ctx->atlas})
+                            &ctx->queueCursor, &ctx->atlas, &ctx->pathImage})
         b->release();
     ctx->hTables.release();
     if (ctx->hGridCounters)
@@ -1670,7 +1719,7 @@ void graph_free(rive_cuda_graph* g)
                             &g->sortTemp, &g->ranges, &g->error, &g->featherPlanes,
                             &g->pathGrids, &g->gridWinding, &g->gridEdge, &g->gridCounters,
                             &g->queueKeys, &g->queueVals, &g->queueKeysAlt, &g->queueValsAlt,
-                            &g->queueTemp, &g->queueCursor, &g->atlas})
+                            &g->queueTemp, &g->queueCursor, &g->atlas, &g->pathImage})
         b->release();
     if (g->hError)
         cudaFreeHost(g->hError);
@@ -1702,6 +1751,8 @@ int graph_build(rive_cuda_context* ctx,
         CK(g->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     if (L.atlasTexels)
         CK(g->atlas.reserve((size_t)L.atlasTexels * 2));
+    if (L.imageSlots)
+        CK(g->pathImage.reserve((size_t)std::max(L.paths, 1u) * 4));
     CK(g->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(g->error.reserve(4));
     const bool queue = ctx->rasterQueue && L.tileLog2 == 4;
@@ -1725,6 +1776,7 @@ int graph_build(rive_cuda_context* ctx,
     S.tris = (TriRecord*)g->tris.ptr;
     S.featherPlanes = L.items[3] ? (float4*)g->featherPlanes.ptr : nullptr;
     S.atlas = L.atlasTexels ? (uint16_t*)g->atlas.ptr : nullptr;
+    S.pathImage = L.imageSlots ? (uint32_t*)g->pathImage.ptr : nullptr;
     S.counts = (uint32_t*)g->counts.ptr;
     S.masks = (uint8_t*)g->masks.ptr;
     S.offsets = (uint32_t*)g->offsets.ptr;
@@ -1980,6 +2032,99 @@ int rive_cuda_read_tess_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->tess.ptr, std::min(bytes, ctx->lastTessBytes), cudaMemcpyDeviceToHost));
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_texture_create(rive_cuda_context* ctx,
+                             uint32_t width,
+                             uint32_t height,
+                             uint32_t mip_levels,
+                             const void* rgba_host,
+                             rive_cuda_texture** out_texture)
+{
+    if (!ctx || !rgba_host || !out_texture || width == 0 || height == 0 || width > 16384 ||
+        height > 16384 || mip_levels == 0)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *out_texture = nullptr;
+    uint32_t full = 0;
+    for (uint32_t m = width | height; m; m >>= 1)
+        ++full;
+    if (mip_levels > full || mip_levels > (uint32_t)kMaxMipLevels)
+        return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                         "%u mip levels for a %ux%u image (at most %u)", mip_levels, width, height,
+                         std::min(full, (uint32_t)kMaxMipLevels));
+    CK(cudaSetDevice(ctx->device));
+    rive_cuda_texture* t = new (std::nothrow) rive_cuda_texture();
+    if (!t)
+        return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+    uint32_t total = 0;
+    for (uint32_t l = 0; l < mip_levels; ++l)
+    {
+        t->desc.off[l] = total;
+        total += std::max(width >> l, 1u) * std::max(height >> l, 1u);
+    }
+    cudaError_t e = cudaMalloc(&t->mem, (size_t)total * 4);
+    if (e != cudaSuccess)
+    {
+        delete t;
+        return cuda_fail(ctx, e, "cudaMalloc(texture)");
+    }
+    t->texels = total;
+    t->desc.texels = (const uchar4*)t->mem;
+    t->desc.width = width;
+    t->desc.height = height;
+    t->desc.levels = mip_levels;
+    e = cudaMemcpyAsync(t->mem, rgba_host, (size_t)width * height * 4, cudaMemcpyHostToDevice,
+                        ctx->stream);
+    uchar4* base = (uchar4*)t->mem;
+    for (uint32_t l = 1; l < mip_levels && e == cudaSuccess; ++l)
+    {
+        const uint32_t sw = std::max(width >> (l - 1), 1u), sh = std::max(height >> (l - 1), 1u);
+        const uint32_t dw = std::max(width >> l, 1u), dh = std::max(height >> l, 1u);
+        mip_level_kernel<<<(dw * dh + 255) / 256, 256, 0, ctx->stream>>>(
+            base + t->desc.off[l - 1], sw, sh, base + t->desc.off[l], dw, dh);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess)
+    {
+        cudaFree(t->mem);
+        delete t;
+        return cuda_fail(ctx, e, "texture upload");
+    }
+    *out_texture = t;
+    return RIVE_CUDA_OK;
+}
+
+void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* texture)
+{
+    if (!texture)
+        return;
+    if (ctx)
+    {
+        // Flushes still in flight may sample it.
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(texture->mem);
+    delete texture;
+}
+
+int rive_cuda_texture_read(rive_cuda_context* ctx,
+                           const rive_cuda_texture* texture,
+                           uint32_t level,
+                           void* dst_host,
+                           size_t bytes)
+{
+    if (!ctx || !texture || !dst_host || level >= texture->desc.levels)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const size_t n = (size_t)std::max(texture->desc.width >> level, 1u) *
+                     std::max(texture->desc.height >> level, 1u) * 4;
+    CK(cudaMemcpy(dst_host, (const uchar4*)texture->mem + texture->desc.off[level],
+                  std::min(bytes, n), cudaMemcpyDeviceToHost));
     return RIVE_CUDA_OK;
 }
 

@@ -166,6 +166,11 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (d->atlas_fill_batch_count || d->atlas_stroke_batch_count)
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                     "the feather atlas needs the allocating path (rive_cuda_flush_device)");
+    if (d->batch_images)
+        for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+            if (d->batch_images[i].texture)
+                return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                            "images need the allocating path (rive_cuda_flush_device)");
     if (d->has_triangle_vertices)
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                     "interior triangulation draws are not supported");
@@ -302,7 +307,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                                       b.shader_features | ((b.shader_misc_flags & MISC_CLOCKWISE_FILL)
                                                                ? FEATURE_CLOCKWISE_FILL
                                                                : 0u),
-                                      instAcc * kPatchTriangleCount, 0u, 0xffffffffu};
+                                      instAcc * kPatchTriangleCount, 0u, 0xffffffffu, kNoImage};
         segBase[segCount] = instAcc;
         ++segCount;
         instAcc += b.element_count;

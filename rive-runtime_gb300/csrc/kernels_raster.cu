@@ -1203,6 +1203,14 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
             sZW[w][v] = zw;
     }
     __syncwarp();
+    // The path's image slot, for the raster's image paint (every patch of
+    // the path writes the same value).
+    if (S.image != kNoImage && lane == 0 && sok[w] && P.pathImage)
+    {
+        const uint32_t pid = sv[w][kVerts - 1].pathID;
+        if (pid < P.pathCount)
+            P.pathImage[pid] = S.image;
+    }
     // With interior tiles as winding records, each midpoint-fan patch also
     // owns a winding slot after its triangles.
     const uint32_t stride = (kList == 0 && B.fanSlotStride) ? B.fanSlotStride : (uint32_t)kTris;
@@ -1446,6 +1454,8 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
             v[k].pathID = pathID;
             v[k].discard = false;
         }
+        if (ok && S.image != kNoImage && P.pathImage)
+            P.pathImage[v[0].pathID] = S.image;
         TriRecord T;
         if (ok && setup_triangle(P, v[0], v[1], v[2], S.features, S.scene, T, bb))
         {
@@ -2193,9 +2203,13 @@ __device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32
 // find_paint_color (draw_path.vert:431-496, evaluated at the pixel): the
 // paint's colour with its alpha multiplied by `coverage`, premultiplied
 // unless advanced blending wants it straight.
+__device__ __noinline__ void image_modulate(const FlushParams& P, uint32_t pathID, float fx,
+                                            float fy, bool unmultiplied, float color[4]);
+
 __device__ __forceinline__ void paint_color(const FlushParams& P, uint32_t paintX, uint32_t paintY,
                                             uint32_t pathID, float fx, float fy, float coverage,
-                                            bool unmultiplied, float color[4])
+                                            bool unmultiplied, float color[4],
+                                            uint32_t features = 0)
 {
     const uint32_t paintType = paintX & 0xfu;
     if (paintType == SOLID_COLOR_PAINT_TYPE)
@@ -2239,6 +2253,105 @@ __device__ __forceinline__ void paint_color(const FlushParams& P, uint32_t paint
     {
         color[0] = color[1] = color[2] = color[3] = 0.f;
     }
+    if ((features & SF_MODULATED_IMAGE) && (paintX & PAINT_FLAG_HAS_IMAGE) && P.pathImage)
+        image_modulate(P, pathID, fx, fy, unmultiplied, color);
+}
+
+// An image texel address under a wrap mode (the Vulkan sampler address modes
+// the reference maps ImageWrap to, pipeline_manager_vulkan.cpp:25-38): clamp
+// to edge, repeat, mirrored repeat.
+__device__ __forceinline__ int wrap_texel(int i, int n, uint32_t wrap)
+{
+    if (wrap == 1)
+    {
+        i %= n;
+        return i < 0 ? i + n : i;
+    }
+    if (wrap == 2)
+    {
+        int m = i % (2 * n);
+        if (m < 0)
+            m += 2 * n;
+        const int a = m - n; // mirror(a) = a >= 0 ? a : -(1 + a)
+        return (n - 1) - (a >= 0 ? a : -(1 + a));
+    }
+    return min(max(i, 0), n - 1);
+}
+
+// The image sampled at normalised coordinates (u, v) with an explicit level of
+// detail (TEXTURE_SAMPLE_DYNAMIC_LOD): the sampler's filter within the level
+// a nearest mip selection picks (VK_SAMPLER_MIPMAP_MODE_NEAREST,
+// pipeline_manager_vulkan.cpp:13-23: level ceil(lod + 1/2) - 1 above 1/2,
+// else 0), RGBA as floats.
+__device__ void sample_image(const ImageTex& t, float u, float v, float lod, float out[4])
+{
+    const uint32_t wrapX = t.sampler % 3u, wrapY = (t.sampler / 3u) % 3u;
+    const bool nearest = t.sampler >= 9u;
+    int level = 0;
+    if (lod > .5f)
+        level = min((int)ceilf(__fadd_rn(lod, .5f)) - 1, (int)t.levels - 1);
+    const int w = max((int)(t.width >> level), 1), h = max((int)(t.height >> level), 1);
+    const uchar4* tex = t.texels + t.off[level];
+    if (nearest)
+    {
+        const int x = wrap_texel((int)floorf(__fmul_rn(u, (float)w)), w, wrapX);
+        const int y = wrap_texel((int)floorf(__fmul_rn(v, (float)h)), h, wrapY);
+        const uchar4 c = tex[(size_t)y * w + x];
+        out[0] = __fdiv_rn((float)c.x, 255.f);
+        out[1] = __fdiv_rn((float)c.y, 255.f);
+        out[2] = __fdiv_rn((float)c.z, 255.f);
+        out[3] = __fdiv_rn((float)c.w, 255.f);
+        return;
+    }
+    const float fx = __fsub_rn(__fmul_rn(u, (float)w), .5f);
+    const float fy = __fsub_rn(__fmul_rn(v, (float)h), .5f);
+    const float x0f = floorf(fx), y0f = floorf(fy);
+    const float ax = __fsub_rn(fx, x0f), ay = __fsub_rn(fy, y0f);
+    const int x0 = (int)x0f, y0 = (int)y0f;
+    out[0] = out[1] = out[2] = out[3] = 0.f;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+        {
+            const int xi = wrap_texel(x0 + i, w, wrapX), yj = wrap_texel(y0 + j, h, wrapY);
+            const float wgt = __fmul_rn(i ? ax : __fsub_rn(1.f, ax), j ? ay : __fsub_rn(1.f, ay));
+            const uchar4 c = tex[(size_t)yj * w + xi];
+            out[0] = __fadd_rn(out[0], __fmul_rn(wgt, __fdiv_rn((float)c.x, 255.f)));
+            out[1] = __fadd_rn(out[1], __fmul_rn(wgt, __fdiv_rn((float)c.y, 255.f)));
+            out[2] = __fadd_rn(out[2], __fmul_rn(wgt, __fdiv_rn((float)c.z, 255.f)));
+            out[3] = __fadd_rn(out[3], __fmul_rn(wgt, __fdiv_rn((float)c.w, 255.f)));
+        }
+}
+
+// ENABLE_MODULATED_IMAGE (draw_path.vert:343-361, 478-493): the paint's
+// colour times the image the path's batch binds, sampled at the image matrix
+// applied to the pixel centre, at the level of detail the front end computed
+// (PaintAuxData words 16-22: image matrix, translate, LOD). The texels are
+// premultiplied; advanced blending wants them straight.
+__device__ __noinline__ void image_modulate(const FlushParams& P, uint32_t pathID, float fx,
+                                            float fy, bool unmultiplied, float color[4])
+{
+    const uint32_t slot = P.pathImage[pathID];
+    if (slot == kNoImage)
+        return;
+    const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+    const float4 m = aux[4], tl = aux[5];
+    const float u = __fadd_rn(__fadd_rn(__fmul_rn(m.x, fx), __fmul_rn(m.z, fy)), tl.x);
+    const float v = __fadd_rn(__fadd_rn(__fmul_rn(m.y, fx), __fmul_rn(m.w, fy)), tl.y);
+    // v_image.z = 1 + lod in the vertex shader, lod = v_image.z - 1 in the
+    // fragment shader.
+    const float lod = __fsub_rn(__fadd_rn(1.f, tl.z), 1.f);
+    float img[4];
+    sample_image(P.images[slot], u, v, lod, img);
+    if (unmultiplied && img[3] != 0.f)
+    {
+        img[0] = __fdiv_rn(img[0], img[3]);
+        img[1] = __fdiv_rn(img[1], img[3]);
+        img[2] = __fdiv_rn(img[2], img[3]);
+    }
+    for (int k = 0; k < 4; ++k)
+        color[k] = __fmul_rn(color[k], img[k]);
 }
 
 // The colour / clip write of the last fragment of a path at this pixel.
@@ -2312,7 +2425,7 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
 
     const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    paint_color(P, paintX, paintY, pathID, fx, fy, coverage, unmultiplied, color);
+    paint_color(P, paintX, paintY, pathID, fx, fy, coverage, unmultiplied, color, features);
 
     float dst[4];
     unpack_rgba8(s.color, dst);
@@ -2391,7 +2504,7 @@ __device__ __noinline__ void resolve_blit(const FlushParams& P, Pixel& s, uint32
     }
     const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    paint_color(P, paintX, paintY, pathID, fx, fy, 1.f, unmultiplied, color);
+    paint_color(P, paintX, paintY, pathID, fx, fy, 1.f, unmultiplied, color, features);
     float dst[4];
     unpack_rgba8(s.color, dst);
     if (unmultiplied)
@@ -3053,5 +3166,26 @@ void feather_table_f16(uint16_t out[kGaussianTableSize])
     build_feather_table(table);
     for (int i = 0; i < kGaussianTableSize; ++i)
         out[i] = __half_as_ushort(__float2half_rn(table[i]));
+}
+
+// One mip level of an image from the level above it: each texel the rounded
+// mean of the (up to) 2x2 texels it covers, edges clamped.
+__global__ void __launch_bounds__(256) mip_level_kernel(const uchar4* __restrict__ src,
+                                                        uint32_t sw, uint32_t sh,
+                                                        uchar4* __restrict__ dst, uint32_t dw,
+                                                        uint32_t dh)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= dw * dh)
+        return;
+    const uint32_t x = i % dw, y = i / dw;
+    const uint32_t x0 = min(2 * x, sw - 1), x1 = min(2 * x + 1, sw - 1);
+    const uint32_t y0 = min(2 * y, sh - 1), y1 = min(2 * y + 1, sh - 1);
+    const uchar4 a = src[(size_t)y0 * sw + x0], b = src[(size_t)y0 * sw + x1];
+    const uchar4 c = src[(size_t)y1 * sw + x0], d = src[(size_t)y1 * sw + x1];
+    dst[i] = make_uchar4((unsigned char)((a.x + b.x + c.x + d.x + 2u) >> 2),
+                         (unsigned char)((a.y + b.y + c.y + d.y + 2u) >> 2),
+                         (unsigned char)((a.z + b.z + c.z + d.z + 2u) >> 2),
+                         (unsigned char)((a.w + b.w + c.w + d.w + 2u) >> 2));
 }
 } // namespace rivecuda

@@ -181,6 +181,20 @@ struct __align__(16) TriRecord
 };
 static_assert(sizeof(TriRecord) == 96, "TriRecord layout");
 
+// An image texture in device memory: RGBA8 premultiplied texels of every mip
+// level, level l at texel offset off[l] with size max(w >> l, 1) x
+// max(h >> l, 1); `sampler` is the ImageSampler key it is drawn with
+// (include/rive/shapes/paint/image_sampler.hpp: wrapX + 3 wrapY + 9 filter).
+constexpr int kMaxMipLevels = 16;
+struct ImageTex
+{
+    const uchar4* texels;
+    uint32_t width, height, levels, sampler;
+    uint32_t off[kMaxMipLevels];
+};
+constexpr uint32_t PAINT_FLAG_HAS_IMAGE = 0x800u;
+constexpr uint32_t kNoImage = 0xffffffffu;
+
 struct FlushParams
 {
     // Record buffers at the frame's element 0.
@@ -220,6 +234,10 @@ struct FlushParams
     uint16_t* atlas;
     uint32_t atlasW, atlasH;
     uint32_t atlasMode;
+    // Images: the batch's image table, and per path of this flush the slot of
+    // the image its paint modulates (kNoImage: none), written by the set-up.
+    const ImageTex* images;
+    uint32_t* pathImage;
 };
 
 // One DrawBatch of one flush in a set-up work list: its first element (patch
@@ -232,6 +250,8 @@ struct PatchSegment
     // left | top << 16 and right | bottom << 16: an atlas batch's scissor, or
     // everything (0, 0xffffffff) for the draw batches of a main scene.
     uint32_t scissorLT, scissorRB;
+    // The draw batch's image: a slot of the batch's image table, or kNoImage.
+    uint32_t image;
 };
 
 // Set-up work lists: midpoint-fan patches, outer-curve patches, interior

@@ -42,7 +42,14 @@ class FlushDesc(ctypes.Structure):
         (n, ctypes.c_uint32) for n in (
             "atlas_texture_width", "atlas_texture_height", "atlas_content_width",
             "atlas_content_height", "atlas_fill_batch_count",
-            "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p)]
+            "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p),
+                                            ("batch_images", ctypes.c_void_p)]
+
+
+class BatchImage(ctypes.Structure):
+    """rive_cuda_batch_image."""
+    _fields_ = [("texture", ctypes.c_void_p), ("sampler_key", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class DeviceBuffers(ctypes.Structure):
@@ -117,6 +124,9 @@ def load():
         "rive_cuda_read_tess_texture": (i32, [vp, vp, sz]),
         "rive_cuda_read_grad_texture": (i32, [vp, vp, sz]),
         "rive_cuda_read_atlas_texture": (i32, [vp, vp, sz]),
+        "rive_cuda_texture_create": (i32, [vp, u32, u32, u32, vp, ctypes.POINTER(vp)]),
+        "rive_cuda_texture_destroy": (None, [vp, vp]),
+        "rive_cuda_texture_read": (i32, [vp, vp, u32, vp, sz]),
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
@@ -140,7 +150,10 @@ def load():
     return lib
 
 
-def make_desc(flush):
+def make_desc(flush, textures=None):
+    """rive_cuda_flush_desc for one capture.Flush. `textures` maps the
+    capture's texture indices to rive_cuda_texture handles (needed when a
+    batch draws an image). Returns (desc, arrays to keep alive)."""
     d = FlushDesc()
     for k, v in flush.desc.items():
         if k.startswith("ub"):
@@ -155,7 +168,17 @@ def make_desc(flush):
     atlas = np.ascontiguousarray(getattr(flush, "atlas", np.zeros((0, 4), np.uint32)),
                                  dtype=np.uint32).reshape(-1, 4)
     d.atlas_batches = atlas.ctypes.data if len(atlas) else None
-    return d, (batches, atlas)
+    images = None
+    if getattr(flush, "has_images", False):
+        if textures is None:
+            raise RiveCudaError("the flush draws images: pass its textures")
+        images = (BatchImage * len(batches))()
+        for i, (tex, key) in enumerate(np.asarray(flush.images, dtype=np.uint32)):
+            if tex != 0xFFFFFFFF:
+                images[i].texture = textures[int(tex)]
+                images[i].sampler_key = int(key)
+        d.batch_images = ctypes.addressof(images)
+    return d, (batches, atlas, images)
 
 
 def feather_table():
@@ -248,12 +271,16 @@ class Context:
         self.h = h
         self._targets = []
         self._capacity = {}
+        self._textures = {}  # id(capture.Texture) -> (texture, handle)
 
     def close(self):
         if self.h:
             for t in self._targets:
                 self.lib.rive_cuda_render_target_destroy(self.h, t)
             self._targets = []
+            for _, handle in self._textures.values():
+                self.lib.rive_cuda_texture_destroy(self.h, handle)
+            self._textures = {}
             self.lib.rive_cuda_context_destroy(self.h)
             self.h = None
 
@@ -297,24 +324,49 @@ class Context:
         self._targets.append(t)
         return t
 
+    def textures_for(self, flush):
+        """Device textures (rive_cuda_texture handles) for the capture
+        textures a flush's batches sample, created once per texture."""
+        if not getattr(flush, "has_images", False):
+            return None
+        out = []
+        for t in flush.textures:
+            key = id(t)
+            if key not in self._textures:
+                h = ctypes.c_void_p()
+                data = np.frombuffer(t.rgba, np.uint8)
+                self.check(self.lib.rive_cuda_texture_create(
+                    self.h, t.width, t.height, t.mip_levels,
+                    data.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h)), "texture_create")
+                self._textures[key] = (t, h)
+            out.append(self._textures[key][1].value)
+        return out
+
+    def read_texture(self, handle, level, width, height):
+        """Mip level `level` (width x height texels) of a device texture."""
+        out = np.zeros((height, width, 4), np.uint8)
+        self.check(self.lib.rive_cuda_texture_read(self.h, ctypes.c_void_p(handle), level,
+                                                    out.ctypes.data_as(ctypes.c_void_p),
+                                                    out.nbytes), "texture_read")
+        return out
+
     def flush(self, flush, target, stream=None):
-        d, keep = make_desc(flush)
+        d, keep = make_desc(flush, self.textures_for(flush))
         self.check(self.lib.rive_cuda_flush(self.h, ctypes.byref(d), target, stream), "flush")
         del keep
 
     def flush_device(self, flush, bufs: DeviceBuffers, target_ptr: int, stream=None):
-        d, keep = make_desc(flush)
+        d, keep = make_desc(flush, self.textures_for(flush))
         self.check(self.lib.rive_cuda_flush_device(self.h, ctypes.byref(d), ctypes.byref(bufs),
                                                    ctypes.c_void_p(target_ptr), stream),
                    "flush_device")
         del keep
 
-    @staticmethod
-    def _batch_array(items):
+    def _batch_array(self, items):
         arr = (BatchFlush * max(len(items), 1))()
         keep = []
         for i, (flush, bufs, target_ptr) in enumerate(items):
-            d, k = make_desc(flush)
+            d, k = make_desc(flush, self.textures_for(flush))
             keep.append((d, k))
             arr[i].desc = ctypes.cast(ctypes.pointer(d), ctypes.c_void_p)
             arr[i].buffers = bufs

@@ -441,3 +441,58 @@ def feathered_atlas(seed: int = 35, width: int = 384, height: int = 320, n_paths
             if paint.style == STYLE_FILL:
                 sc.paths[a].fill_rule = FILL_CLOCKWISE
     return sc
+
+
+def _procedural_image(rng, w: int, h: int) -> Image:
+    """A w x h test image: a two-colour checker under a diagonal gradient with
+    a soft transparent disc, premultiplied RGBA8."""
+    y, x = np.mgrid[0:h, 0:w].astype(np.float32)
+    cell = float(rng.integers(2, 9))
+    check = ((np.floor(x / cell) + np.floor(y / cell)) % 2)[..., None]
+    c0, c1 = rng.uniform(0, 1, 3), rng.uniform(0, 1, 3)
+    rgb = c0 * (1 - check) + c1 * check
+    t = ((x / max(w - 1, 1) + y / max(h - 1, 1)) * .5)[..., None]
+    rgb = rgb * (1 - .5 * t) + rng.uniform(0, 1, 3) * (.5 * t)
+    cx, cy, r = w * rng.uniform(.3, .7), h * rng.uniform(.3, .7), min(w, h) * rng.uniform(.2, .45)
+    d = np.sqrt((x - cx) ** 2 + (y - cy) ** 2)
+    a = np.clip(.35 + (d - r) / max(r * .5, 1.0), .35, 1.0)[..., None]
+    rgba = np.concatenate([rgb * a, a], -1)
+    return Image(np.clip(np.rint(rgba * 255), 0, 255).astype(np.uint8))
+
+
+def images(seed: int = 41, width: int = 384, height: int = 320, n_images: int = 6,
+           n_draws: int = 24, n_paths: int = 16) -> Scene:
+    """Images drawn with Renderer::drawImage between full-feature paths: each of
+    `n_images` procedural images (power-of-two and odd sizes, 7..200 px)
+    drawn under random affine transforms (magnified and minified, so the mip
+    chain is sampled), with every ImageSampler (bilinear / nearest, clamp /
+    repeat / mirror), opacity in [0.3, 1], some with advanced blend modes and
+    some under clip paths."""
+    rng = np.random.default_rng(seed)
+    sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=8,
+                      p_clip=0.2, scale_range=(0.5, 2.0))
+    sizes = [(64, 64), (128, 32), (7, 13), (200, 90), (33, 33), (16, 128)]
+    for k in range(n_images):
+        w, h = sizes[k % len(sizes)]
+        sc.add_image(_procedural_image(rng, w, h))
+    clip_paths = [i for i, _ in enumerate(sc.paths)]
+    for k in range(n_draws):
+        im = int(rng.integers(0, n_images))
+        w, h = sc.images[im].rgba.shape[1], sc.images[im].rgba.shape[0]
+        # Target size 12..260 px along the longer side, rotated.
+        target = float(np.exp(rng.uniform(np.log(12), np.log(260))))
+        s = target / max(w, h)
+        th = rng.uniform(0, 2 * np.pi)
+        c, sn = np.cos(th) * s, np.sin(th) * s
+        tx, ty = rng.uniform(0, width), rng.uniform(0, height)
+        sc.cmd(CMD_SAVE)
+        sc.cmd(CMD_TRANSFORM, m=(c, sn, -sn, c, tx - (c * w - sn * h) / 2,
+                                 ty - (sn * w + c * h) / 2))
+        if clip_paths and rng.uniform() < 0.2:
+            sc.cmd(CMD_CLIP_PATH, int(rng.choice(clip_paths)))
+        blend = int(rng.choice(BLEND_MODES)) if rng.uniform() < 0.25 else BLEND_SRC_OVER
+        sampler = sampler_key(int(rng.integers(0, 3)), int(rng.integers(0, 3)),
+                              int(rng.integers(0, 2)))
+        sc.draw_image(im, float(rng.uniform(0.3, 1.0)), blend, sampler)
+        sc.cmd(CMD_RESTORE)
+    return sc

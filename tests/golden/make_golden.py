@@ -108,6 +108,11 @@ SCENES["feather_atlas_s35"] = lambda: scene.feathered_atlas(seed=35)
 # direct feathers of feathered_s33, within the image tolerance.
 SCENES["feathered_atlas_s33"] = lambda: _atlas_always(scene.feathered(seed=33))
 
+# Images drawn with Renderer::drawImage (a rectangle path with an image paint
+# in rasterOrdering, rive_renderer.cpp:383-446): every ImageSampler, magnified
+# and minified (mip levels), opacity, blend modes, clips.
+SCENES["images_s41"] = lambda: scene.images(seed=41)
+
 # Real frames whose wide feathers the reference front end sends through the
 # feather atlas (feathered draws kept).
 ATLAS_SILVERS = {

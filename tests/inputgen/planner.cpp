@@ -2781,6 +2781,8 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
                     r.stack.back().modulatedOpacity =
                         std::max(0.0f, r.stack.back().modulatedOpacity * c.m[0]);
                     break;
+                case RIVE_SCENE_CMD_DRAW_IMAGE:
+                    throw PlanError("image draws are not planned here (the reference front end plans them)");
                 default:
                     throw PlanError("bad command");
             }

@@ -41,6 +41,11 @@ def test_planner_matches_golden_capture(name):
         with pytest.raises(RuntimeError, match="feathered"):
             planner.plan(scene_bytes)
         return
+    if cap.textures:
+        # And image draws.
+        with pytest.raises(RuntimeError, match="image"):
+            planner.plan(scene_bytes)
+        return
     got = planner.plan(scene_bytes)
     assert diff_captures(cap, got) == []
 

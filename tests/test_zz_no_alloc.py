@@ -32,9 +32,9 @@ def _fits(cap):
 
 def _fans_only(cap):
     # The no-allocation path draws midpoint-fan batches only (no interior
-    # triangulation, no center-AA fans of feathered fills).
-    return not any(f.desc["has_triangle_vertices"] or (f.batches[:, 0] != 0).any()
-                   for f in cap.flushes)
+    # triangulation, no center-AA fans of feathered fills) and no images.
+    return not cap.textures and not any(
+        f.desc["has_triangle_vertices"] or (f.batches[:, 0] != 0).any() for f in cap.flushes)
 
 
 def _context_image(cap, bufs, stream):
