@@ -562,7 +562,9 @@ struct BatchLayout
     // table), and the per-path image slots of every main scene.
     uint32_t imageSlots = 0;
     size_t oImages = 0;
-    bool feather = false; // some batch draws with ENABLE_FEATHER
+    // The extended kernel variants: some batch feathers, blits the feather
+    // atlas or samples an image.
+    bool feather = false;
     // Interior tiles as winding records for this batch: midpoint-fan patches
     // then take fanStride slots (their 24 triangles and a winding slot).
     bool winding = false;
@@ -622,7 +624,10 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             if ((db.shader_features & SF_FEATHER) || db.draw_type == DRAW_FEATHER_ATLAS_BLIT)
                 L.feather = true;
             if (d->batch_images && d->batch_images[b].texture)
+            {
                 ++L.imageSlots;
+                L.feather = true; // the raster's extended variant samples images
+            }
         }
         L.tessRow0[i] = L.tessRows;
         L.gradRow0[i] = L.gradRows;

@@ -2363,6 +2363,10 @@ __device__ __noinline__ void image_modulate(const FlushParams& P, uint32_t pathI
 // gives the same result. The one value an earlier fragment feeds forward is
 // the nested-clip stash, which the reference keeps in RGBA8: its
 // quantisation is applied when the path had more than one fragment here.
+// kImages: the image paint is compiled in (the raster's feather variants,
+// which batches with images or feathers use); the plain variant's resolve
+// stays without it.
+template <bool kImages>
 __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float fx, float fy,
                                           float dither)
 {
@@ -2425,7 +2429,8 @@ __device__ __noinline__ void resolve_path(const FlushParams& P, Pixel& s, float 
 
     const bool unmultiplied = (features & SF_ADVANCED_BLEND) != 0;
     float color[4];
-    paint_color(P, paintX, paintY, pathID, fx, fy, coverage, unmultiplied, color, features);
+    paint_color(P, paintX, paintY, pathID, fx, fy, coverage, unmultiplied, color,
+                kImages ? features : 0u);
 
     float dst[4];
     unpack_rgba8(s.color, dst);
@@ -2790,7 +2795,7 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                 {
                     if (s.pendMeta)
                     {
-                        resolve_path(P, s, fx, fy, dither);
+                        resolve_path<kFeather>(P, s, fx, fy, dither);
                         s.pendMeta = 0;
                     }
                     streamPath = vPathID;
@@ -2816,7 +2821,7 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                     // (key and count) to whichever path owns it.
                     if (s.pendMeta)
                     {
-                        resolve_path(P, s, fx, fy, dither);
+                        resolve_path<kFeather>(P, s, fx, fy, dither);
                         s.pendMeta = 0;
                     }
                     const uint4 v4 = T.v4;
@@ -2827,7 +2832,7 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                 if (s.key != vPathID)
                 {
                     if (s.pendMeta)
-                        resolve_path(P, s, fx, fy, dither);
+                        resolve_path<kFeather>(P, s, fx, fy, dither);
                     const uint4 v4 = T.v4;
                     s.pendMeta = v4.z;
                     s.pendPaintX = v4.x;
@@ -2865,7 +2870,7 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
         __syncthreads();
     }
     if (s.pendMeta)
-        resolve_path(P, s, fx, fy, dither);
+        resolve_path<kFeather>(P, s, fx, fy, dither);
     if (inBounds)
         fb[(size_t)py * P.width + px] = s.color;
 }
