@@ -23,7 +23,7 @@
 extern "C" {
 #endif
 
-#define RIVE_CUDA_ABI_VERSION 1
+#define RIVE_CUDA_ABI_VERSION 2 /* 2: image meshes (render buffers, batch_meshes, image_draws) */
 
 /* Status codes. */
 enum
@@ -53,7 +53,7 @@ enum
     RIVE_CUDA_BUFFER_GRAD_SPAN = 5,     /* gpu::GradientSpan, 16 B each        */
     RIVE_CUDA_BUFFER_TESS_SPAN = 6,     /* gpu::TessVertexSpan, 64 B each      */
     RIVE_CUDA_BUFFER_TRIANGLE = 7,      /* gpu::TriangleVertex, 12 B each      */
-    RIVE_CUDA_BUFFER_IMAGE_DRAW = 8,    /* gpu::ImageDrawInstance (unsupported)*/
+    RIVE_CUDA_BUFFER_IMAGE_DRAW = 8,    /* gpu::ImageDrawInstance, 64 B each   */
     RIVE_CUDA_BUFFER_KIND_COUNT = 9,
 };
 
@@ -107,6 +107,39 @@ typedef struct rive_cuda_batch_image
     uint32_t sampler_key;
     uint32_t reserved;
 } rive_cuda_batch_image;
+
+/*
+ * A RenderBuffer (RenderContextImpl::makeRenderBuffer,
+ * render_context_impl.hpp:36-39): the vertex, texture-coordinate or index data
+ * of image meshes, in device memory. Created, written and destroyed with
+ * rive_cuda_render_buffer_create / _write / _destroy.
+ */
+typedef struct rive_cuda_render_buffer rive_cuda_render_buffer;
+
+/* rive::RenderBufferType (include/rive/renderer.hpp:37-41). */
+enum
+{
+    RIVE_CUDA_RENDER_BUFFER_INDEX = 0,
+    RIVE_CUDA_RENDER_BUFFER_VERTEX = 1,
+};
+
+/*
+ * The mesh an imageMesh draw batch draws (gpu::DrawBatch::vertexBuffer,
+ * uvBuffer, indexBuffer and indexCountPerInstance, gpu.hpp:1257-1264;
+ * RiveRenderer::drawImageMesh, rive_renderer.cpp:448-495): float2 positions
+ * in the draw's local space, float2 texture coordinates, and a uint16
+ * triangle list. The batch's ImageDrawInstance (its base_element) carries the
+ * matrix, opacity, clip and blend mode; its rive_cuda_batch_image the texture
+ * and sampler.
+ */
+typedef struct rive_cuda_batch_mesh
+{
+    const rive_cuda_render_buffer* vertices; /* NULL: the batch draws no mesh */
+    const rive_cuda_render_buffer* uvs;
+    const rive_cuda_render_buffer* indices;
+    uint32_t index_count;
+    uint32_t reserved;
+} rive_cuda_batch_mesh;
 
 /*
  * One gpu::DrawBatch (gpu.hpp:1219-1282), flattened. The reference keeps the
@@ -179,6 +212,9 @@ typedef struct rive_cuda_flush_desc
     /* Images: NULL, or one entry per draw batch (the batch's texture and
      * sampler; paths with an image paint, ENABLE_MODULATED_IMAGE). */
     const rive_cuda_batch_image* batch_images;
+    /* Image meshes: NULL, or one entry per draw batch (the mesh of each
+     * imageMesh batch; others NULL). */
+    const rive_cuda_batch_mesh* batch_meshes;
 } rive_cuda_flush_desc;
 
 typedef struct rive_cuda_context rive_cuda_context;
@@ -243,6 +279,25 @@ int rive_cuda_texture_read(rive_cuda_context* ctx,
                            size_t bytes);
 
 /*
+ * RenderContextImpl::makeRenderBuffer (render_context_impl.hpp:36-39): a
+ * device buffer of `bytes` bytes (zeroed) of type RIVE_CUDA_RENDER_BUFFER_*.
+ * rive_cuda_render_buffer_write copies bytes from host memory into it at
+ * `offset` (RenderBuffer::unmap), ordered after the work already queued on
+ * the context's stream, and returns once they are on the device. Destroying
+ * a buffer waits for the context's stream first.
+ */
+int rive_cuda_render_buffer_create(rive_cuda_context* ctx,
+                                   uint32_t type,
+                                   size_t bytes,
+                                   rive_cuda_render_buffer** out_buffer);
+int rive_cuda_render_buffer_write(rive_cuda_context* ctx,
+                                  rive_cuda_render_buffer* buffer,
+                                  size_t offset,
+                                  const void* src_host,
+                                  size_t bytes);
+void rive_cuda_render_buffer_destroy(rive_cuda_context* ctx, rive_cuda_render_buffer* buffer);
+
+/*
  * Render targets (gpu::RenderTarget, render_target.hpp): an RGBA8 image in
  * device memory, rows of width*4 bytes, row 0 at the top.
  */
@@ -304,6 +359,7 @@ typedef struct rive_cuda_device_buffers
     const void* grad_spans;
     const void* tess_spans;
     const void* triangle_vertices; /* gpu::TriangleVertex, 12 B each; may be NULL */
+    const void* image_draws;       /* gpu::ImageDrawInstance, 64 B each; may be NULL */
 } rive_cuda_device_buffers;
 
 int rive_cuda_flush_device(rive_cuda_context* ctx,
@@ -404,7 +460,7 @@ void rive_cuda_graph_destroy(rive_cuda_graph* graph);
 #define RIVE_CUDA_NOALLOC_MAX_PATCHES 8192u /* 32 rows x 2048 vertices / 8 */
 #define RIVE_CUDA_NOALLOC_MAX_GRAD_ROWS 64u
 #define RIVE_CUDA_NOALLOC_MAX_BIN_ENTRIES 1048576u
-#define RIVE_CUDA_NOALLOC_POOL_BYTES 42902528u /* about 40.9 MiB */
+#define RIVE_CUDA_NOALLOC_POOL_BYTES 42903552u /* about 40.9 MiB */
 int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* desc,
                                    const rive_cuda_device_buffers* buffers,
                                    void* target_pixels_device,

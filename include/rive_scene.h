@@ -17,6 +17,11 @@
  * and, only when the frame draws images:
  *   rive_scene_images { magic "RSI1", count }
  *   count x { rive_scene_image, uint8_t rgba[width * height * 4] }
+ * and after them, only when the frame draws image meshes:
+ *   rive_scene_meshes { magic "RSM1", count }
+ *   count x { rive_scene_mesh, float xy[vertex_count * 2],
+ *             float uv[vertex_count * 2],
+ *             uint16_t indices[index_count] (padded to 4 bytes) }
  */
 #ifndef RIVE_SCENE_H
 #define RIVE_SCENE_H
@@ -48,6 +53,11 @@ enum
      * mode | ImageSampler key << 8, m[0] = opacity. The image covers the unit
      * square scaled to its size under the current transform. */
     RIVE_SCENE_CMD_DRAW_IMAGE = 6,
+    /* Renderer::drawImageMesh (renderer.hpp:222-230): a = image index, b =
+     * blend mode | ImageSampler key << 8, m[0] = opacity, m[1] = mesh index
+     * (an integer held exactly in the float). The mesh's vertex, uv and index
+     * data become three RenderBuffers. */
+    RIVE_SCENE_CMD_DRAW_IMAGE_MESH = 7,
 };
 
 /* rive::RenderPaintStyle / gradient kinds. */
@@ -152,5 +162,21 @@ typedef struct rive_scene_image
     uint32_t width;
     uint32_t height;
 } rive_scene_image;
+
+#define RIVE_SCENE_MESHES_MAGIC 0x314d5352u /* "RSM1" */
+
+typedef struct rive_scene_meshes
+{
+    uint32_t magic;
+    uint32_t count;
+} rive_scene_meshes;
+
+/* A mesh: local positions, texture coordinates (normalised; the sampler
+ * wraps them) and a triangle list. */
+typedef struct rive_scene_mesh
+{
+    uint32_t vertex_count;
+    uint32_t index_count;
+} rive_scene_mesh;
 
 #endif /* RIVE_SCENE_H */

@@ -15,13 +15,23 @@
 #include <string.h>
 
 #define KINDS RIVE_CUDA_BUFFER_KIND_COUNT
-#define CAPTURED_KINDS 7 /* flush uniforms .. tess spans (+ triangle vertices) */
+#define CAPTURED_KINDS 7 /* flush uniforms .. tess spans (+ triangle vertices, image draws) */
 #define MAX_FLUSHES 256
 #define MAX_TEXTURES 4096
+#define MAX_SNAPSHOTS 4096
 
 struct rive_cuda_texture
 {
     uint32_t index; /* in the context's texture table */
+};
+
+/* A render buffer: its bytes, and a version each write advances. */
+struct rive_cuda_render_buffer
+{
+    uint32_t type;
+    size_t bytes;
+    unsigned char* data;
+    uint64_t id, version;
 };
 
 struct rive_cuda_context
@@ -39,6 +49,13 @@ struct rive_cuda_context
     uint32_t texture_dims[3 * MAX_TEXTURES];
     unsigned char* texture_texels[MAX_TEXTURES];
     rive_cuda_texture* textures[MAX_TEXTURES];
+    uint32_t* meshes[MAX_FLUSHES]; /* 4 per batch, or NULL */
+    /* Render-buffer contents the flushes drew (one per buffer and version). */
+    uint32_t snapshot_count;
+    uint64_t snapshot_id[MAX_SNAPSHOTS], snapshot_version[MAX_SNAPSHOTS];
+    uint32_t snapshot_type[MAX_SNAPSHOTS], snapshot_bytes[MAX_SNAPSHOTS];
+    unsigned char* snapshot_data[MAX_SNAPSHOTS];
+    uint64_t next_buffer_id;
     uint32_t width, height;
     int failed;
 };
@@ -74,7 +91,10 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         free(ctx->batches[i]);
         free(ctx->atlas[i]);
         free(ctx->images[i]);
+        free(ctx->meshes[i]);
     }
+    for (uint32_t i = 0; i < ctx->snapshot_count; ++i)
+        free(ctx->snapshot_data[i]);
     for (uint32_t i = 0; i < ctx->texture_count; ++i)
     {
         free(ctx->texture_texels[i]);
@@ -120,6 +140,76 @@ int rive_cuda_texture_create(rive_cuda_context* ctx,
 void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* texture)
 {
     (void)ctx, (void)texture;
+}
+
+int rive_cuda_render_buffer_create(rive_cuda_context* ctx,
+                                   uint32_t type,
+                                   size_t bytes,
+                                   rive_cuda_render_buffer** out)
+{
+    if (!ctx || !out || bytes == 0)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    rive_cuda_render_buffer* b = (rive_cuda_render_buffer*)calloc(1, sizeof(*b));
+    unsigned char* data = (unsigned char*)calloc(1, bytes);
+    if (!b || !data)
+    {
+        free(b);
+        free(data);
+        return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+    }
+    b->type = type;
+    b->bytes = bytes;
+    b->data = data;
+    b->id = ctx->next_buffer_id++;
+    *out = b;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_render_buffer_write(rive_cuda_context* ctx,
+                                  rive_cuda_render_buffer* b,
+                                  size_t offset,
+                                  const void* src,
+                                  size_t bytes)
+{
+    if (!ctx || !b || offset > b->bytes || bytes > b->bytes - offset || (!src && bytes))
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    if (bytes)
+        memcpy(b->data + offset, src, bytes);
+    ++b->version;
+    return RIVE_CUDA_OK;
+}
+
+void rive_cuda_render_buffer_destroy(rive_cuda_context* ctx, rive_cuda_render_buffer* b)
+{
+    (void)ctx;
+    if (!b)
+        return;
+    free(b->data);
+    free(b);
+}
+
+/* The snapshot index of a buffer's current contents (recorded on first use). */
+static uint32_t snapshot(rive_cuda_context* ctx, const rive_cuda_render_buffer* b)
+{
+    for (uint32_t i = 0; i < ctx->snapshot_count; ++i)
+        if (ctx->snapshot_id[i] == b->id && ctx->snapshot_version[i] == b->version)
+            return i;
+    if (ctx->snapshot_count >= MAX_SNAPSHOTS)
+    {
+        ctx->failed = 1;
+        return 0xffffffffu;
+    }
+    const uint32_t i = ctx->snapshot_count++;
+    ctx->snapshot_id[i] = b->id;
+    ctx->snapshot_version[i] = b->version;
+    ctx->snapshot_type[i] = b->type;
+    ctx->snapshot_bytes[i] = (uint32_t)b->bytes;
+    ctx->snapshot_data[i] = (unsigned char*)malloc(b->bytes);
+    if (ctx->snapshot_data[i])
+        memcpy(ctx->snapshot_data[i], b->data, b->bytes);
+    else
+        ctx->failed = 1;
+    return i;
 }
 
 int rive_cuda_texture_read(rive_cuda_context* ctx,
@@ -259,6 +349,36 @@ int rive_cuda_flush(rive_cuda_context* ctx,
         else
             free(im);
     }
+    ctx->descs[i].batch_meshes = NULL;
+    ctx->meshes[i] = NULL;
+    if (desc->batch_meshes && n)
+    {
+        int any = 0;
+        uint32_t* me = (uint32_t*)malloc(n * 16);
+        if (!me)
+            return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+        for (size_t b = 0; b < n; ++b)
+        {
+            const rive_cuda_batch_mesh* m = &desc->batch_meshes[b];
+            if (m->vertices && m->uvs && m->indices)
+            {
+                me[4 * b] = snapshot(ctx, m->vertices);
+                me[4 * b + 1] = snapshot(ctx, m->uvs);
+                me[4 * b + 2] = snapshot(ctx, m->indices);
+                me[4 * b + 3] = m->index_count;
+                any = 1;
+            }
+            else
+            {
+                me[4 * b] = me[4 * b + 1] = me[4 * b + 2] = 0xffffffffu;
+                me[4 * b + 3] = 0;
+            }
+        }
+        if (any)
+            ctx->meshes[i] = me;
+        else
+            free(me);
+    }
     return RIVE_CUDA_OK;
 }
 
@@ -277,13 +397,26 @@ int abi_recorder_write(const char* path)
     FILE* f = fopen(path, "wb");
     if (!f)
         return 1;
-    /* Seven kinds, or eight when the frame has interior triangles. */
-    const uint32_t kinds = ctx->bytes[CAPTURED_KINDS] ? CAPTURED_KINDS + 1 : CAPTURED_KINDS;
-    int v2 = ctx->texture_count != 0;
+    /* Seven kinds, eight when the frame has interior triangles, nine when it
+     * has image draw instances. */
+    const uint32_t kinds = ctx->bytes[CAPTURED_KINDS + 1]  ? CAPTURED_KINDS + 2
+                           : ctx->bytes[CAPTURED_KINDS] ? CAPTURED_KINDS + 1
+                                                        : CAPTURED_KINDS;
+    if (ctx->failed)
+    {
+        fclose(f);
+        return 1;
+    }
+    int v3 = ctx->snapshot_count != 0;
+    for (uint32_t i = 0; i < ctx->flush_count; ++i)
+        v3 = v3 || ctx->meshes[i] != NULL;
+    int v2 = v3 || ctx->texture_count != 0;
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
         v2 = v2 || rive_capture_flush_has_atlas(&ctx->descs[i]) || ctx->images[i] != NULL;
-    uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, ctx->width,
-                        ctx->height, kinds};
+    uint32_t head[4] = {v3   ? RIVE_CAPTURE_MAGIC_V3
+                        : v2 ? RIVE_CAPTURE_MAGIC_V2
+                             : RIVE_CAPTURE_MAGIC_V1,
+                        ctx->width, ctx->height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const unsigned char zeros[8] = {0};
     for (uint32_t k = 0; k < kinds; ++k)
@@ -297,10 +430,14 @@ int abi_recorder_write(const char* path)
     fwrite(&ctx->flush_count, sizeof(uint32_t), 1, f);
     for (uint32_t i = 0; i < ctx->flush_count; ++i)
         rive_capture_write_flush(f, &ctx->descs[i], ctx->batches[i], ctx->atlas[i], ctx->images[i],
-                                 v2);
+                                 ctx->meshes[i], v2, v3);
     if (v2)
         rive_capture_write_textures(f, ctx->texture_count, ctx->texture_dims,
                                     (const uint8_t* const*)ctx->texture_texels);
+    if (v3)
+        rive_capture_write_render_buffers(f, ctx->snapshot_count, ctx->snapshot_type,
+                                          ctx->snapshot_bytes,
+                                          (const uint8_t* const*)ctx->snapshot_data);
     fclose(f);
     return 0;
 }

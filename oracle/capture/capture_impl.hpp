@@ -18,7 +18,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <utility>
 #include <vector>
 
 namespace capture
@@ -54,6 +56,27 @@ struct FlushRecord
     std::vector<rive_cuda_draw_batch> batches;
     std::vector<rive_cuda_atlas_batch> atlasBatches; // fills, then strokes
     std::vector<uint32_t> images; // per batch: texture index (~0u: none), sampler key
+    // Per batch: vertex, uv and index render-buffer indices (~0u: not a
+    // mesh) and the index count; empty when no batch draws an image mesh.
+    std::vector<uint32_t> meshes;
+};
+
+// A RenderBuffer the front end asked for (makeRenderBuffer): host bytes, and
+// a version that each unmap advances, so a flush records the contents it
+// drew.
+class CaptureRenderBuffer : public RenderBuffer
+{
+public:
+    CaptureRenderBuffer(RenderBufferType type, RenderBufferFlags flags, size_t bytes, uint64_t id) :
+        RenderBuffer(type, flags, bytes), data(bytes), id(id)
+    {}
+    std::vector<uint8_t> data;
+    uint64_t id;
+    uint64_t version = 0;
+
+protected:
+    void* onMap() override { return data.data(); }
+    void onUnmap() override { ++version; }
 };
 
 // An image texture the front end asked for (makeImageTexture): its index in
@@ -68,12 +91,37 @@ public:
 class CaptureImpl : public RenderContextNULL
 {
 public:
-    // Buffers in rive_cuda.h kind order 0..7.
-    std::vector<uint8_t> buffers[8];
+    // Buffers in rive_cuda.h kind order 0..8.
+    std::vector<uint8_t> buffers[9];
     std::vector<FlushRecord> flushes;
     // Image textures: width, height, mip levels and level-0 texels.
     std::vector<uint32_t> textureDims;
     std::vector<std::vector<uint8_t>> textureTexels;
+    // Render-buffer contents the flushes drew: type and bytes.
+    std::vector<uint32_t> renderBufferTypes;
+    std::vector<std::vector<uint8_t>> renderBufferData;
+
+    rcp<RenderBuffer> makeRenderBuffer(RenderBufferType type,
+                                       RenderBufferFlags flags,
+                                       size_t bytes) override
+    {
+        return make_rcp<CaptureRenderBuffer>(type, flags, bytes, m_nextBufferID++);
+    }
+
+    // The render-buffer table index of a buffer's current contents.
+    uint32_t snapshot(const RenderBuffer* b)
+    {
+        const auto* cb = static_cast<const CaptureRenderBuffer*>(b);
+        const auto key = std::make_pair(cb->id, cb->version);
+        auto it = m_snapshots.find(key);
+        if (it != m_snapshots.end())
+            return it->second;
+        const uint32_t index = static_cast<uint32_t>(renderBufferData.size());
+        renderBufferTypes.push_back(static_cast<uint32_t>(cb->type()));
+        renderBufferData.push_back(cb->data);
+        m_snapshots.emplace(key, index);
+        return index;
+    }
 
     rcp<Texture> makeImageTexture(uint32_t width,
                                   uint32_t height,
@@ -158,7 +206,7 @@ public:
     }
     void resizeImageDrawInstanceBuffer(size_t n) override
     {
-        m_nextVertexSink = &m_discard;
+        m_nextVertexSink = &buffers[8];
         RenderContextHelperImpl::resizeImageDrawInstanceBuffer(n);
     }
 
@@ -224,8 +272,24 @@ public:
                 const auto* tex = static_cast<const CaptureTexture*>(b.imageTexture);
                 rec.images.push_back(tex ? tex->index : ~0u);
                 rec.images.push_back(b.imageSampler.asKey());
+                if (b.drawType == DrawType::imageMesh)
+                {
+                    rec.meshes.push_back(snapshot(b.vertexBuffer));
+                    rec.meshes.push_back(snapshot(b.uvBuffer));
+                    rec.meshes.push_back(snapshot(b.indexBuffer));
+                    rec.meshes.push_back(b.indexCountPerInstance);
+                }
+                else
+                {
+                    rec.meshes.insert(rec.meshes.end(), {~0u, ~0u, ~0u, 0u});
+                }
             }
         }
+        bool anyMesh = false;
+        for (size_t i = 0; i < rec.meshes.size(); i += 4)
+            anyMesh = anyMesh || rec.meshes[i] != ~0u;
+        if (!anyMesh)
+            rec.meshes.clear();
         bool anyImage = false;
         for (size_t i = 0; i < rec.images.size(); i += 2)
             anyImage = anyImage || rec.images[i] != ~0u;
@@ -261,6 +325,8 @@ private:
     std::vector<uint8_t>* m_nextStorageSink = &m_discard;
     std::vector<uint8_t>* m_nextVertexSink = &m_discard;
     std::vector<uint8_t> m_discard;
+    uint64_t m_nextBufferID = 0;
+    std::map<std::pair<uint64_t, uint64_t>, uint32_t> m_snapshots;
 };
 
 inline std::vector<uint8_t> read_file(const char* path)
@@ -288,12 +354,19 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
     FILE* f = fopen(path, "wb");
     if (!f)
         return false;
-    // Seven buffer kinds, or eight when the frame has interior triangles.
-    const uint32_t kinds = impl.buffers[7].empty() ? 7u : 8u;
-    bool v2 = !impl.textureTexels.empty();
+    // Seven buffer kinds, eight when the frame has interior triangles, nine
+    // when it has image draw instances.
+    const uint32_t kinds = !impl.buffers[8].empty() ? 9u : impl.buffers[7].empty() ? 7u : 8u;
+    bool v3 = !impl.renderBufferData.empty();
+    for (const FlushRecord& r : impl.flushes)
+        v3 = v3 || !r.meshes.empty();
+    bool v2 = v3 || !impl.textureTexels.empty();
     for (const FlushRecord& r : impl.flushes)
         v2 = v2 || rive_capture_flush_has_atlas(&r.desc) || !r.images.empty();
-    uint32_t head[4] = {v2 ? RIVE_CAPTURE_MAGIC_V2 : RIVE_CAPTURE_MAGIC_V1, width, height, kinds};
+    uint32_t head[4] = {v3   ? RIVE_CAPTURE_MAGIC_V3
+                        : v2 ? RIVE_CAPTURE_MAGIC_V2
+                             : RIVE_CAPTURE_MAGIC_V1,
+                        width, height, kinds};
     fwrite(head, sizeof(head), 1, f);
     static const uint8_t zeros[8] = {};
     for (uint32_t k = 0; k < kinds; ++k)
@@ -308,7 +381,8 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
     fwrite(&nf, sizeof(nf), 1, f);
     for (const FlushRecord& r : impl.flushes)
         rive_capture_write_flush(f, &r.desc, r.batches.data(), r.atlasBatches.data(),
-                                 r.images.empty() ? nullptr : r.images.data(), v2);
+                                 r.images.empty() ? nullptr : r.images.data(),
+                                 r.meshes.empty() ? nullptr : r.meshes.data(), v2, v3);
     if (v2)
     {
         std::vector<const uint8_t*> texels;
@@ -316,6 +390,19 @@ inline bool write_capture(const char* path, const CaptureImpl& impl, uint32_t wi
             texels.push_back(t.data());
         rive_capture_write_textures(f, static_cast<uint32_t>(texels.size()),
                                     impl.textureDims.data(), texels.data());
+    }
+    if (v3)
+    {
+        std::vector<const uint8_t*> data;
+        std::vector<uint32_t> sizes;
+        for (const auto& b : impl.renderBufferData)
+        {
+            data.push_back(b.data());
+            sizes.push_back(static_cast<uint32_t>(b.size()));
+        }
+        rive_capture_write_render_buffers(f, static_cast<uint32_t>(data.size()),
+                                          impl.renderBufferTypes.data(), sizes.data(),
+                                          data.data());
     }
     fclose(f);
     return true;

@@ -39,6 +39,15 @@ struct SceneView
     // Images (only when the recording has an images section).
     std::vector<rive_scene_image> images;
     std::vector<const uint8_t*> imageTexels;
+    // Meshes (only when the recording has a meshes section).
+    struct Mesh
+    {
+        uint32_t vertexCount, indexCount;
+        const float* xy;
+        const float* uv;
+        const uint16_t* indices;
+    };
+    std::vector<Mesh> meshes;
 };
 
 // Returns nullptr on success, else a message.
@@ -87,6 +96,34 @@ inline const char* parse_scene(const std::vector<uint8_t>& scene, SceneView* v)
             off += bytes;
         }
     }
+    if (off + sizeof(rive_scene_meshes) <= scene.size())
+    {
+        rive_scene_meshes mh;
+        memcpy(&mh, scene.data() + off, sizeof(mh));
+        if (mh.magic != RIVE_SCENE_MESHES_MAGIC)
+            return "bad meshes magic";
+        off += sizeof(mh);
+        for (uint32_t i = 0; i < mh.count; ++i)
+        {
+            rive_scene_mesh m;
+            if (off + sizeof(m) > scene.size())
+                return "truncated meshes";
+            memcpy(&m, scene.data() + off, sizeof(m));
+            off += sizeof(m);
+            const size_t vbytes = (size_t)m.vertex_count * 8;
+            const size_t ibytes = ((size_t)m.index_count * 2 + 3) & ~(size_t)3;
+            if (m.vertex_count == 0 || m.index_count == 0 || off + 2 * vbytes + ibytes > scene.size())
+                return "truncated mesh";
+            SceneView::Mesh mv;
+            mv.vertexCount = m.vertex_count;
+            mv.indexCount = m.index_count;
+            mv.xy = reinterpret_cast<const float*>(scene.data() + off);
+            mv.uv = reinterpret_cast<const float*>(scene.data() + off + vbytes);
+            mv.indices = reinterpret_cast<const uint16_t*>(scene.data() + off + 2 * vbytes);
+            v->meshes.push_back(mv);
+            off += 2 * vbytes + ibytes;
+        }
+    }
     return nullptr;
 }
 
@@ -109,7 +146,54 @@ struct SceneResources
     std::vector<rive::rcp<rive::RenderPath>> paths;
     std::vector<rive::rcp<rive::RenderPaint>> paints;
     std::vector<rive::rcp<rive::RenderImage>> images;
+    struct Mesh
+    {
+        rive::rcp<rive::RenderBuffer> vertices, uvs, indices;
+        uint32_t vertexCount, indexCount;
+    };
+    std::vector<Mesh> meshes;
 };
+
+// A RenderBuffer of `factory` holding `bytes` bytes (Factory::makeRenderBuffer,
+// then map / copy / unmap, as an app fills one).
+inline rive::rcp<rive::RenderBuffer> make_filled_buffer(rive::Factory* factory,
+                                                        rive::RenderBufferType type,
+                                                        const void* data,
+                                                        size_t bytes)
+{
+    rive::rcp<rive::RenderBuffer> b =
+        factory->makeRenderBuffer(type, rive::RenderBufferFlags::none, bytes);
+    if (!b)
+        return nullptr;
+    void* p = b->map();
+    memcpy(p, data, bytes);
+    b->unmap();
+    return b;
+}
+
+// The scene's meshes as RenderBuffers of `factory` (vertex, uv, index).
+inline const char* make_scene_meshes(rive::Factory* factory,
+                                     const SceneView& v,
+                                     SceneResources* out)
+{
+    using namespace rive;
+    for (const SceneView::Mesh& m : v.meshes)
+    {
+        SceneResources::Mesh r;
+        r.vertexCount = m.vertexCount;
+        r.indexCount = m.indexCount;
+        r.vertices = make_filled_buffer(factory, RenderBufferType::vertex, m.xy,
+                                        (size_t)m.vertexCount * 8);
+        r.uvs = make_filled_buffer(factory, RenderBufferType::vertex, m.uv,
+                                   (size_t)m.vertexCount * 8);
+        r.indices = make_filled_buffer(factory, RenderBufferType::index, m.indices,
+                                       (size_t)m.indexCount * 2);
+        if (!r.vertices || !r.uvs || !r.indices)
+            return "cannot make a mesh buffer";
+        out->meshes.push_back(std::move(r));
+    }
+    return nullptr;
+}
 
 // The scene's images as textures of `impl` (RenderContextImpl::makeImageTexture
 // with one level of RGBA8 texels and the rest generated), wrapped as the
@@ -259,6 +343,18 @@ inline const char* issue_scene_commands(rive::Renderer* renderer,
                                     ImageSampler::SamplerFromKey(static_cast<uint8_t>(c.b >> 8)),
                                     static_cast<BlendMode>(c.b & 0xffu), c.m[0]);
                 break;
+            case RIVE_SCENE_CMD_DRAW_IMAGE_MESH:
+            {
+                const size_t mi = static_cast<size_t>(c.m[1]);
+                if (c.a >= res.images.size() || mi >= res.meshes.size())
+                    return "mesh draw references a missing image or mesh";
+                const SceneResources::Mesh& m = res.meshes[mi];
+                renderer->drawImageMesh(
+                    res.images[c.a].get(), ImageSampler::SamplerFromKey(static_cast<uint8_t>(c.b >> 8)),
+                    m.vertices, m.uvs, m.indices, m.vertexCount, m.indexCount,
+                    static_cast<BlendMode>(c.b & 0xffu), c.m[0]);
+                break;
+            }
             default:
                 return "bad command";
         }
@@ -304,6 +400,8 @@ const char* replay_scene(rive::gpu::RenderContext* ctx,
     if (const char* err = make_scene_resources(ctx, v, &res))
         return err;
     if (const char* err = make_scene_images(ctx->impl(), v, &res))
+        return err;
+    if (const char* err = make_scene_meshes(ctx, v, &res))
         return err;
     rcp<RenderTarget> target = makeTarget(v.hdr.width, v.hdr.height);
     if (!target)

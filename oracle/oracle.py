@@ -23,7 +23,7 @@ ADAPTER_CAPTURE = os.path.join(HERE, "_ref", "adapter_capture")
 REFERENCE_SOURCES = os.environ.get("RIVE_REFERENCE_DIR", "/root/reference")
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
-                "grad_spans", "tess_spans", "triangles")
+                "grad_spans", "tess_spans", "triangles", "image_draws")
 
 
 class FlushDesc(ctypes.Structure):
@@ -44,7 +44,8 @@ class FlushDesc(ctypes.Structure):
             "atlas_texture_width", "atlas_texture_height", "atlas_content_width",
             "atlas_content_height", "atlas_fill_batch_count",
             "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p),
-                                            ("batch_images", ctypes.c_void_p)]
+                                            ("batch_images", ctypes.c_void_p),
+                                            ("batch_meshes", ctypes.c_void_p)]
 
 
 class OracleTexture(ctypes.Structure):
@@ -57,6 +58,18 @@ class OracleTexture(ctypes.Structure):
 class BatchImage(ctypes.Structure):
     """rive_cuda_batch_image, its texture pointing at an OracleTexture."""
     _fields_ = [("texture", ctypes.c_void_p), ("sampler_key", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class OracleRenderBuffer(ctypes.Structure):
+    """oracle_render_buffer (passes.h)."""
+    _fields_ = [("data", ctypes.c_void_p), ("bytes", ctypes.c_size_t)]
+
+
+class BatchMesh(ctypes.Structure):
+    """rive_cuda_batch_mesh, its buffers pointing at OracleRenderBuffers."""
+    _fields_ = [("vertices", ctypes.c_void_p), ("uvs", ctypes.c_void_p),
+                ("indices", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32)]
 
 
@@ -87,6 +100,8 @@ def lib():
         _lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
         _lib.oracle_f16_to_f32.restype = ctypes.c_float
         _lib.oracle_f16_to_f32.argtypes = [ctypes.c_uint16]
+        _lib.oracle_mesh_mip_level.restype = ctypes.c_int
+        _lib.oracle_mesh_mip_level.argtypes = [ctypes.c_float, ctypes.c_float, ctypes.c_uint32]
     return _lib
 
 
@@ -115,7 +130,19 @@ def make_desc(flush):
                 images[i].texture = ctypes.addressof(textures[int(tex)][0])
                 images[i].sampler_key = int(key)
         d.batch_images = ctypes.addressof(images)
-    return d, (batches, atlas, images, textures)
+    meshes = rbufs = None
+    if getattr(flush, "has_meshes", False):
+        rbufs = [(OracleRenderBuffer(ctypes.cast(ctypes.c_char_p(b.data), ctypes.c_void_p).value,
+                                     len(b.data)), b) for b in flush.render_buffers]
+        meshes = (BatchMesh * len(batches))()
+        for i, (vb, ub, ib, n) in enumerate(np.asarray(flush.meshes, dtype=np.uint32)):
+            if vb != 0xFFFFFFFF:
+                meshes[i].vertices = ctypes.addressof(rbufs[int(vb)][0])
+                meshes[i].uvs = ctypes.addressof(rbufs[int(ub)][0])
+                meshes[i].indices = ctypes.addressof(rbufs[int(ib)][0])
+                meshes[i].index_count = int(n)
+        d.batch_meshes = ctypes.addressof(meshes)
+    return d, (batches, atlas, images, textures, meshes, rbufs)
 
 
 # Prepared oracle textures (mip chains made by oracle_texture_prepare), kept
@@ -223,6 +250,11 @@ def render_flush(cap, fi, fb, threads=0):
     _check(lib().oracle_flush(ctypes.byref(d), ctypes.byref(b),
                               fb.ctypes.data_as(ctypes.c_void_p), int(threads)), "flush")
     return fb
+
+
+def mesh_mip_level(rho2, bias=-0.5, levels=16):
+    """The mip level an image-mesh triangle samples (passes.c mesh_mip_level)."""
+    return lib().oracle_mesh_mip_level(float(rho2), float(bias), int(levels))
 
 
 def last_stats():

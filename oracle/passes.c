@@ -132,6 +132,7 @@ static void build_inverse_feather_table(void);
 #define DRAW_TYPE_OUTER_CURVE_PATCHES 2u
 #define DRAW_TYPE_INTERIOR_TRIANGULATION 3u
 #define DRAW_TYPE_FEATHER_ATLAS_BLIT 4u
+#define DRAW_TYPE_IMAGE_MESH 6u
 
 /* Sub-pixel precision of the rasteriser (Vulkan minimum is 4 bits; desktop
  * parts use 8). */
@@ -1562,6 +1563,13 @@ typedef struct
     int negate;   /* an atlas fill triangle that faced away: coverage negated */
     const oracle_texture* image; /* the batch's image (NULL: none) */
     uint32_t sampler;            /* its ImageSampler key */
+    /* An image-mesh triangle: its texture-coordinate planes (u0, du/dx,
+     * du/dy, v0, dv/dx, dv/dy, anchor x, anchor y), ImageDrawInstance and
+     * mip level. */
+    int mesh;
+    float planes[8];
+    uint32_t imageDraw;
+    int level;
 } tri_rec;
 
 static inline int64_t snap(float v)
@@ -2071,18 +2079,11 @@ static int wrap_texel(int i, int n, uint32_t wrap)
 /* The image at normalised (u, v) with an explicit level of detail: nearest
  * mip selection (VK_SAMPLER_MIPMAP_MODE_NEAREST: level ceil(lod + 1/2) - 1
  * above 1/2, else 0), the sampler's filter within the level. */
-static void sample_image(const oracle_texture* t, uint32_t sampler, float u, float v, float lod,
-                         float out[4])
+static void sample_image_level(const oracle_texture* t, uint32_t sampler, int level, float u,
+                               float v, float out[4])
 {
     const uint32_t wrapX = sampler % 3u, wrapY = (sampler / 3u) % 3u;
     const int nearest = sampler >= 9u;
-    int level = 0;
-    if (lod > .5f)
-    {
-        level = (int)ceilf(lod + .5f) - 1;
-        if (level > (int)t->levels - 1)
-            level = (int)t->levels - 1;
-    }
     int w = (int)(t->width >> level), h = (int)(t->height >> level);
     w = w ? w : 1;
     h = h ? h : 1;
@@ -2109,6 +2110,160 @@ static void sample_image(const oracle_texture* t, uint32_t sampler, float u, flo
             for (int k = 0; k < 4; ++k)
                 out[k] += wgt * ((float)tex[((size_t)yj * w + xi) * 4 + k] / 255.f);
         }
+}
+
+static void sample_image(const oracle_texture* t, uint32_t sampler, float u, float v, float lod,
+                         float out[4])
+{
+    int level = 0;
+    if (lod > .5f)
+    {
+        level = (int)ceilf(lod + .5f) - 1;
+        if (level > (int)t->levels - 1)
+            level = (int)t->levels - 1;
+    }
+    sample_image_level(t, sampler, level, u, v, out);
+}
+
+/* ---- Image meshes (draw_image_mesh.vert, draw_mesh.frag) ----------------- */
+
+static float clip_rect_distance(const float* aux, float fragX, float fragY);
+
+/* The mip level of an image-mesh triangle: the implicit level of detail plus
+ * FlushUniforms::mipMapLODBias under the Vulkan rules (lambda = log2(rho) +
+ * bias, rho the larger texel-space length of d(uv)/dx and d(uv)/dy, clamped
+ * to [0, levels - 1]; nearest mip ceil(lambda + 1/2) - 1). Level k is reached
+ * when rho^2 > 2^(2k - 1 - 2 bias), a power-of-two comparison (bias taken to
+ * the nearest half-integer; the reference's is -1/2). */
+static int mesh_mip_level(float rho2, float bias, uint32_t levels)
+{
+    const int twoBias = (int)rintf(2.f * bias);
+    int level = 0;
+    for (uint32_t k = 1; k < levels; ++k)
+    {
+        if (!(rho2 > ldexpf(1.f, 2 * (int)k - 1 - twoBias)))
+            break;
+        level = (int)k;
+    }
+    return level;
+}
+
+int oracle_mesh_mip_level(float rho2, float bias, uint32_t levels)
+{
+    return mesh_mip_level(rho2, bias, levels);
+}
+
+/* The texture-coordinate planes of a set-up mesh triangle (vertex order after
+ * the two-sided turn), anchored at its first snapped vertex, and its mip
+ * level for `tex`: texture coordinates are affine over the triangle, so the
+ * derivatives the implicit level of detail uses are the planes' slopes. */
+static void mesh_planes(tri_rec* t, const oracle_texture* tex, float bias)
+{
+    const float s = 1.f / 256.f;
+    const float p0x = (float)t->x[0] * s, p0y = (float)t->y[0] * s;
+    const float p1x = (float)t->x[1] * s, p1y = (float)t->y[1] * s;
+    const float p2x = (float)t->x[2] * s, p2y = (float)t->y[2] * s;
+    const int64_t area2 = (t->x[1] - t->x[0]) * (t->y[2] - t->y[0]) -
+                          (t->x[2] - t->x[0]) * (t->y[1] - t->y[0]);
+    const float d1x = p1x - p0x, d1y = p1y - p0y;
+    const float d2x = p2x - p0x, d2y = p2y - p0y;
+    const float inv = 1.f / ((float)area2 * (s * s));
+    const float uA = t->cov[0][0], uB = t->cov[1][0], uC = t->cov[2][0];
+    const float vA = t->cov[0][1], vB = t->cov[1][1], vC = t->cov[2][1];
+    const float ugx = ((uB - uA) * d2y - (uC - uA) * d1y) * inv;
+    const float ugy = ((uC - uA) * d1x - (uB - uA) * d2x) * inv;
+    const float vgx = ((vB - vA) * d2y - (vC - vA) * d1y) * inv;
+    const float vgy = ((vC - vA) * d1x - (vB - vA) * d2x) * inv;
+    const float pl[8] = {uA, ugx, ugy, vA, vgx, vgy, p0x, p0y};
+    memcpy(t->planes, pl, sizeof(pl));
+    const float W = (float)tex->width, H = (float)tex->height;
+    const float ux = ugx * W, vx = vgx * H, uy = ugy * W, vy = vgy * H;
+    const float rho2 = maxf(ux * ux + vx * vx, uy * uy + vy * vy);
+    t->level = mesh_mip_level(rho2, bias, tex->levels);
+}
+
+/* One fragment of an image-mesh triangle (draw_mesh.frag:60-225 with
+ * DRAW_IMAGE_MESH): the image at the pixel's texture coordinates and the
+ * triangle's mip level, coverage 1 cut by the clip rect and the clip, times
+ * the opacity; advanced blending unmultiplies the texel; dither, then
+ * src-over, straight into the colour plane. */
+static void mesh_fragment(const frag_ctx* fc, const tri_rec* t, int px, int py, pls_pixel* pls)
+{
+    const uint32_t features = t->features;
+    const float fragX = (float)px + .5f, fragY = (float)py + .5f;
+    const float* pl = t->planes;
+    const float dx = fragX - pl[6], dy = fragY - pl[7];
+    const float u = (pl[0] + pl[1] * dx) + pl[2] * dy;
+    const float v = (pl[3] + pl[4] * dx) + pl[5] * dy;
+    float color[4];
+    sample_image_level(t->image, t->sampler, t->level, u, v, color);
+    /* ImageDrawInstance (gpu.hpp:1742-1774): view matrix, clip-rect inverse
+     * matrix, translates, then opacity, clip ID, blend mode, z index. */
+    const float* inst = (const float*)fc->b->image_draws + 16 * (size_t)t->imageDraw;
+    uint32_t clipIDBits, blendMode;
+    memcpy(&clipIDBits, inst + 13, 4);
+    memcpy(&blendMode, inst + 14, 4);
+    float coverage = 1.f;
+    if (features & SF_CLIP_RECT)
+    {
+        /* clip_rect_distance reads PaintAuxData words 8-13. */
+        float aux[14] = {0};
+        memcpy(aux + 8, inst + 4, 4 * sizeof(float));
+        aux[12] = inst[10];
+        aux[13] = inst[11];
+        coverage = minf(maxf(clip_rect_distance(aux, fragX, fragY), 0.f), coverage);
+    }
+    if (features & SF_CLIPPING)
+    {
+        uint16_t clipID = id_bits_to_f16(clipIDBits, fc->granularity);
+        if (clipID != 0)
+        {
+            uint16_t clipContentID = (uint16_t)(pls->clip >> 16);
+            float clipCoverage = clipContentID == clipID ? h2f((uint16_t)(pls->clip & 0xffffu))
+                                                         : 0.f;
+            coverage = minf(coverage, maxf(clipCoverage, 0.f));
+        }
+    }
+    coverage *= inst[12]; /* opacity, after clipping */
+    float dst[4];
+    for (int k = 0; k < 4; ++k)
+        dst[k] = (float)pls->color[k] / 255.f;
+    if (features & SF_ADVANCED_BLEND)
+    {
+        /* unmultiply_rgb (common.glsl:210-216). */
+        const float r = color[3] != 0.f ? 1.f / color[3] : 0.f;
+        color[0] *= r;
+        color[1] *= r;
+        color[2] *= r;
+        if (blendMode != BLEND_SRC_OVER &&
+            ((int)blendMode < BLEND_MODE_HUE || (features & SF_HSL_BLEND_MODES)))
+        {
+            float rgb[3];
+            oracle_advanced_blend(color, dst, (int)blendMode, rgb);
+            color[0] = rgb[0];
+            color[1] = rgb[1];
+            color[2] = rgb[2];
+        }
+        color[3] *= coverage;
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    else
+    {
+        for (int k = 0; k < 4; ++k)
+            color[k] *= coverage;
+    }
+    if ((features & SF_DITHER) && color[3] != 0.f)
+    {
+        float n = ign(fragX, fragY, fc->ditherScale, fc->ditherBias);
+        color[0] += n;
+        color[1] += n;
+        color[2] += n;
+    }
+    const float a = color[3];
+    for (int k = 0; k < 4; ++k)
+        pls->color[k] = unorm8(dst[k] * (1.f - a) + color[k]);
 }
 
 /* ENABLE_MODULATED_IMAGE (draw_path.vert:343-361, 478-493): the paint's
@@ -2607,6 +2762,7 @@ static int setup_triangle_rect(const vtx_out* a,
     t->blit = 0;
     t->image = NULL;
     t->sampler = 0;
+    t->mesh = 0;
     return 1;
 }
 
@@ -2675,7 +2831,9 @@ static void raster_triangle_rows(const frag_ctx* fc,
                 covz = l0 * t->cov[0][2] + l1 * t->cov[1][2] + l2 * t->cov[2][2];
                 covw = l0 * t->cov[0][3] + l1 * t->cov[1][3] + l2 * t->cov[2][3];
             }
-            if (t->blit)
+            if (t->mesh)
+                mesh_fragment(fc, t, px, py, pls + (size_t)py * W + px);
+            else if (t->blit)
                 blit_fragment(fc, t, covx, covy, px, py, pls + (size_t)py * W + px);
             else
                 fragment(fc, t, covx, covy, covz, covw, px, py, pls + (size_t)py * W + px);
@@ -2875,8 +3033,9 @@ int oracle_draw(const rive_cuda_flush_desc* d,
     /* FlushUniforms (gpu.hpp:1466-1537): pathIDGranularity at byte 72,
      * ditherScale at 88, ditherBias at 92. */
     uint32_t granularity;
-    float ditherScale, ditherBias;
+    float ditherScale, ditherBias, mipLodBias;
     memcpy(&granularity, uni + 72, 4);
+    memcpy(&mipLodBias, uni + 80, 4);
     memcpy(&ditherScale, uni + 88, 4);
     memcpy(&ditherBias, uni + 92, 4);
 
@@ -3034,6 +3193,66 @@ int oracle_draw(const rive_cuda_flush_desc* d,
                         rc = r;
                     else if (r > 0)
                         tris[n++].blit = 1;
+                }
+            }
+        }
+        else if (batch->draw_type == DRAW_TYPE_IMAGE_MESH)
+        {
+            /* draw_image_mesh.vert: per index triple, the view matrix times
+             * the local position plus the translate (ImageDrawInstance
+             * batch->base_element), carrying the texture coordinates; no
+             * face culled (get_cull_face, gpu.cpp:1552-1593). */
+            const rive_cuda_batch_mesh* m = d->batch_meshes ? &d->batch_meshes[bi] : NULL;
+            const oracle_texture* tex =
+                d->batch_images ? (const oracle_texture*)d->batch_images[bi].texture : NULL;
+            if (!m || !m->vertices || !m->uvs || !m->indices || !tex || m->index_count % 3 ||
+                ((size_t)batch->base_element + 1) * 64 > b->image_draws_bytes)
+                rc = -1;
+            const oracle_render_buffer* vb = m ? (const oracle_render_buffer*)m->vertices : NULL;
+            const oracle_render_buffer* ub = m ? (const oracle_render_buffer*)m->uvs : NULL;
+            const oracle_render_buffer* ib = m ? (const oracle_render_buffer*)m->indices : NULL;
+            if (rc == 0 && (size_t)m->index_count * 2 > ib->bytes)
+                rc = -1;
+            const size_t nv = rc == 0 ? (vb->bytes < ub->bytes ? vb->bytes : ub->bytes) / 8 : 0;
+            const float* inst =
+                rc == 0 ? (const float*)b->image_draws + 16 * (size_t)batch->base_element : NULL;
+            for (uint32_t k3 = 0; rc == 0 && k3 < m->index_count; k3 += 3)
+            {
+                vtx_out vo[3];
+                for (int k = 0; k < 3 && rc == 0; ++k)
+                {
+                    const uint16_t vi = ((const uint16_t*)ib->data)[k3 + k];
+                    if (vi >= nv)
+                    {
+                        rc = -1;
+                        break;
+                    }
+                    const float* p = (const float*)vb->data + 2 * (size_t)vi;
+                    const float* uv = (const float*)ub->data + 2 * (size_t)vi;
+                    vo[k].pos = (f2){inst[0] * p[0] + inst[2] * p[1] + inst[8],
+                                     inst[1] * p[0] + inst[3] * p[1] + inst[9]};
+                    vo[k].cov[0] = uv[0];
+                    vo[k].cov[1] = uv[1];
+                    vo[k].cov[2] = vo[k].cov[3] = 0.f;
+                    vo[k].pathID = 0;
+                    vo[k].discard = 0;
+                }
+                if (rc == 0)
+                    rc = grow_tris(&tris, &cap, n);
+                if (rc == 0)
+                {
+                    int r = setup_triangle_rect(&vo[0], &vo[1], &vo[2], features, 0, 0, W, H, 1,
+                                                &tris[n]);
+                    if (r < 0)
+                        rc = r;
+                    else if (r > 0)
+                    {
+                        tris[n].mesh = 1;
+                        tris[n].imageDraw = batch->base_element;
+                        tris[n].negate = 0;
+                        mesh_planes(&tris[n], tex, mipLodBias);
+                        ++n;
+                    }
                 }
             }
         }

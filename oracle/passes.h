@@ -53,7 +53,18 @@ typedef struct oracle_buffers
     size_t tess_spans_bytes;
     const void* triangles; /* gpu::TriangleVertex, 12 B each (interior triangulation) */
     size_t triangles_bytes;
+    const void* image_draws; /* gpu::ImageDrawInstance, 64 B each (image meshes) */
+    size_t image_draws_bytes;
 } oracle_buffers;
+
+/* A RenderBuffer for the passes: in a flush descriptor given to the oracle,
+ * each rive_cuda_batch_mesh buffer pointer points at one of these (host
+ * bytes and their size). */
+typedef struct oracle_render_buffer
+{
+    const void* data;
+    size_t bytes;
+} oracle_render_buffer;
 
 /* Pass 1 into grad (512 x grad_data_height RGBA8). Returns 0 on success. */
 int oracle_color_ramps(const rive_cuda_flush_desc* d,
@@ -111,6 +122,11 @@ int oracle_atlas(const rive_cuda_flush_desc* d,
                  const oracle_buffers* b,
                  uint16_t* out,
                  int threads);
+
+/* The mip level an image-mesh triangle samples, from the squared texel-space
+ * length rho2 of its steeper texture-coordinate derivative, the LOD bias and
+ * the texture's level count. */
+int oracle_mesh_mip_level(float rho2, float bias, uint32_t levels);
 
 /* Counters of the last oracle_draw (triangles after culling, fragments). */
 void oracle_last_stats(uint64_t* triangles, uint64_t* fragments);

@@ -10,6 +10,12 @@ the atlas sizes, its gpu::AtlasDrawBatch lists (gpu.hpp:827-833, 1361-1426)
 and each draw batch's image (texture index and ImageSampler key), and the
 capture ends with the image textures the front end created
 (RenderContextImpl::makeImageTexture: size, mip levels, level-0 RGBA).
+A frame that draws image meshes is an "RCP3" capture: an RCP2 capture whose
+flushes also name each imageMesh batch's vertex, uv and index RenderBuffers
+and index count, whose buffers include the ImageDrawInstance records, and
+which ends with the RenderBuffer contents each flush drew
+(RenderContextImpl::makeRenderBuffer; a buffer rewritten between flushes
+appears once per distinct content).
 """
 from __future__ import annotations
 
@@ -20,9 +26,11 @@ import numpy as np
 
 CAPTURE_MAGIC = 0x31504352  # "RCP1"
 CAPTURE_MAGIC_V2 = 0x32504352  # "RCP2": with feather atlas batches
+CAPTURE_MAGIC_V3 = 0x33504352  # "RCP3": RCP2 with image meshes
 
 BUFFER_NAMES = ("flush_uniforms", "paths", "paints", "paint_aux", "contours",
-                "grad_spans", "tess_spans", "triangles")
+                "grad_spans", "tess_spans", "triangles", "image_draws")
+NO_BUFFER = 0xFFFFFFFF
 
 # rive_cuda_flush_desc field order (include/rive_cuda.h); 36 u32-sized fields,
 # then the draw_batches pointer (8 bytes, LP64).
@@ -59,6 +67,12 @@ class Texture:
 
 
 @dataclass
+class RenderBuffer:
+    type: int  # rive::RenderBufferType: 0 index, 1 vertex
+    data: bytes
+
+
+@dataclass
 class Flush:
     desc: dict
     batches: np.ndarray  # (n, 8) uint32
@@ -68,6 +82,11 @@ class Flush:
     images: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.uint32))
     # The capture's textures (the indices above refer to them).
     textures: list = field(default_factory=list)
+    # Per draw batch: (vertex buffer, uv buffer, index buffer, index count),
+    # buffers as indices into render_buffers (NO_BUFFER: not a mesh); empty
+    # when no batch draws an image mesh.
+    meshes: np.ndarray = field(default_factory=lambda: np.zeros((0, 4), np.uint32))
+    render_buffers: list = field(default_factory=list)
 
     @property
     def has_atlas(self) -> bool:
@@ -77,6 +96,10 @@ class Flush:
     def has_images(self) -> bool:
         return bool(len(self.images)) and bool((self.images[:, 0] != 0xFFFFFFFF).any())
 
+    @property
+    def has_meshes(self) -> bool:
+        return bool(len(self.meshes)) and bool((self.meshes[:, 0] != NO_BUFFER).any())
+
 
 @dataclass
 class Capture:
@@ -85,6 +108,7 @@ class Capture:
     buffers: dict = field(default_factory=dict)  # name -> bytes
     flushes: list = field(default_factory=list)
     textures: list = field(default_factory=list)  # Texture
+    render_buffers: list = field(default_factory=list)  # RenderBuffer
 
     def buffer_array(self, name, dtype=np.uint32):
         return np.frombuffer(self.buffers[name], dtype=dtype)
@@ -96,9 +120,10 @@ class Capture:
 
 def parse(data: bytes) -> Capture:
     magic, w, h, nk = struct.unpack_from("<4I", data, 0)
-    if magic not in (CAPTURE_MAGIC, CAPTURE_MAGIC_V2):
+    if magic not in (CAPTURE_MAGIC, CAPTURE_MAGIC_V2, CAPTURE_MAGIC_V3):
         raise ValueError("not a flush capture")
-    v2 = magic == CAPTURE_MAGIC_V2
+    v3 = magic == CAPTURE_MAGIC_V3
+    v2 = v3 or magic == CAPTURE_MAGIC_V2
     off = 16
     cap = Capture(w, h)
     for k in range(nk):
@@ -131,7 +156,13 @@ def parse(data: bytes) -> Capture:
             off += ni * 8
         else:
             images = np.zeros((0, 2), np.uint32)
-        cap.flushes.append(Flush(desc, batches, atlas, images))
+        meshes = np.zeros((0, 4), np.uint32)
+        if v3:
+            (nm,) = struct.unpack_from("<I", data, off)
+            off += 4
+            meshes = np.frombuffer(data, dtype="<u4", count=nm * 4, offset=off).reshape(nm, 4).copy()
+            off += nm * 16
+        cap.flushes.append(Flush(desc, batches, atlas, images, meshes=meshes))
     if v2:
         (nt,) = struct.unpack_from("<I", data, off)
         off += 4
@@ -140,17 +171,29 @@ def parse(data: bytes) -> Capture:
             off += 12
             cap.textures.append(Texture(w, h, levels, bytes(data[off:off + w * h * 4])))
             off += w * h * 4
+    if v3:
+        (nb,) = struct.unpack_from("<I", data, off)
+        off += 4
+        for _ in range(nb):
+            kind, n = struct.unpack_from("<2I", data, off)
+            off += 8
+            cap.render_buffers.append(RenderBuffer(kind, bytes(data[off:off + n])))
+            off += n + ((4 - (n & 3)) & 3)
     for f in cap.flushes:
         f.textures = cap.textures
+        f.render_buffers = cap.render_buffers
     return cap
 
 
 def serialize(cap: Capture) -> bytes:
-    # Seven kinds, or eight when the frame has interior triangles.
-    kinds = BUFFER_NAMES if cap.buffers.get("triangles") else BUFFER_NAMES[:7]
-    v2 = any(f.has_atlas or f.has_images for f in cap.flushes) or bool(cap.textures)
-    out = bytearray(struct.pack("<4I", CAPTURE_MAGIC_V2 if v2 else CAPTURE_MAGIC, cap.width,
-                                cap.height, len(kinds)))
+    # Seven kinds, eight when the frame has interior triangles, nine when it
+    # has image draw instances.
+    kinds = BUFFER_NAMES if cap.buffers.get("image_draws") else \
+        BUFFER_NAMES[:8] if cap.buffers.get("triangles") else BUFFER_NAMES[:7]
+    v3 = any(f.has_meshes for f in cap.flushes) or bool(cap.render_buffers)
+    v2 = v3 or any(f.has_atlas or f.has_images for f in cap.flushes) or bool(cap.textures)
+    magic = CAPTURE_MAGIC_V3 if v3 else CAPTURE_MAGIC_V2 if v2 else CAPTURE_MAGIC
+    out = bytearray(struct.pack("<4I", magic, cap.width, cap.height, len(kinds)))
     for name in kinds:
         b = cap.buffers.get(name, b"")
         out += struct.pack("<Q", len(b)) + b + bytes((8 - (len(b) & 7)) & 7)
@@ -167,8 +210,17 @@ def serialize(cap: Capture) -> bytes:
             im = np.asarray(f.images, dtype="<u4").reshape(-1, 2) if f.has_images else \
                 np.zeros((0, 2), "<u4")
             out += struct.pack("<I", len(im)) + im.tobytes()
+        if v3:
+            me = np.asarray(f.meshes, dtype="<u4").reshape(-1, 4) if f.has_meshes else \
+                np.zeros((0, 4), "<u4")
+            out += struct.pack("<I", len(me)) + me.tobytes()
     if v2:
         out += struct.pack("<I", len(cap.textures))
         for t in cap.textures:
             out += struct.pack("<3I", t.width, t.height, t.mip_levels) + bytes(t.rgba)
+    if v3:
+        out += struct.pack("<I", len(cap.render_buffers))
+        for b in cap.render_buffers:
+            n = len(b.data)
+            out += struct.pack("<2I", b.type, n) + bytes(b.data) + bytes((4 - (n & 3)) & 3)
     return bytes(out)

@@ -223,6 +223,14 @@ struct rive_cuda_texture
     uint32_t texels = 0;
 };
 
+// A RenderBuffer of image-mesh data (rive_cuda_render_buffer_create).
+struct rive_cuda_render_buffer
+{
+    void* mem = nullptr;
+    size_t bytes = 0;
+    uint32_t type = 0;
+};
+
 struct rive_cuda_render_target
 {
     uint32_t width = 0, height = 0;
@@ -372,8 +380,8 @@ void stage_end(rive_cuda_context* ctx, cudaStream_t s)
 }
 
 // The record buffers a flush reads, in buffer-kind order (flush uniforms ..
-// triangle vertices).
-constexpr int kResolvedKinds = 8;
+// triangle vertices, image draw instances).
+constexpr int kResolvedKinds = 9;
 struct ResolvedBuffers
 {
     const void* ptr[kResolvedKinds];
@@ -385,7 +393,7 @@ ResolvedBuffers resolve_device_buffers(const rive_cuda_device_buffers& b)
 {
     const void* p[kResolvedKinds] = {b.flush_uniforms, b.paths,      b.paints,
                                      b.paint_aux,      b.contours,   b.grad_spans,
-                                     b.tess_spans,     b.triangle_vertices};
+                                     b.tess_spans,     b.triangle_vertices, b.image_draws};
     ResolvedBuffers rb;
     for (int k = 0; k < kResolvedKinds; ++k)
     {
@@ -411,14 +419,27 @@ int setup_list(uint32_t drawType)
            : drawType == DRAW_INTERIOR_TRIANGULATION ? 2
            : drawType == DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES ? 3
            : drawType == DRAW_FEATHER_ATLAS_BLIT ? 2 // a rectangle of triangle vertices
+           : drawType == DRAW_IMAGE_MESH ? 2 // the mesh's triangles
                                                              : -1;
 }
 constexpr uint32_t kTrianglesPerItem[kSetupLists] = {
     kPatchTriangleCount, kOuterPatchTriangleCount, 1, kCenterPatchTriangleCount};
 
-// Items (patch instances or triangles) of a draw batch.
-uint32_t batch_items(const rive_cuda_draw_batch& b)
+// The mesh of draw batch i of a flush, or null.
+const rive_cuda_batch_mesh* batch_mesh(const rive_cuda_flush_desc* d, uint32_t i)
 {
+    return d->batch_meshes && d->batch_meshes[i].vertices ? &d->batch_meshes[i] : nullptr;
+}
+
+// Items (patch instances or triangles) of draw batch i of a flush.
+uint32_t batch_items(const rive_cuda_flush_desc* d, uint32_t i)
+{
+    const rive_cuda_draw_batch& b = d->draw_batches[i];
+    if (b.draw_type == DRAW_IMAGE_MESH)
+    {
+        const rive_cuda_batch_mesh* m = batch_mesh(d, i);
+        return m ? m->index_count / 3 : 0u;
+    }
     return b.draw_type == DRAW_INTERIOR_TRIANGULATION || b.draw_type == DRAW_FEATHER_ATLAS_BLIT
                ? b.element_count / 3
                : b.element_count;
@@ -491,7 +512,30 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
             return set_error(ctx, RIVE_CUDA_ERR_UNSUPPORTED,
                              "shader misc flags 0x%x not supported (rasterOrdering: clockwiseFill only)",
                              b.shader_misc_flags);
-        if (list == 2)
+        if (b.draw_type == DRAW_IMAGE_MESH)
+        {
+            // An image mesh: its buffers, its ImageDrawInstance and its
+            // texture (RiveRenderer::drawImageMesh draws nothing without one).
+            const rive_cuda_batch_mesh* m = batch_mesh(d, i);
+            if (!m || !m->uvs || !m->indices)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "image mesh batch %u has no vertex, uv or index buffer", i);
+            if (m->index_count % 3 || (uint64_t)m->index_count * 2 > m->indices->bytes)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "image mesh batch %u: %u indices in a %zu-byte index buffer", i,
+                                 m->index_count, m->indices->bytes);
+            if (!d->batch_images || !d->batch_images[i].texture)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "image mesh batch %u has no texture", i);
+            if (b.element_count != 1 || !rb.ptr[RIVE_CUDA_BUFFER_IMAGE_DRAW] ||
+                ((uint64_t)b.base_element + 1) * 64 > rb.bytes[RIVE_CUDA_BUFFER_IMAGE_DRAW])
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "image mesh batch %u reads past the image draw instances", i);
+            if (d->path_count == 0)
+                return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
+                                 "a flush with image meshes has path 0 (the clear path)");
+        }
+        else if (list == 2)
         {
             if (b.element_count % 3 || !rb.ptr[RIVE_CUDA_BUFFER_TRIANGLE] ||
                 ((uint64_t)b.base_element + b.element_count) * 12 >
@@ -507,7 +551,7 @@ int validate_flush(rive_cuda_context* ctx, const rive_cuda_flush_desc* d, const 
                 return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT,
                                  "batch %u reads past the tessellation texture", i);
         }
-        slots += (uint64_t)batch_items(b) * kTrianglesPerItem[list];
+        slots += (uint64_t)batch_items(d, i) * kTrianglesPerItem[list];
     }
     // Images: a known sampler for every batch that samples a texture.
     if (d->batch_images)
@@ -562,6 +606,12 @@ struct BatchLayout
     // table), and the per-path image slots of every main scene.
     uint32_t imageSlots = 0;
     size_t oImages = 0;
+    // Image meshes: the batch's mesh table.
+    uint32_t meshes = 0;
+    size_t oMeshes = 0;
+    // Per-slot planes: feathered fills' third and fourth coverage
+    // components, image meshes' texture coordinates.
+    bool planes() const { return items[3] != 0 || meshes != 0; }
     // The extended kernel variants: some batch feathers, blits the feather
     // atlas or samples an image.
     bool feather = false;
@@ -615,7 +665,7 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
         {
             const rive_cuda_draw_batch& db = d->draw_batches[b];
-            const uint32_t k = batch_items(db);
+            const uint32_t k = batch_items(d, b);
             if (!k)
                 continue;
             const int list = setup_list(db.draw_type);
@@ -623,6 +673,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
             items[list] += k;
             if ((db.shader_features & SF_FEATHER) || db.draw_type == DRAW_FEATHER_ATLAS_BLIT)
                 L.feather = true;
+            if (db.draw_type == DRAW_IMAGE_MESH)
+                ++L.meshes;
             if (d->batch_images && d->batch_images[b].texture)
             {
                 ++L.imageSlots;
@@ -704,7 +756,8 @@ int plan_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, BatchLa
     L.oSceneTiles = align16(L.oTileBase + 4 * (ns + 1));
     L.oPathBase = align16(L.oSceneTiles + 8 * ns);
     L.oImages = align16(L.oPathBase + 4 * (ns + 1));
-    size_t o = align16(L.oImages + sizeof(ImageTex) * std::max(L.imageSlots, 1u));
+    L.oMeshes = align16(L.oImages + sizeof(ImageTex) * std::max(L.imageSlots, 1u));
+    size_t o = align16(L.oMeshes + sizeof(MeshDesc) * std::max(L.meshes, 1u));
     for (int l = 0; l < kSetupLists; ++l)
     {
         L.oSegments[l] = o;
@@ -764,7 +817,8 @@ BatchTables write_tables(rive_cuda_context* ctx,
     auto* sceneTiles = (uint2*)(h + L.oSceneTiles);
     auto* pathBase = (uint32_t*)(h + L.oPathBase);
     auto* images = (ImageTex*)(h + L.oImages);
-    uint32_t imageAcc = 0;
+    auto* meshes = (MeshDesc*)(h + L.oMeshes);
+    uint32_t imageAcc = 0, meshAcc = 0;
     PatchSegment* segs[kSetupLists];
     uint32_t* segBase[kSetupLists];
     for (int l = 0; l < kSetupLists; ++l)
@@ -829,6 +883,9 @@ BatchTables write_tables(rive_cuda_context* ctx,
             P.images = (const ImageTex*)(S.tables + L.oImages);
             P.pathImage = S.pathImage + pathAcc;
         }
+        P.imageDraws = (const float4*)rb.ptr[RIVE_CUDA_BUFFER_IMAGE_DRAW];
+        P.imageDrawCount = (uint32_t)std::min<size_t>(rb.bytes[RIVE_CUDA_BUFFER_IMAGE_DRAW] / 64,
+                                                      0xffffffffu);
 
         gradBase[i] = gAcc;
         tessBase[i] = tAcc;
@@ -843,7 +900,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
         for (uint32_t b = 0; b < d->draw_batch_count; ++b)
         {
             const rive_cuda_draw_batch& db = d->draw_batches[b];
-            const uint32_t k = batch_items(db);
+            const uint32_t k = batch_items(d, b);
             if (!k)
                 continue;
             const int l = setup_list(db.draw_type);
@@ -854,12 +911,29 @@ BatchTables write_tables(rive_cuda_context* ctx,
                 images[image] = d->batch_images[b].texture->desc;
                 images[image].sampler = d->batch_images[b].sampler_key;
             }
+            uint32_t mesh = kNoMesh;
+            if (db.draw_type == DRAW_IMAGE_MESH)
+            {
+                const rive_cuda_batch_mesh& m = *batch_mesh(d, b);
+                mesh = meshAcc++;
+                MeshDesc& M = meshes[mesh];
+                M.positions = (const float2*)m.vertices->mem;
+                M.uvs = (const float2*)m.uvs->mem;
+                M.indices = (const uint16_t*)m.indices->mem;
+                M.vertexCount = (uint32_t)std::min<size_t>(
+                    std::min(m.vertices->bytes, m.uvs->bytes) / 8, 0xffffffffu);
+                M.indexCount = m.index_count;
+                M.imageDraw = db.base_element;
+                M.image = image;
+                M.pad = 0;
+            }
             segs[l][segAcc[l]] = PatchSegment{
                 i, db.base_element,
                 db.shader_features |
                     ((db.shader_misc_flags & MISC_CLOCKWISE_FILL) ? FEATURE_CLOCKWISE_FILL : 0u) |
-                    (db.draw_type == DRAW_FEATHER_ATLAS_BLIT ? FEATURE_ATLAS_BLIT : 0u),
-                slotAcc, 0u, 0xffffffffu, image};
+                    (db.draw_type == DRAW_FEATHER_ATLAS_BLIT ? FEATURE_ATLAS_BLIT : 0u) |
+                    (db.draw_type == DRAW_IMAGE_MESH ? FEATURE_IMAGE_MESH : 0u),
+                slotAcc, 0u, 0xffffffffu, image, mesh};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += k;
@@ -904,7 +978,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
             segs[l][segAcc[l]] = PatchSegment{
                 j, ab.base_patch, SF_FEATHER, slotAcc,
                 (uint32_t)ab.scissor[0] | ((uint32_t)ab.scissor[1] << 16),
-                (uint32_t)ab.scissor[2] | ((uint32_t)ab.scissor[3] << 16), kNoImage};
+                (uint32_t)ab.scissor[2] | ((uint32_t)ab.scissor[3] << 16), kNoImage, kNoMesh};
             segBase[l][segAcc[l]] = itemAcc[l];
             ++segAcc[l];
             itemAcc[l] += ab.patch_count;
@@ -937,6 +1011,7 @@ BatchTables write_tables(rive_cuda_context* ctx,
     B.mainTiles = L.mainTiles;
     B.tileLog2 = L.tileLog2;
     B.featherPlanes = S.featherPlanes;
+    B.meshes = L.meshes ? (const MeshDesc*)(dT + L.oMeshes) : nullptr;
     B.fanSlotStride = L.fanStride;
     B.pathBase = (const uint32_t*)(dT + L.oPathBase);
     if (L.winding)
@@ -1257,7 +1332,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     CK(ctx->tileCounts.reserve((size_t)std::max(L.slots, 1u) * 4));
     CK(ctx->tileMasks.reserve((size_t)std::max(L.slots, 1u)));
     CK(ctx->offsets.reserve((size_t)L.slots * 4 + 4));
-    if (L.items[3])
+    if (L.planes())
         CK(ctx->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     if (L.atlasTexels)
         CK(ctx->atlas.reserve((size_t)L.atlasTexels * 2));
@@ -1299,7 +1374,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     S.tess = (uint4*)ctx->tess.ptr;
     S.grad = (uchar4*)ctx->grad.ptr;
     S.tris = (TriRecord*)ctx->tris.ptr;
-    S.featherPlanes = L.items[3] ? (float4*)ctx->featherPlanes.ptr : nullptr;
+    S.featherPlanes = L.planes() ? (float4*)ctx->featherPlanes.ptr : nullptr;
     S.atlas = L.atlasTexels ? (uint16_t*)ctx->atlas.ptr : nullptr;
     S.pathImage = L.imageSlots ? (uint32_t*)ctx->pathImage.ptr : nullptr;
     S.counts = (uint32_t*)ctx->tileCounts.ptr;
@@ -1752,7 +1827,7 @@ int graph_build(rive_cuda_context* ctx,
     CK(g->counts.reserve((size_t)std::max(L.slots, 1u) * 4));
     CK(g->masks.reserve((size_t)std::max(L.slots, 1u)));
     CK(g->offsets.reserve((size_t)L.slots * 4 + 4));
-    if (L.items[3])
+    if (L.planes())
         CK(g->featherPlanes.reserve((size_t)L.slots * 2 * sizeof(float4)));
     if (L.atlasTexels)
         CK(g->atlas.reserve((size_t)L.atlasTexels * 2));
@@ -1779,7 +1854,7 @@ int graph_build(rive_cuda_context* ctx,
     S.tess = (uint4*)g->tess.ptr;
     S.grad = (uchar4*)g->grad.ptr;
     S.tris = (TriRecord*)g->tris.ptr;
-    S.featherPlanes = L.items[3] ? (float4*)g->featherPlanes.ptr : nullptr;
+    S.featherPlanes = L.planes() ? (float4*)g->featherPlanes.ptr : nullptr;
     S.atlas = L.atlasTexels ? (uint16_t*)g->atlas.ptr : nullptr;
     S.pathImage = L.imageSlots ? (uint32_t*)g->pathImage.ptr : nullptr;
     S.counts = (uint32_t*)g->counts.ptr;
@@ -2024,7 +2099,7 @@ int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)
         CK(cudaStreamSynchronize(s));
         return set_error(ctx, RIVE_CUDA_ERR_DEVICE_STATUS,
                          "device status 0x%x (1 tess index, 2 contour, 4 path, "
-                         "16 coordinate range, 32 bin overflow)",
+                         "16 coordinate range, 32 bin overflow, 64 mesh index)",
                          err);
     }
     return RIVE_CUDA_OK;
@@ -2114,6 +2189,68 @@ void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* textur
     }
     cudaFree(texture->mem);
     delete texture;
+}
+
+int rive_cuda_render_buffer_create(rive_cuda_context* ctx,
+                                   uint32_t type,
+                                   size_t bytes,
+                                   rive_cuda_render_buffer** out_buffer)
+{
+    if (!ctx || !out_buffer || type > RIVE_CUDA_RENDER_BUFFER_VERTEX || bytes == 0)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *out_buffer = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    rive_cuda_render_buffer* b = new (std::nothrow) rive_cuda_render_buffer();
+    if (!b)
+        return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+    // Rounded up to 16 bytes so float2 and uint16 reads of the last element
+    // stay inside the allocation.
+    cudaError_t e = cudaMalloc(&b->mem, (bytes + 15) & ~(size_t)15);
+    if (e == cudaSuccess)
+        e = cudaMemset(b->mem, 0, (bytes + 15) & ~(size_t)15);
+    if (e != cudaSuccess)
+    {
+        cudaFree(b->mem);
+        delete b;
+        return cuda_fail(ctx, e, "cudaMalloc(render buffer)");
+    }
+    b->bytes = bytes;
+    b->type = type;
+    *out_buffer = b;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_render_buffer_write(rive_cuda_context* ctx,
+                                  rive_cuda_render_buffer* buffer,
+                                  size_t offset,
+                                  const void* src_host,
+                                  size_t bytes)
+{
+    if (!ctx || !buffer || (!src_host && bytes) || offset > buffer->bytes ||
+        bytes > buffer->bytes - offset)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    if (!bytes)
+        return RIVE_CUDA_OK;
+    CK(cudaSetDevice(ctx->device));
+    // After the flushes already queued (they may still read the old bytes).
+    CK(cudaMemcpyAsync((uint8_t*)buffer->mem + offset, src_host, bytes, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return RIVE_CUDA_OK;
+}
+
+void rive_cuda_render_buffer_destroy(rive_cuda_context* ctx, rive_cuda_render_buffer* buffer)
+{
+    if (!buffer)
+        return;
+    if (ctx)
+    {
+        // Flushes still in flight may read it.
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(buffer->mem);
+    delete buffer;
 }
 
 int rive_cuda_texture_read(rive_cuda_context* ctx,

@@ -171,6 +171,11 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
             if (d->batch_images[i].texture)
                 return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                             "images need the allocating path (rive_cuda_flush_device)");
+    if (d->batch_meshes)
+        for (uint32_t i = 0; i < d->draw_batch_count; ++i)
+            if (d->batch_meshes[i].vertices)
+                return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
+                            "image meshes need the allocating path (rive_cuda_flush_device)");
     if (d->has_triangle_vertices)
         return fail(err, err_len, RIVE_CUDA_ERR_UNSUPPORTED,
                     "interior triangulation draws are not supported");
@@ -307,7 +312,8 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
                                       b.shader_features | ((b.shader_misc_flags & MISC_CLOCKWISE_FILL)
                                                                ? FEATURE_CLOCKWISE_FILL
                                                                : 0u),
-                                      instAcc * kPatchTriangleCount, 0u, 0xffffffffu, kNoImage};
+                                      instAcc * kPatchTriangleCount, 0u, 0xffffffffu, kNoImage,
+                                      kNoMesh};
         segBase[segCount] = instAcc;
         ++segCount;
         instAcc += b.element_count;
@@ -414,7 +420,7 @@ extern "C" int rive_cuda_flush_device_noalloc(const rive_cuda_flush_desc* d,
     if (status)
         return fail(err, err_len, RIVE_CUDA_ERR_DEVICE_STATUS,
                     "device status 0x%x (1 tess index, 2 contour, 4 path, "
-                    "16 coordinate range, 32 bin overflow)",
+                    "16 coordinate range, 32 bin overflow, 64 mesh index)",
                     status);
     return RIVE_CUDA_OK;
 }

@@ -1378,6 +1378,80 @@ __global__ void __launch_bounds__(128) center_setup_kernel(BatchTables B,
     patch_setup<3, true>(B, tris, tileCounts, tileMasks);
 }
 
+// The mip level of an image-mesh triangle. draw_mesh.frag samples with the
+// implicit level of detail plus FlushUniforms::mipMapLODBias
+// (TEXTURE_SAMPLE_DYNAMIC_LODBIAS); under the Vulkan rules the reference
+// backend follows, lambda = log2(rho) + bias with rho the larger of the
+// texel-space lengths of d(uv)/dx and d(uv)/dy, clamped to [0, levels - 1],
+// and the nearest mip level ceil(lambda + 1/2) - 1
+// (VK_SAMPLER_MIPMAP_MODE_NEAREST). Texture coordinates are affine over a
+// triangle, so rho is the triangle's constant. Level k is reached when
+// lambda > k - 1/2, i.e. rho^2 > 2^(2k - 1 - 2 bias): a comparison with a
+// power of two, exact for the reference's bias of -1/2 (other biases are
+// taken to the nearest half-integer).
+__device__ __forceinline__ uint32_t mesh_mip_level(float rho2, float bias, uint32_t levels)
+{
+    const int twoBias = (int)rintf(__fmul_rn(2.f, bias));
+    uint32_t level = 0;
+    for (uint32_t k = 1; k < levels; ++k)
+    {
+        if (!(rho2 > ldexpf(1.f, 2 * (int)k - 1 - twoBias)))
+            break;
+        level = k;
+    }
+    return level;
+}
+
+// One triangle of an image mesh (draw_image_mesh.vert): the vertices of its
+// three indices, each the view matrix times the local position plus the
+// translate (ImageDrawInstance), with its texture coordinates; no face is
+// culled (get_cull_face, gpu.cpp:1552-1593). The texture coordinates become
+// exact planes in the slot's feather-plane pair; the record carries the
+// ImageDrawInstance index and the image slot with the triangle's mip level
+// where paths keep their paint words, and the coverage key of path 0.
+__device__ bool mesh_triangle(const BatchTables& B, const FlushParams& P, const PatchSegment& S,
+                              uint32_t local, uint32_t slot, TriRecord& T, int4& bb)
+{
+    bb = make_int4(0, 0, 0, 0);
+    const MeshDesc& M = B.meshes[S.mesh];
+    const float4* inst = P.imageDraws + 4 * (size_t)M.imageDraw;
+    const float4 vm = inst[0], tr = inst[2];
+    VertexOut v[3];
+    float2 uv[3];
+    for (int k = 0; k < 3; ++k)
+    {
+        const uint32_t vi = M.indices[3 * local + k];
+        if (vi >= M.vertexCount)
+        {
+            atomicOr(P.error, ERR_BAD_MESH_INDEX);
+            return false;
+        }
+        const float2 p = M.positions[vi];
+        uv[k] = M.uvs[vi];
+        v[k].pos = make_float2(__fadd_rn(__fadd_rn(__fmul_rn(vm.x, p.x), __fmul_rn(vm.z, p.y)), tr.x),
+                               __fadd_rn(__fadd_rn(__fmul_rn(vm.y, p.x), __fmul_rn(vm.w, p.y)), tr.y));
+        v[k].cov = uv[k];
+        v[k].pathID = 0;
+        v[k].discard = false;
+    }
+    float4* planes = B.featherPlanes + 2 * (size_t)slot;
+    if (!setup_triangle(P, v[0], v[1], v[2], S.features, S.scene, T, bb, planes, uv[0], uv[1], uv[2],
+                        make_int4(0, 0, 0x7fffffff, 0x7fffffff), true))
+        return false;
+    const float4 f0 = planes[0], f1 = planes[1];
+    const ImageTex& tex = P.images[M.image];
+    const float W = (float)tex.width, H = (float)tex.height;
+    const float ux = __fmul_rn(f0.y, W), vx = __fmul_rn(f1.x, H);
+    const float uy = __fmul_rn(f0.z, W), vy = __fmul_rn(f1.y, H);
+    const float rho2 = fmaxf(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(vx, vx)),
+                             __fadd_rn(__fmul_rn(uy, uy), __fmul_rn(vy, vy)));
+    const uint32_t level = mesh_mip_level(rho2, P.mipLodBias, tex.levels);
+    T.cov1.z = __uint_as_float(M.imageDraw);
+    T.cov1.w = __uint_as_float(M.image | (level << 24));
+    T.meta.w = S.scene << 16;
+    return true;
+}
+
 // Interior triangulation (DrawType::interiorTriangulation): one thread per
 // triangle of the batch's TriangleVertex records. A vertex is the path-space
 // point mapped by the path's matrix, and its coverage is the triangle's
@@ -1410,7 +1484,22 @@ __global__ void __launch_bounds__(256) interior_setup_kernel(BatchTables B,
         slot = S.slotBase + local;
         VertexOut v[3];
         bool ok = true;
-        for (int k = 0; k < 3; ++k)
+        if (S.features & FEATURE_IMAGE_MESH)
+        {
+            TriRecord T;
+            if (mesh_triangle(B, P, S, local, slot, T, bb))
+            {
+                tris[slot] = T;
+                e[0] = T.e0;
+                e[1] = T.e1;
+                e[2] = T.e2;
+                sEdges[w][lane][0] = T.e0;
+                sEdges[w][lane][1] = T.e1;
+                sEdges[w][lane][2] = T.e2;
+            }
+            ok = false; // set up already
+        }
+        for (int k = 0; k < 3 && ok; ++k)
         {
             const uint32_t vi = S.baseElement + 3 * local + k;
             if (vi >= P.triangleVertexCount)
@@ -1767,6 +1856,7 @@ __global__ void scene_uniforms_kernel(FlushParams* __restrict__ scenes, uint32_t
     scenes[i].pathIDGranularity = granularity ? granularity : 1u;
     scenes[i].ditherScale = *reinterpret_cast<const float*>(u + 88);
     scenes[i].ditherBias = *reinterpret_cast<const float*>(u + 92);
+    scenes[i].mipLodBias = *reinterpret_cast<const float*>(u + 80);
 }
 
 // Fixed-capacity binning: entries [total, capacity) get the sentinel key (one
@@ -2174,12 +2264,10 @@ struct Pixel
 };
 
 // min_component of find_clip_rect_coverage_distances (common.glsl:376-400)
-// at the pixel centre.
-__device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32_t pathID, float fx,
-                                                    float fy)
+// at the pixel centre, for the clip-rect inverse matrix cm (2x2) and its
+// translate ct.xy.
+__device__ __forceinline__ float clip_rect_distance_m(float4 cm, float4 ct, float fx, float fy)
 {
-    const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
-    float4 cm = aux[2], ct = aux[3];
     float awx = fabsf(cm.x) + fabsf(cm.z), awy = fabsf(cm.y) + fabsf(cm.w);
     float d0, d1, d2, d3;
     if (awx != 0.f && awy != 0.f)
@@ -2198,6 +2286,14 @@ __device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32
         d1 = d3 = ct.y;
     }
     return fminf(fminf(d0, d1), fminf(d2, d3));
+}
+
+// A path's clip rect: the inverse matrix of its PaintAuxData (words 8-13).
+__device__ __forceinline__ float clip_rect_distance(const FlushParams& P, uint32_t pathID, float fx,
+                                                    float fy)
+{
+    const float4* aux = P.paintAux + 8 * (size_t)(P.firstPaintAux + pathID);
+    return clip_rect_distance_m(aux[2], aux[3], fx, fy);
 }
 
 // find_paint_color (draw_path.vert:431-496, evaluated at the pixel): the
@@ -2283,13 +2379,10 @@ __device__ __forceinline__ int wrap_texel(int i, int n, uint32_t wrap)
 // a nearest mip selection picks (VK_SAMPLER_MIPMAP_MODE_NEAREST,
 // pipeline_manager_vulkan.cpp:13-23: level ceil(lod + 1/2) - 1 above 1/2,
 // else 0), RGBA as floats.
-__device__ void sample_image(const ImageTex& t, float u, float v, float lod, float out[4])
+__device__ void sample_image_level(const ImageTex& t, int level, float u, float v, float out[4])
 {
     const uint32_t wrapX = t.sampler % 3u, wrapY = (t.sampler / 3u) % 3u;
     const bool nearest = t.sampler >= 9u;
-    int level = 0;
-    if (lod > .5f)
-        level = min((int)ceilf(__fadd_rn(lod, .5f)) - 1, (int)t.levels - 1);
     const int w = max((int)(t.width >> level), 1), h = max((int)(t.height >> level), 1);
     const uchar4* tex = t.texels + t.off[level];
     if (nearest)
@@ -2322,6 +2415,88 @@ __device__ void sample_image(const ImageTex& t, float u, float v, float lod, flo
             out[2] = __fadd_rn(out[2], __fmul_rn(wgt, __fdiv_rn((float)c.z, 255.f)));
             out[3] = __fadd_rn(out[3], __fmul_rn(wgt, __fdiv_rn((float)c.w, 255.f)));
         }
+}
+
+__device__ void sample_image(const ImageTex& t, float u, float v, float lod, float out[4])
+{
+    int level = 0;
+    if (lod > .5f)
+        level = min((int)ceilf(__fadd_rn(lod, .5f)) - 1, (int)t.levels - 1);
+    sample_image_level(t, level, u, v, out);
+}
+
+// One fragment of an image-mesh triangle (draw_mesh.frag:60-225 with
+// DRAW_IMAGE_MESH), written at once: the image at the triangle's texture
+// coordinates of the pixel (planes in the slot's feather-plane pair, exact
+// per pixel), at the mip level the set-up chose for the triangle; coverage 1,
+// cut by the clip rect and the clip, then times the draw's opacity; advanced
+// blending unmultiplies the texel first; dither, then src-over onto the
+// colour. The coverage plane keeps what it held (a mesh is no path).
+__device__ __noinline__ void resolve_mesh(const FlushParams& P, Pixel& s, uint32_t meta,
+                                          uint32_t imageDraw, uint32_t imageWord,
+                                          const float4* __restrict__ planes, float fx, float fy,
+                                          float dither)
+{
+    const uint32_t features = meta >> 16;
+    const float4 f0 = planes[0], f1 = planes[1];
+    const float dx = __fsub_rn(fx, f1.z), dy = __fsub_rn(fy, f1.w);
+    const float u = __fadd_rn(__fadd_rn(f0.x, __fmul_rn(f0.y, dx)), __fmul_rn(f0.z, dy));
+    const float v = __fadd_rn(__fadd_rn(f0.w, __fmul_rn(f1.x, dx)), __fmul_rn(f1.y, dy));
+    float color[4];
+    sample_image_level(P.images[imageWord & 0xffffffu], (int)(imageWord >> 24), u, v, color);
+    const float4* inst = P.imageDraws + 4 * (size_t)imageDraw;
+    const float4 packed = inst[3];
+    float coverage = 1.f;
+    if (features & SF_CLIP_RECT)
+    {
+        const float4 tr = inst[2];
+        coverage = fminf(fmaxf(clip_rect_distance_m(inst[1], make_float4(tr.z, tr.w, 0.f, 0.f),
+                                                    fx, fy),
+                               0.f),
+                         coverage);
+    }
+    if (features & SF_CLIPPING)
+    {
+        const uint32_t clipBits = id_bits_to_f16(__float_as_uint(packed.y), P.pathIDGranularity);
+        if (clipBits != 0)
+        {
+            const float clipCoverage = (s.clip >> 16) == clipBits ? h2f(s.clip & 0xffffu) : 0.f;
+            coverage = fminf(coverage, fmaxf(clipCoverage, 0.f));
+        }
+    }
+    coverage = __fmul_rn(coverage, packed.x); // opacity, after clipping
+    float dst[4];
+    unpack_rgba8(s.color, dst);
+    if (features & SF_ADVANCED_BLEND)
+    {
+        // unmultiply_rgb (common.glsl:210-216): images are premultiplied.
+        const float r = color[3] != 0.f ? __fdiv_rn(1.f, color[3]) : 0.f;
+        color[0] = __fmul_rn(color[0], r);
+        color[1] = __fmul_rn(color[1], r);
+        color[2] = __fmul_rn(color[2], r);
+        const uint32_t mode = __float_as_uint(packed.z);
+        if (mode != 0 && (mode < 12 || (features & SF_HSL_BLEND_MODES)))
+            advanced_blend(color, dst, mode);
+        color[3] *= coverage;
+        color[0] *= color[3];
+        color[1] *= color[3];
+        color[2] *= color[3];
+    }
+    else
+    {
+        for (int k = 0; k < 4; ++k)
+            color[k] *= coverage;
+    }
+    if ((features & SF_DITHER) && color[3] != 0.f)
+    {
+        color[0] += dither;
+        color[1] += dither;
+        color[2] += dither;
+    }
+    const float a = color[3];
+    for (int k = 0; k < 4; ++k)
+        color[k] = dst[k] * (1.f - a) + color[k];
+    s.color = pack_rgba8(color);
 }
 
 // ENABLE_MODULATED_IMAGE (draw_path.vert:343-361, 478-493): the paint's
@@ -2814,6 +2989,19 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
                 const float4 v3 = T.v3;
                 const float covx = __fmaf_rn(v2.w, lx, __fmaf_rn(v3.x, ly, v2.z));
                 const float covy = __fmaf_rn(v3.z, lx, __fmaf_rn(v3.w, ly, v3.y));
+                if (kFeather && ((T.v4.z >> 16) & FEATURE_IMAGE_MESH))
+                {
+                    // An image-mesh triangle blends at once, like a blit.
+                    if (s.pendMeta)
+                    {
+                        resolve_path<kFeather>(P, s, fx, fy, dither);
+                        s.pendMeta = 0;
+                    }
+                    const uint4 v4 = T.v4;
+                    resolve_mesh(P, s, v4.z, v4.x, v4.y, B.featherPlanes + 2 * (size_t)v4.w, fx, fy,
+                                 dither);
+                    continue;
+                }
                 if (kFeather && ((T.v4.z >> 16) & FEATURE_ATLAS_BLIT))
                 {
                     // A blit: the pending path is complete here; the blit

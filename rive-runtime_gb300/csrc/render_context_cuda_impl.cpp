@@ -19,25 +19,44 @@
 
 namespace rive::gpu
 {
-namespace
-{
-// Host memory for RenderBuffers (vertex/index data of image meshes, which
-// this backend does not draw; kept so Factory calls still succeed).
-class HostRenderBuffer : public RenderBuffer
+// A RenderBuffer of image-mesh data (vertex positions, texture coordinates or
+// indices): the app writes a host shadow between map and unmap; unmap copies
+// it into the device buffer (rive_cuda_render_buffer_write), which the
+// flushes of imageMesh batches then read.
+class RenderBufferCUDA : public RenderBuffer
 {
 public:
-    HostRenderBuffer(RenderBufferType type, RenderBufferFlags flags, size_t bytes) :
-        RenderBuffer(type, flags, bytes), m_bytes(bytes)
-    {}
+    RenderBufferCUDA(rive_cuda_context* ctx,
+                     RenderBufferType type,
+                     RenderBufferFlags flags,
+                     size_t bytes) :
+        RenderBuffer(type, flags, bytes), m_ctx(ctx), m_shadow(bytes)
+    {
+        m_status = rive_cuda_render_buffer_create(
+            ctx,
+            type == RenderBufferType::index ? RIVE_CUDA_RENDER_BUFFER_INDEX
+                                            : RIVE_CUDA_RENDER_BUFFER_VERTEX,
+            bytes, &m_buffer);
+    }
+    ~RenderBufferCUDA() override { rive_cuda_render_buffer_destroy(m_ctx, m_buffer); }
+    const rive_cuda_render_buffer* handle() const { return m_buffer; }
+    int status() const { return m_status; }
 
 protected:
-    void* onMap() override { return m_bytes.data(); }
-    void onUnmap() override {}
+    void* onMap() override { return m_shadow.data(); }
+    void onUnmap() override
+    {
+        if (m_buffer)
+            m_status = rive_cuda_render_buffer_write(m_ctx, m_buffer, 0, m_shadow.data(),
+                                                     m_shadow.size());
+    }
 
 private:
-    std::vector<uint8_t> m_bytes;
+    rive_cuda_context* m_ctx;
+    std::vector<uint8_t> m_shadow;
+    rive_cuda_render_buffer* m_buffer = nullptr;
+    int m_status = RIVE_CUDA_OK;
 };
-} // namespace
 
 RenderTargetCUDA::RenderTargetCUDA(rive_cuda_context* ctx,
                                    rive_cuda_render_target* target,
@@ -115,7 +134,9 @@ rcp<RenderBuffer> RenderContextCUDAImpl::makeRenderBuffer(RenderBufferType type,
                                                           RenderBufferFlags flags,
                                                           size_t bytes)
 {
-    return make_rcp<HostRenderBuffer>(type, flags, bytes);
+    auto buffer = make_rcp<RenderBufferCUDA>(m_ctx, type, flags, bytes);
+    note(buffer->status());
+    return buffer->handle() ? buffer : nullptr;
 }
 
 // A texture in device memory with its mip chain (rive_cuda_texture_create).
@@ -262,7 +283,8 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
 
     std::vector<rive_cuda_draw_batch> batches;
     std::vector<rive_cuda_batch_image> images;
-    bool anyImage = false;
+    std::vector<rive_cuda_batch_mesh> meshes;
+    bool anyImage = false, anyMesh = false;
     if (d.drawList != nullptr)
     {
         for (const DrawBatch& b : *d.drawList)
@@ -275,6 +297,18 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
                 anyImage = true;
             }
             images.push_back(im);
+            // An imageMesh batch's buffers (gpu.hpp:1261-1264).
+            rive_cuda_batch_mesh mesh = {};
+            if (b.drawType == DrawType::imageMesh && b.vertexBuffer && b.uvBuffer &&
+                b.indexBuffer)
+            {
+                mesh.vertices = static_cast<const RenderBufferCUDA*>(b.vertexBuffer)->handle();
+                mesh.uvs = static_cast<const RenderBufferCUDA*>(b.uvBuffer)->handle();
+                mesh.indices = static_cast<const RenderBufferCUDA*>(b.indexBuffer)->handle();
+                mesh.index_count = b.indexCountPerInstance;
+                anyMesh = true;
+            }
+            meshes.push_back(mesh);
             rive_cuda_draw_batch ob;
             ob.draw_type = static_cast<uint32_t>(b.drawType);
             ob.element_count = b.elementCount;
@@ -290,6 +324,7 @@ void RenderContextCUDAImpl::flush(const FlushDescriptor& d)
     o.draw_batch_count = static_cast<uint32_t>(batches.size());
     o.draw_batches = batches.empty() ? nullptr : batches.data();
     o.batch_images = anyImage ? images.data() : nullptr;
+    o.batch_meshes = anyMesh ? meshes.data() : nullptr;
 
     // The feather atlas batches: fills, then strokes.
     std::vector<rive_cuda_atlas_batch> atlas;

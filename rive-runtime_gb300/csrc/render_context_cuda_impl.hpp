@@ -22,10 +22,11 @@
 // plus interior triangles; i.e. fills (nonzero, even-odd, clockwise), strokes
 // with every join and cap, feathers of any radius (fills and strokes), linear
 // and radial gradients, clip paths (nested), clip rects, all blend modes,
-// dither, and image paints (drawImage draws a rectangle path with an image
-// paint in this mode) on RGBA textures with their mip chains. A flush that
-// needs anything else (image meshes, atomic/MSAA/clockwise interlock modes) is
-// not rendered: flush() records RIVE_CUDA_ERR_UNSUPPORTED in lastStatus().
+// dither, image paints (drawImage draws a rectangle path with an image paint
+// in this mode) and image meshes (drawImageMesh; RenderBuffers live on the
+// device) on RGBA textures with their mip chains. A flush that needs anything
+// else (atomic/MSAA/clockwise interlock modes) is not rendered: flush()
+// records RIVE_CUDA_ERR_UNSUPPORTED in lastStatus().
 #pragma once
 
 // texture.hpp first: render_context_impl.hpp destroys rcp<Texture> inline.

@@ -33,6 +33,7 @@ constexpr uint32_t DRAW_MIDPOINT_FAN_CENTER_AA_PATCHES = 1u;
 constexpr uint32_t DRAW_OUTER_CURVE_PATCHES = 2u;
 constexpr uint32_t DRAW_INTERIOR_TRIANGULATION = 3u;
 constexpr uint32_t DRAW_FEATHER_ATLAS_BLIT = 4u;
+constexpr uint32_t DRAW_IMAGE_MESH = 6u;
 
 constexpr float kPi = 3.14159265359f;
 constexpr float k2Pi = 6.28318530718f;
@@ -111,6 +112,10 @@ constexpr uint32_t FEATURE_ATLAS_BLIT = 1u << 12;
 // An atlas fill triangle that faced away (the atlas fill pipeline culls
 // nothing): turned clockwise, its coverage is subtracted.
 constexpr uint32_t FEATURE_ATLAS_NEGATE = 1u << 11;
+// An image-mesh triangle: its colour is the batch's image at the texture
+// coordinates of the pixel (planes in the feather-plane slots), blended at
+// once, triangle by triangle.
+constexpr uint32_t FEATURE_IMAGE_MESH = 1u << 10;
 // Two more bits of a triangle record's feature half-word, set only when the
 // batch draws interior tiles as winding records: a fan triangle whose tiles
 // are counted after its path's winding grid is complete, and the record of a
@@ -161,6 +166,7 @@ constexpr uint32_t ERR_BAD_PATH = 1u << 2;
 constexpr uint32_t ERR_RESERVED_8 = 1u << 3; // no longer raised (feathers are drawn)
 constexpr uint32_t ERR_COORD_RANGE = 1u << 4;
 constexpr uint32_t ERR_BIN_OVERFLOW = 1u << 5;
+constexpr uint32_t ERR_BAD_MESH_INDEX = 1u << 6;
 
 // One set-up triangle, ready for the tile raster (96 bytes). Edge k is
 // E_k(p) = A_k * (p.x - ax_k) + B_k * (p.y - ay_k), positive inside. Each edge
@@ -194,6 +200,20 @@ struct ImageTex
 };
 constexpr uint32_t PAINT_FLAG_HAS_IMAGE = 0x800u;
 constexpr uint32_t kNoImage = 0xffffffffu;
+
+// The mesh of an imageMesh draw batch: its render buffers (float2 positions,
+// float2 texture coordinates, uint16 triangle list), the vertices both
+// vertex buffers hold, its ImageDrawInstance and its image slot.
+struct MeshDesc
+{
+    const float2* positions;
+    const float2* uvs;
+    const uint16_t* indices;
+    uint32_t vertexCount, indexCount;
+    uint32_t imageDraw, image;
+    uint32_t pad;
+};
+constexpr uint32_t kNoMesh = 0xffffffffu;
 
 struct FlushParams
 {
@@ -238,6 +258,13 @@ struct FlushParams
     // the image its paint modulates (kNoImage: none), written by the set-up.
     const ImageTex* images;
     uint32_t* pathImage;
+    // Image meshes: the flush's ImageDrawInstance records (4 x float4 each:
+    // view matrix, clip-rect inverse matrix, translates, then opacity, clip
+    // ID, blend mode, z index as words), and FlushUniforms::mipMapLODBias
+    // (copied by scene_uniforms_kernel).
+    const float4* imageDraws;
+    uint32_t imageDrawCount;
+    float mipLodBias;
 };
 
 // One DrawBatch of one flush in a set-up work list: its first element (patch
@@ -252,6 +279,8 @@ struct PatchSegment
     uint32_t scissorLT, scissorRB;
     // The draw batch's image: a slot of the batch's image table, or kNoImage.
     uint32_t image;
+    // An imageMesh batch's entry in the batch's mesh table, or kNoMesh.
+    uint32_t mesh;
 };
 
 // Set-up work lists: midpoint-fan patches, outer-curve patches, interior
@@ -281,10 +310,13 @@ struct BatchTables
     // feather atlases (scenes after the main ones).
     uint32_t mainTiles;
     int tileLog2; // raster tile size of this batch (3, 4 or 5)
-    // Per triangle slot, when the batch holds feathered fills: the planes of
-    // the feather coverage's third and fourth components (cotTheta, y0) as
-    // (z0, dz/dx, dz/dy, w0), (dw/dx, dw/dy, anchor x, anchor y).
+    // Per triangle slot, when the batch holds feathered fills or image
+    // meshes: the planes of the feather coverage's third and fourth
+    // components (cotTheta, y0), or of a mesh triangle's texture coordinates
+    // (u, v), as (z0, dz/dx, dz/dy, w0), (dw/dx, dw/dy, anchor x, anchor y).
     float4* featherPlanes;
+    // Image meshes of the batch (PatchSegment::mesh indexes it).
+    const MeshDesc* meshes;
     // Interior tiles as winding records (null grids: off). Midpoint-fan
     // patches then take fanSlotStride = 25 slots (24 triangles and the
     // winding slot), otherwise 24.

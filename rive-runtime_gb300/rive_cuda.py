@@ -43,7 +43,8 @@ class FlushDesc(ctypes.Structure):
             "atlas_texture_width", "atlas_texture_height", "atlas_content_width",
             "atlas_content_height", "atlas_fill_batch_count",
             "atlas_stroke_batch_count")] + [("atlas_batches", ctypes.c_void_p),
-                                            ("batch_images", ctypes.c_void_p)]
+                                            ("batch_images", ctypes.c_void_p),
+                                            ("batch_meshes", ctypes.c_void_p)]
 
 
 class BatchImage(ctypes.Structure):
@@ -52,11 +53,18 @@ class BatchImage(ctypes.Structure):
                 ("reserved", ctypes.c_uint32)]
 
 
+class BatchMesh(ctypes.Structure):
+    """rive_cuda_batch_mesh."""
+    _fields_ = [("vertices", ctypes.c_void_p), ("uvs", ctypes.c_void_p),
+                ("indices", ctypes.c_void_p), ("index_count", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
 class DeviceBuffers(ctypes.Structure):
-    # rive_cuda_device_buffers; the last field is triangle_vertices.
+    # rive_cuda_device_buffers (triangles = triangle_vertices).
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "flush_uniforms", "paths", "paints", "paint_aux", "contours",
-        "grad_spans", "tess_spans", "triangles")]
+        "grad_spans", "tess_spans", "triangles", "image_draws")]
 
 
 class BatchFlush(ctypes.Structure):
@@ -127,6 +135,9 @@ def load():
         "rive_cuda_texture_create": (i32, [vp, u32, u32, u32, vp, ctypes.POINTER(vp)]),
         "rive_cuda_texture_destroy": (None, [vp, vp]),
         "rive_cuda_texture_read": (i32, [vp, vp, u32, vp, sz]),
+        "rive_cuda_render_buffer_create": (i32, [vp, u32, sz, ctypes.POINTER(vp)]),
+        "rive_cuda_render_buffer_write": (i32, [vp, vp, sz, vp, sz]),
+        "rive_cuda_render_buffer_destroy": (None, [vp, vp]),
         "rive_cuda_last_flush_stats": (i32, [vp, ctypes.POINTER(FlushStats)]),
         "rive_cuda_set_profiling": (i32, [vp, i32]),
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
@@ -150,10 +161,12 @@ def load():
     return lib
 
 
-def make_desc(flush, textures=None):
+def make_desc(flush, textures=None, buffers=None):
     """rive_cuda_flush_desc for one capture.Flush. `textures` maps the
     capture's texture indices to rive_cuda_texture handles (needed when a
-    batch draws an image). Returns (desc, arrays to keep alive)."""
+    batch draws an image), `buffers` its render-buffer indices to
+    rive_cuda_render_buffer handles (needed when a batch draws an image
+    mesh). Returns (desc, arrays to keep alive)."""
     d = FlushDesc()
     for k, v in flush.desc.items():
         if k.startswith("ub"):
@@ -178,7 +191,19 @@ def make_desc(flush, textures=None):
                 images[i].texture = textures[int(tex)]
                 images[i].sampler_key = int(key)
         d.batch_images = ctypes.addressof(images)
-    return d, (batches, atlas, images)
+    meshes = None
+    if getattr(flush, "has_meshes", False):
+        if buffers is None:
+            raise RiveCudaError("the flush draws image meshes: pass its render buffers")
+        meshes = (BatchMesh * len(batches))()
+        for i, (vb, ub, ib, n) in enumerate(np.asarray(flush.meshes, dtype=np.uint32)):
+            if vb != 0xFFFFFFFF:
+                meshes[i].vertices = buffers[int(vb)]
+                meshes[i].uvs = buffers[int(ub)]
+                meshes[i].indices = buffers[int(ib)]
+                meshes[i].index_count = int(n)
+        d.batch_meshes = ctypes.addressof(meshes)
+    return d, (batches, atlas, images, meshes)
 
 
 def feather_table():
@@ -272,6 +297,7 @@ class Context:
         self._targets = []
         self._capacity = {}
         self._textures = {}  # id(capture.Texture) -> (texture, handle)
+        self._buffers = {}  # id(capture.RenderBuffer) -> (buffer, handle)
 
     def close(self):
         if self.h:
@@ -281,6 +307,9 @@ class Context:
             for _, handle in self._textures.values():
                 self.lib.rive_cuda_texture_destroy(self.h, handle)
             self._textures = {}
+            for _, handle in self._buffers.values():
+                self.lib.rive_cuda_render_buffer_destroy(self.h, handle)
+            self._buffers = {}
             self.lib.rive_cuda_context_destroy(self.h)
             self.h = None
 
@@ -342,6 +371,32 @@ class Context:
             out.append(self._textures[key][1].value)
         return out
 
+    def buffers_for(self, flush):
+        """Device render buffers (rive_cuda_render_buffer handles) for the
+        capture render buffers a flush's image meshes draw, created and
+        written once per buffer."""
+        if not getattr(flush, "has_meshes", False):
+            return None
+        out = []
+        for b in flush.render_buffers:
+            key = id(b)
+            if key not in self._buffers:
+                h = ctypes.c_void_p()
+                data = np.frombuffer(b.data, np.uint8)
+                self.check(self.lib.rive_cuda_render_buffer_create(
+                    self.h, b.type, max(len(b.data), 1), ctypes.byref(h)), "render_buffer_create")
+                self._buffers[key] = (b, h)
+                if len(b.data):
+                    self.check(self.lib.rive_cuda_render_buffer_write(
+                        self.h, h, 0, data.ctypes.data_as(ctypes.c_void_p), len(b.data)),
+                        "render_buffer_write")
+            out.append(self._buffers[key][1].value)
+        return out
+
+    def desc_for(self, flush):
+        """make_desc with this context's textures and render buffers."""
+        return make_desc(flush, self.textures_for(flush), self.buffers_for(flush))
+
     def read_texture(self, handle, level, width, height):
         """Mip level `level` (width x height texels) of a device texture."""
         out = np.zeros((height, width, 4), np.uint8)
@@ -351,12 +406,12 @@ class Context:
         return out
 
     def flush(self, flush, target, stream=None):
-        d, keep = make_desc(flush, self.textures_for(flush))
+        d, keep = self.desc_for(flush)
         self.check(self.lib.rive_cuda_flush(self.h, ctypes.byref(d), target, stream), "flush")
         del keep
 
     def flush_device(self, flush, bufs: DeviceBuffers, target_ptr: int, stream=None):
-        d, keep = make_desc(flush, self.textures_for(flush))
+        d, keep = self.desc_for(flush)
         self.check(self.lib.rive_cuda_flush_device(self.h, ctypes.byref(d), ctypes.byref(bufs),
                                                    ctypes.c_void_p(target_ptr), stream),
                    "flush_device")
@@ -366,7 +421,7 @@ class Context:
         arr = (BatchFlush * max(len(items), 1))()
         keep = []
         for i, (flush, bufs, target_ptr) in enumerate(items):
-            d, k = make_desc(flush, self.textures_for(flush))
+            d, k = self.desc_for(flush)
             keep.append((d, k))
             arr[i].desc = ctypes.cast(ctypes.pointer(d), ctypes.c_void_p)
             arr[i].buffers = bufs

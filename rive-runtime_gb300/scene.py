@@ -42,6 +42,10 @@ CMD_MODULATE_OPACITY = 5  # m[0] = opacity (Renderer::modulateOpacity)
 # m[0] = opacity.
 CMD_DRAW_IMAGE = 6
 IMAGES_MAGIC = 0x31495352  # "RSI1"
+# Renderer::drawImageMesh: a = image index, b = blend mode | sampler key << 8,
+# m[0] = opacity, m[1] = mesh index.
+CMD_DRAW_IMAGE_MESH = 7
+MESHES_MAGIC = 0x314D5352  # "RSM1"
 # ImageSampler (include/rive/shapes/paint/image_sampler.hpp): key =
 # wrapX + 3 wrapY + 9 filter; wrap 0 clamp, 1 repeat, 2 mirror; filter 0
 # bilinear, 1 nearest.
@@ -100,6 +104,15 @@ class Image:
 
 
 @dataclass
+class Mesh:
+    """An image mesh: local positions (n, 2), texture coordinates (n, 2) and a
+    uint16 triangle list."""
+    xy: np.ndarray
+    uv: np.ndarray
+    indices: np.ndarray
+
+
+@dataclass
 class Scene:
     width: int
     height: int
@@ -110,6 +123,7 @@ class Scene:
     paints: list = field(default_factory=list)
     cmds: list = field(default_factory=list)  # (op, a, b, m6)
     images: list = field(default_factory=list)  # Image
+    meshes: list = field(default_factory=list)  # Mesh
 
     def add_path(self, p: Path) -> int:
         self.paths.append(p)
@@ -126,6 +140,15 @@ class Scene:
     def draw_image(self, image: int, opacity: float = 1.0, blend_mode: int = BLEND_SRC_OVER,
                    sampler: int = 0):
         self.cmd(CMD_DRAW_IMAGE, image, blend_mode | (sampler << 8), (opacity, 0, 0, 0, 0, 0))
+
+    def add_mesh(self, m: Mesh) -> int:
+        self.meshes.append(m)
+        return len(self.meshes) - 1
+
+    def draw_image_mesh(self, image: int, mesh: int, opacity: float = 1.0,
+                        blend_mode: int = BLEND_SRC_OVER, sampler: int = 0):
+        self.cmd(CMD_DRAW_IMAGE_MESH, image, blend_mode | (sampler << 8),
+                 (opacity, float(mesh), 0, 0, 0, 0))
 
     def cmd(self, op, a=0, b=0, m=(0, 0, 0, 0, 0, 0)):
         self.cmds.append((op, a, b, tuple(float(v) for v in m)))
@@ -161,14 +184,25 @@ class Scene:
         stop_bytes = b"".join(struct.pack("<fI", float(s), c & 0xFFFFFFFF)
                               for s, c in stops)
         image_bytes = b""
-        if self.images:
+        if self.images or self.meshes:
             image_bytes = struct.pack("<2I", IMAGES_MAGIC, len(self.images))
             for im in self.images:
                 a = np.ascontiguousarray(im.rgba, dtype=np.uint8)
                 image_bytes += struct.pack("<2I", a.shape[1], a.shape[0]) + a.tobytes()
+        mesh_bytes = b""
+        if self.meshes:
+            mesh_bytes = struct.pack("<2I", MESHES_MAGIC, len(self.meshes))
+            for m in self.meshes:
+                xy = np.ascontiguousarray(m.xy, dtype="<f4").reshape(-1, 2)
+                uv = np.ascontiguousarray(m.uv, dtype="<f4").reshape(-1, 2)
+                ix = np.ascontiguousarray(m.indices, dtype="<u2").reshape(-1)
+                assert len(xy) == len(uv) and len(ix) % 3 == 0
+                ib = ix.tobytes()
+                mesh_bytes += (struct.pack("<2I", len(xy), len(ix)) + xy.tobytes() + uv.tobytes()
+                               + ib + bytes((4 - len(ib) % 4) % 4))
         return (header + b"".join(path_recs) + b"".join(paint_recs)
                 + b"".join(cmd_recs) + bytes(verbs) + vpad + pts_bytes + stop_bytes
-                + image_bytes)
+                + image_bytes + mesh_bytes)
 
     @property
     def draw_count(self):
@@ -495,4 +529,116 @@ def images(seed: int = 41, width: int = 384, height: int = 320, n_images: int = 
                               int(rng.integers(0, 2)))
         sc.draw_image(im, float(rng.uniform(0.3, 1.0)), blend, sampler)
         sc.cmd(CMD_RESTORE)
+    return sc
+
+
+def _grid_mesh(rng, w: float, h: float, gx: int, gy: int, uv_scale: float, warp: float) -> Mesh:
+    """A (gx x gy)-cell grid over [0, w] x [0, h], its inner vertices moved by
+    up to `warp` cells, texture coordinates (i / gx, j / gy) * uv_scale; two
+    triangles per cell, alternating diagonals (both windings occur)."""
+    jj, ii = np.meshgrid(np.arange(gy + 1), np.arange(gx + 1), indexing="ij")
+    x = ii * (w / gx)
+    y = jj * (h / gy)
+    inner = (ii > 0) & (ii < gx) & (jj > 0) & (jj < gy)
+    x = x + inner * rng.uniform(-warp, warp, x.shape) * (w / gx)
+    y = y + inner * rng.uniform(-warp, warp, y.shape) * (h / gy)
+    xy = np.stack([x.ravel(), y.ravel()], 1).astype(np.float32)
+    uv = (np.stack([(ii / gx).ravel(), (jj / gy).ravel()], 1) * uv_scale).astype(np.float32)
+    idx = []
+    for j in range(gy):
+        for i in range(gx):
+            a, b = j * (gx + 1) + i, j * (gx + 1) + i + 1
+            c, d = a + gx + 1, b + gx + 1
+            if (i + j) % 2:
+                idx += [a, b, d, a, d, c]
+            else:
+                idx += [a, b, c, b, d, c]
+    return Mesh(xy, uv, np.array(idx, np.uint16))
+
+
+def _soup_mesh(rng, w: float, h: float, n_tris: int) -> Mesh:
+    """`n_tris` random triangles over [0, w] x [0, h] that overlap one another
+    (every covering triangle blends), random windings and texture coordinates
+    in [-0.5, 1.5], some vertices shared."""
+    nv = max(3, int(n_tris * 1.5))
+    xy = np.stack([rng.uniform(0, w, nv), rng.uniform(0, h, nv)], 1).astype(np.float32)
+    uv = rng.uniform(-0.5, 1.5, (nv, 2)).astype(np.float32)
+    idx = rng.integers(0, nv, (n_tris, 3)).astype(np.uint16)
+    return Mesh(xy, uv, idx.ravel())
+
+
+def image_meshes(seed: int = 43, width: int = 384, height: int = 320, n_images: int = 5,
+                 n_draws: int = 22, n_paths: int = 14) -> Scene:
+    """Image meshes drawn with Renderer::drawImageMesh between full-feature
+    paths: warped grids (texture coordinates up to 2.5, so repeat and mirror
+    wrap) and overlapping triangle soups, magnified and minified under
+    rotations (so the implicit level of detail picks different mip levels),
+    with every ImageSampler, opacity in [0.3, 1], some advanced blend modes,
+    some under clip paths and some under axis-aligned rectangle clips (clip
+    rects); a few drawImage rectangles too."""
+    rng = np.random.default_rng(seed)
+    sc = full_feature(seed=seed, width=width, height=height, n_paths=n_paths, max_cubics=8,
+                      p_clip=0.2, scale_range=(0.5, 2.0))
+    sizes = [(64, 64), (128, 32), (9, 15), (200, 90), (33, 33)]
+    for k in range(n_images):
+        w, h = sizes[k % len(sizes)]
+        sc.add_image(_procedural_image(rng, w, h))
+    clip_paths = [i for i, _ in enumerate(sc.paths)]
+    # Axis-aligned rectangles: clipPath turns these into clip rects.
+    rects = []
+    for _ in range(3):
+        x0, y0 = rng.uniform(0, width * .6), rng.uniform(0, height * .6)
+        x1, y1 = x0 + rng.uniform(40, width * .5), y0 + rng.uniform(40, height * .5)
+        pts = np.array([[x0, y0], [x1, y0], [x1, y1], [x0, y1]], np.float32)
+        rects.append(sc.add_path(Path([VERB_MOVE, VERB_LINE, VERB_LINE, VERB_LINE, VERB_CLOSE],
+                                      pts, FILL_NONZERO)))
+    for k in range(n_draws):
+        im = int(rng.integers(0, n_images))
+        iw, ih = sc.images[im].rgba.shape[1], sc.images[im].rgba.shape[0]
+        if rng.uniform() < 0.6:
+            mesh = _grid_mesh(rng, float(iw), float(ih), int(rng.integers(1, 7)),
+                              int(rng.integers(1, 6)), float(rng.choice([1.0, 1.0, 2.5])),
+                              float(rng.uniform(0, .35)))
+        else:
+            mesh = _soup_mesh(rng, float(iw), float(ih), int(rng.integers(2, 12)))
+        mi = sc.add_mesh(mesh)
+        target = float(np.exp(rng.uniform(np.log(10), np.log(300))))
+        s = target / max(iw, ih)
+        th = rng.uniform(0, 2 * np.pi)
+        c, sn = np.cos(th) * s, np.sin(th) * s
+        tx, ty = rng.uniform(0, width), rng.uniform(0, height)
+        sc.cmd(CMD_SAVE)
+        r = rng.uniform()
+        if r < 0.15:
+            sc.cmd(CMD_CLIP_PATH, int(rng.choice(rects)))
+        elif r < 0.3 and clip_paths:
+            sc.cmd(CMD_CLIP_PATH, int(rng.choice(clip_paths)))
+        sc.cmd(CMD_TRANSFORM, m=(c, sn, -sn, c, tx - (c * iw - sn * ih) / 2,
+                                 ty - (sn * iw + c * ih) / 2))
+        blend = int(rng.choice(BLEND_MODES)) if rng.uniform() < 0.25 else BLEND_SRC_OVER
+        sampler = sampler_key(int(rng.integers(0, 3)), int(rng.integers(0, 3)),
+                              int(rng.integers(0, 2)))
+        opacity = float(rng.uniform(0.3, 1.0))
+        if k % 7 == 3:
+            sc.draw_image(im, opacity, blend, sampler)
+        else:
+            sc.draw_image_mesh(im, mi, opacity, blend, sampler)
+        sc.cmd(CMD_RESTORE)
+    return sc
+
+
+def mesh_overlap(opacity: float = 0.5) -> Scene:
+    """Two overlapping triangles of one image mesh, one clockwise and one
+    counterclockwise, textured by an opaque red 4x4 image with a nearest
+    sampler, at `opacity` on white without dither: where both cover a pixel
+    it blends twice."""
+    sc = Scene(64, 64, clear_color=0xFFFFFFFF, dither_mode=0)
+    rgba = np.zeros((4, 4, 4), np.uint8)
+    rgba[..., 0] = 255
+    rgba[..., 3] = 255
+    sc.add_image(Image(rgba))
+    xy = np.array([[8, 8], [56, 8], [8, 56], [16, 16], [16, 60], [60, 16]], np.float32)
+    uv = np.array([[0, 0], [1, 0], [0, 1], [0, 0], [0, 1], [1, 0]], np.float32)
+    sc.add_mesh(Mesh(xy, uv, np.arange(6, dtype=np.uint16)))
+    sc.draw_image_mesh(0, 0, opacity, BLEND_SRC_OVER, sampler_key(filt=FILTER_NEAREST))
     return sc

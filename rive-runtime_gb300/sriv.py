@@ -16,10 +16,14 @@ transform and modulateOpacity carry over as commands. The renderer state is
 per frame, as a test harness that calls Artboard::draw once per frame leaves
 it (every draw is bracketed by save/restore).
 
-What the scene format does not carry is dropped and counted in `FrameStats`:
-image draws and image meshes (no image paints behind this boundary). Draws
-with a feathered paint are dropped and counted too unless `keep_feathered`
-(the backend renders feathered strokes; feathered fills are refused).
+Image draws and image meshes are dropped and counted in `FrameStats` unless
+`images`: then each decodeImage's bytes are decoded (image_decode: PNG and
+baseline JPEG) and premultiplied as RenderContext::decodeImage does
+(render_context.cpp:237-262), drawImage becomes a scene image draw and
+drawImageMesh a scene mesh of the RenderBuffer contents at that call, both
+with ImageSampler::LinearClamp as the reference's replay draws them
+(utils/serialized_replay.cpp:293-330). Draws with a feathered paint are
+dropped and counted too unless `keep_feathered`.
 """
 from __future__ import annotations
 
@@ -139,6 +143,8 @@ class FrameStats:
     clips: int = 0
     dropped_feathered: int = 0
     dropped_images: int = 0
+    images: int = 0
+    meshes: int = 0
 
 
 @dataclass
@@ -154,13 +160,48 @@ class SrivStream:
     height: int
     frames: list  # list of lists of _Call
     shaders: dict  # id -> (kind, stops [(pos, color)], g4)
+    encoded_images: dict = field(default_factory=dict)  # id -> encoded bytes
+    _decoded: dict = field(default_factory=dict)  # id -> premultiplied RGBA or None
+
+    def decoded_image(self, iid):
+        """The premultiplied RGBA8 texels of image `iid`, or None when it
+        cannot be decoded here."""
+        if iid not in self._decoded:
+            from . import image_decode
+            data = self.encoded_images.get(iid)
+            try:
+                self._decoded[iid] = (image_decode.premultiply(image_decode.decode(data))
+                                      if data is not None else None)
+            except image_decode.DecodeError:
+                self._decoded[iid] = None
+        return self._decoded[iid]
 
     def frame_scene(self, k: int, clear_color: int = 0x00000000,
-                    dither_mode: int = S.DITHER_IGN, keep_feathered: bool = False):
+                    dither_mode: int = S.DITHER_IGN, keep_feathered: bool = False,
+                    images: bool = False):
         """Frame k as a scene.Scene plus its FrameStats."""
         sc = S.Scene(self.width, self.height, clear_color=clear_color, dither_mode=dither_mode)
         st = FrameStats()
-        path_ix, paint_ix = {}, {}
+        path_ix, paint_ix, image_ix, mesh_ix = {}, {}, {}, {}
+
+        def image_of(iid):
+            if iid not in image_ix:
+                rgba = self.decoded_image(iid)
+                image_ix[iid] = None if rgba is None else sc.add_image(S.Image(rgba))
+            return image_ix[iid]
+
+        def mesh_of(bufs):
+            key = tuple((b[0], b[1]) for b in bufs)
+            if key not in mesh_ix:
+                pos, uv, idx = (b[3] for b in bufs)
+                xy = np.frombuffer(pos, "<f4").reshape(-1, 2)
+                tc = np.zeros_like(xy)
+                uvs = np.frombuffer(uv, "<f4")[:2 * len(xy)].reshape(-1, 2)
+                tc[:len(uvs)] = uvs
+                ix = np.frombuffer(idx, "<u2")
+                ix = ix[:len(ix) - len(ix) % 3]
+                mesh_ix[key] = sc.add_mesh(S.Mesh(xy, tc, ix)) if len(ix) and len(xy) else None
+            return mesh_ix[key]
 
         def path_of(snap):
             key = snap[0]
@@ -204,7 +245,21 @@ class SrivStream:
                 st.draws += 1
                 sc.cmd(S.CMD_DRAW_PATH, path_of(c.a), paint_of(c.b))
             elif c.op in (OP_DRAW_IMAGE, OP_DRAW_IMAGE_MESH):
-                st.dropped_images += 1
+                im = image_of(c.a[0]) if images else None
+                if im is None:
+                    st.dropped_images += 1
+                    continue
+                iid, blend, opacity = c.a
+                if c.op == OP_DRAW_IMAGE:
+                    st.images += 1
+                    sc.draw_image(im, opacity, blend, S.sampler_key())
+                else:
+                    mi = mesh_of(c.b)
+                    if mi is None:
+                        st.dropped_images += 1
+                        continue
+                    st.meshes += 1
+                    sc.draw_image_mesh(im, mi, opacity, blend, S.sampler_key())
         return sc, st
 
 
@@ -249,7 +304,8 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
     paths: dict[int, _PathState] = {}
     paints: dict[int, _PaintState] = {}
     shaders: dict[int, tuple] = {}
-    buffers: dict[int, int] = {}  # id -> size in bytes
+    buffers: dict[int, list] = {}  # id -> [size, type, version, bytes]
+    encoded: dict[int, bytes] = {}
     frames = [[]]
     width = height = 0
     serial = [0]
@@ -370,23 +426,31 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
                 g = (r.f32(), r.f32(), r.f32(), 0.0)
                 shaders[sid] = (S.SHADER_RADIAL, stops, g)
         elif op == OP_DECODE_IMAGE:
-            r.varuint()
-            r.skip(r.varuint())
+            iid = r.varuint()
+            n = r.varuint()
+            start = r.p
+            r.skip(n)
+            encoded[iid] = bytes(r.b[start:start + n])
         elif op == OP_MAKE_RENDER_BUFFER:
             bid = r.varuint()
             size = r.varuint()
-            r.varuint()  # RenderBufferType
+            kind = r.varuint()  # RenderBufferType
             r.varuint()  # RenderBufferFlags
-            buffers[bid] = size
+            buffers[bid] = [size, kind, 0, bytes(size)]
         elif op in (OP_SET_VERTEX_BUFFER_DATA, OP_SET_INDEX_BUFFER_DATA):
             bid = r.varuint()
             if bid not in buffers:
                 raise SrivError(f"unknown buffer {bid}")
+            size = buffers[bid][0]
             if op == OP_SET_VERTEX_BUFFER_DATA:
-                r.skip(4 * (buffers[bid] // 4))
+                data_bytes = bytes(r.f32s(size // 4).astype("<f4").tobytes())
             else:
-                for _ in range(buffers[bid] // 2):
-                    r.varuint()
+                vals = [r.varuint() & 0xFFFF for _ in range(size // 2)]
+                data_bytes = np.array(vals, "<u2").tobytes()
+            buf = buffers[bid]
+            buf[3] = data_bytes + bytes(size - len(data_bytes))
+            serial[0] += 1
+            buf[2] = serial[0]
         elif op == OP_SAVE or op == OP_RESTORE:
             frames[-1].append(_Call(op))
         elif op == OP_TRANSFORM:
@@ -400,17 +464,19 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
         elif op == OP_CLIP_PATH:
             frames[-1].append(_Call(op, path_snap(r.varuint())))
         elif op == OP_DRAW_IMAGE:
-            r.varuint()
-            r.varuint()
-            r.f32()
-            frames[-1].append(_Call(op))
+            iid = r.varuint()
+            blend = r.varuint()
+            opacity = float(r.f32())
+            frames[-1].append(_Call(op, (iid, blend, opacity)))
         elif op == OP_DRAW_IMAGE_MESH:
-            r.varuint()
-            r.varuint()
-            r.f32()
-            for _ in range(3):
-                r.varuint()
-            frames[-1].append(_Call(op))
+            iid = r.varuint()
+            blend = r.varuint()
+            opacity = float(r.f32())
+            ids = [r.varuint() for _ in range(3)]
+            # The buffers' contents at this call: (id, version, type, bytes).
+            snaps = tuple((b, buffers[b][2], buffers[b][1], buffers[b][3]) if b in buffers
+                          else (b, -1, 0, b"") for b in ids)
+            frames[-1].append(_Call(op, (iid, blend, opacity), snaps))
         elif op == OP_FRAME:
             frames.append([])
         elif op == OP_FRAME_SIZE:
@@ -421,4 +487,4 @@ def read_sriv(data: bytes, default_size=None) -> SrivStream:
         width, height = default_size
     if width == 0 or height == 0:
         raise SrivError("no frame size")
-    return SrivStream(width, height, frames, shaders)
+    return SrivStream(width, height, frames, shaders, encoded)

@@ -113,6 +113,15 @@ SCENES["feathered_atlas_s33"] = lambda: _atlas_always(scene.feathered(seed=33))
 # and minified (mip levels), opacity, blend modes, clips.
 SCENES["images_s41"] = lambda: scene.images(seed=41)
 
+# Image meshes drawn with Renderer::drawImageMesh (rive_renderer.cpp:448-495;
+# draw_image_mesh.vert, draw_mesh.frag): warped grids and overlapping
+# triangle soups, both windings, every ImageSampler, implicit mip levels,
+# opacity, blend modes, clip paths and clip rects, beside drawImage draws.
+SCENES["image_meshes_s43"] = lambda: scene.image_meshes(seed=43)
+# Two overlapping mesh triangles of opposite windings: both are drawn and
+# both blend where they overlap (a known answer).
+SCENES["mesh_overlap"] = lambda: scene.mesh_overlap()
+
 # Real frames whose wide feathers the reference front end sends through the
 # feather atlas (feathered draws kept).
 ATLAS_SILVERS = {
@@ -122,16 +131,27 @@ ATLAS_SILVERS = {
 }
 
 
+# Real frames with their images: the recorded PNG / JPEG bytes decoded
+# (image_decode) and premultiplied as RenderContext::decodeImage does;
+# drawImage draws and, in image_fit_alignment_2, a drawImageMesh with the
+# RenderBuffer contents the stream recorded.
+IMAGE_SILVERS = {
+    "silver_image_mesh_f10": ("image_fit_alignment_2", 10),
+    "silver_clipping_images_f6": ("clipping_and_draw_order", 6),
+    "silver_superbowl_images_f5": ("superbowl", 5),
+}
+
+
 def _atlas_always(sc):
     sc.flags = scene.FLAG_FEATHER_ATLAS
     return sc
 
 
-def _silver(stream, frame, keep_feathered=False):
+def _silver(stream, frame, keep_feathered=False, images=False):
     from rive_runtime_gb300 import sriv
     with open(os.path.join(SILVER_DIR, stream + ".sriv"), "rb") as f:
         st = sriv.read_sriv(f.read())
-    return st.frame_scene(frame, keep_feathered=keep_feathered)[0]
+    return st.frame_scene(frame, keep_feathered=keep_feathered, images=images)[0]
 
 
 for _name, (_stream, _frame) in SILVERS.items():
@@ -140,6 +160,8 @@ for _name, (_stream, _frame) in FEATHERED_SILVERS.items():
     SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True))
 for _name, (_stream, _frame) in ATLAS_SILVERS.items():
     SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True))
+for _name, (_stream, _frame) in IMAGE_SILVERS.items():
+    SCENES[_name] = (lambda s=_stream, k=_frame: _silver(s, k, keep_feathered=True, images=True))
 
 
 def _triangulated(sc):

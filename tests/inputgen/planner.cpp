@@ -2782,6 +2782,7 @@ std::vector<uint8_t> plan(const uint8_t* data, size_t size)
                         std::max(0.0f, r.stack.back().modulatedOpacity * c.m[0]);
                     break;
                 case RIVE_SCENE_CMD_DRAW_IMAGE:
+                case RIVE_SCENE_CMD_DRAW_IMAGE_MESH:
                     throw PlanError("image draws are not planned here (the reference front end plans them)");
                 default:
                     throw PlanError("bad command");
