@@ -571,6 +571,20 @@ int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled);
 int rive_cuda_get_winding_tiles(const rive_cuda_context* ctx, int* enabled);
 
 /*
+ * Speculative bins (no counterpart in the reference; on by default). A flush
+ * on the context's own stream sizes its bins from the largest bin-entry total
+ * the context has seen (plus a quarter) instead of waiting for the scan's
+ * total, so rive_cuda_flush returns without waiting for the device and the
+ * caller can write the next frame's records while this one renders. The
+ * total is checked at the next call into the context; when it did not fit,
+ * the flush's back half runs again with exact bins before anything else, and
+ * read-backs enqueued after it are repeated. The image is the same either
+ * way. Flushes on a caller's stream and batches always size bins exactly.
+ */
+int rive_cuda_set_bin_speculation(rive_cuda_context* ctx, int enabled);
+int rive_cuda_get_bin_speculation(const rive_cuda_context* ctx, int* enabled);
+
+/*
  * Per-stage device timing with CUDA events recorded on the flush stream
  * (off by default; no counterpart in the reference, whose backends time
  * nothing). Stages of one flush, in launch order:

@@ -76,6 +76,10 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    uint32_t tileCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
+__global__ void ranges_guard_kernel(const uint32_t* pairTotal,
+                                    uint32_t capacity,
+                                    uint2* ranges,
+                                    uint32_t tiles);
 // The work-queue raster (kernels_raster.cu).
 __global__ void raster_queue_kernel(BatchTables B,
                                     const TriRecord* tris,
@@ -209,13 +213,28 @@ struct RecordRing
     size_t capacity = 0;
     int current = 0;
     bool mapped = false;
-    DeviceBuffer device;
-    size_t deviceValidBytes = 0;
+    // Two device copies in turn: an upload goes to the copy the flushes in
+    // flight do not read, on the context's copy stream, so frame k+1's
+    // records cross while frame k renders. `slot` is the copy the next flush
+    // reads; `used` says a flush has read it since its upload (the next
+    // upload then takes the other copy, once the flushes that read that one
+    // are done: `readDone`). `copied` orders a flush after its slot's upload.
+    DeviceBuffer device[2];
+    size_t deviceValidBytes[2] = {};
+    int slot = 0;
+    bool used = false;
+    cudaEvent_t readDone[2] = {};
+    cudaEvent_t copied[2] = {};
 };
 } // namespace
 
 // An image texture (rive_cuda_texture_create): one device allocation with
 // every mip level, and its descriptor for the kernels.
+namespace
+{
+struct PendingFlush;
+} // namespace
+
 struct rive_cuda_texture
 {
     void* mem = nullptr;
@@ -241,6 +260,7 @@ struct rive_cuda_context
 {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copyStream = nullptr; // record uploads (rive_cuda_unmap_buffer)
     std::string lastError;
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
@@ -248,8 +268,23 @@ struct rive_cuda_context
     DeviceBuffer tris, tileCounts, tileMasks, offsets, featherPlanes;
     DeviceBuffer keys, vals, keysAlt, valsAlt, sortTemp, scanTemp, ranges;
     DeviceBuffer dTables;  // batch tables (device)
-    HostBuffer hTables;    // pinned staging of the tables
-    cudaEvent_t tablesCopied = nullptr;
+    // Pinned staging of the tables, a ring of three, so the host writes the
+    // next flush's tables while earlier copies are still queued.
+    static constexpr int kTableRing = 3;
+    HostBuffer hTables[kTableRing];
+    cudaEvent_t tablesCopied[kTableRing] = {};
+    int tableSlot = 0;
+    // Speculative bins (flushes on the context's own stream): the back half
+    // of a flush is enqueued with bins sized from the largest bin-entry total
+    // seen (plus a quarter) instead of waiting for the scan's total; the
+    // total is read back without a wait and checked at the next call
+    // (settle_pending), which re-runs the back half with exact bins in the
+    // rare case it did not fit. binHighWater = 0: no total seen yet.
+    bool speculate = true;
+    uint32_t binHighWater = 0;
+    PendingFlush* pending = nullptr;
+    uint32_t* hSpecTotal = nullptr;    // pinned: the pending flush's scanned total
+    uint32_t* dSpecOverflow = nullptr; // bin overflow status of speculative passes
     uint32_t* dError = nullptr;
     uint32_t* hError = nullptr;  // pinned
     uint32_t* hPairs = nullptr;  // pinned: scanned pair total
@@ -785,6 +820,10 @@ struct Scratch
     size_t sortTempBytes = 0;
     uint2* ranges = nullptr;
     uint32_t* error = nullptr;
+    // Where the binner reports entries past the bins' capacity (error when
+    // null; a scratch word for speculative passes, whose overflow is
+    // handled by re-running the back half).
+    uint32_t* binError = nullptr;
     float4* featherPlanes = nullptr; // 2 per slot, only with center-AA patches
     uint16_t* atlas = nullptr;       // the batch's feather atlases, fp16 texels
     uint32_t* pathImage = nullptr;   // per path of the batch: its image slot
@@ -1231,8 +1270,10 @@ int enqueue_back(rive_cuda_context* ctx,
                  const Scratch& S,
                  uint32_t entries,
                  bool padded,
-                 cudaStream_t stream)
+                 cudaStream_t stream,
+                 bool guarded = false)
 {
+    uint32_t* const binError = S.binError ? S.binError : S.error;
     const uint32_t* sortedSlots = nullptr;
     if (entries && L.slots)
     {
@@ -1242,11 +1283,11 @@ int enqueue_back(rive_cuda_context* ctx,
                                                                       L.tiles, S.keys);
         if (L.winding)
             bin_scatter_winding_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
-                B, S.tris, S.counts, S.masks, S.offsets, L.slots, entries, S.error, S.keys, S.vals);
+                B, S.tris, S.counts, S.masks, S.offsets, L.slots, entries, binError, S.keys, S.vals);
         else
             bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
                 L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries,
-                S.error, S.keys, S.vals);
+                binError, S.keys, S.vals);
         stage_end(ctx, stream);
         cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
         cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
@@ -1256,6 +1297,13 @@ int enqueue_back(rive_cuda_context* ctx,
                                            L.endBit(), stream));
         tile_ranges_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(entries, L.tiles, k.Current(),
                                                                     S.ranges);
+        // A speculative pass whose total did not fit: every range emptied,
+        // so the raster leaves the target as it was (or clears it) until the
+        // back half runs again with exact bins.
+        if (guarded)
+            ranges_guard_kernel<<<(L.tiles + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots,
+                                                                          entries, S.ranges,
+                                                                          L.tiles);
         stage_end(ctx, stream);
         sortedSlots = v.Current();
     }
@@ -1310,22 +1358,106 @@ size_t sort_temp_bytes(uint32_t entries, int endBit)
 // Runs a batch of independent logical flushes (distinct targets) as one
 // sequence of launches: every stage covers the work of all flushes at once.
 // The bin-entry total is read back after the scan, so bins are sized exactly.
-int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStream_t stream)
+// The flush whose back half ran on speculative bins and whose bin-entry total
+// has not been checked yet (at most one per context).
+struct PendingFlush
+{
+    BatchLayout L;
+    BatchTables B;
+    Scratch S;
+    uint32_t capacity = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t counted = nullptr;
+    bool active = false;
+    // Read-backs enqueued after it, to enqueue again after a re-run.
+    std::vector<std::pair<rive_cuda_render_target*, void*>> reads;
+};
+
+// Reserves the sort keys/values and sort temporaries for `entries` bin
+// entries and points S at them.
+int reserve_bins(rive_cuda_context* ctx, const BatchLayout& L, uint32_t entries, Scratch& S)
+{
+    CK(ctx->keys.reserve((size_t)entries * 4));
+    CK(ctx->vals.reserve((size_t)entries * 4));
+    CK(ctx->keysAlt.reserve((size_t)entries * 4));
+    CK(ctx->valsAlt.reserve((size_t)entries * 4));
+    S.sortTempBytes = sort_temp_bytes(entries, L.endBit());
+    CK(ctx->sortTemp.reserve(S.sortTempBytes));
+    S.keys = (uint32_t*)ctx->keys.ptr;
+    S.vals = (uint32_t*)ctx->vals.ptr;
+    S.keysAlt = (uint32_t*)ctx->keysAlt.ptr;
+    S.valsAlt = (uint32_t*)ctx->valsAlt.ptr;
+    S.sortTemp = ctx->sortTemp.ptr;
+    return RIVE_CUDA_OK;
+}
+
+// Checks the pending speculative flush, if any: waits for its scanned total
+// and, when the total did not fit its bins (the guarded raster then left the
+// target untouched), runs its back half again with exact bins and repeats
+// the read-backs enqueued after it. Every call that enqueues work on the
+// context, reads its results or changes its configuration settles first.
+int settle_pending(rive_cuda_context* ctx)
+{
+    PendingFlush* p = ctx->pending;
+    if (!p || !p->active)
+        return RIVE_CUDA_OK;
+    p->active = false;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventSynchronize(p->counted));
+    const uint32_t total = *ctx->hSpecTotal;
+    ctx->binHighWater = std::max(ctx->binHighWater, total);
+    ctx->stats.bin_entries = total;
+    if (total > p->capacity)
+    {
+        Scratch S = p->S;
+        S.binError = nullptr;
+        int rc = reserve_bins(ctx, p->L, total, S);
+        if (!rc)
+            rc = enqueue_back(ctx, p->L, p->B, S, total, false, p->stream);
+        for (auto& r : p->reads)
+            if (!rc)
+            {
+                cudaError_t e =
+                    cudaMemcpyAsync(r.second, r.first->pixels,
+                                    (size_t)r.first->width * r.first->height * 4,
+                                    cudaMemcpyDeviceToHost, p->stream);
+                if (e != cudaSuccess)
+                    rc = cuda_fail(ctx, e, "read-back after a re-run");
+            }
+        p->reads.clear();
+        return rc;
+    }
+    p->reads.clear();
+    return RIVE_CUDA_OK;
+}
+
+int run_batch(rive_cuda_context* ctx,
+              const FlushInput* in,
+              uint32_t n,
+              cudaStream_t stream,
+              bool speculative = false)
 {
     if (n == 0)
         return RIVE_CUDA_OK;
+    {
+        const int rc = settle_pending(ctx);
+        if (rc)
+            return rc;
+    }
     BatchLayout L;
     int rc = plan_batch(ctx, in, n, L);
     if (!rc)
         rc = prepare_raster(ctx);
     if (rc)
         return rc;
-    // The previous batch's tables may still be in flight from the staging.
-    if (ctx->tablesCopied)
-        CK(cudaEventSynchronize(ctx->tablesCopied));
+    // The staging slot's last tables may still be in flight.
+    const int tslot = ctx->tableSlot;
+    ctx->tableSlot = (tslot + 1) % rive_cuda_context::kTableRing;
+    if (ctx->tablesCopied[tslot])
+        CK(cudaEventSynchronize(ctx->tablesCopied[tslot]));
     CK(ctx->tess.reserve(L.tessBytes()));
     CK(ctx->grad.reserve(L.gradBytes()));
-    CK(ctx->hTables.reserve(L.tableBytes));
+    CK(ctx->hTables[tslot].reserve(L.tableBytes));
     CK(ctx->dTables.reserve(L.tableBytes));
     CK(ctx->ranges.reserve((size_t)L.tiles * sizeof(uint2)));
     CK(ctx->tris.reserve((size_t)std::max(L.slots, 1u) * sizeof(TriRecord)));
@@ -1402,15 +1534,57 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
         S.qTempBytes = queueBytes;
         S.qCursor = (uint32_t*)ctx->queueCursor.ptr;
     }
-    BatchTables B = write_tables(ctx, in, L, S, (uint8_t*)ctx->hTables.ptr);
-    CK(cudaMemcpyAsync(S.tables, ctx->hTables.ptr, L.tableBytes, cudaMemcpyHostToDevice, stream));
-    if (!ctx->tablesCopied)
-        CK(cudaEventCreateWithFlags(&ctx->tablesCopied, cudaEventDisableTiming));
-    CK(cudaEventRecord(ctx->tablesCopied, stream));
+    BatchTables B = write_tables(ctx, in, L, S, (uint8_t*)ctx->hTables[tslot].ptr);
+    CK(cudaMemcpyAsync(S.tables, ctx->hTables[tslot].ptr, L.tableBytes, cudaMemcpyHostToDevice,
+                       stream));
+    if (!ctx->tablesCopied[tslot])
+        CK(cudaEventCreateWithFlags(&ctx->tablesCopied[tslot], cudaEventDisableTiming));
+    CK(cudaEventRecord(ctx->tablesCopied[tslot], stream));
 
     rc = enqueue_front(ctx, L, B, S, stream);
     if (rc)
         return rc;
+    // Speculative bins: a single flush on the context's stream, once a total
+    // has been seen, without winding records (their cell counts are read
+    // back too).
+    if (speculative && ctx->speculate && n == 1 && L.slots && !L.winding && ctx->binHighWater)
+    {
+        if (!ctx->pending)
+        {
+            ctx->pending = new (std::nothrow) PendingFlush();
+            if (!ctx->pending)
+                return RIVE_CUDA_ERR_OUT_OF_MEMORY;
+            CK(cudaEventCreateWithFlags(&ctx->pending->counted, cudaEventDisableTiming));
+        }
+        PendingFlush& p = *ctx->pending;
+        const uint64_t cap = (uint64_t)ctx->binHighWater + ctx->binHighWater / 4 + 4096;
+        p.capacity = (uint32_t)std::min<uint64_t>(cap, 0x7fffffffu);
+        rc = reserve_bins(ctx, L, p.capacity, S);
+        if (rc)
+            return rc;
+        S.binError = ctx->dSpecOverflow;
+        CK(cudaMemcpyAsync(ctx->hSpecTotal, S.offsets + L.slots, 4, cudaMemcpyDeviceToHost,
+                           stream));
+        CK(cudaEventRecord(p.counted, stream));
+        rc = enqueue_back(ctx, L, B, S, p.capacity, true, stream, true);
+        if (rc)
+            return rc;
+        p.L = L;
+        p.B = B;
+        p.S = S;
+        p.stream = stream;
+        p.reads.clear();
+        p.active = true;
+        ctx->stats.tess_vertices = (uint64_t)L.tessRows * kTessTextureWidth;
+        ctx->stats.patches = (uint64_t)L.items[0] + L.items[1] + L.items[3];
+        ctx->stats.triangles = L.slots;
+        ctx->stats.bin_entries = 0; // known when the flush settles
+        ctx->stats.winding_entries = 0;
+        ctx->stats.tiles = L.tiles;
+        ctx->stats.kernel_launches = 1 + (L.gradSpans ? 1 : 0) + (L.tessSpans ? 1 : 0) + 1 + 5 +
+                                     1 + (L.tiles > L.mainTiles ? 1 : 0);
+        return RIVE_CUDA_OK;
+    }
     uint32_t pairs = 0, windingEntries = 0;
     if (L.slots)
     {
@@ -1420,6 +1594,7 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
                                stream));
         CK(cudaStreamSynchronize(stream));
         pairs = *ctx->hPairs;
+        ctx->binHighWater = std::max(ctx->binHighWater, pairs);
         if (L.winding)
         {
             windingEntries = ctx->hGridCounters[1];
@@ -1430,17 +1605,9 @@ int run_batch(rive_cuda_context* ctx, const FlushInput* in, uint32_t n, cudaStre
     }
     if (pairs)
     {
-        CK(ctx->keys.reserve((size_t)pairs * 4));
-        CK(ctx->vals.reserve((size_t)pairs * 4));
-        CK(ctx->keysAlt.reserve((size_t)pairs * 4));
-        CK(ctx->valsAlt.reserve((size_t)pairs * 4));
-        S.sortTempBytes = sort_temp_bytes(pairs, L.endBit());
-        CK(ctx->sortTemp.reserve(S.sortTempBytes));
-        S.keys = (uint32_t*)ctx->keys.ptr;
-        S.vals = (uint32_t*)ctx->vals.ptr;
-        S.keysAlt = (uint32_t*)ctx->keysAlt.ptr;
-        S.valsAlt = (uint32_t*)ctx->valsAlt.ptr;
-        S.sortTemp = ctx->sortTemp.ptr;
+        rc = reserve_bins(ctx, L, pairs, S);
+        if (rc)
+            return rc;
     }
     rc = enqueue_back(ctx, L, B, S, pairs, false, stream);
     if (rc)
@@ -1462,10 +1629,11 @@ int run_flush(rive_cuda_context* ctx,
               const rive_cuda_flush_desc* d,
               const ResolvedBuffers& rb,
               uint32_t* fbDevice,
-              cudaStream_t stream)
+              cudaStream_t stream,
+              bool speculative = false)
 {
     FlushInput in{d, rb, fbDevice};
-    return run_batch(ctx, &in, 1, stream);
+    return run_batch(ctx, &in, 1, stream, speculative);
 }
 } // namespace
 
@@ -1484,6 +1652,8 @@ int rive_cuda_context_create(int device, rive_cuda_context** out_ctx)
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
         e = cudaMalloc(&ctx->dError, 4);
     if (e == cudaSuccess)
         e = cudaMemset(ctx->dError, 0, 4);
@@ -1493,6 +1663,10 @@ int rive_cuda_context_create(int device, rive_cuda_context** out_ctx)
         e = cudaMallocHost(&ctx->hPairs, 4);
     if (e == cudaSuccess)
         e = cudaMallocHost(&ctx->hGridCounters, 8);
+    if (e == cudaSuccess)
+        e = cudaMallocHost(&ctx->hSpecTotal, 4);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&ctx->dSpecOverflow, 4);
     if (e == cudaSuccess)
         e = ensure_feather_lut(device);
     if (e != cudaSuccess)
@@ -1510,8 +1684,21 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
     if (!ctx)
         return;
     cudaSetDevice(ctx->device);
+    settle_pending(ctx);
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
+    if (ctx->copyStream)
+        cudaStreamSynchronize(ctx->copyStream);
+    if (ctx->pending)
+    {
+        if (ctx->pending->counted)
+            cudaEventDestroy(ctx->pending->counted);
+        delete ctx->pending;
+    }
+    if (ctx->hSpecTotal)
+        cudaFreeHost(ctx->hSpecTotal);
+    if (ctx->dSpecOverflow)
+        cudaFree(ctx->dSpecOverflow);
     for (auto& r : ctx->rings)
     {
         for (int i = 0; i < kRingSize; ++i)
@@ -1521,7 +1708,14 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
             if (r.done[i])
                 cudaEventDestroy(r.done[i]);
         }
-        r.device.release();
+        for (int i = 0; i < 2; ++i)
+        {
+            r.device[i].release();
+            if (r.readDone[i])
+                cudaEventDestroy(r.readDone[i]);
+            if (r.copied[i])
+                cudaEventDestroy(r.copied[i]);
+        }
     }
     for (DeviceBuffer* b : {&ctx->tess, &ctx->grad, &ctx->tris, &ctx->tileCounts, &ctx->tileMasks,
                             &ctx->offsets, &ctx->featherPlanes,
@@ -1532,11 +1726,14 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
                             &ctx->queueKeysAlt, &ctx->queueValsAlt, &ctx->queueTemp,
                             &ctx->queueCursor, &ctx->atlas, &ctx->pathImage})
         b->release();
-    ctx->hTables.release();
+    for (int i = 0; i < rive_cuda_context::kTableRing; ++i)
+    {
+        ctx->hTables[i].release();
+        if (ctx->tablesCopied[i])
+            cudaEventDestroy(ctx->tablesCopied[i]);
+    }
     if (ctx->hGridCounters)
         cudaFreeHost(ctx->hGridCounters);
-    if (ctx->tablesCopied)
-        cudaEventDestroy(ctx->tablesCopied);
     if (ctx->dError)
         cudaFree(ctx->dError);
     if (ctx->hError)
@@ -1553,6 +1750,8 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         cudaEventDestroy(e);
     if (ctx->stream)
         cudaStreamDestroy(ctx->stream);
+    if (ctx->copyStream)
+        cudaStreamDestroy(ctx->copyStream);
     delete ctx;
 }
 
@@ -1568,11 +1767,17 @@ int rive_cuda_resize_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
 {
     if (!ctx || kind < 0 || kind >= RIVE_CUDA_BUFFER_KIND_COUNT)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "bad buffer kind %d", kind);
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     RecordRing& r = ctx->rings[kind];
     if (r.mapped)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "resize while mapped");
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamSynchronize(ctx->copyStream));
     for (int i = 0; i < kRingSize; ++i)
     {
         if (r.host[i])
@@ -1580,8 +1785,17 @@ int rive_cuda_resize_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
         r.host[i] = nullptr;
     }
     r.capacity = 0;
-    r.device.release();
-    r.deviceValidBytes = 0;
+    for (int i = 0; i < 2; ++i)
+    {
+        r.device[i].release();
+        r.deviceValidBytes[i] = 0;
+        if (!r.readDone[i])
+            CK(cudaEventCreateWithFlags(&r.readDone[i], cudaEventDisableTiming));
+        if (!r.copied[i])
+            CK(cudaEventCreateWithFlags(&r.copied[i], cudaEventDisableTiming));
+    }
+    r.slot = 0;
+    r.used = false;
     if (bytes == 0)
         return RIVE_CUDA_OK;
     for (int i = 0; i < kRingSize; ++i)
@@ -1593,8 +1807,9 @@ int rive_cuda_resize_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
         if (!r.done[i])
             CK(cudaEventCreateWithFlags(&r.done[i], cudaEventDisableTiming));
     }
-    if (r.device.reserve(bytes) != cudaSuccess)
-        return set_error(ctx, RIVE_CUDA_ERR_OUT_OF_MEMORY, "device alloc of %zu bytes", bytes);
+    for (int i = 0; i < 2; ++i)
+        if (r.device[i].reserve(bytes) != cudaSuccess)
+            return set_error(ctx, RIVE_CUDA_ERR_OUT_OF_MEMORY, "device alloc of %zu bytes", bytes);
     r.capacity = bytes;
     return RIVE_CUDA_OK;
 }
@@ -1632,11 +1847,20 @@ int rive_cuda_unmap_buffer(rive_cuda_context* ctx, int kind, size_t bytes)
     if (bytes > r.capacity)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "unmap size too large");
     CK(cudaSetDevice(ctx->device));
+    if (r.used)
+    {
+        // The current copy feeds flushes in flight: fill the other one once
+        // the flushes that read it last are done.
+        r.slot ^= 1;
+        r.used = false;
+        CK(cudaStreamWaitEvent(ctx->copyStream, r.readDone[r.slot], 0));
+    }
     if (bytes)
-        CK(cudaMemcpyAsync(r.device.ptr, r.host[r.current], bytes, cudaMemcpyHostToDevice,
-                           ctx->stream));
-    CK(cudaEventRecord(r.done[r.current], ctx->stream));
-    r.deviceValidBytes = bytes;
+        CK(cudaMemcpyAsync(r.device[r.slot].ptr, r.host[r.current], bytes, cudaMemcpyHostToDevice,
+                           ctx->copyStream));
+    CK(cudaEventRecord(r.done[r.current], ctx->copyStream));
+    CK(cudaEventRecord(r.copied[r.slot], ctx->copyStream));
+    r.deviceValidBytes[r.slot] = bytes;
     return RIVE_CUDA_OK;
 }
 
@@ -1700,6 +1924,9 @@ int rive_cuda_render_target_create(rive_cuda_context* ctx,
 
 void rive_cuda_render_target_destroy(rive_cuda_context* ctx, rive_cuda_render_target* t)
 {
+    // A pending flush that may run again could still read it.
+    if (ctx)
+        settle_pending(ctx);
     if (!t)
         return;
     if (ctx)
@@ -1723,6 +1950,11 @@ int rive_cuda_render_target_read(rive_cuda_context* ctx,
 {
     if (!ctx || !t || !dst)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "bad read-back arguments");
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4, cudaMemcpyDeviceToHost, s));
@@ -1738,8 +1970,20 @@ int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
     if (!ctx || !t || !dst)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "bad read-back arguments");
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+    // Behind a pending speculative flush on the same stream the copy is
+    // enqueued at once and repeated should that flush run again; on another
+    // stream the flush is settled first.
+    const bool behindPending = ctx->pending && ctx->pending->active && ctx->pending->stream == s;
+    if (!behindPending)
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4, cudaMemcpyDeviceToHost, s));
+    if (behindPending)
+        ctx->pending->reads.emplace_back(t, dst);
     return RIVE_CUDA_OK;
 }
 
@@ -1756,7 +2000,8 @@ int rive_cuda_flush(rive_cuda_context* ctx,
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     if (s != ctx->stream)
     {
-        // Uploads were enqueued on the context stream; order them first.
+        // Work already queued on the context stream (texture and render
+        // buffer uploads, earlier flushes) comes first.
         cudaEvent_t ev;
         CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         CK(cudaEventRecord(ev, ctx->stream));
@@ -1766,10 +2011,24 @@ int rive_cuda_flush(rive_cuda_context* ctx,
     ResolvedBuffers rb;
     for (int k = 0; k < kResolvedKinds; ++k)
     {
-        rb.ptr[k] = ctx->rings[k].device.ptr;
-        rb.bytes[k] = ctx->rings[k].deviceValidBytes;
+        RecordRing& r = ctx->rings[k];
+        rb.ptr[k] = r.device[r.slot].ptr;
+        rb.bytes[k] = r.deviceValidBytes[r.slot];
+        if (r.copied[r.slot])
+            CK(cudaStreamWaitEvent(s, r.copied[r.slot], 0));
     }
-    return run_flush(ctx, desc, rb, target->pixels, s);
+    const int rc = run_flush(ctx, desc, rb, target->pixels, s, s == ctx->stream);
+    // The next upload of each kind goes to its other copy, after this flush.
+    for (int k = 0; k < kResolvedKinds; ++k)
+    {
+        RecordRing& r = ctx->rings[k];
+        if (r.readDone[r.slot])
+        {
+            CK(cudaEventRecord(r.readDone[r.slot], s));
+            r.used = true;
+        }
+    }
+    return rc;
 }
 
 int rive_cuda_flush_device(rive_cuda_context* ctx,
@@ -1986,6 +2245,11 @@ int rive_cuda_graph_create(rive_cuda_context* ctx,
     if (!ctx || !out || !count || !flushes)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "NULL argument to graph_create");
     *out = nullptr;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     std::vector<FlushInput> in(count);
     for (uint32_t i = 0; i < count; ++i)
     {
@@ -2088,6 +2352,11 @@ int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(ctx->hError, ctx->dError, 4, cudaMemcpyDeviceToHost, s));
@@ -2109,6 +2378,11 @@ int rive_cuda_read_tess_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
 {
     if (!ctx || !dst)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->tess.ptr, std::min(bytes, ctx->lastTessBytes), cudaMemcpyDeviceToHost));
@@ -2125,6 +2399,11 @@ int rive_cuda_texture_create(rive_cuda_context* ctx,
     if (!ctx || !rgba_host || !out_texture || width == 0 || height == 0 || width > 16384 ||
         height > 16384 || mip_levels == 0)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     *out_texture = nullptr;
     uint32_t full = 0;
     for (uint32_t m = width | height; m; m >>= 1)
@@ -2179,6 +2458,9 @@ int rive_cuda_texture_create(rive_cuda_context* ctx,
 
 void rive_cuda_texture_destroy(rive_cuda_context* ctx, rive_cuda_texture* texture)
 {
+    // A pending flush that may run again could still read it.
+    if (ctx)
+        settle_pending(ctx);
     if (!texture)
         return;
     if (ctx)
@@ -2229,6 +2511,11 @@ int rive_cuda_render_buffer_write(rive_cuda_context* ctx,
     if (!ctx || !buffer || (!src_host && bytes) || offset > buffer->bytes ||
         bytes > buffer->bytes - offset)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     if (!bytes)
         return RIVE_CUDA_OK;
     CK(cudaSetDevice(ctx->device));
@@ -2241,6 +2528,9 @@ int rive_cuda_render_buffer_write(rive_cuda_context* ctx,
 
 void rive_cuda_render_buffer_destroy(rive_cuda_context* ctx, rive_cuda_render_buffer* buffer)
 {
+    // A pending flush that may run again could still read it.
+    if (ctx)
+        settle_pending(ctx);
     if (!buffer)
         return;
     if (ctx)
@@ -2274,6 +2564,11 @@ int rive_cuda_read_atlas_texture(rive_cuda_context* ctx, void* dst, size_t bytes
 {
     if (!ctx || !dst)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     const size_t n = std::min(bytes, ctx->lastAtlasBytes);
@@ -2286,6 +2581,11 @@ int rive_cuda_read_grad_texture(rive_cuda_context* ctx, void* dst, size_t bytes)
 {
     if (!ctx || !dst)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpy(dst, ctx->grad.ptr, std::min(bytes, ctx->lastGradBytes), cudaMemcpyDeviceToHost));
@@ -2315,6 +2615,11 @@ int rive_cuda_set_raster_config(rive_cuda_context* ctx, int tile_size, int ctas_
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     const int log2 = tile_size == 8 ? 3 : tile_size == 16 ? 4 : tile_size == 32 ? 5 : -1;
     if (log2 < 0)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "tile size %d (8, 16 or 32)",
@@ -2346,6 +2651,11 @@ int rive_cuda_set_raster_queue(rive_cuda_context* ctx, int enabled)
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     ctx->rasterQueue = enabled != 0;
     return RIVE_CUDA_OK;
 }
@@ -2362,7 +2672,33 @@ int rive_cuda_set_winding_tiles(rive_cuda_context* ctx, int enabled)
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     ctx->windingTiles = enabled != 0;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_set_bin_speculation(rive_cuda_context* ctx, int enabled)
+{
+    if (!ctx)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
+    ctx->speculate = enabled != 0;
+    return RIVE_CUDA_OK;
+}
+
+int rive_cuda_get_bin_speculation(const rive_cuda_context* ctx, int* enabled)
+{
+    if (!ctx || !enabled)
+        return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    *enabled = ctx->speculate ? 1 : 0;
     return RIVE_CUDA_OK;
 }
 
@@ -2378,6 +2714,11 @@ int rive_cuda_set_profiling(rive_cuda_context* ctx, int enabled)
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     ctx->profiling = enabled != 0;
     return RIVE_CUDA_OK;
 }
@@ -2388,6 +2729,11 @@ int rive_cuda_profile_collect(rive_cuda_context* ctx,
 {
     if (!ctx)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     CK(cudaSetDevice(ctx->device));
     for (int st = 0; st < RIVE_CUDA_STAGE_COUNT; ++st)
     {
@@ -2410,8 +2756,16 @@ int rive_cuda_profile_collect(rive_cuda_context* ctx,
     return RIVE_CUDA_OK;
 }
 
-int rive_cuda_last_flush_stats(const rive_cuda_context* ctx, rive_cuda_flush_stats* out)
+int rive_cuda_last_flush_stats(const rive_cuda_context* cctx, rive_cuda_flush_stats* out)
 {
+    // The bin-entry total of a pending speculative flush is read here.
+    rive_cuda_context* ctx = const_cast<rive_cuda_context*>(cctx);
+    if (ctx)
+    {
+        const int src = settle_pending(ctx);
+        if (src)
+            return src;
+    }
     if (!ctx || !out)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
     *out = ctx->stats;

@@ -2053,6 +2053,21 @@ __global__ void __launch_bounds__(256) bin_scatter_winding_kernel(BatchTables B,
                       offsets, capacity, error, keys, vals);
 }
 
+// A speculative pass whose scanned bin-entry total exceeds the capacity its
+// bins were sized for has incomplete bins: every tile's range is emptied, so
+// the raster leaves a loaded target as it was (a cleared one is cleared),
+// until the back half runs again with exact bins.
+__global__ void __launch_bounds__(256) ranges_guard_kernel(const uint32_t* __restrict__ pairTotal,
+                                                           uint32_t capacity,
+                                                           uint2* __restrict__ ranges,
+                                                           uint32_t tiles)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= tiles || *pairTotal <= capacity)
+        return;
+    ranges[i] = make_uint2(0u, 0u);
+}
+
 __global__ void __launch_bounds__(256) tile_ranges_kernel(uint32_t pairCount,
                                                           uint32_t tileCount,
                                                           const uint32_t* __restrict__ keys,

@@ -143,6 +143,8 @@ def load():
         "rive_cuda_set_raster_config": (i32, [vp, i32, i32]),
         "rive_cuda_set_winding_tiles": (i32, [vp, i32]),
         "rive_cuda_set_raster_queue": (i32, [vp, i32]),
+        "rive_cuda_set_bin_speculation": (i32, [vp, i32]),
+        "rive_cuda_get_bin_speculation": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_get_raster_queue": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
         "rive_cuda_eval_tessellation_math": (i32, [i32, vp, vp, sz]),
         "rive_cuda_get_winding_tiles": (i32, [vp, ctypes.POINTER(ctypes.c_int)]),
@@ -396,6 +398,13 @@ class Context:
     def desc_for(self, flush):
         """make_desc with this context's textures and render buffers."""
         return make_desc(flush, self.textures_for(flush), self.buffers_for(flush))
+
+    def set_bin_speculation(self, enabled: bool):
+        """rive_cuda_set_bin_speculation: flushes on the context's stream size
+        their bins from the largest total seen instead of waiting for the
+        scan (checked, and re-run exactly when short, at the next call)."""
+        self.check(self.lib.rive_cuda_set_bin_speculation(self.h, int(bool(enabled))),
+                   "set_bin_speculation")
 
     def read_texture(self, handle, level, width, height):
         """Mip level `level` (width x height texels) of a device texture."""
