@@ -2828,6 +2828,11 @@ __device__ __noinline__ float feathered_fragment(const float4* __restrict__ plan
 #ifndef RIVE_RASTER_MIN_BLOCKS
 #define RIVE_RASTER_MIN_BLOCKS 5
 #endif
+// Prefetch of the next chunk's records into L2 while a chunk is walked (off:
+// measured slower, the staging's loads are not what the barrier waits for).
+#ifndef RIVE_RASTER_PREFETCH
+#define RIVE_RASTER_PREFETCH 0
+#endif
 // Bin entries each thread stages per chunk (8x8 and 16x16 tiles): a chunk of
 // kStage x threads entries between two CTA barriers.
 #ifndef RIVE_RASTER_STAGE
@@ -2965,6 +2970,21 @@ __device__ __forceinline__ void raster_tile(const BatchTables& B,
         sMask[si] = (typename G::Mask)m;
         }
         __syncthreads();
+#if RIVE_RASTER_PREFETCH
+        // The next chunk's records are pulled into L2 while this one is
+        // walked, so the staging after the next barrier does not wait on DRAM.
+        if (kStage == 1)
+        {
+            const uint32_t kn = base + kChunk + threadIdx.x;
+            if (kn < range.y)
+            {
+                const uint32_t en = __ldg(sortedSlots + kn) & ~BIN_WINDING_ENTRY;
+                const char* a = reinterpret_cast<const char*>(tris + en);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(a + sizeof(TriRecord) - 1));
+            }
+        }
+#endif
         const uint32_t n = min(kChunk, range.y - base);
         for (uint32_t g = 0; g < n; g += 32)
         {
