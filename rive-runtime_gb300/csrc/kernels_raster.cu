@@ -1335,7 +1335,12 @@ __device__ __forceinline__ void patch_setup(const BatchTables& B,
     }
 }
 
-__global__ void __launch_bounds__(128) patch_setup_kernel(BatchTables B,
+// Resident 128-thread CTAs per SM the midpoint-fan set-up's registers are
+// bounded for.
+#ifndef RIVE_SETUP_MIN_BLOCKS
+#define RIVE_SETUP_MIN_BLOCKS 9
+#endif
+__global__ void __launch_bounds__(128, RIVE_SETUP_MIN_BLOCKS) patch_setup_kernel(BatchTables B,
                                                           TriRecord* __restrict__ tris,
                                                           uint32_t* __restrict__ tileCounts,
                                                           uint8_t* __restrict__ tileMasks)
