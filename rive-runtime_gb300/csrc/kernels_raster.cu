@@ -2026,7 +2026,13 @@ __device__ __forceinline__ void bin_scatter(const BatchTables* __restrict__ Bw,
     }
 }
 
-__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t slotCount,
+// Resident 256-thread CTAs per SM the binner's registers are bounded for: 6
+// (no spills) bins the full-feature frame in 0.98 ms against 1.10 ms at the
+// compiler's 45 registers (5 CTAs).
+#ifndef RIVE_BIN_MIN_BLOCKS
+#define RIVE_BIN_MIN_BLOCKS 6
+#endif
+__global__ void __launch_bounds__(256, RIVE_BIN_MIN_BLOCKS) bin_scatter_kernel(uint32_t slotCount,
                                                           int tileLog2,
                                                           const uint2* __restrict__ sceneTiles,
                                                           const TriRecord* __restrict__ tris,
