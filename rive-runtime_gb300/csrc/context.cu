@@ -76,6 +76,26 @@ __global__ void tile_ranges_kernel(uint32_t pairCount,
                                    uint32_t tileCount,
                                    const uint32_t* keys,
                                    uint2* ranges);
+// The same three with 16-bit tile keys (batches of at most 65,535 tiles).
+__global__ void bin_fill16_kernel(const uint32_t* pairTotal,
+                                  uint32_t capacity,
+                                  uint32_t sentinel,
+                                  uint16_t* keys);
+__global__ void bin_scatter16_kernel(uint32_t slotCount,
+                                     int tileLog2,
+                                     const uint2* sceneTiles,
+                                     const TriRecord* tris,
+                                     const uint32_t* tileCounts,
+                                     const uint8_t* tileMasks,
+                                     const uint32_t* offsets,
+                                     uint32_t capacity,
+                                     uint32_t* error,
+                                     uint16_t* keys,
+                                     uint32_t* vals);
+__global__ void tile_ranges16_kernel(uint32_t pairCount,
+                                     uint32_t tileCount,
+                                     const uint16_t* keys,
+                                     uint2* ranges);
 __global__ void ranges_guard_kernel(const uint32_t* pairTotal,
                                     uint32_t capacity,
                                     uint2* ranges,
@@ -661,6 +681,9 @@ struct BatchLayout
            oPathBase = 0, oSegments[kSetupLists] = {}, oSegBase[kSetupLists] = {}, tableBytes = 0;
     size_t tessBytes() const { return (size_t)kTessTextureWidth * tessRows * 16; }
     size_t gradBytes() const { return (size_t)kGradTextureWidth * gradRows * 4; }
+    // Bin keys fit 16 bits (the sentinel key `tiles` included) without
+    // winding entries, whose binner writes 32-bit keys.
+    bool keys16() const { return tiles <= 0xffffu && !winding; }
     int endBit() const
     {
         int b = 1;
@@ -813,7 +836,10 @@ struct Scratch
     uint32_t* counts = nullptr;
     uint8_t* masks = nullptr;    // per slot: tiles overlapped, for boxes of <= 8 tiles
     uint32_t* offsets = nullptr; // slots + 1 entries
-    uint32_t *keys = nullptr, *vals = nullptr, *keysAlt = nullptr, *valsAlt = nullptr;
+    // Bin keys: tile indices, 16-bit when keys16 (set by reserve_bins).
+    void *keys = nullptr, *keysAlt = nullptr;
+    uint32_t *vals = nullptr, *valsAlt = nullptr;
+    bool keys16 = false;
     void* scanTemp = nullptr;
     size_t scanTempBytes = 0;
     void* sortTemp = nullptr;
@@ -1278,25 +1304,51 @@ int enqueue_back(rive_cuda_context* ctx,
     if (entries && L.slots)
     {
         stage_begin(ctx, RIVE_CUDA_STAGE_BIN, stream);
-        if (padded)
-            bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(S.offsets + L.slots, entries,
-                                                                      L.tiles, S.keys);
-        if (L.winding)
-            bin_scatter_winding_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
-                B, S.tris, S.counts, S.masks, S.offsets, L.slots, entries, binError, S.keys, S.vals);
-        else
-            bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+        if (S.keys16)
+        {
+            uint16_t* keys = (uint16_t*)S.keys;
+            if (padded)
+                bin_fill16_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(
+                    S.offsets + L.slots, entries, L.tiles, keys);
+            bin_scatter16_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
                 L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries,
-                binError, S.keys, S.vals);
+                binError, keys, S.vals);
+        }
+        else
+        {
+            uint32_t* keys = (uint32_t*)S.keys;
+            if (padded)
+                bin_fill_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(
+                    S.offsets + L.slots, entries, L.tiles, keys);
+            if (L.winding)
+                bin_scatter_winding_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+                    B, S.tris, S.counts, S.masks, S.offsets, L.slots, entries, binError, keys,
+                    S.vals);
+            else
+                bin_scatter_kernel<<<(L.slots + 255) / 256, 256, 0, stream>>>(
+                    L.slots, L.tileLog2, B.sceneTiles, S.tris, S.counts, S.masks, S.offsets, entries,
+                    binError, keys, S.vals);
+        }
         stage_end(ctx, stream);
-        cub::DoubleBuffer<uint32_t> k(S.keys, S.keysAlt);
         cub::DoubleBuffer<uint32_t> v(S.vals, S.valsAlt);
         size_t tempBytes = S.sortTempBytes;
         stage_begin(ctx, RIVE_CUDA_STAGE_SORT, stream);
-        CK(cub::DeviceRadixSort::SortPairs(S.sortTemp, tempBytes, k, v, (int)entries, 0,
-                                           L.endBit(), stream));
-        tile_ranges_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(entries, L.tiles, k.Current(),
-                                                                    S.ranges);
+        if (S.keys16)
+        {
+            cub::DoubleBuffer<uint16_t> k((uint16_t*)S.keys, (uint16_t*)S.keysAlt);
+            CK(cub::DeviceRadixSort::SortPairs(S.sortTemp, tempBytes, k, v, (int)entries, 0,
+                                               L.endBit(), stream));
+            tile_ranges16_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(entries, L.tiles,
+                                                                          k.Current(), S.ranges);
+        }
+        else
+        {
+            cub::DoubleBuffer<uint32_t> k((uint32_t*)S.keys, (uint32_t*)S.keysAlt);
+            CK(cub::DeviceRadixSort::SortPairs(S.sortTemp, tempBytes, k, v, (int)entries, 0,
+                                               L.endBit(), stream));
+            tile_ranges_kernel<<<(entries + 255) / 256, 256, 0, stream>>>(entries, L.tiles,
+                                                                        k.Current(), S.ranges);
+        }
         // A speculative pass whose total did not fit: every range emptied,
         // so the raster leaves the target as it was (or clears it) until the
         // back half runs again with exact bins.
@@ -1347,11 +1399,20 @@ size_t queue_temp_bytes(uint32_t tiles)
     return b;
 }
 
-size_t sort_temp_bytes(uint32_t entries, int endBit)
+size_t sort_temp_bytes(uint32_t entries, int endBit, bool keys16 = false)
 {
     size_t b = 0;
-    cub::DoubleBuffer<uint32_t> k(nullptr, nullptr), v(nullptr, nullptr);
-    cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, (int)std::max(entries, 1u), 0, endBit);
+    cub::DoubleBuffer<uint32_t> v(nullptr, nullptr);
+    if (keys16)
+    {
+        cub::DoubleBuffer<uint16_t> k(nullptr, nullptr);
+        cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, (int)std::max(entries, 1u), 0, endBit);
+    }
+    else
+    {
+        cub::DoubleBuffer<uint32_t> k(nullptr, nullptr);
+        cub::DeviceRadixSort::SortPairs(nullptr, b, k, v, (int)std::max(entries, 1u), 0, endBit);
+    }
     return b;
 }
 
@@ -1377,15 +1438,17 @@ struct PendingFlush
 // entries and points S at them.
 int reserve_bins(rive_cuda_context* ctx, const BatchLayout& L, uint32_t entries, Scratch& S)
 {
-    CK(ctx->keys.reserve((size_t)entries * 4));
+    S.keys16 = L.keys16();
+    const size_t keyBytes = S.keys16 ? 2 : 4;
+    CK(ctx->keys.reserve((size_t)entries * keyBytes));
     CK(ctx->vals.reserve((size_t)entries * 4));
-    CK(ctx->keysAlt.reserve((size_t)entries * 4));
+    CK(ctx->keysAlt.reserve((size_t)entries * keyBytes));
     CK(ctx->valsAlt.reserve((size_t)entries * 4));
-    S.sortTempBytes = sort_temp_bytes(entries, L.endBit());
+    S.sortTempBytes = sort_temp_bytes(entries, L.endBit(), S.keys16);
     CK(ctx->sortTemp.reserve(S.sortTempBytes));
-    S.keys = (uint32_t*)ctx->keys.ptr;
+    S.keys = ctx->keys.ptr;
     S.vals = (uint32_t*)ctx->vals.ptr;
-    S.keysAlt = (uint32_t*)ctx->keysAlt.ptr;
+    S.keysAlt = ctx->keysAlt.ptr;
     S.valsAlt = (uint32_t*)ctx->valsAlt.ptr;
     S.sortTemp = ctx->sortTemp.ptr;
     return RIVE_CUDA_OK;
