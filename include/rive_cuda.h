@@ -308,7 +308,8 @@ int rive_cuda_render_target_create(rive_cuda_context* ctx,
                                    rive_cuda_render_target** out_target);
 void rive_cuda_render_target_destroy(rive_cuda_context* ctx,
                                      rive_cuda_render_target* target);
-/* Device address of the target's pixels (for zero-copy consumers). */
+/* Device address of the target's pixels (for zero-copy consumers, after
+ * rive_cuda_sync). */
 void* rive_cuda_render_target_device_ptr(rive_cuda_render_target* target);
 /* Copies the target's pixels to host memory (width*height*4 bytes). */
 int rive_cuda_render_target_read(rive_cuda_context* ctx,
@@ -579,7 +580,10 @@ int rive_cuda_get_winding_tiles(const rive_cuda_context* ctx, int* enabled);
  * total is checked at the next call into the context; when it did not fit,
  * the flush's back half runs again with exact bins before anything else, and
  * read-backs enqueued after it are repeated. The image is the same either
- * way. Flushes on a caller's stream and batches always size bins exactly.
+ * way. A caller that reads a target's device memory itself
+ * (rive_cuda_render_target_device_ptr) calls rive_cuda_sync first, which
+ * settles it. Flushes on a caller's stream and batches always size bins
+ * exactly.
  */
 int rive_cuda_set_bin_speculation(rive_cuda_context* ctx, int enabled);
 int rive_cuda_get_bin_speculation(const rive_cuda_context* ctx, int* enabled);
