@@ -274,6 +274,10 @@ struct rive_cuda_render_target
 {
     uint32_t width = 0, height = 0;
     uint32_t* pixels = nullptr;
+    // An asynchronous read-back on the context's read stream that the next
+    // raster into this target waits for (readPending until a flush took it).
+    cudaEvent_t readDone = nullptr;
+    bool readPending = false;
 };
 
 struct rive_cuda_context
@@ -281,6 +285,10 @@ struct rive_cuda_context
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copyStream = nullptr; // record uploads (rive_cuda_unmap_buffer)
+    cudaStream_t readStream = nullptr; // asynchronous read-backs of targets
+    // Set by rive_cuda_flush for one flush: the raster waits for it (a
+    // read-back of the target still in flight), the front half does not.
+    cudaEvent_t rasterWait = nullptr;
     std::string lastError;
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
@@ -1374,6 +1382,8 @@ int enqueue_back(rive_cuda_context* ctx,
             raster_atlas_kernel<<<atlasTiles, 256, 0, stream>>>(B, S.tris, sortedSlots, S.ranges,
                                                                 L.mainTiles);
     }
+    if (ctx->rasterWait)
+        CK(cudaStreamWaitEvent(stream, ctx->rasterWait, 0));
     int rc = launch_raster(ctx, L, B, S, S.tris, sortedSlots, S.ranges, stream);
     stage_end(ctx, stream);
     if (rc)
@@ -1472,6 +1482,13 @@ int settle_pending(rive_cuda_context* ctx)
     ctx->stats.bin_entries = total;
     if (total > p->capacity)
     {
+        // Read-backs already on the read stream finish first: the re-run
+        // rewrites their target, and its own read-backs land after them.
+        cudaEvent_t readsDone = nullptr;
+        CK(cudaEventCreateWithFlags(&readsDone, cudaEventDisableTiming));
+        CK(cudaEventRecord(readsDone, ctx->readStream));
+        CK(cudaStreamWaitEvent(p->stream, readsDone, 0));
+        CK(cudaEventDestroy(readsDone));
         Scratch S = p->S;
         S.binError = nullptr;
         int rc = reserve_bins(ctx, p->L, total, S);
@@ -1717,6 +1734,8 @@ int rive_cuda_context_create(int device, rive_cuda_context** out_ctx)
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&ctx->copyStream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&ctx->readStream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
         e = cudaMalloc(&ctx->dError, 4);
     if (e == cudaSuccess)
         e = cudaMemset(ctx->dError, 0, 4);
@@ -1752,6 +1771,8 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         cudaStreamSynchronize(ctx->stream);
     if (ctx->copyStream)
         cudaStreamSynchronize(ctx->copyStream);
+    if (ctx->readStream)
+        cudaStreamSynchronize(ctx->readStream);
     if (ctx->pending)
     {
         if (ctx->pending->counted)
@@ -1815,6 +1836,8 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         cudaStreamDestroy(ctx->stream);
     if (ctx->copyStream)
         cudaStreamDestroy(ctx->copyStream);
+    if (ctx->readStream)
+        cudaStreamDestroy(ctx->readStream);
     delete ctx;
 }
 
@@ -1996,7 +2019,10 @@ void rive_cuda_render_target_destroy(rive_cuda_context* ctx, rive_cuda_render_ta
     {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
+        cudaStreamSynchronize(ctx->readStream);
     }
+    if (t->readDone)
+        cudaEventDestroy(t->readDone);
     cudaFree(t->pixels);
     delete t;
 }
@@ -2044,7 +2070,25 @@ int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
             return src;
     }
     CK(cudaSetDevice(ctx->device));
-    CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4, cudaMemcpyDeviceToHost, s));
+    if (s == ctx->stream)
+    {
+        // On the read stream, after the flushes queued so far: the context's
+        // stream goes on with the next flush's front half meanwhile, and only
+        // the next raster into this target waits for the copy.
+        if (!t->readDone)
+            CK(cudaEventCreateWithFlags(&t->readDone, cudaEventDisableTiming));
+        CK(cudaEventRecord(t->readDone, s));
+        CK(cudaStreamWaitEvent(ctx->readStream, t->readDone, 0));
+        CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4,
+                           cudaMemcpyDeviceToHost, ctx->readStream));
+        CK(cudaEventRecord(t->readDone, ctx->readStream));
+        t->readPending = true;
+    }
+    else
+    {
+        CK(cudaMemcpyAsync(dst, t->pixels, (size_t)t->width * t->height * 4,
+                           cudaMemcpyDeviceToHost, s));
+    }
     if (behindPending)
         ctx->pending->reads.emplace_back(t, dst);
     return RIVE_CUDA_OK;
@@ -2080,7 +2124,11 @@ int rive_cuda_flush(rive_cuda_context* ctx,
         if (r.copied[r.slot])
             CK(cudaStreamWaitEvent(s, r.copied[r.slot], 0));
     }
+    // A read-back of this target still in flight: the raster waits for it.
+    ctx->rasterWait = target->readPending ? target->readDone : nullptr;
+    target->readPending = false;
     const int rc = run_flush(ctx, desc, rb, target->pixels, s, s == ctx->stream);
+    ctx->rasterWait = nullptr;
     // The next upload of each kind goes to its other copy, after this flush.
     for (int k = 0; k < kResolvedKinds; ++k)
     {
@@ -2424,6 +2472,8 @@ int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemcpyAsync(ctx->hError, ctx->dError, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (s == ctx->stream)
+        CK(cudaStreamSynchronize(ctx->readStream)); // its asynchronous read-backs
     uint32_t err = *ctx->hError;
     if (err)
     {
