@@ -317,13 +317,15 @@ int rive_cuda_render_target_read(rive_cuda_context* ctx,
                                   void* dst_host,
                                   void* cuda_stream);
 /*
- * The same copy, enqueued on the stream (the context's when NULL) after the
- * flushes already there, without waiting for it: a caller that pipelines
+ * The same copy, enqueued after the flushes already on the stream (the
+ * context's when NULL), without waiting for it: a caller that pipelines
  * frames writes frame k+1's records into the mapped rings while frame k
  * renders and reads back. dst_host should be page-locked for the copy to run
  * asynchronously, and must stay valid until rive_cuda_sync on that stream
- * returns. Later flushes on the same stream may overwrite the target only
- * after this copy, in stream order.
+ * returns. Later flushes overwrite the target only after this copy. With the
+ * context's stream the copy runs on a read stream of its own, so the next
+ * flush's front half overlaps it and only its raster into this target
+ * waits; flushes into caller-given device memory wait for it too.
  */
 int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
                                         rive_cuda_render_target* target,

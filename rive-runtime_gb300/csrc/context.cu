@@ -286,6 +286,7 @@ struct rive_cuda_context
     cudaStream_t stream = nullptr;
     cudaStream_t copyStream = nullptr; // record uploads (rive_cuda_unmap_buffer)
     cudaStream_t readStream = nullptr; // asynchronous read-backs of targets
+    bool readsInFlight = false;        // read-backs queued since the last sync
     // Set by rive_cuda_flush for one flush: the raster waits for it (a
     // read-back of the target still in flight), the front half does not.
     cudaEvent_t rasterWait = nullptr;
@@ -1705,6 +1706,20 @@ int run_batch(rive_cuda_context* ctx,
     return RIVE_CUDA_OK;
 }
 
+// Flushes into caller-given device memory cannot tell a target with a
+// read-back in flight: while any is, their stream waits for the read stream.
+int order_after_reads(rive_cuda_context* ctx, cudaStream_t s)
+{
+    if (!ctx->readsInFlight)
+        return RIVE_CUDA_OK;
+    cudaEvent_t ev = nullptr;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, ctx->readStream));
+    CK(cudaStreamWaitEvent(s, ev, 0));
+    CK(cudaEventDestroy(ev));
+    return RIVE_CUDA_OK;
+}
+
 int run_flush(rive_cuda_context* ctx,
               const rive_cuda_flush_desc* d,
               const ResolvedBuffers& rb,
@@ -2083,6 +2098,7 @@ int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
                            cudaMemcpyDeviceToHost, ctx->readStream));
         CK(cudaEventRecord(t->readDone, ctx->readStream));
         t->readPending = true;
+        ctx->readsInFlight = true;
     }
     else
     {
@@ -2153,6 +2169,8 @@ int rive_cuda_flush_device(rive_cuda_context* ctx,
     CK(cudaSetDevice(ctx->device));
     const ResolvedBuffers rb = resolve_device_buffers(*buffers);
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+    if (const int rc = order_after_reads(ctx, s))
+        return rc;
     return run_flush(ctx, desc, rb, (uint32_t*)target_pixels_device, s);
 }
 
@@ -2393,7 +2411,10 @@ int rive_cuda_graph_launch(rive_cuda_graph* g, void* cuda_stream)
         return RIVE_CUDA_ERR_INVALID_ARGUMENT;
     rive_cuda_context* ctx = g->ctx;
     CK(cudaSetDevice(ctx->device));
-    CK(cudaGraphLaunch(g->exec, cuda_stream ? (cudaStream_t)cuda_stream : g->stream));
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : g->stream;
+    if (const int rc = order_after_reads(ctx, s))
+        return rc;
+    CK(cudaGraphLaunch(g->exec, s));
     return RIVE_CUDA_OK;
 }
 
@@ -2456,6 +2477,8 @@ int rive_cuda_flush_batch(rive_cuda_context* ctx,
     }
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
+    if (const int rc = order_after_reads(ctx, s))
+        return rc;
     return run_batch(ctx, in.data(), count, s);
 }
 
@@ -2473,7 +2496,10 @@ int rive_cuda_sync(rive_cuda_context* ctx, void* cuda_stream)
     CK(cudaMemcpyAsync(ctx->hError, ctx->dError, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (s == ctx->stream)
+    {
         CK(cudaStreamSynchronize(ctx->readStream)); // its asynchronous read-backs
+        ctx->readsInFlight = false;
+    }
     uint32_t err = *ctx->hError;
     if (err)
     {
