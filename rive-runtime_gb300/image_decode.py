@@ -26,10 +26,17 @@ class DecodeError(ValueError):
 
 
 def decode(data: bytes) -> np.ndarray:
-    if data[:8] == b"\x89PNG\r\n\x1a\n":
-        return decode_png(data)
-    if data[:2] == b"\xff\xd8":
-        return decode_jpeg(data)
+    """Straight RGBA8 (height, width, 4); DecodeError for anything malformed,
+    truncated or in a form not handled here."""
+    try:
+        if data[:8] == b"\x89PNG\r\n\x1a\n":
+            return decode_png(data)
+        if data[:2] == b"\xff\xd8":
+            return decode_jpeg(data)
+    except DecodeError:
+        raise
+    except (ValueError, KeyError, IndexError, struct.error, zlib.error) as e:
+        raise DecodeError(f"malformed image: {e}") from e
     raise DecodeError("neither a PNG nor a JPEG")
 
 
@@ -186,7 +193,8 @@ class _Bits:
                         b = 0
                 else:
                     self.p += 1
-            self.acc = (self.acc << 8) | b
+            # Keep only the bits not yet consumed.
+            self.acc = ((self.acc << 8) | b) & ((1 << (self.n + 8)) - 1)
             self.n += 8
 
     def bits(self, k: int) -> int:

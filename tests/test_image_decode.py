@@ -134,3 +134,11 @@ def test_recorded_frame_keeps_its_images_and_mesh():
     # Without `images` the same frame drops them, as before.
     _, plain = st.frame_scene(10)
     assert plain.dropped_images == 5 and plain.images == 0
+
+
+def test_malformed_images_are_refused():
+    png = _png(np.zeros((4, 4, 4), np.uint8), [0])
+    for bad in (png[:40], png[:-20], b"\xff\xd8\xff\xdb\x00", _jpeg_dc_only([5], 8, 8)[:-12],
+                b"GIF89a"):
+        with pytest.raises(image_decode.DecodeError):
+            image_decode.decode(bad)
