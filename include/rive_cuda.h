@@ -339,7 +339,9 @@ int rive_cuda_render_target_read_async(rive_cuda_context* ctx,
  * last unmapped, into `target`. `cuda_stream` carries the role of
  * FlushDescriptor::externalCommandBuffer (gpu.hpp:1416): a cudaStream_t, or
  * NULL for the context's own stream. Returns once the work is enqueued;
- * device-side overflow is reported by rive_cuda_sync().
+ * device-side overflow is reported by rive_cuda_sync(). The flushes of one
+ * context run in the order they are issued, whatever their streams (a flush
+ * on another stream than the previous one waits for it).
  */
 int rive_cuda_flush(rive_cuda_context* ctx,
                     const rive_cuda_flush_desc* desc,

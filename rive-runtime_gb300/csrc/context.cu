@@ -290,6 +290,10 @@ struct rive_cuda_context
     // Set by rive_cuda_flush for one flush: the raster waits for it (a
     // read-back of the target still in flight), the front half does not.
     cudaEvent_t rasterWait = nullptr;
+    // The stream of the last batch and an event after its work (the next
+    // batch on another stream waits for it).
+    cudaStream_t lastStream = nullptr;
+    cudaEvent_t lastDone = nullptr;
     std::string lastError;
     RecordRing rings[RIVE_CUDA_BUFFER_KIND_COUNT];
     DeviceBuffer tess, grad;
@@ -1495,6 +1499,11 @@ int settle_pending(rive_cuda_context* ctx)
         int rc = reserve_bins(ctx, p->L, total, S);
         if (!rc)
             rc = enqueue_back(ctx, p->L, p->B, S, total, false, p->stream);
+        if (!rc && ctx->lastDone)
+        {
+            CK(cudaEventRecord(ctx->lastDone, p->stream));
+            ctx->lastStream = p->stream;
+        }
         for (auto& r : p->reads)
             if (!rc)
             {
@@ -1512,19 +1521,12 @@ int settle_pending(rive_cuda_context* ctx)
     return RIVE_CUDA_OK;
 }
 
-int run_batch(rive_cuda_context* ctx,
-              const FlushInput* in,
-              uint32_t n,
-              cudaStream_t stream,
-              bool speculative = false)
+int run_batch_body(rive_cuda_context* ctx,
+                   const FlushInput* in,
+                   uint32_t n,
+                   cudaStream_t stream,
+                   bool speculative)
 {
-    if (n == 0)
-        return RIVE_CUDA_OK;
-    {
-        const int rc = settle_pending(ctx);
-        if (rc)
-            return rc;
-    }
     BatchLayout L;
     int rc = plan_batch(ctx, in, n, L);
     if (!rc)
@@ -1706,6 +1708,29 @@ int run_batch(rive_cuda_context* ctx,
     return RIVE_CUDA_OK;
 }
 
+// Runs a batch in order after the context's previous one: the flushes of one
+// context share its intermediates (tessellation texture, triangle records,
+// bins), so a batch on another stream waits for the last one's work first.
+int run_batch(rive_cuda_context* ctx,
+              const FlushInput* in,
+              uint32_t n,
+              cudaStream_t stream,
+              bool speculative = false)
+{
+    if (n == 0)
+        return RIVE_CUDA_OK;
+    if (const int rc = settle_pending(ctx))
+        return rc;
+    if (ctx->lastDone && ctx->lastStream != stream)
+        CK(cudaStreamWaitEvent(stream, ctx->lastDone, 0));
+    const int rc = run_batch_body(ctx, in, n, stream, speculative);
+    if (!ctx->lastDone)
+        CK(cudaEventCreateWithFlags(&ctx->lastDone, cudaEventDisableTiming));
+    CK(cudaEventRecord(ctx->lastDone, stream));
+    ctx->lastStream = stream;
+    return rc;
+}
+
 // Flushes into caller-given device memory cannot tell a target with a
 // read-back in flight: while any is, their stream waits for the read stream.
 int order_after_reads(rive_cuda_context* ctx, cudaStream_t s)
@@ -1853,6 +1878,8 @@ void rive_cuda_context_destroy(rive_cuda_context* ctx)
         cudaStreamDestroy(ctx->copyStream);
     if (ctx->readStream)
         cudaStreamDestroy(ctx->readStream);
+    if (ctx->lastDone)
+        cudaEventDestroy(ctx->lastDone);
     delete ctx;
 }
 
@@ -2120,6 +2147,10 @@ int rive_cuda_flush(rive_cuda_context* ctx,
     if (desc->render_target_width != target->width || desc->render_target_height != target->height)
         return set_error(ctx, RIVE_CUDA_ERR_INVALID_ARGUMENT, "render target size mismatch");
     CK(cudaSetDevice(ctx->device));
+    // A pending speculative flush settles first, so a re-run of it is queued
+    // before anything this flush waits for.
+    if (const int src = settle_pending(ctx))
+        return src;
     cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : ctx->stream;
     if (s != ctx->stream)
     {
