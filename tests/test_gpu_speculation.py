@@ -80,3 +80,35 @@ def test_speculation_is_on_by_default_and_switchable():
         assert v.value == 0
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+def test_flushes_on_two_streams_run_in_issue_order(exact):
+    """A speculative flush on the context's stream, then at once a flush of
+    another frame on a caller's stream into caller-owned memory: they share
+    the context's intermediates, so the second waits for the first; both
+    images equal exactly sized, one-stream renders."""
+    from conftest import device_buffers
+    from rive_runtime_gb300 import rive_cuda
+    a, _ = load_golden("full_odd_s11")
+    b, _ = load_golden("silver_hunter_x_f0")
+    want_a = _render(exact, a)
+    want_b = _render(exact, b)
+    ctx = rive_cuda.Context(0)
+    try:
+        _render(ctx, a)  # a total seen: the next flushes speculate
+        bufs, keep = device_buffers(b)
+        side = torch.cuda.Stream()
+        out_b = torch.zeros((b.height, b.width, 4), dtype=torch.uint8, device="cuda")
+        t = ctx.render_target(a.width, a.height)
+        ctx.upload_frame(a)
+        for f in a.flushes:
+            ctx.flush(f, t)
+        for f in b.flushes:
+            ctx.flush_device(f, bufs, out_b.data_ptr(), side.cuda_stream)
+        got_a = ctx.read_target(t, a.width, a.height)
+        ctx.sync(side.cuda_stream)
+        assert np.array_equal(got_a, want_a)
+        assert np.array_equal(out_b.cpu().numpy(), want_b)
+    finally:
+        ctx.close()
