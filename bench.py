@@ -366,6 +366,7 @@ def run_ours(args, cap, wname, rank, world, scene_bytes=None):
         line["serving_recorded"] = run_serving_recorded(args, dev, raster)
     if args.feather_steps > 0 and world == 1:
         line["feathered"] = run_feathered(args, dev)
+        line["images"] = run_images(args, dev)
     if args.stress_canvases > 0 and world == 1:
         line["stroke_stress"] = run_stress(args, dev, raster)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -399,15 +400,15 @@ FEATHERED_CAPTURE = ("silver_police_files_f60",
                      "fills and strokes below the atlas threshold, planned by the reference front end")
 
 
-def run_feathered(args, dev):
-    """Frames/s of a recorded frame with feathered draws (the feather kernel
-    variants and the center-AA fans), records resident in HBM, timed with CUDA
-    events on the flush stream."""
+def _recorded_frame_fps(args, dev, name):
+    """(capture, frames/s, ms per frame) of golden capture `name` rendered
+    args.feather_steps times, records resident in HBM, timed with CUDA events
+    on the flush stream (textures and render buffers are made during the
+    warm-up)."""
     import numpy as np
     import torch
     from rive_runtime_gb300 import capture, rive_cuda
     from rive_runtime_gb300.capture import BUFFER_NAMES
-    name, what = FEATHERED_CAPTURE
     with open(os.path.join(REPO, "tests", "golden", name + ".cap"), "rb") as f:
         cap = capture.parse(f.read())
     stream = torch.cuda.Stream()
@@ -440,12 +441,41 @@ def run_feathered(args, dev):
     ms = ev0.elapsed_time(ev1)
     ctx.sync(stream.cuda_stream)
     ctx.close()
+    return cap, args.feather_steps / (ms / 1e3), ms / args.feather_steps
+
+
+def run_feathered(args, dev):
+    """Frames/s of a recorded frame with feathered draws (the feather kernel
+    variants and the center-AA fans)."""
+    name, what = FEATHERED_CAPTURE
+    cap, fps, ms = _recorded_frame_fps(args, dev, name)
     center = sum(int((fl.batches[:, 0] == 1).sum()) for fl in cap.flushes)
     return {"workload": name, "content": what, "width": cap.width, "height": cap.height,
             "center_aa_batches": center, "steps": args.feather_steps,
-            "frames_per_s": args.feather_steps / (ms / 1e3),
-            "ms_per_frame": ms / args.feather_steps,
+            "frames_per_s": fps, "ms_per_frame": ms,
             "raster": "16x16 tiles, full occupancy (not autotuned)"}
+
+
+# Recorded frames with images: drawImage draws (image paints) and a
+# drawImageMesh, with the images the recordings carry.
+IMAGE_CAPTURES = (
+    ("silver_superbowl_images_f5", "recorded frame 5 of superbowl (2914x296): 4 PNG images "
+     "drawn with drawImage among 99 path draws"),
+    ("silver_image_mesh_f10", "recorded frame 10 of image_fit_alignment_2 (500x500): drawImage "
+     "draws and a drawImageMesh"),
+)
+
+
+def run_images(args, dev):
+    """Frames/s of recorded frames with image paints and an image mesh."""
+    out = []
+    for name, what in IMAGE_CAPTURES:
+        cap, fps, ms = _recorded_frame_fps(args, dev, name)
+        out.append({"workload": name, "content": what, "width": cap.width,
+                    "height": cap.height, "textures": len(cap.textures),
+                    "image_meshes": sum(int((fl.batches[:, 0] == 6).sum()) for fl in cap.flushes),
+                    "steps": args.feather_steps, "frames_per_s": fps, "ms_per_frame": ms})
+    return out
 
 
 def run_serving(args, dev, raster=None):
